@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Exact top-k QPS on one GB300: 1M x 384 unit rows (cosine), k = 10, by batch size.
+
+Workload (the full-shape plain FP32 configuration): N = 1,000,000 base rows x d = 384
+from a 1,024-cluster Gaussian mixture (centroids ~ N(0, 1), sigma = 0.35), each row
+L2-normalised; 10,000 queries from the same mixture; inner product (cosine distance
+1 - q.x); k = 10. Synthetic data stands in for the reference's tweet embeddings
+(same 1M x 384 cosine shape).
+
+A step is one exact search of one batch (default batch 1: the HBM-bound case).
+  value      queries/s with queries and results resident in HBM (device API), timed
+             with CUDA events on the launching stream over exactly --steps steps.
+  e2e        the same through the public host API (pinned host queries in, host
+             results out, both copies inside the timed region).
+  roofline   the scan kernel: algorithmic bytes (base + queries + results) per launch
+             / its CUDA-event time, against the measured HBM copy bandwidth.
+  cpu_baseline  the reference's CPU algorithm (oracle port of brute_force.cpp
+             search_batch) on this host's cores, on a bounded sample.
+  sweep      QPS for the batch sweep 1 .. 4096 (fewer steps each).
+The base (1.536 GB) is larger than L2 (129 MB), so no L2 flush is needed between steps.
+
+--impl reference times the reference's CPU path (oracle port, all host threads) on the
+same workload and prints the same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# DRAM bytes per scan launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+# keyed by (n, dim, batch, k, metric); the summaries are committed under profiles/.
+MEASURED_TRAFFIC = {}
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--dim", type=int, default=384)
+    ap.add_argument("--k", type=int, default=10)
+    ap.add_argument("--metric", default="ip", choices=["ip", "l2"])
+    ap.add_argument("--clusters", type=int, default=1024)
+    ap.add_argument("--queries", type=int, default=10_000)
+    ap.add_argument("--sweep", default="1,8,32,128,512,1024,4096", help="comma list; empty to skip")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU-baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-recall", action="store_true")
+    return ap.parse_args()
+
+
+def make_data(a):
+    from vecsearch_gb300 import datasets as D
+    unit = a.metric == "ip"
+    x, _ = D.clustered(a.n, a.dim, a.clusters, 0.35, seed=0, centroid_seed=2, unit=unit)
+    q, _ = D.clustered(a.queries, a.dim, a.clusters, 0.35, seed=1, centroid_seed=2, unit=unit)
+    return x, q
+
+
+def workload(a):
+    return {
+        "workload": f"exact top-{a.k} {'cosine' if a.metric == 'ip' else 'L2'}, {a.n:,} x {a.dim} fp32 rows "
+                    f"({a.clusters}-cluster mixture, sigma 0.35{', unit rows' if a.metric == 'ip' else ''}), "
+                    f"batch {a.batch}",
+        "n": a.n, "dim": a.dim, "k": a.k, "batch": a.batch, "metric": a.metric, "global_batch": a.batch,
+        "l2_flush": "none needed: base rows (%.3f GB) exceed the 129 MB L2" % (a.n * a.dim * 4 / 1e9),
+    }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [s.strip() for s in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(x, q, a, threads):
+    """The reference's CPU search (oracle port) on a bounded sample: batches of a.batch queries."""
+    from oracle import oracle as O
+    O.search(x, q[:1], a.k, a.metric, num_threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    calls = 0
+    while True:
+        s = (calls * a.batch) % (len(q) - a.batch + 1)
+        O.search(x, q[s:s + a.batch], a.k, a.metric, num_threads=threads)
+        calls += 1
+        el = time.perf_counter() - t0
+        if el >= a.cpu_seconds or calls >= 1000:
+            break
+    return {"value": round(calls * a.batch / el, 2), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{calls} searches of batch {a.batch} over the full {a.n}x{a.dim} base, {el:.1f} s, "
+                      f"{threads} threads (oracle/bf_oracle.c: brute_force.cpp search_batch restated)"}
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    x, q = make_data(a)
+    from oracle import oracle as O
+    O.search(x, q[:a.batch], a.k, a.metric, num_threads=threads)  # warm-up
+    for _ in range(max(0, min(a.warmup, 2) - 1)):
+        O.search(x, q[:a.batch], a.k, a.metric, num_threads=threads)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < a.steps:
+        s = (steps * a.batch) % (len(q) - a.batch + 1)
+        O.search(x, q[s:s + a.batch], a.k, a.metric, num_threads=threads)
+        steps += 1
+        if time.perf_counter() - t0 > 120:  # bound the arm's run time
+            break
+    el = time.perf_counter() - t0
+    v = steps * a.batch / el
+    line = {
+        "impl": "reference", "metric": f"exact top-{a.k} QPS at {a.n // 1000}Kx{a.dim}", "value": round(v, 2),
+        "unit": "queries/s", "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+        "ms_per_step": round(el * 1e3 / steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(a),
+        "cpu_baseline": {"value": round(v, 2), "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} searches of batch {a.batch} over the full base ({el:.1f} s)"},
+        "e2e": {"value": round(v, 2), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None):
+    """Device-resident search: (ms total over `steps`, scan ms total, merge ms total, launches)."""
+    k = a.k
+    out_i = torch.empty((batch, k), dtype=torch.int32, device=qd.device)
+    out_d = torch.empty((batch, k), dtype=torch.float32, device=qd.device)
+    nq = qd.shape[0]
+    sp = stream.cuda_stream
+
+    def step(i):
+        s = (i * batch) % (nq - batch + 1)
+        idx.search_device(qd[s].data_ptr(), a.dim, batch, k, out_i.data_ptr(), out_d.data_ptr(), stream=sp)
+
+    for i in range(warmup):
+        step(i)
+    torch.cuda.synchronize()
+    idx.profile(True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        step(warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    scan_ms, merge_ms, launches = idx.profile_read()
+    idx.profile(False)
+    idx.sync()
+    return ms, scan_ms, merge_ms, launches
+
+
+def run_ours(a):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import vecsearch_gb300 as vsg
+    from vecsearch_gb300 import build as B
+    B.build()
+
+    x, q = make_data(a)
+    idx = vsg.GpuBruteForceIndex(a.dim, "cosine" if a.metric == "ip" else "l2", device=local)
+    idx.add(x)
+    qd = torch.from_numpy(q).to(f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+
+    sampler = ClockSampler(local)
+    ms, scan_ms, merge_ms, launches = time_device(idx, torch, qd, a, a.batch, a.steps, a.warmup, stream, dist)
+    clocks = sampler.stop()
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    qps = world * a.batch * a.steps / (ms / 1e3)
+
+    # e2e: public host API with pinned buffers; copies inside the timed region.
+    qh = torch.from_numpy(q).pin_memory()
+    oi = torch.empty((a.batch, a.k), dtype=torch.int32).pin_memory()
+    od = torch.empty((a.batch, a.k), dtype=torch.float32).pin_memory()
+    nq = q.shape[0]
+    e2e_steps = min(a.steps, max(20, int(2000 / a.batch)))
+    for i in range(min(a.warmup, 5)):
+        idx.search_host_ptr(qh[(i * a.batch) % (nq - a.batch + 1)].data_ptr(), a.batch, a.k, oi.data_ptr(),
+                            od.data_ptr())
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        s = (i * a.batch) % (nq - a.batch + 1)
+        idx.search_host_ptr(qh[s].data_ptr(), a.batch, a.k, oi.data_ptr(), od.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_qps = world * a.batch * e2e_steps / e2e_s
+
+    # roofline of the scan kernel
+    scan_avg_ms = scan_ms / max(launches, 1)
+    alg_bytes = a.n * a.dim * 4 + a.batch * a.dim * 4 + a.batch * a.k * 8
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (scan_avg_ms / 1e3) / 1e9
+    traffic = MEASURED_TRAFFIC.get((a.n, a.dim, a.batch, a.k, a.metric))
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                "kernel": "scan_kernel (fused FP32 scan + top-k)", "kernel_ms_avg": round(scan_avg_ms, 5),
+                "merge_ms_avg": round(merge_ms / max(launches, 1), 5)}
+
+    extra = {}
+    if rank == 0 and a.sweep and world == 1:
+        sweep = []
+        for b in [int(s) for s in a.sweep.split(",") if s]:
+            if b > q.shape[0]:
+                continue
+            st = max(3, min(300, int(3e4 / b)))
+            ms_b, scan_b, _, l_b = time_device(idx, torch, qd, a, b, st, 3, stream)
+            flops = 2.0 * a.n * a.dim * b
+            sweep.append({"batch": b, "qps": round(b * st / (ms_b / 1e3), 1),
+                          "ms_per_batch": round(ms_b / st, 4),
+                          "scan_gbs": round((a.n * a.dim * 4) / (scan_b / l_b / 1e3) / 1e9, 1),
+                          "scan_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)})
+        extra["sweep"] = sweep
+
+    if rank == 0 and not a.no_recall:
+        from oracle import oracle as O
+        nchk = min(a.batch, 16) if a.batch > 1 else 8
+        ids, _ = idx.search(q[:nchk], a.k)
+        gi, _ = O.fp64_topk(x, q[:nchk], a.k, a.metric)
+        extra["recall_vs_fp64"] = vsg.recall_at_k(ids, gi, a.k)
+        try:
+            extra["near_ties_tolerated"] = O.check_ids(ids, gi, x, q[:nchk], a.metric)
+            extra["ids_match_fp64_rule"] = True
+        except AssertionError as e:
+            extra["ids_match_fp64_rule"] = False
+            extra["id_mismatch"] = str(e)[:200]
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(x, q, a, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": f"exact top-{a.k} QPS at {a.n // 1000}Kx{a.dim}", "value": round(qps, 2),
+            "unit": "queries/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": round(ms / a.steps, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(workload(a),
+                                                                                     parallelism=f"replicas{world}"),
+            "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_qps, 2), "unit": "queries/s", "h2d_bytes_per_step": a.batch * a.dim * 4,
+                    "d2h_bytes_per_step": a.batch * a.k * 8, "steps": e2e_steps},
+            "gpu_launches": int(launches) * 2, "clocks": clocks,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

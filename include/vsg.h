@@ -1,0 +1,132 @@
+/*
+ * vsg.h - C ABI of the GB300 exact k-NN engine (libvsg_gb300.so).
+ *
+ * The drop-in boundary for vecsearch's exact-search path. Every entry point
+ * below names the reference interface it replaces (paths relative to the
+ * vecsearch project). Plain pointers and sizes only; no C++ or torch types.
+ *
+ * Conventions
+ *   - Every function that can fail returns a status code (VSG_OK = 0) and
+ *     leaves a message for the calling thread in vsg_last_error().
+ *   - Results are nq x k, row-major, nearest first, ordered by (dist, id):
+ *     equal distances go to the lower id. Missing results (k > rows, or fewer
+ *     allowed rows than k) are id VSG_NONE with dist +inf.
+ *   - Distances: VSG_METRIC_L2 = squared Euclidean (no sqrt);
+ *     VSG_METRIC_IP = 1 - <q, x> (cosine distance on unit-norm rows).
+ *   - One index serialises its own calls (a mutex, as the reference's
+ *     GpuBruteForceIndex does); separate indexes may be used from separate
+ *     threads.
+ */
+#ifndef VSG_H_
+#define VSG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference throws instead (src/gpu_brute_force.cu:11-16,
+ * :294-298, :387, :408); the C++ wrapper re-throws the same exception types. */
+#define VSG_OK 0
+#define VSG_ERR_INVALID 1        /* std::invalid_argument (Python: ValueError) */
+#define VSG_ERR_LENGTH 2         /* std::length_error (Python: ValueError) */
+#define VSG_ERR_CUDA 3           /* std::runtime_error from a CUDA call (Python: RuntimeError) */
+#define VSG_ERR_DEVICE_TIMEOUT 4 /* a kernel's bounded wait ran out (Python: RuntimeError) */
+#define VSG_ERR_NOMEM 5          /* device or pinned host allocation failed (Python: MemoryError) */
+
+/* Same values as vecsearch::Metric (include/vecsearch/distance.h:15). */
+#define VSG_METRIC_L2 0u
+#define VSG_METRIC_IP 1u
+
+/* Same values as vecsearch::GpuMethod (include/vecsearch/gpu_brute_force.h:16-21).
+ * All methods return the same exact top-k; the method only picks the kernel. */
+#define VSG_METHOD_AUTO 0u
+#define VSG_METHOD_NAIVE 1u
+#define VSG_METHOD_SKINNY 2u
+#define VSG_METHOD_TILED 3u
+
+#define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
+#define VSG_MAX_K 128u       /* GpuBruteForceIndex::kMaxK (gpu_brute_force.h:27) */
+
+typedef struct vsg_index vsg_index;
+
+/* cuda_available() (include/vecsearch/gpu_brute_force.h:24, src/gpu_brute_force.cu:334-341):
+ * 1 if the CUDA runtime sees at least one device, else 0 (clears the sticky error). */
+int vsg_cuda_available(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* vsg_last_error(void);
+
+/* GpuBruteForceIndex(dim, metric, device) (gpu_brute_force.h:31, src/gpu_brute_force.cu:386-396).
+ * dim == 0 or an unknown metric -> VSG_ERR_INVALID. */
+int vsg_create(size_t dim, uint32_t metric, int device, vsg_index** out);
+
+/* ~GpuBruteForceIndex(): frees every device and pinned buffer of the index. NULL is a no-op. */
+void vsg_destroy(vsg_index* index);
+
+/* GpuBruteForceIndex::add (gpu_brute_force.h:36, src/gpu_brute_force.cu:404-423).
+ * n host rows, row-major with stride dim floats; ids continue from vsg_size().
+ * More than 2^32 - 2 rows in total -> VSG_ERR_LENGTH. */
+int vsg_add(vsg_index* index, const float* rows, size_t n);
+
+/* GpuBruteForceIndex::search (gpu_brute_force.h:40-41, src/gpu_brute_force.cu:425-488).
+ * nq host queries (stride dim) -> host out_ids / out_dists (nq x k). k > VSG_MAX_K or an
+ * unknown method -> VSG_ERR_INVALID. nq == 0 or k == 0 is a no-op; an empty index fills
+ * VSG_NONE / +inf. Blocks until the results are in the host arrays. */
+int vsg_search(vsg_index* index, const float* queries, size_t nq, size_t k, uint32_t* out_ids,
+               float* out_dists, uint32_t method);
+
+/* search() with a filter (the spec extension of gpu_brute_force.h:40-41 with the semantics
+ * of python/bindings.cpp:28-36 as_mask): a row may be returned only if its allow-bit is set.
+ * mask_words: bit (r & 31) of word (r >> 5) is row r. per_query == 0: one mask of
+ * ceil(size / 32) words for every query; per_query != 0: nq masks, mask_ld words apart
+ * (mask_ld >= ceil(size / 32)). */
+int vsg_search_filtered(vsg_index* index, const float* queries, size_t nq, size_t k,
+                        const uint32_t* mask_words, int per_query, size_t mask_ld, uint32_t* out_ids,
+                        float* out_dists, uint32_t method);
+
+/* The HNSW index's exact_below switch (include/vecsearch/hnsw.h:29-33 SearchFilter,
+ * src/hnsw.cpp:325-328). allowed: one byte per row (nonzero = allowed), allowed_len == size.
+ * If the mask allows no row, fills VSG_NONE / +inf and sets *handled = 1 (hnsw.cpp:326).
+ * If 0 < allowed rows <= exact_below, runs the exact filtered scan on the GPU (in place of
+ * search_exact, hnsw.cpp:336-354) and sets *handled = 1. Otherwise sets *handled = 0 and
+ * writes nothing: the caller runs its graph search (hnsw.cpp:329-333). */
+int vsg_hnsw_exact_below(vsg_index* index, const float* queries, size_t nq, size_t k,
+                         const uint8_t* allowed, size_t allowed_len, size_t exact_below,
+                         uint32_t* out_ids, float* out_dists, int* handled);
+
+/* Device-resident search (new: the serving/throughput form of search()). Queries, mask and
+ * outputs are device pointers; queries have row stride ldq floats (ldq >= dim). Work is queued
+ * on `stream` (a cudaStream_t; NULL = legacy default stream) and the call returns without
+ * waiting. Calls on one index are ordered on the device even across streams. Device-side
+ * failures are reported by the next vsg_sync() or host-side search on the index. */
+int vsg_search_device(vsg_index* index, const float* d_queries, size_t ldq, size_t nq, size_t k,
+                      const uint32_t* d_mask_words, int per_query, size_t mask_ld, uint32_t* d_out_ids,
+                      float* d_out_dists, uint32_t method, void* stream);
+
+/* Waits for the index's queued device work; reports a device-side failure, if any. */
+int vsg_sync(vsg_index* index);
+
+/* size(), dim(), metric() (gpu_brute_force.h:44-46). */
+size_t vsg_size(const vsg_index* index);
+size_t vsg_dim(const vsg_index* index);
+uint32_t vsg_metric(const vsg_index* index);
+
+/* Device pointer to the resident rows (size x padded_dim floats, padding zero) and the padded
+ * dim, for zero-copy consumers of the index (e.g. a ground-truth or rerank pass). */
+const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
+
+/* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
+ * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for
+ * the recorded events, returns the summed milliseconds and the number of searches, and clears
+ * them. Enabling or disabling also clears. */
+int vsg_profile_enable(vsg_index* index, int enable);
+int vsg_profile_read(vsg_index* index, double* scan_ms, double* merge_ms, size_t* searches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSG_H_ */

@@ -1,0 +1,70 @@
+"""CPU: the C-ABI library builds, loads, exports every declared symbol, and validates arguments."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+
+def declared_symbols():
+    names = []
+    for f in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if f.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", f)).read()
+            names += re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(vsg_\w+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from vecsearch_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert "vsg_search" in syms and "vsg_create" in syms and len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_python_signatures_cover_header():
+    from vecsearch_gb300 import _native
+    assert set(declared_symbols()) <= set(_native.SIGNATURES), set(declared_symbols()) - set(_native.SIGNATURES)
+
+
+def test_create_validates_before_touching_cuda():
+    import vecsearch_gb300 as vsg
+    with pytest.raises(ValueError):
+        vsg.GpuBruteForceIndex(0)  # dim == 0 -> invalid_argument (gpu_brute_force.cu:387)
+    with pytest.raises(ValueError):
+        vsg.GpuBruteForceIndex(8, metric="hamming")  # parse_metric (bindings.cpp:38-42)
+
+
+def test_cuda_available_is_false_without_gpu():
+    import vecsearch_gb300 as vsg
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert vsg.cuda_available() is False
+
+
+def test_null_index_is_rejected(lib):
+    from vecsearch_gb300 import _native
+    l = _native.lib()
+    ids = np.zeros(4, np.uint32)
+    assert l.vsg_search(None, None, 1, 1, ids.ctypes.data, ids.ctypes.data, 0) == _native.ERR_INVALID
+    assert l.vsg_sync(None) == _native.ERR_INVALID
+    assert b"NULL" in l.vsg_last_error()
+
+
+def test_helpers():
+    import vecsearch_gb300 as vsg
+    x = np.array([[3.0, 4.0], [0.0, 0.0]], np.float32)
+    n = vsg.normalize(x)
+    assert np.allclose(n[0], [0.6, 0.8]) and np.all(np.isfinite(n))
+    assert vsg.recall_at_k(np.array([[1, 2, 3]]), np.array([[3, 2, 9]]), 3) == pytest.approx(2 / 3)

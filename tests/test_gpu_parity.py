@@ -1,0 +1,154 @@
+"""GPU: the CUDA path against the reference's outputs (golden fixtures) and the oracle.
+
+Parity rule (stated with every check): ids equal the reference's, except at near-ties,
+where both disagreeing rows' float64 distances lie within 1e-6 (relative) of each other
+or of the k-th float64 distance; distances equal the reference's within
+rtol 1e-5 + atol 2e-6 (FP32 sums in a different order).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import load_golden
+from tests.golden.make_golden import CASES
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL, REL_TIE = 1e-5, 2e-6, 1e-6
+METHODS = ["naive", "skinny", "tiled", "auto"]
+BF_CASES = [c["name"] for c in CASES if not c["name"].startswith("filter")]
+
+
+def assert_parity(ids, dists, want_i, want_d, x, q, metric):
+    want64 = O.ids_to_int64(want_i)
+    assert ids.shape == want64.shape and ids.dtype == np.int64 and dists.dtype == np.float32
+    np.testing.assert_allclose(dists, want_d, rtol=RTOL, atol=ATOL)
+    O.check_ids(ids, want64, x, q, metric, rel=REL_TIE)
+    fin = np.isfinite(dists)
+    assert np.all(np.diff(np.where(fin, dists, np.inf), axis=1) >= 0)
+    assert ((ids >= 0) == fin).all()
+
+
+@pytest.mark.parametrize("name", BF_CASES)
+def test_golden(gpu_ready, name):
+    vsg = gpu_ready
+    want_i, want_d, x, q, k, metric, _ = load_golden(name)
+    idx = vsg.GpuBruteForceIndex(x.shape[1], metric)
+    idx.add(x)
+    ids, dists = idx.search(q, k)
+    assert_parity(ids, dists, want_i, want_d, x, q, metric)
+
+
+@pytest.mark.parametrize("metric", ["l2", "ip"])
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("d", [37, 128])
+@pytest.mark.parametrize("nq", [1, 5, 300])
+def test_matches_cpu(gpu_ready, metric, method, d, nq):
+    # tests/python/test_gpu.py:17-33, with two adds so the device buffer grows.
+    vsg = gpu_ready
+    want_i, want_d, x, q, k, _, _ = load_golden(f"gpu_cpu_d{d}_{metric}")
+    gpu = vsg.GpuBruteForceIndex(d, metric)
+    gpu.add(x[:1000])
+    gpu.add(x[1000:])
+    assert len(gpu) == 3000 and gpu.dim == d
+    ids, dists = gpu.search(q[:nq], k, method=method)
+    assert_parity(ids, dists, want_i[:nq], want_d[:nq], x, q[:nq], metric)
+
+
+@pytest.mark.parametrize("k", [1, 16, 17, 100, 128])
+def test_k_buckets(gpu_ready, k):
+    # tests/python/test_gpu.py:36-45 (there: recall > 0.99; here: the parity rule)
+    vsg = gpu_ready
+    want_i, want_d, x, q, _, metric, _ = load_golden("kbuckets")
+    gpu = vsg.GpuBruteForceIndex(64)
+    gpu.add(x)
+    ids, dists = gpu.search(q, k)
+    assert_parity(ids, dists, want_i[:, :k], want_d[:, :k], x, q, metric)
+
+
+def test_many_queries_and_chunks(gpu_ready):
+    # tests/python/test_gpu.py:48-57: 5000 queries over 70000 rows.
+    vsg = gpu_ready
+    want_i, want_d, x, q, k, metric, _ = load_golden("chunks")
+    gpu = vsg.GpuBruteForceIndex(16)
+    gpu.add(x)
+    ids, dists = gpu.search(q, k)
+    assert_parity(ids, dists, want_i, want_d, x, q, metric)
+
+
+def test_missing_results_and_limits(gpu_ready):
+    # tests/python/test_gpu.py:60-70
+    vsg = gpu_ready
+    gpu = vsg.GpuBruteForceIndex(8)
+    ids, dists = gpu.search(np.zeros((2, 8), np.float32), 5)  # empty index
+    assert (ids == -1).all() and np.isinf(dists).all()
+    from vecsearch_gb300 import datasets as D
+    gpu.add(D.portable(3, 8, 7))
+    ids, dists = gpu.search(np.zeros(8, np.float32), 5)
+    assert (ids[0, :3] >= 0).all() and (ids[0, 3:] == -1).all() and np.isinf(dists[0, 3:]).all()
+    with pytest.raises(ValueError):
+        gpu.search(np.zeros(8, np.float32), 129)
+    with pytest.raises(ValueError):
+        gpu.search(np.zeros(8, np.float32), 5, method="fast")
+    with pytest.raises(ValueError):
+        gpu.search(np.zeros((2, 9), np.float32), 5)
+    ids, dists = gpu.search(np.zeros((0, 8), np.float32), 5)
+    assert ids.shape == (0, 5)
+    ids, dists = gpu.search(np.zeros((2, 8), np.float32), 0)
+    assert ids.shape == (2, 0)
+
+
+def test_padding_known_answers(gpu_ready):
+    # tests/cpp/test_brute_force.cpp:9-20 and :45-65
+    vsg = gpu_ready
+    for name in ("line", "pad", "clamp"):
+        want_i, want_d, x, q, k, metric, _ = load_golden(name)
+        gpu = vsg.GpuBruteForceIndex(x.shape[1], metric)
+        gpu.add(x)
+        ids, dists = gpu.search(q, k)
+        np.testing.assert_array_equal(ids, O.ids_to_int64(want_i))
+        np.testing.assert_allclose(dists, want_d, rtol=RTOL, atol=ATOL)
+
+
+def test_batch_invariance_bitwise(gpu_ready):
+    # A query's result does not depend on the batch it is searched in.
+    vsg = gpu_ready
+    _, _, x, q, k, metric, _ = load_golden("gpu_cpu_d128_ip")
+    gpu = vsg.GpuBruteForceIndex(128, metric)
+    gpu.add(x)
+    all_i, all_d = gpu.search(q, k)
+    for sl in (slice(0, 1), slice(7, 9), slice(100, 105), slice(37, 300)):
+        i, d = gpu.search(q[sl], k)
+        np.testing.assert_array_equal(i, all_i[sl])
+        np.testing.assert_array_equal(d.view(np.uint32), all_d[sl].view(np.uint32))
+
+
+def test_duplicate_rows_tie_to_lower_id(gpu_ready):
+    # Equal distances go to the lower id (brute_force.cpp:152-169 merge order).
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    base = D.portable(200, 24, 12)
+    x = np.concatenate([base, base, base])  # every row three times
+    q = D.portable(9, 24, 13)
+    gpu = vsg.GpuBruteForceIndex(24, "l2")
+    gpu.add(x)
+    ids, dists = gpu.search(q, 12)
+    oi, od = O.search(x, q, 12, "l2")
+    np.testing.assert_array_equal(ids % 200, O.ids_to_int64(oi) % 200)
+    for row_i, row_d in zip(ids, dists):
+        for a in range(0, 12, 3):
+            assert (row_d[a] == row_d[a:a + 3]).all() and list(row_i[a:a + 3]) == sorted(row_i[a:a + 3])
+
+
+def test_c1_config_against_fp64(gpu_ready):
+    # Config 1 (100k x 384 clustered unit rows, IP, k = 10): reference ids and FP64 recall 1.0.
+    vsg = gpu_ready
+    want_i, want_d, x, q, k, metric, _ = load_golden("c1")
+    gpu = vsg.GpuBruteForceIndex(384, "cosine")
+    gpu.add(x)
+    for b in (1, 8, 64):
+        ids, dists = gpu.search(q[:b], k)
+        assert_parity(ids, dists, want_i[:b], want_d[:b], x, q[:b], metric)
+    gi, _ = O.fp64_topk(x, q, k, metric)
+    ids, _ = gpu.search(q, k)
+    O.check_ids(ids, gi, x, q, metric, rel=REL_TIE)

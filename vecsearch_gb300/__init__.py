@@ -1,0 +1,212 @@
+"""vecsearch_gb300 - GB300-native exact k-NN behind vecsearch's exact-search API.
+
+Drop-in names (python/vecsearch/__init__.py and python/bindings.cpp of vecsearch):
+
+* :class:`GpuBruteForceIndex` - ``(dim, metric="l2", device=0)``, ``add(x)``,
+  ``search(queries, k=10, method="auto", filter=None)`` -> ``(ids int64, dists float32)``,
+  ``dim``, ``len()``; the same argument coercion, errors and -1 / +inf padding as the
+  reference's bindings (bindings.cpp:151-189). ``filter`` is new: None, a 1-D bool/uint8
+  mask of length ``len(index)`` shared by all queries, or a 2-D (nq, len(index)) mask with
+  one row per query.
+* :func:`cuda_available`, :func:`normalize`, :func:`recall_at_k`.
+* :class:`HNSWExactRoute` - the HNSW index's ``exact_below`` switch on the GPU.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .datasets import pack_bits
+
+__all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "cuda_available", "normalize", "recall_at_k",
+           "DeviceTimeoutError"]
+__version__ = "0.1.0"
+
+DeviceTimeoutError = _native.DeviceTimeoutError
+
+
+def cuda_available() -> bool:
+    """True if the CUDA runtime sees a GPU (cuda_available(), gpu_brute_force.cu:334-341)."""
+    return bool(_native.lib().vsg_cuda_available())
+
+
+def normalize(x: np.ndarray) -> np.ndarray:
+    """L2-normalize rows so inner product == cosine similarity (vecsearch/__init__.py:15-18)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return x / np.maximum(np.linalg.norm(x, axis=1, keepdims=True), 1e-12)
+
+
+def recall_at_k(found: np.ndarray, truth: np.ndarray, k: int = 10) -> float:
+    """Fraction of the true top-k found in the returned top-k (vecsearch/__init__.py:21-24)."""
+    hits = sum(len(set(f[:k]) & set(t[:k])) for f, t in zip(found, truth))
+    return hits / (len(found) * k)
+
+
+def _parse_metric(metric):
+    if metric == "l2":
+        return _native.METRIC_L2
+    if metric in ("ip", "cosine"):
+        return _native.METRIC_IP
+    raise ValueError("metric must be 'l2', 'ip' or 'cosine' (cosine expects normalized vectors)")
+
+
+def _as_f32(a):
+    """py::array_t<float, c_style | forcecast> (bindings.cpp:18)."""
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _check_2d(a, dim):
+    if a.ndim != 2 or a.shape[1] != dim:
+        raise ValueError(f"expected array of shape (n, {dim})")
+
+
+def _ids_to_int64(ids):
+    out = ids.astype(np.int64)
+    out[ids == _native.NONE] = -1
+    return out
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class GpuBruteForceIndex:
+    """Exact k-NN on one GB300 (vecsearch.GpuBruteForceIndex, gpu_brute_force.h:25-50)."""
+
+    kNone = _native.NONE
+    kMaxK = _native.MAX_K
+
+    def __init__(self, dim, metric="l2", device=0):
+        lib = _native.lib()
+        self._h = ctypes.c_void_p()
+        _native.check(lib.vsg_create(int(dim), _parse_metric(metric), int(device), ctypes.byref(self._h)))
+        self._dim = int(dim)
+        self._metric = metric
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _native.lib().vsg_destroy(h)
+            self._h = None
+
+    @property
+    def dim(self):
+        return self._dim
+
+    @property
+    def metric(self):
+        return "l2" if _native.lib().vsg_metric(self._h) == _native.METRIC_L2 else "ip"
+
+    def __len__(self):
+        return int(_native.lib().vsg_size(self._h))
+
+    def add(self, x):
+        """Append rows (bindings.cpp:157-164); ids continue from len(self)."""
+        x = _as_f32(x)
+        _check_2d(x, self._dim)
+        _native.check(_native.lib().vsg_add(self._h, _ptr(x), x.shape[0]))
+
+    def _mask_words(self, filter, nq):
+        """(words, per_query, ld) for the C ABI, with as_mask's validation (bindings.cpp:28-36)."""
+        n = len(self)
+        f = np.asarray(filter)
+        if f.ndim == 1 and f.shape[0] == n:
+            return np.ascontiguousarray(pack_bits(f)), 0, 0
+        if f.ndim == 2 and f.shape == (nq, n):
+            w = np.ascontiguousarray(pack_bits(f))
+            return w, 1, w.shape[1]
+        raise ValueError(f"filter must be a 1-D bool array of length {n} or a 2-D array of shape ({nq}, {n})")
+
+    def search(self, queries, k=10, method="auto", filter=None):
+        """Exact top-k (bindings.cpp:165-186); returns (ids[int64, nq x k], dists[float32, nq x k])."""
+        if method not in _native.METHODS:
+            raise ValueError("method must be 'auto', 'naive', 'skinny' or 'tiled'")
+        q = _as_f32(queries)
+        if q.ndim == 1:
+            q = q.reshape(1, q.shape[0])
+        _check_2d(q, self._dim)
+        k = int(k)
+        if k < 0:
+            raise ValueError("k must be >= 0")
+        nq = q.shape[0]
+        ids = np.empty((nq, k), np.uint32)
+        dists = np.empty((nq, k), np.float32)
+        lib = _native.lib()
+        if filter is None:
+            rc = lib.vsg_search(self._h, _ptr(q), nq, k, _ptr(ids), _ptr(dists), _native.METHODS[method])
+        else:
+            words, per_query, ld = self._mask_words(filter, nq)
+            rc = lib.vsg_search_filtered(self._h, _ptr(q), nq, k, _ptr(words), per_query, ld, _ptr(ids),
+                                         _ptr(dists), _native.METHODS[method])
+        _native.check(rc)
+        return _ids_to_int64(ids), dists
+
+    # ---- device-resident form (for serving and benchmarks) ------------------------------------
+    def search_device(self, q_ptr, ldq, nq, k, out_ids_ptr, out_dists_ptr, stream=0, mask_ptr=0,
+                      per_query=False, mask_ld=0, method="auto"):
+        """Queue a search on device buffers (raw pointers, e.g. torch ``data_ptr()``); no sync."""
+        _native.check(_native.lib().vsg_search_device(
+            self._h, ctypes.c_void_p(q_ptr), ldq, nq, k, ctypes.c_void_p(mask_ptr or None), int(per_query),
+            mask_ld, ctypes.c_void_p(out_ids_ptr), ctypes.c_void_p(out_dists_ptr), _native.METHODS[method],
+            ctypes.c_void_p(stream or None)))
+
+    def search_host_ptr(self, q_ptr, nq, k, out_ids_ptr, out_dists_ptr, method="auto"):
+        """search() on raw host pointers (e.g. pinned buffers), blocking; no numpy conversion."""
+        _native.check(_native.lib().vsg_search(self._h, ctypes.c_void_p(q_ptr), nq, k,
+                                               ctypes.c_void_p(out_ids_ptr), ctypes.c_void_p(out_dists_ptr),
+                                               _native.METHODS[method]))
+
+    def sync(self):
+        """Wait for queued device work; raises if a kernel reported a failure."""
+        _native.check(_native.lib().vsg_sync(self._h))
+
+    def profile(self, enable=True):
+        """Start (or stop) recording CUDA-event times of the scan and merge kernels."""
+        _native.check(_native.lib().vsg_profile_enable(self._h, int(enable)))
+
+    def profile_read(self):
+        """(scan_ms_total, merge_ms_total, searches) since the last read; clears the record."""
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
+        _native.check(_native.lib().vsg_profile_read(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
+        return a.value, b.value, n.value
+
+
+class HNSWExactRoute:
+    """The HNSW index's exact_below switch (hnsw.cpp:322-334) with the exact scan on the GPU.
+
+    Wraps any object with the reference's ``HNSWIndex.search`` signature (the graph) and a
+    :class:`GpuBruteForceIndex` holding the same rows. ``search(queries, k, ef, num_threads,
+    filter, exact_below)`` behaves like ``HNSWIndex.search`` (bindings.cpp:77-111): with a filter
+    that allows no row the result is all -1 / +inf; with 0 < allowed <= exact_below it is the
+    exact filtered scan (search_exact, hnsw.cpp:336-354) computed on the GPU; otherwise the
+    wrapped graph search answers. ``graph`` may be None when only the exact route is used.
+    """
+
+    def __init__(self, gpu_index, graph=None):
+        self.gpu = gpu_index
+        self.graph = graph
+
+    def search(self, queries, k=10, ef=64, num_threads=1, filter=None, exact_below=0):
+        q = _as_f32(queries)
+        if q.ndim == 1:
+            q = q.reshape(1, q.shape[0])
+        _check_2d(q, self.gpu.dim)
+        nq = q.shape[0]
+        k = int(k)
+        handled = ctypes.c_int(0)
+        ids = np.empty((nq, k), np.uint32)
+        dists = np.empty((nq, k), np.float32)
+        if filter is not None:
+            mask = np.asarray(filter)
+            if mask.ndim != 1 or mask.shape[0] != len(self.gpu):
+                raise ValueError(f"filter must be a 1-D bool array of length {len(self.gpu)}")
+            mask = np.ascontiguousarray(mask != 0, dtype=np.uint8)
+            _native.check(_native.lib().vsg_hnsw_exact_below(
+                self.gpu._h, _ptr(q), nq, k, _ptr(mask), mask.shape[0], int(exact_below), _ptr(ids), _ptr(dists),
+                ctypes.byref(handled)))
+        if handled.value:
+            return _ids_to_int64(ids), dists
+        if self.graph is None:
+            raise NotImplementedError("the graph search is not part of the GPU route; pass graph=HNSWIndex")
+        return self.graph.search(queries, k=k, ef=ef, num_threads=num_threads, filter=filter,
+                                 exact_below=exact_below)

@@ -1,0 +1,194 @@
+// Device-side building blocks shared by the exact k-NN kernels (sm_103a).
+//
+//  * PTX wrappers for mbarriers and bulk (TMA) global->shared copies. Every
+//    wait is bounded by the global timer: a wait that runs past kWaitLimitNs
+//    returns false, the kernel records kDevTimeout in its error word and winds
+//    down instead of spinning forever.
+//  * A warp-owned sorted top-k list in shared memory, ordered by (dist, id):
+//    ties go to the lower id, the rule of the reference's final merge
+//    (src/brute_force.cpp:152-169) and of its GPU select (src/gpu_brute_force.cu:276).
+//  * A warp reduce-scatter: 32 lanes each holding V partial sums end with
+//    lane L holding the full sum of value L * V / 32.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vsg {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kMaxK = 128;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s for any single wait
+
+enum DevStatus : int { kDevOk = 0, kDevTimeout = 1 };
+
+__device__ __forceinline__ bool nb_less(float ad, uint32_t ai, float bd, uint32_t bi) {
+  return ad < bd || (ad == bd && ai < bi);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete. False after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+// Bulk copy of `bytes` contiguous bytes (multiple of 16, both addresses 16-byte
+// aligned) from global to shared memory; completion is signalled on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Same, with an L2 evict-first hint: the base rows are streamed once per search.
+__device__ __forceinline__ void bulk_load_stream(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+      "%4;" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// ---- warp reduce-scatter ------------------------------------------------------------------
+// N values per lane, at lane-mask M. After the full recursion (M = 16 .. 1) lane L holds, in
+// v[0], the warp-wide sum of value index L / (32 / N) (N <= 32, a power of two).
+template <int N, int M>
+struct ReduceScatter {
+  static __device__ __forceinline__ void run(float* v, int lane) {
+    if constexpr (M == 0) {
+      return;
+    } else if constexpr (N > 1) {
+      constexpr int H = N / 2;
+      const bool up = (lane & M) != 0;
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const float send = up ? v[i] : v[i + H];
+        const float keep = up ? v[i + H] : v[i];
+        v[i] = keep + __shfl_xor_sync(kFull, send, M);
+      }
+      ReduceScatter<H, M / 2>::run(v, lane);
+    } else {
+      v[0] += __shfl_xor_sync(kFull, v[0], M);
+      ReduceScatter<1, M / 2>::run(v, lane);
+    }
+  }
+};
+
+// ---- warp-owned sorted top-k list ------------------------------------------------------------
+// ld/li hold k entries sorted by (dist, id), padded with (inf, kNone). Inserts (cd, ci), which
+// the caller has checked to be below entry k-1, and drops the last entry. Whole warp, uniform args.
+__device__ __forceinline__ void list_insert(float* ld, uint32_t* li, int k, float cd, uint32_t ci, int lane) {
+  int pos = 0;
+#pragma unroll
+  for (int e = 0; e < kMaxK / 32; ++e) {
+    if (e * 32 < k) {
+      const int j = e * 32 + lane;
+      const bool lt = j < k && nb_less(ld[j], li[j], cd, ci);
+      pos += __popc(__ballot_sync(kFull, lt));
+    }
+  }
+  float vd[kMaxK / 32];
+  uint32_t vi[kMaxK / 32];
+#pragma unroll
+  for (int e = 0; e < kMaxK / 32; ++e) {
+    const int j = e * 32 + lane;
+    if (e * 32 < k && j >= pos && j + 1 < k) {
+      vd[e] = ld[j];
+      vi[e] = li[j];
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < kMaxK / 32; ++e) {
+    const int j = e * 32 + lane;
+    if (e * 32 < k && j >= pos && j + 1 < k) {
+      ld[j + 1] = vd[e];
+      li[j + 1] = vi[e];
+    }
+  }
+  if (lane == 0) {
+    ld[pos] = cd;
+    li[pos] = ci;
+  }
+  __syncwarp();
+}
+
+// Merges `len` entries of a list sorted by (dist, id) into the warp's top-k list. Since the
+// source is sorted and the list's last entry only decreases, the first rejected entry ends it.
+__device__ __forceinline__ void list_merge_sorted(float* ld, uint32_t* li, int k, const float* sd,
+                                                  const uint32_t* si, int len, int lane) {
+  for (int c0 = 0; c0 < len; c0 += 32) {
+    const int j = c0 + lane;
+    const bool valid = j < len;
+    const float d = valid ? sd[j] : __int_as_float(0x7f800000);
+    const uint32_t id = valid ? si[j] : kNone;
+    const float td = ld[k - 1];
+    const uint32_t ti = li[k - 1];
+    const bool pass = valid && nb_less(d, id, td, ti);
+    unsigned m = __ballot_sync(kFull, pass);
+    const unsigned vmask = __ballot_sync(kFull, valid);
+    const bool ended = m != vmask;
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const float cd = __shfl_sync(kFull, d, src);
+      const uint32_t ci = __shfl_sync(kFull, id, src);
+      if (nb_less(cd, ci, ld[k - 1], li[k - 1])) list_insert(ld, li, k, cd, ci, lane);
+    }
+    if (ended) break;
+  }
+}
+
+}  // namespace vsg

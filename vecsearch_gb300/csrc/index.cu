@@ -1,0 +1,558 @@
+// Host side of the GB300 exact index: device-resident rows, search planning,
+// kernel launches and the C ABI of include/vsg.h.
+//
+// Mirrors the reference's GpuBruteForceIndex (src/gpu_brute_force.cu:343-488):
+// grow-only device storage with zero-padded rows, one mutex per index, CUDA
+// errors surfaced as runtime errors with the failing expression. Unlike the
+// reference, the search never materialises a query x row distance block: one
+// fused scan kernel per search plus one merge kernel, on the index's own
+// stream, with queries in and results out through pinned staging buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/vsg.h"
+#include "scan.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct DeviceTimeout : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define VSG_CUDA(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t err_ = (expr);                                                            \
+    if (err_ != cudaSuccess) {                                                            \
+      if (err_ == cudaErrorMemoryAllocation) {                                            \
+        cudaGetLastError();                                                               \
+        throw std::bad_alloc();                                                           \
+      }                                                                                   \
+      throw std::runtime_error(std::string(#expr) + ": " + cudaGetErrorString(err_));     \
+    }                                                                                     \
+  } while (0)
+
+size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
+
+// Grow-only device buffer, zero-filled when (re)allocated; `keep` bytes of the old
+// contents are copied over (gpu_brute_force.cu:37-56).
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  ~DeviceBuffer() {
+    if (p_) cudaFree(p_);
+  }
+  void* get() const { return p_; }
+  size_t bytes() const { return n_; }
+  void reserve(size_t bytes, size_t keep, cudaStream_t s) {
+    if (bytes <= n_) return;
+    void* raw = nullptr;
+    VSG_CUDA(cudaMalloc(&raw, bytes));
+    cudaError_t e = cudaMemsetAsync(raw, 0, bytes, s);
+    if (e == cudaSuccess && keep) e = cudaMemcpyAsync(raw, p_, keep, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFree(raw);
+      VSG_CUDA(e);
+    }
+    if (p_) cudaFree(p_);
+    p_ = raw;
+    n_ = bytes;
+  }
+
+ private:
+  void* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+class PinnedBuffer {
+ public:
+  PinnedBuffer() = default;
+  PinnedBuffer(const PinnedBuffer&) = delete;
+  PinnedBuffer& operator=(const PinnedBuffer&) = delete;
+  ~PinnedBuffer() {
+    if (p_) cudaFreeHost(p_);
+  }
+  void* get() const { return p_; }
+  void reserve(size_t bytes) {
+    if (bytes <= n_) return;
+    void* raw = nullptr;
+    VSG_CUDA(cudaMallocHost(&raw, bytes));
+    if (p_) cudaFreeHost(p_);
+    p_ = raw;
+    n_ = bytes;
+  }
+
+ private:
+  void* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+bool host_is_pinned(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
+struct vsg_index {
+  size_t dim = 0, dp = 0;
+  uint32_t metric = 0;
+  int device = 0, sms = 1;
+  size_t smem_optin = 0;
+  size_t n = 0, cap = 0;
+  DeviceBuffer x;       // cap x dp floats
+  DeviceBuffer q;       // staged queries
+  DeviceBuffer part;    // per-split top-k lists: dists then ids
+  DeviceBuffer res;     // [status int | pad to 16][ids nq*k][dists nq*k]
+  DeviceBuffer mask;    // staged filter words
+  PinnedBuffer pin_in, pin_out;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
+  std::mutex mu;
+
+  ~vsg_index() {
+    if (stream) {
+      cudaSetDevice(device);
+      cudaStreamSynchronize(stream);
+    }
+    destroy_timings();
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int* status_word() const { return static_cast<int*>(res.get()); }
+
+  // Allocates the result block (and status word) for nq x k results.
+  void reserve_results(size_t nq, size_t k) {
+    res.reserve(16 + nq * k * 8, 0, stream);
+  }
+  uint32_t* res_ids() const { return reinterpret_cast<uint32_t*>(static_cast<char*>(res.get()) + 16); }
+  float* res_dists(size_t nq, size_t k) const {
+    return reinterpret_cast<float*>(static_cast<char*>(res.get()) + 16 + nq * k * 4);
+  }
+
+  // Reads and clears the device status word (the result block must exist).
+  void check_status_sync() {
+    int st = 0;
+    VSG_CUDA(cudaMemcpyAsync(&st, status_word(), sizeof(int), cudaMemcpyDeviceToHost, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    if (st != 0) {
+      VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
+      throw DeviceTimeout("a search kernel's wait ran past its time limit");
+    }
+  }
+
+  struct Plan {
+    vsg::ScanShape shape;
+    uint32_t stages, nsplit, rows_per_split, nqb;
+  };
+
+  Plan plan(size_t nq, size_t k) const {
+    Plan p{};
+    p.shape.l2 = metric == VSG_METRIC_L2;
+    p.shape.qb = 1;  // next power of two >= nq, at most 8
+    while (size_t(p.shape.qb) < nq && p.shape.qb < 8) p.shape.qb *= 2;
+    const size_t budget = smem_optin;
+    p.stages = 0;
+    for (int rw : {4, 2, 1}) {
+      p.shape.rw = rw;
+      const size_t fixed = vsg::scan_smem_bytes(p.shape, uint32_t(dp), uint32_t(k), 0);
+      const size_t tile = size_t(vsg::kScanWarps) * rw * dp * sizeof(float);
+      if (fixed + 2 * tile > budget) continue;
+      p.stages = uint32_t(std::min<size_t>(4, (budget - fixed) / tile));
+      break;
+    }
+    if (p.stages < 2)
+      throw std::invalid_argument("dim " + std::to_string(dim) + " with k " + std::to_string(k) +
+                                  " does not fit the scan kernel's shared memory");
+    p.nqb = uint32_t(ceil_div(nq, size_t(p.shape.qb)));
+    size_t want = std::max<size_t>(1, size_t(sms) / p.nqb);        // one CTA per SM in all
+    want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
+    p.rows_per_split = uint32_t(ceil_div(ceil_div(n, want), 32) * 32);
+    p.nsplit = uint32_t(ceil_div(n, p.rows_per_split));
+    return p;
+  }
+
+  // Queues the scan + merge for device queries (stride ldq floats) on `s`. Results go to
+  // out_ids / out_dists (device). Caller holds mu and has validated k, nq, n > 0.
+  void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
+               size_t mask_ld, uint32_t* out_ids, float* out_dists, cudaStream_t s) {
+    const Plan p = plan(nq, k);
+    const size_t parts = nq * p.nsplit * k;
+    part.reserve(parts * 8, 0, stream);
+    vsg::ScanArgs a{};
+    a.x = static_cast<const float*>(x.get());
+    a.q = dq;
+    a.ldq = uint32_t(ldq);
+    a.mask = dmask;
+    a.mask_ld = per_query ? mask_ld : 0;
+    a.part_d = static_cast<float*>(part.get());
+    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
+    a.status = status_word();
+    a.n = uint32_t(n);
+    a.dp = uint32_t(dp);
+    a.nq = uint32_t(nq);
+    a.k = uint32_t(k);
+    a.rows_per_split = p.rows_per_split;
+    a.nsplit = p.nsplit;
+    a.stages = p.stages;
+    Timing* tm = profiling ? next_timing() : nullptr;
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
+    VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
+    vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), p.nsplit, uint32_t(k)};
+    VSG_CUDA(vsg::launch_merge(m, s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
+  }
+
+  // ---- kernel timing (vsg_profile_*) ----
+  struct Timing {
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  };
+  bool profiling = false;
+  std::vector<Timing> timings;  // event pool; the first `used` are recorded
+  size_t used = 0;
+
+  Timing* next_timing() {
+    if (used == timings.size()) {
+      Timing t;
+      for (auto& e : t.ev) VSG_CUDA(cudaEventCreate(&e));
+      timings.push_back(t);
+    }
+    return &timings[used++];
+  }
+
+  void read_timings(double* scan_ms, double* merge_ms, size_t* count) {
+    double a = 0, b = 0;
+    for (size_t i = 0; i < used; ++i) {
+      VSG_CUDA(cudaEventSynchronize(timings[i].ev[2]));
+      float x = 0, y = 0;
+      VSG_CUDA(cudaEventElapsedTime(&x, timings[i].ev[0], timings[i].ev[1]));
+      VSG_CUDA(cudaEventElapsedTime(&y, timings[i].ev[1], timings[i].ev[2]));
+      a += x;
+      b += y;
+    }
+    if (scan_ms) *scan_ms = a;
+    if (merge_ms) *merge_ms = b;
+    if (count) *count = used;
+    used = 0;
+  }
+
+  void destroy_timings() {
+    for (auto& t : timings)
+      for (auto& e : t.ev)
+        if (e) cudaEventDestroy(e);
+    timings.clear();
+    used = 0;
+  }
+
+  // Host queries -> device staging (dp stride). Pageable inputs go through pinned staging.
+  const float* stage_queries(const float* host_q, size_t nq) {
+    q.reserve(nq * dp * sizeof(float), 0, stream);
+    float* dq = static_cast<float*>(q.get());
+    if (host_is_pinned(host_q)) {
+      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), host_q, dim * sizeof(float), dim * sizeof(float), nq,
+                                 cudaMemcpyHostToDevice, stream));
+    } else {
+      pin_in.reserve(nq * dim * sizeof(float));
+      std::memcpy(pin_in.get(), host_q, nq * dim * sizeof(float));
+      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), pin_in.get(), dim * sizeof(float), dim * sizeof(float),
+                                 nq, cudaMemcpyHostToDevice, stream));
+    }
+    return dq;
+  }
+
+  const uint32_t* stage_mask(const uint32_t* host_words, size_t words) {
+    mask.reserve(words * 4, 0, stream);
+    VSG_CUDA(cudaMemcpyAsync(mask.get(), host_words, words * 4, cudaMemcpyHostToDevice, stream));
+    return static_cast<const uint32_t*>(mask.get());
+  }
+
+  // Full host-to-host search: stage, enqueue, copy the result block back, check status.
+  void search_host(const float* host_q, size_t nq, size_t k, const uint32_t* host_mask, bool per_query,
+                   size_t mask_ld, uint32_t* out_ids, float* out_dists) {
+    VSG_CUDA(cudaSetDevice(device));
+    VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
+    reserve_results(nq, k);
+    const float* dq = stage_queries(host_q, nq);
+    const uint32_t* dm = nullptr;
+    if (host_mask) {
+      const size_t words = per_query ? nq * mask_ld : ceil_div(n, 32);
+      dm = stage_mask(host_mask, words);
+    }
+    uint32_t* di = res_ids();
+    float* dd = res_dists(nq, k);
+    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, di, dd, stream);
+    const size_t bytes = 16 + nq * k * 8;
+    pin_out.reserve(bytes);
+    VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));
+    VSG_CUDA(cudaEventRecord(done, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    const char* h = static_cast<const char*>(pin_out.get());
+    int st = 0;
+    std::memcpy(&st, h, sizeof(int));
+    if (st != 0) {
+      VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
+      VSG_CUDA(cudaStreamSynchronize(stream));
+      throw DeviceTimeout("a search kernel's wait ran past its time limit");
+    }
+    std::memcpy(out_ids, h + 16, nq * k * 4);
+    std::memcpy(out_dists, h + 16 + nq * k * 4, nq * k * 4);
+  }
+};
+
+namespace {
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    g_last_error.clear();
+    f();
+    return VSG_OK;
+  } catch (const std::invalid_argument& e) {
+    return fail(VSG_ERR_INVALID, e.what());
+  } catch (const std::length_error& e) {
+    return fail(VSG_ERR_LENGTH, e.what());
+  } catch (const DeviceTimeout& e) {
+    return fail(VSG_ERR_DEVICE_TIMEOUT, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(VSG_ERR_NOMEM, "out of device or pinned host memory");
+  } catch (const std::exception& e) {
+    return fail(VSG_ERR_CUDA, e.what());
+  } catch (...) {
+    return fail(VSG_ERR_CUDA, "unknown error");
+  }
+}
+
+void check_method(uint32_t method) {
+  if (method > VSG_METHOD_TILED) throw std::invalid_argument("method must be 'auto', 'naive', 'skinny' or 'tiled'");
+}
+
+void check_k(size_t k) {
+  if (k > VSG_MAX_K) throw std::invalid_argument("k must be <= " + std::to_string(VSG_MAX_K));
+}
+
+void fill_missing_host(uint32_t* ids, float* dists, size_t count) {
+  std::fill(ids, ids + count, VSG_NONE);
+  std::fill(dists, dists + count, __builtin_inff());
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsg_cuda_available(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return count > 0 ? 1 : 0;
+}
+
+const char* vsg_last_error(void) { return g_last_error.c_str(); }
+
+int vsg_create(size_t dim, uint32_t metric, int device, vsg_index** out) {
+  if (!out) return fail(VSG_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  return guarded([&] {
+    if (dim == 0) throw std::invalid_argument("dim must be > 0");
+    if (metric != VSG_METRIC_L2 && metric != VSG_METRIC_IP)
+      throw std::invalid_argument("metric must be 'l2', 'ip' or 'cosine' (cosine expects normalized vectors)");
+    auto* h = new vsg_index();
+    try {
+      h->dim = dim;
+      h->dp = (dim + 7) / 8 * 8;
+      h->metric = metric;
+      h->device = device;
+      VSG_CUDA(cudaSetDevice(device));
+      cudaDeviceProp prop;
+      VSG_CUDA(cudaGetDeviceProperties(&prop, device));
+      h->sms = prop.multiProcessorCount;
+      h->smem_optin = prop.sharedMemPerBlockOptin;
+      VSG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+      VSG_CUDA(cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming));
+      VSG_CUDA(cudaEventRecord(h->done, h->stream));
+      h->reserve_results(1, 1);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+void vsg_destroy(vsg_index* h) { delete h; }
+
+int vsg_add(vsg_index* h, const float* rows, size_t m) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    if (m == 0) return;
+    if (!rows) throw std::invalid_argument("rows is NULL");
+    if (h->n + m >= VSG_NONE) throw std::length_error("GpuBruteForceIndex holds at most 2^32 - 2 vectors");
+    VSG_CUDA(cudaSetDevice(h->device));
+    VSG_CUDA(cudaStreamWaitEvent(h->stream, h->done, 0));
+    if (h->n + m > h->cap) {
+      const size_t cap = std::max({h->n + m, h->cap * 2, size_t(1024)});
+      h->x.reserve(cap * h->dp * sizeof(float), h->n * h->dp * sizeof(float), h->stream);
+      h->cap = cap;
+    }
+    float* dst = static_cast<float*>(h->x.get()) + h->n * h->dp;
+    VSG_CUDA(cudaMemcpy2DAsync(dst, h->dp * sizeof(float), rows, h->dim * sizeof(float), h->dim * sizeof(float), m,
+                               cudaMemcpyHostToDevice, h->stream));
+    VSG_CUDA(cudaEventRecord(h->done, h->stream));
+    VSG_CUDA(cudaStreamSynchronize(h->stream));
+    h->n += m;
+  });
+}
+
+int vsg_search(vsg_index* h, const float* queries, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
+               uint32_t method) {
+  return vsg_search_filtered(h, queries, nq, k, nullptr, 0, 0, out_ids, out_dists, method);
+}
+
+int vsg_search_filtered(vsg_index* h, const float* queries, size_t nq, size_t k, const uint32_t* mask_words,
+                        int per_query, size_t mask_ld, uint32_t* out_ids, float* out_dists, uint32_t method) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    check_method(method);
+    check_k(k);
+    if (nq == 0 || k == 0) return;
+    if (!queries || !out_ids || !out_dists) throw std::invalid_argument("NULL query or output pointer");
+    std::lock_guard<std::mutex> g(h->mu);
+    if (mask_words && per_query && mask_ld < ceil_div(h->n, 32))
+      throw std::invalid_argument("mask_ld must be >= ceil(size / 32)");
+    if (h->n == 0) {
+      fill_missing_host(out_ids, out_dists, nq * k);
+      return;
+    }
+    h->search_host(queries, nq, k, mask_words, mask_words && per_query, mask_ld, out_ids, out_dists);
+  });
+}
+
+int vsg_hnsw_exact_below(vsg_index* h, const float* queries, size_t nq, size_t k, const uint8_t* allowed,
+                         size_t allowed_len, size_t exact_below, uint32_t* out_ids, float* out_dists,
+                         int* handled) {
+  if (!h || !handled) return fail(VSG_ERR_INVALID, "index or handled is NULL");
+  *handled = 0;
+  return guarded([&] {
+    check_k(k);
+    if (!allowed) return;  // no filter: the graph path (hnsw.cpp:329-333)
+    std::lock_guard<std::mutex> g(h->mu);
+    if (allowed_len != h->n) throw std::invalid_argument("filter must be a 1-D bool array of length " +
+                                                         std::to_string(h->n));
+    size_t n_allowed = 0;
+    for (size_t i = 0; i < allowed_len; ++i) n_allowed += allowed[i] != 0;
+    if (n_allowed != 0 && n_allowed > exact_below) return;  // graph path
+    *handled = 1;
+    if (nq == 0 || k == 0) return;
+    if (!queries || !out_ids || !out_dists) throw std::invalid_argument("NULL query or output pointer");
+    if (n_allowed == 0) {
+      fill_missing_host(out_ids, out_dists, nq * k);
+      return;
+    }
+    std::vector<uint32_t> words(ceil_div(h->n, 32), 0u);
+    for (size_t i = 0; i < allowed_len; ++i)
+      if (allowed[i]) words[i >> 5] |= 1u << (i & 31);
+    h->search_host(queries, nq, k, words.data(), false, 0, out_ids, out_dists);
+  });
+}
+
+int vsg_search_device(vsg_index* h, const float* d_queries, size_t ldq, size_t nq, size_t k,
+                      const uint32_t* d_mask_words, int per_query, size_t mask_ld, uint32_t* d_out_ids,
+                      float* d_out_dists, uint32_t method, void* stream) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    check_method(method);
+    check_k(k);
+    if (nq == 0 || k == 0) return;
+    if (!d_queries || !d_out_ids || !d_out_dists) throw std::invalid_argument("NULL query or output pointer");
+    if (ldq < h->dim) throw std::invalid_argument("ldq must be >= dim");
+    std::lock_guard<std::mutex> g(h->mu);
+    if (d_mask_words && per_query && mask_ld < ceil_div(h->n, 32))
+      throw std::invalid_argument("mask_ld must be >= ceil(size / 32)");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    VSG_CUDA(cudaSetDevice(h->device));
+    VSG_CUDA(cudaStreamWaitEvent(s, h->done, 0));
+    if (h->n == 0) {
+      VSG_CUDA(vsg::launch_fill_missing(d_out_dists, d_out_ids, nq * k, s));
+    } else {
+      const float* dq = d_queries;
+      size_t ld = ldq;
+      // The kernel reads dp floats per query row and 16-byte chunks: use the caller's rows in
+      // place only when they need no zero padding and are aligned; else repack (pads stay zero).
+      const bool direct = h->dim == h->dp && ldq % 4 == 0 && reinterpret_cast<uintptr_t>(d_queries) % 16 == 0;
+      if (!direct) {
+        h->q.reserve(nq * h->dp * sizeof(float), 0, h->stream);
+        VSG_CUDA(cudaMemcpy2DAsync(h->q.get(), h->dp * sizeof(float), d_queries, ldq * sizeof(float),
+                                   h->dim * sizeof(float), nq, cudaMemcpyDeviceToDevice, s));
+        dq = static_cast<const float*>(h->q.get());
+        ld = h->dp;
+      }
+      h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, d_out_ids, d_out_dists, s);
+    }
+    VSG_CUDA(cudaEventRecord(h->done, s));
+  });
+}
+
+int vsg_sync(vsg_index* h) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    VSG_CUDA(cudaStreamWaitEvent(h->stream, h->done, 0));
+    h->check_status_sync();
+  });
+}
+
+size_t vsg_size(const vsg_index* h) { return h ? h->n : 0; }
+size_t vsg_dim(const vsg_index* h) { return h ? h->dim : 0; }
+uint32_t vsg_metric(const vsg_index* h) { return h ? h->metric : 0; }
+
+const float* vsg_device_rows(const vsg_index* h, size_t* padded_dim) {
+  if (!h) return nullptr;
+  if (padded_dim) *padded_dim = h->dp;
+  return static_cast<const float*>(h->x.get());
+}
+
+int vsg_profile_enable(vsg_index* h, int enable) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    h->read_timings(nullptr, nullptr, nullptr);
+    h->profiling = enable != 0;
+  });
+}
+
+int vsg_profile_read(vsg_index* h, double* scan_ms, double* merge_ms, size_t* searches) {
+  if (!h) return fail(VSG_ERR_INVALID, "index is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    h->read_timings(scan_ms, merge_ms, searches);
+  });
+}
+
+}  // extern "C"

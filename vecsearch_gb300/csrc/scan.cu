@@ -1,0 +1,342 @@
+// Fused exact scan + top-k for FP32 rows resident in HBM (sm_103a).
+//
+// Replaces the reference's distance-block + select round trip
+// (src/gpu_brute_force.cu:97-140 skinny_kernel, :220-292 select_kernel, :475-482
+// merge loop): no query x row score block is ever written to memory.
+//
+// Grid (query blocks, row splits). Each CTA owns QB queries and one contiguous
+// row range of the base:
+//   * a producer warp streams tiles of R = 8*RW consecutive rows into a ring of
+//     shared-memory slots with bulk (TMA) copies, one mbarrier pair per slot;
+//   * 8 consumer warps each take RW rows of a tile. Lanes split the dims in
+//     16-byte chunks (lane l reads chunks l, l+32, ...: conflict-free), every
+//     lane accumulates RW x QB partial dot products (or squared differences),
+//     and a warp reduce-scatter leaves one finished distance per lane;
+//   * a distance enters the warp's sorted top-k list of its query when it beats
+//     the list's last entry in (dist, id) order and the row passes the filter
+//     bit. Tiles whose filter bits are all clear for the CTA's queries are
+//     skipped before they are loaded.
+// At the end the 8 warp lists of each query are merged and written as the
+// split's top-k; merge_kernel then merges the splits.
+#include <mutex>
+
+#include "device_common.cuh"
+#include "scan.cuh"
+
+namespace vsg {
+
+namespace {
+
+__host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
+
+struct SmemLayout {
+  size_t q_off, ring_off, ld_off, li_off, total;
+};
+
+__host__ __device__ inline SmemLayout scan_layout(int qb, int rw, uint32_t dp, uint32_t k, uint32_t stages) {
+  SmemLayout L;
+  const size_t bars = 2 * kMaxStages * sizeof(uint64_t);
+  L.q_off = align128(bars);
+  L.ring_off = L.q_off + align128(size_t(qb) * dp * sizeof(float));
+  const size_t tile = size_t(kScanWarps) * rw * dp * sizeof(float);
+  L.ld_off = L.ring_off + align128(size_t(stages) * tile);
+  const size_t lists = size_t(kScanWarps) * qb * k * sizeof(float);
+  L.li_off = L.ld_off + align128(lists);
+  L.total = L.li_off + align128(lists);
+  return L;
+}
+
+template <bool L2>
+__device__ __forceinline__ float acc4(const float4 q, const float4 x, float a) {
+  if constexpr (L2) {
+    float e = q.x - x.x;
+    a = fmaf(e, e, a);
+    e = q.y - x.y;
+    a = fmaf(e, e, a);
+    e = q.z - x.z;
+    a = fmaf(e, e, a);
+    e = q.w - x.w;
+    return fmaf(e, e, a);
+  } else {
+    a = fmaf(q.x, x.x, a);
+    a = fmaf(q.y, x.y, a);
+    a = fmaf(q.z, x.z, a);
+    return fmaf(q.w, x.w, a);
+  }
+}
+
+// True when no query of the block may return any row of the tile [r0, r0 + R).
+template <int QB, int R>
+__device__ __forceinline__ bool tile_filtered_out(const ScanArgs& a, uint32_t qbase, uint32_t r0) {
+  const uint32_t w = r0 >> 5;
+  const uint32_t span = R >= 32 ? 0xFFFFFFFFu : (((1u << R) - 1u) << (r0 & 31));
+  uint32_t any = 0;
+  if (a.mask_ld == 0) {
+    any = __ldg(a.mask + w);
+  } else {
+#pragma unroll
+    for (int b = 0; b < QB; ++b)
+      if (qbase + b < a.nq) any |= __ldg(a.mask + (qbase + b) * a.mask_ld + w);
+  }
+  return (any & span) == 0;
+}
+
+template <int QB, int RW, bool L2>
+__global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a) {
+  constexpr int R = kScanWarps * RW;  // rows per tile
+  constexpr int V = RW * QB;          // partial sums per lane
+  constexpr int G = 32 / V;           // lanes sharing one finished distance
+  static_assert(V <= 32 && (V & (V - 1)) == 0, "RW * QB must be a power of two <= 32");
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t dp = a.dp, nc = dp / 4, k = a.k;
+  const SmemLayout L = scan_layout(QB, RW, dp, k, a.stages);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + kMaxStages;
+  float* qs = reinterpret_cast<float*>(smem + L.q_off);
+  float* ring = reinterpret_cast<float*>(smem + L.ring_off);
+  float* lst_d = reinterpret_cast<float*>(smem + L.ld_off);
+  uint32_t* lst_i = reinterpret_cast<uint32_t*>(smem + L.li_off);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t qbase = blockIdx.x * QB;
+  const uint32_t split = blockIdx.y;
+  const uint32_t row_begin = split * a.rows_per_split;
+  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
+  const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + R - 1) / R : 0;
+  const uint32_t stages = a.stages;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kScanWarps);
+    }
+    mbar_fence_init();
+  }
+  {  // queries of the block (rows >= nq become zeros), and empty lists
+    float4* qs4 = reinterpret_cast<float4*>(qs);
+    for (uint32_t i = tid; i < QB * nc; i += kScanThreads) {
+      const uint32_t b = i / nc, c = i % nc;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (qbase + b < a.nq) v = *reinterpret_cast<const float4*>(a.q + size_t(qbase + b) * a.ldq + c * 4);
+      qs4[i] = v;
+    }
+    for (uint32_t i = tid; i < kScanWarps * QB * k; i += kScanThreads) {
+      lst_d[i] = __int_as_float(0x7f800000);
+      lst_i[i] = kNone;
+    }
+  }
+  __syncthreads();
+
+  if (warp == kScanWarps) {
+    // ---------------- producer: one lane streams the row tiles ----------------
+    if (lane == 0) {
+      const uint64_t policy = policy_evict_first();
+      uint32_t s = 0, ph = 0;
+      uint32_t pending = 0, last_ph = 0;  // per-slot bit: a copy was issued; parity of that issue
+      bool ok = true;
+      for (uint32_t t = 0; t < ntiles; ++t) {
+        const uint32_t r0 = row_begin + t * R;
+        if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0)) continue;
+        if (!mbar_wait(&empty[s], ph ^ 1)) {
+          ok = false;
+          break;
+        }
+        const uint32_t rows = min(uint32_t(R), row_end - r0);
+        const uint32_t bytes = rows * dp * uint32_t(sizeof(float));
+        mbar_arrive_expect_tx(&full[s], bytes);
+        bulk_load_stream(ring + size_t(s) * R * dp, a.x + size_t(r0) * dp, bytes, &full[s], policy);
+        pending |= 1u << s;
+        last_ph = (last_ph & ~(1u << s)) | (ph << s);
+        if (++s == stages) {
+          s = 0;
+          ph ^= 1;
+        }
+      }
+      // Wait (bounded) until every issued copy has landed before the CTA may exit.
+      for (uint32_t i = 0; i < stages; ++i)
+        if ((pending >> i) & 1u)
+          if (!mbar_wait(&full[i], (last_ph >> i) & 1u)) ok = false;
+      if (!ok) atomicExch(a.status, kDevTimeout);
+    }
+  } else {
+    // ---------------- consumers ----------------
+    float* my_d = lst_d + size_t(warp) * QB * k;
+    uint32_t* my_i = lst_i + size_t(warp) * QB * k;
+    const float4* qs4 = reinterpret_cast<const float4*>(qs);
+    const int vi = lane / G;  // value this lane finishes
+    const int vr = vi / QB, vb = vi % QB;
+    const bool owner = (lane % G) == 0;
+    uint32_t s = 0, ph = 0;
+    bool ok = true;
+    for (uint32_t t = 0; t < ntiles && ok; ++t) {
+      const uint32_t r0 = row_begin + t * R;
+      if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0)) continue;
+      // warp-uniform decision, so no lane leaves while the others shuffle
+      if (!__all_sync(kFull, mbar_wait(&full[s], ph))) {
+        ok = false;
+        if (lane == 0) atomicExch(a.status, kDevTimeout);
+        break;
+      }
+      const float4* xs4 = reinterpret_cast<const float4*>(ring + size_t(s) * R * dp) + size_t(warp) * RW * nc;
+      float acc[V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) acc[i] = 0.f;
+#pragma unroll 2
+      for (uint32_t c = lane; c < nc; c += 32) {
+        float4 xv[RW];
+#pragma unroll
+        for (int r = 0; r < RW; ++r) xv[r] = xs4[r * nc + c];
+#pragma unroll
+        for (int b = 0; b < QB; ++b) {
+          const float4 qv = qs4[b * nc + c];
+#pragma unroll
+          for (int r = 0; r < RW; ++r) acc[r * QB + b] = acc4<L2>(qv, xv[r], acc[r * QB + b]);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (++s == stages) {
+        s = 0;
+        ph ^= 1;
+      }
+
+      ReduceScatter<V, 16>::run(acc, lane);
+      const float dist = L2 ? acc[0] : 1.0f - acc[0];
+      const uint32_t lrow = uint32_t(warp * RW + vr);
+      const uint32_t row = r0 + lrow;
+      bool pass = owner && row < row_end && qbase + vb < a.nq;  // padded query slots never compete
+      if (pass && a.mask) {
+        const uint32_t* m = a.mask + (a.mask_ld ? (qbase + vb) * a.mask_ld : 0);
+        pass = (__ldg(m + (row >> 5)) >> (row & 31)) & 1u;
+      }
+      if (pass) pass = nb_less(dist, row, my_d[vb * k + k - 1], my_i[vb * k + k - 1]);
+      unsigned bal = __ballot_sync(kFull, pass);
+      while (bal) {
+        const int src = __ffs(bal) - 1;
+        bal &= bal - 1;
+        const float cd = __shfl_sync(kFull, dist, src);
+        const uint32_t ci = __shfl_sync(kFull, row, src);
+        const int cb = (src / G) % QB;
+        float* ld = my_d + cb * k;
+        uint32_t* li = my_i + cb * k;
+        if (nb_less(cd, ci, ld[k - 1], li[k - 1])) list_insert(ld, li, int(k), cd, ci, lane);
+      }
+    }
+  }
+  __syncthreads();
+
+  // Merge the 8 warp lists of each query into warp 0's list, then write the split's top-k.
+  if (warp < QB) {
+    const int b = warp;
+    float* ld = lst_d + size_t(b) * k;  // warp 0's list for query b
+    uint32_t* li = lst_i + size_t(b) * k;
+    for (int w = 1; w < kScanWarps; ++w)
+      list_merge_sorted(ld, li, int(k), lst_d + (size_t(w) * QB + b) * k, lst_i + (size_t(w) * QB + b) * k,
+                        int(k), lane);
+    const uint32_t qg = qbase + b;
+    if (qg < a.nq) {
+      const size_t o = (size_t(qg) * a.nsplit + split) * k;
+      for (uint32_t j = lane; j < k; j += 32) {
+        a.part_d[o + j] = ld[j];
+        a.part_i[o + j] = li[j];
+      }
+    }
+  }
+}
+
+// One CTA per query: warps merge the splits' lists, then warp 0 merges the warps' lists.
+__global__ void __launch_bounds__(256) merge_kernel(const MergeArgs m) {
+  __shared__ float ld[8][kMaxK];
+  __shared__ uint32_t li[8][kMaxK];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t q = blockIdx.x, k = m.k;
+  for (uint32_t j = lane; j < k; j += 32) {
+    ld[warp][j] = __int_as_float(0x7f800000);
+    li[warp][j] = kNone;
+  }
+  __syncwarp();
+  for (uint32_t s = warp; s < m.nsplit; s += 8) {
+    const size_t o = (size_t(q) * m.nsplit + s) * k;
+    list_merge_sorted(ld[warp], li[warp], int(k), m.part_d + o, m.part_i + o, int(k), lane);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    for (int w = 1; w < 8; ++w) list_merge_sorted(ld[0], li[0], int(k), ld[w], li[w], int(k), lane);
+    for (uint32_t j = lane; j < k; j += 32) {
+      m.out_d[size_t(q) * k + j] = ld[0][j];
+      m.out_i[size_t(q) * k + j] = li[0][j];
+    }
+  }
+}
+
+__global__ void fill_missing_kernel(float* d, uint32_t* i, size_t count) {
+  for (size_t j = blockIdx.x * size_t(blockDim.x) + threadIdx.x; j < count; j += size_t(gridDim.x) * blockDim.x) {
+    d[j] = __int_as_float(0x7f800000);
+    i[j] = kNone;
+  }
+}
+
+template <int QB, int RW, bool L2>
+cudaError_t launch_one(const ScanArgs& a, dim3 grid, cudaStream_t stream) {
+  const size_t smem = scan_layout(QB, RW, a.dp, a.k, a.stages).total;
+  // Largest dynamic shared-memory size already allowed for this instantiation, per device.
+  static std::mutex mu;
+  static size_t configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 64 || smem > configured[dev]) {
+      e = cudaFuncSetAttribute(scan_kernel<QB, RW, L2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      if (dev < 64) configured[dev] = smem;
+    }
+  }
+  scan_kernel<QB, RW, L2><<<grid, kScanThreads, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+template <int QB, int RW>
+cudaError_t launch_metric(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st) {
+  return s.l2 ? launch_one<QB, RW, true>(a, grid, st) : launch_one<QB, RW, false>(a, grid, st);
+}
+
+template <int QB>
+cudaError_t launch_rw(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st) {
+  switch (s.rw) {
+    case 1: return launch_metric<QB, 1>(s, a, grid, st);
+    case 2: return launch_metric<QB, 2>(s, a, grid, st);
+    default: return launch_metric<QB, 4>(s, a, grid, st);
+  }
+}
+
+}  // namespace
+
+size_t scan_smem_bytes(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t stages) {
+  return scan_layout(s.qb, s.rw, dp, k, stages).total;
+}
+
+cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream) {
+  switch (s.qb) {
+    case 1: return launch_rw<1>(s, a, grid, stream);
+    case 2: return launch_rw<2>(s, a, grid, stream);
+    case 4: return launch_rw<4>(s, a, grid, stream);
+    default: return launch_rw<8>(s, a, grid, stream);
+  }
+}
+
+cudaError_t launch_merge(const MergeArgs& m, cudaStream_t stream) {
+  merge_kernel<<<m.nq, 256, 0, stream>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_missing(float* out_d, uint32_t* out_i, size_t count, cudaStream_t stream) {
+  if (count == 0) return cudaSuccess;
+  const unsigned blocks = unsigned(count / 256 + 1 < 1024 ? count / 256 + 1 : 1024);
+  fill_missing_kernel<<<blocks, 256, 0, stream>>>(out_d, out_i, count);
+  return cudaGetLastError();
+}
+
+}  // namespace vsg

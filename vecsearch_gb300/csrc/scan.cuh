@@ -1,0 +1,51 @@
+// Launch interface of the exact-scan kernels (host side). Argument blocks are
+// plain structs so they can be filled by the index code and by tests alike.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace vsg {
+
+constexpr int kScanWarps = 8;                       // consumer warps per scan CTA
+constexpr int kScanThreads = (kScanWarps + 1) * 32;  // + one producer warp
+constexpr int kMaxStages = 8;
+
+// One fused pass: distances of a block of QB queries against a row range, the
+// filter applied per (query, row), and each warp's running top-k.
+struct ScanArgs {
+  const float* x;          // base rows, n x dp floats (dp = padded dim, multiple of 8)
+  const float* q;          // queries, row stride ldq floats; rows >= nq are never read
+  const uint32_t* mask;    // nullptr, or allow-bits: bit (r & 31) of word (r >> 5)
+  uint64_t mask_ld;        // words between two queries' masks; 0 = one mask for all queries
+  float* part_d;           // [nq][nsplit][k] per-split top-k, sorted by (dist, id)
+  uint32_t* part_i;
+  int* status;             // device status word (kDevOk / kDevTimeout)
+  uint32_t n, dp, ldq, nq, k;
+  uint32_t rows_per_split;  // multiple of 32
+  uint32_t nsplit;
+  uint32_t stages;          // ring depth (2..kMaxStages)
+};
+
+struct MergeArgs {
+  const float* part_d;
+  const uint32_t* part_i;
+  float* out_d;            // [nq][k]
+  uint32_t* out_i;
+  uint32_t nq, nsplit, k;
+};
+
+struct ScanShape {
+  int qb;      // queries per CTA: 1, 2, 4 or 8
+  int rw;      // rows per warp per tile: 1, 2 or 4 (tile = 8 * rw rows)
+  bool l2;
+};
+
+// Shared-memory bytes the scan kernel needs for a shape, dim and k with `stages` ring slots.
+size_t scan_smem_bytes(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t stages);
+
+cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream);
+cudaError_t launch_merge(const MergeArgs& m, cudaStream_t stream);
+cudaError_t launch_fill_missing(float* out_d, uint32_t* out_i, size_t count, cudaStream_t stream);
+
+}  // namespace vsg

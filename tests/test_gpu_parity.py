@@ -25,7 +25,7 @@ def assert_parity(ids, dists, want_i, want_d, x, q, metric):
     np.testing.assert_allclose(dists, want_d, rtol=RTOL, atol=ATOL)
     O.check_ids(ids, want64, x, q, metric, rel=REL_TIE)
     fin = np.isfinite(dists)
-    assert np.all(np.diff(np.where(fin, dists, np.inf), axis=1) >= 0)
+    assert np.all(np.diff(np.where(fin, dists, np.finfo(np.float32).max), axis=1) >= 0)
     assert ((ids >= 0) == fin).all()
 
 

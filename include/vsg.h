@@ -125,6 +125,26 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
 int vsg_profile_enable(vsg_index* index, int enable);
 int vsg_profile_read(vsg_index* index, double* scan_ms, double* merge_ms, size_t* searches);
 
+/* Exact top-k over caller-owned device buffers, for callers that cannot allocate device memory
+ * on their search path (a serving thread that must not stall on cudaMalloc / cudaFree, which can
+ * synchronise the device; a host framework that owns all device memory through its own pool; a
+ * plugin handed only its buffers). No counterpart in the reference: it has no allocation-free form.
+ *
+ * d_rows: n x dim device floats (row stride dim); d_queries: nq x dim device floats; dim a multiple
+ * of 4, both pointers 16-byte aligned. Results go to d_out_ids / d_out_dists (nq x k, device), with
+ * the same order and padding as vsg_search. Work is queued on `stream` (a cudaStream_t, NULL =
+ * legacy default stream), and the call waits for it so it can report a device-side failure.
+ *
+ * It allocates nothing: its scratch (the per-split top-k lists and a status word) is one static
+ * 4 MiB device array in the library, which every GPU that loads the library holds until exit.
+ * The first call on a device looks up that array's device address (set-up, once per device, with
+ * the device current); make that first call before any stream capture. nq x splits x k top-k
+ * entries beyond the array (at most 524,256; splits is up to one per SM for small batches) are
+ * rejected with VSG_ERR_INVALID. Every call shares the array and it keeps the last call's contents;
+ * calls whose device work overlaps (two streams, two threads) race on it and give wrong results. */
+int vsg_search_rows_noalloc(const float* d_rows, size_t n, size_t dim, uint32_t metric, const float* d_queries,
+                            size_t nq, size_t k, uint32_t* d_out_ids, float* d_out_dists, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -98,6 +98,15 @@ class PinnedBuffer {
   size_t n_ = 0;
 };
 
+}  // namespace
+
+namespace vsg {
+// The calling thread's vsg_last_error() text, for entry points defined in other files.
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace vsg
+
+namespace {
+
 bool host_is_pinned(const void* p) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {

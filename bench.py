@@ -37,7 +37,10 @@ sys.path.insert(0, ROOT)
 
 # DRAM bytes per scan launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum),
 # keyed by (n, dim, batch, k, metric); the summaries are committed under profiles/.
-MEASURED_TRAFFIC = {}
+# The 1M-row entry is the 262,144-row capture (profiles/scan_kernel_1Mx384_b1.md: 402.69 MB read +
+# 3.31 MB written per launch) scaled by rows scanned (x 1,000,000 / 262,144); reads equal the
+# algorithmic bytes there, so traffic grows in proportion to the rows.
+MEASURED_TRAFFIC = {(1_000_000, 384, 1, 10, "ip"): 1_548_800_000}
 
 
 def parse():
@@ -57,6 +60,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
+    ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
     return ap.parse_args()
 
 
@@ -210,6 +214,45 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None):
     return ms, scan_ms, merge_ms, launches
 
 
+def filtered_sweep(idx, torch, x, q, a, stream, batch=16, targets=(100, 1000, 10000, 50000, 100000, 200000)):
+    """Config 3: Zipf(1.1) group labels over 2,000 groups; each query filters to one group (per-query
+    1M-bit masks on the device). For groups near each allowed count, device QPS of the gather scan
+    (reads only allowed rows) and of the masked full scan (reads every tile holding an allowed row)."""
+    from vecsearch_gb300 import datasets as D
+    groups = D.zipf_groups(a.n, 2000, 1.1, seed=3)
+    sizes = np.bincount(groups, minlength=2000)
+    qd = torch.from_numpy(q[:batch]).to(x.device if hasattr(x, "device") else "cuda")
+    out_i = torch.empty((batch, a.k), dtype=torch.int32, device=qd.device)
+    out_d = torch.empty((batch, a.k), dtype=torch.float32, device=qd.device)
+    res = []
+    for t in targets:
+        g = int(np.argmin(np.abs(sizes - t)))
+        words = D.group_masks(groups, [g] * batch)
+        wd = torch.from_numpy(words.view(np.int32)).to(qd.device)
+        row = {"target": t, "allowed": int(sizes[g]), "batch": batch}
+        for mode, frac in (("gather", 1.0), ("masked_full_scan", 0.0)):
+            idx.set_tunable("gather_max_fraction", frac)
+            steps = 20
+            for i in range(steps + 3):
+                if i == 3:
+                    torch.cuda.synchronize()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                idx.search_device(qd.data_ptr(), a.dim, batch, a.k, out_i.data_ptr(), out_d.data_ptr(),
+                                  stream=stream.cuda_stream, mask_ptr=wd.data_ptr(), per_query=True,
+                                  mask_ld=words.shape[1])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            row[mode + "_qps"] = round(batch / (ms / 1e3), 1)
+            row[mode + "_ms"] = round(ms, 4)
+        res.append(row)
+    idx.set_tunable("gather_max_fraction", 1.0)
+    idx.sync()
+    return res
+
+
 def run_ours(a):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -287,6 +330,9 @@ def run_ours(a):
                           "scan_gbs": round((a.n * a.dim * 4) / (scan_b / l_b / 1e3) / 1e9, 1),
                           "scan_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)})
         extra["sweep"] = sweep
+
+    if rank == 0 and world == 1 and a.metric == "ip" and not a.no_filtered:
+        extra["filtered_sweep"] = filtered_sweep(idx, torch, qd, q, a, stream)
 
     if rank == 0 and not a.no_recall:
         from oracle import oracle as O

@@ -118,6 +118,15 @@ uint32_t vsg_metric(const vsg_index* index);
  * dim, for zero-copy consumers of the index (e.g. a ground-truth or rerank pass). */
 const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
 
+/* Named tunables of an index (new; the reference fixes its tunables at compile time,
+ * src/gpu_brute_force.cu:23-31). Unknown names or out-of-range values -> VSG_ERR_INVALID.
+ *   "gather_max_fraction" (default 0.10): a filtered search reads only the allowed rows (gather
+ *   mode) when the largest allowed fraction of its masks is at most this, else it scans every
+ *   tile holding an allowed row (masked full scan). Device-resident masks are not counted:
+ *   they use gather mode unless the value is 0. */
+int vsg_set_tunable(vsg_index* index, const char* name, double value);
+int vsg_get_tunable(vsg_index* index, const char* name, double* value);
+
 /* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
  * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for
  * the recorded events, returns the summed milliseconds and the number of searches, and clears

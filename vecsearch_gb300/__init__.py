@@ -160,6 +160,15 @@ class GpuBruteForceIndex:
         """Wait for queued device work; raises if a kernel reported a failure."""
         _native.check(_native.lib().vsg_sync(self._h))
 
+    def set_tunable(self, name, value):
+        """Set a named tunable (e.g. "gather_max_fraction"); see include/vsg.h."""
+        _native.check(_native.lib().vsg_set_tunable(self._h, name.encode(), float(value)))
+
+    def get_tunable(self, name):
+        v = ctypes.c_double()
+        _native.check(_native.lib().vsg_get_tunable(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
     def profile(self, enable=True):
         """Start (or stop) recording CUDA-event times of the scan and merge kernels."""
         _native.check(_native.lib().vsg_profile_enable(self._h, int(enable)))

@@ -40,6 +40,8 @@ SIGNATURES = {
     "vsg_profile_enable": (_INT, [_P, _INT]),
     "vsg_profile_read": (_INT, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(_SZ)]),
+    "vsg_set_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.c_double]),
+    "vsg_get_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
     "vsg_search_rows_noalloc": (_INT, [_P, _SZ, _SZ, _U32, _P, _SZ, _SZ, _P, _P, _P]),
 }
 

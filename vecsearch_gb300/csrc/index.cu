@@ -133,6 +133,11 @@ struct vsg_index {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
   std::mutex mu;
+  // Filtered searches read only the allowed rows (gather mode) when the allowed fraction is
+  // at most this; above it they scan every tile that holds an allowed row (masked full scan).
+  // 0.10 from the filtered sweep on GB300 (1M x 384, batch 16): gather wins up to ~8 % allowed,
+  // the masked full scan from ~17 %, where it shares each loaded tile among 8 queries.
+  double gather_max_fraction = 0.10;
 
   ~vsg_index() {
     if (stream) {
@@ -171,11 +176,13 @@ struct vsg_index {
     uint32_t stages, nsplit, rows_per_split, nqb;
   };
 
-  Plan plan(size_t nq, size_t k) const {
+  // filtered: the scan runs in gather mode; per_query: every query has its own mask.
+  Plan plan(size_t nq, size_t k, bool filtered = false, bool per_query = false) const {
     Plan p{};
     p.shape.l2 = metric == VSG_METRIC_L2;
-    p.shape.qb = 1;  // next power of two >= nq, at most 8
-    while (size_t(p.shape.qb) < nq && p.shape.qb < 8) p.shape.qb *= 2;
+    p.shape.qb = 1;  // next power of two >= nq, at most 8; one query per CTA for per-query masks,
+                     // so a CTA never loads rows only other queries may return
+    while (!per_query && size_t(p.shape.qb) < nq && p.shape.qb < 8) p.shape.qb *= 2;
     const size_t budget = smem_optin;
     p.stages = 0;
     for (int rw : {4, 2, 1}) {
@@ -190,8 +197,16 @@ struct vsg_index {
       throw std::invalid_argument("dim " + std::to_string(dim) + " with k " + std::to_string(k) +
                                   " does not fit the scan kernel's shared memory");
     p.nqb = uint32_t(ceil_div(nq, size_t(p.shape.qb)));
-    size_t want = std::max<size_t>(1, size_t(sms) / p.nqb);        // one CTA per SM in all
-    want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
+    size_t want;
+    if (!filtered) {
+      want = std::max<size_t>(1, size_t(sms) / p.nqb);              // one CTA per SM in all
+      want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
+    } else {
+      // Allowed rows are spread unevenly over queries and row ranges: cap a split at 32K rows
+      // and aim for two CTAs per SM, with at least 1024 rows per split.
+      want = std::max(ceil_div(n, 32768), ceil_div(2 * size_t(sms), p.nqb));
+      want = std::max<size_t>(1, std::min(want, ceil_div(n, 1024)));
+    }
     p.rows_per_split = uint32_t(ceil_div(ceil_div(n, want), 32) * 32);
     p.nsplit = uint32_t(ceil_div(n, p.rows_per_split));
     return p;
@@ -200,8 +215,9 @@ struct vsg_index {
   // Queues the scan + merge for device queries (stride ldq floats) on `s`. Results go to
   // out_ids / out_dists (device). Caller holds mu and has validated k, nq, n > 0.
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
-               size_t mask_ld, uint32_t* out_ids, float* out_dists, cudaStream_t s) {
-    const Plan p = plan(nq, k);
+               size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s) {
+    gather = gather && dmask != nullptr;
+    const Plan p = plan(nq, k, gather, gather && per_query);
     const size_t parts = nq * p.nsplit * k;
     part.reserve(parts * 8, 0, stream);
     vsg::ScanArgs a{};
@@ -220,6 +236,7 @@ struct vsg_index {
     a.rows_per_split = p.rows_per_split;
     a.nsplit = p.nsplit;
     a.stages = p.stages;
+    a.gather = gather ? 1u : 0u;
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
@@ -292,6 +309,21 @@ struct vsg_index {
     return static_cast<const uint32_t*>(mask.get());
   }
 
+  // Largest fraction of rows any of `masks` masks (ld words apart) allows.
+  double allowed_fraction(const uint32_t* words, size_t masks, size_t ld) const {
+    const size_t nw = ceil_div(n, 32);
+    size_t best = 0;
+    for (size_t m = 0; m < masks; ++m) {
+      const uint32_t* w = words + m * ld;
+      size_t c = 0;
+      for (size_t i = 0; i + 1 < nw; ++i) c += size_t(__builtin_popcount(w[i]));
+      const uint32_t tail = (n % 32) ? (1u << (n % 32)) - 1u : 0xFFFFFFFFu;
+      c += size_t(__builtin_popcount(w[nw - 1] & tail));
+      best = std::max(best, c);
+    }
+    return n ? double(best) / double(n) : 0.0;
+  }
+
   // Full host-to-host search: stage, enqueue, copy the result block back, check status.
   void search_host(const float* host_q, size_t nq, size_t k, const uint32_t* host_mask, bool per_query,
                    size_t mask_ld, uint32_t* out_ids, float* out_dists) {
@@ -300,13 +332,16 @@ struct vsg_index {
     reserve_results(nq, k);
     const float* dq = stage_queries(host_q, nq);
     const uint32_t* dm = nullptr;
+    bool gather = false;
     if (host_mask) {
       const size_t words = per_query ? nq * mask_ld : ceil_div(n, 32);
       dm = stage_mask(host_mask, words);
+      gather = allowed_fraction(host_mask, per_query ? nq : 1, per_query ? mask_ld : ceil_div(n, 32)) <=
+               gather_max_fraction;
     }
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
-    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, di, dd, stream);
+    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream);
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
     VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));
@@ -519,7 +554,9 @@ int vsg_search_device(vsg_index* h, const float* d_queries, size_t ldq, size_t n
         dq = static_cast<const float*>(h->q.get());
         ld = h->dp;
       }
-      h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, d_out_ids, d_out_dists, s);
+      // Device masks cannot be counted here without a sync: gather unless it is switched off.
+      h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, h->gather_max_fraction > 0.0,
+                 d_out_ids, d_out_dists, s);
     }
     VSG_CUDA(cudaEventRecord(h->done, s));
   });
@@ -543,6 +580,30 @@ const float* vsg_device_rows(const vsg_index* h, size_t* padded_dim) {
   if (!h) return nullptr;
   if (padded_dim) *padded_dim = h->dp;
   return static_cast<const float*>(h->x.get());
+}
+
+int vsg_set_tunable(vsg_index* h, const char* name, double value) {
+  if (!h || !name) return fail(VSG_ERR_INVALID, "index or name is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    const std::string nm(name);
+    if (nm == "gather_max_fraction") {
+      if (!(value >= 0.0 && value <= 1.0)) throw std::invalid_argument("gather_max_fraction must be in [0, 1]");
+      h->gather_max_fraction = value;
+    } else {
+      throw std::invalid_argument("unknown tunable '" + nm + "'");
+    }
+  });
+}
+
+int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
+  if (!h || !name || !value) return fail(VSG_ERR_INVALID, "index, name or value is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    const std::string nm(name);
+    if (nm == "gather_max_fraction") *value = h->gather_max_fraction;
+    else throw std::invalid_argument("unknown tunable '" + nm + "'");
+  });
 }
 
 int vsg_profile_enable(vsg_index* h, int enable) {

@@ -13,9 +13,12 @@
 //     lane accumulates RW x QB partial dot products (or squared differences),
 //     and a warp reduce-scatter leaves one finished distance per lane;
 //   * a distance enters the warp's sorted top-k list of its query when it beats
-//     the list's last entry in (dist, id) order and the row passes the filter
-//     bit. Tiles whose filter bits are all clear for the CTA's queries are
-//     skipped before they are loaded.
+//     the list's last entry in (dist, id) order and the row passes the filter.
+// With a filter, the producer warp instead reads the filter bits of 1024 rows per
+// step, compacts the allowed rows (warp prefix sum of popcounts) and copies only
+// those, R per slot: one copy for a run of consecutive rows, else one per row.
+// The filtered scan therefore reads only allowed rows from HBM (the allowed-id
+// gather scan), whether the mask is shared or per query, on the host or device.
 // At the end the 8 warp lists of each query are merged and written as the
 // split's top-k; merge_kernel then merges the splits.
 #include <mutex>
@@ -29,15 +32,22 @@ namespace {
 
 __host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
 
+constexpr uint32_t kEndOfRows = 0xFFFFFFFFu;  // slot_rows value that ends a filtered scan
+constexpr int kChunkRows = 1024;               // rows whose filter bits the producer warp reads per step
+
 struct SmemLayout {
-  size_t q_off, ring_off, ld_off, li_off, total;
+  size_t rows_off, q_off, ids_off, chunk_off, ring_off, ld_off, li_off, total;
 };
 
+// [full/empty mbarriers | rows per slot | queries | row ids per slot | compaction buffer |
+//  ring of row tiles | per-warp top-k dists | per-warp top-k ids]
 __host__ __device__ inline SmemLayout scan_layout(int qb, int rw, uint32_t dp, uint32_t k, uint32_t stages) {
   SmemLayout L;
-  const size_t bars = 2 * kMaxStages * sizeof(uint64_t);
-  L.q_off = align128(bars);
-  L.ring_off = L.q_off + align128(size_t(qb) * dp * sizeof(float));
+  L.rows_off = 2 * kMaxStages * sizeof(uint64_t);
+  L.q_off = align128(L.rows_off + kMaxStages * sizeof(uint32_t));
+  L.ids_off = L.q_off + align128(size_t(qb) * dp * sizeof(float));
+  L.chunk_off = L.ids_off + align128(size_t(kMaxStages) * 32 * sizeof(uint32_t));
+  L.ring_off = L.chunk_off + align128(size_t(kChunkRows) * sizeof(uint32_t));
   const size_t tile = size_t(kScanWarps) * rw * dp * sizeof(float);
   L.ld_off = L.ring_off + align128(size_t(stages) * tile);
   const size_t lists = size_t(kScanWarps) * qb * k * sizeof(float);
@@ -65,20 +75,29 @@ __device__ __forceinline__ float acc4(const float4 q, const float4 x, float a) {
   }
 }
 
-// True when no query of the block may return any row of the tile [r0, r0 + R).
-template <int QB, int R>
-__device__ __forceinline__ bool tile_filtered_out(const ScanArgs& a, uint32_t qbase, uint32_t r0) {
-  const uint32_t w = r0 >> 5;
-  const uint32_t span = R >= 32 ? 0xFFFFFFFFu : (((1u << R) - 1u) << (r0 & 31));
-  uint32_t any = 0;
+// Filter bits of mask word w for the block's queries (their union), clipped to rows < row_end.
+template <int QB>
+__device__ __forceinline__ uint32_t block_bits(const ScanArgs& a, uint32_t qbase, uint32_t w, uint32_t row_end) {
+  uint32_t bits = 0;
   if (a.mask_ld == 0) {
-    any = __ldg(a.mask + w);
+    bits = __ldg(a.mask + w);
   } else {
 #pragma unroll
     for (int b = 0; b < QB; ++b)
-      if (qbase + b < a.nq) any |= __ldg(a.mask + (qbase + b) * a.mask_ld + w);
+      if (qbase + b < a.nq) bits |= __ldg(a.mask + size_t(qbase + b) * a.mask_ld + w);
   }
-  return (any & span) == 0;
+  const uint32_t lo = w * 32;
+  if (lo + 32 > row_end) bits &= (1u << (row_end - lo)) - 1u;  // 0 < row_end - lo < 32 here
+  return bits;
+}
+
+// Masked full scan: true when no query of the block may return any row of the tile
+// [r0, r0 + R). R divides 32 and tiles start at multiples of R, so one word covers a tile.
+template <int QB, int R>
+__device__ __forceinline__ bool tile_filtered_out(const ScanArgs& a, uint32_t qbase, uint32_t r0,
+                                                  uint32_t row_end) {
+  const uint32_t span = R >= 32 ? 0xFFFFFFFFu : (((1u << R) - 1u) << (r0 & 31));
+  return (block_bits<QB>(a, qbase, r0 >> 5, row_end) & span) == 0;
 }
 
 template <int QB, int RW, bool L2>
@@ -87,13 +106,17 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   constexpr int V = RW * QB;          // partial sums per lane
   constexpr int G = 32 / V;           // lanes sharing one finished distance
   static_assert(V <= 32 && (V & (V - 1)) == 0, "RW * QB must be a power of two <= 32");
+  static_assert(R <= 32, "a tile's row ids fit one warp");
 
   extern __shared__ __align__(128) unsigned char smem[];
   const uint32_t dp = a.dp, nc = dp / 4, k = a.k;
   const SmemLayout L = scan_layout(QB, RW, dp, k, a.stages);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + kMaxStages;
+  uint32_t* slot_rows = reinterpret_cast<uint32_t*>(smem + L.rows_off);
   float* qs = reinterpret_cast<float*>(smem + L.q_off);
+  uint32_t* slot_ids = reinterpret_cast<uint32_t*>(smem + L.ids_off);
+  uint32_t* chunk = reinterpret_cast<uint32_t*>(smem + L.chunk_off);
   float* ring = reinterpret_cast<float*>(smem + L.ring_off);
   float* lst_d = reinterpret_cast<float*>(smem + L.ld_off);
   uint32_t* lst_i = reinterpret_cast<uint32_t*>(smem + L.li_off);
@@ -101,10 +124,14 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t qbase = blockIdx.x * QB;
   const uint32_t split = blockIdx.y;
-  const uint32_t row_begin = split * a.rows_per_split;
+  const uint32_t row_begin = split * a.rows_per_split;  // a multiple of 32
   const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
   const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + R - 1) / R : 0;
   const uint32_t stages = a.stages;
+  // Without a filter, or for a masked full scan, the producer copies whole tiles of
+  // consecutive rows (skipping tiles with no allowed row). In gather mode it compacts the
+  // allowed rows from the filter bits and copies only those.
+  const bool gather = a.mask != nullptr && a.gather != 0;
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -129,30 +156,119 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   __syncthreads();
 
   if (warp == kScanWarps) {
-    // ---------------- producer: one lane streams the row tiles ----------------
-    if (lane == 0) {
-      const uint64_t policy = policy_evict_first();
-      uint32_t s = 0, ph = 0;
-      uint32_t pending = 0, last_ph = 0;  // per-slot bit: a copy was issued; parity of that issue
-      bool ok = true;
-      for (uint32_t t = 0; t < ntiles; ++t) {
-        const uint32_t r0 = row_begin + t * R;
-        if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0)) continue;
-        if (!mbar_wait(&empty[s], ph ^ 1)) {
-          ok = false;
-          break;
-        }
-        const uint32_t rows = min(uint32_t(R), row_end - r0);
-        const uint32_t bytes = rows * dp * uint32_t(sizeof(float));
-        mbar_arrive_expect_tx(&full[s], bytes);
-        bulk_load_stream(ring + size_t(s) * R * dp, a.x + size_t(r0) * dp, bytes, &full[s], policy);
-        pending |= 1u << s;
-        last_ph = (last_ph & ~(1u << s)) | (ph << s);
-        if (++s == stages) {
-          s = 0;
-          ph ^= 1;
+    // ---------------- producer warp ----------------
+    const uint64_t policy = policy_evict_first();
+    uint32_t s = 0, ph = 0;
+    uint32_t pending = 0, last_ph = 0;  // lane 0: per-slot bit "a copy was issued", and its parity
+    bool ok = true;
+    auto note_issue = [&](uint32_t slot) {
+      pending |= 1u << slot;
+      last_ph = (last_ph & ~(1u << slot)) | (ph << slot);
+    };
+    auto advance = [&]() {
+      if (++s == stages) {
+        s = 0;
+        ph ^= 1;
+      }
+    };
+    if (!gather) {
+      if (lane == 0) {
+        for (uint32_t t = 0; t < ntiles; ++t) {
+          const uint32_t r0 = row_begin + t * R;
+          if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0, row_end)) continue;
+          if (!mbar_wait(&empty[s], ph ^ 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t rows = min(uint32_t(R), row_end - r0);
+          const uint32_t bytes = rows * dp * uint32_t(sizeof(float));
+          mbar_arrive_expect_tx(&full[s], bytes);
+          bulk_load_stream(ring + size_t(s) * R * dp, a.x + size_t(r0) * dp, bytes, &full[s], policy);
+          note_issue(s);
+          advance();
         }
       }
+    } else {
+      // Rows whose filter bit is set, in increasing order, R per slot; the slot's row ids go
+      // to slot_ids. Consecutive rows are fetched with one copy, others one copy per row.
+      uint32_t cnt = 0;  // rows placed in the open slot (warp-uniform)
+      auto commit = [&]() {
+        __syncwarp();
+        const uint32_t first = slot_ids[s * 32], last = slot_ids[s * 32 + cnt - 1];
+        const bool dense = last - first == cnt - 1;
+        if (lane == 0) {
+          slot_rows[s] = cnt;
+          mbar_arrive_expect_tx(&full[s], cnt * dp * uint32_t(sizeof(float)));
+          note_issue(s);
+        }
+        __syncwarp();
+        float* dst = ring + size_t(s) * R * dp;
+        if (dense) {
+          if (lane == 0)
+            bulk_load_stream(dst, a.x + size_t(first) * dp, cnt * dp * uint32_t(sizeof(float)), &full[s], policy);
+        } else if (uint32_t(lane) < cnt) {
+          bulk_load_stream(dst + size_t(lane) * dp, a.x + size_t(slot_ids[s * 32 + lane]) * dp,
+                           dp * uint32_t(sizeof(float)), &full[s], policy);
+        }
+        advance();
+        cnt = 0;
+      };
+      auto open_slot = [&]() -> bool {
+        bool got = true;
+        if (lane == 0) got = mbar_wait(&empty[s], ph ^ 1);
+        return __shfl_sync(kFull, got ? 1 : 0, 0) != 0;
+      };
+      const uint32_t wend = (row_end + 31) >> 5;
+      // The next step's filter words are loaded before this step is processed, so the
+      // global-load latency overlaps the compaction and the slot filling.
+      uint32_t next = (row_begin >> 5) + lane < wend ? block_bits<QB>(a, qbase, (row_begin >> 5) + lane, row_end) : 0u;
+      for (uint32_t w0 = row_begin >> 5; w0 < wend && ok; w0 += kChunkRows / 32) {
+        const uint32_t w = w0 + lane;
+        uint32_t bits = next;
+        const uint32_t wn = w + kChunkRows / 32;
+        next = wn < wend ? block_bits<QB>(a, qbase, wn, row_end) : 0u;
+        const uint32_t pc = __popc(bits);
+        uint32_t incl = pc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        uint32_t e = incl - pc;
+        while (bits) {
+          const int i = __ffs(bits) - 1;
+          bits &= bits - 1;
+          chunk[e++] = w * 32 + uint32_t(i);
+        }
+        __syncwarp();
+        for (uint32_t pos = 0; pos < total;) {
+          if (cnt == 0 && !open_slot()) {
+            ok = false;
+            break;
+          }
+          const uint32_t take = min(uint32_t(R) - cnt, total - pos);
+          if (uint32_t(lane) < take) slot_ids[s * 32 + cnt + lane] = chunk[pos + lane];
+          cnt += take;
+          pos += take;
+          if (cnt == uint32_t(R)) commit();
+        }
+        __syncwarp();  // the compaction buffer is rewritten by the next step
+      }
+      if (ok && cnt > 0) commit();
+      if (ok) {  // end marker: a slot with no rows
+        if (!open_slot()) {
+          ok = false;
+        } else if (lane == 0) {
+          // The slot was empty: its previous copy landed and was consumed. The marker moves
+          // this barrier one more phase, so the drain below must not wait on that copy.
+          pending &= ~(1u << s);
+          slot_rows[s] = kEndOfRows;
+          mbar_arrive(&full[s]);
+        }
+      }
+    }
+    if (lane == 0) {
       // Wait (bounded) until every issued copy has landed before the CTA may exit.
       for (uint32_t i = 0; i < stages; ++i)
         if ((pending >> i) & 1u)
@@ -160,23 +276,34 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
       if (!ok) atomicExch(a.status, kDevTimeout);
     }
   } else {
-    // ---------------- consumers ----------------
+    // ---------------- consumer warps ----------------
     float* my_d = lst_d + size_t(warp) * QB * k;
     uint32_t* my_i = lst_i + size_t(warp) * QB * k;
     const float4* qs4 = reinterpret_cast<const float4*>(qs);
     const int vi = lane / G;  // value this lane finishes
     const int vr = vi / QB, vb = vi % QB;
     const bool owner = (lane % G) == 0;
+    const uint32_t lrow = uint32_t(warp * RW + vr);  // the finished value's row within a tile
+    // A masked full scan checks every pair; gather slots hold only allowed rows, but for
+    // per-query masks with QB > 1 they hold the block's union.
+    const bool check_bits = a.mask != nullptr && (!gather || (a.mask_ld != 0 && QB > 1));
     uint32_t s = 0, ph = 0;
-    bool ok = true;
-    for (uint32_t t = 0; t < ntiles && ok; ++t) {
-      const uint32_t r0 = row_begin + t * R;
-      if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0)) continue;
+    for (uint32_t t = 0; gather || t < ntiles; ++t) {
+      if (!gather && a.mask && tile_filtered_out<QB, R>(a, qbase, row_begin + t * R, row_end)) continue;
       // warp-uniform decision, so no lane leaves while the others shuffle
       if (!__all_sync(kFull, mbar_wait(&full[s], ph))) {
-        ok = false;
         if (lane == 0) atomicExch(a.status, kDevTimeout);
         break;
+      }
+      uint32_t rows, row;
+      if (gather) {
+        rows = slot_rows[s];
+        if (rows == kEndOfRows) break;
+        row = lrow < rows ? slot_ids[s * 32 + lrow] : kNone;  // read before the slot is released
+      } else {
+        const uint32_t r0 = row_begin + t * R;
+        rows = min(uint32_t(R), row_end - r0);
+        row = r0 + lrow;
       }
       const float4* xs4 = reinterpret_cast<const float4*>(ring + size_t(s) * R * dp) + size_t(warp) * RW * nc;
       float acc[V];
@@ -203,13 +330,9 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
 
       ReduceScatter<V, 16>::run(acc, lane);
       const float dist = L2 ? acc[0] : 1.0f - acc[0];
-      const uint32_t lrow = uint32_t(warp * RW + vr);
-      const uint32_t row = r0 + lrow;
-      bool pass = owner && row < row_end && qbase + vb < a.nq;  // padded query slots never compete
-      if (pass && a.mask) {
-        const uint32_t* m = a.mask + (a.mask_ld ? (qbase + vb) * a.mask_ld : 0);
-        pass = (__ldg(m + (row >> 5)) >> (row & 31)) & 1u;
-      }
+      bool pass = owner && lrow < rows && qbase + vb < a.nq;  // padded query slots never compete
+      if (pass && check_bits)
+        pass = (__ldg(a.mask + size_t(qbase + vb) * a.mask_ld + (row >> 5)) >> (row & 31)) & 1u;
       if (pass) pass = nb_less(dist, row, my_d[vb * k + k - 1], my_i[vb * k + k - 1]);
       unsigned bal = __ballot_sync(kFull, pass);
       while (bal) {

@@ -25,6 +25,7 @@ struct ScanArgs {
   uint32_t rows_per_split;  // multiple of 32
   uint32_t nsplit;
   uint32_t stages;          // ring depth (2..kMaxStages)
+  uint32_t gather;          // with a mask: 1 = copy only allowed rows, 0 = masked full scan
 };
 
 struct MergeArgs {

@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--metric", default="ip", choices=["ip", "l2"])
     ap.add_argument("--clusters", type=int, default=1024)
     ap.add_argument("--queries", type=int, default=10_000)
-    ap.add_argument("--sweep", default="1,8,32,128,512,1024,4096", help="comma list; empty to skip")
+    ap.add_argument("--sweep", default="1,8,16,32,48,64,96,128,256,512,1024,4096", help="comma list; empty to skip")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
@@ -179,7 +179,7 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None):
+def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, method="auto"):
     """Device-resident search: (ms total over `steps`, scan ms total, merge ms total, launches)."""
     k = a.k
     out_i = torch.empty((batch, k), dtype=torch.int32, device=qd.device)
@@ -189,7 +189,8 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None):
 
     def step(i):
         s = (i * batch) % (nq - batch + 1)
-        idx.search_device(qd[s].data_ptr(), a.dim, batch, k, out_i.data_ptr(), out_d.data_ptr(), stream=sp)
+        idx.search_device(qd[s].data_ptr(), a.dim, batch, k, out_i.data_ptr(), out_d.data_ptr(), stream=sp,
+                          method=method)
 
     for i in range(warmup):
         step(i)
@@ -325,10 +326,14 @@ def run_ours(a):
             st = max(3, min(300, int(3e4 / b)))
             ms_b, scan_b, _, l_b = time_device(idx, torch, qd, a, b, st, 3, stream)
             flops = 2.0 * a.n * a.dim * b
-            sweep.append({"batch": b, "qps": round(b * st / (ms_b / 1e3), 1),
-                          "ms_per_batch": round(ms_b / st, 4),
-                          "scan_gbs": round((a.n * a.dim * 4) / (scan_b / l_b / 1e3) / 1e9, 1),
-                          "scan_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)})
+            row = {"batch": b, "qps": round(b * st / (ms_b / 1e3), 1), "ms_per_batch": round(ms_b / st, 4),
+                   "kernel_gbs": round((a.n * a.dim * 4) / (scan_b / l_b / 1e3) / 1e9, 1),
+                   "kernel_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)}
+            if 8 <= b <= 256:  # both plain kernels near the auto crossover
+                for m in ("skinny", "tiled"):
+                    ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method=m)
+                    row[m + "_qps"] = round(b * max(3, st // 2) / (ms_m / 1e3), 1)
+            sweep.append(row)
         extra["sweep"] = sweep
 
     if rank == 0 and world == 1 and a.metric == "ip" and not a.no_filtered:

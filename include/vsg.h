@@ -123,7 +123,9 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   "gather_max_fraction" (default 0.10): a filtered search reads only the allowed rows (gather
  *   mode) when the largest allowed fraction of its masks is at most this, else it scans every
  *   tile holding an allowed row (masked full scan). Device-resident masks are not counted:
- *   they use gather mode unless the value is 0. */
+ *   they use gather mode unless the value is 0.
+ *   "tiled_min_batch" (default 32): method "auto" runs unfiltered batches of at least this many
+ *   queries in the register-blocked tiled kernel, smaller ones in the streaming scan kernel. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

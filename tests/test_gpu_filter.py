@@ -70,10 +70,15 @@ def test_allow_all_equals_unfiltered(gpu_ready):
     _, _, x, q, k, metric, _ = load_golden("gpu_cpu_d128_ip")
     gpu = vsg.GpuBruteForceIndex(128, metric)
     gpu.add(x)
-    a = gpu.search(q, k)
+    # filters run in the streaming scan kernel; the same kernel unfiltered is bit-identical
+    a = gpu.search(q, k, method="skinny")
     b = gpu.search(q, k, filter=np.ones(len(x), np.uint8))
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+    # the large-batch tiled kernel sums in another order: equal within the FP32 tolerance
+    t = gpu.search(q, k, method="tiled")
+    np.testing.assert_allclose(t[1], b[1], rtol=1e-5, atol=2e-6)
+    O.check_ids(t[0], b[0], x, q, metric)
 
 
 @pytest.mark.parametrize("mode", sorted(MODES))

@@ -110,17 +110,23 @@ def test_padding_known_answers(gpu_ready):
         np.testing.assert_allclose(dists, want_d, rtol=RTOL, atol=ATOL)
 
 
-def test_batch_invariance_bitwise(gpu_ready):
-    # A query's result does not depend on the batch it is searched in.
+@pytest.mark.parametrize("method", ["skinny", "tiled"])
+def test_batch_invariance_bitwise(gpu_ready, method):
+    # Within one kernel a query's result does not depend on the batch it is searched in: each
+    # kernel sums a (query, row) pair in an order fixed by the dims alone.
     vsg = gpu_ready
     _, _, x, q, k, metric, _ = load_golden("gpu_cpu_d128_ip")
     gpu = vsg.GpuBruteForceIndex(128, metric)
     gpu.add(x)
-    all_i, all_d = gpu.search(q, k)
+    all_i, all_d = gpu.search(q, k, method=method)
     for sl in (slice(0, 1), slice(7, 9), slice(100, 105), slice(37, 300)):
-        i, d = gpu.search(q[sl], k)
+        i, d = gpu.search(q[sl], k, method=method)
         np.testing.assert_array_equal(i, all_i[sl])
         np.testing.assert_array_equal(d.view(np.uint32), all_d[sl].view(np.uint32))
+    # across kernels (method "auto" picks by batch size) the sums agree within the FP32 tolerance
+    other = gpu.search(q, k, method="tiled" if method == "skinny" else "skinny")
+    np.testing.assert_allclose(other[1], all_d, rtol=RTOL, atol=ATOL)
+    O.check_ids(other[0], all_i, x, q, metric, rel=REL_TIE)
 
 
 def test_duplicate_rows_tie_to_lower_id(gpu_ready):

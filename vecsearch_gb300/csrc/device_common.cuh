@@ -191,4 +191,15 @@ __device__ __forceinline__ void list_merge_sorted(float* ld, uint32_t* li, int k
   }
 }
 
+// Copies `count` (dist, id) entries from global memory written by other CTAs of the running
+// kernel into shared memory with L1-bypassing loads (the caller has fenced after observing
+// that the writers are done). Whole CTA.
+__device__ __forceinline__ void stage_lists_cg(float* dd, uint32_t* di, const float* sd, const uint32_t* si,
+                                               size_t count, int tid, int nthreads) {
+  for (size_t j = tid; j < count; j += nthreads) {
+    dd[j] = __ldcg(sd + j);
+    di[j] = __ldcg(si + j);
+  }
+}
+
 }  // namespace vsg

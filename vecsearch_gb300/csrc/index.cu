@@ -19,6 +19,7 @@
 
 #include "../../include/vsg.h"
 #include "scan.cuh"
+#include "tiled.cuh"
 
 namespace {
 
@@ -129,6 +130,7 @@ struct vsg_index {
   DeviceBuffer part;    // per-split top-k lists: dists then ids
   DeviceBuffer res;     // [status int | pad to 16][ids nq*k][dists nq*k]
   DeviceBuffer mask;    // staged filter words
+  DeviceBuffer counters;  // per query block: CTAs done (the scan kernel's fused merge); kept zero
   PinnedBuffer pin_in, pin_out;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
@@ -138,6 +140,8 @@ struct vsg_index {
   // 0.10 from the filtered sweep on GB300 (1M x 384, batch 16): gather wins up to ~8 % allowed,
   // the masked full scan from ~17 %, where it shares each loaded tile among 8 queries.
   double gather_max_fraction = 0.10;
+  // method "auto" uses the register-blocked tiled kernel from this batch size up.
+  double tiled_min_batch = 32;
 
   ~vsg_index() {
     if (stream) {
@@ -166,9 +170,16 @@ struct vsg_index {
     VSG_CUDA(cudaMemcpyAsync(&st, status_word(), sizeof(int), cudaMemcpyDeviceToHost, stream));
     VSG_CUDA(cudaStreamSynchronize(stream));
     if (st != 0) {
-      VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
+      reset_after_failure();
       throw DeviceTimeout("a search kernel's wait ran past its time limit");
     }
+  }
+
+  // After a kernel gave up on a wait: clear the status word and the merge counters.
+  void reset_after_failure() {
+    VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
+    if (counters.get()) VSG_CUDA(cudaMemsetAsync(counters.get(), 0, counters.bytes(), stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
   }
 
   struct Plan {
@@ -183,7 +194,7 @@ struct vsg_index {
     p.shape.qb = 1;  // next power of two >= nq, at most 8; one query per CTA for per-query masks,
                      // so a CTA never loads rows only other queries may return
     while (!per_query && size_t(p.shape.qb) < nq && p.shape.qb < 8) p.shape.qb *= 2;
-    const size_t budget = smem_optin;
+    const size_t budget = smem_optin - 1024;  // headroom for the kernel's static shared memory
     p.stages = 0;
     for (int rw : {4, 2, 1}) {
       p.shape.rw = rw;
@@ -214,8 +225,66 @@ struct vsg_index {
 
   // Queues the scan + merge for device queries (stride ldq floats) on `s`. Results go to
   // out_ids / out_dists (device). Caller holds mu and has validated k, nq, n > 0.
+  // Splits of a row range for `blocks` CTA columns: at least `min_splits`, rows per split a
+  // multiple of `align`, and a total CTA count that fills whole waves of one CTA per SM.
+  void choose_splits(size_t blocks, size_t align, size_t min_rows, uint32_t* rows_per_split,
+                     uint32_t* nsplit) const {
+    const size_t s0 = std::max<size_t>(1, size_t(sms) / blocks);
+    const size_t smax = std::max<size_t>(1, std::min(ceil_div(n, min_rows), 4 * s0));
+    size_t best = std::min(s0, smax);
+    double best_eff = 0;
+    for (size_t sp = std::min(s0, smax); sp <= smax; ++sp) {
+      const size_t ctas = blocks * sp;
+      const double eff = double(ctas) / double(ceil_div(ctas, size_t(sms)) * size_t(sms));
+      if (eff > best_eff + 1e-9) {
+        best_eff = eff;
+        best = sp;
+      }
+    }
+    const size_t rps = ceil_div(ceil_div(n, best), align) * align;
+    *rows_per_split = uint32_t(rps);
+    *nsplit = uint32_t(ceil_div(n, rps));
+  }
+
+  void enqueue_tiled(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
+                     cudaStream_t s) {
+    const size_t bm = size_t(vsg::tiled_block_queries(uint32_t(k), uint32_t(nq)));
+    const size_t nqb = ceil_div(nq, bm);
+    vsg::TiledArgs a{};
+    choose_splits(nqb, 128, 1024, &a.rows_per_split, &a.nsplit);
+    const size_t parts = nq * a.nsplit * k;
+    part.reserve(parts * 8, 0, stream);
+    a.x = static_cast<const float*>(x.get());
+    a.q = dq;
+    a.ldq = uint32_t(ldq);
+    a.part_d = static_cast<float*>(part.get());
+    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
+    a.n = uint32_t(n);
+    a.dp = uint32_t(dp);
+    a.nq = uint32_t(nq);
+    a.k = uint32_t(k);
+    Timing* tm = profiling ? next_timing() : nullptr;
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
+    VSG_CUDA(vsg::launch_tiled(a, metric == VSG_METRIC_L2, dim3(unsigned(nqb), a.nsplit), s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
+    vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), a.nsplit, uint32_t(k)};
+    VSG_CUDA(vsg::launch_merge(m, s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
+  }
+
+  bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
+    if (dmask) return false;  // filters run in the scan kernel
+    if (method == VSG_METHOD_TILED) return true;
+    return method == VSG_METHOD_AUTO && double(nq) >= tiled_min_batch;
+  }
+
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
-               size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s) {
+               size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
+               uint32_t method = VSG_METHOD_AUTO) {
+    if (use_tiled(method, nq, dmask)) {
+      enqueue_tiled(dq, ldq, nq, k, out_ids, out_dists, s);
+      return;
+    }
     gather = gather && dmask != nullptr;
     const Plan p = plan(nq, k, gather, gather && per_query);
     const size_t parts = nq * p.nsplit * k;
@@ -239,10 +308,13 @@ struct vsg_index {
     a.gather = gather ? 1u : 0u;
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
+    // The last CTA of each query block merges the splits in the scan kernel itself.
+    counters.reserve(size_t(p.nqb) * sizeof(uint32_t), 0, stream);
+    a.counters = static_cast<uint32_t*>(counters.get());
+    a.out_d = out_dists;
+    a.out_i = out_ids;
     VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), p.nsplit, uint32_t(k)};
-    VSG_CUDA(vsg::launch_merge(m, s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
@@ -326,7 +398,7 @@ struct vsg_index {
 
   // Full host-to-host search: stage, enqueue, copy the result block back, check status.
   void search_host(const float* host_q, size_t nq, size_t k, const uint32_t* host_mask, bool per_query,
-                   size_t mask_ld, uint32_t* out_ids, float* out_dists) {
+                   size_t mask_ld, uint32_t* out_ids, float* out_dists, uint32_t method = VSG_METHOD_AUTO) {
     VSG_CUDA(cudaSetDevice(device));
     VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
     reserve_results(nq, k);
@@ -341,7 +413,7 @@ struct vsg_index {
     }
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
-    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream);
+    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method);
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
     VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));
@@ -351,8 +423,7 @@ struct vsg_index {
     int st = 0;
     std::memcpy(&st, h, sizeof(int));
     if (st != 0) {
-      VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
-      VSG_CUDA(cudaStreamSynchronize(stream));
+      reset_after_failure();
       throw DeviceTimeout("a search kernel's wait ran past its time limit");
     }
     std::memcpy(out_ids, h + 16, nq * k * 4);
@@ -491,7 +562,7 @@ int vsg_search_filtered(vsg_index* h, const float* queries, size_t nq, size_t k,
       fill_missing_host(out_ids, out_dists, nq * k);
       return;
     }
-    h->search_host(queries, nq, k, mask_words, mask_words && per_query, mask_ld, out_ids, out_dists);
+    h->search_host(queries, nq, k, mask_words, mask_words && per_query, mask_ld, out_ids, out_dists, method);
   });
 }
 
@@ -556,7 +627,7 @@ int vsg_search_device(vsg_index* h, const float* d_queries, size_t ldq, size_t n
       }
       // Device masks cannot be counted here without a sync: gather unless it is switched off.
       h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, h->gather_max_fraction > 0.0,
-                 d_out_ids, d_out_dists, s);
+                 d_out_ids, d_out_dists, s, method);
     }
     VSG_CUDA(cudaEventRecord(h->done, s));
   });
@@ -590,6 +661,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     if (nm == "gather_max_fraction") {
       if (!(value >= 0.0 && value <= 1.0)) throw std::invalid_argument("gather_max_fraction must be in [0, 1]");
       h->gather_max_fraction = value;
+    } else if (nm == "tiled_min_batch") {
+      if (!(value >= 1.0)) throw std::invalid_argument("tiled_min_batch must be >= 1");
+      h->tiled_min_batch = value;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -602,6 +676,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     std::lock_guard<std::mutex> g(h->mu);
     const std::string nm(name);
     if (nm == "gather_max_fraction") *value = h->gather_max_fraction;
+    else if (nm == "tiled_min_batch") *value = h->tiled_min_batch;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

@@ -366,6 +366,55 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
       }
     }
   }
+  if (a.counters == nullptr) return;
+
+  // ---- fused merge: the last CTA of this query block merges every split's list ----
+  __shared__ int last_cta;
+  __threadfence();  // this CTA's lists are visible device-wide before it is counted
+  __syncthreads();
+  if (tid == 0) last_cta = atomicAdd(a.counters + blockIdx.x, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!last_cta) return;
+  __threadfence();
+  const uint32_t nvalid = min(uint32_t(QB), a.nq - qbase);
+  // The ring is free now: stage split lists there (one query at a time, in rounds that fit;
+  // the ring holds at least 512 entries and k <= 128), and let all 8 warps merge them.
+  const size_t ring_entries = (L.ld_off - L.ring_off) / (2 * sizeof(float));
+  float* st_d = ring;
+  uint32_t* st_i = reinterpret_cast<uint32_t*>(ring + ring_entries);
+  for (uint32_t i = tid; i < kScanWarps * QB * k; i += kScanThreads) {
+    lst_d[i] = __int_as_float(0x7f800000);
+    lst_i[i] = kNone;
+  }
+  const size_t per_query = size_t(a.nsplit) * k;
+  const uint32_t lists_per_round = uint32_t(ring_entries / k > 1 ? ring_entries / k : 1);
+  for (uint32_t b = 0; b < nvalid; ++b) {
+    for (uint32_t s0 = 0; s0 < a.nsplit; s0 += lists_per_round) {
+      const uint32_t ns = min(lists_per_round, a.nsplit - s0);
+      __syncthreads();  // the previous round's staged lists are merged
+      stage_lists_cg(st_d, st_i, a.part_d + size_t(qbase + b) * per_query + size_t(s0) * k,
+                     a.part_i + size_t(qbase + b) * per_query + size_t(s0) * k, size_t(ns) * k, tid, kScanThreads);
+      __syncthreads();
+      if (warp < kScanWarps)
+        for (uint32_t sl = warp; sl < ns; sl += kScanWarps)
+          list_merge_sorted(lst_d + (size_t(warp) * QB + b) * k, lst_i + (size_t(warp) * QB + b) * k, int(k),
+                            st_d + size_t(sl) * k, st_i + size_t(sl) * k, int(k), lane);
+    }
+  }
+  __syncthreads();
+  if (warp < int(nvalid)) {
+    const int b = warp;
+    float* ld = lst_d + size_t(b) * k;
+    uint32_t* li = lst_i + size_t(b) * k;
+    for (int w = 1; w < kScanWarps; ++w)
+      list_merge_sorted(ld, li, int(k), lst_d + (size_t(w) * QB + b) * k, lst_i + (size_t(w) * QB + b) * k,
+                        int(k), lane);
+    for (uint32_t j = lane; j < k; j += 32) {
+      a.out_d[size_t(qbase + b) * k + j] = ld[j];
+      a.out_i[size_t(qbase + b) * k + j] = li[j];
+    }
+  }
+  if (tid == 0) a.counters[blockIdx.x] = 0;  // ready for the next launch
 }
 
 // One CTA per query: warps merge the splits' lists, then warp 0 merges the warps' lists.

@@ -26,6 +26,12 @@ struct ScanArgs {
   uint32_t nsplit;
   uint32_t stages;          // ring depth (2..kMaxStages)
   uint32_t gather;          // with a mask: 1 = copy only allowed rows, 0 = masked full scan
+  // Fused merge (optional): when `counters` is set, the last CTA of each query block to
+  // finish merges all splits' lists and writes the final nq x k results to out_d / out_i.
+  // counters: one zeroed uint32 per query block; the merging CTA resets its word to 0.
+  uint32_t* counters;
+  float* out_d;
+  uint32_t* out_i;
 };
 
 struct MergeArgs {

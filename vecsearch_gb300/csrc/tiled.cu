@@ -1,0 +1,257 @@
+// Large-batch exact scan: register-blocked FP32 distance tiles fused with top-k selection.
+//
+// Replaces the reference's tiled_kernel (src/gpu_brute_force.cu:142-218), which writes a
+// 128 x 128 tile of q.x per CTA into a global distance block, and the select passes that
+// read it back (:220-314, :475-482). Here each CTA owns BM queries and a range of rows:
+//   * k-slices of 32 dims of the query block and of a 128-row tile are staged in shared
+//     memory with 16-byte cp.async copies into a 3-deep ring (rows padded by 4 floats, so
+//     the 128-bit shared reads below are free of bank conflicts);
+//   * each of 256 threads accumulates a (BM/16) x 8 block of dot products (or squared
+//     differences for L2) in registers: queries ty + 16 i, rows tx + 16 j;
+//   * after the last k-slice the block is written to a shared score tile as distances, and
+//     each warp scans the scores of its queries against the query's current k-th best
+//     (dist, id), inserting the few that beat it into the query's sorted list;
+//   * at the end the lists are written as the split's top-k for merge_kernel.
+// No distance ever reaches global memory. FP32 FMA-bound: 2 * BM * 128 * d flops per tile.
+#include <mutex>
+
+#include "device_common.cuh"
+#include "tiled.cuh"
+
+namespace vsg {
+
+namespace {
+
+constexpr int kBN = 128;       // rows per tile
+constexpr int kBK = 32;        // dims per k-slice
+constexpr int kPad = 4;        // floats of padding per staged row
+constexpr int kLd = kBK + kPad;
+constexpr int kThreads = 256;
+constexpr int kTN = 8;         // rows per thread
+constexpr int kSLd = kBN + 4;  // score tile row stride
+
+__host__ __device__ constexpr size_t al128(size_t v) { return (v + 127) & ~size_t(127); }
+
+struct TiledLayout {
+  size_t score_off, ld_off, li_off, total;
+};
+
+__host__ __device__ inline TiledLayout tiled_layout(int bm, uint32_t k, int stages) {
+  TiledLayout L;
+  const size_t stage = size_t(bm + kBN) * kLd * sizeof(float);
+  L.score_off = al128(size_t(stages) * stage);
+  L.ld_off = L.score_off + al128(size_t(bm) * kSLd * sizeof(float));
+  L.li_off = L.ld_off + al128(size_t(bm) * k * sizeof(float));
+  L.total = L.li_off + al128(size_t(bm) * k * sizeof(uint32_t));
+  return L;
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int BM, bool L2>
+__global__ void __launch_bounds__(kThreads, 1) tiled_kernel(const TiledArgs a) {
+  constexpr int TM = BM / 16;
+  constexpr int kStages = 3;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t dp = a.dp, k = a.k;
+  const TiledLayout L = tiled_layout(BM, k, kStages);
+  float* stage_base = reinterpret_cast<float*>(smem);
+  float* score = reinterpret_cast<float*>(smem + L.score_off);
+  float* lst_d = reinterpret_cast<float*>(smem + L.ld_off);
+  uint32_t* lst_i = reinterpret_cast<uint32_t*>(smem + L.li_off);
+  constexpr int kStageFloats = (BM + kBN) * kLd;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ty = tid >> 4, tx = tid & 15;
+  const uint32_t qbase = blockIdx.x * BM;
+  const uint32_t split = blockIdx.y;
+  const uint32_t row_begin = split * a.rows_per_split;
+  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
+  const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kBN - 1) / kBN : 0;
+  const uint32_t nk = (dp + kBK - 1) / kBK;
+  const uint32_t nsteps = ntiles * nk;  // (tile, k-slice) pairs, streamed through one ring
+
+  for (uint32_t i = tid; i < BM * k; i += kThreads) {
+    lst_d[i] = __int_as_float(0x7f800000);
+    lst_i[i] = kNone;
+  }
+
+  // Issues the copies of step t = tile * nk + kslice into ring slot t % kStages.
+  auto load_step = [&](uint32_t t) {
+    const uint32_t tile = t / nk, k0 = (t % nk) * kBK;
+    float* st = stage_base + (t % kStages) * kStageFloats;
+    const uint32_t r0 = row_begin + tile * kBN;
+    constexpr int kChunks = (BM + kBN) * (kBK / 4);
+#pragma unroll
+    for (int c = tid; c < kChunks; c += kThreads) {
+      const int row = c / (kBK / 4), col = (c % (kBK / 4)) * 4;
+      const uint32_t kk = k0 + col;
+      if (row < BM) {
+        const uint32_t qg = qbase + row;
+        const bool ok = qg < a.nq && kk < dp;
+        const float* src = ok ? a.q + size_t(qg) * a.ldq + kk : a.q;
+        cp_async16(st + row * kLd + col, src, ok);
+      } else {
+        const uint32_t xr = r0 + (row - BM);
+        const bool ok = xr < row_end && kk < dp;
+        const float* src = ok ? a.x + size_t(xr) * dp + kk : a.x;
+        cp_async16(st + row * kLd + col, src, ok);
+      }
+    }
+  };
+
+#pragma unroll
+  for (int s = 0; s < kStages - 1; ++s) {
+    if (uint32_t(s) < nsteps) load_step(s);
+    cp_async_commit();
+  }
+
+  float acc[TM][kTN];
+  for (uint32_t t = 0; t < nsteps; ++t) {
+    const uint32_t kslice = t % nk;
+    if (kslice == 0) {
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) acc[i][j] = 0.f;
+    }
+    cp_async_wait<kStages - 2>();
+    __syncthreads();
+    // Refill the slot freed at step t - 1 (every thread has passed the barrier above).
+    if (t + kStages - 1 < nsteps) load_step(t + kStages - 1);
+    cp_async_commit();
+
+    const float* qs = stage_base + (t % kStages) * kStageFloats;
+    const float* xs = qs + BM * kLd;
+#pragma unroll
+    for (int kk = 0; kk < kBK; kk += 4) {
+      float4 xv[kTN];
+#pragma unroll
+      for (int j = 0; j < kTN; ++j) xv[j] = *reinterpret_cast<const float4*>(xs + (tx + 16 * j) * kLd + kk);
+#pragma unroll
+      for (int i = 0; i < TM; ++i) {
+        const float4 qv = *reinterpret_cast<const float4*>(qs + (ty + 16 * i) * kLd + kk);
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) {
+          float s = acc[i][j];
+          if constexpr (L2) {
+            float e = qv.x - xv[j].x;
+            s = fmaf(e, e, s);
+            e = qv.y - xv[j].y;
+            s = fmaf(e, e, s);
+            e = qv.z - xv[j].z;
+            s = fmaf(e, e, s);
+            e = qv.w - xv[j].w;
+            s = fmaf(e, e, s);
+          } else {
+            s = fmaf(qv.x, xv[j].x, s);
+            s = fmaf(qv.y, xv[j].y, s);
+            s = fmaf(qv.z, xv[j].z, s);
+            s = fmaf(qv.w, xv[j].w, s);
+          }
+          acc[i][j] = s;
+        }
+      }
+    }
+
+    if (kslice == nk - 1) {
+      // Distances of the finished tile into the score tile (+inf for rows past the range).
+      const uint32_t r0 = row_begin + (t / nk) * kBN;
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) {
+          const int n = tx + 16 * j;
+          const float d = L2 ? acc[i][j] : 1.0f - acc[i][j];
+          score[(ty + 16 * i) * kSLd + n] = r0 + n < row_end ? d : __int_as_float(0x7f800000);
+        }
+      __syncthreads();
+      // Each warp filters its queries' 128 scores against the k-th best and inserts winners.
+      for (int m = warp; m < BM; m += kThreads / 32) {
+        if (qbase + m >= a.nq) break;
+        float* ld = lst_d + size_t(m) * k;
+        uint32_t* li = lst_i + size_t(m) * k;
+        const float td = ld[k - 1];
+        const uint32_t ti = li[k - 1];
+        float cd[kBN / 32];
+        unsigned any = 0;
+#pragma unroll
+        for (int c = 0; c < kBN / 32; ++c) {
+          cd[c] = score[m * kSLd + c * 32 + lane];
+          any |= __ballot_sync(kFull, nb_less(cd[c], r0 + c * 32 + lane, td, ti));
+        }
+        if (!any) continue;
+#pragma unroll
+        for (int c = 0; c < kBN / 32; ++c) {
+          const uint32_t id = r0 + c * 32 + lane;
+          unsigned bal = __ballot_sync(kFull, nb_less(cd[c], id, ld[k - 1], li[k - 1]));
+          while (bal) {
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const float v = __shfl_sync(kFull, cd[c], src);
+            const uint32_t vid = r0 + c * 32 + src;
+            if (nb_less(v, vid, ld[k - 1], li[k - 1])) list_insert(ld, li, int(k), v, vid, lane);
+          }
+        }
+      }
+      __syncthreads();  // the score tile is rewritten by the next tile
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+
+  for (int m = warp; m < BM; m += kThreads / 32) {
+    const uint32_t qg = qbase + m;
+    if (qg >= a.nq) break;
+    const size_t o = (size_t(qg) * a.nsplit + split) * k;
+    for (uint32_t j = lane; j < k; j += 32) {
+      a.part_d[o + j] = lst_d[size_t(m) * k + j];
+      a.part_i[o + j] = lst_i[size_t(m) * k + j];
+    }
+  }
+}
+
+template <int BM, bool L2>
+cudaError_t launch_tiled_one(const TiledArgs& a, dim3 grid, cudaStream_t stream) {
+  const size_t smem = tiled_layout(BM, a.k, 3).total;
+  static std::mutex mu;
+  static size_t configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 64 || smem > configured[dev]) {
+      e = cudaFuncSetAttribute(tiled_kernel<BM, L2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      if (dev < 64) configured[dev] = smem;
+    }
+  }
+  tiled_kernel<BM, L2><<<grid, kThreads, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int tiled_block_queries(uint32_t k, uint32_t nq) { return k <= 32 && nq > 64 ? 128 : 64; }
+
+size_t tiled_smem_bytes(uint32_t k, uint32_t nq) {
+  return tiled_layout(tiled_block_queries(k, nq), k, 3).total;
+}
+
+cudaError_t launch_tiled(const TiledArgs& a, bool l2, dim3 grid, cudaStream_t stream) {
+  if (tiled_block_queries(a.k, a.nq) == 128)
+    return l2 ? launch_tiled_one<128, true>(a, grid, stream) : launch_tiled_one<128, false>(a, grid, stream);
+  return l2 ? launch_tiled_one<64, true>(a, grid, stream) : launch_tiled_one<64, false>(a, grid, stream);
+}
+
+}  // namespace vsg

@@ -191,6 +191,116 @@ __device__ __forceinline__ void list_merge_sorted(float* ld, uint32_t* li, int k
   }
 }
 
+// ---- warp top-k held in registers, merged with bitonic networks -----------------------------
+// Entry j of a K = 32 * E list lives in register j / 32 of lane j % 32. Merging a sorted list B
+// into a sorted list A: C[j] = min(A[j], B[K - 1 - j]) is bitonic and holds the K smallest of
+// A and B (Batcher); a bitonic merge network (log2 K compare-exchange stages, across registers
+// for strides >= 32 and across lanes by shuffles below) sorts it. Order is (dist, id).
+template <int E>
+struct WarpTopK {
+  float d[E];
+  uint32_t i[E];
+
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      d[e] = __int_as_float(0x7f800000);
+      i[e] = kNone;
+    }
+  }
+  // Loads len <= 32 * E sorted entries (the rest become (inf, kNone)).
+  __device__ __forceinline__ void load(const float* sd, const uint32_t* si, int len, int lane) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int j = e * 32 + lane;
+      d[e] = j < len ? sd[j] : __int_as_float(0x7f800000);
+      i[e] = j < len ? si[j] : kNone;
+    }
+  }
+  __device__ __forceinline__ void store(float* dd, uint32_t* di, int len, int lane) const {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int j = e * 32 + lane;
+      if (j < len) {
+        dd[j] = d[e];
+        di[j] = i[e];
+      }
+    }
+  }
+  // Entry j (0 <= j < 32 E), broadcast to the warp.
+  __device__ __forceinline__ void entry(int j, float& od, uint32_t& oi) const {
+    float vd = d[0];
+    uint32_t vi = i[0];
+#pragma unroll
+    for (int e = 1; e < E; ++e)
+      if (j / 32 == e) {
+        vd = d[e];
+        vi = i[e];
+      }
+    od = __shfl_sync(kFull, vd, j & 31);
+    oi = __shfl_sync(kFull, vi, j & 31);
+  }
+  template <int R>
+  __device__ __forceinline__ void cross() {
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      if (!(e & R) && nb_less(d[e | R], i[e | R], d[e], i[e])) {
+        const float td = d[e];
+        const uint32_t ti = i[e];
+        d[e] = d[e | R];
+        i[e] = i[e | R];
+        d[e | R] = td;
+        i[e | R] = ti;
+      }
+  }
+  // this = the 32 E smallest of this and b (both sorted). Whole warp.
+  __device__ __forceinline__ void merge(const WarpTopK& b, int lane) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const float rd = __shfl_sync(kFull, b.d[E - 1 - e], 31 - lane);
+      const uint32_t ri = __shfl_sync(kFull, b.i[E - 1 - e], 31 - lane);
+      if (nb_less(rd, ri, d[e], i[e])) {
+        d[e] = rd;
+        i[e] = ri;
+      }
+    }
+    // strides of r * 32 entries: between registers of the same lane
+    if constexpr (E >= 4) cross<2>();
+    if constexpr (E >= 2) cross<1>();
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1)  // strides below 32: across lanes
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const float od = __shfl_xor_sync(kFull, d[e], s);
+        const uint32_t oi = __shfl_xor_sync(kFull, i[e], s);
+        const bool lower = (lane & s) == 0;  // the lower index keeps the smaller entry
+        if (lower == nb_less(od, oi, d[e], i[e])) {
+          d[e] = od;
+          i[e] = oi;
+        }
+      }
+  }
+};
+
+// Merges `nlists` sorted lists of k entries (list j at sd + j * stride) into acc, skipping a
+// list whose best entry does not beat acc's k-th. Whole warp.
+template <int E>
+__device__ __forceinline__ void warp_merge_lists(WarpTopK<E>& acc, const float* sd, const uint32_t* si,
+                                                 int nlists, size_t stride, int k, int lane) {
+  float kd;
+  uint32_t ki;
+  acc.entry(k - 1, kd, ki);
+  for (int j = 0; j < nlists; ++j) {
+    const float* ld = sd + size_t(j) * stride;
+    const uint32_t* li = si + size_t(j) * stride;
+    if (!nb_less(ld[0], li[0], kd, ki)) continue;  // broadcast reads; nothing in this list wins
+    WarpTopK<E> b;
+    b.load(ld, li, k, lane);
+    acc.merge(b, lane);
+    acc.entry(k - 1, kd, ki);
+  }
+}
+
 // Copies `count` (dist, id) entries from global memory written by other CTAs of the running
 // kernel into shared memory with L1-bypassing loads (the caller has fenced after observing
 // that the writers are done). Whole CTA.

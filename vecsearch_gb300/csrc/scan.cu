@@ -100,6 +100,73 @@ __device__ __forceinline__ bool tile_filtered_out(const ScanArgs& a, uint32_t qb
   return (block_bits<QB>(a, qbase, r0 >> 5, row_end) & span) == 0;
 }
 
+// The scan kernel's tail. (1) Warp b merges the 8 warp lists of query b (registers, bitonic)
+// and writes the split's top-k. (2) With a.counters set, the last CTA of the query block to
+// finish stages every split's list of each query in the (now free) ring, the 8 consumer warps
+// merge a share each, warp b merges the 8 results and writes the final top-k, and the
+// block's counter is reset for the next launch.
+template <int E, int QB>
+__device__ __forceinline__ void scan_epilogue(const ScanArgs& a, const SmemLayout& L, float* ring, float* lst_d,
+                                              uint32_t* lst_i, uint32_t qbase, uint32_t split, int tid, int warp,
+                                              int lane) {
+  const uint32_t k = a.k;
+  if (warp < QB) {
+    const int b = warp;
+    WarpTopK<E> acc;
+    acc.load(lst_d + size_t(b) * k, lst_i + size_t(b) * k, int(k), lane);
+    warp_merge_lists<E>(acc, lst_d + size_t(QB + b) * k, lst_i + size_t(QB + b) * k, kScanWarps - 1,
+                        size_t(QB) * k, int(k), lane);
+    const uint32_t qg = qbase + b;
+    if (qg < a.nq) {
+      const size_t o = (size_t(qg) * a.nsplit + split) * k;
+      acc.store(a.part_d + o, a.part_i + o, int(k), lane);
+    }
+  }
+  if (a.counters == nullptr) return;
+
+  __shared__ int last_cta;
+  __threadfence();  // this CTA's lists are visible device-wide before it is counted
+  __syncthreads();
+  if (tid == 0) last_cta = atomicAdd(a.counters + blockIdx.x, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (!last_cta) return;
+  __threadfence();
+  const uint32_t nvalid = min(uint32_t(QB), a.nq - qbase);
+  // Stage split lists in the ring, one query at a time, in rounds that fit (the ring holds at
+  // least 512 entries; k <= 128).
+  const size_t ring_entries = (L.ld_off - L.ring_off) / (2 * sizeof(float));
+  float* st_d = ring;
+  uint32_t* st_i = reinterpret_cast<uint32_t*>(ring + ring_entries);
+  const size_t per_query = size_t(a.nsplit) * k;
+  const uint32_t lists_per_round = uint32_t(ring_entries / k > 1 ? ring_entries / k : 1);
+  for (uint32_t b = 0; b < nvalid; ++b) {
+    WarpTopK<E> acc;
+    acc.clear();
+    for (uint32_t s0 = 0; s0 < a.nsplit; s0 += lists_per_round) {
+      const uint32_t ns = min(lists_per_round, a.nsplit - s0);
+      __syncthreads();  // the previous round's staged lists are merged
+      stage_lists_cg(st_d, st_i, a.part_d + size_t(qbase + b) * per_query + size_t(s0) * k,
+                     a.part_i + size_t(qbase + b) * per_query + size_t(s0) * k, size_t(ns) * k, tid, kScanThreads);
+      __syncthreads();
+      if (warp < kScanWarps && uint32_t(warp) < ns)
+        warp_merge_lists<E>(acc, st_d + size_t(warp) * k, st_i + size_t(warp) * k,
+                            int((ns - warp + kScanWarps - 1) / kScanWarps), size_t(kScanWarps) * k, int(k), lane);
+    }
+    if (warp < kScanWarps) acc.store(lst_d + (size_t(warp) * QB + b) * k, lst_i + (size_t(warp) * QB + b) * k,
+                                     int(k), lane);
+  }
+  __syncthreads();
+  if (warp < int(nvalid)) {
+    const int b = warp;
+    WarpTopK<E> acc;
+    acc.load(lst_d + size_t(b) * k, lst_i + size_t(b) * k, int(k), lane);
+    warp_merge_lists<E>(acc, lst_d + size_t(QB + b) * k, lst_i + size_t(QB + b) * k, kScanWarps - 1,
+                        size_t(QB) * k, int(k), lane);
+    acc.store(a.out_d + size_t(qbase + b) * k, a.out_i + size_t(qbase + b) * k, int(k), lane);
+  }
+  if (tid == 0) a.counters[blockIdx.x] = 0;  // ready for the next launch
+}
+
 template <int QB, int RW, bool L2>
 __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a) {
   constexpr int R = kScanWarps * RW;  // rows per tile
@@ -349,96 +416,34 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   }
   __syncthreads();
 
-  // Merge the 8 warp lists of each query into warp 0's list, then write the split's top-k.
-  if (warp < QB) {
-    const int b = warp;
-    float* ld = lst_d + size_t(b) * k;  // warp 0's list for query b
-    uint32_t* li = lst_i + size_t(b) * k;
-    for (int w = 1; w < kScanWarps; ++w)
-      list_merge_sorted(ld, li, int(k), lst_d + (size_t(w) * QB + b) * k, lst_i + (size_t(w) * QB + b) * k,
-                        int(k), lane);
-    const uint32_t qg = qbase + b;
-    if (qg < a.nq) {
-      const size_t o = (size_t(qg) * a.nsplit + split) * k;
-      for (uint32_t j = lane; j < k; j += 32) {
-        a.part_d[o + j] = ld[j];
-        a.part_i[o + j] = li[j];
-      }
-    }
+  if (k <= 32) {
+    scan_epilogue<1, QB>(a, L, ring, lst_d, lst_i, qbase, split, tid, warp, lane);
+  } else if (k <= 64) {
+    scan_epilogue<2, QB>(a, L, ring, lst_d, lst_i, qbase, split, tid, warp, lane);
+  } else {
+    scan_epilogue<4, QB>(a, L, ring, lst_d, lst_i, qbase, split, tid, warp, lane);
   }
-  if (a.counters == nullptr) return;
-
-  // ---- fused merge: the last CTA of this query block merges every split's list ----
-  __shared__ int last_cta;
-  __threadfence();  // this CTA's lists are visible device-wide before it is counted
-  __syncthreads();
-  if (tid == 0) last_cta = atomicAdd(a.counters + blockIdx.x, 1u) == gridDim.y - 1;
-  __syncthreads();
-  if (!last_cta) return;
-  __threadfence();
-  const uint32_t nvalid = min(uint32_t(QB), a.nq - qbase);
-  // The ring is free now: stage split lists there (one query at a time, in rounds that fit;
-  // the ring holds at least 512 entries and k <= 128), and let all 8 warps merge them.
-  const size_t ring_entries = (L.ld_off - L.ring_off) / (2 * sizeof(float));
-  float* st_d = ring;
-  uint32_t* st_i = reinterpret_cast<uint32_t*>(ring + ring_entries);
-  for (uint32_t i = tid; i < kScanWarps * QB * k; i += kScanThreads) {
-    lst_d[i] = __int_as_float(0x7f800000);
-    lst_i[i] = kNone;
-  }
-  const size_t per_query = size_t(a.nsplit) * k;
-  const uint32_t lists_per_round = uint32_t(ring_entries / k > 1 ? ring_entries / k : 1);
-  for (uint32_t b = 0; b < nvalid; ++b) {
-    for (uint32_t s0 = 0; s0 < a.nsplit; s0 += lists_per_round) {
-      const uint32_t ns = min(lists_per_round, a.nsplit - s0);
-      __syncthreads();  // the previous round's staged lists are merged
-      stage_lists_cg(st_d, st_i, a.part_d + size_t(qbase + b) * per_query + size_t(s0) * k,
-                     a.part_i + size_t(qbase + b) * per_query + size_t(s0) * k, size_t(ns) * k, tid, kScanThreads);
-      __syncthreads();
-      if (warp < kScanWarps)
-        for (uint32_t sl = warp; sl < ns; sl += kScanWarps)
-          list_merge_sorted(lst_d + (size_t(warp) * QB + b) * k, lst_i + (size_t(warp) * QB + b) * k, int(k),
-                            st_d + size_t(sl) * k, st_i + size_t(sl) * k, int(k), lane);
-    }
-  }
-  __syncthreads();
-  if (warp < int(nvalid)) {
-    const int b = warp;
-    float* ld = lst_d + size_t(b) * k;
-    uint32_t* li = lst_i + size_t(b) * k;
-    for (int w = 1; w < kScanWarps; ++w)
-      list_merge_sorted(ld, li, int(k), lst_d + (size_t(w) * QB + b) * k, lst_i + (size_t(w) * QB + b) * k,
-                        int(k), lane);
-    for (uint32_t j = lane; j < k; j += 32) {
-      a.out_d[size_t(qbase + b) * k + j] = ld[j];
-      a.out_i[size_t(qbase + b) * k + j] = li[j];
-    }
-  }
-  if (tid == 0) a.counters[blockIdx.x] = 0;  // ready for the next launch
 }
 
-// One CTA per query: warps merge the splits' lists, then warp 0 merges the warps' lists.
+// One CTA per query: warp w merges split lists w, w + 8, ... in registers, then warp 0
+// merges the 8 warp results.
+template <int E>
 __global__ void __launch_bounds__(256) merge_kernel(const MergeArgs m) {
-  __shared__ float ld[8][kMaxK];
-  __shared__ uint32_t li[8][kMaxK];
+  __shared__ float sd[8][kMaxK];
+  __shared__ uint32_t si[8][kMaxK];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q = blockIdx.x, k = m.k;
-  for (uint32_t j = lane; j < k; j += 32) {
-    ld[warp][j] = __int_as_float(0x7f800000);
-    li[warp][j] = kNone;
-  }
-  __syncwarp();
-  for (uint32_t s = warp; s < m.nsplit; s += 8) {
-    const size_t o = (size_t(q) * m.nsplit + s) * k;
-    list_merge_sorted(ld[warp], li[warp], int(k), m.part_d + o, m.part_i + o, int(k), lane);
-  }
+  const size_t base = size_t(q) * m.nsplit * k;
+  WarpTopK<E> acc;
+  acc.clear();
+  if (uint32_t(warp) < m.nsplit)
+    warp_merge_lists<E>(acc, m.part_d + base + size_t(warp) * k, m.part_i + base + size_t(warp) * k,
+                        int((m.nsplit - warp + 7) / 8), size_t(8) * k, int(k), lane);
+  acc.store(sd[warp], si[warp], int(k), lane);
   __syncthreads();
   if (warp == 0) {
-    for (int w = 1; w < 8; ++w) list_merge_sorted(ld[0], li[0], int(k), ld[w], li[w], int(k), lane);
-    for (uint32_t j = lane; j < k; j += 32) {
-      m.out_d[size_t(q) * k + j] = ld[0][j];
-      m.out_i[size_t(q) * k + j] = li[0][j];
-    }
+    warp_merge_lists<E>(acc, sd[1], si[1], 7, kMaxK, int(k), lane);
+    acc.store(m.out_d + size_t(q) * k, m.out_i + size_t(q) * k, int(k), lane);
   }
 }
 
@@ -500,7 +505,12 @@ cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaSt
 }
 
 cudaError_t launch_merge(const MergeArgs& m, cudaStream_t stream) {
-  merge_kernel<<<m.nq, 256, 0, stream>>>(m);
+  if (m.k <= 32)
+    merge_kernel<1><<<m.nq, 256, 0, stream>>>(m);
+  else if (m.k <= 64)
+    merge_kernel<2><<<m.nq, 256, 0, stream>>>(m);
+  else
+    merge_kernel<4><<<m.nq, 256, 0, stream>>>(m);
   return cudaGetLastError();
 }
 

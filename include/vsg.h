@@ -41,11 +41,17 @@ extern "C" {
 #define VSG_METRIC_IP 1u
 
 /* Same values as vecsearch::GpuMethod (include/vecsearch/gpu_brute_force.h:16-21).
- * All methods return the same exact top-k; the method only picks the kernel. */
+ * Methods 0-3 return the same exact top-k; the method only picks the kernel (naive and skinny:
+ * the streaming scan kernel; tiled: the register-blocked kernel; auto: by batch size).
+ * VSG_METHOD_BF16 (new) is the precision form: a BF16 tensor-core pass keeps a shortlist of
+ * k' = min(128, max(k, oversample x k)) rows per query by approximate distance, then an exact
+ * FP32 rerank of the shortlist returns the top-k with the streaming kernel's arithmetic. It is
+ * exact whenever the shortlist holds the true top-k. Filtered searches ignore it. */
 #define VSG_METHOD_AUTO 0u
 #define VSG_METHOD_NAIVE 1u
 #define VSG_METHOD_SKINNY 2u
 #define VSG_METHOD_TILED 3u
+#define VSG_METHOD_BF16 4u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
 #define VSG_MAX_K 128u       /* GpuBruteForceIndex::kMaxK (gpu_brute_force.h:27) */
@@ -124,8 +130,9 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   mode) when the largest allowed fraction of its masks is at most this, else it scans every
  *   tile holding an allowed row (masked full scan). Device-resident masks are not counted:
  *   they use gather mode unless the value is 0.
- *   "tiled_min_batch" (default 32): method "auto" runs unfiltered batches of at least this many
- *   queries in the register-blocked tiled kernel, smaller ones in the streaming scan kernel. */
+ *   "tiled_min_batch" (default 48): method "auto" runs unfiltered batches of at least this many
+ *   queries in the register-blocked tiled kernel, smaller ones in the streaming scan kernel.
+ *   "shortlist_oversample" (default 4): shortlist size factor of VSG_METHOD_BF16. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

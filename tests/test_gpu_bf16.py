@@ -1,0 +1,75 @@
+"""GPU: the precision form (BF16 tcgen05 shortlist + exact FP32 rerank) against the plain path.
+
+The rerank recomputes each shortlisted row with the streaming scan kernel's arithmetic, so for
+every query whose shortlist holds the true top-k the result is bit-identical to method "skinny".
+Recall@k is checked against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, nq, d, clusters, unit, seed):
+    from vecsearch_gb300 import datasets as D
+    x, _ = D.portable_clustered(n, d, clusters, 0.35, seed=seed, centroid_seed=seed + 1, unit=unit)
+    q, _ = D.portable_clustered(nq, d, clusters, 0.35, seed=seed + 2, centroid_seed=seed + 1, unit=unit)
+    return x, q
+
+
+@pytest.mark.parametrize("metric,unit", [("ip", True), ("l2", False)])
+def test_bf16_shortlist_equals_plain(gpu_ready, metric, unit):
+    vsg = gpu_ready
+    x, q = _data(100_000, 300, 384, 256, unit, 40)
+    gpu = vsg.GpuBruteForceIndex(384, metric)
+    gpu.add(x)
+    pi, pd = gpu.search(q, 10, method="skinny")
+    bi, bd = gpu.search(q, 10, method="bf16")
+    same = (bi == pi).all(1)
+    assert same.mean() >= 0.99, same.mean()
+    np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))
+    gi, _ = O.fp64_topk(x, q, 10, metric)
+    assert vsg.recall_at_k(bi, gi, 10) >= 0.999
+    assert np.all(np.diff(bd, axis=1) >= 0)
+
+
+def test_bf16_odd_shapes(gpu_ready):
+    # dim not a multiple of 64, fewer rows than a tile, queries not a multiple of 128, k > rows
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    for n, d, nq, k in ((90, 37, 5, 10), (5000, 40, 131, 17), (300, 200, 1, 128)):
+        x = D.portable(n, d, 50 + n, normalize=True)
+        q = D.portable(nq, d, 60 + n, normalize=True)
+        gpu = vsg.GpuBruteForceIndex(d, "cosine")
+        gpu.add(x)
+        pi, pd = gpu.search(q, k, method="skinny")
+        bi, bd = gpu.search(q, k, method="bf16")
+        np.testing.assert_array_equal(bi, pi)
+        np.testing.assert_array_equal(bd, pd)
+
+
+def test_bf16_copy_follows_adds(gpu_ready):
+    vsg = gpu_ready
+    x, q = _data(20_000, 40, 128, 64, True, 70)
+    gpu = vsg.GpuBruteForceIndex(128, "cosine")
+    gpu.add(x[:5000])
+    gpu.search(q, 10, method="bf16")  # builds the bf16 copy of 5000 rows
+    gpu.add(x[5000:])                 # the copy must follow (and survive the buffer growth)
+    bi, bd = gpu.search(q, 10, method="bf16")
+    pi, pd = gpu.search(q, 10, method="skinny")
+    np.testing.assert_array_equal(bi, pi)
+    np.testing.assert_array_equal(bd, pd)
+
+
+def test_bf16_k100_recall(gpu_ready):
+    vsg = gpu_ready
+    x, q = _data(50_000, 64, 384, 128, True, 80)
+    gpu = vsg.GpuBruteForceIndex(384, "cosine")
+    gpu.add(x)
+    bi, _ = gpu.search(q, 100, method="bf16")  # k' = 128
+    gi, _ = O.fp64_topk(x, q, 100, "ip")
+    assert vsg.recall_at_k(bi, gi, 100) >= 0.99
+    gpu.set_tunable("shortlist_oversample", 1.0)
+    assert gpu.get_tunable("shortlist_oversample") == 1.0

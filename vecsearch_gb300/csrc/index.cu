@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -20,6 +21,7 @@
 #include "../../include/vsg.h"
 #include "scan.cuh"
 #include "tiled.cuh"
+#include "tc.cuh"
 
 namespace {
 
@@ -131,6 +133,13 @@ struct vsg_index {
   DeviceBuffer res;     // [status int | pad to 16][ids nq*k][dists nq*k]
   DeviceBuffer mask;    // staged filter words
   DeviceBuffer counters;  // per query block: CTAs done (the scan kernel's fused merge); kept zero
+  // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
+  // and kept current by later adds; bf16 query staging; merged shortlist candidates.
+  DeviceBuffer xb, xnorm, qb, qnorm, cand;
+  size_t bf16_rows = 0;
+  CUtensorMap xmap{};
+  const void* xmap_base = nullptr;
+  size_t xmap_rows = 0;
   PinnedBuffer pin_in, pin_out;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
@@ -141,7 +150,9 @@ struct vsg_index {
   // the masked full scan from ~17 %, where it shares each loaded tile among 8 queries.
   double gather_max_fraction = 0.10;
   // method "auto" uses the register-blocked tiled kernel from this batch size up.
-  double tiled_min_batch = 32;
+  double tiled_min_batch = 48;
+  // method "bf16": the tensor-core pass keeps k' = min(128, max(k, oversample x k)) per query.
+  double shortlist_oversample = 4;
 
   ~vsg_index() {
     if (stream) {
@@ -272,6 +283,72 @@ struct vsg_index {
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
+  // Brings the BF16 copy and the norms up to the current rows (after a grow they are rebuilt).
+  void ensure_bf16() {
+    if (bf16_rows == n && xb.bytes() >= cap * dp * 2) return;
+    const size_t keep = xb.bytes() >= cap * dp * 2 ? bf16_rows : 0;
+    xb.reserve(cap * dp * 2, keep * dp * 2, stream);
+    xnorm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
+    VSG_CUDA(vsg::launch_to_bf16(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dp),
+                                 uint32_t(dp), static_cast<char*>(xb.get()) + keep * dp * 2,
+                                 static_cast<float*>(xnorm.get()) + keep, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    bf16_rows = n;
+  }
+
+  uint32_t shortlist_size(size_t k) const {
+    const double want = std::max<double>(double(k), shortlist_oversample * double(k));
+    return uint32_t(std::min<double>(double(VSG_MAX_K), std::ceil(want)));
+  }
+
+  void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
+                    cudaStream_t s) {
+    const uint32_t kp = shortlist_size(k);
+    const uint32_t stages = vsg::tc_pick_stages(kp, smem_optin - 1024);
+    if (stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
+    // Queries to bf16 (rows past nq are zero-filled by the copy engine) and their norms.
+    qb.reserve(nq * dp * 2, 0, stream);
+    qnorm.reserve(nq * sizeof(float), 0, stream);
+    VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
+                                 static_cast<float*>(qnorm.get()), s));
+    CUtensorMap qmap;
+    VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
+    if (xmap_base != xb.get() || xmap_rows != n) {
+      VSG_CUDA(vsg::tc_encode_map(&xmap, xb.get(), n, dp));
+      xmap_base = xb.get();
+      xmap_rows = n;
+    }
+    const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
+    vsg::TcArgs a{};
+    choose_splits(nqb, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit);
+    const size_t parts = nq * a.nsplit * kp;
+    part.reserve(parts * 8, 0, stream);
+    cand.reserve(nq * kp * 8, 0, stream);
+    a.n = uint32_t(n);
+    a.dp = uint32_t(dp);
+    a.nq = uint32_t(nq);
+    a.kp = kp;
+    a.stages = stages;
+    a.l2 = metric == VSG_METRIC_L2 ? 1u : 0u;
+    a.xnorm = static_cast<const float*>(xnorm.get());
+    a.qnorm = static_cast<const float*>(qnorm.get());
+    a.part_d = static_cast<float*>(part.get());
+    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
+    a.status = status_word();
+    Timing* tm = profiling ? next_timing() : nullptr;
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
+    VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, dim3(unsigned(nqb), a.nsplit), s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
+    float* cd = static_cast<float*>(cand.get());
+    uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
+    vsg::MergeArgs m{a.part_d, a.part_i, cd, ci, uint32_t(nq), a.nsplit, kp};
+    VSG_CUDA(vsg::launch_merge(m, s));
+    vsg::RerankArgs r{static_cast<const float*>(x.get()), dq, ci, out_dists, out_ids, uint32_t(dp),
+                      uint32_t(ldq), uint32_t(nq), kp, uint32_t(k), a.l2};
+    VSG_CUDA(vsg::launch_rerank(r, s));
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
+  }
+
   bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
     if (dmask) return false;  // filters run in the scan kernel
     if (method == VSG_METHOD_TILED) return true;
@@ -281,6 +358,10 @@ struct vsg_index {
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
                uint32_t method = VSG_METHOD_AUTO) {
+    if (method == VSG_METHOD_BF16 && !dmask) {
+      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
+      return;
+    }
     if (use_tiled(method, nq, dmask)) {
       enqueue_tiled(dq, ldq, nq, k, out_ids, out_dists, s);
       return;
@@ -413,6 +494,7 @@ struct vsg_index {
     }
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
+    if (method == VSG_METHOD_BF16 && !dm) ensure_bf16();
     enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method);
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
@@ -460,7 +542,8 @@ int guarded(F&& f) {
 }
 
 void check_method(uint32_t method) {
-  if (method > VSG_METHOD_TILED) throw std::invalid_argument("method must be 'auto', 'naive', 'skinny' or 'tiled'");
+  if (method > VSG_METHOD_BF16)
+    throw std::invalid_argument("method must be 'auto', 'naive', 'skinny', 'tiled' or 'bf16'");
 }
 
 void check_k(size_t k) {
@@ -626,6 +709,7 @@ int vsg_search_device(vsg_index* h, const float* d_queries, size_t ldq, size_t n
         ld = h->dp;
       }
       // Device masks cannot be counted here without a sync: gather unless it is switched off.
+      if (method == VSG_METHOD_BF16 && !d_mask_words) h->ensure_bf16();
       h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, h->gather_max_fraction > 0.0,
                  d_out_ids, d_out_dists, s, method);
     }
@@ -664,6 +748,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "tiled_min_batch") {
       if (!(value >= 1.0)) throw std::invalid_argument("tiled_min_batch must be >= 1");
       h->tiled_min_batch = value;
+    } else if (nm == "shortlist_oversample") {
+      if (!(value >= 1.0)) throw std::invalid_argument("shortlist_oversample must be >= 1");
+      h->shortlist_oversample = value;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -677,6 +764,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     const std::string nm(name);
     if (nm == "gather_max_fraction") *value = h->gather_max_fraction;
     else if (nm == "tiled_min_batch") *value = h->tiled_min_batch;
+    else if (nm == "shortlist_oversample") *value = h->shortlist_oversample;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

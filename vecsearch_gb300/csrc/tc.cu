@@ -1,0 +1,475 @@
+// Precision form: BF16 tensor-core shortlist (tcgen05 + TMEM + TMA) and exact FP32 rerank.
+//
+// The reference has no tensor-core path; its large-batch kernel is a CUDA-core SGEMM
+// (src/gpu_brute_force.cu:142-218). Here the base keeps an FP32 master copy and a BF16 copy.
+//
+// tc_shortlist_kernel: CTA = 128 queries x one row range; 6 warps.
+//   warp 0   TMA producer: per 128-row tile, 64-dim chunks of the bf16 query block (A) and of
+//            the bf16 rows (B), 16 KB each, 128-byte swizzled, into a ring of `stages` slots.
+//   warp 1   allocates 256 TMEM columns (two 128 x 128 FP32 accumulators); one lane issues
+//            tcgen05.mma kind::f16 (M = 128 queries, N = 128 rows, K = 16) over each chunk and
+//            commits the slot back to the producer and the finished tile to the epilogue.
+//   warps 2-5 epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. one query per thread;
+//            each thread streams its query's 128 scores (tcgen05.ld 32x32b.x32) and keeps the
+//            kp best approximate distances (1 - s, or |q|^2 + |x|^2 - 2 s) in a private sorted
+//            list in shared memory, then releases the accumulator.
+//   At the end each thread writes its list: the split's shortlist for merge_kernel.
+// rerank_kernel: per query, exact FP32 distances of the merged top-kp candidates with the
+//   streaming scan kernel's arithmetic (lane l sums 16-byte chunks l, l + 32, ... in order, then
+//   a butterfly over lanes 16, 8, 4, 2, 1), so a shortlist that holds the true top-k yields the
+//   scan kernel's results bit for bit; then the top-k by (dist, id).
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "device_common.cuh"
+#include "tc.cuh"
+
+namespace vsg {
+
+namespace {
+
+constexpr int kTcThreads = 192;
+constexpr uint32_t kChunkBytes = kTcQueries * kTcKChunk * 2;  // 16 KB; A and B chunks alike
+constexpr uint32_t kStageBytes = 2 * kChunkBytes;
+constexpr uint32_t kTmemCols = 2 * kTcRows;
+constexpr int kMaxTcStages = 6;
+
+// Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16
+// (bits 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kTcRows >> 3) << 17) |
+                            (uint32_t(kTcQueries >> 4) << 24);
+
+struct TcLayout {
+  size_t lists_d, lists_i, bars, total;  // offsets from the 1024-aligned base
+};
+
+__host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t kp) {
+  TcLayout L;
+  L.lists_d = size_t(stages) * kStageBytes;
+  L.lists_i = L.lists_d + size_t(kp) * kTcQueries * 4;
+  L.bars = L.lists_i + size_t(kp) * kTcQueries * 4;
+  L.total = L.bars + 256;
+  return L;
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows 128 bytes apart, 8-row
+// groups 1024 bytes apart (the layout a 64 x R box TMA copy with 128-byte swizzle writes).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = uint64_t((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= uint64_t(1) << 16;                          // leading byte offset (unused with this swizzle)
+  d |= uint64_t(1024 >> 4) << 32;                  // stride byte offset: 8 rows x 128 bytes
+  d |= uint64_t(1) << 46;                          // descriptor version
+  d |= uint64_t(2) << 61;                          // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                            uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar)), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_shortlist_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap xmap,
+                        const TcArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  // 128-byte swizzled tiles need 1024-byte aligned addresses.
+  const uint32_t raw = smem_addr(smem_raw);
+  unsigned char* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  const uint32_t stages = a.stages, kp = a.kp;
+  const TcLayout L = tc_layout(stages, kp);
+  float* lists_d = reinterpret_cast<float*>(smem + L.lists_d);
+  uint32_t* lists_i = reinterpret_cast<uint32_t*>(smem + L.lists_i);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars);
+  uint64_t* empty = full + kMaxTcStages;
+  uint64_t* tfull = empty + kMaxTcStages;   // [2]
+  uint64_t* tempty = tfull + 2;             // [2]
+  uint64_t* done = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t qbase = blockIdx.x * kTcQueries;
+  const uint32_t split = blockIdx.y;
+  const uint32_t row_begin = split * a.rows_per_split;
+  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
+  const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
+  const uint32_t nkc = (a.dp + kTcKChunk - 1) / kTcKChunk;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+    }
+    mbar_init(done, 1);
+    mbar_fence_init();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp >= 2) {
+    const int m = (warp & 3) * 32 + lane;
+    for (uint32_t j = 0; j < kp; ++j) {
+      lists_d[j * kTcQueries + m] = __int_as_float(0x7f800000);
+      lists_i[j * kTcQueries + m] = kNone;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      const uint64_t stream_policy = policy_evict_first();
+      const uint64_t keep_policy = policy_evict_last();
+      uint32_t s = 0, ph = 0, pending = 0, last_ph = 0;
+      bool ok = true;
+      for (uint32_t t = 0; t < ntiles && ok; ++t) {
+        const int y = int(row_begin + t * kTcRows);
+        for (uint32_t kc = 0; kc < nkc; ++kc) {
+          if (!mbar_wait(&empty[s], ph ^ 1)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = smem + size_t(s) * kStageBytes;
+          mbar_arrive_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
+          tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+          pending |= 1u << s;
+          last_ph = (last_ph & ~(1u << s)) | (ph << s);
+          if (++s == stages) {
+            s = 0;
+            ph ^= 1;
+          }
+        }
+      }
+      for (uint32_t i = 0; i < stages; ++i)
+        if ((pending >> i) & 1u)
+          if (!mbar_wait(&full[i], (last_ph >> i) & 1u)) ok = false;
+      if (!ok) atomicExch(a.status, kDevTimeout);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t s = 0, ph = 0;
+      bool ok = true;
+      for (uint32_t t = 0; t < ntiles && ok; ++t) {
+        const uint32_t b = t & 1, use = t >> 1;
+        if (!mbar_wait(&tempty[b], (use & 1) ^ 1)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem_base + b * kTcRows;
+        for (uint32_t kc = 0; kc < nkc; ++kc) {
+          if (!mbar_wait(&full[s], ph)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_addr(smem + size_t(s) * kStageBytes);
+          const uint32_t sb = sa + kChunkBytes;
+#pragma unroll
+          for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
+            tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
+          tc_commit(&empty[s]);  // the slot is free once these MMAs have read it
+          if (++s == stages) {
+            s = 0;
+            ph ^= 1;
+          }
+        }
+        if (ok) tc_commit(&tfull[b]);  // the accumulator is complete once all MMAs so far are
+      }
+      // Every MMA has finished before TMEM may be released.
+      tc_commit(done);
+      if (!mbar_wait(done, 0)) ok = false;
+      if (!ok) atomicExch(a.status, kDevTimeout);
+    }
+  } else {
+    // ---------------- epilogue: one query per thread ----------------
+    const uint32_t quarter = uint32_t(warp & 3);
+    const int m = int(quarter) * 32 + lane;
+    const uint32_t qg = qbase + uint32_t(m);
+    const bool qvalid = qg < a.nq;
+    const float qn = (a.l2 && qvalid) ? a.qnorm[qg] : 0.f;
+    float* ld = lists_d + m;
+    uint32_t* li = lists_i + m;
+    float thr_d = __int_as_float(0x7f800000);
+    uint32_t thr_i = kNone;
+    uint32_t cnt = 0;
+    for (uint32_t t = 0; t < ntiles; ++t) {
+      const uint32_t b = t & 1, use = t >> 1;
+      if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1))) {
+        if (lane == 0) atomicExch(a.status, kDevTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t r0 = row_begin + t * kTcRows;
+#pragma unroll 1
+      for (uint32_t c = 0; c < kTcRows / 32; ++c) {
+        uint32_t v[32];
+        tmem_ld32(tmem_base + ((quarter * 32) << 16) + b * kTcRows + c * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const uint32_t row = r0 + c * 32 + uint32_t(j);
+          const float sc = __uint_as_float(v[j]);
+          float dist;
+          if (a.l2) {
+            dist = row < row_end ? qn + __ldg(a.xnorm + row) - 2.f * sc : 0.f;
+          } else {
+            dist = 1.f - sc;
+          }
+          if (qvalid && row < row_end && nb_less(dist, row, thr_d, thr_i)) {
+            // insert into the thread's sorted list (entry j of thread m at j * 128 + m)
+            uint32_t p = cnt < kp ? cnt : kp - 1;
+            while (p > 0 && nb_less(dist, row, ld[(p - 1) * kTcQueries], li[(p - 1) * kTcQueries])) {
+              ld[p * kTcQueries] = ld[(p - 1) * kTcQueries];
+              li[p * kTcQueries] = li[(p - 1) * kTcQueries];
+              --p;
+            }
+            ld[p * kTcQueries] = dist;
+            li[p * kTcQueries] = row;
+            if (cnt < kp) ++cnt;
+            if (cnt == kp) {
+              thr_d = ld[(kp - 1) * kTcQueries];
+              thr_i = li[(kp - 1) * kTcQueries];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);
+    }
+    if (qvalid) {
+      const size_t o = (size_t(qg) * a.nsplit + split) * kp;
+      for (uint32_t j = 0; j < kp; ++j) {
+        a.part_d[o + j] = ld[j * kTcQueries];
+        a.part_i[o + j] = li[j * kTcQueries];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// FP32 rows -> bf16 rows of stride dp (columns >= dim are zero); optional squared norms (FP32).
+__global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim,
+                               uint32_t dp, __nv_bfloat16* __restrict__ dst, float* __restrict__ norms) {
+  const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const float* s = src + row * ld_src;
+  __nv_bfloat16* d = dst + row * dp;
+  float acc = 0.f;
+  for (uint32_t c = lane; c < dp; c += 32) {
+    const float v = c < dim ? s[c] : 0.f;
+    acc = fmaf(v, v, acc);
+    d[c] = __float2bfloat16_rn(v);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if (norms && lane == 0) norms[row] = acc;
+}
+
+template <bool L2>
+__device__ __forceinline__ float exact_distance(const float4* q4, const float4* x4, uint32_t nc, int lane) {
+  float acc = 0.f;
+  for (uint32_t c = lane; c < nc; c += 32) {
+    const float4 qv = q4[c], xv = __ldg(x4 + c);
+    if constexpr (L2) {
+      float e = qv.x - xv.x;
+      acc = fmaf(e, e, acc);
+      e = qv.y - xv.y;
+      acc = fmaf(e, e, acc);
+      e = qv.z - xv.z;
+      acc = fmaf(e, e, acc);
+      e = qv.w - xv.w;
+      acc = fmaf(e, e, acc);
+    } else {
+      acc = fmaf(qv.x, xv.x, acc);
+      acc = fmaf(qv.y, xv.y, acc);
+      acc = fmaf(qv.z, xv.z, acc);
+      acc = fmaf(qv.w, xv.w, acc);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  return L2 ? acc : 1.0f - acc;
+}
+
+// One CTA per query: warps compute exact distances of the candidates, then each candidate's
+// rank in (dist, id) order places the first k.
+template <bool L2>
+__global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
+  __shared__ float cd[kMaxK];
+  __shared__ uint32_t ci[kMaxK];
+  __shared__ __align__(16) float qs[4096];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t q = blockIdx.x, kp = a.kp, nc = a.dp / 4;
+  const bool q_in_smem = a.dp <= 4096;
+  if (q_in_smem)
+    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
+  __syncthreads();
+  const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.ldq);
+  for (uint32_t j = warp; j < kp; j += blockDim.x / 32) {
+    const uint32_t id = a.cand[size_t(q) * kp + j];
+    float d = __int_as_float(0x7f800000);
+    if (id != kNone) d = exact_distance<L2>(q4, reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp), nc, lane);
+    if (lane == 0) {
+      cd[j] = d;
+      ci[j] = id;
+    }
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < kp; j += blockDim.x) {
+    const float dj = cd[j];
+    const uint32_t ij = ci[j];
+    uint32_t rank = 0;
+    for (uint32_t t = 0; t < kp; ++t)
+      rank += nb_less(cd[t], ci[t], dj, ij) || (cd[t] == dj && ci[t] == ij && t < j);
+    if (rank < a.k) {
+      a.out_d[size_t(q) * a.k + rank] = dj;
+      a.out_i[size_t(q) * a.k + rank] = ij;
+    }
+  }
+  for (uint32_t j = kp + threadIdx.x; j < a.k; j += blockDim.x) {  // k > kp: pad
+    a.out_d[size_t(q) * a.k + j] = __int_as_float(0x7f800000);
+    a.out_i[size_t(q) * a.k + j] = kNone;
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+}  // namespace
+
+size_t tc_smem_bytes(uint32_t stages, uint32_t kp) { return tc_layout(stages, kp).total + 1024; }
+
+uint32_t tc_pick_stages(uint32_t kp, size_t budget) {
+  for (uint32_t s = kMaxTcStages; s >= 2; --s)
+    if (tc_smem_bytes(s, kp) <= budget) return s;
+  return 0;
+}
+
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {dp, rows};
+  const cuuint64_t strides[1] = {dp * 2};
+  const cuuint32_t box[2] = {uint32_t(kTcKChunk), uint32_t(kTcRows)};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
+                                cudaStream_t stream) {
+  if (a.stages < 2 || a.stages > uint32_t(kMaxTcStages) || a.kp == 0 || a.kp > uint32_t(kMaxK))
+    return cudaErrorInvalidValue;
+  const size_t smem = tc_smem_bytes(a.stages, a.kp);
+  static std::mutex mu;
+  static size_t configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 64 || smem > configured[dev]) {
+      e = cudaFuncSetAttribute(tc_shortlist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      if (dev < 64) configured[dev] = smem;
+    }
+  }
+  tc_shortlist_kernel<<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
+                           float* norms, cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  const size_t threads = rows * 32;
+  to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp,
+                                                                      static_cast<__nv_bfloat16*>(dst), norms);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream) {
+  if (a.kp > uint32_t(kMaxK)) return cudaErrorInvalidValue;
+  if (a.l2)
+    rerank_kernel<true><<<a.nq, 256, 0, stream>>>(a);
+  else
+    rerank_kernel<false><<<a.nq, 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace vsg

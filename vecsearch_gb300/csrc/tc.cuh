@@ -1,0 +1,52 @@
+// Launch interface of the tensor-core shortlist path (host side).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace vsg {
+
+constexpr int kTcQueries = 128;  // queries per CTA (TMEM lanes, MMA M)
+constexpr int kTcRows = 128;     // base rows per tile (MMA N)
+constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swizzle row)
+
+struct TcArgs {
+  uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 128)
+  uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
+  uint32_t stages;
+  uint32_t l2;                     // 1: approximate L2 from norms, 0: 1 - q.x
+  const float* xnorm;              // squared row norms (L2 only)
+  const float* qnorm;              // squared query norms (L2 only)
+  float* part_d;                   // [nq][nsplit][kp] approximate distances, sorted
+  uint32_t* part_i;
+  int* status;
+};
+
+struct RerankArgs {
+  const float* x;          // FP32 master rows, n x dp
+  const float* q;          // FP32 queries, row stride ldq
+  const uint32_t* cand;    // [nq][kp] candidate ids (kNone = missing)
+  float* out_d;            // [nq][k]
+  uint32_t* out_i;
+  uint32_t dp, ldq, nq, kp, k;
+  uint32_t l2;
+};
+
+// Shared memory of the shortlist kernel for a given ring depth and shortlist size.
+size_t tc_smem_bytes(uint32_t stages, uint32_t kp);
+// Deepest ring (<= 6) that fits `budget` bytes, or 0.
+uint32_t tc_pick_stages(uint32_t kp, size_t budget);
+
+// Encodes a 2-D bf16 tensor map (rows x dp, row stride dp * 2 bytes) with a 64 x 128 box and
+// 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp);
+
+cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
+                                cudaStream_t stream);
+// FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
+cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
+                           float* norms, cudaStream_t stream);
+cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
+
+}  // namespace vsg

@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
+    ap.add_argument("--mode", default="plain", choices=["plain", "precision"],
+                    help="precision: config 4 (BF16 shortlist + rerank) sweep instead of the default line")
+    ap.add_argument("--big", action="store_true", help="precision mode: add the 4M x 384 base")
     return ap.parse_args()
 
 
@@ -333,6 +336,13 @@ def run_ours(a):
                 for m in ("skinny", "tiled"):
                     ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method=m)
                     row[m + "_qps"] = round(b * max(3, st // 2) / (ms_m / 1e3), 1)
+            # precision form: BF16 tensor-core shortlist (k' = 4k) + exact FP32 rerank
+            sb = max(3, min(200, int(2e5 / b)))
+            ms_t, tc_t, rr_t, l_t = time_device(idx, torch, qd, a, b, sb, 3, stream, method="bf16")
+            row["bf16_qps"] = round(b * sb / (ms_t / 1e3), 1)
+            row["bf16_tc_tflops"] = round(flops / (tc_t / l_t / 1e3) / 1e12, 1)
+            row["bf16_tc_gbs"] = round(a.n * a.dim * 2 / (tc_t / l_t / 1e3) / 1e9, 1)
+            row["bf16_rerank_ms"] = round(rr_t / l_t, 4)
             sweep.append(row)
         extra["sweep"] = sweep
 
@@ -374,8 +384,65 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+def run_precision(a):
+    """Config 4: BF16 shortlist (k' = 4k and 8k, capped at 128) + exact FP32 rerank vs the plain FP32
+    path, on the 1M x 384 base (1,024 clusters) and, with --big, a 4M x 384 base (4,096 clusters):
+    device QPS by batch, recall@k and max |distance error| against the FP64 oracle."""
+    import torch
+    import vecsearch_gb300 as vsg
+    from oracle import oracle as O
+    from vecsearch_gb300 import datasets as D
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    bases = [(1_000_000, 1024)] + ([(4_000_000, 4096)] if a.big else [])
+    batches = [int(b) for b in a.sweep.split(",") if b]
+    out = []
+    for n, clusters in bases:
+        x, _ = D.clustered(n, a.dim, clusters, 0.35, seed=0, centroid_seed=2)
+        q, _ = D.clustered(a.queries, a.dim, clusters, 0.35, seed=1, centroid_seed=2)
+        idx = vsg.GpuBruteForceIndex(a.dim, "cosine")
+        idx.add(x)
+        qd = torch.from_numpy(q).cuda()
+        nchk = 32
+        truth = {k: O.fp64_topk(x, q[:nchk], k, "ip") for k in (10, 100)}
+        for k in (10, 100):
+            for over in (4, 8):
+                idx.set_tunable("shortlist_oversample", over)
+                kp = min(128, over * k)
+                a2 = argparse.Namespace(**vars(a))
+                a2.k = k
+                row = {"n": n, "k": k, "k_prime": kp, "qps": {}, "plain_qps": {}}
+                for b in batches:
+                    st = max(3, min(100, int(1e5 / b)))
+                    ms, tc_ms, rr_ms, l = time_device(idx, torch, qd, a2, b, st, 3, stream, method="bf16")
+                    row["qps"][b] = round(b * st / (ms / 1e3), 1)
+                    if over == 4 and b >= 8:
+                        stp = max(3, min(50, int(2e4 / b)))
+                        msp, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method="auto")
+                        row["plain_qps"][b] = round(b * stp / (msp / 1e3), 1)
+                ids, dists = idx.search(q[:nchk], k, method="bf16")
+                gi, gd = truth[k]
+                row["recall_vs_fp64"] = vsg.recall_at_k(ids, gi, k)
+                errs = []
+                for i in range(nchk):
+                    ok = ids[i] >= 0
+                    d64 = O.fp64_distances(x, q[i:i + 1], "ip", ids[i][ok])[0]
+                    errs.append(np.max(np.abs(dists[i][ok].astype(np.float64) - d64)))
+                row["max_abs_dist_err_vs_fp64"] = float(max(errs))
+                out.append(row)
+                print(json.dumps(row), flush=True)
+        idx.set_tunable("shortlist_oversample", 4)
+        del idx
+    print(json.dumps({"metric": "precision form: BF16 shortlist + FP32 rerank QPS by batch", "unit": "queries/s",
+                      "data": "synthetic", "config": {"workload": "1M (and 4M) x 384 unit rows, cosine",
+                                                        "batches": batches}, "results": out}), flush=True)
+
+
 def main():
     a = parse()
+    if a.mode == "precision":
+        run_precision(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

@@ -253,6 +253,48 @@ struct WarpTopK {
         i[e | R] = ti;
       }
   }
+  // Compare-exchange of entries j and j ^ stride for every j, ascending where (j & size) == 0.
+  template <int SIZE, int STRIDE>
+  __device__ __forceinline__ void sort_stage(int lane) {
+    if constexpr (STRIDE >= 32) {
+      constexpr int R = STRIDE / 32;
+#pragma unroll
+      for (int e = 0; e < E; ++e)
+        if (!(e & R)) {
+          const bool up = ((e * 32 + lane) & SIZE) == 0;
+          if (up == nb_less(d[e | R], i[e | R], d[e], i[e])) {
+            const float td = d[e];
+            const uint32_t ti = i[e];
+            d[e] = d[e | R];
+            i[e] = i[e | R];
+            d[e | R] = td;
+            i[e | R] = ti;
+          }
+        }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const float od = __shfl_xor_sync(kFull, d[e], STRIDE);
+        const uint32_t oi = __shfl_xor_sync(kFull, i[e], STRIDE);
+        const bool up = ((e * 32 + lane) & SIZE) == 0;
+        const bool lower = (lane & STRIDE) == 0;
+        // ascending: the lower index keeps the smaller entry; descending: the larger
+        if ((lower == up) == nb_less(od, oi, d[e], i[e])) {
+          d[e] = od;
+          i[e] = oi;
+        }
+      }
+    }
+    if constexpr (STRIDE > 1) sort_stage<SIZE, STRIDE / 2>(lane);
+  }
+  template <int SIZE>
+  __device__ __forceinline__ void sort_from(int lane) {
+    sort_stage<SIZE, SIZE / 2>(lane);
+    if constexpr (SIZE < 32 * E) sort_from<SIZE * 2>(lane);
+  }
+  // Bitonic sort of all 32 E entries, ascending by (dist, id). Whole warp.
+  __device__ __forceinline__ void sort(int lane) { sort_from<2>(lane); }
+
   // this = the 32 E smallest of this and b (both sorted). Whole warp.
   __device__ __forceinline__ void merge(const WarpTopK& b, int lane) {
 #pragma unroll

@@ -10,9 +10,10 @@
 //            tcgen05.mma kind::f16 (M = 128 queries, N = 128 rows, K = 16) over each chunk and
 //            commits the slot back to the producer and the finished tile to the epilogue.
 //   warps 2-5 epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. one query per thread;
-//            each thread streams its query's 128 scores (tcgen05.ld 32x32b.x32) and keeps the
-//            kp best approximate distances (1 - s, or |q|^2 + |x|^2 - 2 s) in a private sorted
-//            list in shared memory, then releases the accumulator.
+//            each thread streams its query's 128 scores (tcgen05.ld 32x32b.x32), appends those
+//            that beat its threshold (approximate distance 1 - s, or |q|^2 + |x|^2 - 2 s) to the
+//            query's buffer in shared memory, and the warp compacts a buffer that may overflow
+//            with a register bitonic sort that keeps the best kp; then it releases the accumulator.
 //   At the end each thread writes its list: the split's shortlist for merge_kernel.
 // rerank_kernel: per query, exact FP32 distances of the merged top-kp candidates with the
 //   streaming scan kernel's arithmetic (lane l sums 16-byte chunks l, l + 32, ... in order, then
@@ -45,13 +46,48 @@ struct TcLayout {
   size_t lists_d, lists_i, bars, total;  // offsets from the 1024-aligned base
 };
 
+// Per-query candidate buffer capacity for a shortlist of kp: room for kp kept entries plus at
+// least one 32-score chunk; E = registers per lane of the warp sort that compacts it (C <= 32 E).
+__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) { return kp <= 32 ? 64 : kp <= 96 ? 128 : 160; }
+
 __host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t kp) {
   TcLayout L;
+  const uint32_t cap = tc_capacity(kp);
   L.lists_d = size_t(stages) * kStageBytes;
-  L.lists_i = L.lists_d + size_t(kp) * kTcQueries * 4;
-  L.bars = L.lists_i + size_t(kp) * kTcQueries * 4;
+  L.lists_i = L.lists_d + size_t(cap) * kTcQueries * 4;
+  L.bars = L.lists_i + size_t(cap) * kTcQueries * 4;
   L.total = L.bars + 256;
   return L;
+}
+
+// Sorts the first `cnt` buffered entries of lane `src`'s query (entry j at j * 128 from bd / bi)
+// and keeps the best min(cnt, kp). Returns the kept count; thr becomes entry kp - 1 when kept == kp.
+template <int E>
+__device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint32_t cnt, uint32_t kp, int lane,
+                                                  float& thr_d, uint32_t& thr_i) {
+  WarpTopK<E> w;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const uint32_t j = uint32_t(e * 32 + lane);
+    w.d[e] = j < cnt ? bd[j * kTcQueries] : __int_as_float(0x7f800000);
+    w.i[e] = j < cnt ? bi[j * kTcQueries] : kNone;
+  }
+  w.sort(lane);
+  __syncwarp();
+  const uint32_t keep = cnt < kp ? cnt : kp;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const uint32_t j = uint32_t(e * 32 + lane);
+    if (j < keep) {
+      bd[j * kTcQueries] = w.d[e];
+      bi[j * kTcQueries] = w.i[e];
+    }
+  }
+  __syncwarp();
+  thr_d = __int_as_float(0x7f800000);
+  thr_i = kNone;
+  if (keep == kp) w.entry(int(kp) - 1, thr_d, thr_i);
+  return keep;
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows 128 bytes apart, 8-row
@@ -109,6 +145,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+template <int E>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_shortlist_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap xmap,
                         const TcArgs a) {
@@ -128,12 +165,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t qbase = blockIdx.x * kTcQueries;
-  const uint32_t split = blockIdx.y;
-  const uint32_t row_begin = split * a.rows_per_split;
-  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
-  const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
+  const bool persistent = a.hdr != nullptr;
+  const uint32_t nq = persistent ? a.hdr->nq : a.nq;
+  const uint32_t nqb = persistent ? a.hdr->nqb : gridDim.x;
+  const uint32_t nsplit = persistent ? a.hdr->nsplit : a.nsplit;
+  const uint32_t rows_per_split = persistent ? a.hdr->rows_per_split : a.rows_per_split;
+  const uint32_t nitems = persistent ? a.hdr->items : gridDim.x * gridDim.y;
   const uint32_t nkc = (a.dp + kTcKChunk - 1) / kTcKChunk;
+  __shared__ uint32_t item_slot;
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -153,149 +192,178 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (warp >= 2) {
-    const int m = (warp & 3) * 32 + lane;
-    for (uint32_t j = 0; j < kp; ++j) {
-      lists_d[j * kTcQueries + m] = __int_as_float(0x7f800000);
-      lists_i[j * kTcQueries + m] = kNone;
-    }
-  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  if (warp == 0) {
-    // ---------------- TMA producer ----------------
-    if (lane == 0) {
-      const uint64_t stream_policy = policy_evict_first();
-      const uint64_t keep_policy = policy_evict_last();
-      uint32_t s = 0, ph = 0, pending = 0, last_ph = 0;
-      bool ok = true;
-      for (uint32_t t = 0; t < ntiles && ok; ++t) {
-        const int y = int(row_begin + t * kTcRows);
-        for (uint32_t kc = 0; kc < nkc; ++kc) {
-          if (!mbar_wait(&empty[s], ph ^ 1)) {
-            ok = false;
-            break;
-          }
-          unsigned char* st = smem + size_t(s) * kStageBytes;
-          mbar_arrive_expect_tx(&full[s], kStageBytes);
-          tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
-          tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
-          pending |= 1u << s;
-          last_ph = (last_ph & ~(1u << s)) | (ph << s);
-          if (++s == stages) {
-            s = 0;
-            ph ^= 1;
+  // Ring and accumulator positions carry over from one item to the next; every role walks the
+  // same items and tiles in the same order, so they stay in step.
+  uint32_t s = 0, ph = 0;      // smem ring (producer and MMA issuer)
+  uint32_t tglob = 0;          // tiles so far (MMA issuer and epilogue): TMEM buffer tglob & 1
+  uint32_t pending = 0, last_ph = 0;
+  bool ok = true;
+  const uint64_t stream_policy = policy_evict_first();
+  const uint64_t keep_policy = policy_evict_last();
+
+  for (uint32_t iter = 0;; ++iter) {
+    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : (iter == 0 ? blockIdx.y * gridDim.x + blockIdx.x : nitems);
+    __syncthreads();
+    const uint32_t item = item_slot;
+    __syncthreads();  // everyone has read the slot before thread 0 may overwrite it
+    if (item >= nitems) break;
+    const uint32_t qb = item % nqb, split = item / nqb;
+    const uint32_t qbase = qb * kTcQueries;
+    const uint32_t row_begin = split * rows_per_split;
+    const uint32_t row_end = min(a.n, row_begin + rows_per_split);
+    const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
+
+    if (warp == 0) {
+      // ---------------- TMA producer ----------------
+      if (lane == 0) {
+        for (uint32_t t = 0; t < ntiles && ok; ++t) {
+          const int y = int(row_begin + t * kTcRows);
+          for (uint32_t kc = 0; kc < nkc; ++kc) {
+            if (!mbar_wait(&empty[s], ph ^ 1)) {
+              ok = false;
+              break;
+            }
+            unsigned char* st = smem + size_t(s) * kStageBytes;
+            mbar_arrive_expect_tx(&full[s], kStageBytes);
+            tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
+            tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+            pending |= 1u << s;
+            last_ph = (last_ph & ~(1u << s)) | (ph << s);
+            if (++s == stages) {
+              s = 0;
+              ph ^= 1;
+            }
           }
         }
       }
-      for (uint32_t i = 0; i < stages; ++i)
-        if ((pending >> i) & 1u)
-          if (!mbar_wait(&full[i], (last_ph >> i) & 1u)) ok = false;
-      if (!ok) atomicExch(a.status, kDevTimeout);
-    }
-  } else if (warp == 1) {
-    // ---------------- MMA issuer ----------------
-    if (lane == 0) {
-      uint32_t s = 0, ph = 0;
-      bool ok = true;
-      for (uint32_t t = 0; t < ntiles && ok; ++t) {
-        const uint32_t b = t & 1, use = t >> 1;
-        if (!mbar_wait(&tempty[b], (use & 1) ^ 1)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t d = tmem_base + b * kTcRows;
-        for (uint32_t kc = 0; kc < nkc; ++kc) {
-          if (!mbar_wait(&full[s], ph)) {
+    } else if (warp == 1) {
+      // ---------------- MMA issuer ----------------
+      if (lane == 0) {
+        for (uint32_t t = 0; t < ntiles && ok; ++t, ++tglob) {
+          const uint32_t b = tglob & 1, use = tglob >> 1;
+          if (!mbar_wait(&tempty[b], (use & 1) ^ 1)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sa = smem_addr(smem + size_t(s) * kStageBytes);
-          const uint32_t sb = sa + kChunkBytes;
+          const uint32_t d = tmem_base + b * kTcRows;
+          for (uint32_t kc = 0; kc < nkc; ++kc) {
+            if (!mbar_wait(&full[s], ph)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = smem_addr(smem + size_t(s) * kStageBytes);
+            const uint32_t sb = sa + kChunkBytes;
 #pragma unroll
-          for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
-            tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
-          tc_commit(&empty[s]);  // the slot is free once these MMAs have read it
-          if (++s == stages) {
-            s = 0;
-            ph ^= 1;
+            for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
+              tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
+            tc_commit(&empty[s]);  // the slot is free once these MMAs have read it
+            if (++s == stages) {
+              s = 0;
+              ph ^= 1;
+            }
+          }
+          if (ok) tc_commit(&tfull[b]);  // the accumulator is complete once all MMAs so far are
+        }
+      }
+    } else {
+      // ---------------- epilogue: one query per thread ----------------
+      // Each thread appends scores that beat its query's threshold to the query's buffer
+      // (no per-thread loops, so lanes never serialise); when a buffer may overflow in the next
+      // 32 scores, the warp sorts it together and keeps the best kp (the new threshold).
+      const uint32_t cap = tc_capacity(a.kp);
+      const uint32_t quarter = uint32_t(warp & 3);
+      const int m = int(quarter) * 32 + lane;
+      const uint32_t qg = qbase + uint32_t(m);
+      const bool qvalid = qg < nq;
+      const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
+      const uint32_t* qmask = (persistent && qvalid) ? a.sq[qg].mask : nullptr;
+      const float qn = (a.l2 && qvalid) ? a.qnorm[qg] : 0.f;
+      float* wd = lists_d + quarter * 32;  // this warp's 32 buffers: lane l's entry j at wd[j * 128 + l]
+      uint32_t* wi = lists_i + quarter * 32;
+      float thr_d = __int_as_float(0x7f800000);
+      uint32_t thr_i = kNone;
+      uint32_t cnt = 0;
+      auto compact_lanes = [&](unsigned lanes) {
+        while (lanes) {
+          const int src = __ffs(lanes) - 1;
+          lanes &= lanes - 1;
+          float td;
+          uint32_t ti;
+          const uint32_t keep = compact_query<E>(wd + src, wi + src, __shfl_sync(kFull, cnt, src),
+                                                 __shfl_sync(kFull, kp, src), lane, td, ti);
+          if (lane == src) {
+            cnt = keep;
+            thr_d = td;
+            thr_i = ti;
           }
         }
-        if (ok) tc_commit(&tfull[b]);  // the accumulator is complete once all MMAs so far are
-      }
-      // Every MMA has finished before TMEM may be released.
-      tc_commit(done);
-      if (!mbar_wait(done, 0)) ok = false;
-      if (!ok) atomicExch(a.status, kDevTimeout);
-    }
-  } else {
-    // ---------------- epilogue: one query per thread ----------------
-    const uint32_t quarter = uint32_t(warp & 3);
-    const int m = int(quarter) * 32 + lane;
-    const uint32_t qg = qbase + uint32_t(m);
-    const bool qvalid = qg < a.nq;
-    const float qn = (a.l2 && qvalid) ? a.qnorm[qg] : 0.f;
-    float* ld = lists_d + m;
-    uint32_t* li = lists_i + m;
-    float thr_d = __int_as_float(0x7f800000);
-    uint32_t thr_i = kNone;
-    uint32_t cnt = 0;
-    for (uint32_t t = 0; t < ntiles; ++t) {
-      const uint32_t b = t & 1, use = t >> 1;
-      if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1))) {
-        if (lane == 0) atomicExch(a.status, kDevTimeout);
-        break;
-      }
-      tc_fence_after();
-      const uint32_t r0 = row_begin + t * kTcRows;
+      };
+      for (uint32_t t = 0; t < ntiles; ++t, ++tglob) {
+        const uint32_t b = tglob & 1, use = tglob >> 1;
+        if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1))) {
+          if (lane == 0) atomicExch(a.status, kDevTimeout);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t r0 = row_begin + t * kTcRows;
 #pragma unroll 1
-      for (uint32_t c = 0; c < kTcRows / 32; ++c) {
-        uint32_t v[32];
-        tmem_ld32(tmem_base + ((quarter * 32) << 16) + b * kTcRows + c * 32, v);
+        for (uint32_t c = 0; c < kTcRows / 32; ++c) {
+          compact_lanes(__ballot_sync(kFull, cnt + 32 > cap));
+          uint32_t v[32];
+          tmem_ld32(tmem_base + ((quarter * 32) << 16) + b * kTcRows + c * 32, v);
+          const uint32_t c0 = r0 + c * 32;
+          uint32_t allow = c0 < row_end ? (row_end - c0 >= 32 ? ~0u : (1u << (row_end - c0)) - 1u) : 0u;
+          if (qmask && allow) allow &= __ldg(qmask + (c0 >> 5));
+          if (!qvalid) allow = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t row = r0 + c * 32 + uint32_t(j);
-          const float sc = __uint_as_float(v[j]);
-          float dist;
-          if (a.l2) {
-            dist = row < row_end ? qn + __ldg(a.xnorm + row) - 2.f * sc : 0.f;
-          } else {
-            dist = 1.f - sc;
-          }
-          if (qvalid && row < row_end && nb_less(dist, row, thr_d, thr_i)) {
-            // insert into the thread's sorted list (entry j of thread m at j * 128 + m)
-            uint32_t p = cnt < kp ? cnt : kp - 1;
-            while (p > 0 && nb_less(dist, row, ld[(p - 1) * kTcQueries], li[(p - 1) * kTcQueries])) {
-              ld[p * kTcQueries] = ld[(p - 1) * kTcQueries];
-              li[p * kTcQueries] = li[(p - 1) * kTcQueries];
-              --p;
-            }
-            ld[p * kTcQueries] = dist;
-            li[p * kTcQueries] = row;
-            if (cnt < kp) ++cnt;
-            if (cnt == kp) {
-              thr_d = ld[(kp - 1) * kTcQueries];
-              thr_i = li[(kp - 1) * kTcQueries];
+          for (int j = 0; j < 32; ++j) {
+            const uint32_t row = c0 + uint32_t(j);
+            const float sc = __uint_as_float(v[j]);
+            const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
+            if (((allow >> j) & 1u) && nb_less(dist, row, thr_d, thr_i)) {
+              wd[cnt * kTcQueries + lane] = dist;
+              wi[cnt * kTcQueries + lane] = row;
+              ++cnt;
             }
           }
         }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[b]);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty[b]);
-    }
-    if (qvalid) {
-      const size_t o = (size_t(qg) * a.nsplit + split) * kp;
-      for (uint32_t j = 0; j < kp; ++j) {
-        a.part_d[o + j] = ld[j * kTcQueries];
-        a.part_i[o + j] = li[j * kTcQueries];
+      // Sort every buffer, keep the best kp, and write the split's shortlist.
+      compact_lanes(ok ? kFull : 0u);
+      if (qvalid) {
+        const size_t o = (size_t(qg) * nsplit + split) * a.kp;  // lists are a.kp apart
+        for (uint32_t j = 0; j < kp; ++j) {
+          a.part_d[o + j] = j < cnt ? wd[j * kTcQueries + lane] : __int_as_float(0x7f800000);
+          a.part_i[o + j] = j < cnt ? wi[j * kTcQueries + lane] : kNone;
+        }
       }
     }
+    if (!__syncthreads_and(ok)) break;  // a role gave up: no further items
+  }
+
+  if (warp == 0 && lane == 0) {
+    // Wait (bounded) until every issued copy has landed before the CTA may exit.
+    for (uint32_t i = 0; i < stages; ++i)
+      if ((pending >> i) & 1u)
+        if (!mbar_wait(&full[i], (last_ph >> i) & 1u)) ok = false;
+    if (!ok) atomicExch(a.status, kDevTimeout);
+  }
+  if (warp == 1 && lane == 0) {
+    // Every MMA has finished before TMEM may be released.
+    tc_commit(done);
+    if (!mbar_wait(done, 0)) ok = false;
+    if (!ok) atomicExch(a.status, kDevTimeout);
   }
   tc_fence_before();
   __syncthreads();
@@ -445,12 +513,22 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
   {
     std::lock_guard<std::mutex> g(mu);
     if (dev >= 64 || smem > configured[dev]) {
-      e = cudaFuncSetAttribute(tc_shortlist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      e = cudaFuncSetAttribute(tc_shortlist_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc_shortlist_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc_shortlist_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
       if (e != cudaSuccess) return e;
       if (dev < 64) configured[dev] = smem;
     }
   }
-  tc_shortlist_kernel<<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  const uint32_t cap = tc_capacity(a.kp);
+  if (cap <= 64)
+    tc_shortlist_kernel<2><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  else if (cap <= 128)
+    tc_shortlist_kernel<4><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  else
+    tc_shortlist_kernel<8><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
   return cudaGetLastError();
 }
 

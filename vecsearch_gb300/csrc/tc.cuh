@@ -11,6 +11,23 @@ constexpr int kTcQueries = 128;  // queries per CTA (TMEM lanes, MMA M)
 constexpr int kTcRows = 128;     // base rows per tile (MMA N)
 constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swizzle row)
 
+// Serving mode: one entry per query of a micro-batch (device memory).
+struct ServeQuery {
+  uint32_t k;              // results wanted
+  uint32_t kp;             // shortlist entries (k <= kp <= TcArgs::kp)
+  const uint32_t* mask;    // allow-bits of this query (device), or nullptr
+  uint32_t out_off;        // first result slot of this query in the output block
+  uint32_t pad;
+};
+
+// Serving mode: the micro-batch shape, written before each launch (device memory).
+struct ServeHeader {
+  uint32_t nq, nqb, nsplit, rows_per_split;
+  uint32_t items;          // nqb * nsplit
+  uint32_t next;           // work counter: CTAs claim items with atomicAdd (zeroed per launch)
+  uint32_t pad[2];
+};
+
 struct TcArgs {
   uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 128)
   uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
@@ -21,6 +38,11 @@ struct TcArgs {
   float* part_d;                   // [nq][nsplit][kp] approximate distances, sorted
   uint32_t* part_i;
   int* status;
+  // Serving mode (persistent): when hdr is set the grid has one CTA per SM, the batch shape
+  // (nq, splits) comes from hdr, CTAs claim (query block, split) items from hdr->next, and each
+  // query's shortlist size and filter come from sq.
+  ServeHeader* hdr;
+  const ServeQuery* sq;
 };
 
 struct RerankArgs {

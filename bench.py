@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
+    ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16"],
+                    help="kernel of the main timed line (auto: the plain FP32 path by batch size)")
     ap.add_argument("--mode", default="plain", choices=["plain", "precision"],
                     help="precision: config 4 (BF16 shortlist + rerank) sweep instead of the default line")
     ap.add_argument("--big", action="store_true", help="precision mode: add the 4M x 384 base")
@@ -278,7 +280,8 @@ def run_ours(a):
     stream = torch.cuda.current_stream()
 
     sampler = ClockSampler(local)
-    ms, scan_ms, merge_ms, launches = time_device(idx, torch, qd, a, a.batch, a.steps, a.warmup, stream, dist)
+    ms, scan_ms, merge_ms, launches = time_device(idx, torch, qd, a, a.batch, a.steps, a.warmup, stream, dist,
+                                                  method=a.method)
     clocks = sampler.stop()
     if dist is not None:
         t = torch.tensor([ms], device=f"cuda:{local}")

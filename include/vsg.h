@@ -44,9 +44,10 @@ extern "C" {
  * Methods 0-3 return the same exact top-k; the method only picks the kernel (naive and skinny:
  * the streaming scan kernel; tiled: the register-blocked kernel; auto: by batch size).
  * VSG_METHOD_BF16 (new) is the precision form: a BF16 tensor-core pass keeps a shortlist of
- * k' = min(128, max(k, oversample x k)) rows per query by approximate distance, then an exact
+ * k' = min(120, max(k, oversample x k)) rows per query by approximate distance, then an exact
  * FP32 rerank of the shortlist returns the top-k with the streaming kernel's arithmetic. It is
- * exact whenever the shortlist holds the true top-k. Filtered searches ignore it. */
+ * exact whenever the shortlist holds the true top-k. Filtered searches and k > 120 run the exact
+ * FP32 kernels instead. */
 #define VSG_METHOD_AUTO 0u
 #define VSG_METHOD_NAIVE 1u
 #define VSG_METHOD_SKINNY 2u

@@ -151,7 +151,7 @@ struct vsg_index {
   double gather_max_fraction = 0.10;
   // method "auto" uses the register-blocked tiled kernel from this batch size up.
   double tiled_min_batch = 48;
-  // method "bf16": the tensor-core pass keeps k' = min(128, max(k, oversample x k)) per query.
+  // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
   double shortlist_oversample = 4;
 
   ~vsg_index() {
@@ -298,7 +298,7 @@ struct vsg_index {
 
   uint32_t shortlist_size(size_t k) const {
     const double want = std::max<double>(double(k), shortlist_oversample * double(k));
-    return uint32_t(std::min<double>(double(VSG_MAX_K), std::ceil(want)));
+    return uint32_t(std::min<double>(double(vsg::kTcMaxShortlist), std::ceil(want)));
   }
 
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
@@ -358,7 +358,8 @@ struct vsg_index {
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
                uint32_t method = VSG_METHOD_AUTO) {
-    if (method == VSG_METHOD_BF16 && !dmask) {
+    // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
+    if (method == VSG_METHOD_BF16 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
       enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
       return;
     }
@@ -494,7 +495,7 @@ struct vsg_index {
     }
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
-    if (method == VSG_METHOD_BF16 && !dm) ensure_bf16();
+    if (method == VSG_METHOD_BF16 && !dm && k <= size_t(vsg::kTcMaxShortlist)) ensure_bf16();
     enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method);
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
@@ -709,7 +710,7 @@ int vsg_search_device(vsg_index* h, const float* d_queries, size_t ldq, size_t n
         ld = h->dp;
       }
       // Device masks cannot be counted here without a sync: gather unless it is switched off.
-      if (method == VSG_METHOD_BF16 && !d_mask_words) h->ensure_bf16();
+      if (method == VSG_METHOD_BF16 && !d_mask_words && k <= size_t(vsg::kTcMaxShortlist)) h->ensure_bf16();
       h->enqueue(dq, ld, nq, k, d_mask_words, d_mask_words && per_query, mask_ld, h->gather_max_fraction > 0.0,
                  d_out_ids, d_out_dists, s, method);
     }

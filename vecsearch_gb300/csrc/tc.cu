@@ -48,20 +48,22 @@ struct TcLayout {
 
 // Per-query candidate buffer capacity for a shortlist of kp: room for kp kept entries plus at
 // least one 32-score chunk; E = registers per lane of the warp sort that compacts it (C <= 32 E).
-__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) { return kp <= 32 ? 64 : kp <= 96 ? 128 : 160; }
+__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) {
+  return kp <= 32 ? 64 : kp <= 64 ? 96 : kp <= 96 ? 128 : 152;
+}
 
 __host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t kp) {
   TcLayout L;
   const uint32_t cap = tc_capacity(kp);
   L.lists_d = size_t(stages) * kStageBytes;
-  L.lists_i = L.lists_d + size_t(cap) * kTcQueries * 4;
-  L.bars = L.lists_i + size_t(cap) * kTcQueries * 4;
+  L.lists_i = L.lists_d + size_t(cap + 1) * kTcQueries * 4;
+  L.bars = L.lists_i + size_t(cap + 1) * kTcQueries * 4;
   L.total = L.bars + 256;
   return L;
 }
 
-// Sorts the first `cnt` buffered entries of lane `src`'s query (entry j at j * 128 from bd / bi)
-// and keeps the best min(cnt, kp). Returns the kept count; thr becomes entry kp - 1 when kept == kp.
+// Sorts the first `cnt` buffered entries of one query (entry j at bd[j] / bi[j]) and keeps the
+// best min(cnt, kp). Returns the kept count; thr becomes entry kp - 1 when kept == kp.
 template <int E>
 __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint32_t cnt, uint32_t kp, int lane,
                                                   float& thr_d, uint32_t& thr_i) {
@@ -69,8 +71,8 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const uint32_t j = uint32_t(e * 32 + lane);
-    w.d[e] = j < cnt ? bd[j * kTcQueries] : __int_as_float(0x7f800000);
-    w.i[e] = j < cnt ? bi[j * kTcQueries] : kNone;
+    w.d[e] = j < cnt ? bd[j] : __int_as_float(0x7f800000);
+    w.i[e] = j < cnt ? bi[j] : kNone;
   }
   w.sort(lane);
   __syncwarp();
@@ -79,8 +81,8 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
   for (int e = 0; e < E; ++e) {
     const uint32_t j = uint32_t(e * 32 + lane);
     if (j < keep) {
-      bd[j * kTcQueries] = w.d[e];
-      bi[j * kTcQueries] = w.i[e];
+      bd[j] = w.d[e];
+      bi[j] = w.i[e];
     }
   }
   __syncwarp();
@@ -285,8 +287,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
       const uint32_t* qmask = (persistent && qvalid) ? a.sq[qg].mask : nullptr;
       const float qn = (a.l2 && qvalid) ? a.qnorm[qg] : 0.f;
-      float* wd = lists_d + quarter * 32;  // this warp's 32 buffers: lane l's entry j at wd[j * 128 + l]
-      uint32_t* wi = lists_i + quarter * 32;
+      // Query m's buffer: entries m * (cap + 1) + j. The odd stride keeps the lanes' appends on
+      // different banks; a compaction reads one query's entries consecutively.
+      const uint32_t qstride = cap + 1;
+      float* wd = lists_d + size_t(quarter * 32) * qstride;  // this warp's 32 buffers
+      uint32_t* wi = lists_i + size_t(quarter * 32) * qstride;
       float thr_d = __int_as_float(0x7f800000);
       uint32_t thr_i = kNone;
       uint32_t cnt = 0;
@@ -296,8 +301,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           lanes &= lanes - 1;
           float td;
           uint32_t ti;
-          const uint32_t keep = compact_query<E>(wd + src, wi + src, __shfl_sync(kFull, cnt, src),
-                                                 __shfl_sync(kFull, kp, src), lane, td, ti);
+          const uint32_t keep = compact_query<E>(wd + size_t(src) * qstride, wi + size_t(src) * qstride,
+                                                 __shfl_sync(kFull, cnt, src), __shfl_sync(kFull, kp, src), lane,
+                                                 td, ti);
           if (lane == src) {
             cnt = keep;
             thr_d = td;
@@ -329,8 +335,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const float sc = __uint_as_float(v[j]);
             const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
             if (((allow >> j) & 1u) && nb_less(dist, row, thr_d, thr_i)) {
-              wd[cnt * kTcQueries + lane] = dist;
-              wi[cnt * kTcQueries + lane] = row;
+              wd[lane * qstride + cnt] = dist;
+              wi[lane * qstride + cnt] = row;
               ++cnt;
             }
           }
@@ -344,8 +350,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if (qvalid) {
         const size_t o = (size_t(qg) * nsplit + split) * a.kp;  // lists are a.kp apart
         for (uint32_t j = 0; j < kp; ++j) {
-          a.part_d[o + j] = j < cnt ? wd[j * kTcQueries + lane] : __int_as_float(0x7f800000);
-          a.part_i[o + j] = j < cnt ? wi[j * kTcQueries + lane] : kNone;
+          a.part_d[o + j] = j < cnt ? wd[lane * qstride + j] : __int_as_float(0x7f800000);
+          a.part_i[o + j] = j < cnt ? wi[lane * qstride + j] : kNone;
         }
       }
     }
@@ -502,7 +508,7 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
 
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
                                 cudaStream_t stream) {
-  if (a.stages < 2 || a.stages > uint32_t(kMaxTcStages) || a.kp == 0 || a.kp > uint32_t(kMaxK))
+  if (a.stages < 2 || a.stages > uint32_t(kMaxTcStages) || a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist))
     return cudaErrorInvalidValue;
   const size_t smem = tc_smem_bytes(a.stages, a.kp);
   static std::mutex mu;

@@ -10,6 +10,7 @@ namespace vsg {
 constexpr int kTcQueries = 128;  // queries per CTA (TMEM lanes, MMA M)
 constexpr int kTcRows = 128;     // base rows per tile (MMA N)
 constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swizzle row)
+constexpr int kTcMaxShortlist = 120;  // largest per-query shortlist (its buffer fits shared memory)
 
 // Serving mode: one entry per query of a micro-batch (device memory).
 struct ServeQuery {
@@ -29,7 +30,7 @@ struct ServeHeader {
 };
 
 struct TcArgs {
-  uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 128)
+  uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 120)
   uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
   uint32_t stages;
   uint32_t l2;                     // 1: approximate L2 from norms, 0: 1 - q.x

@@ -135,7 +135,7 @@ struct vsg_index {
   DeviceBuffer counters;  // per query block: CTAs done (the scan kernel's fused merge); kept zero
   // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
   // and kept current by later adds; bf16 query staging; merged shortlist candidates.
-  DeviceBuffer xb, xnorm, qb, qnorm, cand;
+  DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
@@ -337,6 +337,23 @@ struct vsg_index {
     a.status = status_word();
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
+    // Batches of 32+ queries first score a sample of at least 16K rows (whole tiles at the head of
+    // every split) and start each query at the k'-th best sampled distance, so the main pass keeps
+    // only rows that can still make the shortlist instead of compacting its buffers again and again.
+    const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
+    if (nq >= 32 && tiles_per_split > 1) {
+      const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(16384, size_t(a.nsplit) * vsg::kTcRows)));
+      const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
+      sample.reserve(nq * per_query * sizeof(float), 0, stream);
+      thr.reserve(nq * sizeof(float), 0, stream);
+      vsg::TcArgs sa = a;
+      sa.dump = static_cast<float*>(sample.get());
+      sa.sample_tiles = st;
+      VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, sa, dim3(unsigned(nqb), a.nsplit), s));
+      VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr, kp,
+                                         static_cast<float*>(thr.get()), s));
+      a.thr_init = static_cast<const float*>(thr.get());
+    }
     VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, dim3(unsigned(nqb), a.nsplit), s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     float* cd = static_cast<float*>(cand.get());

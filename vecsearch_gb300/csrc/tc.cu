@@ -217,7 +217,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t qb = item % nqb, split = item / nqb;
     const uint32_t qbase = qb * kTcQueries;
     const uint32_t row_begin = split * rows_per_split;
-    const uint32_t row_end = min(a.n, row_begin + rows_per_split);
+    uint32_t row_end = min(a.n, row_begin + rows_per_split);
+    if (a.dump) row_end = min(row_end, row_begin + a.sample_tiles * kTcRows);  // sample pass
     const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
 
     if (warp == 0) {
@@ -292,9 +293,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t qstride = cap + 1;
       float* wd = lists_d + size_t(quarter * 32) * qstride;  // this warp's 32 buffers
       uint32_t* wi = lists_i + size_t(quarter * 32) * qstride;
-      float thr_d = __int_as_float(0x7f800000);
+      // A sampled threshold bounds the k'-th best from above: rows at or below it are kept.
+      float thr_d = (a.thr_init && qvalid) ? a.thr_init[qg] : __int_as_float(0x7f800000);
       uint32_t thr_i = kNone;
       uint32_t cnt = 0;
+      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * a.sample_tiles * kTcRows
+                                           : nullptr;
       auto compact_lanes = [&](unsigned lanes) {
         while (lanes) {
           const int src = __ffs(lanes) - 1;
@@ -322,13 +326,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const uint32_t r0 = row_begin + t * kTcRows;
 #pragma unroll 1
         for (uint32_t c = 0; c < kTcRows / 32; ++c) {
-          compact_lanes(__ballot_sync(kFull, cnt + 32 > cap));
+          if (!a.dump) compact_lanes(__ballot_sync(kFull, cnt + 32 > cap));
           uint32_t v[32];
           tmem_ld32(tmem_base + ((quarter * 32) << 16) + b * kTcRows + c * 32, v);
           const uint32_t c0 = r0 + c * 32;
           uint32_t allow = c0 < row_end ? (row_end - c0 >= 32 ? ~0u : (1u << (row_end - c0)) - 1u) : 0u;
           if (qmask && allow) allow &= __ldg(qmask + (c0 >> 5));
           if (!qvalid) allow = 0;
+          if (dump_row) {  // sample pass: raw distances out, nothing kept
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const uint32_t row = c0 + uint32_t(j);
+              const float sc = __uint_as_float(v[j]);
+              const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
+              dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
+            }
+            continue;
+          }
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const uint32_t row = c0 + uint32_t(j);
@@ -345,6 +359,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[b]);
       }
+      if (a.dump) {  // sample pass: tiles past the split's end read as +inf
+        if (dump_row)
+          for (uint32_t j = ntiles * kTcRows; j < a.sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
+      } else {
       // Sort every buffer, keep the best kp, and write the split's shortlist.
       compact_lanes(ok ? kFull : 0u);
       if (qvalid) {
@@ -353,6 +371,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           a.part_d[o + j] = j < cnt ? wd[lane * qstride + j] : __int_as_float(0x7f800000);
           a.part_i[o + j] = j < cnt ? wi[lane * qstride + j] : kNone;
         }
+      }
       }
     }
     if (!__syncthreads_and(ok)) break;  // a role gave up: no further items
@@ -465,6 +484,54 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   }
 }
 
+// Float -> unsigned key with the same order (negative values flipped).
+__device__ __forceinline__ uint32_t order_key(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// One CTA per query: the kp-th smallest of `count` values by radix selection on the order key,
+// 8 bits per round (4 rounds). Ties resolve to the shared value, so the threshold is exact.
+__global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uint32_t count, uint32_t nq,
+                                                             const uint32_t* kp_per_query, uint32_t kp_all,
+                                                             float* thr) {
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t sel_prefix, sel_rank;
+  const uint32_t q = blockIdx.x;
+  if (q >= nq) return;
+  const float* v = in + size_t(q) * count;
+  const uint32_t kp = kp_per_query ? kp_per_query[q] : kp_all;
+  if (threadIdx.x == 0) {
+    sel_prefix = 0;
+    sel_rank = kp;  // 1-based rank still to find inside the current prefix
+  }
+  for (int round = 0; round < 4; ++round) {
+    const int shift = 24 - 8 * round;
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const uint32_t prefix = sel_prefix;
+    const uint32_t hi_mask = round == 0 ? 0u : (0xFFFFFFFFu << (32 - 8 * round));
+    for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
+      const uint32_t key = order_key(v[j]);
+      if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t r = sel_rank, b = 0;
+      while (b < 255 && hist[b] < r) r -= hist[b++];
+      sel_prefix = prefix | (b << shift);
+      sel_rank = r;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const uint32_t key = sel_prefix;
+    const uint32_t u = (key & 0x80000000u) ? (key & 0x7FFFFFFFu) : ~key;
+    // Fewer than kp finite values: no bound (+inf keeps everything).
+    thr[q] = kp > count ? __int_as_float(0x7f800000) : __uint_as_float(u);
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -544,6 +611,13 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
   const size_t threads = rows * 32;
   to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp,
                                                                       static_cast<__nv_bfloat16*>(dst), norms);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
+                                 uint32_t kp, float* thr, cudaStream_t stream) {
+  if (nq == 0) return cudaSuccess;
+  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr);
   return cudaGetLastError();
 }
 

@@ -44,7 +44,18 @@ struct TcArgs {
   // query's shortlist size and filter come from sq.
   ServeHeader* hdr;
   const ServeQuery* sq;
+  // Sample pass: when dump is set, each CTA scores only the first sample_tiles tiles of its split
+  // and writes the raw approximate distances (+inf where the filter or the range excludes a row)
+  // to dump[q][split * sample_tiles * 128 + j]; no shortlist is kept.
+  float* dump;
+  uint32_t sample_tiles;
+  // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
+  const float* thr_init;
 };
+
+// Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q].
+cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
+                                 uint32_t kp, float* thr, cudaStream_t stream);
 
 struct RerankArgs {
   const float* x;          // FP32 master rows, n x dp

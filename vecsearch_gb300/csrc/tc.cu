@@ -297,6 +297,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       float thr_d = (a.thr_init && qvalid) ? a.thr_init[qg] : __int_as_float(0x7f800000);
       uint32_t thr_i = kNone;
       uint32_t cnt = 0;
+      // Inner product: a cheap prefilter on the raw score. 1 - s <= thr needs s >= 1 - thr up to
+      // rounding; the bound is lowered by 8 ulps of max(1, |thr|) so no candidate is lost.
+      auto score_bound = [](float td) { return (1.f - td) - 8.f * 1.1920929e-7f * fmaxf(1.f, fabsf(td)); };
+      float s_lo = score_bound(thr_d);
       float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * a.sample_tiles * kTcRows
                                            : nullptr;
       auto compact_lanes = [&](unsigned lanes) {
@@ -312,6 +316,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             cnt = keep;
             thr_d = td;
             thr_i = ti;
+            s_lo = score_bound(td);
           }
         }
       };
@@ -343,15 +348,29 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             continue;
           }
+          // Lane l holds row c0 + l's squared norm; every lane gets row j's by a shuffle.
+          const float xn_l = a.l2 ? __ldg(a.xnorm + min(c0 + uint32_t(lane), a.n - 1)) : 0.f;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const uint32_t row = c0 + uint32_t(j);
             const float sc = __uint_as_float(v[j]);
-            const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
-            if (((allow >> j) & 1u) && nb_less(dist, row, thr_d, thr_i)) {
-              wd[lane * qstride + cnt] = dist;
-              wi[lane * qstride + cnt] = row;
-              ++cnt;
+            float dist;
+            bool p;
+            if (a.l2) {
+              dist = qn + __shfl_sync(kFull, xn_l, j) - 2.f * sc;
+              p = dist <= thr_d;
+            } else {
+              dist = 0.f;
+              p = sc >= s_lo;
+            }
+            p = p && ((allow >> j) & 1u);
+            if (__any_sync(kFull, p)) {  // rare once the threshold is tight
+              if (!a.l2) dist = 1.f - sc;
+              if (p && nb_less(dist, row, thr_d, thr_i)) {
+                wd[lane * qstride + cnt] = dist;
+                wi[lane * qstride + cnt] = row;
+                ++cnt;
+              }
             }
           }
         }

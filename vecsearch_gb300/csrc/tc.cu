@@ -135,7 +135,10 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
+// tcgen05.ld and tcgen05.wait::ld are .sync.aligned: every lane of the warp must execute them
+// together, so the warp is reconverged first (the score filter before it branches per lane).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  __syncwarp();
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
@@ -189,6 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     mbar_fence_init();
   }
   if (warp == 1) {
+    __syncwarp();  // .sync.aligned: the whole warp, converged
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
                  "r"(kTmemCols)
                  : "memory");
@@ -413,6 +417,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
+    __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
                  : "memory");
   }

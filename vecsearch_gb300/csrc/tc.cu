@@ -342,13 +342,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           uint32_t allow = c0 < row_end ? (row_end - c0 >= 32 ? ~0u : (1u << (row_end - c0)) - 1u) : 0u;
           if (qmask && allow) allow &= __ldg(qmask + (c0 >> 5));
           if (!qvalid) allow = 0;
-          if (dump_row) {  // sample pass: raw distances out, nothing kept
+          if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-uniform
+                         // (a.dump): lanes of padded query slots take it too and store nothing.
+            if (dump_row) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const uint32_t row = c0 + uint32_t(j);
-              const float sc = __uint_as_float(v[j]);
-              const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
-              dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
+              for (int j = 0; j < 32; ++j) {
+                const uint32_t row = c0 + uint32_t(j);
+                const float sc = __uint_as_float(v[j]);
+                const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
+                dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
+              }
             }
             continue;
           }

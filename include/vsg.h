@@ -144,6 +144,30 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 int vsg_profile_enable(vsg_index* index, int enable);
 int vsg_profile_read(vsg_index* index, double* scan_ms, double* merge_ms, size_t* searches);
 
+/* Serving loop (new; the reference answers one call at a time, python/bindings.cpp:165-186, and its
+ * shard worker calls the index per request, distributed/shard_worker.py:26-36). A worker thread
+ * batches requests continuously onto the BF16 shortlist + exact FP32 rerank path: requests that
+ * arrive while others run join the next free slot; each slot replays one CUDA graph (persistent
+ * shortlist kernel, fused merge + rerank). Results equal vsg_search with VSG_METHOD_BF16 and do not
+ * depend on the other requests in a batch.
+ *   vsg_server_create: max_batch queries per slot (a request may not exceed it), k <= max_k <= 120,
+ *     up to `slots` slots, fewer if half of the free HBM cannot hold them (VSG_ERR_NOMEM if none
+ *     fits). The index must not be added to while a server uses it.
+ *   vsg_server_submit: host queries (nq x dim), optional host allow-bits (ceil(size / 32) words,
+ *     shared by the request's queries; NULL = no filter) and host outputs (nq x k) that must stay
+ *     valid until vsg_server_wait returns; returns a ticket.
+ *   vsg_server_wait: blocks until the request is done (or timeout_s > 0 passes:
+ *     VSG_ERR_DEVICE_TIMEOUT); latency_ms = submit to completion. A ticket is waited for once.
+ *   vsg_server_stats: micro-batches launched, queries and requests submitted, slots. */
+typedef struct vsg_server vsg_server;
+int vsg_server_create(vsg_index* index, size_t max_batch, size_t max_k, size_t slots, vsg_server** out);
+int vsg_server_submit(vsg_server* server, const float* queries, size_t nq, size_t k, const uint32_t* mask_words,
+                      uint32_t* out_ids, float* out_dists, uint64_t* ticket);
+int vsg_server_wait(vsg_server* server, uint64_t ticket, double timeout_s, double* latency_ms);
+int vsg_server_stats(vsg_server* server, uint64_t* batches, uint64_t* queries, uint64_t* requests,
+                     uint64_t* slots);
+void vsg_server_destroy(vsg_server* server);
+
 /* Exact top-k over caller-owned device buffers, for callers that cannot allocate device memory
  * on their search path (a serving thread that must not stall on cudaMalloc / cudaFree, which can
  * synchronise the device; a host framework that owns all device memory through its own pool; a

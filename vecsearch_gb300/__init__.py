@@ -18,7 +18,7 @@ import numpy as np
 from . import _native
 from .datasets import pack_bits
 
-__all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "cuda_available", "normalize", "recall_at_k",
+__all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "Server", "cuda_available", "normalize", "recall_at_k",
            "DeviceTimeoutError"]
 __version__ = "0.1.0"
 
@@ -178,6 +178,65 @@ class GpuBruteForceIndex:
         a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_size_t()
         _native.check(_native.lib().vsg_profile_read(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
         return a.value, b.value, n.value
+
+
+class Server:
+    """Continuous-batching search over a GpuBruteForceIndex (BF16 shortlist + exact FP32 rerank).
+
+    ``submit(queries, k, filter=None)`` queues a request and returns a ticket; ``wait(ticket)``
+    returns ``(ids int64 [nq, k], dists float32 [nq, k], latency_ms)``. Requests arriving while
+    others run are batched into the next free slot; results do not depend on the batch.
+    ``filter`` is None or a 1-D bool/uint8 mask over the index rows, shared by the request's queries.
+    """
+
+    def __init__(self, index, max_batch=1024, max_k=100, slots=2):
+        self._h = ctypes.c_void_p()
+        self.index = index
+        _native.check(_native.lib().vsg_server_create(index._h, int(max_batch), int(max_k), int(slots),
+                                                      ctypes.byref(self._h)))
+        self._pending = {}
+
+    def submit(self, queries, k=10, filter=None):
+        q = _as_f32(queries)
+        if q.ndim == 1:
+            q = q.reshape(1, q.shape[0])
+        _check_2d(q, self.index.dim)
+        nq = q.shape[0]
+        ids = np.empty((nq, int(k)), np.uint32)
+        dists = np.empty((nq, int(k)), np.float32)
+        words = None
+        if filter is not None:
+            f = np.asarray(filter)
+            if f.ndim != 1 or f.shape[0] != len(self.index):
+                raise ValueError(f"filter must be a 1-D bool array of length {len(self.index)}")
+            words = np.ascontiguousarray(pack_bits(f))
+        t = ctypes.c_uint64()
+        _native.check(_native.lib().vsg_server_submit(self._h, _ptr(q), nq, int(k),
+                                                      _ptr(words) if words is not None else None,
+                                                      _ptr(ids), _ptr(dists), ctypes.byref(t)))
+        self._pending[t.value] = (q, words, ids, dists)  # kept alive until wait()
+        return t.value
+
+    def wait(self, ticket, timeout=0.0):
+        lat = ctypes.c_double()
+        rc = _native.lib().vsg_server_wait(self._h, ctypes.c_uint64(ticket), float(timeout), ctypes.byref(lat))
+        q, words, ids, dists = self._pending.pop(ticket)
+        _native.check(rc)
+        return _ids_to_int64(ids), dists, lat.value
+
+    def stats(self):
+        v = [ctypes.c_uint64() for _ in range(4)]
+        _native.check(_native.lib().vsg_server_stats(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("batches", "queries", "requests", "slots"), (x.value for x in v)))
+
+    def close(self):
+        if self._h:
+            _native.lib().vsg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self.close()
 
 
 class HNSWExactRoute:

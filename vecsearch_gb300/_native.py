@@ -42,6 +42,11 @@ SIGNATURES = {
                                 ctypes.POINTER(_SZ)]),
     "vsg_set_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.c_double]),
     "vsg_get_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
+    "vsg_server_create": (_INT, [_P, _SZ, _SZ, _SZ, ctypes.POINTER(_P)]),
+    "vsg_server_submit": (_INT, [_P, _P, _SZ, _SZ, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64)]),
+    "vsg_server_wait": (_INT, [_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "vsg_server_stats": (_INT, [_P] + [ctypes.POINTER(ctypes.c_uint64)] * 4),
+    "vsg_server_destroy": (None, [_P]),
     "vsg_search_rows_noalloc": (_INT, [_P, _SZ, _SZ, _U32, _P, _SZ, _SZ, _P, _P, _P]),
 }
 

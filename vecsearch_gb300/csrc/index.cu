@@ -7,529 +7,17 @@
 // reference, the search never materialises a query x row distance block: one
 // fused scan kernel per search plus one merge kernel, on the index's own
 // stream, with queries in and results out through pinned staging buffers.
-#include <cuda_runtime.h>
+#include "index_impl.cuh"
 
-#include <algorithm>
-#include <cmath>
-#include <cstring>
-#include <mutex>
-#include <new>
-#include <stdexcept>
-#include <string>
-#include <vector>
-
-#include "../../include/vsg.h"
-#include "scan.cuh"
-#include "tiled.cuh"
-#include "tc.cuh"
-
-namespace {
-
+namespace vsg_detail {
 thread_local std::string g_last_error;
-
-struct DeviceTimeout : std::runtime_error {
-  using std::runtime_error::runtime_error;
-};
-
-#define VSG_CUDA(expr)                                                                    \
-  do {                                                                                    \
-    cudaError_t err_ = (expr);                                                            \
-    if (err_ != cudaSuccess) {                                                            \
-      if (err_ == cudaErrorMemoryAllocation) {                                            \
-        cudaGetLastError();                                                               \
-        throw std::bad_alloc();                                                           \
-      }                                                                                   \
-      throw std::runtime_error(std::string(#expr) + ": " + cudaGetErrorString(err_));     \
-    }                                                                                     \
-  } while (0)
-
-size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
-
-// Grow-only device buffer, zero-filled when (re)allocated; `keep` bytes of the old
-// contents are copied over (gpu_brute_force.cu:37-56).
-class DeviceBuffer {
- public:
-  DeviceBuffer() = default;
-  DeviceBuffer(const DeviceBuffer&) = delete;
-  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
-  ~DeviceBuffer() {
-    if (p_) cudaFree(p_);
-  }
-  void* get() const { return p_; }
-  size_t bytes() const { return n_; }
-  void reserve(size_t bytes, size_t keep, cudaStream_t s) {
-    if (bytes <= n_) return;
-    void* raw = nullptr;
-    VSG_CUDA(cudaMalloc(&raw, bytes));
-    cudaError_t e = cudaMemsetAsync(raw, 0, bytes, s);
-    if (e == cudaSuccess && keep) e = cudaMemcpyAsync(raw, p_, keep, cudaMemcpyDeviceToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      cudaFree(raw);
-      VSG_CUDA(e);
-    }
-    if (p_) cudaFree(p_);
-    p_ = raw;
-    n_ = bytes;
-  }
-
- private:
-  void* p_ = nullptr;
-  size_t n_ = 0;
-};
-
-class PinnedBuffer {
- public:
-  PinnedBuffer() = default;
-  PinnedBuffer(const PinnedBuffer&) = delete;
-  PinnedBuffer& operator=(const PinnedBuffer&) = delete;
-  ~PinnedBuffer() {
-    if (p_) cudaFreeHost(p_);
-  }
-  void* get() const { return p_; }
-  void reserve(size_t bytes) {
-    if (bytes <= n_) return;
-    void* raw = nullptr;
-    VSG_CUDA(cudaMallocHost(&raw, bytes));
-    if (p_) cudaFreeHost(p_);
-    p_ = raw;
-    n_ = bytes;
-  }
-
- private:
-  void* p_ = nullptr;
-  size_t n_ = 0;
-};
-
-}  // namespace
+}  // namespace vsg_detail
 
 namespace vsg {
 // The calling thread's vsg_last_error() text, for entry points defined in other files.
-void set_last_error(const std::string& msg) { g_last_error = msg; }
+void set_last_error(const std::string& msg) { vsg_detail::g_last_error = msg; }
 }  // namespace vsg
 
-namespace {
-
-bool host_is_pinned(const void* p) {
-  cudaPointerAttributes at{};
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeHost;
-}
-
-}  // namespace
-
-struct vsg_index {
-  size_t dim = 0, dp = 0;
-  uint32_t metric = 0;
-  int device = 0, sms = 1;
-  size_t smem_optin = 0;
-  size_t n = 0, cap = 0;
-  DeviceBuffer x;       // cap x dp floats
-  DeviceBuffer q;       // staged queries
-  DeviceBuffer part;    // per-split top-k lists: dists then ids
-  DeviceBuffer res;     // [status int | pad to 16][ids nq*k][dists nq*k]
-  DeviceBuffer mask;    // staged filter words
-  DeviceBuffer counters;  // per query block: CTAs done (the scan kernel's fused merge); kept zero
-  // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
-  // and kept current by later adds; bf16 query staging; merged shortlist candidates.
-  DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
-  size_t bf16_rows = 0;
-  CUtensorMap xmap{};
-  const void* xmap_base = nullptr;
-  size_t xmap_rows = 0;
-  PinnedBuffer pin_in, pin_out;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
-  std::mutex mu;
-  // Filtered searches read only the allowed rows (gather mode) when the allowed fraction is
-  // at most this; above it they scan every tile that holds an allowed row (masked full scan).
-  // 0.10 from the filtered sweep on GB300 (1M x 384, batch 16): gather wins up to ~8 % allowed,
-  // the masked full scan from ~17 %, where it shares each loaded tile among 8 queries.
-  double gather_max_fraction = 0.10;
-  // method "auto" uses the register-blocked tiled kernel from this batch size up.
-  double tiled_min_batch = 48;
-  // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
-  double shortlist_oversample = 4;
-
-  ~vsg_index() {
-    if (stream) {
-      cudaSetDevice(device);
-      cudaStreamSynchronize(stream);
-    }
-    destroy_timings();
-    if (done) cudaEventDestroy(done);
-    if (stream) cudaStreamDestroy(stream);
-  }
-
-  int* status_word() const { return static_cast<int*>(res.get()); }
-
-  // Allocates the result block (and status word) for nq x k results.
-  void reserve_results(size_t nq, size_t k) {
-    res.reserve(16 + nq * k * 8, 0, stream);
-  }
-  uint32_t* res_ids() const { return reinterpret_cast<uint32_t*>(static_cast<char*>(res.get()) + 16); }
-  float* res_dists(size_t nq, size_t k) const {
-    return reinterpret_cast<float*>(static_cast<char*>(res.get()) + 16 + nq * k * 4);
-  }
-
-  // Reads and clears the device status word (the result block must exist).
-  void check_status_sync() {
-    int st = 0;
-    VSG_CUDA(cudaMemcpyAsync(&st, status_word(), sizeof(int), cudaMemcpyDeviceToHost, stream));
-    VSG_CUDA(cudaStreamSynchronize(stream));
-    if (st != 0) {
-      reset_after_failure();
-      throw DeviceTimeout("a search kernel's wait ran past its time limit");
-    }
-  }
-
-  // After a kernel gave up on a wait: clear the status word and the merge counters.
-  void reset_after_failure() {
-    VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
-    if (counters.get()) VSG_CUDA(cudaMemsetAsync(counters.get(), 0, counters.bytes(), stream));
-    VSG_CUDA(cudaStreamSynchronize(stream));
-  }
-
-  struct Plan {
-    vsg::ScanShape shape;
-    uint32_t stages, nsplit, rows_per_split, nqb;
-  };
-
-  // filtered: the scan runs in gather mode; per_query: every query has its own mask.
-  Plan plan(size_t nq, size_t k, bool filtered = false, bool per_query = false) const {
-    Plan p{};
-    p.shape.l2 = metric == VSG_METRIC_L2;
-    p.shape.qb = 1;  // next power of two >= nq, at most 8; one query per CTA for per-query masks,
-                     // so a CTA never loads rows only other queries may return
-    while (!per_query && size_t(p.shape.qb) < nq && p.shape.qb < 8) p.shape.qb *= 2;
-    const size_t budget = smem_optin - 1024;  // headroom for the kernel's static shared memory
-    p.stages = 0;
-    for (int rw : {4, 2, 1}) {
-      p.shape.rw = rw;
-      const size_t fixed = vsg::scan_smem_bytes(p.shape, uint32_t(dp), uint32_t(k), 0);
-      const size_t tile = size_t(vsg::kScanWarps) * rw * dp * sizeof(float);
-      if (fixed + 2 * tile > budget) continue;
-      p.stages = uint32_t(std::min<size_t>(4, (budget - fixed) / tile));
-      break;
-    }
-    if (p.stages < 2)
-      throw std::invalid_argument("dim " + std::to_string(dim) + " with k " + std::to_string(k) +
-                                  " does not fit the scan kernel's shared memory");
-    p.nqb = uint32_t(ceil_div(nq, size_t(p.shape.qb)));
-    size_t want;
-    if (!filtered) {
-      want = std::max<size_t>(1, size_t(sms) / p.nqb);              // one CTA per SM in all
-      want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
-    } else {
-      // Allowed rows are spread unevenly over queries and row ranges: cap a split at 32K rows
-      // and aim for two CTAs per SM, with at least 1024 rows per split.
-      want = std::max(ceil_div(n, 32768), ceil_div(2 * size_t(sms), p.nqb));
-      want = std::max<size_t>(1, std::min(want, ceil_div(n, 1024)));
-    }
-    p.rows_per_split = uint32_t(ceil_div(ceil_div(n, want), 32) * 32);
-    p.nsplit = uint32_t(ceil_div(n, p.rows_per_split));
-    return p;
-  }
-
-  // Queues the scan + merge for device queries (stride ldq floats) on `s`. Results go to
-  // out_ids / out_dists (device). Caller holds mu and has validated k, nq, n > 0.
-  // Splits of a row range for `blocks` CTA columns: at least `min_splits`, rows per split a
-  // multiple of `align`, and a total CTA count that fills whole waves of one CTA per SM.
-  void choose_splits(size_t blocks, size_t align, size_t min_rows, uint32_t* rows_per_split,
-                     uint32_t* nsplit) const {
-    const size_t s0 = std::max<size_t>(1, size_t(sms) / blocks);
-    const size_t smax = std::max<size_t>(1, std::min(ceil_div(n, min_rows), 4 * s0));
-    size_t best = std::min(s0, smax);
-    double best_eff = 0;
-    for (size_t sp = std::min(s0, smax); sp <= smax; ++sp) {
-      const size_t ctas = blocks * sp;
-      const double eff = double(ctas) / double(ceil_div(ctas, size_t(sms)) * size_t(sms));
-      if (eff > best_eff + 1e-9) {
-        best_eff = eff;
-        best = sp;
-      }
-    }
-    const size_t rps = ceil_div(ceil_div(n, best), align) * align;
-    *rows_per_split = uint32_t(rps);
-    *nsplit = uint32_t(ceil_div(n, rps));
-  }
-
-  void enqueue_tiled(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                     cudaStream_t s) {
-    const size_t bm = size_t(vsg::tiled_block_queries(uint32_t(k), uint32_t(nq)));
-    const size_t nqb = ceil_div(nq, bm);
-    vsg::TiledArgs a{};
-    choose_splits(nqb, 128, 1024, &a.rows_per_split, &a.nsplit);
-    const size_t parts = nq * a.nsplit * k;
-    part.reserve(parts * 8, 0, stream);
-    a.x = static_cast<const float*>(x.get());
-    a.q = dq;
-    a.ldq = uint32_t(ldq);
-    a.part_d = static_cast<float*>(part.get());
-    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
-    a.n = uint32_t(n);
-    a.dp = uint32_t(dp);
-    a.nq = uint32_t(nq);
-    a.k = uint32_t(k);
-    Timing* tm = profiling ? next_timing() : nullptr;
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
-    VSG_CUDA(vsg::launch_tiled(a, metric == VSG_METRIC_L2, dim3(unsigned(nqb), a.nsplit), s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), a.nsplit, uint32_t(k)};
-    VSG_CUDA(vsg::launch_merge(m, s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
-  }
-
-  // Brings the BF16 copy and the norms up to the current rows (after a grow they are rebuilt).
-  void ensure_bf16() {
-    if (bf16_rows == n && xb.bytes() >= cap * dp * 2) return;
-    const size_t keep = xb.bytes() >= cap * dp * 2 ? bf16_rows : 0;
-    xb.reserve(cap * dp * 2, keep * dp * 2, stream);
-    xnorm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
-    VSG_CUDA(vsg::launch_to_bf16(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dp),
-                                 uint32_t(dp), static_cast<char*>(xb.get()) + keep * dp * 2,
-                                 static_cast<float*>(xnorm.get()) + keep, stream));
-    VSG_CUDA(cudaStreamSynchronize(stream));
-    bf16_rows = n;
-  }
-
-  uint32_t shortlist_size(size_t k) const {
-    const double want = std::max<double>(double(k), shortlist_oversample * double(k));
-    return uint32_t(std::min<double>(double(vsg::kTcMaxShortlist), std::ceil(want)));
-  }
-
-  void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                    cudaStream_t s) {
-    const uint32_t kp = shortlist_size(k);
-    const uint32_t stages = vsg::tc_pick_stages(kp, smem_optin - 1024);
-    if (stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
-    // Queries to bf16 (rows past nq are zero-filled by the copy engine) and their norms.
-    qb.reserve(nq * dp * 2, 0, stream);
-    qnorm.reserve(nq * sizeof(float), 0, stream);
-    VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
-                                 static_cast<float*>(qnorm.get()), s));
-    CUtensorMap qmap;
-    VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
-    if (xmap_base != xb.get() || xmap_rows != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap, xb.get(), n, dp));
-      xmap_base = xb.get();
-      xmap_rows = n;
-    }
-    const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
-    vsg::TcArgs a{};
-    choose_splits(nqb, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit);
-    const size_t parts = nq * a.nsplit * kp;
-    part.reserve(parts * 8, 0, stream);
-    cand.reserve(nq * kp * 8, 0, stream);
-    a.n = uint32_t(n);
-    a.dp = uint32_t(dp);
-    a.nq = uint32_t(nq);
-    a.kp = kp;
-    a.stages = stages;
-    a.l2 = metric == VSG_METRIC_L2 ? 1u : 0u;
-    a.xnorm = static_cast<const float*>(xnorm.get());
-    a.qnorm = static_cast<const float*>(qnorm.get());
-    a.part_d = static_cast<float*>(part.get());
-    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
-    a.status = status_word();
-    Timing* tm = profiling ? next_timing() : nullptr;
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
-    // Batches of 32+ queries first score a sample of at least 16K rows (whole tiles at the head of
-    // every split) and start each query at the k'-th best sampled distance, so the main pass keeps
-    // only rows that can still make the shortlist instead of compacting its buffers again and again.
-    const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
-    if (nq >= 32 && tiles_per_split > 1) {
-      const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(16384, size_t(a.nsplit) * vsg::kTcRows)));
-      const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
-      sample.reserve(nq * per_query * sizeof(float), 0, stream);
-      thr.reserve(nq * sizeof(float), 0, stream);
-      vsg::TcArgs sa = a;
-      sa.dump = static_cast<float*>(sample.get());
-      sa.sample_tiles = st;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, sa, dim3(unsigned(nqb), a.nsplit), s));
-      VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr, kp,
-                                         static_cast<float*>(thr.get()), s));
-      a.thr_init = static_cast<const float*>(thr.get());
-    }
-    VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, dim3(unsigned(nqb), a.nsplit), s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    float* cd = static_cast<float*>(cand.get());
-    uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
-    vsg::MergeArgs m{a.part_d, a.part_i, cd, ci, uint32_t(nq), a.nsplit, kp};
-    VSG_CUDA(vsg::launch_merge(m, s));
-    vsg::RerankArgs r{static_cast<const float*>(x.get()), dq, ci, out_dists, out_ids, uint32_t(dp),
-                      uint32_t(ldq), uint32_t(nq), kp, uint32_t(k), a.l2};
-    VSG_CUDA(vsg::launch_rerank(r, s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
-  }
-
-  bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
-    if (dmask) return false;  // filters run in the scan kernel
-    if (method == VSG_METHOD_TILED) return true;
-    return method == VSG_METHOD_AUTO && double(nq) >= tiled_min_batch;
-  }
-
-  void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
-               size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
-               uint32_t method = VSG_METHOD_AUTO) {
-    // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
-    if (method == VSG_METHOD_BF16 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
-      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
-      return;
-    }
-    if (use_tiled(method, nq, dmask)) {
-      enqueue_tiled(dq, ldq, nq, k, out_ids, out_dists, s);
-      return;
-    }
-    gather = gather && dmask != nullptr;
-    const Plan p = plan(nq, k, gather, gather && per_query);
-    const size_t parts = nq * p.nsplit * k;
-    part.reserve(parts * 8, 0, stream);
-    vsg::ScanArgs a{};
-    a.x = static_cast<const float*>(x.get());
-    a.q = dq;
-    a.ldq = uint32_t(ldq);
-    a.mask = dmask;
-    a.mask_ld = per_query ? mask_ld : 0;
-    a.part_d = static_cast<float*>(part.get());
-    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
-    a.status = status_word();
-    a.n = uint32_t(n);
-    a.dp = uint32_t(dp);
-    a.nq = uint32_t(nq);
-    a.k = uint32_t(k);
-    a.rows_per_split = p.rows_per_split;
-    a.nsplit = p.nsplit;
-    a.stages = p.stages;
-    a.gather = gather ? 1u : 0u;
-    Timing* tm = profiling ? next_timing() : nullptr;
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
-    // The last CTA of each query block merges the splits in the scan kernel itself.
-    counters.reserve(size_t(p.nqb) * sizeof(uint32_t), 0, stream);
-    a.counters = static_cast<uint32_t*>(counters.get());
-    a.out_d = out_dists;
-    a.out_i = out_ids;
-    VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
-  }
-
-  // ---- kernel timing (vsg_profile_*) ----
-  struct Timing {
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  };
-  bool profiling = false;
-  std::vector<Timing> timings;  // event pool; the first `used` are recorded
-  size_t used = 0;
-
-  Timing* next_timing() {
-    if (used == timings.size()) {
-      Timing t;
-      for (auto& e : t.ev) VSG_CUDA(cudaEventCreate(&e));
-      timings.push_back(t);
-    }
-    return &timings[used++];
-  }
-
-  void read_timings(double* scan_ms, double* merge_ms, size_t* count) {
-    double a = 0, b = 0;
-    for (size_t i = 0; i < used; ++i) {
-      VSG_CUDA(cudaEventSynchronize(timings[i].ev[2]));
-      float x = 0, y = 0;
-      VSG_CUDA(cudaEventElapsedTime(&x, timings[i].ev[0], timings[i].ev[1]));
-      VSG_CUDA(cudaEventElapsedTime(&y, timings[i].ev[1], timings[i].ev[2]));
-      a += x;
-      b += y;
-    }
-    if (scan_ms) *scan_ms = a;
-    if (merge_ms) *merge_ms = b;
-    if (count) *count = used;
-    used = 0;
-  }
-
-  void destroy_timings() {
-    for (auto& t : timings)
-      for (auto& e : t.ev)
-        if (e) cudaEventDestroy(e);
-    timings.clear();
-    used = 0;
-  }
-
-  // Host queries -> device staging (dp stride). Pageable inputs go through pinned staging.
-  const float* stage_queries(const float* host_q, size_t nq) {
-    q.reserve(nq * dp * sizeof(float), 0, stream);
-    float* dq = static_cast<float*>(q.get());
-    if (host_is_pinned(host_q)) {
-      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), host_q, dim * sizeof(float), dim * sizeof(float), nq,
-                                 cudaMemcpyHostToDevice, stream));
-    } else {
-      pin_in.reserve(nq * dim * sizeof(float));
-      std::memcpy(pin_in.get(), host_q, nq * dim * sizeof(float));
-      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), pin_in.get(), dim * sizeof(float), dim * sizeof(float),
-                                 nq, cudaMemcpyHostToDevice, stream));
-    }
-    return dq;
-  }
-
-  const uint32_t* stage_mask(const uint32_t* host_words, size_t words) {
-    mask.reserve(words * 4, 0, stream);
-    VSG_CUDA(cudaMemcpyAsync(mask.get(), host_words, words * 4, cudaMemcpyHostToDevice, stream));
-    return static_cast<const uint32_t*>(mask.get());
-  }
-
-  // Largest fraction of rows any of `masks` masks (ld words apart) allows.
-  double allowed_fraction(const uint32_t* words, size_t masks, size_t ld) const {
-    const size_t nw = ceil_div(n, 32);
-    size_t best = 0;
-    for (size_t m = 0; m < masks; ++m) {
-      const uint32_t* w = words + m * ld;
-      size_t c = 0;
-      for (size_t i = 0; i + 1 < nw; ++i) c += size_t(__builtin_popcount(w[i]));
-      const uint32_t tail = (n % 32) ? (1u << (n % 32)) - 1u : 0xFFFFFFFFu;
-      c += size_t(__builtin_popcount(w[nw - 1] & tail));
-      best = std::max(best, c);
-    }
-    return n ? double(best) / double(n) : 0.0;
-  }
-
-  // Full host-to-host search: stage, enqueue, copy the result block back, check status.
-  void search_host(const float* host_q, size_t nq, size_t k, const uint32_t* host_mask, bool per_query,
-                   size_t mask_ld, uint32_t* out_ids, float* out_dists, uint32_t method = VSG_METHOD_AUTO) {
-    VSG_CUDA(cudaSetDevice(device));
-    VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
-    reserve_results(nq, k);
-    const float* dq = stage_queries(host_q, nq);
-    const uint32_t* dm = nullptr;
-    bool gather = false;
-    if (host_mask) {
-      const size_t words = per_query ? nq * mask_ld : ceil_div(n, 32);
-      dm = stage_mask(host_mask, words);
-      gather = allowed_fraction(host_mask, per_query ? nq : 1, per_query ? mask_ld : ceil_div(n, 32)) <=
-               gather_max_fraction;
-    }
-    uint32_t* di = res_ids();
-    float* dd = res_dists(nq, k);
-    if (method == VSG_METHOD_BF16 && !dm && k <= size_t(vsg::kTcMaxShortlist)) ensure_bf16();
-    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method);
-    const size_t bytes = 16 + nq * k * 8;
-    pin_out.reserve(bytes);
-    VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));
-    VSG_CUDA(cudaEventRecord(done, stream));
-    VSG_CUDA(cudaStreamSynchronize(stream));
-    const char* h = static_cast<const char*>(pin_out.get());
-    int st = 0;
-    std::memcpy(&st, h, sizeof(int));
-    if (st != 0) {
-      reset_after_failure();
-      throw DeviceTimeout("a search kernel's wait ran past its time limit");
-    }
-    std::memcpy(out_ids, h + 16, nq * k * 4);
-    std::memcpy(out_dists, h + 16 + nq * k * 4, nq * k * 4);
-  }
-};
 
 namespace {
 

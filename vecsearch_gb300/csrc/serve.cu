@@ -1,0 +1,427 @@
+// Serving loop: continuous batching over the tensor-core shortlist path.
+//
+// The reference serves queries one call at a time (python/bindings.cpp:165-186; its gRPC shard
+// worker, distributed/shard_worker.py:26-36, calls the index per request). Here a worker thread
+// keeps requests of any size, k and filter flowing onto the GPU:
+//   * a request (host queries, k, optional allow-bits, host outputs) is queued by submit();
+//   * each slot owns device and pinned buffers sized for `max_batch` queries and a CUDA graph
+//     captured once: queries -> bf16, reset of the work counter, the persistent shortlist kernel
+//     (one CTA per SM claiming (query block, split) items; per-query k' and filter), and the
+//     fused merge + exact FP32 rerank kernel;
+//   * the worker admits queued requests into every free slot as soon as it frees (up to the
+//     slot's query and filter capacity), copies the micro-batch in, launches the graph and the
+//     copies out on the slot's stream, and completes requests when the slot's event fires. So
+//     requests that arrive while others are on the GPU join the next free slot, and the slots'
+//     copies and kernels overlap on the device;
+//   * the number of slots is bounded by free HBM at creation (half of it at most).
+// A request's result does not depend on the other requests in its micro-batch: every query's
+// scores, shortlist and rerank are computed independently (bitwise).
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+
+#include "index_impl.cuh"
+
+namespace vsg {
+void set_last_error(const std::string& msg);
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  const float* q = nullptr;
+  size_t nq = 0;
+  uint32_t k = 0;
+  const uint32_t* mask = nullptr;
+  uint32_t* out_i = nullptr;
+  float* out_d = nullptr;
+  Clock::time_point t_submit, t_done;
+  int status = -1;  // -1 pending, else a VSG_* code
+  std::string error;
+};
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  DeviceBuffer d_in, d_qb, d_qn, d_part, d_out;
+  PinnedBuffer h_in, h_out;
+  CUtensorMap qmap{};
+  std::vector<Request*> reqs;
+  bool busy = false;
+  uint32_t total_k = 0;
+};
+
+}  // namespace
+
+struct vsg_server {
+  vsg_index* idx = nullptr;
+  size_t cap_q = 0, cap_masks = 0, max_k = 0, kp_max = 0, mwords = 0, stages = 0;
+  size_t off_sq = 0, off_q = 0, off_m = 0, in_bytes = 0, out_k = 0;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::deque<Request*> queue;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::thread worker;
+  bool stop = false;
+  uint64_t next_ticket = 1;
+  uint64_t n_batches = 0, n_queries = 0, n_requests = 0;
+
+  uint32_t shortlist(uint32_t k) const {
+    const double want = std::max<double>(double(k), idx->shortlist_oversample * double(k));
+    return uint32_t(std::min<double>(double(kp_max), std::ceil(want)));
+  }
+
+  void build_slot(Slot& s) {
+    VSG_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+    VSG_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    s.d_in.reserve(in_bytes, 0, s.stream);
+    s.h_in.reserve(in_bytes);
+    std::memset(s.h_in.get(), 0, in_bytes);
+    s.d_qb.reserve(cap_q * idx->dp * 2, 0, s.stream);
+    s.d_qn.reserve(cap_q * sizeof(float), 0, s.stream);
+    // split lists: at most max(cap_q, 128 * SMs) (query, split) pairs of kp_max entries
+    const size_t pairs = std::max(cap_q, size_t(vsg::kTcQueries) * size_t(idx->sms));
+    s.d_part.reserve(pairs * kp_max * 8, 0, s.stream);
+    s.d_out.reserve(out_k * 8 + 16, 0, s.stream);
+    s.h_out.reserve(out_k * 8 + 16);
+    char* din = static_cast<char*>(s.d_in.get());
+    auto* hdr = reinterpret_cast<vsg::ServeHeader*>(din);
+    auto* sq = reinterpret_cast<vsg::ServeQuery*>(din + off_sq);
+    float* dq = reinterpret_cast<float*>(din + off_q);
+    VSG_CUDA(vsg::tc_encode_map(&s.qmap, s.d_qb.get(), cap_q, idx->dp));
+    float* out_d = static_cast<float*>(s.d_out.get());
+    uint32_t* out_i = reinterpret_cast<uint32_t*>(out_d + out_k);
+    int* status = reinterpret_cast<int*>(out_i + out_k);
+    vsg::TcArgs a{};
+    a.n = uint32_t(idx->n);
+    a.dp = uint32_t(idx->dp);
+    a.kp = uint32_t(kp_max);
+    a.stages = uint32_t(stages);
+    a.l2 = idx->metric == VSG_METRIC_L2 ? 1u : 0u;
+    a.xnorm = static_cast<const float*>(idx->xnorm.get());
+    a.qnorm = static_cast<const float*>(s.d_qn.get());
+    a.part_d = static_cast<float*>(s.d_part.get());
+    a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_part.get()) + pairs * kp_max * 4);
+    a.status = status;
+    a.hdr = hdr;
+    a.sq = sq;
+    vsg::ServeFinishArgs f{hdr, sq, a.part_d, a.part_i, static_cast<const float*>(idx->x.get()), dq, out_d, out_i,
+                           uint32_t(idx->dp), uint32_t(kp_max), a.l2};
+    VSG_CUDA(vsg::tc_prepare(a.kp, a.stages));  // kernel attributes are set before capture
+    VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+    VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
+                                 static_cast<float*>(s.d_qn.get()), s.stream));
+    VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
+    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, a, dim3(unsigned(idx->sms), 1), s.stream));
+    VSG_CUDA(vsg::launch_serve_finish(f, uint32_t(cap_q), s.stream));
+    VSG_CUDA(cudaStreamEndCapture(s.stream, &s.graph));
+    VSG_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
+  }
+
+  ~vsg_server() {
+    {
+      std::lock_guard<std::mutex> g(mu);
+      stop = true;
+    }
+    cv_work.notify_all();
+    if (worker.joinable()) worker.join();
+    for (auto& sp : slots) {
+      Slot& s = *sp;
+      if (s.stream) cudaStreamSynchronize(s.stream);
+      if (s.exec) cudaGraphExecDestroy(s.exec);
+      if (s.graph) cudaGraphDestroy(s.graph);
+      if (s.done) cudaEventDestroy(s.done);
+      if (s.stream) cudaStreamDestroy(s.stream);
+    }
+  }
+
+  // Packs `batch` into slot s and queues copies in, the graph and copies out. Caller holds no lock.
+  void launch(Slot& s, std::vector<Request*> batch) {
+    char* hin = static_cast<char*>(s.h_in.get());
+    auto* hdr = reinterpret_cast<vsg::ServeHeader*>(hin);
+    auto* sq = reinterpret_cast<vsg::ServeQuery*>(hin + off_sq);
+    float* hq = reinterpret_cast<float*>(hin + off_q);
+    uint32_t* hm = reinterpret_cast<uint32_t*>(hin + off_m);
+    const char* din = static_cast<const char*>(s.d_in.get());
+    const uint32_t* dm = reinterpret_cast<const uint32_t*>(din + off_m);
+    size_t nq = 0, nm = 0;
+    uint32_t out = 0;
+    for (Request* r : batch) {
+      const uint32_t* mask_dev = nullptr;
+      if (r->mask) {
+        std::memcpy(hm + nm * mwords, r->mask, mwords * sizeof(uint32_t));
+        mask_dev = dm + nm * mwords;
+        ++nm;
+      }
+      const uint32_t kp = shortlist(r->k);
+      for (size_t i = 0; i < r->nq; ++i, ++nq) {
+        std::memcpy(hq + nq * idx->dp, r->q + i * idx->dim, idx->dim * sizeof(float));
+        sq[nq] = vsg::ServeQuery{r->k, kp, mask_dev, out, 0};
+        out += r->k;
+      }
+    }
+    const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
+    const size_t want = std::max<size_t>(1, size_t(idx->sms) / nqb);
+    const size_t rps = ceil_div(ceil_div(idx->n, want), size_t(vsg::kTcRows)) * vsg::kTcRows;
+    hdr->nq = uint32_t(nq);
+    hdr->nqb = uint32_t(nqb);
+    hdr->rows_per_split = uint32_t(rps);
+    hdr->nsplit = uint32_t(ceil_div(idx->n, rps));
+    hdr->items = hdr->nqb * hdr->nsplit;
+    hdr->next = 0;
+    s.reqs = std::move(batch);
+    s.total_k = out;
+    char* dout = static_cast<char*>(s.d_out.get());
+    char* hout = static_cast<char*>(s.h_out.get());
+    cudaError_t e = cudaMemcpyAsync(s.d_in.get(), hin, off_q + nq * idx->dp * sizeof(float), cudaMemcpyHostToDevice,
+                                    s.stream);
+    if (e == cudaSuccess && nm)
+      e = cudaMemcpyAsync(const_cast<uint32_t*>(dm), hm, nm * mwords * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                          s.stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(s.exec, s.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hout, dout, size_t(out) * 4, cudaMemcpyDeviceToHost, s.stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hout + out_k * 4, dout + out_k * 4, size_t(out) * 4, cudaMemcpyDeviceToHost, s.stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hout + out_k * 8, dout + out_k * 8, sizeof(int), cudaMemcpyDeviceToHost, s.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail_slot(s, std::string("serving launch: ") + cudaGetErrorString(e));
+    }
+  }
+
+  void fail_slot(Slot& s, const std::string& msg) {
+    std::lock_guard<std::mutex> g(mu);
+    for (Request* r : s.reqs) {
+      r->status = VSG_ERR_CUDA;
+      r->error = msg;
+      r->t_done = Clock::now();
+    }
+    s.reqs.clear();
+    s.busy = false;
+    cv_done.notify_all();
+  }
+
+  // Results of a finished slot into the requests' host arrays.
+  void complete(Slot& s) {
+    const char* hout = static_cast<const char*>(s.h_out.get());
+    const float* od = reinterpret_cast<const float*>(hout);
+    const uint32_t* oi = reinterpret_cast<const uint32_t*>(hout + out_k * 4);
+    int st = 0;
+    std::memcpy(&st, hout + out_k * 8, sizeof(int));
+    uint32_t off = 0;
+    const auto now = Clock::now();
+    for (Request* r : s.reqs) {
+      const size_t cnt = r->nq * r->k;
+      if (st == 0) {
+        std::memcpy(r->out_d, od + off, cnt * sizeof(float));
+        std::memcpy(r->out_i, oi + off, cnt * sizeof(uint32_t));
+      }
+      off += uint32_t(cnt);
+    }
+    if (st != 0) {  // a kernel gave up on a wait: clear the status word before the slot is reused
+      int zero = 0;
+      char* dout = static_cast<char*>(s.d_out.get());
+      cudaMemcpyAsync(dout + out_k * 8, &zero, sizeof(int), cudaMemcpyHostToDevice, s.stream);
+      cudaStreamSynchronize(s.stream);
+    }
+    std::lock_guard<std::mutex> g(mu);
+    for (Request* r : s.reqs) {
+      r->status = st == 0 ? VSG_OK : VSG_ERR_DEVICE_TIMEOUT;
+      if (st != 0) r->error = "a search kernel's wait ran past its time limit";
+      r->t_done = now;
+    }
+    n_batches += 1;
+    s.reqs.clear();
+    s.busy = false;
+    cv_done.notify_all();
+  }
+
+  void run() {
+    cudaSetDevice(idx->device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+      bool progressed = false;
+      for (auto& sp : slots) {
+        Slot& s = *sp;
+        if (!s.busy) continue;
+        const cudaError_t e = cudaEventQuery(s.done);
+        if (e == cudaErrorNotReady) continue;
+        lk.unlock();
+        if (e == cudaSuccess) {
+          complete(s);
+        } else {
+          cudaGetLastError();
+          fail_slot(s, std::string("serving slot: ") + cudaGetErrorString(e));
+        }
+        lk.lock();
+        progressed = true;
+      }
+      for (auto& sp : slots) {
+        Slot& s = *sp;
+        if (s.busy || queue.empty()) continue;
+        std::vector<Request*> batch;
+        size_t nq = 0, nm = 0;
+        while (!queue.empty()) {
+          Request* r = queue.front();
+          if (nq + r->nq > cap_q || nm + (r->mask ? 1 : 0) > cap_masks) break;
+          nq += r->nq;
+          nm += r->mask ? 1 : 0;
+          batch.push_back(r);
+          queue.pop_front();
+        }
+        if (batch.empty()) continue;
+        s.busy = true;
+        n_queries += nq;
+        lk.unlock();
+        launch(s, std::move(batch));
+        lk.lock();
+        progressed = true;
+      }
+      bool any_busy = false;
+      for (auto& sp : slots) any_busy = any_busy || sp->busy;
+      if (stop && queue.empty() && !any_busy) break;
+      if (!progressed) {
+        if (any_busy)
+          cv_work.wait_for(lk, std::chrono::microseconds(20));
+        else
+          cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+      }
+    }
+  }
+};
+
+namespace {
+
+int sfail(int code, const std::string& msg) {
+  vsg::set_last_error(msg);
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots, vsg_server** out) {
+  if (!h || !out) return sfail(VSG_ERR_INVALID, "index or out is NULL");
+  *out = nullptr;
+  vsg::set_last_error("");
+  try {
+    if (max_batch == 0 || slots == 0) throw std::invalid_argument("max_batch and slots must be > 0");
+    if (max_k == 0 || max_k > size_t(vsg::kTcMaxShortlist))
+      throw std::invalid_argument("max_k must be in [1, " + std::to_string(vsg::kTcMaxShortlist) + "]");
+    std::unique_ptr<vsg_server> s(new vsg_server());
+    s->idx = h;
+    {
+      std::lock_guard<std::mutex> g(h->mu);
+      if (h->n == 0) throw std::invalid_argument("the index is empty");
+      VSG_CUDA(cudaSetDevice(h->device));
+      h->ensure_bf16();
+      h->ensure_xmap();
+    }
+    s->cap_q = max_batch;
+    s->cap_masks = std::min<size_t>(max_batch, 128);
+    s->max_k = max_k;
+    s->kp_max = std::min<size_t>(vsg::kTcMaxShortlist, size_t(std::ceil(std::max<double>(
+                                                           double(max_k), h->shortlist_oversample * double(max_k)))));
+    s->stages = vsg::tc_pick_stages(uint32_t(s->kp_max), h->smem_optin - 1024);
+    if (s->stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
+    s->mwords = ceil_div(h->n, 32);
+    s->off_sq = 256;
+    s->off_q = align256(s->off_sq + max_batch * sizeof(vsg::ServeQuery));
+    s->off_m = align256(s->off_q + max_batch * h->dp * sizeof(float));
+    s->in_bytes = s->off_m + s->cap_masks * s->mwords * sizeof(uint32_t);
+    s->out_k = max_batch * max_k;
+    // Admission by free HBM: each slot's workspace is fixed; use at most half of what is free.
+    const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms));
+    const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * s->kp_max * 8 +
+                            s->out_k * 8 + 16;
+    size_t free_b = 0, total_b = 0;
+    VSG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t fit = (free_b / 2) / std::max<size_t>(per_slot, 1);
+    if (fit == 0) throw std::bad_alloc();
+    const size_t nslots = std::min(slots, fit);
+    for (size_t i = 0; i < nslots; ++i) {
+      s->slots.emplace_back(new Slot());
+      s->build_slot(*s->slots.back());
+    }
+    vsg_server* raw = s.get();
+    s->worker = std::thread([raw] { raw->run(); });
+    *out = s.release();
+    return VSG_OK;
+  } catch (const std::invalid_argument& e) {
+    return sfail(VSG_ERR_INVALID, e.what());
+  } catch (const std::bad_alloc&) {
+    return sfail(VSG_ERR_NOMEM, "not enough device or pinned host memory for one serving slot");
+  } catch (const std::exception& e) {
+    return sfail(VSG_ERR_CUDA, e.what());
+  }
+}
+
+void vsg_server_destroy(vsg_server* s) { delete s; }
+
+int vsg_server_submit(vsg_server* s, const float* queries, size_t nq, size_t k, const uint32_t* mask_words,
+                      uint32_t* out_ids, float* out_dists, uint64_t* ticket) {
+  if (!s || !queries || !out_ids || !out_dists || !ticket) return sfail(VSG_ERR_INVALID, "NULL argument");
+  if (nq == 0 || nq > s->cap_q)
+    return sfail(VSG_ERR_INVALID, "a request must hold 1.." + std::to_string(s->cap_q) + " queries");
+  if (k == 0 || k > s->max_k) return sfail(VSG_ERR_INVALID, "k must be in [1, " + std::to_string(s->max_k) + "]");
+  std::unique_ptr<Request> r(new Request());
+  r->q = queries;
+  r->nq = nq;
+  r->k = uint32_t(k);
+  r->mask = mask_words;
+  r->out_i = out_ids;
+  r->out_d = out_dists;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    *ticket = s->next_ticket++;
+    s->queue.push_back(r.get());
+    s->reqs.emplace(*ticket, std::move(r));
+    s->n_requests += 1;
+  }
+  s->cv_work.notify_one();
+  return VSG_OK;
+}
+
+int vsg_server_wait(vsg_server* s, uint64_t ticket, double timeout_s, double* latency_ms) {
+  if (!s) return sfail(VSG_ERR_INVALID, "server is NULL");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return sfail(VSG_ERR_INVALID, "unknown ticket");
+  Request* r = it->second.get();
+  const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(
+                                           timeout_s > 0 ? timeout_s : 1e9));
+  if (!s->cv_done.wait_until(lk, deadline, [&] { return r->status != -1; }))
+    return sfail(VSG_ERR_DEVICE_TIMEOUT, "request not finished before the timeout");
+  const int st = r->status;
+  const std::string err = r->error;
+  if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  s->reqs.erase(it);
+  if (st != VSG_OK) return sfail(st, err);
+  return VSG_OK;
+}
+
+int vsg_server_stats(vsg_server* s, uint64_t* batches, uint64_t* queries, uint64_t* requests, uint64_t* slots) {
+  if (!s) return sfail(VSG_ERR_INVALID, "server is NULL");
+  std::lock_guard<std::mutex> g(s->mu);
+  if (batches) *batches = s->n_batches;
+  if (queries) *queries = s->n_queries;
+  if (requests) *requests = s->n_requests;
+  if (slots) *slots = s->slots.size();
+  return VSG_OK;
+}
+
+}  // extern "C"

@@ -559,6 +559,63 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
   }
 }
 
+// Serving mode tail, one CTA per query: warps merge split shortlists (approximate distances) in
+// registers, warp 0 merges the 8 results into the query's best kp, the 8 warps rerank those
+// exactly (the scan kernel's arithmetic) and the first k by (dist, id) are written.
+template <int E, bool L2>
+__global__ void __launch_bounds__(256) serve_finish_kernel(const ServeFinishArgs a) {
+  __shared__ float sd[8][32 * E];
+  __shared__ uint32_t si[8][32 * E];
+  __shared__ float cd[32 * E];
+  __shared__ uint32_t ci[32 * E];
+  __shared__ __align__(16) float qs[4096];
+  const uint32_t q = blockIdx.x;
+  if (q >= a.hdr->nq) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ServeQuery sq = a.sq[q];
+  const uint32_t kp = sq.kp, k = sq.k, nsplit = a.hdr->nsplit;
+  const size_t base = size_t(q) * nsplit * a.kp_max;
+  WarpTopK<E> acc;
+  acc.clear();
+  if (uint32_t(warp) < nsplit)
+    warp_merge_lists<E>(acc, a.part_d + base + size_t(warp) * a.kp_max, a.part_i + base + size_t(warp) * a.kp_max,
+                        int((nsplit - warp + 7) / 8), size_t(8) * a.kp_max, int(kp), lane);
+  acc.store(sd[warp], si[warp], int(kp), lane);
+  const bool q_in_smem = a.dp <= 4096;
+  if (q_in_smem)
+    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.dp + c];
+  __syncthreads();
+  if (warp == 0) {
+    warp_merge_lists<E>(acc, sd[1], si[1], 7, 32 * E, int(kp), lane);
+    acc.store(cd, ci, int(kp), lane);
+  }
+  __syncthreads();
+  const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.dp);
+  for (uint32_t j = warp; j < kp; j += 8) {
+    const uint32_t id = ci[j];
+    float d = __int_as_float(0x7f800000);
+    if (id != kNone) d = exact_distance<L2>(q4, reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp), a.dp / 4, lane);
+    __syncwarp();
+    if (lane == 0) cd[j] = d;
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < kp; j += blockDim.x) {
+    const float dj = cd[j];
+    const uint32_t ij = ci[j];
+    uint32_t rank = 0;
+    for (uint32_t t = 0; t < kp; ++t)
+      rank += nb_less(cd[t], ci[t], dj, ij) || (cd[t] == dj && ci[t] == ij && t < j);
+    if (rank < k) {
+      a.out_d[sq.out_off + rank] = dj;
+      a.out_i[sq.out_off + rank] = ij;
+    }
+  }
+  for (uint32_t j = kp + threadIdx.x; j < k; j += blockDim.x) {
+    a.out_d[sq.out_off + j] = __int_as_float(0x7f800000);
+    a.out_i[sq.out_off + j] = kNone;
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -600,28 +657,33 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
-                                cudaStream_t stream) {
-  if (a.stages < 2 || a.stages > uint32_t(kMaxTcStages) || a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist))
+cudaError_t tc_prepare(uint32_t kp, uint32_t stages) {
+  if (stages < 2 || stages > uint32_t(kMaxTcStages) || kp == 0 || kp > uint32_t(kTcMaxShortlist))
     return cudaErrorInvalidValue;
-  const size_t smem = tc_smem_bytes(a.stages, a.kp);
+  const size_t smem = tc_smem_bytes(stages, kp);
   static std::mutex mu;
   static size_t configured[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  {
-    std::lock_guard<std::mutex> g(mu);
-    if (dev >= 64 || smem > configured[dev]) {
-      e = cudaFuncSetAttribute(tc_shortlist_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc_shortlist_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc_shortlist_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess) return e;
-      if (dev < 64) configured[dev] = smem;
-    }
+  std::lock_guard<std::mutex> g(mu);
+  if (dev >= 64 || smem > configured[dev]) {
+    e = cudaFuncSetAttribute(tc_shortlist_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(tc_shortlist_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(tc_shortlist_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    if (dev < 64) configured[dev] = smem;
   }
+  return cudaSuccess;
+}
+
+cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
+                                cudaStream_t stream) {
+  cudaError_t e = tc_prepare(a.kp, a.stages);
+  if (e != cudaSuccess) return e;
+  const size_t smem = tc_smem_bytes(a.stages, a.kp);
   const uint32_t cap = tc_capacity(a.kp);
   if (cap <= 64)
     tc_shortlist_kernel<2><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
@@ -638,6 +700,21 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
   const size_t threads = rows * 32;
   to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp,
                                                                       static_cast<__nv_bfloat16*>(dst), norms);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, cudaStream_t stream) {
+  if (max_queries == 0) return cudaSuccess;
+  if (a.kp_max <= 32) {
+    if (a.l2) serve_finish_kernel<1, true><<<max_queries, 256, 0, stream>>>(a);
+    else serve_finish_kernel<1, false><<<max_queries, 256, 0, stream>>>(a);
+  } else if (a.kp_max <= 64) {
+    if (a.l2) serve_finish_kernel<2, true><<<max_queries, 256, 0, stream>>>(a);
+    else serve_finish_kernel<2, false><<<max_queries, 256, 0, stream>>>(a);
+  } else {
+    if (a.l2) serve_finish_kernel<4, true><<<max_queries, 256, 0, stream>>>(a);
+    else serve_finish_kernel<4, false><<<max_queries, 256, 0, stream>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -53,6 +53,22 @@ struct TcArgs {
   const float* thr_init;
 };
 
+// Serving mode, after the persistent shortlist kernel: per query (one CTA each, CTAs past
+// hdr->nq exit), merge the splits' shortlists by approximate distance, rerank the best kp
+// exactly in FP32 and write the top k at out + sq[q].out_off.
+struct ServeFinishArgs {
+  const ServeHeader* hdr;
+  const ServeQuery* sq;
+  const float* part_d;     // [nq][nsplit][kp_max]
+  const uint32_t* part_i;
+  const float* x;          // FP32 master rows
+  const float* q;          // FP32 queries, stride dp
+  float* out_d;
+  uint32_t* out_i;
+  uint32_t dp, kp_max, l2;
+};
+cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, cudaStream_t stream);
+
 // Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q].
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
                                  uint32_t kp, float* thr, cudaStream_t stream);
@@ -76,6 +92,9 @@ uint32_t tc_pick_stages(uint32_t kp, size_t budget);
 // 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp);
 
+// Sets the shortlist kernels' shared-memory limit for (kp, stages); launch_tc_shortlist does it
+// too, but a launch being captured into a CUDA graph should find it done.
+cudaError_t tc_prepare(uint32_t kp, uint32_t stages);
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
                                 cudaStream_t stream);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.

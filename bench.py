@@ -63,7 +63,10 @@ def parse():
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
     ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16"],
                     help="kernel of the main timed line (auto: the plain FP32 path by batch size)")
-    ap.add_argument("--mode", default="plain", choices=["plain", "precision"],
+    ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serve mode: offered queries/s")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve mode: seconds of arrivals per rate")
+    ap.add_argument("--plain-max-rate", type=int, default=10000, help="serve mode: highest rate for the plain path")
+    ap.add_argument("--mode", default="plain", choices=["plain", "precision", "serve"],
                     help="precision: config 4 (BF16 shortlist + rerank) sweep instead of the default line")
     ap.add_argument("--big", action="store_true", help="precision mode: add the 4M x 384 base")
     return ap.parse_args()
@@ -441,8 +444,95 @@ def run_precision(a):
                                                         "batches": batches}, "results": out}), flush=True)
 
 
+def serve_load(idx, srv, x, q, groups, words_by_group, rate, duration, seed, plain=False):
+    """Open-loop Poisson arrivals at `rate` queries/s for `duration` s; each request 1-64 queries
+    (log-uniform), k 10 or 100, 30% with one group's filter. Latency = completion - scheduled arrival."""
+    import threading
+    rng = np.random.default_rng(seed)
+    mean_q = 63.0 / np.log(64.0)  # E[m] for m = floor(exp(U(0, ln 64))) is close to this
+    req_rate = rate / mean_q
+    t, reqs, pos = 0.0, [], 0
+    while t < duration:
+        t += rng.exponential(1.0 / req_rate)
+        m = max(1, min(64, int(np.exp(rng.uniform(0, np.log(64))))))
+        if pos + m > len(q):
+            pos = 0
+        k = int(rng.choice([10, 100]))
+        g = int(rng.choice(list(words_by_group))) if rng.random() < 0.3 else None
+        reqs.append((t, pos, m, k, g))
+        pos += m
+    lat = [0.0] * len(reqs)
+    start = time.perf_counter() + 0.05
+    if plain:
+        for i, (ts, p0, m, k, g) in enumerate(reqs):
+            now = time.perf_counter() - start
+            if now < ts:
+                time.sleep(ts - now)
+            idx.search(q[p0:p0 + m], k, filter=None if g is None else (groups == g))
+            lat[i] = (time.perf_counter() - start - ts) * 1e3
+    else:
+        tickets = [None] * len(reqs)
+        done = threading.Event()
+
+        def waiter():
+            for i in range(len(reqs)):
+                while tickets[i] is None:
+                    time.sleep(20e-6)
+                srv.wait(tickets[i], timeout=60)
+                lat[i] = (time.perf_counter() - start - reqs[i][0]) * 1e3
+            done.set()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        for i, (ts, p0, m, k, g) in enumerate(reqs):
+            now = time.perf_counter() - start
+            if now < ts:
+                time.sleep(ts - now)
+            tickets[i] = srv.submit(q[p0:p0 + m], k, filter_words=None if g is None else words_by_group[g])
+        th.join()
+    end = time.perf_counter() - start
+    nq = sum(r[2] for r in reqs)
+    return {"offered_qps": rate, "requests": len(reqs), "queries": nq, "achieved_qps": round(nq / end, 1),
+            "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3)}
+
+
+def run_serve(a):
+    """Config 5: the continuous-batching server vs the plain per-call FP32 path under open-loop load."""
+    import torch
+    import vecsearch_gb300 as vsg
+    from vecsearch_gb300 import datasets as D
+    torch.cuda.set_device(0)
+    x, q = make_data(a)
+    groups = D.zipf_groups(a.n, 2000, 1.1, seed=3)
+    sizes = np.bincount(groups, minlength=2000)
+    idx = vsg.GpuBruteForceIndex(a.dim, "cosine")
+    idx.add(x)
+    cand = [g for g in range(2000) if sizes[g] >= 100][:64]
+    words_by_group = {g: D.pack_bits(groups == g) for g in cand}
+    srv = vsg.Server(idx, max_batch=1024, max_k=100, slots=2)
+    rates = [int(r) for r in a.rates.split(",") if r]
+    serve_load(idx, srv, x, q, groups, words_by_group, 2000, 0.3, 1)  # warm-up
+    server_rows = [serve_load(idx, srv, x, q, groups, words_by_group, r, a.duration, 10 + i)
+                   for i, r in enumerate(rates)]
+    st = srv.stats()
+    srv.close()
+    plain_rows = [serve_load(idx, None, x, q, groups, words_by_group, r, min(a.duration, 1.0), 10 + i, plain=True)
+                  for i, r in enumerate(rates) if r <= a.plain_max_rate]
+    line = {"metric": "served p50/p99 latency and QPS (open-loop Poisson)", "unit": "ms",
+            "data": "synthetic",
+            "config": {"workload": f"{a.n:,} x {a.dim} unit rows, requests of 1-64 queries (log-uniform), k 10 or 100,"
+                                   " 30% filtered to one Zipf(1.1) group of 2,000", "duration_s": a.duration,
+                       "server": "2 slots x 1024 queries, BF16 shortlist (k' = min(120, 4k)) + exact FP32 rerank",
+                       "plain": "one idx.search call per request (exact FP32 kernels), in arrival order"},
+            "server": server_rows, "plain": plain_rows, "server_stats": st}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.mode == "serve":
+        run_serve(a)
+        return
     if a.mode == "precision":
         run_precision(a)
         return

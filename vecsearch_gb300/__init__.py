@@ -196,7 +196,8 @@ class Server:
                                                       ctypes.byref(self._h)))
         self._pending = {}
 
-    def submit(self, queries, k=10, filter=None):
+    def submit(self, queries, k=10, filter=None, filter_words=None):
+        """Queue a request; ``filter_words`` may pass an already packed mask (datasets.pack_bits)."""
         q = _as_f32(queries)
         if q.ndim == 1:
             q = q.reshape(1, q.shape[0])
@@ -205,7 +206,11 @@ class Server:
         ids = np.empty((nq, int(k)), np.uint32)
         dists = np.empty((nq, int(k)), np.float32)
         words = None
-        if filter is not None:
+        if filter_words is not None:
+            words = np.ascontiguousarray(filter_words, np.uint32)
+            if words.ndim != 1 or words.shape[0] != (len(self.index) + 31) // 32:
+                raise ValueError("filter_words must hold ceil(len(index) / 32) uint32 words")
+        elif filter is not None:
             f = np.asarray(filter)
             if f.ndim != 1 or f.shape[0] != len(self.index):
                 raise ValueError(f"filter must be a 1-D bool array of length {len(self.index)}")

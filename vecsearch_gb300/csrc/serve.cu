@@ -52,7 +52,7 @@ struct Slot {
   cudaEvent_t done = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  DeviceBuffer d_in, d_qb, d_qn, d_part, d_out;
+  DeviceBuffer d_in, d_qb, d_qn, d_part, d_out, d_sample, d_thr;
   PinnedBuffer h_in, h_out;
   CUtensorMap qmap{};
   std::vector<Request*> reqs;
@@ -62,8 +62,11 @@ struct Slot {
 
 }  // namespace
 
+constexpr size_t kSampleRows = 16384;
+
 struct vsg_server {
   vsg_index* idx = nullptr;
+  size_t sample_per_query = 0;  // capacity of a query's sampled distances
   size_t cap_q = 0, cap_masks = 0, max_k = 0, kp_max = 0, mwords = 0, stages = 0;
   size_t off_sq = 0, off_q = 0, off_m = 0, in_bytes = 0, out_k = 0;
   std::vector<std::unique_ptr<Slot>> slots;
@@ -93,6 +96,9 @@ struct vsg_server {
     const size_t pairs = std::max(cap_q, size_t(vsg::kTcQueries) * size_t(idx->sms));
     s.d_part.reserve(pairs * kp_max * 8, 0, s.stream);
     s.d_out.reserve(out_k * 8 + 16, 0, s.stream);
+    // sample pass: per query nsplit * sample_tiles * 128 <= max(kSample + one split's tiles, ...) distances
+    s.d_sample.reserve(cap_q * sample_per_query * sizeof(float), 0, s.stream);
+    s.d_thr.reserve(cap_q * sizeof(float), 0, s.stream);
     s.h_out.reserve(out_k * 8 + 16);
     char* din = static_cast<char*>(s.d_in.get());
     auto* hdr = reinterpret_cast<vsg::ServeHeader*>(din);
@@ -121,6 +127,14 @@ struct vsg_server {
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
                                  static_cast<float*>(s.d_qn.get()), s.stream));
+    // Sample pass: the head tiles of every split give each query a starting threshold.
+    vsg::TcArgs sa = a;
+    sa.dump = static_cast<float*>(s.d_sample.get());
+    VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
+    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, sa, dim3(unsigned(idx->sms), 1), s.stream));
+    VSG_CUDA(vsg::launch_serve_select(hdr, sq, sa.dump, static_cast<float*>(s.d_thr.get()), uint32_t(cap_q),
+                                      s.stream));
+    a.thr_init = static_cast<const float*>(s.d_thr.get());
     VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
     VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, a, dim3(unsigned(idx->sms), 1), s.stream));
     VSG_CUDA(vsg::launch_serve_finish(f, uint32_t(cap_q), s.stream));
@@ -179,6 +193,9 @@ struct vsg_server {
     hdr->nsplit = uint32_t(ceil_div(idx->n, rps));
     hdr->items = hdr->nqb * hdr->nsplit;
     hdr->next = 0;
+    // Sample at least 16K rows per query (whole tiles at the head of each split).
+    const size_t tiles_per_split = ceil_div(rps, size_t(vsg::kTcRows));
+    hdr->sample_tiles = uint32_t(std::min(tiles_per_split, ceil_div(kSampleRows, size_t(hdr->nsplit) * vsg::kTcRows)));
     s.reqs = std::move(batch);
     s.total_k = out;
     char* dout = static_cast<char*>(s.d_out.get());
@@ -343,10 +360,12 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     s->off_m = align256(s->off_q + max_batch * h->dp * sizeof(float));
     s->in_bytes = s->off_m + s->cap_masks * s->mwords * sizeof(uint32_t);
     s->out_k = max_batch * max_k;
+    // nsplit * sample_tiles * 128 < kSampleRows + nsplit * 128 <= kSampleRows + 128 * SMs
+    s->sample_per_query = kSampleRows + size_t(vsg::kTcRows) * size_t(h->sms);
     // Admission by free HBM: each slot's workspace is fixed; use at most half of what is free.
     const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms));
     const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * s->kp_max * 8 +
-                            s->out_k * 8 + 16;
+                            s->out_k * 8 + 16 + max_batch * (s->sample_per_query + 1) * sizeof(float);
     size_t free_b = 0, total_b = 0;
     VSG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const size_t fit = (free_b / 2) / std::max<size_t>(per_slot, 1);

@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t qbase = qb * kTcQueries;
     const uint32_t row_begin = split * rows_per_split;
     uint32_t row_end = min(a.n, row_begin + rows_per_split);
-    if (a.dump) row_end = min(row_end, row_begin + a.sample_tiles * kTcRows);  // sample pass
+    const uint32_t sample_tiles = persistent ? a.hdr->sample_tiles : a.sample_tiles;
+    if (a.dump) row_end = min(row_end, row_begin + sample_tiles * kTcRows);  // sample pass
     const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
 
     if (warp == 0) {
@@ -305,7 +306,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // rounding; the bound is lowered by 8 ulps of max(1, |thr|) so no candidate is lost.
       auto score_bound = [](float td) { return (1.f - td) - 8.f * 1.1920929e-7f * fmaxf(1.f, fabsf(td)); };
       float s_lo = score_bound(thr_d);
-      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * a.sample_tiles * kTcRows
+      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * sample_tiles * kTcRows
                                            : nullptr;
       auto compact_lanes = [&](unsigned lanes) {
         while (lanes) {
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       if (a.dump) {  // sample pass: tiles past the split's end read as +inf
         if (dump_row)
-          for (uint32_t j = ntiles * kTcRows; j < a.sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
+          for (uint32_t j = ntiles * kTcRows; j < sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
       } else {
       // Sort every buffer, keep the best kp, and write the split's shortlist.
       compact_lanes(ok ? kFull : 0u);
@@ -521,13 +522,18 @@ __device__ __forceinline__ uint32_t order_key(float f) {
 // 8 bits per round (4 rounds). Ties resolve to the shared value, so the threshold is exact.
 __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uint32_t count, uint32_t nq,
                                                              const uint32_t* kp_per_query, uint32_t kp_all,
-                                                             float* thr) {
+                                                             float* thr, const ServeHeader* hdr,
+                                                             const ServeQuery* sq) {
   __shared__ uint32_t hist[256];
   __shared__ uint32_t sel_prefix, sel_rank;
   const uint32_t q = blockIdx.x;
+  if (hdr) {  // serving mode: the batch shape comes from the header
+    nq = hdr->nq;
+    count = hdr->nsplit * hdr->sample_tiles * uint32_t(kTcRows);
+  }
   if (q >= nq) return;
   const float* v = in + size_t(q) * count;
-  const uint32_t kp = kp_per_query ? kp_per_query[q] : kp_all;
+  const uint32_t kp = sq ? sq[q].kp : kp_per_query ? kp_per_query[q] : kp_all;
   if (threadIdx.x == 0) {
     sel_prefix = 0;
     sel_rank = kp;  // 1-based rank still to find inside the current prefix
@@ -721,7 +727,14 @@ cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, 
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
                                  uint32_t kp, float* thr, cudaStream_t stream) {
   if (nq == 0) return cudaSuccess;
-  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr);
+  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
+                                uint32_t max_queries, cudaStream_t stream) {
+  if (max_queries == 0) return cudaSuccess;
+  sample_select_kernel<<<max_queries, 256, 0, stream>>>(in, 0, 0, nullptr, 0, thr, hdr, sq);
   return cudaGetLastError();
 }
 

@@ -26,7 +26,8 @@ struct ServeHeader {
   uint32_t nq, nqb, nsplit, rows_per_split;
   uint32_t items;          // nqb * nsplit
   uint32_t next;           // work counter: CTAs claim items with atomicAdd (zeroed per launch)
-  uint32_t pad[2];
+  uint32_t sample_tiles;   // tiles per split scored by the sample pass
+  uint32_t pad;
 };
 
 struct TcArgs {
@@ -72,6 +73,10 @@ cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, 
 // Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q].
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
                                  uint32_t kp, float* thr, cudaStream_t stream);
+// Serving mode: the same with nq, count (nsplit * sample_tiles * 128) from hdr and each query's
+// k' from sq; CTAs past hdr->nq exit.
+cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
+                                uint32_t max_queries, cudaStream_t stream);
 
 struct RerankArgs {
   const float* x;          // FP32 master rows, n x dp

@@ -16,6 +16,8 @@ A step is one exact search of one batch (default batch 1: the HBM-bound case).
              / its CUDA-event time, against the measured HBM copy bandwidth.
   cpu_baseline  the reference's CPU algorithm (oracle port of brute_force.cpp
              search_batch) on this host's cores, on a bounded sample.
+  autotune   the schedule tables vsg_autotune picked for the sweep's batch sizes (taken after
+             the headline line; method auto in the sweep follows them).
   sweep      QPS for the batch sweep 1 .. 4096 (fewer steps each).
 The base (1.536 GB) is larger than L2 (129 MB), so no L2 flush is needed between steps.
 
@@ -60,6 +62,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-recall", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="sweep with the built-in schedule rules")
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
     ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16"],
                     help="kernel of the main timed line (auto: the plain FP32 path by batch size)")
@@ -329,6 +332,11 @@ def run_ours(a):
     extra = {}
     if rank == 0 and a.sweep and world == 1:
         sweep = []
+        tb = [int(s) for s in a.sweep.split(",") if s and int(s) <= q.shape[0]]
+        if not a.no_autotune:  # method auto then follows the tuned table (after the headline line)
+            t0 = time.perf_counter()
+            extra["autotune"] = {"table": idx.autotune(tb, a.k), "bf16": idx.autotune(tb, a.k, method="bf16"),
+                                 "seconds": round(time.perf_counter() - t0, 2)}
         for b in [int(s) for s in a.sweep.split(",") if s]:
             if b > q.shape[0]:
                 continue

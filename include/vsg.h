@@ -137,6 +137,20 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 
+/* Autotuner (new; the reference's tunables are compile-time constants, src/gpu_brute_force.cu:23-31).
+ * vsg_autotune times candidate schedules for each batch size (the index's own rows serve as queries;
+ * CUDA events, median of 3 after a warm-up) and keeps the fastest per batch size:
+ *   method VSG_METHOD_AUTO: streaming scan or tiled kernel, and 1x or 2x the row splits, used by
+ *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
+ *   method VSG_METHOD_BF16: whether the shortlist path runs its sampled-threshold pass.
+ * vsg_autotune_table copies a table out (count: capacity in, entries out; choice = kernel or
+ * sample flag). vsg_autotune_save / _load persist both tables as a small text file. */
+int vsg_autotune(vsg_index* index, const size_t* batches, size_t count, size_t k, uint32_t method);
+int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
+                       double* split);
+int vsg_autotune_save(vsg_index* index, const char* path);
+int vsg_autotune_load(vsg_index* index, const char* path);
+
 /* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
  * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for
  * the recorded events, returns the summed milliseconds and the number of searches, and clears

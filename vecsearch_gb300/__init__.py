@@ -169,6 +169,30 @@ class GpuBruteForceIndex:
         _native.check(_native.lib().vsg_get_tunable(self._h, name.encode(), ctypes.byref(v)))
         return v.value
 
+    def autotune(self, batches=(1, 8, 32, 64, 128, 512, 2048), k=10, method="auto"):
+        """Time candidate schedules per batch size and keep the fastest; returns the table."""
+        b = (ctypes.c_size_t * len(batches))(*[int(v) for v in batches])
+        _native.check(_native.lib().vsg_autotune(self._h, b, len(batches), int(k), _native.METHODS[method]))
+        return self.tuning(method)
+
+    def tuning(self, method="auto"):
+        """The tuned table: [{"batch", "kernel"|"sample", "split"}]."""
+        cnt = ctypes.c_size_t(64)
+        bt = (ctypes.c_uint32 * 64)()
+        ch = (ctypes.c_uint32 * 64)()
+        sp = (ctypes.c_double * 64)()
+        _native.check(_native.lib().vsg_autotune_table(self._h, _native.METHODS[method], ctypes.byref(cnt), bt, ch, sp))
+        key = "sample" if method == "bf16" else "kernel"
+        names = {0: "skinny", 1: "tiled"}
+        return [{"batch": bt[i], key: (bool(ch[i]) if key == "sample" else names[ch[i]]), "split": sp[i]}
+                for i in range(min(cnt.value, 64))]
+
+    def save_tuning(self, path):
+        _native.check(_native.lib().vsg_autotune_save(self._h, str(path).encode()))
+
+    def load_tuning(self, path):
+        _native.check(_native.lib().vsg_autotune_load(self._h, str(path).encode()))
+
     def profile(self, enable=True):
         """Start (or stop) recording CUDA-event times of the scan and merge kernels."""
         _native.check(_native.lib().vsg_profile_enable(self._h, int(enable)))

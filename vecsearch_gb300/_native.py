@@ -42,6 +42,11 @@ SIGNATURES = {
                                 ctypes.POINTER(_SZ)]),
     "vsg_set_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.c_double]),
     "vsg_get_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
+    "vsg_autotune": (_INT, [_P, ctypes.POINTER(_SZ), _SZ, _SZ, _U32]),
+    "vsg_autotune_table": (_INT, [_P, _U32, ctypes.POINTER(_SZ), ctypes.POINTER(_U32), ctypes.POINTER(_U32),
+                                  ctypes.POINTER(ctypes.c_double)]),
+    "vsg_autotune_save": (_INT, [_P, ctypes.c_char_p]),
+    "vsg_autotune_load": (_INT, [_P, ctypes.c_char_p]),
     "vsg_server_create": (_INT, [_P, _SZ, _SZ, _SZ, ctypes.POINTER(_P)]),
     "vsg_server_submit": (_INT, [_P, _P, _SZ, _SZ, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_server_wait": (_INT, [_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),

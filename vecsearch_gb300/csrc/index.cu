@@ -9,6 +9,8 @@
 // stream, with queries in and results out through pinned staging buffers.
 #include "index_impl.cuh"
 
+#include <cstdio>
+
 namespace vsg_detail {
 thread_local std::string g_last_error;
 }  // namespace vsg_detail
@@ -272,6 +274,82 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "tiled_min_batch") *value = h->tiled_min_batch;
     else if (nm == "shortlist_oversample") *value = h->shortlist_oversample;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
+  });
+}
+
+int vsg_autotune(vsg_index* h, const size_t* batches, size_t count, size_t k, uint32_t method) {
+  if (!h || (!batches && count)) return fail(VSG_ERR_INVALID, "index or batches is NULL");
+  return guarded([&] {
+    if (method != VSG_METHOD_AUTO && method != VSG_METHOD_BF16)
+      throw std::invalid_argument("the tuner covers method auto (FP32 kernels) and bf16");
+    std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    VSG_CUDA(cudaStreamWaitEvent(h->stream, h->done, 0));
+    h->autotune(batches, count, k, method);
+    VSG_CUDA(cudaEventRecord(h->done, h->stream));
+  });
+}
+
+int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
+                       double* split) {
+  if (!h || !count) return fail(VSG_ERR_INVALID, "index or count is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    const auto& t = method == VSG_METHOD_BF16 ? h->tune_bf16 : h->tune_plain;
+    const size_t cap = *count;
+    *count = t.size();
+    for (size_t i = 0; i < t.size() && i < cap; ++i) {
+      if (batch) batch[i] = t[i].batch;
+      if (choice) choice[i] = method == VSG_METHOD_BF16 ? t[i].sample : t[i].kernel;
+      if (split) split[i] = t[i].split;
+    }
+  });
+}
+
+int vsg_autotune_save(vsg_index* h, const char* path) {
+  if (!h || !path) return fail(VSG_ERR_INVALID, "index or path is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    FILE* f = std::fopen(path, "w");
+    if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    std::fprintf(f, "vsg-tuning 1 dim %zu rows %zu metric %u sms %d\n", h->dim, h->n, h->metric, h->sms);
+    for (const auto& e : h->tune_plain) std::fprintf(f, "plain %u %u %.3f\n", e.batch, e.kernel, e.split);
+    for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u\n", e.batch, e.sample);
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) throw std::runtime_error(std::string("write failed: ") + path);
+  });
+}
+
+int vsg_autotune_load(vsg_index* h, const char* path) {
+  if (!h || !path) return fail(VSG_ERR_INVALID, "index or path is NULL");
+  return guarded([&] {
+    FILE* f = std::fopen(path, "r");
+    if (!f) throw std::invalid_argument(std::string("cannot open ") + path);
+    std::vector<vsg_index::TuneEntry> plain, bf16;
+    char line[256];
+    bool header = false;
+    while (std::fgets(line, sizeof line, f)) {
+      vsg_index::TuneEntry e;
+      unsigned b = 0, c = 0;
+      double sp = 1.0;
+      if (std::strncmp(line, "vsg-tuning 1", 12) == 0) {
+        header = true;
+      } else if (std::sscanf(line, "plain %u %u %lf", &b, &c, &sp) == 3 && c <= 1 && sp > 0) {
+        e.batch = b;
+        e.kernel = c;
+        e.split = sp;
+        plain.push_back(e);
+      } else if (std::sscanf(line, "bf16 %u %u", &b, &c) == 2 && c <= 1) {
+        e.batch = b;
+        e.sample = c;
+        bf16.push_back(e);
+      }
+    }
+    std::fclose(f);
+    if (!header) throw std::invalid_argument(std::string(path) + " is not a vsg tuning file");
+    std::lock_guard<std::mutex> g(h->mu);
+    h->tune_plain = plain;
+    h->tune_bf16 = bf16;
   });
 }
 

@@ -141,6 +141,32 @@ struct vsg_index {
   // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
   double shortlist_oversample = 4;
 
+  // ---- autotuned schedules (vsg_autotune) ----
+  // plain: for unfiltered method "auto" searches of at least `batch` queries (largest such entry),
+  // which kernel (0 streaming scan, 1 tiled) and a factor on the number of row splits.
+  // bf16: whether the sampled-threshold pass runs.
+  struct TuneEntry {
+    uint32_t batch = 0, kernel = 0, sample = 1;
+    double split = 1.0;
+  };
+  std::vector<TuneEntry> tune_plain, tune_bf16;
+  // Overrides used while the tuner times a candidate (-1 / 0 = not forced).
+  int force_kernel = -1, force_sample = -1;
+  double force_split = 0.0;
+
+  static const TuneEntry* lookup(const std::vector<TuneEntry>& t, size_t nq) {
+    const TuneEntry* best = nullptr;
+    for (const TuneEntry& e : t)
+      if (e.batch <= nq && (!best || e.batch > best->batch)) best = &e;
+    return best;
+  }
+  double split_factor(size_t nq, bool filtered) const {
+    if (force_split > 0) return force_split;
+    if (filtered) return 1.0;
+    const TuneEntry* e = lookup(tune_plain, nq);
+    return e ? e->split : 1.0;
+  }
+
   ~vsg_index() {
     if (stream) {
       cudaSetDevice(device);
@@ -208,7 +234,7 @@ struct vsg_index {
     p.nqb = uint32_t(ceil_div(nq, size_t(p.shape.qb)));
     size_t want;
     if (!filtered) {
-      want = std::max<size_t>(1, size_t(sms) / p.nqb);              // one CTA per SM in all
+      want = std::max<size_t>(1, size_t(double(std::max<size_t>(1, size_t(sms) / p.nqb)) * split_factor(nq, false)));
       want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
     } else {
       // Allowed rows are spread unevenly over queries and row ranges: cap a split at 32K rows
@@ -225,9 +251,9 @@ struct vsg_index {
   // out_ids / out_dists (device). Caller holds mu and has validated k, nq, n > 0.
   // Splits of a row range for `blocks` CTA columns: at least `min_splits`, rows per split a
   // multiple of `align`, and a total CTA count that fills whole waves of one CTA per SM.
-  void choose_splits(size_t blocks, size_t align, size_t min_rows, uint32_t* rows_per_split,
-                     uint32_t* nsplit) const {
-    const size_t s0 = std::max<size_t>(1, size_t(sms) / blocks);
+  void choose_splits(size_t blocks, size_t align, size_t min_rows, uint32_t* rows_per_split, uint32_t* nsplit,
+                     double factor = 1.0) const {
+    const size_t s0 = std::max<size_t>(1, size_t(double(std::max<size_t>(1, size_t(sms) / blocks)) * factor));
     const size_t smax = std::max<size_t>(1, std::min(ceil_div(n, min_rows), 4 * s0));
     size_t best = std::min(s0, smax);
     double best_eff = 0;
@@ -249,7 +275,7 @@ struct vsg_index {
     const size_t bm = size_t(vsg::tiled_block_queries(uint32_t(k), uint32_t(nq)));
     const size_t nqb = ceil_div(nq, bm);
     vsg::TiledArgs a{};
-    choose_splits(nqb, 128, 1024, &a.rows_per_split, &a.nsplit);
+    choose_splits(nqb, 128, 1024, &a.rows_per_split, &a.nsplit, split_factor(nq, false));
     const size_t parts = nq * a.nsplit * k;
     part.reserve(parts * 8, 0, stream);
     a.x = static_cast<const float*>(x.get());
@@ -333,7 +359,9 @@ struct vsg_index {
     // every split) and start each query at the k'-th best sampled distance, so the main pass keeps
     // only rows that can still make the shortlist instead of compacting its buffers again and again.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
-    if (nq >= 32 && tiles_per_split > 1) {
+    const TuneEntry* te = lookup(tune_bf16, nq);
+    const bool run_sample = force_sample >= 0 ? force_sample != 0 : te ? te->sample != 0 : nq >= 32;
+    if (run_sample && tiles_per_split > 1) {
       const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(16384, size_t(a.nsplit) * vsg::kTcRows)));
       const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
       sample.reserve(nq * per_query * sizeof(float), 0, stream);
@@ -361,7 +389,99 @@ struct vsg_index {
   bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
     if (dmask) return false;  // filters run in the scan kernel
     if (method == VSG_METHOD_TILED) return true;
-    return method == VSG_METHOD_AUTO && double(nq) >= tiled_min_batch;
+    if (method != VSG_METHOD_AUTO) return false;
+    if (force_kernel >= 0) return force_kernel == 1;
+    if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 1;
+    return double(nq) >= tiled_min_batch;
+  }
+
+  // Times each candidate schedule for every batch size on the index's own rows as queries and
+  // keeps the fastest (CUDA events, median of 3 after a warm-up). family: VSG_METHOD_AUTO for the
+  // FP32 kernels, VSG_METHOD_BF16 for the shortlist path. Caller holds mu.
+  void autotune(const size_t* batches, size_t count, size_t k, uint32_t family) {
+    if (n == 0) throw std::invalid_argument("the index is empty");
+    if (k == 0 || k > VSG_MAX_K) throw std::invalid_argument("k must be in [1, 128]");
+    if (family == VSG_METHOD_BF16) {
+      if (k > size_t(vsg::kTcMaxShortlist)) throw std::invalid_argument("k must be <= 120 for the bf16 path");
+      ensure_bf16();
+    }
+    size_t bmax = 0;
+    for (size_t i = 0; i < count; ++i) bmax = std::max(bmax, batches[i]);
+    if (bmax == 0) throw std::invalid_argument("batch sizes must be > 0");
+    DeviceBuffer qbuf, obuf;
+    qbuf.reserve(bmax * dp * sizeof(float), 0, stream);
+    obuf.reserve(bmax * k * 8, 0, stream);
+    for (size_t r = 0; r < bmax; r += n)  // the rows themselves as queries (repeated if needed)
+      VSG_CUDA(cudaMemcpyAsync(static_cast<float*>(qbuf.get()) + r * dp, x.get(),
+                               std::min(n, bmax - r) * dp * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    cudaEvent_t e0, e1;
+    VSG_CUDA(cudaEventCreate(&e0));
+    VSG_CUDA(cudaEventCreate(&e1));
+    auto time_it = [&](size_t b, uint32_t method) {
+      float best = 1e30f;
+      std::vector<float> ts;
+      for (int rep = 0; rep < 4; ++rep) {
+        VSG_CUDA(cudaEventRecord(e0, stream));
+        enqueue(static_cast<const float*>(qbuf.get()), dp, b, k, nullptr, false, 0, false,
+                static_cast<uint32_t*>(obuf.get()), reinterpret_cast<float*>(static_cast<char*>(obuf.get()) + b * k * 4),
+                stream, method);
+        VSG_CUDA(cudaEventRecord(e1, stream));
+        VSG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        VSG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) ts.push_back(ms);  // the first run warms up
+      }
+      std::sort(ts.begin(), ts.end());
+      best = ts[ts.size() / 2];
+      return best;
+    };
+    std::vector<TuneEntry> table;
+    try {
+      for (size_t i = 0; i < count; ++i) {
+        const size_t b = batches[i];
+        TuneEntry pick;
+        pick.batch = uint32_t(b);
+        float best = 1e30f;
+        if (family == VSG_METHOD_BF16) {
+          for (int smp : {0, 1}) {
+            force_sample = smp;
+            const float t = time_it(b, VSG_METHOD_BF16);
+            if (t < best) {
+              best = t;
+              pick.sample = uint32_t(smp);
+            }
+          }
+        } else {
+          for (int kern : {0, 1}) {
+            if (kern == 1 && b < 8) continue;  // the tiled kernel's tile is 64 queries at least
+            for (double f : {1.0, 2.0}) {
+              force_kernel = kern;
+              force_split = f;
+              const float t = time_it(b, VSG_METHOD_AUTO);
+              if (t < best) {
+                best = t;
+                pick.kernel = uint32_t(kern);
+                pick.split = f;
+              }
+            }
+          }
+        }
+        table.push_back(pick);
+      }
+    } catch (...) {
+      force_kernel = -1;
+      force_sample = -1;
+      force_split = 0;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    force_kernel = -1;
+    force_sample = -1;
+    force_split = 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    (family == VSG_METHOD_BF16 ? tune_bf16 : tune_plain) = table;
   }
 
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,

@@ -35,6 +35,7 @@ extern "C" {
 #define VSG_ERR_CUDA 3           /* std::runtime_error from a CUDA call (Python: RuntimeError) */
 #define VSG_ERR_DEVICE_TIMEOUT 4 /* a kernel's bounded wait ran out (Python: RuntimeError) */
 #define VSG_ERR_NOMEM 5          /* device or pinned host allocation failed (Python: MemoryError) */
+#define VSG_ERR_IO 6             /* a file could not be read (std::runtime_error; Python: RuntimeError) */
 
 /* Same values as vecsearch::Metric (include/vecsearch/distance.h:15). */
 #define VSG_METRIC_L2 0u
@@ -103,6 +104,16 @@ int vsg_search_filtered(vsg_index* index, const float* queries, size_t nq, size_
 int vsg_hnsw_exact_below(vsg_index* index, const float* queries, size_t nq, size_t k,
                          const uint8_t* allowed, size_t allowed_len, size_t exact_below,
                          uint32_t* out_ids, float* out_dists, int* handled);
+
+/* Vectors of a saved HNSW index (the VSHNSW01 file of HNSWIndex::save, src/hnsw.cpp:368-389)
+ * straight into a device index, so the exact_below route shares the HNSW file without a second
+ * host copy of the base (HNSWIndex::load, hnsw.cpp:391-420, reads them into host memory).
+ * vsg_hnsw_file_info reads the header (dim, rows, metric 0 = L2 / 1 = inner product) and needs no
+ * GPU. vsg_add_hnsw_file appends the file's rows (ids continue from size) after checking that
+ * its dim and metric equal the index's (else VSG_ERR_INVALID). Bad magic ("not a vecsearch HNSW
+ * file"), an unreadable or truncated file -> VSG_ERR_IO, and the index is left unchanged. */
+int vsg_hnsw_file_info(const char* path, size_t* dim, size_t* rows, uint32_t* metric);
+int vsg_add_hnsw_file(vsg_index* index, const char* path, size_t* added);
 
 /* Device-resident search (new: the serving/throughput form of search()). Queries, mask and
  * outputs are device pointers; queries have row stride ldq floats (ldq >= dim). Work is queued

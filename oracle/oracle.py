@@ -177,7 +177,21 @@ class Reference:
         lib.vsref_hnsw_search.argtypes = [ctypes.c_void_p, _f32p, ctypes.c_size_t, ctypes.c_size_t,
                                           ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, _u32p, _f32p,
                                           ctypes.c_int]
+        lib.vsref_hnsw_save.restype = ctypes.c_int
+        lib.vsref_hnsw_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         self.lib = lib
+
+    def hnsw_save(self, x, path, metric="l2", num_threads=1):
+        """HNSWIndex(dim, n, metric).add(x).save(path): the reference's own index file."""
+        x = np.ascontiguousarray(x, np.float32)
+        h = self.lib.vsref_hnsw_create(x.shape[1], x.shape[0], _metric_code(metric))
+        try:
+            if self.lib.vsref_hnsw_add(h, x, x.shape[0], num_threads) != 0:
+                raise RuntimeError("reference HNSW add failed")
+            if self.lib.vsref_hnsw_save(h, str(path).encode()) != 0:
+                raise RuntimeError("reference HNSW save failed")
+        finally:
+            self.lib.vsref_hnsw_destroy(h)
 
     def bf_search(self, x, q, k, metric="ip", num_threads=1):
         """BruteForceIndex(dim, metric).add(x).search_batch(q, k): uint32 ids, float32 dists."""

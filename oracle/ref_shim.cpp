@@ -6,7 +6,7 @@
 //
 // Reference interfaces used: include/vecsearch/brute_force.h:10-25
 // (BruteForceIndex ctor/add/search/search_batch), include/vecsearch/hnsw.h:29-62
-// (SearchFilter, HNSWIndex ctor/add/search_batch).
+// (SearchFilter, HNSWIndex ctor/add/search_batch/save).
 #include <cstddef>
 #include <cstdint>
 #include <exception>
@@ -60,6 +60,15 @@ void vsref_hnsw_destroy(void* h) { delete static_cast<HNSWIndex*>(h); }
 int vsref_hnsw_add(void* h, const float* x, size_t n, int threads) {
   try {
     static_cast<HNSWIndex*>(h)->add(x, n, threads);
+    return 0;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+int vsref_hnsw_save(void* h, const char* path) {
+  try {
+    static_cast<HNSWIndex*>(h)->save(path);
     return 0;
   } catch (const std::exception&) {
     return -1;

@@ -17,6 +17,8 @@ The cases restate the reference's own tests:
   filter_exact  tests/cpp/test_filter.cpp:87-97        5000 x 32, 100 queries, ~1% mask, exact_below 1000
   filter_third  tests/python/test_bindings.py:76-91    3000 x 64, mask[::3], exact_below = n
   c1            config 1: 100k x 384 unit rows, 256-cluster mixture, IP, 64 queries, k = 10
+  hnsw_small_l2.vshnsw   HNSWIndex::save (src/hnsw.cpp:375-389) of 150 x 13 rows, L2: the file
+                the device index loads its vectors from (HNSW_FILE below regenerates the rows)
 
 Run from the repository root: ``python tests/golden/make_golden.py``.
 """
@@ -101,10 +103,18 @@ def path(name):
     return os.path.join(OUT, name + ".npz")
 
 
+HNSW_FILE = {"name": "hnsw_small_l2.vshnsw", "n": 150, "d": 13, "seed": 31, "metric": "l2"}
+
+
+def hnsw_file_rows():
+    return D.portable(HNSW_FILE["n"], HNSW_FILE["d"], HNSW_FILE["seed"])
+
+
 def main():
     if build_reference() is None:
         sys.exit("the reference sources are not present; fixtures can only be made where they are")
     ref = Reference()
+    ref.hnsw_save(hnsw_file_rows(), os.path.join(OUT, HNSW_FILE["name"]), HNSW_FILE["metric"])
     for c in CASES:
         x, q, k, metric, extra = inputs(c)
         if "mask" in extra:

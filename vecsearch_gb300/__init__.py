@@ -19,7 +19,7 @@ from . import _native
 from .datasets import pack_bits
 
 __all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "Server", "cuda_available", "normalize", "recall_at_k",
-           "DeviceTimeoutError"]
+           "hnsw_file_info", "DeviceTimeoutError"]
 __version__ = "0.1.0"
 
 DeviceTimeoutError = _native.DeviceTimeoutError
@@ -40,6 +40,14 @@ def recall_at_k(found: np.ndarray, truth: np.ndarray, k: int = 10) -> float:
     """Fraction of the true top-k found in the returned top-k (vecsearch/__init__.py:21-24)."""
     hits = sum(len(set(f[:k]) & set(t[:k])) for f, t in zip(found, truth))
     return hits / (len(found) * k)
+
+
+def hnsw_file_info(path):
+    """(dim, rows, metric) from the header of a saved HNSWIndex file (src/hnsw.cpp:368-389)."""
+    dim, rows, metric = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_uint32()
+    _native.check(_native.lib().vsg_hnsw_file_info(str(path).encode(), ctypes.byref(dim), ctypes.byref(rows),
+                                                   ctypes.byref(metric)))
+    return dim.value, rows.value, ("l2" if metric.value == _native.METRIC_L2 else "ip")
 
 
 def _parse_metric(metric):
@@ -99,6 +107,20 @@ class GpuBruteForceIndex:
 
     def __len__(self):
         return int(_native.lib().vsg_size(self._h))
+
+    @classmethod
+    def from_hnsw_file(cls, path, device=0):
+        """A device index holding the vectors of a saved HNSWIndex (HNSWIndex.save's file)."""
+        dim, _, metric = hnsw_file_info(path)
+        idx = cls(dim, metric, device=device)
+        idx.add_hnsw_file(path)
+        return idx
+
+    def add_hnsw_file(self, path):
+        """Append the vectors of a saved HNSWIndex (same dim and metric); returns the rows added."""
+        added = ctypes.c_size_t(0)
+        _native.check(_native.lib().vsg_add_hnsw_file(self._h, str(path).encode(), ctypes.byref(added)))
+        return added.value
 
     def add(self, x):
         """Append rows (bindings.cpp:157-164); ids continue from len(self)."""

@@ -73,3 +73,37 @@ def test_bf16_k100_recall(gpu_ready):
     assert vsg.recall_at_k(bi, gi, 100) >= 0.99
     gpu.set_tunable("shortlist_oversample", 1.0)
     assert gpu.get_tunable("shortlist_oversample") == 1.0
+
+
+@pytest.mark.parametrize("metric,unit", [("ip", True), ("l2", False)])
+def test_bf16_large_shortlist_many_items(gpu_ready, metric, unit):
+    # k = 100 (k' = 120): candidate buffers of 256, several (query block, split) items per CTA and
+    # thresholds shared across splits; ids must still match the plain path wherever the shortlist
+    # holds the top k (recall 1.0 against FP64).
+    vsg = gpu_ready
+    x, q = _data(120_000, 300, 128, 128, unit, 80)
+    q = np.concatenate([q, q[:212] + 0.001])  # 512 queries: 4 query blocks
+    gpu = vsg.GpuBruteForceIndex(128, metric)
+    gpu.add(x)
+    pi, pd = gpu.search(q, 100, method="skinny")
+    bi, bd = gpu.search(q, 100, method="bf16")
+    same = (bi == pi).all(1)
+    assert same.mean() >= 0.99, same.mean()
+    np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))
+    gi, _ = O.fp64_topk(x, q[:64], 100, metric)
+    assert vsg.recall_at_k(bi[:64], gi, 100) >= 0.999
+
+
+def test_bf16_wide_rows_stream_query_chunks(gpu_ready):
+    # dim 700 (> 640): the query block does not stay resident; each ring slot carries its chunk.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x = D.portable(30_000, 700, 81, normalize=True)
+    q = np.concatenate([x[:150] * 0.9 + D.portable(150, 700, 82, normalize=True) * 0.1])
+    gpu = vsg.GpuBruteForceIndex(700, "cosine")
+    gpu.add(x)
+    pi, pd = gpu.search(q, 10, method="skinny")
+    bi, bd = gpu.search(q, 10, method="bf16")
+    same = (bi == pi).all(1)
+    assert same.mean() >= 0.99, same.mean()
+    np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))

@@ -227,18 +227,20 @@ struct WarpTopK {
       }
     }
   }
-  // Entry j (0 <= j < 32 E), broadcast to the warp.
+  // Entry j (0 <= j < 32 E), broadcast to the warp. Every register is shuffled and the wanted
+  // one selected afterwards: a select over the array itself with a run-time j would make the
+  // compiler keep the array in local memory.
   __device__ __forceinline__ void entry(int j, float& od, uint32_t& oi) const {
-    float vd = d[0];
-    uint32_t vi = i[0];
+    const int src = j & 31, reg = j >> 5;
+    od = __shfl_sync(kFull, d[0], src);
+    oi = __shfl_sync(kFull, i[0], src);
 #pragma unroll
-    for (int e = 1; e < E; ++e)
-      if (j / 32 == e) {
-        vd = d[e];
-        vi = i[e];
-      }
-    od = __shfl_sync(kFull, vd, j & 31);
-    oi = __shfl_sync(kFull, vi, j & 31);
+    for (int e = 1; e < E; ++e) {
+      const float td = __shfl_sync(kFull, d[e], src);
+      const uint32_t ti = __shfl_sync(kFull, i[e], src);
+      od = reg == e ? td : od;
+      oi = reg == e ? ti : oi;
+    }
   }
   template <int R>
   __device__ __forceinline__ void cross() {

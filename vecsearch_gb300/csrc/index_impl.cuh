@@ -123,6 +123,8 @@ struct vsg_index {
   // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
   // and kept current by later adds; bf16 query staging; merged shortlist candidates.
   DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
+  DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
+  DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
@@ -326,8 +328,9 @@ struct vsg_index {
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                     cudaStream_t s) {
     const uint32_t kp = shortlist_size(k);
-    const uint32_t stages = vsg::tc_pick_stages(kp, smem_optin - 1024);
-    if (stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
+    uint32_t resident = 0;
+    const uint32_t stages = vsg::tc_pick_stages(uint32_t(dp), smem_optin - 1024, &resident);
+    if (stages < 2) throw std::invalid_argument("rows do not fit the tensor-core kernel's shared memory");
     // Queries to bf16 (rows past nq are zero-filled by the copy engine) and their norms.
     qb.reserve(nq * dp * 2, 0, stream);
     qnorm.reserve(nq * sizeof(float), 0, stream);
@@ -342,11 +345,22 @@ struct vsg_index {
     const size_t parts = nq * a.nsplit * kp;
     part.reserve(parts * 8, 0, stream);
     cand.reserve(nq * kp * 8, 0, stream);
+    // CTAs take (query block, split) items round-robin; one candidate buffer per CTA.
+    const unsigned grid = unsigned(std::min<size_t>(nqb * a.nsplit, size_t(sms)));
+    const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
+    cbuf.reserve(cbuf_entries * 8, 0, stream);
+    gthr.reserve(nq * sizeof(uint32_t), 0, stream);
+    VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
     a.n = uint32_t(n);
     a.dp = uint32_t(dp);
     a.nq = uint32_t(nq);
+    a.nqb = uint32_t(nqb);
     a.kp = kp;
     a.stages = stages;
+    a.resident = resident;
+    a.cbuf_d = static_cast<float*>(cbuf.get());
+    a.cbuf_i = reinterpret_cast<uint32_t*>(static_cast<char*>(cbuf.get()) + cbuf_entries * 4);
+    a.gthr = static_cast<uint32_t*>(gthr.get());
     a.l2 = metric == VSG_METRIC_L2 ? 1u : 0u;
     a.xnorm = static_cast<const float*>(xnorm.get());
     a.qnorm = static_cast<const float*>(qnorm.get());
@@ -369,12 +383,13 @@ struct vsg_index {
       vsg::TcArgs sa = a;
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, sa, dim3(unsigned(nqb), a.nsplit), s));
+      sa.gthr = nullptr;
+      VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, sa, grid, s));
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr, kp,
                                          static_cast<float*>(thr.get()), s));
       a.thr_init = static_cast<const float*>(thr.get());
     }
-    VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, dim3(unsigned(nqb), a.nsplit), s));
+    VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, grid, s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     float* cd = static_cast<float*>(cand.get());
     uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);

@@ -52,7 +52,7 @@ struct Slot {
   cudaEvent_t done = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  DeviceBuffer d_in, d_qb, d_qn, d_part, d_out, d_sample, d_thr;
+  DeviceBuffer d_in, d_qb, d_qn, d_part, d_out, d_sample, d_thr, d_cbuf, d_gthr;
   PinnedBuffer h_in, h_out;
   CUtensorMap qmap{};
   std::vector<Request*> reqs;
@@ -68,6 +68,7 @@ struct vsg_server {
   vsg_index* idx = nullptr;
   size_t sample_per_query = 0;  // capacity of a query's sampled distances
   size_t cap_q = 0, cap_masks = 0, max_k = 0, kp_max = 0, mwords = 0, stages = 0;
+  uint32_t resident = 0;
   size_t off_sq = 0, off_q = 0, off_m = 0, in_bytes = 0, out_k = 0;
   std::vector<std::unique_ptr<Slot>> slots;
   std::deque<Request*> queue;
@@ -99,6 +100,10 @@ struct vsg_server {
     // sample pass: per query nsplit * sample_tiles * 128 <= max(kSample + one split's tiles, ...) distances
     s.d_sample.reserve(cap_q * sample_per_query * sizeof(float), 0, s.stream);
     s.d_thr.reserve(cap_q * sizeof(float), 0, s.stream);
+    // one candidate buffer per CTA of the persistent kernel, one shared threshold per query
+    const size_t cbuf_entries = size_t(idx->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(kp_max));
+    s.d_cbuf.reserve(cbuf_entries * 8, 0, s.stream);
+    s.d_gthr.reserve(cap_q * sizeof(uint32_t), 0, s.stream);
     s.h_out.reserve(out_k * 8 + 16);
     char* din = static_cast<char*>(s.d_in.get());
     auto* hdr = reinterpret_cast<vsg::ServeHeader*>(din);
@@ -113,7 +118,11 @@ struct vsg_server {
     a.dp = uint32_t(idx->dp);
     a.kp = uint32_t(kp_max);
     a.stages = uint32_t(stages);
+    a.resident = resident;
     a.l2 = idx->metric == VSG_METRIC_L2 ? 1u : 0u;
+    a.cbuf_d = static_cast<float*>(s.d_cbuf.get());
+    a.cbuf_i = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_cbuf.get()) + cbuf_entries * 4);
+    a.gthr = static_cast<uint32_t*>(s.d_gthr.get());
     a.xnorm = static_cast<const float*>(idx->xnorm.get());
     a.qnorm = static_cast<const float*>(s.d_qn.get());
     a.part_d = static_cast<float*>(s.d_part.get());
@@ -123,20 +132,22 @@ struct vsg_server {
     a.sq = sq;
     vsg::ServeFinishArgs f{hdr, sq, a.part_d, a.part_i, static_cast<const float*>(idx->x.get()), dq, out_d, out_i,
                            uint32_t(idx->dp), uint32_t(kp_max), a.l2};
-    VSG_CUDA(vsg::tc_prepare(a.kp, a.stages));  // kernel attributes are set before capture
+    VSG_CUDA(vsg::tc_prepare(a.stages, a.dp, a.resident));  // kernel attributes are set before capture
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
                                  static_cast<float*>(s.d_qn.get()), s.stream));
     // Sample pass: the head tiles of every split give each query a starting threshold.
     vsg::TcArgs sa = a;
     sa.dump = static_cast<float*>(s.d_sample.get());
+    sa.gthr = nullptr;
     VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
-    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, sa, dim3(unsigned(idx->sms), 1), s.stream));
+    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, sa, unsigned(idx->sms), s.stream));
     VSG_CUDA(vsg::launch_serve_select(hdr, sq, sa.dump, static_cast<float*>(s.d_thr.get()), uint32_t(cap_q),
                                       s.stream));
     a.thr_init = static_cast<const float*>(s.d_thr.get());
     VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
-    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, a, dim3(unsigned(idx->sms), 1), s.stream));
+    VSG_CUDA(cudaMemsetAsync(a.gthr, 0xFF, cap_q * sizeof(uint32_t), s.stream));
+    VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, a, unsigned(idx->sms), s.stream));
     VSG_CUDA(vsg::launch_serve_finish(f, uint32_t(cap_q), s.stream));
     VSG_CUDA(cudaStreamEndCapture(s.stream, &s.graph));
     VSG_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
@@ -352,7 +363,7 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     s->max_k = max_k;
     s->kp_max = std::min<size_t>(vsg::kTcMaxShortlist, size_t(std::ceil(std::max<double>(
                                                            double(max_k), h->shortlist_oversample * double(max_k)))));
-    s->stages = vsg::tc_pick_stages(uint32_t(s->kp_max), h->smem_optin - 1024);
+    s->stages = vsg::tc_pick_stages(uint32_t(h->dp), h->smem_optin - 1024, &s->resident);
     if (s->stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
     s->mwords = ceil_div(h->n, 32);
     s->off_sq = 256;
@@ -365,7 +376,8 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     // Admission by free HBM: each slot's workspace is fixed; use at most half of what is free.
     const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms));
     const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * s->kp_max * 8 +
-                            s->out_k * 8 + 16 + max_batch * (s->sample_per_query + 1) * sizeof(float);
+                            s->out_k * 8 + 16 + max_batch * (s->sample_per_query + 2) * sizeof(float) +
+                            size_t(h->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(s->kp_max)) * 8;
     size_t free_b = 0, total_b = 0;
     VSG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const size_t fit = (free_b / 2) / std::max<size_t>(per_slot, 1);

@@ -32,41 +32,64 @@ namespace vsg {
 namespace {
 
 constexpr int kTcThreads = 192;
-constexpr uint32_t kChunkBytes = kTcQueries * kTcKChunk * 2;  // 16 KB; A and B chunks alike
-constexpr uint32_t kStageBytes = 2 * kChunkBytes;
+constexpr uint32_t kChunkBytes = kTcQueries * kTcKChunk * 2;  // 16 KB: a 64-dim chunk of 128 rows
 constexpr uint32_t kTmemCols = 2 * kTcRows;
-constexpr int kMaxTcStages = 6;
+constexpr int kMaxTcStages = 8;
+constexpr uint32_t kKeyNone = 0xFFFFFFFFu;  // shared threshold not set
 
 // Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16
 // (bits 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at 24-28.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kTcRows >> 3) << 17) |
                             (uint32_t(kTcQueries >> 4) << 24);
 
+// Shared memory: [resident query block: nkc chunks][ring of `stages` slots][barriers]. A slot
+// holds a 16 KB chunk of base rows, plus the matching query chunk when the block is not resident.
 struct TcLayout {
-  size_t lists_d, lists_i, bars, total;  // offsets from the 1024-aligned base
+  size_t a, ring, slot, bars, total;  // offsets from the 1024-aligned base; slot = bytes per slot
 };
 
-// Per-query candidate buffer capacity for a shortlist of kp: room for kp kept entries plus at
-// least one 32-score chunk; E = registers per lane of the warp sort that compacts it (C <= 32 E).
-__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) {
-  return kp <= 32 ? 64 : kp <= 64 ? 96 : kp <= 96 ? 128 : 152;
-}
-
-__host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t kp) {
+__host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t dp, bool resident) {
+  const uint32_t nkc = (dp + kTcKChunk - 1) / kTcKChunk;
   TcLayout L;
-  const uint32_t cap = tc_capacity(kp);
-  L.lists_d = size_t(stages) * kStageBytes;
-  L.lists_i = L.lists_d + size_t(cap + 1) * kTcQueries * 4;
-  L.bars = L.lists_i + size_t(cap + 1) * kTcQueries * 4;
+  L.a = 0;
+  L.slot = resident ? kChunkBytes : 2 * kChunkBytes;
+  L.ring = resident ? size_t(nkc) * kChunkBytes : 0;
+  L.bars = L.ring + size_t(stages) * L.slot;
   L.total = L.bars + 256;
   return L;
 }
 
-// Sorts the first `cnt` buffered entries of one query (entry j at bd[j] / bi[j]) and keeps the
-// best min(cnt, kp). Returns the kept count; thr becomes entry kp - 1 when kept == kp.
+// Candidate-buffer capacity per query: the kp kept entries plus room for many appends between
+// compactions (one is due when the next 32 scores might not fit). The warp sort holds 32 E = cap.
+__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) { return kp <= 16 ? 64 : kp <= 48 ? 128 : 256; }
+
+// Approximate L2 distance from squared norms and the bf16 score: |q|^2 + |x|^2 - 2 s, rounded
+// the same way wherever it is computed (the prefilter, the append and the sample pass agree).
+__device__ __forceinline__ float l2_approx(float qn, float xn, float sc) { return __fmaf_rn(-2.f, sc, __fadd_rn(qn, xn)); }
+
+// Float -> unsigned key with the same order (negative values flipped), and back.
+__device__ __forceinline__ uint32_t order_key(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t key) {
+  return __uint_as_float((key & 0x80000000u) ? (key & 0x7FFFFFFFu) : ~key);
+}
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Sorts the first `cnt` buffered entries of one query (entry j at bd[j] / bi[j], global memory)
+// and keeps the best min(cnt, kp): back into the buffer, or, when out_d is set, into out_d /
+// out_i as a sorted list of kp entries padded with (+inf, none). Returns the kept count; thr
+// becomes entry kp - 1 when kept == kp, else (+inf, none).
 template <int E>
 __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint32_t cnt, uint32_t kp, int lane,
-                                                  float& thr_d, uint32_t& thr_i) {
+                                                  float& thr_d, uint32_t& thr_i, float* out_d, uint32_t* out_i) {
+  __syncwarp();  // the lanes' appends are visible to the whole warp
   WarpTopK<E> w;
 #pragma unroll
   for (int e = 0; e < E; ++e) {
@@ -75,21 +98,77 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
     w.i[e] = j < cnt ? bi[j] : kNone;
   }
   w.sort(lane);
-  __syncwarp();
   const uint32_t keep = cnt < kp ? cnt : kp;
+  if (out_d) {
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const uint32_t j = uint32_t(e * 32 + lane);
-    if (j < keep) {
-      bd[j] = w.d[e];
-      bi[j] = w.i[e];
+    for (int e = 0; e < E; ++e) {
+      const uint32_t j = uint32_t(e * 32 + lane);
+      if (j < kp) {
+        out_d[j] = j < keep ? w.d[e] : __int_as_float(0x7f800000);
+        out_i[j] = j < keep ? w.i[e] : kNone;
+      }
     }
+    for (uint32_t j = uint32_t(32 * E + lane); j < kp; j += 32) {  // a smaller sort than the list
+      out_d[j] = __int_as_float(0x7f800000);
+      out_i[j] = kNone;
+    }
+  } else {
+    __syncwarp();  // every lane has read its entries before any is overwritten
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const uint32_t j = uint32_t(e * 32 + lane);
+      if (j < keep) {
+        bd[j] = w.d[e];
+        bi[j] = w.i[e];
+      }
+    }
+    __syncwarp();
   }
-  __syncwarp();
   thr_d = __int_as_float(0x7f800000);
   thr_i = kNone;
   if (keep == kp) w.entry(int(kp) - 1, thr_d, thr_i);
   return keep;
+}
+
+struct CompactResult {
+  uint32_t keep;  // entries kept (this lane's query, if it was compacted)
+  float td;       // its kp-th entry when keep == kp, else (+inf, none)
+  uint32_t ti;
+};
+
+// Compacts the buffers (cap = 32 E entries apart from wd / wi) of the lanes in `lanes`
+// (warp-uniform) one after another; each lane passes its own count, kp and, for the final lists,
+// its output list (else nullptr). Kept out of line: it is large and rarely runs, and the loop
+// that calls it must stay small enough for the instruction cache.
+template <int E>
+__device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsigned lanes, uint32_t cnt,
+                                                   uint32_t kp, float* out_d, uint32_t* out_i, int lane) {
+  CompactResult r{cnt, __int_as_float(0x7f800000), kNone};
+  while (lanes) {
+    const int src = __ffs(lanes) - 1;
+    lanes &= lanes - 1;
+    float* od = reinterpret_cast<float*>(__shfl_sync(kFull, reinterpret_cast<unsigned long long>(out_d), src));
+    uint32_t* oi = reinterpret_cast<uint32_t*>(__shfl_sync(kFull, reinterpret_cast<unsigned long long>(out_i), src));
+    float td;
+    uint32_t ti;
+    const uint32_t n = __shfl_sync(kFull, cnt, src), k = __shfl_sync(kFull, kp, src);
+    float* bd = wd + size_t(src) * (32 * E);
+    uint32_t* bi = wi + size_t(src) * (32 * E);
+    // The smallest sort that holds the buffered entries (a final list is often short).
+    uint32_t keep;
+    if (E > 1 && n <= 32)
+      keep = compact_query<1>(bd, bi, n, k, lane, td, ti, od, oi);
+    else if (E > 2 && n <= 64)
+      keep = compact_query<(E > 2 ? 2 : E)>(bd, bi, n, k, lane, td, ti, od, oi);
+    else
+      keep = compact_query<E>(bd, bi, n, k, lane, td, ti, od, oi);
+    if (lane == src) {
+      r.keep = keep;
+      r.td = td;
+      r.ti = ti;
+    }
+  }
+  return r;
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows 128 bytes apart, 8-row
@@ -136,8 +215,10 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
 }
 
 // tcgen05.ld and tcgen05.wait::ld are .sync.aligned: every lane of the warp must execute them
-// together, so the warp is reconverged first (the score filter before it branches per lane).
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// together, so the warp is reconverged first (the score filter before them branches per lane).
+// The load is asynchronous: its registers are valid only after tmem_wait32, which names them as
+// read-write operands so that no use can be scheduled before it.
+__device__ __forceinline__ void tmem_issue32(uint32_t taddr, uint32_t (&v)[32]) {
   __syncwarp();
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
@@ -147,10 +228,47 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
         "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
         "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-template <int E>
+__device__ __forceinline__ void tmem_wait32(uint32_t (&v)[32]) {
+  __syncwarp();
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                 "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                 "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]),
+                 "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]),
+                 "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+               :
+               : "memory");
+}
+
+
+// One column: every lane gets its own query's score in that column.
+__device__ __forceinline__ uint32_t tmem_ld1(uint32_t taddr) {
+  uint32_t v;
+  __syncwarp();
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(v) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(v) : : "memory");
+  return v;
+}
+
+// The same for 64 columns at once (two loads and two waits per tile).
+__device__ __forceinline__ void tmem_issue64(uint32_t taddr, uint32_t (&v)[64]) {
+  __syncwarp();
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]), "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]), "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]), "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]), "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+               : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait64(uint32_t (&v)[64]) {
+  __syncwarp();
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]), "+r"(v[30]), "+r"(v[31]), "+r"(v[32]), "+r"(v[33]), "+r"(v[34]), "+r"(v[35]), "+r"(v[36]), "+r"(v[37]), "+r"(v[38]), "+r"(v[39]), "+r"(v[40]), "+r"(v[41]), "+r"(v[42]), "+r"(v[43]), "+r"(v[44]), "+r"(v[45]), "+r"(v[46]), "+r"(v[47]), "+r"(v[48]), "+r"(v[49]), "+r"(v[50]), "+r"(v[51]), "+r"(v[52]), "+r"(v[53]), "+r"(v[54]), "+r"(v[55]), "+r"(v[56]), "+r"(v[57]), "+r"(v[58]), "+r"(v[59]), "+r"(v[60]), "+r"(v[61]), "+r"(v[62]), "+r"(v[63])
+               :
+               : "memory");
+}
+
+template <int E, bool L2>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_shortlist_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap xmap,
                         const TcArgs a) {
@@ -158,26 +276,31 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // 128-byte swizzled tiles need 1024-byte aligned addresses.
   const uint32_t raw = smem_addr(smem_raw);
   unsigned char* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  const uint32_t stages = a.stages, kp = a.kp;
-  const TcLayout L = tc_layout(stages, kp);
-  float* lists_d = reinterpret_cast<float*>(smem + L.lists_d);
-  uint32_t* lists_i = reinterpret_cast<uint32_t*>(smem + L.lists_i);
+  const uint32_t stages = a.stages;
+  const bool resident = a.resident != 0;
+  const TcLayout L = tc_layout(stages, a.dp, resident);
+  unsigned char* qres = smem + L.a;    // resident query block: chunk kc at kc * kChunkBytes
+  unsigned char* ring = smem + L.ring;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars);
   uint64_t* empty = full + kMaxTcStages;
-  uint64_t* tfull = empty + kMaxTcStages;   // [2]
-  uint64_t* tempty = tfull + 2;             // [2]
-  uint64_t* done = tempty + 2;
+  uint64_t* tfull = empty + kMaxTcStages;  // [2]
+  uint64_t* tempty = tfull + 2;            // [2]
+  uint64_t* afull = tempty + 2;            // resident query block landed
+  uint64_t* aempty = afull + 1;            // ... and no MMA reads it any more
+  uint64_t* done = aempty + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool persistent = a.hdr != nullptr;
   const uint32_t nq = persistent ? a.hdr->nq : a.nq;
-  const uint32_t nqb = persistent ? a.hdr->nqb : gridDim.x;
+  const uint32_t nqb = persistent ? a.hdr->nqb : a.nqb;
   const uint32_t nsplit = persistent ? a.hdr->nsplit : a.nsplit;
   const uint32_t rows_per_split = persistent ? a.hdr->rows_per_split : a.rows_per_split;
-  const uint32_t nitems = persistent ? a.hdr->items : gridDim.x * gridDim.y;
+  const uint32_t nitems = persistent ? a.hdr->items : nqb * nsplit;
   const uint32_t nkc = (a.dp + kTcKChunk - 1) / kTcKChunk;
+  constexpr uint32_t cap = 32u * E;
   __shared__ uint32_t item_slot;
+  __shared__ __align__(16) float xs_buf[4][128];  // epilogue warps' row norms of a tile (L2)
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -188,6 +311,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
     }
+    mbar_init(afull, 1);
+    mbar_init(aempty, 1);
     mbar_init(done, 1);
     mbar_fence_init();
   }
@@ -203,17 +328,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  // Ring and accumulator positions carry over from one item to the next; every role walks the
-  // same items and tiles in the same order, so they stay in step.
+  // Ring, accumulator and query-block positions carry over from one item to the next; every
+  // role walks the same items and tiles in the same order, so they stay in step.
   uint32_t s = 0, ph = 0;      // smem ring (producer and MMA issuer)
   uint32_t tglob = 0;          // tiles so far (MMA issuer and epilogue): TMEM buffer tglob & 1
+  uint32_t aitem = 0;          // items that loaded a resident query block (its barrier phases)
   uint32_t pending = 0, last_ph = 0;
+  bool a_pending = false;
+  uint32_t a_last = 0;
   bool ok = true;
   const uint64_t stream_policy = policy_evict_first();
   const uint64_t keep_policy = policy_evict_last();
 
   for (uint32_t iter = 0;; ++iter) {
-    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : (iter == 0 ? blockIdx.y * gridDim.x + blockIdx.x : nitems);
+    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : blockIdx.x + iter * gridDim.x;
     __syncthreads();
     const uint32_t item = item_slot;
     __syncthreads();  // everyone has read the slot before thread 0 may overwrite it
@@ -225,10 +353,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t sample_tiles = persistent ? a.hdr->sample_tiles : a.sample_tiles;
     if (a.dump) row_end = min(row_end, row_begin + sample_tiles * kTcRows);  // sample pass
     const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kTcRows - 1) / kTcRows : 0;
+    const bool load_a = resident && ntiles > 0;
+    const uint32_t aph = aitem & 1u;
 
     if (warp == 0) {
       // ---------------- TMA producer ----------------
       if (lane == 0) {
+        if (load_a) {
+          // The previous block's MMAs have finished before its chunks are overwritten.
+          if (!mbar_wait(aempty, aph ^ 1u)) {
+            ok = false;
+          } else {
+            mbar_arrive_expect_tx(afull, nkc * kChunkBytes);
+            for (uint32_t kc = 0; kc < nkc; ++kc)
+              tma_load_2d(qres + size_t(kc) * kChunkBytes, &qmap, int(kc * kTcKChunk), int(qbase), afull,
+                          keep_policy);
+            a_pending = true;
+            a_last = aph;
+          }
+        }
         for (uint32_t t = 0; t < ntiles && ok; ++t) {
           const int y = int(row_begin + t * kTcRows);
           for (uint32_t kc = 0; kc < nkc; ++kc) {
@@ -236,10 +379,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               ok = false;
               break;
             }
-            unsigned char* st = smem + size_t(s) * kStageBytes;
-            mbar_arrive_expect_tx(&full[s], kStageBytes);
-            tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
-            tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+            unsigned char* st = ring + size_t(s) * L.slot;
+            if (resident) {
+              mbar_arrive_expect_tx(&full[s], kChunkBytes);
+              tma_load_2d(st, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+            } else {
+              mbar_arrive_expect_tx(&full[s], 2 * kChunkBytes);
+              tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
+              tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+            }
             pending |= 1u << s;
             last_ph = (last_ph & ~(1u << s)) | (ph << s);
             if (++s == stages) {
@@ -252,6 +400,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == 1) {
       // ---------------- MMA issuer ----------------
       if (lane == 0) {
+        if (load_a) {
+          if (!mbar_wait(afull, aph)) ok = false;
+          tc_fence_after();
+        }
         for (uint32_t t = 0; t < ntiles && ok; ++t, ++tglob) {
           const uint32_t b = tglob & 1, use = tglob >> 1;
           if (!mbar_wait(&tempty[b], (use & 1) ^ 1)) {
@@ -266,8 +418,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               break;
             }
             tc_fence_after();
-            const uint32_t sa = smem_addr(smem + size_t(s) * kStageBytes);
-            const uint32_t sb = sa + kChunkBytes;
+            const uint32_t slot = smem_addr(ring + size_t(s) * L.slot);
+            const uint32_t sa = resident ? smem_addr(qres + size_t(kc) * kChunkBytes) : slot;
+            const uint32_t sb = resident ? slot : slot + kChunkBytes;
 #pragma unroll
             for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
               tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
@@ -279,25 +432,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           if (ok) tc_commit(&tfull[b]);  // the accumulator is complete once all MMAs so far are
         }
+        if (load_a && ok) tc_commit(aempty);  // the block may be replaced once these MMAs are done
       }
     } else {
       // ---------------- epilogue: one query per thread ----------------
-      // Each thread appends scores that beat its query's threshold to the query's buffer
-      // (no per-thread loops, so lanes never serialise); when a buffer may overflow in the next
-      // 32 scores, the warp sorts it together and keeps the best kp (the new threshold).
-      const uint32_t cap = tc_capacity(a.kp);
+      // Each thread appends scores that beat its query's threshold to the query's buffer (global
+      // memory, rarely touched once the threshold is tight); when a buffer may overflow in the
+      // next 32 scores, the warp sorts it together and keeps the best kp (the new threshold).
       const uint32_t quarter = uint32_t(warp & 3);
       const int m = int(quarter) * 32 + lane;
       const uint32_t qg = qbase + uint32_t(m);
       const bool qvalid = qg < nq;
       const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
       const uint32_t* qmask = (persistent && qvalid) ? a.sq[qg].mask : nullptr;
-      const float qn = (a.l2 && qvalid) ? a.qnorm[qg] : 0.f;
-      // Query m's buffer: entries m * (cap + 1) + j. The odd stride keeps the lanes' appends on
-      // different banks; a compaction reads one query's entries consecutively.
-      const uint32_t qstride = cap + 1;
-      float* wd = lists_d + size_t(quarter * 32) * qstride;  // this warp's 32 buffers
-      uint32_t* wi = lists_i + size_t(quarter * 32) * qstride;
+      const float qn = (L2 && qvalid) ? a.qnorm[qg] : 0.f;
+      float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers
+      uint32_t* wi = a.cbuf_i + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;
+      uint32_t* gq = (a.gthr && qvalid && !a.dump) ? a.gthr + qg : nullptr;
       // A sampled threshold bounds the k'-th best from above: rows at or below it are kept.
       float thr_d = (a.thr_init && qvalid) ? a.thr_init[qg] : __int_as_float(0x7f800000);
       uint32_t thr_i = kNone;
@@ -306,27 +457,47 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // rounding; the bound is lowered by 8 ulps of max(1, |thr|) so no candidate is lost.
       auto score_bound = [](float td) { return (1.f - td) - 8.f * 1.1920929e-7f * fmaxf(1.f, fabsf(td)); };
       float s_lo = score_bound(thr_d);
-      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * sample_tiles * kTcRows
-                                           : nullptr;
-      auto compact_lanes = [&](unsigned lanes) {
-        while (lanes) {
-          const int src = __ffs(lanes) - 1;
-          lanes &= lanes - 1;
-          float td;
-          uint32_t ti;
-          const uint32_t keep = compact_query<E>(wd + size_t(src) * qstride, wi + size_t(src) * qstride,
-                                                 __shfl_sync(kFull, cnt, src), __shfl_sync(kFull, kp, src), lane,
-                                                 td, ti);
-          if (lane == src) {
-            cnt = keep;
-            thr_d = td;
-            thr_i = ti;
-            s_lo = score_bound(td);
+      // Another split's k'-th best also bounds this query's k'-th best (ties kept).
+      auto tighten = [&](uint32_t key) {
+        if (key != kKeyNone) {
+          const float g = key_float(key);
+          if (g < thr_d) {
+            thr_d = g;
+            thr_i = kNone;
+            s_lo = score_bound(g);
           }
         }
       };
+      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * sample_tiles * kTcRows
+                                           : nullptr;
+      auto compact_lanes = [&](unsigned lanes, bool final_list) {
+        if (!lanes) return;
+        const bool mine = (lanes >> lane) & 1u;
+        float* od = nullptr;
+        uint32_t* oi = nullptr;
+        if (final_list && mine) {  // the split's shortlist (lists are a.kp apart)
+          const size_t o = (size_t(qg) * nsplit + split) * a.kp;
+          od = a.part_d + o;
+          oi = a.part_i + o;
+        }
+        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, od, oi, lane);
+        if (mine) {
+          cnt = r.keep;
+          if (r.keep == kp) {
+            if (nb_less(r.td, r.ti, thr_d, thr_i)) {
+              thr_d = r.td;
+              thr_i = r.ti;
+              s_lo = score_bound(r.td);
+            }
+            if (gq) atomicMin(gq, order_key(r.td));
+          }
+        }
+      };
+      uint32_t gkey = kKeyNone;  // other splits' published k'-th best, loaded one tile ahead
       for (uint32_t t = 0; t < ntiles; ++t, ++tglob) {
         const uint32_t b = tglob & 1, use = tglob >> 1;
+        tighten(gkey);
+        gkey = gq ? ld_relaxed(gq) : kKeyNone;
         if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1))) {
           if (lane == 0) atomicExch(a.status, kDevTimeout);
           ok = false;
@@ -334,53 +505,90 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         tc_fence_after();
         const uint32_t r0 = row_begin + t * kTcRows;
+        const uint32_t tbase = tmem_base + ((quarter * 32) << 16) + b * kTcRows;
+        // Allowed rows of chunk c (32 rows from c0): inside the split, real query, filter bit.
+        auto allowed = [&](uint32_t c0) {
+          uint32_t al = c0 < row_end ? (row_end - c0 >= 32 ? ~0u : (1u << (row_end - c0)) - 1u) : 0u;
+          if (qmask && al) al &= __ldg(qmask + (c0 >> 5));
+          return qvalid ? al : 0u;
+        };
+        if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-uniform
+                       // (a.dump): lanes of padded query slots take it too and store nothing.
 #pragma unroll 1
-        for (uint32_t c = 0; c < kTcRows / 32; ++c) {
-          if (!a.dump) compact_lanes(__ballot_sync(kFull, cnt + 32 > cap));
-          uint32_t v[32];
-          tmem_ld32(tmem_base + ((quarter * 32) << 16) + b * kTcRows + c * 32, v);
-          const uint32_t c0 = r0 + c * 32;
-          uint32_t allow = c0 < row_end ? (row_end - c0 >= 32 ? ~0u : (1u << (row_end - c0)) - 1u) : 0u;
-          if (qmask && allow) allow &= __ldg(qmask + (c0 >> 5));
-          if (!qvalid) allow = 0;
-          if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-uniform
-                         // (a.dump): lanes of padded query slots take it too and store nothing.
+          for (uint32_t c = 0; c < kTcRows / 32; ++c) {
+            uint32_t v[32];
+            tmem_issue32(tbase + c * 32, v);
+            tmem_wait32(v);
+            const uint32_t c0 = r0 + c * 32;
+            const uint32_t allow = allowed(c0);
             if (dump_row) {
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
                 const uint32_t row = c0 + uint32_t(j);
                 const float sc = __uint_as_float(v[j]);
-                const float dist = a.l2 ? qn + __ldg(a.xnorm + min(row, a.n - 1)) - 2.f * sc : 1.f - sc;
+                const float dist = L2 ? l2_approx(qn, __ldg(a.xnorm + min(row, a.n - 1)), sc) : 1.f - sc;
                 dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
               }
             }
-            continue;
           }
-          // Lane l holds row c0 + l's squared norm; every lane gets row j's by a shuffle.
-          const float xn_l = a.l2 ? __ldg(a.xnorm + min(c0 + uint32_t(lane), a.n - 1)) : 0.f;
+        } else {
+          // The tile's scores arrive in two loads of 64 columns. One reduction per 32 columns
+          // (the largest score, or the smallest distance with the same expression as the
+          // append) and one vote per half; the per-score path runs only when some lane may have
+          // a candidate.
+          float* xs = xs_buf[quarter];
+          if constexpr (L2) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const uint32_t row = c0 + uint32_t(j);
-            const float sc = __uint_as_float(v[j]);
-            float dist;
-            bool p;
-            if (a.l2) {
-              dist = qn + __shfl_sync(kFull, xn_l, j) - 2.f * sc;
-              p = dist <= thr_d;
-            } else {
-              dist = 0.f;
-              p = sc >= s_lo;
+            for (int c = 0; c < 4; ++c) xs[c * 32 + lane] = __ldg(a.xnorm + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
+            __syncwarp();
+          }
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h) {
+            uint32_t v[64];
+            tmem_issue64(tbase + uint32_t(h) * 64, v);
+            tmem_wait64(v);
+            // Per 32 columns, the entries that may beat the threshold (the prefilter's test) as a
+            // bit mask; one vote per half, and only the columns some lane needs go further.
+            uint32_t bits[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+              const int cg = h * 2 + c;
+              uint32_t m[4] = {0u, 0u, 0u, 0u};  // four interleaved chains
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const float sc = __uint_as_float(v[c * 32 + j]);
+                const bool p = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) <= thr_d : sc >= s_lo;
+                m[j & 3] |= p ? (1u << j) : 0u;
+              }
+              bits[c] = (m[0] | m[1] | m[2] | m[3]) & allowed(r0 + uint32_t(cg) * 32);
             }
-            p = p && ((allow >> j) & 1u);
-            if (__any_sync(kFull, p)) {  // rare once the threshold is tight
-              if (!a.l2) dist = 1.f - sc;
-              if (p && nb_less(dist, row, thr_d, thr_i)) {
-                wd[lane * qstride + cnt] = dist;
-                wi[lane * qstride + cnt] = row;
-                ++cnt;
+            if (__any_sync(kFull, (bits[0] | bits[1]) != 0u)) {  // rare once the threshold is tight
+#pragma unroll
+              for (int c = 0; c < 2; ++c) {
+                uint32_t cols = __reduce_or_sync(kFull, bits[c]);
+                if (!cols) continue;
+                compact_lanes(__ballot_sync(kFull, cnt + 32 > cap), false);
+                const int cg = h * 2 + c;
+                const uint32_t c0 = r0 + uint32_t(cg) * 32;
+                // Columns some lane needs, in a rolled warp-uniform loop (the code stays small):
+                // the column is read again from TMEM and its lanes append.
+                while (cols) {
+                  const int j = __ffs(cols) - 1;
+                  cols &= cols - 1;
+                  const float sc = __uint_as_float(tmem_ld1(tbase + uint32_t(cg * 32 + j)));
+                  if ((bits[c] >> j) & 1u) {
+                    const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
+                    if (nb_less(dist, c0 + uint32_t(j), thr_d, thr_i)) {
+                      wd[size_t(lane) * cap + cnt] = dist;
+                      wi[size_t(lane) * cap + cnt] = c0 + uint32_t(j);
+                      ++cnt;
+                    }
+                  }
+                }
               }
             }
           }
+          if (L2) __syncwarp();  // the next tile rewrites xs
         }
         tc_fence_before();
         __syncwarp();
@@ -390,17 +598,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (dump_row)
           for (uint32_t j = ntiles * kTcRows; j < sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
       } else {
-      // Sort every buffer, keep the best kp, and write the split's shortlist.
-      compact_lanes(ok ? kFull : 0u);
-      if (qvalid) {
-        const size_t o = (size_t(qg) * nsplit + split) * a.kp;  // lists are a.kp apart
-        for (uint32_t j = 0; j < kp; ++j) {
-          a.part_d[o + j] = j < cnt ? wd[lane * qstride + j] : __int_as_float(0x7f800000);
-          a.part_i[o + j] = j < cnt ? wi[lane * qstride + j] : kNone;
-        }
-      }
+        // Sort every buffer, keep the best kp and write the split's shortlist.
+        compact_lanes(ok ? __ballot_sync(kFull, qvalid) : 0u, true);
       }
     }
+    if (load_a) ++aitem;
     if (!__syncthreads_and(ok)) break;  // a role gave up: no further items
   }
 
@@ -409,6 +611,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (uint32_t i = 0; i < stages; ++i)
       if ((pending >> i) & 1u)
         if (!mbar_wait(&full[i], (last_ph >> i) & 1u)) ok = false;
+    if (a_pending && !mbar_wait(afull, a_last)) ok = false;
     if (!ok) atomicExch(a.status, kDevTimeout);
   }
   if (warp == 1 && lane == 0) {
@@ -510,12 +713,6 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
     a.out_d[size_t(q) * a.k + j] = __int_as_float(0x7f800000);
     a.out_i[size_t(q) * a.k + j] = kNone;
   }
-}
-
-// Float -> unsigned key with the same order (negative values flipped).
-__device__ __forceinline__ uint32_t order_key(float f) {
-  const uint32_t u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
 // One CTA per query: the kp-th smallest of `count` values by radix selection on the order key,
@@ -642,13 +839,26 @@ EncodeTiledFn encode_fn() {
 
 }  // namespace
 
-size_t tc_smem_bytes(uint32_t stages, uint32_t kp) { return tc_layout(stages, kp).total + 1024; }
+size_t tc_smem_bytes(uint32_t stages, uint32_t dp, uint32_t resident) {
+  return tc_layout(stages, dp, resident != 0).total + 1024;
+}
 
-uint32_t tc_pick_stages(uint32_t kp, size_t budget) {
-  for (uint32_t s = kMaxTcStages; s >= 2; --s)
-    if (tc_smem_bytes(s, kp) <= budget) return s;
+uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident) {
+  // The kernel's static shared memory (work slot, row norms: 2,064 bytes) comes on top.
+  constexpr size_t kStatic = 3072;
+  budget = budget > kStatic ? budget - kStatic : 0;
+  for (uint32_t s = kMaxTcStages; s >= 4; --s)
+    if (tc_smem_bytes(s, dp, 1) <= budget) {
+      *resident = 1;
+      return s;
+    }
+  *resident = 0;
+  for (uint32_t s = 6; s >= 2; --s)
+    if (tc_smem_bytes(s, dp, 0) <= budget) return s;
   return 0;
 }
+
+uint32_t tc_buffer_capacity(uint32_t kp) { return tc_capacity(kp); }
 
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp) {
   EncodeTiledFn fn = encode_fn();
@@ -663,10 +873,9 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-cudaError_t tc_prepare(uint32_t kp, uint32_t stages) {
-  if (stages < 2 || stages > uint32_t(kMaxTcStages) || kp == 0 || kp > uint32_t(kTcMaxShortlist))
-    return cudaErrorInvalidValue;
-  const size_t smem = tc_smem_bytes(stages, kp);
+cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident) {
+  if (stages < 2 || stages > uint32_t(kMaxTcStages) || dp == 0) return cudaErrorInvalidValue;
+  const size_t smem = tc_smem_bytes(stages, dp, resident);
   static std::mutex mu;
   static size_t configured[64] = {};
   int dev = 0;
@@ -674,29 +883,47 @@ cudaError_t tc_prepare(uint32_t kp, uint32_t stages) {
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> g(mu);
   if (dev >= 64 || smem > configured[dev]) {
-    e = cudaFuncSetAttribute(tc_shortlist_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tc_shortlist_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tc_shortlist_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const void* fns[] = {reinterpret_cast<const void*>(tc_shortlist_kernel<2, false>),
+                         reinterpret_cast<const void*>(tc_shortlist_kernel<4, false>),
+                         reinterpret_cast<const void*>(tc_shortlist_kernel<8, false>),
+                         reinterpret_cast<const void*>(tc_shortlist_kernel<2, true>),
+                         reinterpret_cast<const void*>(tc_shortlist_kernel<4, true>),
+                         reinterpret_cast<const void*>(tc_shortlist_kernel<8, true>)};
+    for (const void* f : fns)
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     if (dev < 64) configured[dev] = smem;
   }
   return cudaSuccess;
 }
 
-cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
+cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream) {
-  cudaError_t e = tc_prepare(a.kp, a.stages);
+  if (a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist) || !a.cbuf_d || !a.cbuf_i) return cudaErrorInvalidValue;
+  if (a.resident) {  // the resident block's chunks and a ring of at least 4 slots
+    const size_t need = tc_smem_bytes(4, a.dp, 1);
+    if (tc_smem_bytes(a.stages, a.dp, 1) < need) return cudaErrorInvalidValue;
+  }
+  if (grid == 0) return cudaSuccess;
+  cudaError_t e = tc_prepare(a.stages, a.dp, a.resident);
   if (e != cudaSuccess) return e;
-  const size_t smem = tc_smem_bytes(a.stages, a.kp);
+  const size_t smem = tc_smem_bytes(a.stages, a.dp, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
-  if (cap <= 64)
-    tc_shortlist_kernel<2><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-  else if (cap <= 128)
-    tc_shortlist_kernel<4><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-  else
-    tc_shortlist_kernel<8><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  if (a.l2) {
+    if (cap == 64)
+      tc_shortlist_kernel<2, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+    else if (cap == 128)
+      tc_shortlist_kernel<4, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+    else
+      tc_shortlist_kernel<8, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  } else {
+    if (cap == 64)
+      tc_shortlist_kernel<2, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+    else if (cap == 128)
+      tc_shortlist_kernel<4, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+    else
+      tc_shortlist_kernel<8, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
+  }
   return cudaGetLastError();
 }
 

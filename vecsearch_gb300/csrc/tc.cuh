@@ -34,15 +34,25 @@ struct TcArgs {
   uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 120)
   uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
   uint32_t stages;
+  uint32_t resident;               // 1: the query block stays in shared memory for a whole item
   uint32_t l2;                     // 1: approximate L2 from norms, 0: 1 - q.x
+  // Per-CTA candidate buffers in global memory: CTA c (linear index) owns entries
+  // [c * 128 * cap, (c + 1) * 128 * cap), cap = tc_buffer_capacity(kp) per query slot.
+  float* cbuf_d;
+  uint32_t* cbuf_i;
+  // Per-query shared thresholds (order keys of approximate distances, 0xFFFFFFFF = none),
+  // or nullptr: a split whose list is full publishes its k'-th best with atomicMin and every
+  // split of the query prunes against the smallest published value. Set to 0xFF bytes first.
   const float* xnorm;              // squared row norms (L2 only)
   const float* qnorm;              // squared query norms (L2 only)
   float* part_d;                   // [nq][nsplit][kp] approximate distances, sorted
   uint32_t* part_i;
   int* status;
+  uint32_t* gthr;
   // Serving mode (persistent): when hdr is set the grid has one CTA per SM, the batch shape
   // (nq, splits) comes from hdr, CTAs claim (query block, split) items from hdr->next, and each
-  // query's shortlist size and filter come from sq.
+  // query's shortlist size and filter come from sq. Otherwise CTA c takes items c, c + grid, ...
+  // of the nqb * nsplit items (query block = item % nqb, split = item / nqb).
   ServeHeader* hdr;
   const ServeQuery* sq;
   // Sample pass: when dump is set, each CTA scores only the first sample_tiles tiles of its split
@@ -52,6 +62,7 @@ struct TcArgs {
   uint32_t sample_tiles;
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
+  uint32_t nqb;  // query blocks (non-serving launches)
 };
 
 // Serving mode, after the persistent shortlist kernel: per query (one CTA each, CTAs past
@@ -88,19 +99,23 @@ struct RerankArgs {
   uint32_t l2;
 };
 
-// Shared memory of the shortlist kernel for a given ring depth and shortlist size.
-size_t tc_smem_bytes(uint32_t stages, uint32_t kp);
-// Deepest ring (<= 6) that fits `budget` bytes, or 0.
-uint32_t tc_pick_stages(uint32_t kp, size_t budget);
+// Shared memory of the shortlist kernel: ring depth, padded dim, resident query block or not.
+size_t tc_smem_bytes(uint32_t stages, uint32_t dp, uint32_t resident);
+// Ring depth for rows of dp bf16 that fits `budget` bytes (0 if none): the query block stays
+// resident (*resident = 1) when that leaves at least 4 slots, else each slot carries a query chunk too.
+uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident);
+// Candidate-buffer entries per query slot for a shortlist of kp (64, 128 or 256).
+uint32_t tc_buffer_capacity(uint32_t kp);
 
 // Encodes a 2-D bf16 tensor map (rows x dp, row stride dp * 2 bytes) with a 64 x 128 box and
 // 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp);
 
-// Sets the shortlist kernels' shared-memory limit for (kp, stages); launch_tc_shortlist does it
-// too, but a launch being captured into a CUDA graph should find it done.
-cudaError_t tc_prepare(uint32_t kp, uint32_t stages);
-cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, dim3 grid,
+// Sets the shortlist kernels' shared-memory limit for (stages, dp, resident); launch_tc_shortlist
+// does it too, but a launch being captured into a CUDA graph should find it done.
+cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident);
+// grid: CTAs (x only); the candidate buffers must hold grid * 128 * tc_buffer_capacity(kp) entries.
+cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,

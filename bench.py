@@ -423,9 +423,11 @@ def run_precision(a):
             for over in ((4, 8) if k == 10 else (4,)):  # k = 100: k' is capped at 120 either way
                 idx.set_tunable("shortlist_oversample", over)
                 kp = min(120, over * k)
+                tune = idx.autotune(batches, k, method="bf16")  # sample size per batch for this k'
                 a2 = argparse.Namespace(**vars(a))
                 a2.k = k
-                row = {"n": n, "k": k, "k_prime": kp, "qps": {}, "plain_qps": {}}
+                row = {"n": n, "k": k, "k_prime": kp, "qps": {}, "plain_qps": {},
+                       "sample_rows": {e["batch"]: e["sample"] for e in tune}}
                 for b in batches:
                     st = max(3, min(100, int(1e5 / b)))
                     ms, tc_ms, rr_ms, l = time_device(idx, torch, qd, a2, b, st, 3, stream, method="bf16")

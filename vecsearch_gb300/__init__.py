@@ -198,7 +198,7 @@ class GpuBruteForceIndex:
         return self.tuning(method)
 
     def tuning(self, method="auto"):
-        """The tuned table: [{"batch", "kernel"|"sample", "split"}]."""
+        """The tuned table: [{"batch", "kernel" (FP32) or "sample" (bf16: rows sampled, 0 = none), "split"}]."""
         cnt = ctypes.c_size_t(64)
         bt = (ctypes.c_uint32 * 64)()
         ch = (ctypes.c_uint32 * 64)()
@@ -206,7 +206,7 @@ class GpuBruteForceIndex:
         _native.check(_native.lib().vsg_autotune_table(self._h, _native.METHODS[method], ctypes.byref(cnt), bt, ch, sp))
         key = "sample" if method == "bf16" else "kernel"
         names = {0: "skinny", 1: "tiled"}
-        return [{"batch": bt[i], key: (bool(ch[i]) if key == "sample" else names[ch[i]]), "split": sp[i]}
+        return [{"batch": bt[i], key: (int(ch[i]) if key == "sample" else names[ch[i]]), "split": sp[i]}
                 for i in range(min(cnt.value, 64))]
 
     def save_tuning(self, path):

@@ -259,6 +259,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "shortlist_oversample") {
       if (!(value >= 1.0)) throw std::invalid_argument("shortlist_oversample must be >= 1");
       h->shortlist_oversample = value;
+    } else if (nm == "sample_rows") {
+      if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("sample_rows must be in [0, 2^20]");
+      h->sample_rows = value;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -273,6 +276,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     if (nm == "gather_max_fraction") *value = h->gather_max_fraction;
     else if (nm == "tiled_min_batch") *value = h->tiled_min_batch;
     else if (nm == "shortlist_oversample") *value = h->shortlist_oversample;
+    else if (nm == "sample_rows") *value = h->sample_rows;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }
@@ -339,7 +343,7 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
         e.kernel = c;
         e.split = sp;
         plain.push_back(e);
-      } else if (std::sscanf(line, "bf16 %u %u", &b, &c) == 2 && c <= 1) {
+      } else if (std::sscanf(line, "bf16 %u %u", &b, &c) == 2 && c <= (1u << 20)) {
         e.batch = b;
         e.sample = c;
         bf16.push_back(e);

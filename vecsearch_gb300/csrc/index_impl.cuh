@@ -142,13 +142,16 @@ struct vsg_index {
   double tiled_min_batch = 48;
   // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
   double shortlist_oversample = 4;
+  // method "bf16": rows sampled for the starting thresholds (0: no sample pass) when nothing
+  // else is tuned for the batch size; batches under 32 queries skip it.
+  double sample_rows = 16384;
 
   // ---- autotuned schedules (vsg_autotune) ----
   // plain: for unfiltered method "auto" searches of at least `batch` queries (largest such entry),
   // which kernel (0 streaming scan, 1 tiled) and a factor on the number of row splits.
-  // bf16: whether the sampled-threshold pass runs.
+  // bf16: rows the sampled-threshold pass scores (0: none).
   struct TuneEntry {
-    uint32_t batch = 0, kernel = 0, sample = 1;
+    uint32_t batch = 0, kernel = 0, sample = 16384;
     double split = 1.0;
   };
   std::vector<TuneEntry> tune_plain, tune_bf16;
@@ -369,14 +372,16 @@ struct vsg_index {
     a.status = status_word();
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
-    // Batches of 32+ queries first score a sample of at least 16K rows (whole tiles at the head of
-    // every split) and start each query at the k'-th best sampled distance, so the main pass keeps
-    // only rows that can still make the shortlist instead of compacting its buffers again and again.
+    // Batches first score a sample of rows (whole tiles at the head of every split; 16K rows for
+    // 32+ queries unless tuned) and start each query at the k'-th best sampled distance, so the
+    // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
     const TuneEntry* te = lookup(tune_bf16, nq);
-    const bool run_sample = force_sample >= 0 ? force_sample != 0 : te ? te->sample != 0 : nq >= 32;
-    if (run_sample && tiles_per_split > 1) {
-      const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(16384, size_t(a.nsplit) * vsg::kTcRows)));
+    const size_t srows = force_sample >= 0 ? size_t(force_sample)
+                         : te ? size_t(te->sample)
+                         : nq >= 32 ? size_t(sample_rows) : 0;
+    if (srows > 0 && tiles_per_split > 1) {
+      const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
       const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
       sample.reserve(nq * per_query * sizeof(float), 0, stream);
       thr.reserve(nq * sizeof(float), 0, stream);
@@ -458,7 +463,7 @@ struct vsg_index {
         pick.batch = uint32_t(b);
         float best = 1e30f;
         if (family == VSG_METHOD_BF16) {
-          for (int smp : {0, 1}) {
+          for (int smp : {0, 4096, 16384}) {
             force_sample = smp;
             const float t = time_it(b, VSG_METHOD_BF16);
             if (t < best) {

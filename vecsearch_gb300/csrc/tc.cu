@@ -715,14 +715,17 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   }
 }
 
-// One CTA per query: the kp-th smallest of `count` values by radix selection on the order key,
-// 8 bits per round (4 rounds). Ties resolve to the shared value, so the threshold is exact.
+// One CTA per query: an upper bound of the kp-th smallest of `count` values, by radix selection
+// on the order key. A first pass finds the keys' minimum and maximum; two 8-bit rounds then
+// resolve the 16 bits below their highest differing bit (the bits above are shared), so the
+// histograms spread instead of piling into one bin. The result is the largest key of the bucket
+// holding the kp-th smallest: at least kp values lie at or below it, within 2^-16 of the range.
 __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uint32_t count, uint32_t nq,
                                                              const uint32_t* kp_per_query, uint32_t kp_all,
                                                              float* thr, const ServeHeader* hdr,
                                                              const ServeQuery* sq) {
   __shared__ uint32_t hist[256];
-  __shared__ uint32_t sel_prefix, sel_rank;
+  __shared__ uint32_t kmin, kmax, sel_prefix, sel_rank;
   const uint32_t q = blockIdx.x;
   if (hdr) {  // serving mode: the batch shape comes from the header
     nq = hdr->nq;
@@ -731,34 +734,62 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
   if (q >= nq) return;
   const float* v = in + size_t(q) * count;
   const uint32_t kp = sq ? sq[q].kp : kp_per_query ? kp_per_query[q] : kp_all;
+  if (kp > count) {  // fewer than kp values: no bound (+inf keeps everything)
+    if (threadIdx.x == 0) thr[q] = __int_as_float(0x7f800000);
+    return;
+  }
   if (threadIdx.x == 0) {
-    sel_prefix = 0;
+    kmin = 0xFFFFFFFFu;
+    kmax = 0u;
     sel_rank = kp;  // 1-based rank still to find inside the current prefix
   }
-  for (int round = 0; round < 4; ++round) {
-    const int shift = 24 - 8 * round;
-    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
-    __syncthreads();
-    const uint32_t prefix = sel_prefix;
-    const uint32_t hi_mask = round == 0 ? 0u : (0xFFFFFFFFu << (32 - 8 * round));
-    for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
-      const uint32_t key = order_key(v[j]);
-      if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+  __syncthreads();
+  uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+  for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
+    const uint32_t key = order_key(v[j]);
+    lo = min(lo, key);
+    hi = max(hi, key);
+  }
+  lo = __reduce_min_sync(kFull, lo);
+  hi = __reduce_max_sync(kFull, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&kmin, lo);
+    atomicMax(&kmax, hi);
+  }
+  __syncthreads();
+  const uint32_t diff = kmin ^ kmax;
+  const int top = diff ? 31 - __clz(diff) : 0;  // highest differing bit
+  int shift = max(top - 7, 0);
+  // Bits above `top` are the same in every key: they are resolved from the start.
+  uint32_t hi_mask = top == 31 ? 0u : (0xFFFFFFFFu << (top + 1));
+  uint32_t prefix = kmin & hi_mask;
+  if (diff) {
+    for (int round = 0; round < 2; ++round) {
+      for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+      __syncthreads();
+      for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
+        const uint32_t key = order_key(v[j]);
+        if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t r = sel_rank, b = 0;
+        while (b < 255 && hist[b] < r) r -= hist[b++];
+        sel_prefix = prefix | (b << shift);
+        sel_rank = r;
+      }
+      __syncthreads();
+      prefix = sel_prefix;
+      hi_mask |= 0xFFu << shift;  // bits resolved so far
+      if (shift == 0) break;
+      shift = max(shift - 8, 0);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t r = sel_rank, b = 0;
-      while (b < 255 && hist[b] < r) r -= hist[b++];
-      sel_prefix = prefix | (b << shift);
-      sel_rank = r;
-    }
-    __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const uint32_t key = sel_prefix;
-    const uint32_t u = (key & 0x80000000u) ? (key & 0x7FFFFFFFu) : ~key;
-    // Fewer than kp finite values: no bound (+inf keeps everything).
-    thr[q] = kp > count ? __int_as_float(0x7f800000) : __uint_as_float(u);
+    // Upper end of the bucket: every key with this prefix is at most prefix | ~mask. A bucket
+    // reaching past +inf (padding entries) gives no bound.
+    const float t = key_float(diff ? (prefix | ~hi_mask) : kmin);
+    thr[q] = t == t ? t : __int_as_float(0x7f800000);
   }
 }
 

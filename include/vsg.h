@@ -154,12 +154,13 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
  *   method VSG_METHOD_AUTO: streaming scan or tiled kernel, and 1x or 2x the row splits, used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
- *     (0, 4096 or 16384; 0 = no sample pass).
+ *     (0, 4096 or 16384; 0 = no sample pass) and how many CTAs share each row tile through a
+ *     multicast cluster (1, 2 or 4; cluster = 0 in a table means the built-in rule).
  * vsg_autotune_table copies a table out (count: capacity in, entries out; choice = kernel or
- * sampled rows). vsg_autotune_save / _load persist both tables as a small text file. */
+ * sampled rows; cluster: CTAs per cluster of bf16 entries). vsg_autotune_save / _load persist both tables as a small text file. */
 int vsg_autotune(vsg_index* index, const size_t* batches, size_t count, size_t k, uint32_t method);
 int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
-                       double* split);
+                       double* split, uint32_t* cluster);
 int vsg_autotune_save(vsg_index* index, const char* path);
 int vsg_autotune_load(vsg_index* index, const char* path);
 

@@ -107,3 +107,29 @@ def test_bf16_wide_rows_stream_query_chunks(gpu_ready):
     same = (bi == pi).all(1)
     assert same.mean() >= 0.99, same.mean()
     np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))
+
+
+@pytest.mark.parametrize("metric,unit", [("ip", True), ("l2", False)])
+def test_bf16_clusters_share_row_tiles(gpu_ready, metric, unit, tmp_path):
+    # Clusters of 2 and 4 CTAs multicast each row tile; 300 queries make 3 query blocks, so a
+    # cluster of 2 has a padding rank and a cluster of 4 one too. Results equal cluster size 1.
+    vsg = gpu_ready
+    x, q = _data(150_000, 300, 256, 128, unit, 83)
+    gpu = vsg.GpuBruteForceIndex(256, metric)
+    gpu.add(x)
+    base_i, base_d = None, None
+    for cl in (1, 2, 4):
+        for sample in (0, 4096):
+            t = tmp_path / f"t{cl}{sample}.txt"
+            t.write_text(f"vsg-tuning 1 dim 256 rows 150000 metric 0 sms 0\nbf16 1 {sample} {cl}\n")
+            gpu.load_tuning(t)
+            assert gpu.tuning("bf16") == [{"batch": 1, "sample": sample, "cluster": cl}]
+            bi, bd = gpu.search(q, 10, method="bf16")
+            if base_i is None:
+                base_i, base_d = bi, bd
+                pi, pd = gpu.search(q, 10, method="skinny")
+                same = (bi == pi).all(1)
+                assert same.mean() >= 0.99, same.mean()
+            else:
+                np.testing.assert_array_equal(bi, base_i)
+                np.testing.assert_array_equal(bd.view(np.uint32), base_d.view(np.uint32))

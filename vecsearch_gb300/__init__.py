@@ -198,16 +198,20 @@ class GpuBruteForceIndex:
         return self.tuning(method)
 
     def tuning(self, method="auto"):
-        """The tuned table: [{"batch", "kernel" (FP32) or "sample" (bf16: rows sampled, 0 = none), "split"}]."""
+        """The tuned table. FP32: [{"batch", "kernel", "split"}]; bf16: [{"batch", "sample" (rows
+        sampled, 0 = none), "cluster" (CTAs sharing each row tile, 0 = built-in rule)}]."""
         cnt = ctypes.c_size_t(64)
         bt = (ctypes.c_uint32 * 64)()
         ch = (ctypes.c_uint32 * 64)()
         sp = (ctypes.c_double * 64)()
-        _native.check(_native.lib().vsg_autotune_table(self._h, _native.METHODS[method], ctypes.byref(cnt), bt, ch, sp))
-        key = "sample" if method == "bf16" else "kernel"
+        cl = (ctypes.c_uint32 * 64)()
+        _native.check(_native.lib().vsg_autotune_table(self._h, _native.METHODS[method], ctypes.byref(cnt), bt, ch,
+                                                       sp, cl))
+        n = min(cnt.value, 64)
+        if method == "bf16":
+            return [{"batch": bt[i], "sample": int(ch[i]), "cluster": int(cl[i])} for i in range(n)]
         names = {0: "skinny", 1: "tiled"}
-        return [{"batch": bt[i], key: (int(ch[i]) if key == "sample" else names[ch[i]]), "split": sp[i]}
-                for i in range(min(cnt.value, 64))]
+        return [{"batch": bt[i], "kernel": names[ch[i]], "split": sp[i]} for i in range(n)]
 
     def save_tuning(self, path):
         _native.check(_native.lib().vsg_autotune_save(self._h, str(path).encode()))

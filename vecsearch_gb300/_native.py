@@ -46,7 +46,7 @@ SIGNATURES = {
     "vsg_add_hnsw_file": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(_SZ)]),
     "vsg_autotune": (_INT, [_P, ctypes.POINTER(_SZ), _SZ, _SZ, _U32]),
     "vsg_autotune_table": (_INT, [_P, _U32, ctypes.POINTER(_SZ), ctypes.POINTER(_U32), ctypes.POINTER(_U32),
-                                  ctypes.POINTER(ctypes.c_double)]),
+                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_U32)]),
     "vsg_autotune_save": (_INT, [_P, ctypes.c_char_p]),
     "vsg_autotune_load": (_INT, [_P, ctypes.c_char_p]),
     "vsg_server_create": (_INT, [_P, _SZ, _SZ, _SZ, ctypes.POINTER(_P)]),

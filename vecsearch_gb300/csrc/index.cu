@@ -295,7 +295,7 @@ int vsg_autotune(vsg_index* h, const size_t* batches, size_t count, size_t k, ui
 }
 
 int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
-                       double* split) {
+                       double* split, uint32_t* cluster) {
   if (!h || !count) return fail(VSG_ERR_INVALID, "index or count is NULL");
   return guarded([&] {
     std::lock_guard<std::mutex> g(h->mu);
@@ -306,6 +306,7 @@ int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* b
       if (batch) batch[i] = t[i].batch;
       if (choice) choice[i] = method == VSG_METHOD_BF16 ? t[i].sample : t[i].kernel;
       if (split) split[i] = t[i].split;
+      if (cluster) cluster[i] = t[i].cluster;
     }
   });
 }
@@ -318,7 +319,7 @@ int vsg_autotune_save(vsg_index* h, const char* path) {
     if (!f) throw std::runtime_error(std::string("cannot open ") + path);
     std::fprintf(f, "vsg-tuning 1 dim %zu rows %zu metric %u sms %d\n", h->dim, h->n, h->metric, h->sms);
     for (const auto& e : h->tune_plain) std::fprintf(f, "plain %u %u %.3f\n", e.batch, e.kernel, e.split);
-    for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u\n", e.batch, e.sample);
+    for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u %u\n", e.batch, e.sample, e.cluster);
     const bool ok = std::fclose(f) == 0;
     if (!ok) throw std::runtime_error(std::string("write failed: ") + path);
   });
@@ -343,10 +344,15 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
         e.kernel = c;
         e.split = sp;
         plain.push_back(e);
-      } else if (std::sscanf(line, "bf16 %u %u", &b, &c) == 2 && c <= (1u << 20)) {
-        e.batch = b;
-        e.sample = c;
-        bf16.push_back(e);
+      } else if (std::strncmp(line, "bf16 ", 5) == 0) {
+        unsigned cl = 0;
+        const int got = std::sscanf(line, "bf16 %u %u %u", &b, &c, &cl);
+        if (got >= 2 && c <= (1u << 20) && (cl == 0 || cl == 1 || cl == 2 || cl == 4)) {
+          e.batch = b;
+          e.sample = c;
+          e.cluster = cl;
+          bf16.push_back(e);
+        }
       }
     }
     std::fclose(f);

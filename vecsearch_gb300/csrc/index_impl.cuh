@@ -129,6 +129,13 @@ struct vsg_index {
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
   size_t xmap_rows = 0;
+  // Row maps with 64- and 32-row boxes (clusters of 2 and 4 multicast slices of a row chunk).
+  CUtensorMap xmap_slice[2]{};
+  const void* xmap_slice_base[2] = {nullptr, nullptr};
+  size_t xmap_slice_rows[2] = {0, 0};
+  // Clusters of 2 / 4 shortlist CTAs resident at once, by (stages, dp) (0: not known yet).
+  uint32_t max_clusters[2] = {0, 0};
+  uint32_t max_clusters_key = 0;
   PinnedBuffer pin_in, pin_out;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
@@ -152,11 +159,12 @@ struct vsg_index {
   // bf16: rows the sampled-threshold pass scores (0: none).
   struct TuneEntry {
     uint32_t batch = 0, kernel = 0, sample = 16384;
+    uint32_t cluster = 0;  // bf16: CTAs per cluster (0: the default rule)
     double split = 1.0;
   };
   std::vector<TuneEntry> tune_plain, tune_bf16;
   // Overrides used while the tuner times a candidate (-1 / 0 = not forced).
-  int force_kernel = -1, force_sample = -1;
+  int force_kernel = -1, force_sample = -1, force_cluster = -1;
   double force_split = 0.0;
 
   static const TuneEntry* lookup(const std::vector<TuneEntry>& t, size_t nq) {
@@ -257,14 +265,16 @@ struct vsg_index {
   // Splits of a row range for `blocks` CTA columns: at least `min_splits`, rows per split a
   // multiple of `align`, and a total CTA count that fills whole waves of one CTA per SM.
   void choose_splits(size_t blocks, size_t align, size_t min_rows, uint32_t* rows_per_split, uint32_t* nsplit,
-                     double factor = 1.0) const {
-    const size_t s0 = std::max<size_t>(1, size_t(double(std::max<size_t>(1, size_t(sms) / blocks)) * factor));
+                     double factor = 1.0, size_t slots = 0) const {
+    // slots: work items that run at once (one per SM unless given)
+    if (slots == 0) slots = size_t(sms);
+    const size_t s0 = std::max<size_t>(1, size_t(double(std::max<size_t>(1, slots / blocks)) * factor));
     const size_t smax = std::max<size_t>(1, std::min(ceil_div(n, min_rows), 4 * s0));
     size_t best = std::min(s0, smax);
     double best_eff = 0;
     for (size_t sp = std::min(s0, smax); sp <= smax; ++sp) {
       const size_t ctas = blocks * sp;
-      const double eff = double(ctas) / double(ceil_div(ctas, size_t(sms)) * size_t(sms));
+      const double eff = double(ctas) / double(ceil_div(ctas, slots) * slots);
       if (eff > best_eff + 1e-9) {
         best_eff = eff;
         best = sp;
@@ -323,6 +333,30 @@ struct vsg_index {
     }
   }
 
+  const CUtensorMap& slice_map(uint32_t cluster) {
+    const int i = cluster == 2 ? 0 : 1;
+    if (xmap_slice_base[i] != xb.get() || xmap_slice_rows[i] != n) {
+      VSG_CUDA(vsg::tc_encode_map(&xmap_slice[i], xb.get(), n, dp, uint32_t(vsg::kTcRows) / cluster));
+      xmap_slice_base[i] = xb.get();
+      xmap_slice_rows[i] = n;
+    }
+    return xmap_slice[i];
+  }
+
+  // CTAs per cluster for a batch of nqb query blocks: the largest of 4 / 2 / 1 that the batch
+  // fills, unless tuned (0 in the table = this rule), and only if such clusters can be resident.
+  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident) {
+    uint32_t c = tuned ? tuned : nqb >= 4 ? 4u : nqb >= 2 ? 2u : 1u;
+    const uint32_t key = stages * 65536u + uint32_t(dp);
+    if (max_clusters_key != key) {
+      max_clusters[0] = vsg::tc_max_clusters(2, stages, uint32_t(dp), resident, metric == VSG_METRIC_L2);
+      max_clusters[1] = vsg::tc_max_clusters(4, stages, uint32_t(dp), resident, metric == VSG_METRIC_L2);
+      max_clusters_key = key;
+    }
+    while (c > 1 && max_clusters[c == 2 ? 0 : 1] == 0) c /= 2;
+    return c;
+  }
+
   uint32_t shortlist_size(size_t k) const {
     const double want = std::max<double>(double(k), shortlist_oversample * double(k));
     return uint32_t(std::min<double>(double(vsg::kTcMaxShortlist), std::ceil(want)));
@@ -343,13 +377,21 @@ struct vsg_index {
     VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
     ensure_xmap();
     const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
+    const TuneEntry* te = lookup(tune_bf16, nq);
+    // Clusters of C CTAs share each row tile (multicast); items are (group of C query blocks,
+    // split), taken round-robin by the clusters that fit on the GPU at once.
+    const uint32_t C = pick_cluster(nqb, force_cluster >= 0 ? uint32_t(force_cluster) : te ? te->cluster : 0u,
+                                    stages, resident);
+    const size_t nqg = ceil_div(nqb, size_t(C));
+    const size_t slots = C > 1 ? size_t(max_clusters[C == 2 ? 0 : 1]) : size_t(sms);
     vsg::TcArgs a{};
-    choose_splits(nqb, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit);
+    choose_splits(nqg, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
     const size_t parts = nq * a.nsplit * kp;
     part.reserve(parts * 8, 0, stream);
     cand.reserve(nq * kp * 8, 0, stream);
-    // CTAs take (query block, split) items round-robin; one candidate buffer per CTA.
-    const unsigned grid = unsigned(std::min<size_t>(nqb * a.nsplit, size_t(sms)));
+    // One candidate buffer per CTA.
+    const unsigned grid = unsigned(std::min<size_t>(nqg * a.nsplit, slots) * C);
+    const CUtensorMap& rowmap = C > 1 ? slice_map(C) : xmap;
     const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
     gthr.reserve(nq * sizeof(uint32_t), 0, stream);
@@ -358,6 +400,7 @@ struct vsg_index {
     a.dp = uint32_t(dp);
     a.nq = uint32_t(nq);
     a.nqb = uint32_t(nqb);
+    a.cluster = C;
     a.kp = kp;
     a.stages = stages;
     a.resident = resident;
@@ -376,7 +419,6 @@ struct vsg_index {
     // 32+ queries unless tuned) and start each query at the k'-th best sampled distance, so the
     // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
-    const TuneEntry* te = lookup(tune_bf16, nq);
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
                          : nq >= 32 ? size_t(sample_rows) : 0;
@@ -389,12 +431,12 @@ struct vsg_index {
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
       sa.gthr = nullptr;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, sa, grid, s));
+      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, grid, s));
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr, kp,
                                          static_cast<float*>(thr.get()), s));
       a.thr_init = static_cast<const float*>(thr.get());
     }
-    VSG_CUDA(vsg::launch_tc_shortlist(qmap, xmap, a, grid, s));
+    VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     float* cd = static_cast<float*>(cand.get());
     uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
@@ -463,12 +505,17 @@ struct vsg_index {
         pick.batch = uint32_t(b);
         float best = 1e30f;
         if (family == VSG_METHOD_BF16) {
-          for (int smp : {0, 4096, 16384}) {
-            force_sample = smp;
-            const float t = time_it(b, VSG_METHOD_BF16);
-            if (t < best) {
-              best = t;
-              pick.sample = uint32_t(smp);
+          for (int cl : {1, 2, 4}) {
+            if (cl > 1 && ceil_div(b, size_t(vsg::kTcQueries)) < size_t(cl)) continue;
+            for (int smp : {0, 4096, 16384}) {
+              force_sample = smp;
+              force_cluster = cl;
+              const float t = time_it(b, VSG_METHOD_BF16);
+              if (t < best) {
+                best = t;
+                pick.sample = uint32_t(smp);
+                pick.cluster = uint32_t(cl);
+              }
             }
           }
         } else {
@@ -491,6 +538,7 @@ struct vsg_index {
     } catch (...) {
       force_kernel = -1;
       force_sample = -1;
+      force_cluster = -1;
       force_split = 0;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
@@ -498,6 +546,7 @@ struct vsg_index {
     }
     force_kernel = -1;
     force_sample = -1;
+    force_cluster = -1;
     force_split = 0;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

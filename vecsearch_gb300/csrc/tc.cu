@@ -22,6 +22,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "device_common.cuh"
@@ -191,6 +192,22 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// The same copy multicast to the CTAs of `mask` in the cluster: the box lands at the same
+// shared-memory offset in each, and each one's barrier at `bar`'s offset counts its bytes.
+__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                               uint16_t mask, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      ".L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5, %6;" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar)), "h"(mask), "l"(policy)
+      : "memory");
+}
+
+// Every thread of every CTA of the cluster: arrives and waits (release / acquire).
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ uint64_t policy_evict_last() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -211,6 +228,14 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
 
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+// The same arrival on the barrier at `bar`'s offset in every CTA of `mask`.
+__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   smem_addr(bar)),
+               "h"(mask)
                : "memory");
 }
 
@@ -296,16 +321,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t nqb = persistent ? a.hdr->nqb : a.nqb;
   const uint32_t nsplit = persistent ? a.hdr->nsplit : a.nsplit;
   const uint32_t rows_per_split = persistent ? a.hdr->rows_per_split : a.rows_per_split;
-  const uint32_t nitems = persistent ? a.hdr->items : nqb * nsplit;
+  const uint32_t nitems = persistent ? a.hdr->items : ((nqb + max(1u, a.cluster) - 1) / max(1u, a.cluster)) * nsplit;
   const uint32_t nkc = (a.dp + kTcKChunk - 1) / kTcKChunk;
   constexpr uint32_t cap = 32u * E;
+  // Cluster of C CTAs (non-serving launches): rank r takes query block qg * C + r of a group.
+  const uint32_t C = persistent ? 1u : max(1u, a.cluster);
+  const uint32_t rank = blockIdx.x % C, cid = blockIdx.x / C, nclusters = gridDim.x / C;
+  const uint16_t cmask = uint16_t((1u << C) - 1u);
+  const uint32_t slice_rows = kTcRows / C;  // rows of each row chunk this CTA loads for all
+  const uint32_t nqg = (nqb + C - 1) / C;
   __shared__ uint32_t item_slot;
   __shared__ __align__(16) float xs_buf[4][128];  // epilogue warps' row norms of a tile (L2)
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], C);  // one arrival from every CTA's MMAs (the slot is shared)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
@@ -327,6 +358,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  if (C > 1) cluster_sync();  // every CTA's barriers exist before any copy or arrival reaches them
 
   // Ring, accumulator and query-block positions carry over from one item to the next; every
   // role walks the same items and tiles in the same order, so they stay in step.
@@ -341,12 +373,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint64_t keep_policy = policy_evict_last();
 
   for (uint32_t iter = 0;; ++iter) {
-    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : blockIdx.x + iter * gridDim.x;
+    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : cid + iter * nclusters;
     __syncthreads();
     const uint32_t item = item_slot;
     __syncthreads();  // everyone has read the slot before thread 0 may overwrite it
     if (item >= nitems) break;
-    const uint32_t qb = item % nqb, split = item / nqb;
+    const uint32_t qb = (item % nqg) * C + rank, split = item / nqg;
     const uint32_t qbase = qb * kTcQueries;
     const uint32_t row_begin = split * rows_per_split;
     uint32_t row_end = min(a.n, row_begin + rows_per_split);
@@ -380,14 +412,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               break;
             }
             unsigned char* st = ring + size_t(s) * L.slot;
-            if (resident) {
-              mbar_arrive_expect_tx(&full[s], kChunkBytes);
-              tma_load_2d(st, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
-            } else {
-              mbar_arrive_expect_tx(&full[s], 2 * kChunkBytes);
-              tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
-              tma_load_2d(st + kChunkBytes, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
-            }
+            unsigned char* sb = resident ? st : st + kChunkBytes;
+            mbar_arrive_expect_tx(&full[s], resident ? kChunkBytes : 2 * kChunkBytes);
+            if (!resident) tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
+            if (C > 1)  // this CTA's slice of the row chunk, for every CTA of the cluster
+              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, int(kc * kTcKChunk),
+                             y + int(rank * slice_rows), &full[s], cmask, stream_policy);
+            else
+              tma_load_2d(sb, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
             pending |= 1u << s;
             last_ph = (last_ph & ~(1u << s)) | (ph << s);
             if (++s == stages) {
@@ -424,7 +456,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
               tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
-            tc_commit(&empty[s]);  // the slot is free once these MMAs have read it
+            // The slot is free once these MMAs have read it (in every CTA it was multicast to).
+            if (C > 1)
+              tc_commit_mc(&empty[s], cmask);
+            else
+              tc_commit(&empty[s]);
             if (++s == stages) {
               s = 0;
               ph ^= 1;
@@ -622,6 +658,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   tc_fence_before();
   __syncthreads();
+  // No CTA leaves while another may still multicast rows or arrivals into its shared memory.
+  if (C > 1) cluster_sync();
   if (warp == 1) {
     tc_fence_after();
     __syncwarp();
@@ -891,12 +929,13 @@ uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident) {
 
 uint32_t tc_buffer_capacity(uint32_t kp) { return tc_capacity(kp); }
 
-cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp) {
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
+  if (box_rows == 0 || box_rows > uint32_t(kTcRows)) return cudaErrorInvalidValue;
   const cuuint64_t dims[2] = {dp, rows};
   const cuuint64_t strides[1] = {dp * 2};
-  const cuuint32_t box[2] = {uint32_t(kTcKChunk), uint32_t(kTcRows)};
+  const cuuint32_t box[2] = {uint32_t(kTcKChunk), box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -936,10 +975,31 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
     if (tc_smem_bytes(a.stages, a.dp, 1) < need) return cudaErrorInvalidValue;
   }
   if (grid == 0) return cudaSuccess;
+  const uint32_t C = a.hdr ? 1u : std::max(1u, a.cluster);
+  if ((C != 1 && C != 2 && C != 4) || grid % C != 0) return cudaErrorInvalidValue;
   cudaError_t e = tc_prepare(a.stages, a.dp, a.resident);
   if (e != cudaSuccess) return e;
   const size_t smem = tc_smem_bytes(a.stages, a.dp, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
+  if (C > 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kTcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const int ei = cap == 64 ? 0 : cap == 128 ? 1 : 2;
+    void (*fns[2][3])(const CUtensorMap, const CUtensorMap, const TcArgs) = {
+        {tc_shortlist_kernel<2, false>, tc_shortlist_kernel<4, false>, tc_shortlist_kernel<8, false>},
+        {tc_shortlist_kernel<2, true>, tc_shortlist_kernel<4, true>, tc_shortlist_kernel<8, true>}};
+    return cudaLaunchKernelEx(&cfg, fns[a.l2 ? 1 : 0][ei], qmap, xmap, a);
+  }
   if (a.l2) {
     if (cap == 64)
       tc_shortlist_kernel<2, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
@@ -956,6 +1016,29 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
       tc_shortlist_kernel<8, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
   }
   return cudaGetLastError();
+}
+
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_t resident, bool l2) {
+  if (tc_prepare(stages, dp, resident) != cudaSuccess) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cluster * 64);
+  cfg.blockDim = dim3(kTcThreads);
+  cfg.dynamicSmemBytes = tc_smem_bytes(stages, dp, resident);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e = l2 ? cudaOccupancyMaxActiveClusters(&n, tc_shortlist_kernel<4, true>, &cfg)
+                           : cudaOccupancyMaxActiveClusters(&n, tc_shortlist_kernel<4, false>, &cfg);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return uint32_t(n);
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,

@@ -63,6 +63,11 @@ struct TcArgs {
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
   uint32_t nqb;  // query blocks (non-serving launches)
+  // Non-serving launches: CTAs per thread-block cluster (1, 2 or 4). The C CTAs of a cluster take
+  // C consecutive query blocks of one split; each loads 128 / C rows of every row chunk and
+  // multicasts them to all C, so the cluster reads each row tile from L2 once. Needs the row map
+  // encoded with a 64 x (128 / C) box (xmap argument of the launch) and grid % C == 0.
+  uint32_t cluster;
 };
 
 // Serving mode, after the persistent shortlist kernel: per query (one CTA each, CTAs past
@@ -107,9 +112,11 @@ uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident);
 // Candidate-buffer entries per query slot for a shortlist of kp (64, 128 or 256).
 uint32_t tc_buffer_capacity(uint32_t kp);
 
-// Encodes a 2-D bf16 tensor map (rows x dp, row stride dp * 2 bytes) with a 64 x 128 box and
-// 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
-cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp);
+// Encodes a 2-D bf16 tensor map (rows x dp, row stride dp * 2 bytes) with a 64 x box_rows box
+// and 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows = 128);
+// Clusters of `cluster` CTAs of the shortlist kernel that can be resident at once (0 on error).
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_t resident, bool l2);
 
 // Sets the shortlist kernels' shared-memory limit for (stages, dp, resident); launch_tc_shortlist
 // does it too, but a launch being captured into a CUDA graph should find it done.

@@ -54,6 +54,14 @@ extern "C" {
 #define VSG_METHOD_SKINNY 2u
 #define VSG_METHOD_TILED 3u
 #define VSG_METHOD_BF16 4u
+/* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The rerank kernel bounds the
+ * difference between each row's bf16 approximate distance and its FP32 distance (from the bf16
+ * rounding of the query and the rows), and proves that no row outside the shortlist can enter
+ * the top k; queries it cannot prove run again in the streaming scan kernel. Results equal
+ * VSG_METHOD_SKINNY bit for bit. Method AUTO uses it for unfiltered batches of at least
+ * "tc_exact_min_batch" queries with k <= 32, or where the autotuner picked it. Filters and
+ * k > 120 run the FP32 kernels. The call waits once on its stream to count the uncertified. */
+#define VSG_METHOD_TC_EXACT 5u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
 #define VSG_MAX_K 128u       /* GpuBruteForceIndex::kMaxK (gpu_brute_force.h:27) */
@@ -163,6 +171,10 @@ int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_
                        double* split, uint32_t* cluster);
 int vsg_autotune_save(vsg_index* index, const char* path);
 int vsg_autotune_load(vsg_index* index, const char* path);
+
+/* Certified exact path counters since the index was created: queries searched, and queries
+ * that were not certified and ran again in the scan kernel. */
+int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* fallbacks);
 
 /* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
  * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for

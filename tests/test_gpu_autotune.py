@@ -26,7 +26,7 @@ def test_autotune_table_and_results(gpu_ready, tmp_path):
     batches = (1, 16, 100, 300)
     table = idx.autotune(batches, k=10)
     assert [e["batch"] for e in table] == list(batches)
-    assert all(e["kernel"] in ("skinny", "tiled") and e["split"] in (1.0, 2.0) for e in table)
+    assert all(e["kernel"] in ("skinny", "tiled", "tc_exact") and e["split"] in (1.0, 2.0) for e in table)
     for e in table:
         q = D.portable(e["batch"], 96, 1000 + e["batch"])
         ti, td = idx.search(q, 10)  # method auto consults the table

@@ -1,0 +1,93 @@
+"""GPU: the certified exact path (method "tc_exact") equals the streaming scan kernel bit for bit.
+
+The shortlist comes from the BF16 tensor-core pass; the rerank kernel certifies each query with a
+bound on the bf16 rounding error, and uncertified queries run again in the scan kernel. Whatever
+the mix, the result must be the scan kernel's (method "skinny"), ids and distance bits.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _clustered(n, nq, d, clusters, unit, seed):
+    from vecsearch_gb300 import datasets as D
+    x, _ = D.portable_clustered(n, d, clusters, 0.35, seed=seed, centroid_seed=seed + 1, unit=unit)
+    q, _ = D.portable_clustered(nq, d, clusters, 0.35, seed=seed + 2, centroid_seed=seed + 1, unit=unit)
+    return x, q
+
+
+def _same(a, b):
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+
+
+@pytest.mark.parametrize("metric,unit", [("ip", True), ("l2", False)])
+def test_tc_exact_equals_scan(gpu_ready, metric, unit):
+    vsg = gpu_ready
+    x, q = _clustered(120_000, 300, 384, 128, unit, 200)
+    gpu = vsg.GpuBruteForceIndex(384, metric)
+    gpu.add(x)
+    q0, f0 = gpu.tc_exact_stats()
+    _same(gpu.search(q, 10, method="tc_exact"), gpu.search(q, 10, method="skinny"))
+    q1, f1 = gpu.tc_exact_stats()
+    assert q1 - q0 == 300
+    assert f1 - f0 < 300  # the certificate holds for most queries on clustered data
+
+
+def test_tc_exact_falls_back_when_it_cannot_prove(gpu_ready):
+    # Rows 1e-4 apart around a few centres: distances closer than the bf16 error bound, so most
+    # queries are not certified and run in the scan kernel; the results must not change.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    centres = D.portable(50, 64, 210, normalize=True)
+    x = vsg.normalize(np.repeat(centres, 400, axis=0) + 1e-4 * D.portable(20_000, 64, 211))
+    q = vsg.normalize(centres[:40] + 1e-3 * D.portable(40, 64, 212))
+    gpu = vsg.GpuBruteForceIndex(64, "cosine")
+    gpu.add(x)
+    q0, f0 = gpu.tc_exact_stats()
+    _same(gpu.search(q, 10, method="tc_exact"), gpu.search(q, 10, method="skinny"))
+    q1, f1 = gpu.tc_exact_stats()
+    assert q1 - q0 == 40 and f1 - f0 > 0
+
+
+@pytest.mark.parametrize("n,d,nq,k", [(90, 37, 5, 10), (5000, 40, 131, 17), (30_000, 128, 200, 100),
+                                      (300, 200, 1, 120)])
+def test_tc_exact_shapes(gpu_ready, n, d, nq, k):
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x = D.portable(n, d, 220 + n, normalize=True)
+    q = D.portable(nq, d, 230 + n, normalize=True)
+    gpu = vsg.GpuBruteForceIndex(d, "cosine")
+    gpu.add(x)
+    _same(gpu.search(q, k, method="tc_exact"), gpu.search(q, k, method="skinny"))
+
+
+def test_tc_exact_duplicates_tie_to_lower_id(gpu_ready):
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    base = D.portable(3000, 96, 240, normalize=True)
+    x = np.concatenate([base, base[:500], base[:500]])  # exact duplicates at higher ids
+    q = base[:64] * 0.999
+    gpu = vsg.GpuBruteForceIndex(96, "cosine")
+    gpu.add(x)
+    got = gpu.search(q, 10, method="tc_exact")
+    _same(got, gpu.search(q, 10, method="skinny"))
+    assert (got[0][:, 0] == np.arange(64)).all()
+
+
+def test_auto_routes_large_batches(gpu_ready):
+    vsg = gpu_ready
+    x, q = _clustered(60_000, 256, 128, 64, True, 250)
+    gpu = vsg.GpuBruteForceIndex(128, "cosine")
+    gpu.add(x)
+    assert gpu.get_tunable("tc_exact_min_batch") == 128
+    q0, _ = gpu.tc_exact_stats()
+    _same(gpu.search(q, 10), gpu.search(q, 10, method="skinny"))  # auto: 256 >= 128, k <= 32
+    q1, _ = gpu.tc_exact_stats()
+    assert q1 - q0 == 256
+    gpu.search(q[:64], 10)  # below the threshold: FP32 kernels
+    gpu.search(q, 64)  # k > 32: FP32 kernels
+    mask = np.ones(len(x), bool)
+    gpu.search(q, 10, filter=mask)  # filtered: FP32 kernels
+    assert gpu.tc_exact_stats()[0] == q1

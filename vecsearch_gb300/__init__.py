@@ -142,7 +142,7 @@ class GpuBruteForceIndex:
     def search(self, queries, k=10, method="auto", filter=None):
         """Exact top-k (bindings.cpp:165-186); returns (ids[int64, nq x k], dists[float32, nq x k])."""
         if method not in _native.METHODS:
-            raise ValueError("method must be 'auto', 'naive', 'skinny', 'tiled' or 'bf16'")
+            raise ValueError("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16' or 'tc_exact'")
         q = _as_f32(queries)
         if q.ndim == 1:
             q = q.reshape(1, q.shape[0])
@@ -210,7 +210,7 @@ class GpuBruteForceIndex:
         n = min(cnt.value, 64)
         if method == "bf16":
             return [{"batch": bt[i], "sample": int(ch[i]), "cluster": int(cl[i])} for i in range(n)]
-        names = {0: "skinny", 1: "tiled"}
+        names = {0: "skinny", 1: "tiled", 2: "tc_exact"}
         return [{"batch": bt[i], "kernel": names[ch[i]], "split": sp[i]} for i in range(n)]
 
     def save_tuning(self, path):
@@ -218,6 +218,12 @@ class GpuBruteForceIndex:
 
     def load_tuning(self, path):
         _native.check(_native.lib().vsg_autotune_load(self._h, str(path).encode()))
+
+    def tc_exact_stats(self):
+        """(queries searched by the certified exact path, queries it re-ran in the scan kernel)."""
+        q, f = ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(_native.lib().vsg_tc_exact_stats(self._h, ctypes.byref(q), ctypes.byref(f)))
+        return q.value, f.value
 
     def profile(self, enable=True):
         """Start (or stop) recording CUDA-event times of the scan and merge kernels."""

@@ -10,7 +10,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libvsg_gb300.so")
 
 OK, ERR_INVALID, ERR_LENGTH, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_NOMEM, ERR_IO = range(7)
 METRIC_L2, METRIC_IP = 0, 1
-METHODS = {"auto": 0, "naive": 1, "skinny": 2, "tiled": 3, "bf16": 4}
+METHODS = {"auto": 0, "naive": 1, "skinny": 2, "tiled": 3, "bf16": 4, "tc_exact": 5}
 NONE = 0xFFFFFFFF
 MAX_K = 128
 
@@ -44,6 +44,7 @@ SIGNATURES = {
     "vsg_get_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
     "vsg_hnsw_file_info": (_INT, [ctypes.c_char_p, ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.POINTER(_U32)]),
     "vsg_add_hnsw_file": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(_SZ)]),
+    "vsg_tc_exact_stats": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_autotune": (_INT, [_P, ctypes.POINTER(_SZ), _SZ, _SZ, _U32]),
     "vsg_autotune_table": (_INT, [_P, _U32, ctypes.POINTER(_SZ), ctypes.POINTER(_U32), ctypes.POINTER(_U32),
                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_U32)]),

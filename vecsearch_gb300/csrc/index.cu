@@ -50,8 +50,8 @@ int guarded(F&& f) {
 }
 
 void check_method(uint32_t method) {
-  if (method > VSG_METHOD_BF16)
-    throw std::invalid_argument("method must be 'auto', 'naive', 'skinny', 'tiled' or 'bf16'");
+  if (method > VSG_METHOD_TC_EXACT)
+    throw std::invalid_argument("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16' or 'tc_exact'");
 }
 
 void check_k(size_t k) {
@@ -259,6 +259,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "shortlist_oversample") {
       if (!(value >= 1.0)) throw std::invalid_argument("shortlist_oversample must be >= 1");
       h->shortlist_oversample = value;
+    } else if (nm == "tc_exact_min_batch") {
+      if (!(value >= 1.0)) throw std::invalid_argument("tc_exact_min_batch must be >= 1");
+      h->tc_exact_min_batch = value;
     } else if (nm == "sample_rows") {
       if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("sample_rows must be in [0, 2^20]");
       h->sample_rows = value;
@@ -277,6 +280,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "tiled_min_batch") *value = h->tiled_min_batch;
     else if (nm == "shortlist_oversample") *value = h->shortlist_oversample;
     else if (nm == "sample_rows") *value = h->sample_rows;
+    else if (nm == "tc_exact_min_batch") *value = h->tc_exact_min_batch;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }
@@ -339,7 +343,7 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
       double sp = 1.0;
       if (std::strncmp(line, "vsg-tuning 1", 12) == 0) {
         header = true;
-      } else if (std::sscanf(line, "plain %u %u %lf", &b, &c, &sp) == 3 && c <= 1 && sp > 0) {
+      } else if (std::sscanf(line, "plain %u %u %lf", &b, &c, &sp) == 3 && c <= 2 && sp > 0) {
         e.batch = b;
         e.kernel = c;
         e.split = sp;
@@ -360,6 +364,15 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
     std::lock_guard<std::mutex> g(h->mu);
     h->tune_plain = plain;
     h->tune_bf16 = bf16;
+  });
+}
+
+int vsg_tc_exact_stats(vsg_index* h, uint64_t* queries, uint64_t* fallbacks) {
+  if (!h || !queries || !fallbacks) return fail(VSG_ERR_INVALID, "index or output is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    *queries = h->tc_exact_queries;
+    *fallbacks = h->tc_exact_fallbacks;
   });
 }
 

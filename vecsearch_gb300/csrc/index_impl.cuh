@@ -53,6 +53,7 @@ class DeviceBuffer {
   size_t bytes() const { return n_; }
   void reserve(size_t bytes, size_t keep, cudaStream_t s) {
     if (bytes <= n_) return;
+    keep = std::min(keep, n_);  // nothing to keep from a buffer not yet allocated
     void* raw = nullptr;
     VSG_CUDA(cudaMalloc(&raw, bytes));
     cudaError_t e = cudaMemsetAsync(raw, 0, bytes, s);
@@ -124,6 +125,11 @@ struct vsg_index {
   // and kept current by later adds; bf16 query staging; merged shortlist candidates.
   DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
   DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
+  // Certified exact path (method tc_exact): rounding bounds of the bf16 rows, uncertified
+  // queries ([count][ids]), their gathered queries and FP32 results.
+  DeviceBuffer xbound, fails, fq, fout;
+  double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
+  uint64_t tc_exact_queries = 0, tc_exact_fallbacks = 0;
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
@@ -317,9 +323,12 @@ struct vsg_index {
     const size_t keep = xb.bytes() >= cap * dp * 2 ? bf16_rows : 0;
     xb.reserve(cap * dp * 2, keep * dp * 2, stream);
     xnorm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
+    xbound.reserve(16, 0, stream);
+    if (keep == 0) VSG_CUDA(cudaMemsetAsync(xbound.get(), 0, 16, stream));  // every row is converted again
     VSG_CUDA(vsg::launch_to_bf16(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dp),
                                  uint32_t(dp), static_cast<char*>(xb.get()) + keep * dp * 2,
-                                 static_cast<float*>(xnorm.get()) + keep, stream));
+                                 static_cast<float*>(xnorm.get()) + keep, stream,
+                                 static_cast<float*>(xbound.get())));
     VSG_CUDA(cudaStreamSynchronize(stream));
     bf16_rows = n;
   }
@@ -357,14 +366,23 @@ struct vsg_index {
     return c;
   }
 
+  // Certified exact path: a wider shortlist (k' >= 80) leaves a gap the error bound can prove.
+  static uint32_t exact_shortlist_size(size_t k) {
+    return uint32_t(std::min<size_t>(vsg::kTcMaxShortlist, std::max<size_t>(4 * k, 80)));
+  }
+
   uint32_t shortlist_size(size_t k) const {
     const double want = std::max<double>(double(k), shortlist_oversample * double(k));
     return uint32_t(std::min<double>(double(vsg::kTcMaxShortlist), std::ceil(want)));
   }
 
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                    cudaStream_t s) {
-    const uint32_t kp = shortlist_size(k);
+                    cudaStream_t s, bool certify = false) {
+    const uint32_t kp = certify ? exact_shortlist_size(k) : shortlist_size(k);
+    // The bf16 copy, its norms and rounding bounds cover every row before any kernel reads them.
+    ensure_bf16();
+    if (!xb.get() || !xnorm.get() || !xbound.get() || bf16_rows != n)
+      throw std::runtime_error("the bf16 copy of the rows is missing");
     uint32_t resident = 0;
     const uint32_t stages = vsg::tc_pick_stages(uint32_t(dp), smem_optin - 1024, &resident);
     if (stages < 2) throw std::invalid_argument("rows do not fit the tensor-core kernel's shared memory");
@@ -442,10 +460,62 @@ struct vsg_index {
     uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
     vsg::MergeArgs m{a.part_d, a.part_i, cd, ci, uint32_t(nq), a.nsplit, kp};
     VSG_CUDA(vsg::launch_merge(m, s));
-    vsg::RerankArgs r{static_cast<const float*>(x.get()), dq, ci, out_dists, out_ids, uint32_t(dp),
-                      uint32_t(ldq), uint32_t(nq), kp, uint32_t(k), a.l2};
+    vsg::RerankArgs r{};
+    r.x = static_cast<const float*>(x.get());
+    r.q = dq;
+    r.cand = ci;
+    r.out_d = out_dists;
+    r.out_i = out_ids;
+    r.dp = uint32_t(dp);
+    r.ldq = uint32_t(ldq);
+    r.nq = uint32_t(nq);
+    r.kp = kp;
+    r.k = uint32_t(k);
+    r.l2 = a.l2;
+    if (certify) {
+      r.cand_d = cd;
+      r.thr_init = a.thr_init;
+      r.xbound = static_cast<const float*>(xbound.get());
+      r.fail_count = static_cast<uint32_t*>(fails.get());
+      r.fail_list = r.fail_count + 1;
+    }
     VSG_CUDA(vsg::launch_rerank(r, s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
+  }
+
+  // Exact top-k through the shortlist: every query whose result the rerank kernel cannot certify
+  // (see RerankArgs) runs again in the streaming scan kernel, so results equal method skinny bit
+  // for bit. Waits on `s` once to read the number of uncertified queries.
+  void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
+                        cudaStream_t s) {
+    fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
+    VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true);
+    uint32_t nf = 0;
+    VSG_CUDA(cudaMemcpyAsync(&nf, fails.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    VSG_CUDA(cudaStreamSynchronize(s));
+    tc_exact_queries += nq;
+    tc_exact_fallbacks += nf;
+    if (nf == 0) return;
+    if (nf > nq) throw std::runtime_error("certification list overflow");
+    const uint32_t* ids = static_cast<const uint32_t*>(fails.get()) + 1;
+    fq.reserve(size_t(nf) * dp * sizeof(float), 0, stream);
+    fout.reserve(size_t(nf) * k * 8, 0, stream);
+    float* q2 = static_cast<float*>(fq.get());
+    uint32_t* oi = static_cast<uint32_t*>(fout.get());
+    float* od = reinterpret_cast<float*>(oi + size_t(nf) * k);
+    VSG_CUDA(vsg::launch_gather_rows(q2, dq, ldq, uint32_t(dp), ids, nf, s));
+    enqueue(q2, dp, nf, k, nullptr, false, 0, false, oi, od, s, VSG_METHOD_SKINNY);
+    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi, od, uint32_t(k), ids, nf, s));
+  }
+
+  bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask) const {
+    if (dmask || k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
+    if (method == VSG_METHOD_TC_EXACT) return true;
+    if (method != VSG_METHOD_AUTO) return false;
+    if (force_kernel >= 0) return force_kernel == 2;
+    if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
+    return double(nq) >= tc_exact_min_batch && k <= 32;
   }
 
   bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
@@ -519,9 +589,11 @@ struct vsg_index {
             }
           }
         } else {
-          for (int kern : {0, 1}) {
+          for (int kern : {0, 1, 2}) {
             if (kern == 1 && b < 8) continue;  // the tiled kernel's tile is 64 queries at least
+            if (kern == 2 && (b < 8 || k > size_t(vsg::kTcMaxShortlist))) continue;
             for (double f : {1.0, 2.0}) {
+              if (kern == 2 && f != 1.0) continue;  // the shortlist path sizes its own splits
               force_kernel = kern;
               force_split = f;
               const float t = time_it(b, VSG_METHOD_AUTO);
@@ -559,6 +631,10 @@ struct vsg_index {
     // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
     if (method == VSG_METHOD_BF16 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
       enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
+      return;
+    }
+    if (use_tc_exact(method, nq, k, dmask)) {
+      enqueue_tc_exact(dq, ldq, nq, k, out_ids, out_dists, s);
       return;
     }
     if (use_tiled(method, nq, dmask)) {

@@ -668,22 +668,59 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
-// FP32 rows -> bf16 rows of stride dp (columns >= dim are zero); optional squared norms (FP32).
+// FP32 rows -> bf16 rows of stride dp (columns >= dim are zero); optional squared norms (FP32)
+// and, for certification, the rows' largest rounding residual and norms.
 __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim,
-                               uint32_t dp, __nv_bfloat16* __restrict__ dst, float* __restrict__ norms) {
+                               uint32_t dp, __nv_bfloat16* __restrict__ dst, float* __restrict__ norms,
+                               float* __restrict__ bounds) {
   const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
   const float* s = src + row * ld_src;
   __nv_bfloat16* d = dst + row * dp;
-  float acc = 0.f;
+  float acc = 0.f, res = 0.f, accb = 0.f;
   for (uint32_t c = lane; c < dp; c += 32) {
     const float v = c < dim ? s[c] : 0.f;
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
     acc = fmaf(v, v, acc);
-    d[c] = __float2bfloat16_rn(v);
+    const float vb = __bfloat162float(b);
+    const float e = vb - v;  // exact: v and its rounding are within a factor of 2
+    res = fmaf(e, e, res);
+    accb = fmaf(vb, vb, accb);
+    d[c] = b;
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-  if (norms && lane == 0) norms[row] = acc;
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(kFull, acc, o);
+    res += __shfl_xor_sync(kFull, res, o);
+    accb += __shfl_xor_sync(kFull, accb, o);
+  }
+  if (lane == 0) {
+    if (norms) norms[row] = acc;
+    if (bounds) {  // non-negative floats order like their bit patterns
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 0, __float_as_uint(sqrtf(res)));
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 1, __float_as_uint(sqrtf(acc)));
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 2, __float_as_uint(sqrtf(accb)));
+    }
+  }
+}
+
+__global__ void gather_rows_kernel(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
+                                   uint32_t count) {
+  const uint32_t j = blockIdx.x;
+  if (j >= count) return;
+  const float* s = src + size_t(ids[j]) * ld;
+  for (uint32_t c = threadIdx.x; c < dp; c += blockDim.x) dst[size_t(j) * dp + c] = s[c];
+}
+
+__global__ void scatter_results_kernel(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
+                                       uint32_t k, const uint32_t* ids, uint32_t count) {
+  const uint32_t j = blockIdx.x;
+  if (j >= count) return;
+  const size_t o = size_t(ids[j]) * k;
+  for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
+    dst_i[o + c] = src_i[size_t(j) * k + c];
+    dst_d[o + c] = src_d[size_t(j) * k + c];
+  }
 }
 
 template <bool L2>
@@ -719,11 +756,36 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   __shared__ float cd[kMaxK];
   __shared__ uint32_t ci[kMaxK];
   __shared__ __align__(16) float qs[4096];
+  __shared__ float red[3][8];
+  __shared__ float dk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q = blockIdx.x, kp = a.kp, nc = a.dp / 4;
   const bool q_in_smem = a.dp <= 4096;
-  if (q_in_smem)
-    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
+  const bool certify = a.fail_count != nullptr;
+  float q2 = 0.f, qb2 = 0.f, r2 = 0.f;  // |q|^2, |q~|^2, |q~ - q|^2 (certification)
+  for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) {
+    const float v = a.q[size_t(q) * a.ldq + c];
+    if (q_in_smem) qs[c] = v;
+    if (certify) {
+      const float vb = __bfloat162float(__float2bfloat16_rn(v));
+      q2 = fmaf(v, v, q2);
+      qb2 = fmaf(vb, vb, qb2);
+      r2 = fmaf(vb - v, vb - v, r2);
+    }
+  }
+  if (certify) {
+    for (int o = 16; o > 0; o >>= 1) {
+      q2 += __shfl_xor_sync(kFull, q2, o);
+      qb2 += __shfl_xor_sync(kFull, qb2, o);
+      r2 += __shfl_xor_sync(kFull, r2, o);
+    }
+    if (lane == 0) {
+      red[0][warp] = q2;
+      red[1][warp] = qb2;
+      red[2][warp] = r2;
+    }
+  }
+  if (threadIdx.x == 0) dk = __int_as_float(0x7f800000);
   __syncthreads();
   const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.ldq);
   for (uint32_t j = warp; j < kp; j += blockDim.x / 32) {
@@ -746,10 +808,40 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
       a.out_d[size_t(q) * a.k + rank] = dj;
       a.out_i[size_t(q) * a.k + rank] = ij;
     }
+    if (rank + 1 == a.k) dk = dj;  // the k-th FP32 distance
   }
   for (uint32_t j = kp + threadIdx.x; j < a.k; j += blockDim.x) {  // k > kp: pad
     a.out_d[size_t(q) * a.k + j] = __int_as_float(0x7f800000);
     a.out_i[size_t(q) * a.k + j] = kNone;
+  }
+  if (!certify) return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sq2 = 0, sqb2 = 0, sr2 = 0;
+    for (int w = 0; w < int(blockDim.x / 32); ++w) {
+      sq2 += red[0][w];
+      sqb2 += red[1][w];
+      sr2 += red[2][w];
+    }
+    // FP32 sums of d non-negative terms: inflate by (1 + d 2^-23) before use.
+    const double u = 5.9604644775390625e-08, dd = double(a.dp), infl = 1.0 + 2.0 * dd * u;
+    const double qn = sqrt(sq2 * infl), qbn = sqrt(sqb2 * infl), rq = sqrt(sr2 * infl);
+    const double R = double(a.xbound[0]) * infl, N = double(a.xbound[1]) * infl, Nb = double(a.xbound[2]) * infl;
+    // |bf16 score - q.x| <= |q~||x~ - x| + |q~ - q||x| + accumulation (8 d u |q~||x~|);
+    // |FP32 q.x - q.x| <= 2 d u |q||x|.
+    const double e_dot = qbn * R + rq * N + 8.0 * dd * u * qbn * Nb + 2.0 * dd * u * qn * N;
+    double e;
+    if (L2)  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
+      e = 2.0 * e_dot + dd * u * (qn * qn + N * N) + 4.0 * u * (qn * qn + N * N + 2.0 * qbn * Nb) +
+          (dd + 2.0) * u * (qn + N) * (qn + N);
+    else  // the two roundings of 1 - s
+      e = e_dot + 4.0 * u * (1.0 + qn * N);
+    e *= 1.5;  // margin
+    const float last = kp > 0 ? a.cand_d[size_t(q) * kp + kp - 1] : __int_as_float(0x7f800000);
+    const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
+    const double L = double(fminf(last, thr0));
+    const bool ok = isinf(L) || (L - e > double(dk));
+    if (!ok) a.fail_list[atomicAdd(a.fail_count, 1u)] = q;
   }
 }
 
@@ -932,7 +1024,7 @@ uint32_t tc_buffer_capacity(uint32_t kp) { return tc_capacity(kp); }
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
-  if (box_rows == 0 || box_rows > uint32_t(kTcRows)) return cudaErrorInvalidValue;
+  if (box_rows == 0 || box_rows > uint32_t(kTcRows) || !base || rows == 0) return cudaErrorInvalidValue;
   const cuuint64_t dims[2] = {dp, rows};
   const cuuint64_t strides[1] = {dp * 2};
   const cuuint32_t box[2] = {uint32_t(kTcKChunk), box_rows};
@@ -1042,11 +1134,25 @@ uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
-                           float* norms, cudaStream_t stream) {
+                           float* norms, cudaStream_t stream, float* bounds) {
   if (rows == 0) return cudaSuccess;
   const size_t threads = rows * 32;
-  to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp,
-                                                                      static_cast<__nv_bfloat16*>(dst), norms);
+  to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(
+      src, ld_src, rows, dim, dp, static_cast<__nv_bfloat16*>(dst), norms, bounds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
+                               uint32_t count, cudaStream_t stream) {
+  if (count == 0) return cudaSuccess;
+  gather_rows_kernel<<<count, 128, 0, stream>>>(dst, src, ld, dp, ids, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
+                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream) {
+  if (count == 0) return cudaSuccess;
+  scatter_results_kernel<<<count, 128, 0, stream>>>(dst_i, dst_d, src_i, src_d, k, ids, count);
   return cudaGetLastError();
 }
 

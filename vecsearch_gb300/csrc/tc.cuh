@@ -102,7 +102,24 @@ struct RerankArgs {
   uint32_t* out_i;
   uint32_t dp, ldq, nq, kp, k;
   uint32_t l2;
+  // Certification (exact results from the shortlist), when fail_count is set. Every row outside
+  // a query's shortlist has an approximate distance >= L = min(k'-th shortlist entry, sample
+  // threshold); a bound E on |approximate - FP32 distance| (from the bf16 rounding residuals of
+  // query and rows, Cauchy-Schwarz, and accumulation terms) then shows that none of them can
+  // enter the top k when L - E > the k-th FP32 distance found. Queries that fail are listed.
+  const float* cand_d;     // [nq][kp] approximate distances of the merged shortlist, ascending
+  const float* thr_init;   // per-query sample threshold, or nullptr (none)
+  const float* xbound;     // [max |x~ - x|, max |x|, max |x~|] over the rows (x~ = bf16 row)
+  uint32_t* fail_count;    // number of uncertified queries (atomic), or nullptr: no check
+  uint32_t* fail_list;     // their query indices
 };
+
+// Gathers rows ids[0..count) of src (stride ld floats, dp copied) into dst (stride dp).
+cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
+                               uint32_t count, cudaStream_t stream);
+// Scatters result rows j of (src_i, src_d) (k each) to rows ids[j] of (dst_i, dst_d).
+cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
+                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream);
 
 // Shared memory of the shortlist kernel: ring depth, padded dim, resident query block or not.
 size_t tc_smem_bytes(uint32_t stages, uint32_t dp, uint32_t resident);
@@ -125,8 +142,10 @@ cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident);
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
+// When bounds != nullptr, raises bounds[0..3) to the rows' max |x~ - x|, max |x| and max |x~|
+// (x~ = the bf16 row; FP32 sums, not yet inflated for their rounding).
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
-                           float* norms, cudaStream_t stream);
+                           float* norms, cudaStream_t stream, float* bounds = nullptr);
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
 
 }  // namespace vsg

@@ -18,7 +18,9 @@ A step is one exact search of one batch (default batch 1: the HBM-bound case).
              search_batch) on this host's cores, on a bounded sample.
   autotune   the schedule tables vsg_autotune picked for the sweep's batch sizes (taken after
              the headline line; method auto in the sweep follows them).
-  sweep      QPS for the batch sweep 1 .. 4096 (fewer steps each).
+  sweep      QPS for the batch sweep 1 .. 4096 (fewer steps each): method auto (tuned), the two
+             FP32 kernels, the precision form (bf16) and the certified exact path (tc_exact, with
+             the fraction of queries it re-ran in the scan kernel).
 The base (1.536 GB) is larger than L2 (129 MB), so no L2 flush is needed between steps.
 
 --impl reference times the reference's CPU path (oracle port, all host threads) on the
@@ -357,6 +359,13 @@ def run_ours(a):
             row["bf16_tc_tflops"] = round(flops / (tc_t / l_t / 1e3) / 1e12, 1)
             row["bf16_tc_gbs"] = round(a.n * a.dim * 2 / (tc_t / l_t / 1e3) / 1e9, 1)
             row["bf16_rerank_ms"] = round(rr_t / l_t, 4)
+            if b >= 8:  # certified exact tensor-core path: the scan kernel's results, bit for bit
+                q0, s0, f0 = idx.tc_exact_stats()
+                ms_e, _, _, _ = time_device(idx, torch, qd, a, b, sb, 3, stream, method="tc_exact")
+                q1, s1, f1 = idx.tc_exact_stats()
+                row["tc_exact_qps"] = round(b * sb / (ms_e / 1e3), 1)
+                row["tc_exact_second_pass"] = round((s1 - s0) / max(q1 - q0, 1), 4)
+                row["tc_exact_scan_fallback"] = round((f1 - f0) / max(q1 - q0, 1), 4)
             sweep.append(row)
         extra["sweep"] = sweep
 

@@ -57,10 +57,11 @@ extern "C" {
 /* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The rerank kernel bounds the
  * difference between each row's bf16 approximate distance and its FP32 distance (from the bf16
  * rounding of the query and the rows), and proves that no row outside the shortlist can enter
- * the top k; queries it cannot prove run again in the streaming scan kernel. Results equal
+ * the top k; queries it cannot prove run the shortlist pass again with k' = 120, and those it
+ * still cannot prove run in the streaming scan kernel. Results equal
  * VSG_METHOD_SKINNY bit for bit. Method AUTO uses it for unfiltered batches of at least
  * "tc_exact_min_batch" queries with k <= 32, or where the autotuner picked it. Filters and
- * k > 120 run the FP32 kernels. The call waits once on its stream to count the uncertified. */
+ * k > 120 run the FP32 kernels. The call waits on its stream to read the uncertified queries. */
 #define VSG_METHOD_TC_EXACT 5u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
@@ -157,9 +158,10 @@ int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 
 /* Autotuner (new; the reference's tunables are compile-time constants, src/gpu_brute_force.cu:23-31).
- * vsg_autotune times candidate schedules for each batch size (the index's own rows serve as queries;
+ * vsg_autotune times candidate schedules for each batch size (queries 0.9 x_i + 0.1 x_j of rows;
  * CUDA events, median of 3 after a warm-up) and keeps the fastest per batch size:
- *   method VSG_METHOD_AUTO: streaming scan or tiled kernel, and 1x or 2x the row splits, used by
+ *   method VSG_METHOD_AUTO: streaming scan, tiled kernel or certified shortlist (VSG_METHOD_TC_EXACT),
+ *     and 1x or 2x the row splits for the FP32 kernels, used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
  *     (0, 4096 or 16384; 0 = no sample pass) and how many CTAs share each row tile through a
@@ -172,9 +174,9 @@ int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_
 int vsg_autotune_save(vsg_index* index, const char* path);
 int vsg_autotune_load(vsg_index* index, const char* path);
 
-/* Certified exact path counters since the index was created: queries searched, and queries
- * that were not certified and ran again in the scan kernel. */
-int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* fallbacks);
+/* Certified exact path counters since the index was created: queries searched, queries that
+ * needed the second shortlist pass (k' = 120), and queries that ran in the scan kernel. */
+int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* second, uint64_t* fallbacks);
 
 /* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
  * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for

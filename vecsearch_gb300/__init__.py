@@ -220,10 +220,11 @@ class GpuBruteForceIndex:
         _native.check(_native.lib().vsg_autotune_load(self._h, str(path).encode()))
 
     def tc_exact_stats(self):
-        """(queries searched by the certified exact path, queries it re-ran in the scan kernel)."""
-        q, f = ctypes.c_uint64(), ctypes.c_uint64()
-        _native.check(_native.lib().vsg_tc_exact_stats(self._h, ctypes.byref(q), ctypes.byref(f)))
-        return q.value, f.value
+        """(queries searched by the certified exact path, queries that needed its second shortlist
+        pass, queries it ran in the scan kernel) since the index was created."""
+        q, s2, f = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(_native.lib().vsg_tc_exact_stats(self._h, ctypes.byref(q), ctypes.byref(s2), ctypes.byref(f)))
+        return q.value, s2.value, f.value
 
     def profile(self, enable=True):
         """Start (or stop) recording CUDA-event times of the scan and merge kernels."""

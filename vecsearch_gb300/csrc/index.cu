@@ -367,11 +367,12 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
   });
 }
 
-int vsg_tc_exact_stats(vsg_index* h, uint64_t* queries, uint64_t* fallbacks) {
-  if (!h || !queries || !fallbacks) return fail(VSG_ERR_INVALID, "index or output is NULL");
+int vsg_tc_exact_stats(vsg_index* h, uint64_t* queries, uint64_t* second, uint64_t* fallbacks) {
+  if (!h || !queries || !second || !fallbacks) return fail(VSG_ERR_INVALID, "index or output is NULL");
   return guarded([&] {
     std::lock_guard<std::mutex> g(h->mu);
     *queries = h->tc_exact_queries;
+    *second = h->tc_exact_second;
     *fallbacks = h->tc_exact_fallbacks;
   });
 }

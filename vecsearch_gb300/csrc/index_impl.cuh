@@ -127,9 +127,9 @@ struct vsg_index {
   DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
   // Certified exact path (method tc_exact): rounding bounds of the bf16 rows, uncertified
   // queries ([count][ids]), their gathered queries and FP32 results.
-  DeviceBuffer xbound, fails, fq, fout;
+  DeviceBuffer xbound, fails, fids, fq, fout;
   double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
-  uint64_t tc_exact_queries = 0, tc_exact_fallbacks = 0;
+  uint64_t tc_exact_queries = 0, tc_exact_second = 0, tc_exact_fallbacks = 0;
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
@@ -377,8 +377,8 @@ struct vsg_index {
   }
 
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                    cudaStream_t s, bool certify = false) {
-    const uint32_t kp = certify ? exact_shortlist_size(k) : shortlist_size(k);
+                    cudaStream_t s, bool certify = false, uint32_t kp_force = 0) {
+    const uint32_t kp = kp_force ? kp_force : certify ? exact_shortlist_size(k) : shortlist_size(k);
     // The bf16 copy, its norms and rounding bounds cover every row before any kernel reads them.
     ensure_bf16();
     if (!xb.get() || !xnorm.get() || !xbound.get() || bf16_rows != n)
@@ -483,30 +483,66 @@ struct vsg_index {
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
-  // Exact top-k through the shortlist: every query whose result the rerank kernel cannot certify
-  // (see RerankArgs) runs again in the streaming scan kernel, so results equal method skinny bit
-  // for bit. Waits on `s` once to read the number of uncertified queries.
+  // Exact top-k through the shortlist. Queries whose result the rerank kernel cannot certify (see
+  // RerankArgs) run the shortlist pass again with the largest shortlist (k' = 120), and those
+  // still uncertified run in the streaming scan kernel, so results equal method skinny bit for
+  // bit. Waits on `s` after each stage to read the uncertified queries.
   void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                         cudaStream_t s) {
     fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
+    auto read_fails = [&](size_t count) {
+      uint32_t nf = 0;
+      VSG_CUDA(cudaMemcpyAsync(&nf, fails.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      VSG_CUDA(cudaStreamSynchronize(s));
+      if (nf > count) throw std::runtime_error("certification list overflow");
+      std::vector<uint32_t> ids(nf);
+      if (nf) {
+        VSG_CUDA(cudaMemcpyAsync(ids.data(), static_cast<uint32_t*>(fails.get()) + 1, nf * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, s));
+        VSG_CUDA(cudaStreamSynchronize(s));
+      }
+      return ids;
+    };
     VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
     enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true);
-    uint32_t nf = 0;
-    VSG_CUDA(cudaMemcpyAsync(&nf, fails.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    VSG_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> f1 = read_fails(nq);
     tc_exact_queries += nq;
-    tc_exact_fallbacks += nf;
-    if (nf == 0) return;
-    if (nf > nq) throw std::runtime_error("certification list overflow");
-    const uint32_t* ids = static_cast<const uint32_t*>(fails.get()) + 1;
-    fq.reserve(size_t(nf) * dp * sizeof(float), 0, stream);
-    fout.reserve(size_t(nf) * k * 8, 0, stream);
-    float* q2 = static_cast<float*>(fq.get());
-    uint32_t* oi = static_cast<uint32_t*>(fout.get());
-    float* od = reinterpret_cast<float*>(oi + size_t(nf) * k);
-    VSG_CUDA(vsg::launch_gather_rows(q2, dq, ldq, uint32_t(dp), ids, nf, s));
-    enqueue(q2, dp, nf, k, nullptr, false, 0, false, oi, od, s, VSG_METHOD_SKINNY);
-    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi, od, uint32_t(k), ids, nf, s));
+    if (f1.empty()) return;
+    // Stage 2: the uncertified queries, gathered, with k' = 120.
+    const size_t n1 = f1.size();
+    fids.reserve(2 * nq * sizeof(uint32_t), 0, stream);
+    uint32_t* d_f1 = static_cast<uint32_t*>(fids.get());
+    uint32_t* d_f2 = d_f1 + nq;
+    VSG_CUDA(cudaMemcpyAsync(d_f1, f1.data(), n1 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    fq.reserve(2 * n1 * dp * sizeof(float), 0, stream);
+    fout.reserve(2 * n1 * k * 8, 0, stream);
+    float* q1 = static_cast<float*>(fq.get());
+    float* q2 = q1 + n1 * dp;
+    uint32_t* oi1 = static_cast<uint32_t*>(fout.get());
+    float* od1 = reinterpret_cast<float*>(oi1 + n1 * k);
+    uint32_t* oi2 = reinterpret_cast<uint32_t*>(od1 + n1 * k);
+    float* od2 = reinterpret_cast<float*>(oi2 + n1 * k);
+    VSG_CUDA(vsg::launch_gather_rows(q1, dq, ldq, uint32_t(dp), d_f1, uint32_t(n1), s));
+    std::vector<uint32_t> f2;
+    if (exact_shortlist_size(k) < uint32_t(vsg::kTcMaxShortlist)) {
+      VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
+      enqueue_bf16(q1, dp, n1, k, oi1, od1, s, true, uint32_t(vsg::kTcMaxShortlist));
+      f2 = read_fails(n1);
+    } else {
+      f2.resize(n1);
+      for (size_t j = 0; j < n1; ++j) f2[j] = uint32_t(j);
+    }
+    // Stage 3: what is still uncertified, in the scan kernel.
+    if (!f2.empty()) {
+      const size_t n2 = f2.size();
+      VSG_CUDA(cudaMemcpyAsync(d_f2, f2.data(), n2 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+      VSG_CUDA(vsg::launch_gather_rows(q2, q1, dp, uint32_t(dp), d_f2, uint32_t(n2), s));
+      enqueue(q2, dp, n2, k, nullptr, false, 0, false, oi2, od2, s, VSG_METHOD_SKINNY);
+      VSG_CUDA(vsg::launch_scatter_results(oi1, od1, oi2, od2, uint32_t(k), d_f2, uint32_t(n2), s));
+      tc_exact_fallbacks += n2;
+    }
+    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi1, od1, uint32_t(k), d_f1, uint32_t(n1), s));
+    tc_exact_second += n1;
   }
 
   bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask) const {
@@ -527,7 +563,7 @@ struct vsg_index {
     return double(nq) >= tiled_min_batch;
   }
 
-  // Times each candidate schedule for every batch size on the index's own rows as queries and
+  // Times each candidate schedule for every batch size on queries made from the index's rows and
   // keeps the fastest (CUDA events, median of 3 after a warm-up). family: VSG_METHOD_AUTO for the
   // FP32 kernels, VSG_METHOD_BF16 for the shortlist path. Caller holds mu.
   void autotune(const size_t* batches, size_t count, size_t k, uint32_t family) {
@@ -543,9 +579,9 @@ struct vsg_index {
     DeviceBuffer qbuf, obuf;
     qbuf.reserve(bmax * dp * sizeof(float), 0, stream);
     obuf.reserve(bmax * k * 8, 0, stream);
-    for (size_t r = 0; r < bmax; r += n)  // the rows themselves as queries (repeated if needed)
-      VSG_CUDA(cudaMemcpyAsync(static_cast<float*>(qbuf.get()) + r * dp, x.get(),
-                               std::min(n, bmax - r) * dp * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+    // Queries near the index's rows (0.9 x_i + 0.1 x_j; none coincides with a row).
+    VSG_CUDA(vsg::launch_midpoint_rows(static_cast<float*>(qbuf.get()), static_cast<const float*>(x.get()),
+                                       uint32_t(dp), uint32_t(n), uint32_t(bmax), stream));
     cudaEvent_t e0, e1;
     VSG_CUDA(cudaEventCreate(&e0));
     VSG_CUDA(cudaEventCreate(&e1));

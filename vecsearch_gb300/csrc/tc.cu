@@ -704,6 +704,18 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, siz
   }
 }
 
+// Tuning queries: row r is 0.9 x_i + 0.1 x_j for two rows picked by a hash of r: near a row of
+// the index, as a real query near its neighbours is, without coinciding with it.
+__global__ void midpoint_rows_kernel(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count) {
+  const uint32_t r = blockIdx.x;
+  if (r >= count) return;
+  uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t(r) + 1);
+  h ^= h >> 31;
+  const uint32_t i = uint32_t(h % n), j = uint32_t((h >> 32) % n);
+  for (uint32_t c = threadIdx.x; c < dp; c += blockDim.x)
+    dst[size_t(r) * dp + c] = 0.9f * src[size_t(i) * dp + c] + 0.1f * src[size_t(j) * dp + c];
+}
+
 __global__ void gather_rows_kernel(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
                                    uint32_t count) {
   const uint32_t j = blockIdx.x;
@@ -836,7 +848,7 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
           (dd + 2.0) * u * (qn + N) * (qn + N);
     else  // the two roundings of 1 - s
       e = e_dot + 4.0 * u * (1.0 + qn * N);
-    e *= 1.5;  // margin
+    e *= 1.1;  // margin over the (already worst-case) terms
     const float last = kp > 0 ? a.cand_d[size_t(q) * kp + kp - 1] : __int_as_float(0x7f800000);
     const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
     const double L = double(fminf(last, thr0));
@@ -1139,6 +1151,13 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
   const size_t threads = rows * 32;
   to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(
       src, ld_src, rows, dim, dp, static_cast<__nv_bfloat16*>(dst), norms, bounds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
+                                 cudaStream_t stream) {
+  if (count == 0 || n == 0) return cudaSuccess;
+  midpoint_rows_kernel<<<count, 128, 0, stream>>>(dst, src, dp, n, count);
   return cudaGetLastError();
 }
 

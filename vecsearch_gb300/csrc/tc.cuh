@@ -114,6 +114,9 @@ struct RerankArgs {
   uint32_t* fail_list;     // their query indices
 };
 
+// count queries near rows of src (0.9 x_i + 0.1 x_j of its n rows, stride dp), for the autotuner.
+cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
+                                 cudaStream_t stream);
 // Gathers rows ids[0..count) of src (stride ld floats, dp copied) into dst (stride dp).
 cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
                                uint32_t count, cudaStream_t stream);

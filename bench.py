@@ -408,7 +408,7 @@ def run_ours(a):
 
 
 def run_precision(a):
-    """Config 4: BF16 shortlist (k' = 4k and 8k, capped at 120) + exact FP32 rerank vs the plain FP32
+    """Config 4: BF16 and FP8-e4m3 shortlists (k' = 4k and 8k, capped at 120) + exact FP32 rerank vs the FP32
     path, on the 1M x 384 base (1,024 clusters) and, with --big, a 4M x 384 base (4,096 clusters):
     device QPS by batch, recall@k and max |distance error| against the FP64 oracle."""
     import torch
@@ -428,37 +428,38 @@ def run_precision(a):
         qd = torch.from_numpy(q).cuda()
         nchk = 32
         truth = {k: O.fp64_topk(x, q[:nchk], k, "ip") for k in (10, 100)}
-        for k in (10, 100):
-            for over in ((4, 8) if k == 10 else (4,)):  # k = 100: k' is capped at 120 either way
-                idx.set_tunable("shortlist_oversample", over)
-                kp = min(120, over * k)
-                tune = idx.autotune(batches, k, method="bf16")  # sample size per batch for this k'
-                a2 = argparse.Namespace(**vars(a))
-                a2.k = k
-                row = {"n": n, "k": k, "k_prime": kp, "qps": {}, "plain_qps": {},
-                       "sample_rows": {e["batch"]: e["sample"] for e in tune}}
-                for b in batches:
-                    st = max(3, min(100, int(1e5 / b)))
-                    ms, tc_ms, rr_ms, l = time_device(idx, torch, qd, a2, b, st, 3, stream, method="bf16")
-                    row["qps"][b] = round(b * st / (ms / 1e3), 1)
-                    if over == 4 and b >= 8:
-                        stp = max(3, min(50, int(2e4 / b)))
-                        msp, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method="auto")
-                        row["plain_qps"][b] = round(b * stp / (msp / 1e3), 1)
-                ids, dists = idx.search(q[:nchk], k, method="bf16")
-                gi, gd = truth[k]
-                row["recall_vs_fp64"] = vsg.recall_at_k(ids, gi, k)
-                errs = []
-                for i in range(nchk):
-                    ok = ids[i] >= 0
-                    d64 = O.fp64_distances(x, q[i:i + 1], "ip", ids[i][ok])[0]
-                    errs.append(np.max(np.abs(dists[i][ok].astype(np.float64) - d64)))
-                row["max_abs_dist_err_vs_fp64"] = float(max(errs))
-                out.append(row)
-                print(json.dumps(row), flush=True)
+        for dtype in ("bf16", "fp8"):
+            for k in (10, 100):
+                for over in ((4, 8) if k == 10 else (4,)):  # k = 100: k' is capped at 120 either way
+                    idx.set_tunable("shortlist_oversample", over)
+                    kp = min(120, over * k)
+                    tune = idx.autotune(batches, k, method="bf16")  # sample size per batch for this k'
+                    a2 = argparse.Namespace(**vars(a))
+                    a2.k = k
+                    row = {"n": n, "dtype": dtype, "k": k, "k_prime": kp, "qps": {}, "plain_qps": {},
+                           "sample_rows": {e["batch"]: e["sample"] for e in tune}}
+                    for b in batches:
+                        st = max(3, min(100, int(1e5 / b)))
+                        ms, tc_ms, rr_ms, l = time_device(idx, torch, qd, a2, b, st, 3, stream, method=dtype)
+                        row["qps"][b] = round(b * st / (ms / 1e3), 1)
+                        if dtype == "bf16" and over == 4 and b >= 8:
+                            stp = max(3, min(50, int(2e4 / b)))
+                            msp, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method="auto")
+                            row["plain_qps"][b] = round(b * stp / (msp / 1e3), 1)
+                    ids, dists = idx.search(q[:nchk], k, method=dtype)
+                    gi, gd = truth[k]
+                    row["recall_vs_fp64"] = vsg.recall_at_k(ids, gi, k)
+                    errs = []
+                    for i in range(nchk):
+                        ok = ids[i] >= 0
+                        d64 = O.fp64_distances(x, q[i:i + 1], "ip", ids[i][ok])[0]
+                        errs.append(np.max(np.abs(dists[i][ok].astype(np.float64) - d64)))
+                    row["max_abs_dist_err_vs_fp64"] = float(max(errs))
+                    out.append(row)
+                    print(json.dumps(row), flush=True)
         idx.set_tunable("shortlist_oversample", 4)
         del idx
-    print(json.dumps({"metric": "precision form: BF16 shortlist + FP32 rerank QPS by batch", "unit": "queries/s",
+    print(json.dumps({"metric": "precision form: BF16 / FP8 shortlist + FP32 rerank QPS by batch", "unit": "queries/s",
                       "data": "synthetic", "config": {"workload": "1M (and 4M) x 384 unit rows, cosine",
                                                         "batches": batches}, "results": out}), flush=True)
 

@@ -63,6 +63,11 @@ extern "C" {
  * "tc_exact_min_batch" queries with k <= 32, or where the autotuner picked it. Filters and
  * k > 120 run the FP32 kernels. The call waits on its stream to read the uncertified queries. */
 #define VSG_METHOD_TC_EXACT 5u
+/* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
+ * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32
+ * rerank of a shortlist of k' = min(120, max(k, oversample x k)) rows. Filters and k > 120 run
+ * the FP32 kernels. */
+#define VSG_METHOD_FP8 6u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
 #define VSG_MAX_K 128u       /* GpuBruteForceIndex::kMaxK (gpu_brute_force.h:27) */

@@ -133,3 +133,40 @@ def test_bf16_clusters_share_row_tiles(gpu_ready, metric, unit, tmp_path):
             else:
                 np.testing.assert_array_equal(bi, base_i)
                 np.testing.assert_array_equal(bd.view(np.uint32), base_d.view(np.uint32))
+
+
+@pytest.mark.parametrize("metric,unit", [("ip", True), ("l2", False)])
+def test_fp8_shortlist(gpu_ready, metric, unit):
+    # FP8-e4m3 copy with per-row scales: a coarser shortlist (k' = 8k here), the same exact rerank.
+    vsg = gpu_ready
+    x, q = _data(100_000, 300, 384, 256, unit, 90)
+    gpu = vsg.GpuBruteForceIndex(384, metric)
+    gpu.add(x)
+    gpu.set_tunable("shortlist_oversample", 8)
+    pi, pd = gpu.search(q, 10, method="skinny")
+    fi, fd = gpu.search(q, 10, method="fp8")
+    same = (fi == pi).all(1)
+    assert same.mean() >= 0.97, same.mean()
+    np.testing.assert_array_equal(fd[same].view(np.uint32), pd[same].view(np.uint32))
+    gi, _ = O.fp64_topk(x, q, 10, metric)
+    assert vsg.recall_at_k(fi, gi, 10) >= 0.99
+    assert np.all(np.diff(fd, axis=1) >= 0)
+
+
+def test_fp8_odd_shapes(gpu_ready):
+    # dim not a multiple of 16, fewer rows than a tile, k' >= rows (then the shortlist is exact)
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    for n, d, nq, k in ((90, 37, 5, 10), (300, 200, 1, 120), (5000, 40, 131, 17)):
+        x = D.portable(n, d, 70 + n, normalize=True)
+        q = D.portable(nq, d, 80 + n, normalize=True)
+        gpu = vsg.GpuBruteForceIndex(d, "cosine")
+        gpu.add(x)
+        gpu.set_tunable("shortlist_oversample", 8)
+        pi, pd = gpu.search(q, k, method="skinny")
+        fi, fd = gpu.search(q, k, method="fp8")
+        if min(120, 8 * k) >= n:
+            np.testing.assert_array_equal(fi, pi)
+            np.testing.assert_array_equal(fd, pd)
+        else:
+            assert vsg.recall_at_k(fi, pi, k) >= 0.95

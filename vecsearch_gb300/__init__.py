@@ -142,7 +142,7 @@ class GpuBruteForceIndex:
     def search(self, queries, k=10, method="auto", filter=None):
         """Exact top-k (bindings.cpp:165-186); returns (ids[int64, nq x k], dists[float32, nq x k])."""
         if method not in _native.METHODS:
-            raise ValueError("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16' or 'tc_exact'")
+            raise ValueError("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16', 'tc_exact' or 'fp8'")
         q = _as_f32(queries)
         if q.ndim == 1:
             q = q.reshape(1, q.shape[0])

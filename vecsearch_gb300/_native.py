@@ -10,7 +10,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libvsg_gb300.so")
 
 OK, ERR_INVALID, ERR_LENGTH, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_NOMEM, ERR_IO = range(7)
 METRIC_L2, METRIC_IP = 0, 1
-METHODS = {"auto": 0, "naive": 1, "skinny": 2, "tiled": 3, "bf16": 4, "tc_exact": 5}
+METHODS = {"auto": 0, "naive": 1, "skinny": 2, "tiled": 3, "bf16": 4, "tc_exact": 5, "fp8": 6}
 NONE = 0xFFFFFFFF
 MAX_K = 128
 

@@ -50,8 +50,8 @@ int guarded(F&& f) {
 }
 
 void check_method(uint32_t method) {
-  if (method > VSG_METHOD_TC_EXACT)
-    throw std::invalid_argument("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16' or 'tc_exact'");
+  if (method > VSG_METHOD_FP8)
+    throw std::invalid_argument("method must be 'auto', 'naive', 'skinny', 'tiled', 'bf16', 'tc_exact' or 'fp8'");
 }
 
 void check_k(size_t k) {

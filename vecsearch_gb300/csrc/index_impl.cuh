@@ -124,6 +124,13 @@ struct vsg_index {
   // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
   // and kept current by later adds; bf16 query staging; merged shortlist candidates.
   DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
+  // method "fp8": e4m3 copy of the rows (cap x dp8 bytes, dp8 = dim rounded up to 16), one FP32
+  // scale per row, FP32 squared norms; e4m3 query staging and query scales.
+  DeviceBuffer x8, x8scale, x8norm, q8, q8scale;
+  size_t fp8_rows = 0;
+  CUtensorMap xmap8{};
+  const void* xmap8_base = nullptr;
+  size_t xmap8_rows = 0;
   DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
   // Certified exact path (method tc_exact): rounding bounds of the bf16 rows, uncertified
   // queries ([count][ids]), their gathered queries and FP32 results.
@@ -136,9 +143,9 @@ struct vsg_index {
   const void* xmap_base = nullptr;
   size_t xmap_rows = 0;
   // Row maps with 64- and 32-row boxes (clusters of 2 and 4 multicast slices of a row chunk).
-  CUtensorMap xmap_slice[2]{};
-  const void* xmap_slice_base[2] = {nullptr, nullptr};
-  size_t xmap_slice_rows[2] = {0, 0};
+  CUtensorMap xmap_slice[4]{};  // [bf16 / e4m3][cluster 2 / 4]
+  const void* xmap_slice_base[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t xmap_slice_rows[4] = {0, 0, 0, 0};
   // Clusters of 2 / 4 shortlist CTAs resident at once, by (stages, dp) (0: not known yet).
   uint32_t max_clusters[2] = {0, 0};
   uint32_t max_clusters_key = 0;
@@ -333,6 +340,28 @@ struct vsg_index {
     bf16_rows = n;
   }
 
+  size_t dp8() const { return (dim + 15) / 16 * 16; }
+
+  void ensure_fp8() {
+    const size_t d8 = dp8();
+    if (fp8_rows == n && x8.bytes() >= cap * d8) return;
+    const size_t keep = x8.bytes() >= cap * d8 ? fp8_rows : 0;
+    x8.reserve(cap * d8, keep * d8, stream);
+    x8scale.reserve(cap * sizeof(float), keep * sizeof(float), stream);
+    x8norm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
+    VSG_CUDA(vsg::launch_to_fp8(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dim),
+                                uint32_t(d8), static_cast<char*>(x8.get()) + keep * d8,
+                                static_cast<float*>(x8scale.get()) + keep, static_cast<float*>(x8norm.get()) + keep,
+                                stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    fp8_rows = n;
+    if (xmap8_base != x8.get() || xmap8_rows != n) {
+      VSG_CUDA(vsg::tc_encode_map(&xmap8, x8.get(), n, d8, 128, true));
+      xmap8_base = x8.get();
+      xmap8_rows = n;
+    }
+  }
+
   // Tensor map of the bf16 rows (re-encoded after a grow or an add).
   void ensure_xmap() {
     if (xmap_base != xb.get() || xmap_rows != n) {
@@ -342,11 +371,12 @@ struct vsg_index {
     }
   }
 
-  const CUtensorMap& slice_map(uint32_t cluster) {
-    const int i = cluster == 2 ? 0 : 1;
-    if (xmap_slice_base[i] != xb.get() || xmap_slice_rows[i] != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap_slice[i], xb.get(), n, dp, uint32_t(vsg::kTcRows) / cluster));
-      xmap_slice_base[i] = xb.get();
+  const CUtensorMap& slice_map(uint32_t cluster, bool f8) {
+    const int i = (cluster == 2 ? 0 : 1) + (f8 ? 2 : 0);
+    const void* base = f8 ? x8.get() : xb.get();
+    if (xmap_slice_base[i] != base || xmap_slice_rows[i] != n) {
+      VSG_CUDA(vsg::tc_encode_map(&xmap_slice[i], base, n, f8 ? dp8() : dp, uint32_t(vsg::kTcRows) / cluster, f8));
+      xmap_slice_base[i] = base;
       xmap_slice_rows[i] = n;
     }
     return xmap_slice[i];
@@ -354,12 +384,12 @@ struct vsg_index {
 
   // CTAs per cluster for a batch of nqb query blocks: the largest of 4 / 2 / 1 that the batch
   // fills, unless tuned (0 in the table = this rule), and only if such clusters can be resident.
-  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident) {
+  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident, uint32_t nkc) {
     uint32_t c = tuned ? tuned : nqb >= 4 ? 4u : nqb >= 2 ? 2u : 1u;
-    const uint32_t key = stages * 65536u + uint32_t(dp);
+    const uint32_t key = stages * 65536u + nkc * 2u + resident;
     if (max_clusters_key != key) {
-      max_clusters[0] = vsg::tc_max_clusters(2, stages, uint32_t(dp), resident, metric == VSG_METRIC_L2);
-      max_clusters[1] = vsg::tc_max_clusters(4, stages, uint32_t(dp), resident, metric == VSG_METRIC_L2);
+      max_clusters[0] = vsg::tc_max_clusters(2, stages, nkc, resident, metric == VSG_METRIC_L2);
+      max_clusters[1] = vsg::tc_max_clusters(4, stages, nkc, resident, metric == VSG_METRIC_L2);
       max_clusters_key = key;
     }
     while (c > 1 && max_clusters[c == 2 ? 0 : 1] == 0) c /= 2;
@@ -376,30 +406,48 @@ struct vsg_index {
     return uint32_t(std::min<double>(double(vsg::kTcMaxShortlist), std::ceil(want)));
   }
 
+  // The shortlist path over the bf16 copy (f8 = false) or the e4m3 copy with row scales (f8).
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                    cudaStream_t s, bool certify = false, uint32_t kp_force = 0) {
+                    cudaStream_t s, bool certify = false, uint32_t kp_force = 0, bool f8 = false) {
     const uint32_t kp = kp_force ? kp_force : certify ? exact_shortlist_size(k) : shortlist_size(k);
-    // The bf16 copy, its norms and rounding bounds cover every row before any kernel reads them.
-    ensure_bf16();
-    if (!xb.get() || !xnorm.get() || !xbound.get() || bf16_rows != n)
-      throw std::runtime_error("the bf16 copy of the rows is missing");
+    // The operand copy, its norms (and rounding bounds or scales) cover every row before any
+    // kernel reads them.
+    if (f8) {
+      ensure_fp8();
+      if (!x8.get() || !x8scale.get() || !x8norm.get() || fp8_rows != n)
+        throw std::runtime_error("the e4m3 copy of the rows is missing");
+    } else {
+      ensure_bf16();
+      if (!xb.get() || !xnorm.get() || !xbound.get() || bf16_rows != n)
+        throw std::runtime_error("the bf16 copy of the rows is missing");
+    }
+    const size_t dpo = f8 ? dp8() : dp;  // padded elements per row of the operand copies
+    const uint32_t nkc = vsg::tc_chunks(uint32_t(dpo), f8);
     uint32_t resident = 0;
-    const uint32_t stages = vsg::tc_pick_stages(uint32_t(dp), smem_optin - 1024, &resident);
+    const uint32_t stages = vsg::tc_pick_stages(nkc, smem_optin - 1024, &resident);
     if (stages < 2) throw std::invalid_argument("rows do not fit the tensor-core kernel's shared memory");
-    // Queries to bf16 (rows past nq are zero-filled by the copy engine) and their norms.
-    qb.reserve(nq * dp * 2, 0, stream);
+    // Queries to bf16 / e4m3 (rows past nq are zero-filled by the copy engine) and their norms.
     qnorm.reserve(nq * sizeof(float), 0, stream);
-    VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
-                                 static_cast<float*>(qnorm.get()), s));
     CUtensorMap qmap;
-    VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
-    ensure_xmap();
+    if (f8) {
+      q8.reserve(nq * dpo, 0, stream);
+      q8scale.reserve(nq * sizeof(float), 0, stream);
+      VSG_CUDA(vsg::launch_to_fp8(dq, ldq, nq, uint32_t(dim), uint32_t(dpo), q8.get(),
+                                  static_cast<float*>(q8scale.get()), static_cast<float*>(qnorm.get()), s));
+      VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, 128, true));
+    } else {
+      qb.reserve(nq * dp * 2, 0, stream);
+      VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
+                                   static_cast<float*>(qnorm.get()), s));
+      VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
+      ensure_xmap();
+    }
     const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
     const TuneEntry* te = lookup(tune_bf16, nq);
     // Clusters of C CTAs share each row tile (multicast); items are (group of C query blocks,
     // split), taken round-robin by the clusters that fit on the GPU at once.
     const uint32_t C = pick_cluster(nqb, force_cluster >= 0 ? uint32_t(force_cluster) : te ? te->cluster : 0u,
-                                    stages, resident);
+                                    stages, resident, nkc);
     const size_t nqg = ceil_div(nqb, size_t(C));
     const size_t slots = C > 1 ? size_t(max_clusters[C == 2 ? 0 : 1]) : size_t(sms);
     vsg::TcArgs a{};
@@ -409,15 +457,18 @@ struct vsg_index {
     cand.reserve(nq * kp * 8, 0, stream);
     // One candidate buffer per CTA.
     const unsigned grid = unsigned(std::min<size_t>(nqg * a.nsplit, slots) * C);
-    const CUtensorMap& rowmap = C > 1 ? slice_map(C) : xmap;
+    const CUtensorMap& rowmap = C > 1 ? slice_map(C, f8) : f8 ? xmap8 : xmap;
     const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
     gthr.reserve(nq * sizeof(uint32_t), 0, stream);
     VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
     a.n = uint32_t(n);
-    a.dp = uint32_t(dp);
+    a.dp = uint32_t(dpo);
     a.nq = uint32_t(nq);
     a.nqb = uint32_t(nqb);
+    a.fp8 = f8 ? 1u : 0u;
+    a.xscale = f8 ? static_cast<const float*>(x8scale.get()) : nullptr;
+    a.qscale = f8 ? static_cast<const float*>(q8scale.get()) : nullptr;
     a.cluster = C;
     a.kp = kp;
     a.stages = stages;
@@ -426,7 +477,7 @@ struct vsg_index {
     a.cbuf_i = reinterpret_cast<uint32_t*>(static_cast<char*>(cbuf.get()) + cbuf_entries * 4);
     a.gthr = static_cast<uint32_t*>(gthr.get());
     a.l2 = metric == VSG_METRIC_L2 ? 1u : 0u;
-    a.xnorm = static_cast<const float*>(xnorm.get());
+    a.xnorm = static_cast<const float*>(f8 ? x8norm.get() : xnorm.get());
     a.qnorm = static_cast<const float*>(qnorm.get());
     a.part_d = static_cast<float*>(part.get());
     a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
@@ -472,7 +523,7 @@ struct vsg_index {
     r.kp = kp;
     r.k = uint32_t(k);
     r.l2 = a.l2;
-    if (certify) {
+    if (certify && !f8) {
       r.cand_d = cd;
       r.thr_init = a.thr_init;
       r.xbound = static_cast<const float*>(xbound.get());
@@ -667,6 +718,10 @@ struct vsg_index {
     // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
     if (method == VSG_METHOD_BF16 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
       enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
+      return;
+    }
+    if (method == VSG_METHOD_FP8 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
+      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, false, 0, true);
       return;
     }
     if (use_tc_exact(method, nq, k, dmask)) {

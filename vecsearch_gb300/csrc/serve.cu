@@ -132,7 +132,7 @@ struct vsg_server {
     a.sq = sq;
     vsg::ServeFinishArgs f{hdr, sq, a.part_d, a.part_i, static_cast<const float*>(idx->x.get()), dq, out_d, out_i,
                            uint32_t(idx->dp), uint32_t(kp_max), a.l2};
-    VSG_CUDA(vsg::tc_prepare(a.stages, a.dp, a.resident));  // kernel attributes are set before capture
+    VSG_CUDA(vsg::tc_prepare(a.stages, vsg::tc_chunks(a.dp, false), a.resident));  // attributes set before capture
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
                                  static_cast<float*>(s.d_qn.get()), s.stream));
@@ -363,7 +363,7 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     s->max_k = max_k;
     s->kp_max = std::min<size_t>(vsg::kTcMaxShortlist, size_t(std::ceil(std::max<double>(
                                                            double(max_k), h->shortlist_oversample * double(max_k)))));
-    s->stages = vsg::tc_pick_stages(uint32_t(h->dp), h->smem_optin - 1024, &s->resident);
+    s->stages = vsg::tc_pick_stages(vsg::tc_chunks(uint32_t(h->dp), false), h->smem_optin - 1024, &s->resident);
     if (s->stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
     s->mwords = ceil_div(h->n, 32);
     s->off_sq = 256;

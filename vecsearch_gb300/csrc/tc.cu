@@ -21,6 +21,7 @@
 //   scan kernel's results bit for bit; then the top-k by (dist, id).
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <mutex>
@@ -49,8 +50,7 @@ struct TcLayout {
   size_t a, ring, slot, bars, total;  // offsets from the 1024-aligned base; slot = bytes per slot
 };
 
-__host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t dp, bool resident) {
-  const uint32_t nkc = (dp + kTcKChunk - 1) / kTcKChunk;
+__host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t nkc, bool resident) {
   TcLayout L;
   L.a = 0;
   L.slot = resident ? kChunkBytes : 2 * kChunkBytes;
@@ -226,6 +226,19 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
       : "memory");
 }
 
+// Instruction descriptor, kind::f8f6f4: D FP32 (bits 4-5 = 1), A and B E4M3 (type 0 at bits 7-9
+// and 10-12), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28. K = 32 per instruction.
+constexpr uint32_t kIdescF8 = (1u << 4) | (uint32_t(kTcRows >> 3) << 17) | (uint32_t(kTcQueries >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdescF8), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
                : "memory");
@@ -293,7 +306,7 @@ __device__ __forceinline__ void tmem_wait64(uint32_t (&v)[64]) {
                : "memory");
 }
 
-template <int E, bool L2>
+template <int E, bool L2, bool F8>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_shortlist_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap xmap,
                         const TcArgs a) {
@@ -303,7 +316,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   unsigned char* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
   const uint32_t stages = a.stages;
   const bool resident = a.resident != 0;
-  const TcLayout L = tc_layout(stages, a.dp, resident);
+  // A 128-byte chunk of a row holds 64 bf16 or 128 e4m3 elements.
+  constexpr uint32_t kChunkElems = F8 ? 128u : uint32_t(kTcKChunk);
+  const uint32_t nkc = (a.dp + kChunkElems - 1) / kChunkElems;
+  const TcLayout L = tc_layout(stages, nkc, resident);
   unsigned char* qres = smem + L.a;    // resident query block: chunk kc at kc * kChunkBytes
   unsigned char* ring = smem + L.ring;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars);
@@ -322,7 +338,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t nsplit = persistent ? a.hdr->nsplit : a.nsplit;
   const uint32_t rows_per_split = persistent ? a.hdr->rows_per_split : a.rows_per_split;
   const uint32_t nitems = persistent ? a.hdr->items : ((nqb + max(1u, a.cluster) - 1) / max(1u, a.cluster)) * nsplit;
-  const uint32_t nkc = (a.dp + kTcKChunk - 1) / kTcKChunk;
   constexpr uint32_t cap = 32u * E;
   // Cluster of C CTAs (non-serving launches): rank r takes query block qg * C + r of a group.
   const uint32_t C = persistent ? 1u : max(1u, a.cluster);
@@ -332,6 +347,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t nqg = (nqb + C - 1) / C;
   __shared__ uint32_t item_slot;
   __shared__ __align__(16) float xs_buf[4][128];  // epilogue warps' row norms of a tile (L2)
+  __shared__ __align__(16) float xsc_buf[4][F8 ? 128 : 1];  // ... and row scales (e4m3 copies)
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -398,7 +414,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           } else {
             mbar_arrive_expect_tx(afull, nkc * kChunkBytes);
             for (uint32_t kc = 0; kc < nkc; ++kc)
-              tma_load_2d(qres + size_t(kc) * kChunkBytes, &qmap, int(kc * kTcKChunk), int(qbase), afull,
+              tma_load_2d(qres + size_t(kc) * kChunkBytes, &qmap, int(kc * kChunkElems), int(qbase), afull,
                           keep_policy);
             a_pending = true;
             a_last = aph;
@@ -414,12 +430,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             unsigned char* st = ring + size_t(s) * L.slot;
             unsigned char* sb = resident ? st : st + kChunkBytes;
             mbar_arrive_expect_tx(&full[s], resident ? kChunkBytes : 2 * kChunkBytes);
-            if (!resident) tma_load_2d(st, &qmap, int(kc * kTcKChunk), int(qbase), &full[s], keep_policy);
+            if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
             if (C > 1)  // this CTA's slice of the row chunk, for every CTA of the cluster
-              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, int(kc * kTcKChunk),
+              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, int(kc * kChunkElems),
                              y + int(rank * slice_rows), &full[s], cmask, stream_policy);
             else
-              tma_load_2d(sb, &xmap, int(kc * kTcKChunk), y, &full[s], stream_policy);
+              tma_load_2d(sb, &xmap, int(kc * kChunkElems), y, &full[s], stream_policy);
             pending |= 1u << s;
             last_ph = (last_ph & ~(1u << s)) | (ph << s);
             if (++s == stages) {
@@ -454,8 +470,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t sa = resident ? smem_addr(qres + size_t(kc) * kChunkBytes) : slot;
             const uint32_t sb = resident ? slot : slot + kChunkBytes;
 #pragma unroll
-            for (uint32_t kk = 0; kk < kTcKChunk / 16; ++kk)
-              tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
+            for (uint32_t kk = 0; kk < 4; ++kk) {  // 32 bytes of K per instruction
+              if constexpr (F8)
+                tc_mma_f8(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
+              else
+                tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
+            }
             // The slot is free once these MMAs have read it (in every CTA it was multicast to).
             if (C > 1)
               tc_commit_mc(&empty[s], cmask);
@@ -482,6 +502,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
       const uint32_t* qmask = (persistent && qvalid) ? a.sq[qg].mask : nullptr;
       const float qn = (L2 && qvalid) ? a.qnorm[qg] : 0.f;
+      const float qsc = (F8 && qvalid) ? a.qscale[qg] : 1.f;  // e4m3 copies: the query's scale
       float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers
       uint32_t* wi = a.cbuf_i + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;
       uint32_t* gq = (a.gthr && qvalid && !a.dump) ? a.gthr + qg : nullptr;
@@ -561,7 +582,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
                 const uint32_t row = c0 + uint32_t(j);
-                const float sc = __uint_as_float(v[j]);
+                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * __ldg(a.xscale + min(row, a.n - 1)))
+                                    : __uint_as_float(v[j]);
                 const float dist = L2 ? l2_approx(qn, __ldg(a.xnorm + min(row, a.n - 1)), sc) : 1.f - sc;
                 dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
               }
@@ -573,11 +595,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           // append) and one vote per half; the per-score path runs only when some lane may have
           // a candidate.
           float* xs = xs_buf[quarter];
+          float* xsc = xsc_buf[quarter];
           if constexpr (L2) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) xs[c * 32 + lane] = __ldg(a.xnorm + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
-            __syncwarp();
           }
+          if constexpr (F8) {  // the rows' scales (shared by the warp; each lane applies its query's)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xsc[c * 32 + lane] = __ldg(a.xscale + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
+          }
+          if (L2 || F8) __syncwarp();
 #pragma unroll 1
           for (int h = 0; h < 2; ++h) {
             uint32_t v[64];
@@ -592,7 +619,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               uint32_t m[4] = {0u, 0u, 0u, 0u};  // four interleaved chains
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
-                const float sc = __uint_as_float(v[c * 32 + j]);
+                const float sc = F8 ? __uint_as_float(v[c * 32 + j]) * (qsc * xsc[cg * 32 + j])
+                                    : __uint_as_float(v[c * 32 + j]);
                 const bool p = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) <= thr_d : sc >= s_lo;
                 m[j & 3] |= p ? (1u << j) : 0u;
               }
@@ -611,7 +639,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 while (cols) {
                   const int j = __ffs(cols) - 1;
                   cols &= cols - 1;
-                  const float sc = __uint_as_float(tmem_ld1(tbase + uint32_t(cg * 32 + j)));
+                  const float raw = __uint_as_float(tmem_ld1(tbase + uint32_t(cg * 32 + j)));
+                  const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
                   if ((bits[c] >> j) & 1u) {
                     const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
                     if (nb_less(dist, c0 + uint32_t(j), thr_d, thr_i)) {
@@ -624,7 +653,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               }
             }
           }
-          if (L2) __syncwarp();  // the next tile rewrites xs
+          if (L2 || F8) __syncwarp();  // the next tile rewrites xs / xsc
         }
         tc_fence_before();
         __syncwarp();
@@ -701,6 +730,35 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, siz
       atomicMax(reinterpret_cast<unsigned*>(bounds) + 1, __float_as_uint(sqrtf(acc)));
       atomicMax(reinterpret_cast<unsigned*>(bounds) + 2, __float_as_uint(sqrtf(accb)));
     }
+  }
+}
+
+// FP32 rows -> e4m3 rows of stride dp8 bytes (columns >= dim are zero), one FP32 scale per row
+// (max |x| / 448, the largest finite e4m3; 1 for a zero row) and optional squared FP32 norms.
+__global__ void to_fp8_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8,
+                              uint8_t* __restrict__ dst, float* __restrict__ scale, float* __restrict__ norms) {
+  const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const float* s = src + row * ld_src;
+  float mx = 0.f, acc = 0.f;
+  for (uint32_t c = lane; c < dim; c += 32) {
+    const float v = s[c];
+    mx = fmaxf(mx, fabsf(v));
+    acc = fmaf(v, v, acc);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    acc += __shfl_xor_sync(kFull, acc, o);
+  }
+  const float sc = mx > 0.f ? mx / 448.f : 1.f;
+  const float inv = 1.f / sc;
+  uint8_t* d = dst + row * dp8;
+  for (uint32_t c = lane; c < dp8; c += 32)
+    d[c] = c < dim ? uint8_t(__nv_cvt_float_to_fp8(s[c] * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+  if (lane == 0) {
+    scale[row] = sc;
+    if (norms) norms[row] = acc;
   }
 }
 
@@ -1012,44 +1070,56 @@ EncodeTiledFn encode_fn() {
 
 }  // namespace
 
-size_t tc_smem_bytes(uint32_t stages, uint32_t dp, uint32_t resident) {
-  return tc_layout(stages, dp, resident != 0).total + 1024;
+uint32_t tc_chunks(uint32_t dp, bool fp8) { return (dp + (fp8 ? 127u : 63u)) / (fp8 ? 128u : 64u); }
+
+size_t tc_smem_bytes(uint32_t stages, uint32_t nkc, uint32_t resident) {
+  return tc_layout(stages, nkc, resident != 0).total + 1024;
 }
 
-uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident) {
-  // The kernel's static shared memory (work slot, row norms: 2,064 bytes) comes on top.
-  constexpr size_t kStatic = 3072;
+uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident) {
+  // The kernel's static shared memory (work slot, row norms and scales: 4,112 bytes) comes on top.
+  constexpr size_t kStatic = 5120;
   budget = budget > kStatic ? budget - kStatic : 0;
   for (uint32_t s = kMaxTcStages; s >= 4; --s)
-    if (tc_smem_bytes(s, dp, 1) <= budget) {
+    if (tc_smem_bytes(s, nkc, 1) <= budget) {
       *resident = 1;
       return s;
     }
   *resident = 0;
   for (uint32_t s = 6; s >= 2; --s)
-    if (tc_smem_bytes(s, dp, 0) <= budget) return s;
+    if (tc_smem_bytes(s, nkc, 0) <= budget) return s;
   return 0;
 }
 
 uint32_t tc_buffer_capacity(uint32_t kp) { return tc_capacity(kp); }
 
-cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows) {
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows,
+                          bool fp8) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
   if (box_rows == 0 || box_rows > uint32_t(kTcRows) || !base || rows == 0) return cudaErrorInvalidValue;
   const cuuint64_t dims[2] = {dp, rows};
-  const cuuint64_t strides[1] = {dp * 2};
-  const cuuint32_t box[2] = {uint32_t(kTcKChunk), box_rows};
+  const cuuint64_t strides[1] = {dp * (fp8 ? 1 : 2)};  // a multiple of 16 bytes
+  const cuuint32_t box[2] = {fp8 ? 128u : uint32_t(kTcKChunk), box_rows};
   const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+  const CUresult r = fn(map, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                        const_cast<void*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident) {
-  if (stages < 2 || stages > uint32_t(kMaxTcStages) || dp == 0) return cudaErrorInvalidValue;
-  const size_t smem = tc_smem_bytes(stages, dp, resident);
+// Every instantiation of the shortlist kernel: [fp8][l2][E = 2, 4, 8].
+using TcKernel = void (*)(const CUtensorMap, const CUtensorMap, const TcArgs);
+const TcKernel kTcKernels[2][2][3] = {
+    {{tc_shortlist_kernel<2, false, false>, tc_shortlist_kernel<4, false, false>, tc_shortlist_kernel<8, false, false>},
+     {tc_shortlist_kernel<2, true, false>, tc_shortlist_kernel<4, true, false>, tc_shortlist_kernel<8, true, false>}},
+    {{tc_shortlist_kernel<2, false, true>, tc_shortlist_kernel<4, false, true>, tc_shortlist_kernel<8, false, true>},
+     {tc_shortlist_kernel<2, true, true>, tc_shortlist_kernel<4, true, true>, tc_shortlist_kernel<8, true, true>}}};
+
+cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident) {
+  if (stages < 2 || stages > uint32_t(kMaxTcStages) || nkc == 0) return cudaErrorInvalidValue;
+  const size_t smem = tc_smem_bytes(stages, nkc, resident);
   static std::mutex mu;
   static size_t configured[64] = {};
   int dev = 0;
@@ -1057,14 +1127,12 @@ cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident) {
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> g(mu);
   if (dev >= 64 || smem > configured[dev]) {
-    const void* fns[] = {reinterpret_cast<const void*>(tc_shortlist_kernel<2, false>),
-                         reinterpret_cast<const void*>(tc_shortlist_kernel<4, false>),
-                         reinterpret_cast<const void*>(tc_shortlist_kernel<8, false>),
-                         reinterpret_cast<const void*>(tc_shortlist_kernel<2, true>),
-                         reinterpret_cast<const void*>(tc_shortlist_kernel<4, true>),
-                         reinterpret_cast<const void*>(tc_shortlist_kernel<8, true>)};
-    for (const void* f : fns)
-      if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    for (const auto& by_l2 : kTcKernels)
+      for (const auto& by_e : by_l2)
+        for (TcKernel f : by_e)
+          if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(reinterpret_cast<const void*>(f), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(smem));
     if (e != cudaSuccess) return e;
     if (dev < 64) configured[dev] = smem;
   }
@@ -1074,17 +1142,19 @@ cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident) {
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream) {
   if (a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist) || !a.cbuf_d || !a.cbuf_i) return cudaErrorInvalidValue;
+  if (a.fp8 && (!a.xscale || !a.qscale)) return cudaErrorInvalidValue;
+  const uint32_t nkc = tc_chunks(a.dp, a.fp8 != 0);
   if (a.resident) {  // the resident block's chunks and a ring of at least 4 slots
-    const size_t need = tc_smem_bytes(4, a.dp, 1);
-    if (tc_smem_bytes(a.stages, a.dp, 1) < need) return cudaErrorInvalidValue;
+    if (a.stages < 4) return cudaErrorInvalidValue;
   }
   if (grid == 0) return cudaSuccess;
   const uint32_t C = a.hdr ? 1u : std::max(1u, a.cluster);
   if ((C != 1 && C != 2 && C != 4) || grid % C != 0) return cudaErrorInvalidValue;
-  cudaError_t e = tc_prepare(a.stages, a.dp, a.resident);
+  cudaError_t e = tc_prepare(a.stages, nkc, a.resident);
   if (e != cudaSuccess) return e;
-  const size_t smem = tc_smem_bytes(a.stages, a.dp, a.resident);
+  const size_t smem = tc_smem_bytes(a.stages, nkc, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
+  const TcKernel fn = kTcKernels[a.fp8 ? 1 : 0][a.l2 ? 1 : 0][cap == 64 ? 0 : cap == 128 ? 1 : 2];
   if (C > 1) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -1098,36 +1168,18 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const int ei = cap == 64 ? 0 : cap == 128 ? 1 : 2;
-    void (*fns[2][3])(const CUtensorMap, const CUtensorMap, const TcArgs) = {
-        {tc_shortlist_kernel<2, false>, tc_shortlist_kernel<4, false>, tc_shortlist_kernel<8, false>},
-        {tc_shortlist_kernel<2, true>, tc_shortlist_kernel<4, true>, tc_shortlist_kernel<8, true>}};
-    return cudaLaunchKernelEx(&cfg, fns[a.l2 ? 1 : 0][ei], qmap, xmap, a);
+    return cudaLaunchKernelEx(&cfg, fn, qmap, xmap, a);
   }
-  if (a.l2) {
-    if (cap == 64)
-      tc_shortlist_kernel<2, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-    else if (cap == 128)
-      tc_shortlist_kernel<4, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-    else
-      tc_shortlist_kernel<8, true><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-  } else {
-    if (cap == 64)
-      tc_shortlist_kernel<2, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-    else if (cap == 128)
-      tc_shortlist_kernel<4, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-    else
-      tc_shortlist_kernel<8, false><<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-  }
+  fn<<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
   return cudaGetLastError();
 }
 
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_t resident, bool l2) {
-  if (tc_prepare(stages, dp, resident) != cudaSuccess) return 0;
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2) {
+  if (tc_prepare(stages, nkc, resident) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster * 64);
   cfg.blockDim = dim3(kTcThreads);
-  cfg.dynamicSmemBytes = tc_smem_bytes(stages, dp, resident);
+  cfg.dynamicSmemBytes = tc_smem_bytes(stages, nkc, resident);
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cluster;
@@ -1136,9 +1188,7 @@ uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  const cudaError_t e = l2 ? cudaOccupancyMaxActiveClusters(&n, tc_shortlist_kernel<4, true>, &cfg)
-                           : cudaOccupancyMaxActiveClusters(&n, tc_shortlist_kernel<4, false>, &cfg);
-  if (e != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, kTcKernels[0][l2 ? 1 : 0][1], &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -1151,6 +1201,16 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
   const size_t threads = rows * 32;
   to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(
       src, ld_src, rows, dim, dp, static_cast<__nv_bfloat16*>(dst), norms, bounds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
+                          float* scale, float* norms, cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  if (dp8 % 16 != 0 || dp8 < dim) return cudaErrorInvalidValue;
+  const size_t threads = rows * 32;
+  to_fp8_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp8,
+                                                                     static_cast<uint8_t*>(dst), scale, norms);
   return cudaGetLastError();
 }
 

@@ -31,11 +31,16 @@ struct ServeHeader {
 };
 
 struct TcArgs {
-  uint32_t n, dp, nq, kp;          // kp: shortlist entries kept per query and split (<= 120)
+  uint32_t n, dp, nq, kp;          // dp: padded elements per row of the operand copies; kp <= 120
   uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
   uint32_t stages;
   uint32_t resident;               // 1: the query block stays in shared memory for a whole item
   uint32_t l2;                     // 1: approximate L2 from norms, 0: 1 - q.x
+  // 1: the operand copies are FP8 e4m3 with a scale per row (xscale) and per query (qscale), the
+  // score being qscale * xscale * (q8 . x8); 0: bf16 copies without scales.
+  uint32_t fp8;
+  const float* xscale;
+  const float* qscale;
   // Per-CTA candidate buffers in global memory: CTA c (linear index) owns entries
   // [c * 128 * cap, (c + 1) * 128 * cap), cap = tc_buffer_capacity(kp) per query slot.
   float* cbuf_d;
@@ -124,23 +129,27 @@ cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t
 cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
                                    uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream);
 
-// Shared memory of the shortlist kernel: ring depth, padded dim, resident query block or not.
-size_t tc_smem_bytes(uint32_t stages, uint32_t dp, uint32_t resident);
-// Ring depth for rows of dp bf16 that fits `budget` bytes (0 if none): the query block stays
+// 128-byte chunks per row of an operand copy: dp bf16 (64 per chunk) or dp e4m3 (128 per chunk).
+uint32_t tc_chunks(uint32_t dp, bool fp8);
+// Shared memory of the shortlist kernel: ring depth, chunks per row, resident query block or not.
+size_t tc_smem_bytes(uint32_t stages, uint32_t nkc, uint32_t resident);
+// Ring depth for rows of nkc chunks that fits `budget` bytes (0 if none): the query block stays
 // resident (*resident = 1) when that leaves at least 4 slots, else each slot carries a query chunk too.
-uint32_t tc_pick_stages(uint32_t dp, size_t budget, uint32_t* resident);
+uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident);
 // Candidate-buffer entries per query slot for a shortlist of kp (64, 128 or 256).
 uint32_t tc_buffer_capacity(uint32_t kp);
 
-// Encodes a 2-D bf16 tensor map (rows x dp, row stride dp * 2 bytes) with a 64 x box_rows box
-// and 128-byte swizzle. The driver's encoder is looked up through the runtime on first use.
-cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows = 128);
+// Encodes a 2-D tensor map over rows x dp elements (bf16: row stride dp * 2 bytes, 64 x box_rows
+// box; fp8: dp bytes, 128 x box_rows box), 128-byte swizzle. The driver's encoder is looked up
+// through the runtime on first use.
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows = 128,
+                          bool fp8 = false);
 // Clusters of `cluster` CTAs of the shortlist kernel that can be resident at once (0 on error).
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t dp, uint32_t resident, bool l2);
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2);
 
-// Sets the shortlist kernels' shared-memory limit for (stages, dp, resident); launch_tc_shortlist
+// Sets the shortlist kernels' shared-memory limit for (stages, nkc, resident); launch_tc_shortlist
 // does it too, but a launch being captured into a CUDA graph should find it done.
-cudaError_t tc_prepare(uint32_t stages, uint32_t dp, uint32_t resident);
+cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident);
 // grid: CTAs (x only); the candidate buffers must hold grid * 128 * tc_buffer_capacity(kp) entries.
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream);
@@ -150,5 +159,9 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
                            float* norms, cudaStream_t stream, float* bounds = nullptr);
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
+// FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
+// zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
+cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
+                          float* scale, float* norms, cudaStream_t stream);
 
 }  // namespace vsg

@@ -231,7 +231,8 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, meth
 def filtered_sweep(idx, torch, x, q, a, stream, batch=16, targets=(100, 1000, 10000, 50000, 100000, 200000)):
     """Config 3: Zipf(1.1) group labels over 2,000 groups; each query filters to one group (per-query
     1M-bit masks on the device). For groups near each allowed count, device QPS of the gather scan
-    (reads only allowed rows) and of the masked full scan (reads every tile holding an allowed row)."""
+    (reads only allowed rows), the masked full scan (reads every tile holding an allowed row) and
+    the certified tensor-core path with the masks (results equal the scans' bit for bit)."""
     from vecsearch_gb300 import datasets as D
     groups = D.zipf_groups(a.n, 2000, 1.1, seed=3)
     sizes = np.bincount(groups, minlength=2000)
@@ -244,9 +245,10 @@ def filtered_sweep(idx, torch, x, q, a, stream, batch=16, targets=(100, 1000, 10
         words = D.group_masks(groups, [g] * batch)
         wd = torch.from_numpy(words.view(np.int32)).to(qd.device)
         row = {"target": t, "allowed": int(sizes[g]), "batch": batch}
-        for mode, frac in (("gather", 1.0), ("masked_full_scan", 0.0)):
+        for mode, frac, method in (("gather", 1.0, "skinny"), ("masked_full_scan", 0.0, "skinny"),
+                                   ("tc_exact", 0.0, "tc_exact")):
             idx.set_tunable("gather_max_fraction", frac)
-            steps = 20
+            steps = 20 if batch <= 64 else 5
             for i in range(steps + 3):
                 if i == 3:
                     torch.cuda.synchronize()
@@ -255,14 +257,14 @@ def filtered_sweep(idx, torch, x, q, a, stream, batch=16, targets=(100, 1000, 10
                     e0.record(stream)
                 idx.search_device(qd.data_ptr(), a.dim, batch, a.k, out_i.data_ptr(), out_d.data_ptr(),
                                   stream=stream.cuda_stream, mask_ptr=wd.data_ptr(), per_query=True,
-                                  mask_ld=words.shape[1])
+                                  mask_ld=words.shape[1], method=method)
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / steps
             row[mode + "_qps"] = round(batch / (ms / 1e3), 1)
             row[mode + "_ms"] = round(ms, 4)
         res.append(row)
-    idx.set_tunable("gather_max_fraction", 1.0)
+    idx.set_tunable("gather_max_fraction", 0.10)
     idx.sync()
     return res
 
@@ -371,6 +373,7 @@ def run_ours(a):
 
     if rank == 0 and world == 1 and a.metric == "ip" and not a.no_filtered:
         extra["filtered_sweep"] = filtered_sweep(idx, torch, qd, q, a, stream)
+        extra["filtered_sweep_b256"] = filtered_sweep(idx, torch, qd, q, a, stream, batch=256)
 
     if rank == 0 and not a.no_recall:
         from oracle import oracle as O

@@ -47,8 +47,8 @@ extern "C" {
  * VSG_METHOD_BF16 (new) is the precision form: a BF16 tensor-core pass keeps a shortlist of
  * k' = min(120, max(k, oversample x k)) rows per query by approximate distance, then an exact
  * FP32 rerank of the shortlist returns the top-k with the streaming kernel's arithmetic. It is
- * exact whenever the shortlist holds the true top-k. Filtered searches and k > 120 run the exact
- * FP32 kernels instead. */
+ * exact whenever the shortlist holds the true top-k. Filters apply to the shortlist; k > 120 runs
+ * the exact FP32 kernels instead. */
 #define VSG_METHOD_AUTO 0u
 #define VSG_METHOD_NAIVE 1u
 #define VSG_METHOD_SKINNY 2u
@@ -59,14 +59,14 @@ extern "C" {
  * rounding of the query and the rows), and proves that no row outside the shortlist can enter
  * the top k; queries it cannot prove run the shortlist pass again with k' = 120, and those it
  * still cannot prove run in the streaming scan kernel. Results equal
- * VSG_METHOD_SKINNY bit for bit. Method AUTO uses it for unfiltered batches of at least
- * "tc_exact_min_batch" queries with k <= 32, or where the autotuner picked it. Filters and
- * k > 120 run the FP32 kernels. The call waits on its stream to read the uncertified queries. */
+ * VSG_METHOD_SKINNY bit for bit, with or without a filter. Method AUTO uses it for batches of at
+ * least "tc_exact_min_batch" queries with k <= 32 (filtered ones unless the allowed rows are few
+ * enough for the gather scan), or where the autotuner picked it. k > 120 runs the FP32 kernels. The call waits on its stream to read the uncertified queries. */
 #define VSG_METHOD_TC_EXACT 5u
 /* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
  * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32
- * rerank of a shortlist of k' = min(120, max(k, oversample x k)) rows. Filters and k > 120 run
- * the FP32 kernels. */
+ * rerank of a shortlist of k' = min(120, max(k, oversample x k)) rows. k > 120 runs the FP32
+ * kernels. */
 #define VSG_METHOD_FP8 6u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */

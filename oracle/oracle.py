@@ -120,14 +120,16 @@ def fp64_topk(x, q, k, metric="ip", allowed=None, chunk=65536):
     return best_i, best_d
 
 
-def check_ids(got_ids, want_ids, x, q, metric="ip", rel=1e-6, abs_floor=0.0):
+def check_ids(got_ids, want_ids, x, q, metric="ip", rel=1e-6, abs_floor=0.0, rel_order=1e-5):
     """Parity rule: two top-k id lists may differ only at near-ties.
 
-    At every rank where ``got`` and ``want`` disagree, the float64 distances of
-    both ids must lie within ``rel`` (relative, plus ``abs_floor``) of the
-    float64 distance of the k-th entry of ``want``, and ``got`` must be the
-    same set size. Returns the number of tolerated disagreements; raises
-    AssertionError on a real mismatch.
+    An id in one list but not the other (a different top-k set) is allowed only at the k-th
+    boundary: its float64 distance and the one it replaces lie within ``rel`` (relative, plus
+    ``abs_floor``) of each other or of the k-th float64 distance of ``want``. Two ids that are in
+    both lists but in swapped places (the same set, another order) are allowed when their float64
+    distances lie within ``rel_order`` relative: FP32 sums in different orders (the reference's
+    AVX2 loop, the GPU's lane split) can order such rows either way. Returns the number of
+    tolerated disagreements; raises AssertionError on a real mismatch.
     """
     got_ids = np.asarray(got_ids, np.int64)
     want_ids = np.asarray(want_ids, np.int64)
@@ -141,14 +143,18 @@ def check_ids(got_ids, want_ids, x, q, metric="ip", rel=1e-6, abs_floor=0.0):
         d = dict(zip(ids.tolist(), fp64_distances(x, q[qi:qi + 1], metric, ids)[0].tolist()))
         kth = d[int(w[w >= 0][-1])]
         tol = rel * abs(kth) + abs_floor
+        tol_order = rel_order * abs(kth) + abs_floor
+        gs, ws = set(g.tolist()), set(w.tolist())
         for a, b in zip(g, w):
             if a == b:
                 continue
             da, db = d[int(a)], d[int(b)]
-            # both sides of a disagreement must sit at the boundary value (a tie) or
-            # swap places with each other inside the list within the tolerance
-            assert abs(da - db) <= tol or (abs(da - kth) <= tol and abs(db - kth) <= tol), (
-                f"query {qi}: id {a} (d64={da!r}) vs {b} (d64={db!r}), k-th d64={kth!r}, tol={tol!r}")
+            if int(a) in ws and int(b) in gs:  # the same rows, another order
+                assert abs(da - db) <= tol_order, (
+                    f"query {qi}: ids {a} (d64={da!r}) and {b} (d64={db!r}) swapped, tol={tol_order!r}")
+            else:  # a different row at the k-th boundary
+                assert abs(da - db) <= tol or (abs(da - kth) <= tol and abs(db - kth) <= tol), (
+                    f"query {qi}: id {a} (d64={da!r}) vs {b} (d64={db!r}), k-th d64={kth!r}, tol={tol!r}")
             tolerated += 1
     return tolerated
 

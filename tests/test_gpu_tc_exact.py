@@ -88,6 +88,49 @@ def test_auto_routes_large_batches(gpu_ready):
     assert q1 - q0 == 256
     gpu.search(q[:64], 10)  # below the threshold: FP32 kernels
     gpu.search(q, 64)  # k > 32: FP32 kernels
-    mask = np.ones(len(x), bool)
-    gpu.search(q, 10, filter=mask)  # filtered: FP32 kernels
+    few = np.zeros(len(x), bool)
+    few[::100] = True
+    gpu.search(q, 10, filter=few)  # 1 % allowed: the gather scan reads only those rows
     assert gpu.tc_exact_stats()[0] == q1
+    wide = np.ones(len(x), bool)
+    _same(gpu.search(q, 10, filter=wide), gpu.search(q, 10, method="skinny", filter=wide))
+    assert gpu.tc_exact_stats()[0] == q1 + 256  # a wide filter takes the certified path
+
+
+def test_tc_exact_filtered(gpu_ready):
+    # A shared mask and per-query masks (Zipf groups: from a handful of rows, fewer than k, to
+    # many): the certified path equals the filtered scan bit for bit.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x, q = _clustered(80_000, 300, 128, 64, True, 260)
+    gpu = vsg.GpuBruteForceIndex(128, "cosine")
+    gpu.add(x)
+    shared = D.portable_mask(len(x), 0.3, seed=261)
+    _same(gpu.search(q, 10, method="tc_exact", filter=shared), gpu.search(q, 10, method="skinny", filter=shared))
+    groups = D.zipf_groups(len(x), 2000, 1.1, seed=262)
+    pick = np.array([0, 1, 5, 50, 500, 1999])[np.arange(300) % 6]  # common to rare groups
+    per_query = groups[None, :] == pick[:, None]
+    assert per_query.sum(1).min() < 10
+    _same(gpu.search(q, 10, method="tc_exact", filter=per_query),
+          gpu.search(q, 10, method="skinny", filter=per_query))
+    # auto: a large batch with a wide mask takes the certified path
+    q0 = gpu.tc_exact_stats()[0]
+    _same(gpu.search(q, 10, filter=shared), gpu.search(q, 10, method="skinny", filter=shared))
+    assert gpu.tc_exact_stats()[0] - q0 == 300
+
+
+def test_bf16_filtered(gpu_ready):
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x, q = _clustered(80_000, 200, 128, 64, True, 270)
+    gpu = vsg.GpuBruteForceIndex(128, "cosine")
+    gpu.add(x)
+    mask = D.portable_mask(len(x), 0.2, seed=271)
+    for m in ("bf16", "fp8"):
+        gpu.set_tunable("shortlist_oversample", 8)
+        bi, bd = gpu.search(q, 10, method=m, filter=mask)
+        pi, pd = gpu.search(q, 10, method="skinny", filter=mask)
+        assert mask[bi[bi >= 0]].all()
+        same = (bi == pi).all(1)
+        assert same.mean() >= 0.97, (m, same.mean())
+        np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))

@@ -89,3 +89,18 @@ def test_oracle_vs_live_reference_dims():
             np.testing.assert_array_equal(rd.view(np.uint32), od.view(np.uint32))
             si, sd = R.bf_search_one(x, q, 10, metric)
             np.testing.assert_array_equal(si, oi)
+
+
+def test_check_ids_rule():
+    # Near-equal rows may swap places inside the list; clearly ordered rows may not; a different
+    # row is allowed only at a k-th boundary near-tie.
+    x = np.array([[1.0, 0.0], [2.0, 0.0], [2.0 + 1e-7, 0.0], [3.0, 0.0], [4.0, 0.0], [4.0 + 1e-7, 0.0]],
+                 np.float32)
+    q = np.zeros((1, 2), np.float32)
+    want = np.array([[0, 1, 2, 3, 4]])
+    assert O.check_ids(np.array([[0, 2, 1, 3, 4]]), want, x, q, "l2") == 2   # near-equal swap
+    with pytest.raises(AssertionError):
+        O.check_ids(np.array([[1, 0, 2, 3, 4]]), want, x, q, "l2")           # 1.0 vs 4.0
+    assert O.check_ids(np.array([[0, 1, 2, 3, 5]]), want, x, q, "l2") == 1   # tie at the k-th place
+    with pytest.raises(AssertionError):
+        O.check_ids(np.array([[0, 1, 2, 4, 5]]), want, x, q, "l2")           # row 3 dropped

@@ -134,7 +134,7 @@ struct vsg_index {
   DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
   // Certified exact path (method tc_exact): rounding bounds of the bf16 rows, uncertified
   // queries ([count][ids]), their gathered queries and FP32 results.
-  DeviceBuffer xbound, fails, fids, fq, fout;
+  DeviceBuffer xbound, fails, fids, fq, fout, fmask;
   double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
   uint64_t tc_exact_queries = 0, tc_exact_second = 0, tc_exact_fallbacks = 0;
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
@@ -408,7 +408,8 @@ struct vsg_index {
 
   // The shortlist path over the bf16 copy (f8 = false) or the e4m3 copy with row scales (f8).
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                    cudaStream_t s, bool certify = false, uint32_t kp_force = 0, bool f8 = false) {
+                    cudaStream_t s, bool certify = false, uint32_t kp_force = 0, bool f8 = false,
+                    const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
     const uint32_t kp = kp_force ? kp_force : certify ? exact_shortlist_size(k) : shortlist_size(k);
     // The operand copy, its norms (and rounding bounds or scales) cover every row before any
     // kernel reads them.
@@ -467,6 +468,8 @@ struct vsg_index {
     a.nq = uint32_t(nq);
     a.nqb = uint32_t(nqb);
     a.fp8 = f8 ? 1u : 0u;
+    a.mask = dmask;  // mask_ld = 0: one mask for every query
+    a.mask_ld = uint32_t(mask_ld);
     a.xscale = f8 ? static_cast<const float*>(x8scale.get()) : nullptr;
     a.qscale = f8 ? static_cast<const float*>(q8scale.get()) : nullptr;
     a.cluster = C;
@@ -539,7 +542,7 @@ struct vsg_index {
   // still uncertified run in the streaming scan kernel, so results equal method skinny bit for
   // bit. Waits on `s` after each stage to read the uncertified queries.
   void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
-                        cudaStream_t s) {
+                        cudaStream_t s, const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
     fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
     auto read_fails = [&](size_t count) {
       uint32_t nf = 0;
@@ -555,7 +558,7 @@ struct vsg_index {
       return ids;
     };
     VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
-    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true);
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, 0, false, dmask, mask_ld);
     std::vector<uint32_t> f1 = read_fails(nq);
     tc_exact_queries += nq;
     if (f1.empty()) return;
@@ -574,10 +577,21 @@ struct vsg_index {
     uint32_t* oi2 = reinterpret_cast<uint32_t*>(od1 + n1 * k);
     float* od2 = reinterpret_cast<float*>(oi2 + n1 * k);
     VSG_CUDA(vsg::launch_gather_rows(q1, dq, ldq, uint32_t(dp), d_f1, uint32_t(n1), s));
+    // Per-query masks follow their queries (a shared mask stays as it is).
+    const uint32_t* m1 = dmask;
+    uint32_t* m2 = nullptr;
+    if (dmask && mask_ld) {
+      fmask.reserve(2 * n1 * mask_ld * sizeof(uint32_t), 0, stream);
+      uint32_t* g1 = static_cast<uint32_t*>(fmask.get());
+      m2 = g1 + n1 * mask_ld;
+      VSG_CUDA(vsg::launch_gather_rows(reinterpret_cast<float*>(g1), reinterpret_cast<const float*>(dmask), mask_ld,
+                                       uint32_t(mask_ld), d_f1, uint32_t(n1), s));
+      m1 = g1;
+    }
     std::vector<uint32_t> f2;
     if (exact_shortlist_size(k) < uint32_t(vsg::kTcMaxShortlist)) {
       VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
-      enqueue_bf16(q1, dp, n1, k, oi1, od1, s, true, uint32_t(vsg::kTcMaxShortlist));
+      enqueue_bf16(q1, dp, n1, k, oi1, od1, s, true, uint32_t(vsg::kTcMaxShortlist), false, m1, mask_ld);
       f2 = read_fails(n1);
     } else {
       f2.resize(n1);
@@ -588,7 +602,14 @@ struct vsg_index {
       const size_t n2 = f2.size();
       VSG_CUDA(cudaMemcpyAsync(d_f2, f2.data(), n2 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
       VSG_CUDA(vsg::launch_gather_rows(q2, q1, dp, uint32_t(dp), d_f2, uint32_t(n2), s));
-      enqueue(q2, dp, n2, k, nullptr, false, 0, false, oi2, od2, s, VSG_METHOD_SKINNY);
+      const uint32_t* mm = m1;
+      if (dmask && mask_ld) {
+        VSG_CUDA(vsg::launch_gather_rows(reinterpret_cast<float*>(m2), reinterpret_cast<const float*>(m1), mask_ld,
+                                         uint32_t(mask_ld), d_f2, uint32_t(n2), s));
+        mm = m2;
+      }
+      // The scan kernel's masked full scan (its gather mode gives the same results).
+      enqueue(q2, dp, n2, k, mm, dmask && mask_ld, mask_ld, false, oi2, od2, s, VSG_METHOD_SKINNY);
       VSG_CUDA(vsg::launch_scatter_results(oi1, od1, oi2, od2, uint32_t(k), d_f2, uint32_t(n2), s));
       tc_exact_fallbacks += n2;
     }
@@ -596,10 +617,12 @@ struct vsg_index {
     tc_exact_second += n1;
   }
 
-  bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask) const {
-    if (dmask || k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
+  bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask, bool gather) const {
+    if (k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
     if (method == VSG_METHOD_TC_EXACT) return true;
     if (method != VSG_METHOD_AUTO) return false;
+    if (dmask)  // small allowed sets read only their rows in the gather scan
+      return !gather && double(nq) >= tc_exact_min_batch && k <= 32;
     if (force_kernel >= 0) return force_kernel == 2;
     if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
     return double(nq) >= tc_exact_min_batch && k <= 32;
@@ -716,16 +739,13 @@ struct vsg_index {
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
                uint32_t method = VSG_METHOD_AUTO) {
     // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
-    if (method == VSG_METHOD_BF16 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
-      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s);
+    const size_t mld = dmask && per_query ? mask_ld : 0;  // 0: one mask for every query
+    if ((method == VSG_METHOD_BF16 || method == VSG_METHOD_FP8) && k <= size_t(vsg::kTcMaxShortlist)) {
+      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, false, 0, method == VSG_METHOD_FP8, dmask, mld);
       return;
     }
-    if (method == VSG_METHOD_FP8 && !dmask && k <= size_t(vsg::kTcMaxShortlist)) {
-      enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, false, 0, true);
-      return;
-    }
-    if (use_tc_exact(method, nq, k, dmask)) {
-      enqueue_tc_exact(dq, ldq, nq, k, out_ids, out_dists, s);
+    if (use_tc_exact(method, nq, k, dmask, gather)) {
+      enqueue_tc_exact(dq, ldq, nq, k, out_ids, out_dists, s, dmask, mld);
       return;
     }
     if (use_tiled(method, nq, dmask)) {

@@ -500,7 +500,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t qg = qbase + uint32_t(m);
       const bool qvalid = qg < nq;
       const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
-      const uint32_t* qmask = (persistent && qvalid) ? a.sq[qg].mask : nullptr;
+      const uint32_t* qmask = !qvalid ? nullptr
+                              : persistent ? a.sq[qg].mask
+                              : a.mask ? a.mask + size_t(qg) * a.mask_ld : nullptr;
       const float qn = (L2 && qvalid) ? a.qnorm[qg] : 0.f;
       const float qsc = (F8 && qvalid) ? a.qscale[qg] : 1.f;  // e4m3 copies: the query's scale
       float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers

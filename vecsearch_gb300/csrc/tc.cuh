@@ -68,6 +68,10 @@ struct TcArgs {
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
   uint32_t nqb;  // query blocks (non-serving launches)
+  // Non-serving launches: allow-bits (bit r & 31 of word r >> 5), one mask for every query
+  // (mask_ld = 0) or one per query, mask_ld words apart; nullptr = no filter.
+  const uint32_t* mask;
+  uint32_t mask_ld;
   // Non-serving launches: CTAs per thread-block cluster (1, 2 or 4). The C CTAs of a cluster take
   // C consecutive query blocks of one split; each loads 128 / C rows of every row chunk and
   // multicasts them to all C, so the cluster reads each row tile from L2 once. Needs the row map

@@ -60,8 +60,9 @@ extern "C" {
  * the top k; queries it cannot prove run the shortlist pass again with k' = 120, and those it
  * still cannot prove run in the streaming scan kernel. Results equal
  * VSG_METHOD_SKINNY bit for bit, with or without a filter. Method AUTO uses it for batches of at
- * least "tc_exact_min_batch" queries with k <= 32 (filtered ones unless the allowed rows are few
- * enough for the gather scan), or where the autotuner picked it. k > 120 runs the FP32 kernels. The call waits on its stream to read the uncertified queries. */
+ * least "tc_exact_min_batch" queries with k <= 32 (filtered ones from twice that, or from it when
+ * the allowed rows are too many for the gather scan), or where the autotuner picked it. k > 120
+ * runs the FP32 kernels. The call waits on its stream to read the uncertified queries. */
 #define VSG_METHOD_TC_EXACT 5u
 /* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
  * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32

@@ -621,8 +621,10 @@ struct vsg_index {
     if (k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
     if (method == VSG_METHOD_TC_EXACT) return true;
     if (method != VSG_METHOD_AUTO) return false;
-    if (dmask)  // small allowed sets read only their rows in the gather scan
-      return !gather && double(nq) >= tc_exact_min_batch && k <= 32;
+    // Filtered: the gather scan reads only the allowed rows of each query, so it wins for small
+    // allowed sets at moderate batch; from twice the threshold the shortlist pass, whose reads
+    // the whole batch shares, wins whatever the selectivity (measured at 1M x 384).
+    if (dmask) return (!gather || double(nq) >= 2 * tc_exact_min_batch) && double(nq) >= tc_exact_min_batch && k <= 32;
     if (force_kernel >= 0) return force_kernel == 2;
     if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
     return double(nq) >= tc_exact_min_batch && k <= 32;

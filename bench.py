@@ -25,6 +25,7 @@ The base (1.536 GB) is larger than L2 (129 MB), so no L2 flush is needed between
 
 --impl reference times the reference's CPU path (oracle port, all host threads) on the
 same workload and prints the same JSON line with "impl": "reference".
+--mode precision / serve / filtered run configs 4 / 5 / 3 on their own.
 """
 import argparse
 import json
@@ -71,7 +72,10 @@ def parse():
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serve mode: offered queries/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve mode: seconds of arrivals per rate")
     ap.add_argument("--plain-max-rate", type=int, default=10000, help="serve mode: highest rate for the plain path")
-    ap.add_argument("--mode", default="plain", choices=["plain", "precision", "serve"],
+    ap.add_argument("--filter-targets", default="100,1000,10000,50000,100000,200000",
+                    help="filtered mode: allowed-row counts to sweep")
+    ap.add_argument("--filter-batch", type=int, default=16, help="filtered mode: queries per search")
+    ap.add_argument("--mode", default="plain", choices=["plain", "precision", "serve", "filtered"],
                     help="precision: config 4 (BF16 shortlist + rerank) sweep instead of the default line")
     ap.add_argument("--big", action="store_true", help="precision mode: add the 4M x 384 base")
     return ap.parse_args()
@@ -93,6 +97,15 @@ def workload(a):
         "n": a.n, "dim": a.dim, "k": a.k, "batch": a.batch, "metric": a.metric, "global_batch": a.batch,
         "l2_flush": "none needed: base rows (%.3f GB) exceed the 129 MB L2" % (a.n * a.dim * 4 / 1e9),
     }
+
+
+def peaks_bf16():
+    """Measured dense bf16 TFLOP/s (burst) from MEASURED_PEAKS.json, else the 1,900 fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
 
 
 def peaks():
@@ -334,6 +347,7 @@ def run_ours(a):
                 "merge_ms_avg": round(merge_ms / max(launches, 1), 5)}
 
     extra = {}
+    bf16_peak = peaks_bf16()
     if rank == 0 and a.sweep and world == 1:
         sweep = []
         tb = [int(s) for s in a.sweep.split(",") if s and int(s) <= q.shape[0]]
@@ -361,6 +375,12 @@ def run_ours(a):
             row["bf16_tc_tflops"] = round(flops / (tc_t / l_t / 1e3) / 1e12, 1)
             row["bf16_tc_gbs"] = round(a.n * a.dim * 2 / (tc_t / l_t / 1e3) / 1e9, 1)
             row["bf16_rerank_ms"] = round(rr_t / l_t, 4)
+            # roofline fractions: HBM (measured copy) for the scan kernel at small batch, FP32 FMA
+            # (nominal 80.5 TFLOP/s) for the FP32 kernels at large batch, bf16 tensor (measured)
+            # for the shortlist kernel
+            row["kernel_frac_hbm"] = round(row["kernel_gbs"] / peak, 4)
+            row["kernel_frac_fp32"] = round(row["kernel_tflops"] / 80.5, 4)
+            row["bf16_tc_frac"] = round(row["bf16_tc_tflops"] / bf16_peak, 4)
             if b >= 8:  # certified exact tensor-core path: the scan kernel's results, bit for bit
                 q0, s0, f0 = idx.tc_exact_stats()
                 ms_e, _, _, _ = time_device(idx, torch, qd, a, b, sb, 3, stream, method="tc_exact")
@@ -408,6 +428,22 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_filtered(a):
+    """Config 3 alone: per-query group masks over the base; gather scan, masked full scan and the
+    certified path at --filter-batch queries for each allowed count in --filter-targets."""
+    import torch
+    import vecsearch_gb300 as vsg
+    torch.cuda.set_device(0)
+    x, q = make_data(a)
+    idx = vsg.GpuBruteForceIndex(a.dim, "cosine" if a.metric == "ip" else "l2")
+    idx.add(x)
+    qd = torch.from_numpy(q).cuda()
+    targets = tuple(int(t) for t in a.filter_targets.split(",") if t)
+    rows = filtered_sweep(idx, torch, qd, q, a, torch.cuda.current_stream(), batch=a.filter_batch, targets=targets)
+    print(json.dumps({"metric": "filtered exact top-k QPS by allowed rows", "unit": "queries/s", "data": "synthetic",
+                      "config": dict(workload(a), batch=a.filter_batch), "results": rows}), flush=True)
 
 
 def run_precision(a):
@@ -558,6 +594,9 @@ def main():
         return
     if a.mode == "precision":
         run_precision(a)
+        return
+    if a.mode == "filtered":
+        run_filtered(a)
         return
     if a.impl == "reference":
         run_reference(a)

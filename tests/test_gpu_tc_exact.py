@@ -90,11 +90,13 @@ def test_auto_routes_large_batches(gpu_ready):
     gpu.search(q, 64)  # k > 32: FP32 kernels
     few = np.zeros(len(x), bool)
     few[::100] = True
-    gpu.search(q, 10, filter=few)  # 1 % allowed: the gather scan reads only those rows
+    gpu.search(q[:200], 10, filter=few)  # 1 % allowed, 200 queries: the gather scan
     assert gpu.tc_exact_stats()[0] == q1
     wide = np.ones(len(x), bool)
-    _same(gpu.search(q, 10, filter=wide), gpu.search(q, 10, method="skinny", filter=wide))
-    assert gpu.tc_exact_stats()[0] == q1 + 256  # a wide filter takes the certified path
+    _same(gpu.search(q[:200], 10, filter=wide), gpu.search(q[:200], 10, method="skinny", filter=wide))
+    assert gpu.tc_exact_stats()[0] == q1 + 200  # a wide filter takes the certified path
+    _same(gpu.search(q, 10, filter=few), gpu.search(q, 10, method="skinny", filter=few))
+    assert gpu.tc_exact_stats()[0] == q1 + 456  # from 256 queries any filter does
 
 
 def test_tc_exact_filtered(gpu_ready):

@@ -356,7 +356,7 @@ struct vsg_index {
     VSG_CUDA(cudaStreamSynchronize(stream));
     fp8_rows = n;
     if (xmap8_base != x8.get() || xmap8_rows != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap8, x8.get(), n, d8, 128, true));
+      VSG_CUDA(vsg::tc_encode_map(&xmap8, x8.get(), n, d8, uint32_t(vsg::kTcRows), true));
       xmap8_base = x8.get();
       xmap8_rows = n;
     }
@@ -365,7 +365,7 @@ struct vsg_index {
   // Tensor map of the bf16 rows (re-encoded after a grow or an add).
   void ensure_xmap() {
     if (xmap_base != xb.get() || xmap_rows != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap, xb.get(), n, dp));
+      VSG_CUDA(vsg::tc_encode_map(&xmap, xb.get(), n, dp, uint32_t(vsg::kTcRows)));
       xmap_base = xb.get();
       xmap_rows = n;
     }
@@ -384,12 +384,12 @@ struct vsg_index {
 
   // CTAs per cluster for a batch of nqb query blocks: the largest of 4 / 2 / 1 that the batch
   // fills, unless tuned (0 in the table = this rule), and only if such clusters can be resident.
-  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident, uint32_t nkc) {
+  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident, uint32_t nkc, bool f8) {
     uint32_t c = tuned ? tuned : nqb >= 4 ? 4u : nqb >= 2 ? 2u : 1u;
-    const uint32_t key = stages * 65536u + nkc * 2u + resident;
+    const uint32_t key = stages * 65536u + nkc * 4u + resident * 2u + (f8 ? 1u : 0u);
     if (max_clusters_key != key) {
-      max_clusters[0] = vsg::tc_max_clusters(2, stages, nkc, resident, metric == VSG_METRIC_L2);
-      max_clusters[1] = vsg::tc_max_clusters(4, stages, nkc, resident, metric == VSG_METRIC_L2);
+      max_clusters[0] = vsg::tc_max_clusters(2, stages, nkc, resident, metric == VSG_METRIC_L2, f8);
+      max_clusters[1] = vsg::tc_max_clusters(4, stages, nkc, resident, metric == VSG_METRIC_L2, f8);
       max_clusters_key = key;
     }
     while (c > 1 && max_clusters[c == 2 ? 0 : 1] == 0) c /= 2;
@@ -425,7 +425,7 @@ struct vsg_index {
     const size_t dpo = f8 ? dp8() : dp;  // padded elements per row of the operand copies
     const uint32_t nkc = vsg::tc_chunks(uint32_t(dpo), f8);
     uint32_t resident = 0;
-    const uint32_t stages = vsg::tc_pick_stages(nkc, smem_optin - 1024, &resident);
+    const uint32_t stages = vsg::tc_pick_stages(nkc, smem_optin - 1024, &resident, metric == VSG_METRIC_L2, f8);
     if (stages < 2) throw std::invalid_argument("rows do not fit the tensor-core kernel's shared memory");
     // Queries to bf16 / e4m3 (rows past nq are zero-filled by the copy engine) and their norms.
     qnorm.reserve(nq * sizeof(float), 0, stream);
@@ -435,12 +435,12 @@ struct vsg_index {
       q8scale.reserve(nq * sizeof(float), 0, stream);
       VSG_CUDA(vsg::launch_to_fp8(dq, ldq, nq, uint32_t(dim), uint32_t(dpo), q8.get(),
                                   static_cast<float*>(q8scale.get()), static_cast<float*>(qnorm.get()), s));
-      VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, 128, true));
+      VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, uint32_t(vsg::kTcQueries), true));
     } else {
       qb.reserve(nq * dp * 2, 0, stream);
       VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
                                    static_cast<float*>(qnorm.get()), s));
-      VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp));
+      VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp, uint32_t(vsg::kTcQueries)));
       ensure_xmap();
     }
     const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
@@ -448,7 +448,7 @@ struct vsg_index {
     // Clusters of C CTAs share each row tile (multicast); items are (group of C query blocks,
     // split), taken round-robin by the clusters that fit on the GPU at once.
     const uint32_t C = pick_cluster(nqb, force_cluster >= 0 ? uint32_t(force_cluster) : te ? te->cluster : 0u,
-                                    stages, resident, nkc);
+                                    stages, resident, nkc, f8);
     const size_t nqg = ceil_div(nqb, size_t(C));
     const size_t slots = C > 1 ? size_t(max_clusters[C == 2 ? 0 : 1]) : size_t(sms);
     vsg::TcArgs a{};

@@ -109,7 +109,7 @@ struct vsg_server {
     auto* hdr = reinterpret_cast<vsg::ServeHeader*>(din);
     auto* sq = reinterpret_cast<vsg::ServeQuery*>(din + off_sq);
     float* dq = reinterpret_cast<float*>(din + off_q);
-    VSG_CUDA(vsg::tc_encode_map(&s.qmap, s.d_qb.get(), cap_q, idx->dp));
+    VSG_CUDA(vsg::tc_encode_map(&s.qmap, s.d_qb.get(), cap_q, idx->dp, uint32_t(vsg::kTcQueries)));
     float* out_d = static_cast<float*>(s.d_out.get());
     uint32_t* out_i = reinterpret_cast<uint32_t*>(out_d + out_k);
     int* status = reinterpret_cast<int*>(out_i + out_k);
@@ -132,7 +132,7 @@ struct vsg_server {
     a.sq = sq;
     vsg::ServeFinishArgs f{hdr, sq, a.part_d, a.part_i, static_cast<const float*>(idx->x.get()), dq, out_d, out_i,
                            uint32_t(idx->dp), uint32_t(kp_max), a.l2};
-    VSG_CUDA(vsg::tc_prepare(a.stages, vsg::tc_chunks(a.dp, false), a.resident));  // attributes set before capture
+    VSG_CUDA(vsg::tc_prepare(a.stages, vsg::tc_chunks(a.dp, false), a.resident, a.l2 != 0, false));  // before capture
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
                                  static_cast<float*>(s.d_qn.get()), s.stream));
@@ -363,7 +363,8 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     s->max_k = max_k;
     s->kp_max = std::min<size_t>(vsg::kTcMaxShortlist, size_t(std::ceil(std::max<double>(
                                                            double(max_k), h->shortlist_oversample * double(max_k)))));
-    s->stages = vsg::tc_pick_stages(vsg::tc_chunks(uint32_t(h->dp), false), h->smem_optin - 1024, &s->resident);
+    s->stages = vsg::tc_pick_stages(vsg::tc_chunks(uint32_t(h->dp), false), h->smem_optin - 1024, &s->resident,
+                                    h->metric == VSG_METRIC_L2, false);
     if (s->stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
     s->mwords = ceil_div(h->n, 32);
     s->off_sq = 256;

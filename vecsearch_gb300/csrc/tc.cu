@@ -34,8 +34,10 @@ namespace vsg {
 namespace {
 
 constexpr int kTcThreads = 192;
-constexpr uint32_t kChunkBytes = kTcQueries * kTcKChunk * 2;  // 16 KB: a 64-dim chunk of 128 rows
-constexpr uint32_t kTmemCols = 2 * kTcRows;
+// A row of either operand copy is cut into chunks of 128 bytes (64 bf16 or 128 e4m3 elements).
+constexpr uint32_t kChunkBytes = kTcQueries * 128;    // 16 KB: a chunk of the 128-query block (A)
+constexpr uint32_t kRowChunkBytes = kTcRows * 128;    // 32 KB: a chunk of a 256-row tile (B)
+constexpr uint32_t kTmemCols = 2 * kTcRows;           // two accumulators: all 512 columns
 constexpr int kMaxTcStages = 8;
 constexpr uint32_t kKeyNone = 0xFFFFFFFFu;  // shared threshold not set
 
@@ -45,7 +47,7 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kTcRo
                             (uint32_t(kTcQueries >> 4) << 24);
 
 // Shared memory: [resident query block: nkc chunks][ring of `stages` slots][barriers]. A slot
-// holds a 16 KB chunk of base rows, plus the matching query chunk when the block is not resident.
+// holds a 32 KB chunk of a row tile, plus the matching query chunk when the block is not resident.
 struct TcLayout {
   size_t a, ring, slot, bars, total;  // offsets from the 1024-aligned base; slot = bytes per slot
 };
@@ -53,7 +55,7 @@ struct TcLayout {
 __host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t nkc, bool resident) {
   TcLayout L;
   L.a = 0;
-  L.slot = resident ? kChunkBytes : 2 * kChunkBytes;
+  L.slot = resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes;
   L.ring = resident ? size_t(nkc) * kChunkBytes : 0;
   L.bars = L.ring + size_t(stages) * L.slot;
   L.total = L.bars + 256;
@@ -346,8 +348,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t slice_rows = kTcRows / C;  // rows of each row chunk this CTA loads for all
   const uint32_t nqg = (nqb + C - 1) / C;
   __shared__ uint32_t item_slot;
-  __shared__ __align__(16) float xs_buf[4][128];  // epilogue warps' row norms of a tile (L2)
-  __shared__ __align__(16) float xsc_buf[4][F8 ? 128 : 1];  // ... and row scales (e4m3 copies)
+  __shared__ __align__(16) float xs_buf[4][L2 ? kTcRows : 1];  // epilogue warps' row norms of a tile (L2)
+  __shared__ __align__(16) float xsc_buf[4][F8 ? kTcRows : 1];  // ... and row scales (e4m3 copies)
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -429,7 +431,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             unsigned char* st = ring + size_t(s) * L.slot;
             unsigned char* sb = resident ? st : st + kChunkBytes;
-            mbar_arrive_expect_tx(&full[s], resident ? kChunkBytes : 2 * kChunkBytes);
+            mbar_arrive_expect_tx(&full[s], resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes);
             if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
             if (C > 1)  // this CTA's slice of the row chunk, for every CTA of the cluster
               tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, int(kc * kChunkElems),
@@ -592,7 +594,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
           }
         } else {
-          // The tile's scores arrive in two loads of 64 columns. One reduction per 32 columns
+          // The tile's scores arrive in loads of 64 columns. One reduction per 32 columns
           // (the largest score, or the smallest distance with the same expression as the
           // append) and one vote per half; the per-score path runs only when some lane may have
           // a candidate.
@@ -600,15 +602,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           float* xsc = xsc_buf[quarter];
           if constexpr (L2) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) xs[c * 32 + lane] = __ldg(a.xnorm + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
+            for (int c = 0; c < kTcRows / 32; ++c)
+              xs[c * 32 + lane] = __ldg(a.xnorm + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
           }
           if constexpr (F8) {  // the rows' scales (shared by the warp; each lane applies its query's)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) xsc[c * 32 + lane] = __ldg(a.xscale + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
+            for (int c = 0; c < kTcRows / 32; ++c)
+              xsc[c * 32 + lane] = __ldg(a.xscale + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
           }
           if (L2 || F8) __syncwarp();
 #pragma unroll 1
-          for (int h = 0; h < 2; ++h) {
+          for (int h = 0; h < kTcRows / 64; ++h) {
             uint32_t v[64];
             tmem_issue64(tbase + uint32_t(h) * 64, v);
             tmem_wait64(v);
@@ -1078,18 +1082,23 @@ size_t tc_smem_bytes(uint32_t stages, uint32_t nkc, uint32_t resident) {
   return tc_layout(stages, nkc, resident != 0).total + 1024;
 }
 
-uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident) {
-  // The kernel's static shared memory (work slot, row norms and scales: 4,112 bytes) comes on top.
-  constexpr size_t kStatic = 5120;
+uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident, bool l2, bool fp8) {
+  // The kernel's static shared memory comes on top: the work slot, and 1 KB of row norms (L2)
+  // and of row scales (e4m3 copies) per epilogue warp.
+  // The deepest ring that fits is taken, so a CTA always uses more than half of an SM's shared
+  // memory: one CTA per SM, which owns all 512 TMEM columns (two CTAs, one waiting for the
+  // other's columns, could otherwise stall clusters that span both SMs).
+  const size_t kStatic = 576 + (l2 ? 4 * kTcRows * 4 : 0) + (fp8 ? 4 * kTcRows * 4 : 0);
+  const size_t half = budget / 2 + 1;
   budget = budget > kStatic ? budget - kStatic : 0;
-  for (uint32_t s = kMaxTcStages; s >= 4; --s)
+  for (uint32_t s = kMaxTcStages; s >= 3; --s)
     if (tc_smem_bytes(s, nkc, 1) <= budget) {
       *resident = 1;
-      return s;
+      return tc_smem_bytes(s, nkc, 1) + kStatic >= half ? s : 0;
     }
   *resident = 0;
   for (uint32_t s = 6; s >= 2; --s)
-    if (tc_smem_bytes(s, nkc, 0) <= budget) return s;
+    if (tc_smem_bytes(s, nkc, 0) <= budget) return tc_smem_bytes(s, nkc, 0) + kStatic >= half ? s : 0;
   return 0;
 }
 
@@ -1099,7 +1108,7 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
                           bool fp8) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
-  if (box_rows == 0 || box_rows > uint32_t(kTcRows) || !base || rows == 0) return cudaErrorInvalidValue;
+  if (box_rows == 0 || box_rows > 256u || !base || rows == 0) return cudaErrorInvalidValue;
   const cuuint64_t dims[2] = {dp, rows};
   const cuuint64_t strides[1] = {dp * (fp8 ? 1 : 2)};  // a multiple of 16 bytes
   const cuuint32_t box[2] = {fp8 ? 128u : uint32_t(kTcKChunk), box_rows};
@@ -1119,24 +1128,22 @@ const TcKernel kTcKernels[2][2][3] = {
     {{tc_shortlist_kernel<2, false, true>, tc_shortlist_kernel<4, false, true>, tc_shortlist_kernel<8, false, true>},
      {tc_shortlist_kernel<2, true, true>, tc_shortlist_kernel<4, true, true>, tc_shortlist_kernel<8, true, true>}}};
 
-cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident) {
+cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8) {
   if (stages < 2 || stages > uint32_t(kMaxTcStages) || nkc == 0) return cudaErrorInvalidValue;
   const size_t smem = tc_smem_bytes(stages, nkc, resident);
   static std::mutex mu;
-  static size_t configured[64] = {};
+  static size_t configured[64][2][2] = {};  // per device and variant (its static size differs)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> g(mu);
-  if (dev >= 64 || smem > configured[dev]) {
-    for (const auto& by_l2 : kTcKernels)
-      for (const auto& by_e : by_l2)
-        for (TcKernel f : by_e)
-          if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(reinterpret_cast<const void*>(f), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(smem));
+  if (dev >= 64 || smem > configured[dev][fp8][l2]) {
+    for (TcKernel f : kTcKernels[fp8 ? 1 : 0][l2 ? 1 : 0])
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(f), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem));
     if (e != cudaSuccess) return e;
-    if (dev < 64) configured[dev] = smem;
+    if (dev < 64) configured[dev][fp8][l2] = smem;
   }
   return cudaSuccess;
 }
@@ -1146,13 +1153,13 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
   if (a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist) || !a.cbuf_d || !a.cbuf_i) return cudaErrorInvalidValue;
   if (a.fp8 && (!a.xscale || !a.qscale)) return cudaErrorInvalidValue;
   const uint32_t nkc = tc_chunks(a.dp, a.fp8 != 0);
-  if (a.resident) {  // the resident block's chunks and a ring of at least 4 slots
-    if (a.stages < 4) return cudaErrorInvalidValue;
+  if (a.resident) {  // the resident block's chunks and a ring of at least 3 slots
+    if (a.stages < 3) return cudaErrorInvalidValue;
   }
   if (grid == 0) return cudaSuccess;
   const uint32_t C = a.hdr ? 1u : std::max(1u, a.cluster);
   if ((C != 1 && C != 2 && C != 4) || grid % C != 0) return cudaErrorInvalidValue;
-  cudaError_t e = tc_prepare(a.stages, nkc, a.resident);
+  cudaError_t e = tc_prepare(a.stages, nkc, a.resident, a.l2 != 0, a.fp8 != 0);
   if (e != cudaSuccess) return e;
   const size_t smem = tc_smem_bytes(a.stages, nkc, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
@@ -1176,8 +1183,8 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
   return cudaGetLastError();
 }
 
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2) {
-  if (tc_prepare(stages, nkc, resident) != cudaSuccess) return 0;
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8) {
+  if (tc_prepare(stages, nkc, resident, l2, fp8) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster * 64);
   cfg.blockDim = dim3(kTcThreads);
@@ -1190,7 +1197,7 @@ uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, kTcKernels[0][l2 ? 1 : 0][1], &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, kTcKernels[fp8 ? 1 : 0][l2 ? 1 : 0][1], &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

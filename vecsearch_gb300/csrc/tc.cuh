@@ -8,7 +8,7 @@
 namespace vsg {
 
 constexpr int kTcQueries = 128;  // queries per CTA (TMEM lanes, MMA M)
-constexpr int kTcRows = 128;     // base rows per tile (MMA N)
+constexpr int kTcRows = 256;     // base rows per tile (MMA N; one accumulator of 256 TMEM columns)
 constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swizzle row)
 constexpr int kTcMaxShortlist = 120;  // largest per-query shortlist (its buffer fits shared memory)
 
@@ -138,22 +138,24 @@ uint32_t tc_chunks(uint32_t dp, bool fp8);
 // Shared memory of the shortlist kernel: ring depth, chunks per row, resident query block or not.
 size_t tc_smem_bytes(uint32_t stages, uint32_t nkc, uint32_t resident);
 // Ring depth for rows of nkc chunks that fits `budget` bytes (0 if none): the query block stays
-// resident (*resident = 1) when that leaves at least 4 slots, else each slot carries a query chunk too.
-uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident);
+// resident (*resident = 1) when that leaves at least 3 slots, else each slot carries a query chunk too.
+uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident, bool l2, bool fp8);
 // Candidate-buffer entries per query slot for a shortlist of kp (64, 128 or 256).
 uint32_t tc_buffer_capacity(uint32_t kp);
 
 // Encodes a 2-D tensor map over rows x dp elements (bf16: row stride dp * 2 bytes, 64 x box_rows
-// box; fp8: dp bytes, 128 x box_rows box), 128-byte swizzle. The driver's encoder is looked up
-// through the runtime on first use.
-cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows = 128,
+// box; fp8: dp bytes, 128 x box_rows box), 128-byte swizzle; box_rows <= 256 (128 for a query
+// block, kTcRows for a row tile, kTcRows / cluster for a multicast slice). The driver's encoder
+// is looked up through the runtime on first use.
+cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows,
                           bool fp8 = false);
 // Clusters of `cluster` CTAs of the shortlist kernel that can be resident at once (0 on error).
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2);
+uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
 
-// Sets the shortlist kernels' shared-memory limit for (stages, nkc, resident); launch_tc_shortlist
-// does it too, but a launch being captured into a CUDA graph should find it done.
-cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident);
+// Sets the shared-memory limit of the shortlist kernels of one variant (metric, operand type) for
+// (stages, nkc, resident); launch_tc_shortlist does it too, but a launch being captured into a
+// CUDA graph should find it done.
+cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
 // grid: CTAs (x only); the candidate buffers must hold grid * 128 * tc_buffer_capacity(kp) entries.
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream);

@@ -165,16 +165,22 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 
 /* Autotuner (new; the reference's tunables are compile-time constants, src/gpu_brute_force.cu:23-31).
  * vsg_autotune times candidate schedules for each batch size (queries 0.9 x_i + 0.1 x_j of rows;
- * CUDA events, median of 3 after a warm-up) and keeps the fastest per batch size:
+ * CUDA events, the mean over 3 different batches after a warm-up) and keeps the fastest per batch size:
  *   method VSG_METHOD_AUTO: streaming scan, tiled kernel or certified shortlist (VSG_METHOD_TC_EXACT),
- *     and 1x or 2x the row splits for the FP32 kernels, used by
+ *     with 1x or 2x the row splits for the FP32 kernels or a first-pass shortlist of 80 or 120 for
+ *     the certified path, used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
  *     (0, 4096 or 16384; 0 = no sample pass) and how many CTAs share each row tile through a
  *     multicast cluster (1, 2 or 4; cluster = 0 in a table means the built-in rule).
  * vsg_autotune_table copies a table out (count: capacity in, entries out; choice = kernel or
- * sampled rows; cluster: CTAs per cluster of bf16 entries). vsg_autotune_save / _load persist both tables as a small text file. */
+ * sampled rows; cluster: CTAs per cluster of bf16 entries, first-pass shortlist of certified
+ * entries). vsg_autotune_save / _load persist both tables as a small text file. */
 int vsg_autotune(vsg_index* index, const size_t* batches, size_t count, size_t k, uint32_t method);
+/* The same timed on a sample of the caller's queries (nq host rows, stride dim; repeated to fill
+ * the largest batch): the certified path's choices depend on how queries sit among the rows. */
+int vsg_autotune_with_queries(vsg_index* index, const float* queries, size_t nq, const size_t* batches,
+                              size_t count, size_t k, uint32_t method);
 int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
                        double* split, uint32_t* cluster);
 int vsg_autotune_save(vsg_index* index, const char* path);

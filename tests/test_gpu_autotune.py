@@ -78,3 +78,19 @@ def test_autotune_rejects_bad_arguments(gpu_ready, tmp_path):
     empty = vsg.GpuBruteForceIndex(16, "l2")
     with pytest.raises(ValueError):
         empty.autotune((8,), k=10)
+    with pytest.raises(ValueError):
+        idx.autotune((8,), k=10, queries=np.zeros((4, 7), np.float32))  # wrong dim
+
+
+def test_autotune_with_query_sample(gpu_ready):
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    idx, x = _index(vsg, n=50_000, d=64, metric="l2", seed=95)
+    sample = D.portable(37, 64, 96)  # fewer than the largest batch: repeated to fill it
+    table = idx.autotune((8, 200), k=10, queries=sample)
+    assert [e["batch"] for e in table] == [8, 200]
+    q = D.portable(200, 64, 97)
+    ti, td = idx.search(q, 10)
+    pi, pd = idx.search(q, 10, method="skinny")
+    O.check_ids(ti, pi, x, q, "l2", rel=1e-6)
+    np.testing.assert_allclose(td, pd, rtol=1e-5, atol=2e-6)

@@ -191,15 +191,23 @@ class GpuBruteForceIndex:
         _native.check(_native.lib().vsg_get_tunable(self._h, name.encode(), ctypes.byref(v)))
         return v.value
 
-    def autotune(self, batches=(1, 8, 32, 64, 128, 512, 2048), k=10, method="auto"):
-        """Time candidate schedules per batch size and keep the fastest; returns the table."""
+    def autotune(self, batches=(1, 8, 32, 64, 128, 512, 2048), k=10, method="auto", queries=None):
+        """Time candidate schedules per batch size and keep the fastest; returns the table.
+        queries: a sample of real queries to time with (else queries near the index's rows)."""
         b = (ctypes.c_size_t * len(batches))(*[int(v) for v in batches])
-        _native.check(_native.lib().vsg_autotune(self._h, b, len(batches), int(k), _native.METHODS[method]))
+        if queries is None:
+            _native.check(_native.lib().vsg_autotune(self._h, b, len(batches), int(k), _native.METHODS[method]))
+        else:
+            qs = _as_f32(queries)
+            _check_2d(qs, self._dim)
+            _native.check(_native.lib().vsg_autotune_with_queries(self._h, _ptr(qs), qs.shape[0], b, len(batches),
+                                                                  int(k), _native.METHODS[method]))
         return self.tuning(method)
 
     def tuning(self, method="auto"):
-        """The tuned table. FP32: [{"batch", "kernel", "split"}]; bf16: [{"batch", "sample" (rows
-        sampled, 0 = none), "cluster" (CTAs sharing each row tile, 0 = built-in rule)}]."""
+        """The tuned table. Exact methods: [{"batch", "kernel", "split"} (+ "shortlist": first-pass k'
+        of the certified path)]; bf16: [{"batch", "sample" (rows sampled, 0 = none), "cluster"
+        (CTAs sharing each row tile, 0 = built-in rule)}]."""
         cnt = ctypes.c_size_t(64)
         bt = (ctypes.c_uint32 * 64)()
         ch = (ctypes.c_uint32 * 64)()
@@ -211,7 +219,8 @@ class GpuBruteForceIndex:
         if method == "bf16":
             return [{"batch": bt[i], "sample": int(ch[i]), "cluster": int(cl[i])} for i in range(n)]
         names = {0: "skinny", 1: "tiled", 2: "tc_exact"}
-        return [{"batch": bt[i], "kernel": names[ch[i]], "split": sp[i]} for i in range(n)]
+        return [dict({"batch": bt[i], "kernel": names[ch[i]], "split": sp[i]},
+                     **({"shortlist": int(cl[i])} if ch[i] == 2 else {})) for i in range(n)]
 
     def save_tuning(self, path):
         _native.check(_native.lib().vsg_autotune_save(self._h, str(path).encode()))

@@ -285,17 +285,23 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
   });
 }
 
-int vsg_autotune(vsg_index* h, const size_t* batches, size_t count, size_t k, uint32_t method) {
+int vsg_autotune_with_queries(vsg_index* h, const float* queries, size_t nq, const size_t* batches, size_t count,
+                              size_t k, uint32_t method) {
   if (!h || (!batches && count)) return fail(VSG_ERR_INVALID, "index or batches is NULL");
   return guarded([&] {
     if (method != VSG_METHOD_AUTO && method != VSG_METHOD_BF16)
-      throw std::invalid_argument("the tuner covers method auto (FP32 kernels) and bf16");
+      throw std::invalid_argument("the tuner covers method auto (exact methods) and bf16");
+    if (nq && !queries) throw std::invalid_argument("queries is NULL");
     std::lock_guard<std::mutex> g(h->mu);
     VSG_CUDA(cudaSetDevice(h->device));
     VSG_CUDA(cudaStreamWaitEvent(h->stream, h->done, 0));
-    h->autotune(batches, count, k, method);
+    h->autotune(batches, count, k, method, queries, nq);
     VSG_CUDA(cudaEventRecord(h->done, h->stream));
   });
+}
+
+int vsg_autotune(vsg_index* h, const size_t* batches, size_t count, size_t k, uint32_t method) {
+  return vsg_autotune_with_queries(h, nullptr, 0, batches, count, k, method);
 }
 
 int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
@@ -310,7 +316,7 @@ int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* b
       if (batch) batch[i] = t[i].batch;
       if (choice) choice[i] = method == VSG_METHOD_BF16 ? t[i].sample : t[i].kernel;
       if (split) split[i] = t[i].split;
-      if (cluster) cluster[i] = t[i].cluster;
+      if (cluster) cluster[i] = method == VSG_METHOD_BF16 ? t[i].cluster : t[i].exact_kp;
     }
   });
 }
@@ -322,7 +328,8 @@ int vsg_autotune_save(vsg_index* h, const char* path) {
     FILE* f = std::fopen(path, "w");
     if (!f) throw std::runtime_error(std::string("cannot open ") + path);
     std::fprintf(f, "vsg-tuning 1 dim %zu rows %zu metric %u sms %d\n", h->dim, h->n, h->metric, h->sms);
-    for (const auto& e : h->tune_plain) std::fprintf(f, "plain %u %u %.3f\n", e.batch, e.kernel, e.split);
+    for (const auto& e : h->tune_plain)
+      std::fprintf(f, "plain %u %u %.3f %u\n", e.batch, e.kernel, e.split, e.exact_kp);
     for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u %u\n", e.batch, e.sample, e.cluster);
     const bool ok = std::fclose(f) == 0;
     if (!ok) throw std::runtime_error(std::string("write failed: ") + path);
@@ -344,9 +351,12 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
       if (std::strncmp(line, "vsg-tuning 1", 12) == 0) {
         header = true;
       } else if (std::sscanf(line, "plain %u %u %lf", &b, &c, &sp) == 3 && c <= 2 && sp > 0) {
+        unsigned kp = 0;
+        std::sscanf(line, "plain %*u %*u %*f %u", &kp);  // first-pass shortlist of kernel 2 (optional)
         e.batch = b;
         e.kernel = c;
         e.split = sp;
+        e.exact_kp = kp <= 128 ? kp : 0;
         plain.push_back(e);
       } else if (std::strncmp(line, "bf16 ", 5) == 0) {
         unsigned cl = 0;

@@ -163,7 +163,7 @@ struct vsg_index {
   // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
   double shortlist_oversample = 4;
   // method "bf16": rows sampled for the starting thresholds (0: no sample pass) when nothing
-  // else is tuned for the batch size; batches under 32 queries skip it.
+  // else is tuned for the batch size; batches under 8 queries skip it.
   double sample_rows = 16384;
 
   // ---- autotuned schedules (vsg_autotune) ----
@@ -173,11 +173,12 @@ struct vsg_index {
   struct TuneEntry {
     uint32_t batch = 0, kernel = 0, sample = 16384;
     uint32_t cluster = 0;  // bf16: CTAs per cluster (0: the default rule)
+    uint32_t exact_kp = 0;  // exact methods, kernel 2: first-pass shortlist of the certified path (0: default)
     double split = 1.0;
   };
   std::vector<TuneEntry> tune_plain, tune_bf16;
   // Overrides used while the tuner times a candidate (-1 / 0 = not forced).
-  int force_kernel = -1, force_sample = -1, force_cluster = -1;
+  int force_kernel = -1, force_sample = -1, force_cluster = -1, force_exact_kp = -1;
   double force_split = 0.0;
 
   static const TuneEntry* lookup(const std::vector<TuneEntry>& t, size_t nq) {
@@ -488,12 +489,12 @@ struct vsg_index {
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     // Batches first score a sample of rows (whole tiles at the head of every split; 16K rows for
-    // 32+ queries unless tuned) and start each query at the k'-th best sampled distance, so the
+    // 8+ queries unless tuned) and start each query at the k'-th best sampled distance, so the
     // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
-                         : nq >= 32 ? size_t(sample_rows) : 0;
+                         : nq >= 8 ? size_t(sample_rows) : 0;
     if (srows > 0 && tiles_per_split > 1) {
       const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
       const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
@@ -557,8 +558,13 @@ struct vsg_index {
       }
       return ids;
     };
+    // First-pass shortlist: tuned per batch size (a wider one can spare the second pass).
+    const TuneEntry* te = dmask ? nullptr : lookup(tune_plain, nq);
+    uint32_t kp1 = force_exact_kp > 0 ? uint32_t(force_exact_kp) : te && te->kernel == 2 ? te->exact_kp : 0u;
+    kp1 = kp1 ? std::max<uint32_t>(std::min<uint32_t>(kp1, uint32_t(vsg::kTcMaxShortlist)), uint32_t(k))
+              : exact_shortlist_size(k);
     VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
-    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, 0, false, dmask, mask_ld);
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);
     std::vector<uint32_t> f1 = read_fails(nq);
     tc_exact_queries += nq;
     if (f1.empty()) return;
@@ -589,7 +595,7 @@ struct vsg_index {
       m1 = g1;
     }
     std::vector<uint32_t> f2;
-    if (exact_shortlist_size(k) < uint32_t(vsg::kTcMaxShortlist)) {
+    if (kp1 < uint32_t(vsg::kTcMaxShortlist)) {
       VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
       enqueue_bf16(q1, dp, n1, k, oi1, od1, s, true, uint32_t(vsg::kTcMaxShortlist), false, m1, mask_ld);
       f2 = read_fails(n1);
@@ -639,10 +645,13 @@ struct vsg_index {
     return double(nq) >= tiled_min_batch;
   }
 
-  // Times each candidate schedule for every batch size on queries made from the index's rows and
-  // keeps the fastest (CUDA events, median of 3 after a warm-up). family: VSG_METHOD_AUTO for the
+  // Times each candidate schedule for every batch size and keeps the fastest (CUDA events, the
+  // mean over 3 different batches after a warm-up). family: VSG_METHOD_AUTO for the
   // FP32 kernels, VSG_METHOD_BF16 for the shortlist path. Caller holds mu.
-  void autotune(const size_t* batches, size_t count, size_t k, uint32_t family) {
+  // sample / nsample: host queries (stride dim) to time with, repeated to fill the largest batch;
+  // nullptr: queries near the index's rows.
+  void autotune(const size_t* batches, size_t count, size_t k, uint32_t family, const float* sample = nullptr,
+                size_t nsample = 0) {
     if (n == 0) throw std::invalid_argument("the index is empty");
     if (k == 0 || k > VSG_MAX_K) throw std::invalid_argument("k must be in [1, 128]");
     if (family == VSG_METHOD_BF16) {
@@ -652,32 +661,40 @@ struct vsg_index {
     size_t bmax = 0;
     for (size_t i = 0; i < count; ++i) bmax = std::max(bmax, batches[i]);
     if (bmax == 0) throw std::invalid_argument("batch sizes must be > 0");
+    // Each timed repetition takes another slice of the queries, so that costs that only some
+    // batches pay (the certified path's second pass) are averaged in.
+    constexpr int kReps = 4;
+    const size_t qrows = std::max(bmax, std::min<size_t>(sample && nsample ? nsample : bmax * kReps, bmax * kReps));
     DeviceBuffer qbuf, obuf;
-    qbuf.reserve(bmax * dp * sizeof(float), 0, stream);
+    qbuf.reserve(qrows * dp * sizeof(float), 0, stream);
     obuf.reserve(bmax * k * 8, 0, stream);
-    // Queries near the index's rows (0.9 x_i + 0.1 x_j; none coincides with a row).
-    VSG_CUDA(vsg::launch_midpoint_rows(static_cast<float*>(qbuf.get()), static_cast<const float*>(x.get()),
-                                       uint32_t(dp), uint32_t(n), uint32_t(bmax), stream));
+    if (sample && nsample) {  // the caller's queries, repeated to fill qrows
+      for (size_t r = 0; r < qrows; r += nsample)
+        VSG_CUDA(cudaMemcpy2DAsync(static_cast<float*>(qbuf.get()) + r * dp, dp * sizeof(float), sample,
+                                   dim * sizeof(float), dim * sizeof(float), std::min(nsample, qrows - r),
+                                   cudaMemcpyHostToDevice, stream));
+    } else {  // queries near the index's rows (0.9 x_i + 0.1 x_j; none coincides with a row)
+      VSG_CUDA(vsg::launch_midpoint_rows(static_cast<float*>(qbuf.get()), static_cast<const float*>(x.get()),
+                                         uint32_t(dp), uint32_t(n), uint32_t(qrows), stream));
+    }
     cudaEvent_t e0, e1;
     VSG_CUDA(cudaEventCreate(&e0));
     VSG_CUDA(cudaEventCreate(&e1));
     auto time_it = [&](size_t b, uint32_t method) {
-      float best = 1e30f;
-      std::vector<float> ts;
-      for (int rep = 0; rep < 4; ++rep) {
+      float sum = 0.f;
+      for (int rep = 0; rep < kReps; ++rep) {
+        const size_t first = (size_t(rep) * b) % (qrows - b + 1);
         VSG_CUDA(cudaEventRecord(e0, stream));
-        enqueue(static_cast<const float*>(qbuf.get()), dp, b, k, nullptr, false, 0, false,
+        enqueue(static_cast<const float*>(qbuf.get()) + first * dp, dp, b, k, nullptr, false, 0, false,
                 static_cast<uint32_t*>(obuf.get()), reinterpret_cast<float*>(static_cast<char*>(obuf.get()) + b * k * 4),
                 stream, method);
         VSG_CUDA(cudaEventRecord(e1, stream));
         VSG_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
         VSG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep > 0) ts.push_back(ms);  // the first run warms up
+        if (rep > 0) sum += ms;  // the first run warms up
       }
-      std::sort(ts.begin(), ts.end());
-      best = ts[ts.size() / 2];
-      return best;
+      return sum / float(kReps - 1);  // the mean over different batches
     };
     std::vector<TuneEntry> table;
     try {
@@ -704,15 +721,21 @@ struct vsg_index {
           for (int kern : {0, 1, 2}) {
             if (kern == 1 && b < 8) continue;  // the tiled kernel's tile is 64 queries at least
             if (kern == 2 && (b < 8 || k > size_t(vsg::kTcMaxShortlist))) continue;
-            for (double f : {1.0, 2.0}) {
-              if (kern == 2 && f != 1.0) continue;  // the shortlist path sizes its own splits
+            // FP32 kernels: 1x or 2x the row splits; certified path: first-pass shortlist size
+            // (the shortlist path sizes its own splits)
+            for (int o = 0; o < 2; ++o) {
+              const double f = kern == 2 ? 1.0 : (o == 0 ? 1.0 : 2.0);
+              const int kp = kern == 2 ? (o == 0 ? int(exact_shortlist_size(k)) : int(vsg::kTcMaxShortlist)) : -1;
+              if (kern == 2 && o == 1 && kp == int(exact_shortlist_size(k))) continue;
               force_kernel = kern;
               force_split = f;
+              force_exact_kp = kp;
               const float t = time_it(b, VSG_METHOD_AUTO);
               if (t < best) {
                 best = t;
                 pick.kernel = uint32_t(kern);
                 pick.split = f;
+                pick.exact_kp = kern == 2 ? uint32_t(kp) : 0u;
               }
             }
           }
@@ -723,6 +746,7 @@ struct vsg_index {
       force_kernel = -1;
       force_sample = -1;
       force_cluster = -1;
+      force_exact_kp = -1;
       force_split = 0;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
@@ -731,6 +755,7 @@ struct vsg_index {
     force_kernel = -1;
     force_sample = -1;
     force_cluster = -1;
+    force_exact_kp = -1;
     force_split = 0;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

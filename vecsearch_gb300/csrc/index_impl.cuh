@@ -138,6 +138,7 @@ struct vsg_index {
   double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
   uint64_t tc_exact_queries = 0, tc_exact_second = 0, tc_exact_fallbacks = 0;
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
+  DeviceBuffer qmargin;  // certified path: per-query margins above the k-th best (launch_cert_margin)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
@@ -397,8 +398,11 @@ struct vsg_index {
     return c;
   }
 
-  // Certified exact path: a wider shortlist (k' >= 80) leaves a gap the error bound can prove.
-  static uint32_t exact_shortlist_size(size_t k) {
+  // Certified exact path: the list keeps the rows within each query's margin of its k-th best,
+  // up to k' entries; the widest k' (120) certifies the most queries. The autotuner also tries
+  // the narrower exact_shortlist_min(k).
+  static uint32_t exact_shortlist_size(size_t) { return uint32_t(vsg::kTcMaxShortlist); }
+  static uint32_t exact_shortlist_min(size_t k) {
     return uint32_t(std::min<size_t>(vsg::kTcMaxShortlist, std::max<size_t>(4 * k, 80)));
   }
 
@@ -464,6 +468,17 @@ struct vsg_index {
     cbuf.reserve(cbuf_entries * 8, 0, stream);
     gthr.reserve(nq * sizeof(uint32_t), 0, stream);
     VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
+    // Certified path: each query keeps only the rows within its margin of its k-th best (k' caps
+    // the list), which is all the certificate needs.
+    const bool margins = certify && !f8;
+    if (margins) {
+      qmargin.reserve(nq * sizeof(float), 0, stream);
+      VSG_CUDA(vsg::launch_cert_margin(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dp),
+                                       static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
+                                       static_cast<float*>(qmargin.get()), s));
+      a.margin = static_cast<const float*>(qmargin.get());
+      a.kk = uint32_t(k);
+    }
     a.n = uint32_t(n);
     a.dp = uint32_t(dpo);
     a.nq = uint32_t(nq);
@@ -505,8 +520,9 @@ struct vsg_index {
       sa.sample_tiles = st;
       sa.gthr = nullptr;
       VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, grid, s));
-      VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr, kp,
-                                         static_cast<float*>(thr.get()), s));
+      // (with margins: the k-th best sampled distance plus the margin)
+      VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
+                                         margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin));
       a.thr_init = static_cast<const float*>(thr.get());
     }
     VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s));
@@ -531,6 +547,7 @@ struct vsg_index {
       r.cand_d = cd;
       r.thr_init = a.thr_init;
       r.xbound = static_cast<const float*>(xbound.get());
+      r.gthr = a.gthr;
       r.fail_count = static_cast<uint32_t*>(fails.get());
       r.fail_list = r.fail_count + 1;
     }
@@ -725,8 +742,8 @@ struct vsg_index {
             // (the shortlist path sizes its own splits)
             for (int o = 0; o < 2; ++o) {
               const double f = kern == 2 ? 1.0 : (o == 0 ? 1.0 : 2.0);
-              const int kp = kern == 2 ? (o == 0 ? int(exact_shortlist_size(k)) : int(vsg::kTcMaxShortlist)) : -1;
-              if (kern == 2 && o == 1 && kp == int(exact_shortlist_size(k))) continue;
+              const int kp = kern == 2 ? (o == 0 ? int(exact_shortlist_min(k)) : int(vsg::kTcMaxShortlist)) : -1;
+              if (kern == 2 && o == 1 && kp == int(exact_shortlist_min(k))) continue;
               force_kernel = kern;
               force_split = f;
               force_exact_kp = kp;

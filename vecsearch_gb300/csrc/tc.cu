@@ -87,11 +87,14 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 
 // Sorts the first `cnt` buffered entries of one query (entry j at bd[j] / bi[j], global memory)
 // and keeps the best min(cnt, kp): back into the buffer, or, when out_d is set, into out_d /
-// out_i as a sorted list of kp entries padded with (+inf, none). Returns the kept count; thr
-// becomes entry kp - 1 when kept == kp, else (+inf, none).
+// out_i as a sorted list of kp entries padded with (+inf, none). thr becomes entry kp - 1 when
+// cnt >= kp, else (+inf, none). With a margin (mg >= 0) and at least kk entries, thr drops to
+// (entry kk - 1) + mg, rounded up, when that is lower, and only the entries at or below it are
+// kept. Returns the kept count.
 template <int E>
-__device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint32_t cnt, uint32_t kp, int lane,
-                                                  float& thr_d, uint32_t& thr_i, float* out_d, uint32_t* out_i) {
+__device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint32_t cnt, uint32_t kp, uint32_t kk,
+                                                  float mg, int lane, float& thr_d, uint32_t& thr_i, float* out_d,
+                                                  uint32_t* out_i) {
   __syncwarp();  // the lanes' appends are visible to the whole warp
   WarpTopK<E> w;
 #pragma unroll
@@ -101,7 +104,24 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
     w.i[e] = j < cnt ? bi[j] : kNone;
   }
   w.sort(lane);
-  const uint32_t keep = cnt < kp ? cnt : kp;
+  uint32_t keep = cnt < kp ? cnt : kp;
+  thr_d = __int_as_float(0x7f800000);
+  thr_i = kNone;
+  if (keep == kp) w.entry(int(kp) - 1, thr_d, thr_i);
+  if (mg >= 0.f && kk > 0 && cnt >= kk) {  // warp-uniform: cnt, kk and mg are one lane's
+    float dk;
+    uint32_t ik;
+    w.entry(int(kk) - 1, dk, ik);
+    const float tm = __fadd_ru(dk, mg);
+    if (nb_less(tm, kNone, thr_d, thr_i)) {
+      thr_d = tm;
+      thr_i = kNone;
+      uint32_t c = 0;  // the list is sorted: the entries at or below tm come first
+#pragma unroll
+      for (int e = 0; e < E; ++e) c += __popc(__ballot_sync(kFull, nb_less(w.d[e], w.i[e], tm, kNone)));
+      keep = c < keep ? c : keep;
+    }
+  }
   if (out_d) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
@@ -127,15 +147,12 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
     }
     __syncwarp();
   }
-  thr_d = __int_as_float(0x7f800000);
-  thr_i = kNone;
-  if (keep == kp) w.entry(int(kp) - 1, thr_d, thr_i);
   return keep;
 }
 
 struct CompactResult {
   uint32_t keep;  // entries kept (this lane's query, if it was compacted)
-  float td;       // its kp-th entry when keep == kp, else (+inf, none)
+  float td;       // its new threshold (compact_query's thr), or (+inf, none)
   uint32_t ti;
 };
 
@@ -145,7 +162,8 @@ struct CompactResult {
 // that calls it must stay small enough for the instruction cache.
 template <int E>
 __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsigned lanes, uint32_t cnt,
-                                                   uint32_t kp, float* out_d, uint32_t* out_i, int lane) {
+                                                   uint32_t kp, uint32_t kk, float mg, float* out_d, uint32_t* out_i,
+                                                   int lane) {
   CompactResult r{cnt, __int_as_float(0x7f800000), kNone};
   while (lanes) {
     const int src = __ffs(lanes) - 1;
@@ -155,16 +173,18 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
     float td;
     uint32_t ti;
     const uint32_t n = __shfl_sync(kFull, cnt, src), k = __shfl_sync(kFull, kp, src);
+    const uint32_t k1 = __shfl_sync(kFull, kk, src);
+    const float m1 = __shfl_sync(kFull, mg, src);
     float* bd = wd + size_t(src) * (32 * E);
     uint32_t* bi = wi + size_t(src) * (32 * E);
     // The smallest sort that holds the buffered entries (a final list is often short).
     uint32_t keep;
     if (E > 1 && n <= 32)
-      keep = compact_query<1>(bd, bi, n, k, lane, td, ti, od, oi);
+      keep = compact_query<1>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     else if (E > 2 && n <= 64)
-      keep = compact_query<(E > 2 ? 2 : E)>(bd, bi, n, k, lane, td, ti, od, oi);
+      keep = compact_query<(E > 2 ? 2 : E)>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     else
-      keep = compact_query<E>(bd, bi, n, k, lane, td, ti, od, oi);
+      keep = compact_query<E>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     if (lane == src) {
       r.keep = keep;
       r.td = td;
@@ -507,6 +527,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                               : a.mask ? a.mask + size_t(qg) * a.mask_ld : nullptr;
       const float qn = (L2 && qvalid) ? a.qnorm[qg] : 0.f;
       const float qsc = (F8 && qvalid) ? a.qscale[qg] : 1.f;  // e4m3 copies: the query's scale
+      // Certified path: the margin above the kk-th best beyond which no row is needed (-1: none).
+      const float mg = (!persistent && a.margin && qvalid) ? a.margin[qg] : -1.f;
       float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers
       uint32_t* wi = a.cbuf_i + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;
       uint32_t* gq = (a.gthr && qvalid && !a.dump) ? a.gthr + qg : nullptr;
@@ -541,10 +563,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           od = a.part_d + o;
           oi = a.part_i + o;
         }
-        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, od, oi, lane);
+        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, a.kk, mg, od, oi, lane);
         if (mine) {
           cnt = r.keep;
-          if (r.keep == kp) {
+          if (r.ti != kNone || r.td != __int_as_float(0x7f800000)) {  // a threshold was set
             if (nb_less(r.td, r.ti, thr_d, thr_i)) {
               thr_d = r.td;
               thr_i = r.ti;
@@ -825,6 +847,59 @@ __device__ __forceinline__ float exact_distance(const float4* q4, const float4* 
   return L2 ? acc : 1.0f - acc;
 }
 
+// The certificate's bound E on |approximate - FP32 distance| for one query, from its sums
+// |q|^2, |q~|^2 and |q~ - q|^2 (FP32, d terms each; q~ = the bf16 query) and the rows' bounds
+// xbound = [max |x~ - x|, max |x|, max |x~|].
+template <bool L2>
+__device__ double cert_error(double sq2, double sqb2, double sr2, uint32_t dp, const float* xbound) {
+  // FP32 sums of d non-negative terms: inflate by (1 + d 2^-23) before use.
+  const double u = 5.9604644775390625e-08, dd = double(dp), infl = 1.0 + 2.0 * dd * u;
+  const double qn = sqrt(sq2 * infl), qbn = sqrt(sqb2 * infl), rq = sqrt(sr2 * infl);
+  const double R = double(xbound[0]) * infl, N = double(xbound[1]) * infl, Nb = double(xbound[2]) * infl;
+  // |bf16 score - q.x| <= |q~||x~ - x| + |q~ - q||x| + accumulation (8 d u |q~||x~|);
+  // |FP32 q.x - q.x| <= 2 d u |q||x|.
+  const double e_dot = qbn * R + rq * N + 8.0 * dd * u * qbn * Nb + 2.0 * dd * u * qn * N;
+  double e;
+  if (L2)  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
+    e = 2.0 * e_dot + dd * u * (qn * qn + N * N) + 4.0 * u * (qn * qn + N * N + 2.0 * qbn * Nb) +
+        (dd + 2.0) * u * (qn + N) * (qn + N);
+  else  // the two roundings of 1 - s
+    e = e_dot + 4.0 * u * (1.0 + qn * N);
+  return e * 1.1;  // margin over the (already worst-case) terms
+}
+
+// The certificate's inputs for one query: |q|^2, |q~|^2 and |q~ - q|^2 over this thread's
+// columns c = first, first + step, ... below dp.
+__device__ __forceinline__ void cert_sums(const float* q, uint32_t dp, uint32_t first, uint32_t step, float& q2,
+                                          float& qb2, float& r2) {
+  for (uint32_t c = first; c < dp; c += step) {
+    const float v = q[c];
+    const float vb = __bfloat162float(__float2bfloat16_rn(v));
+    q2 = fmaf(v, v, q2);
+    qb2 = fmaf(vb, vb, qb2);
+    r2 = fmaf(vb - v, vb - v, r2);
+  }
+}
+
+// One warp per query: margin[q] = 2.2 E (rounded up). A shortlist that keeps every row within
+// this margin of its k-th best approximate distance certifies: the k-th FP32 distance is at most
+// that k-th best + E, and every row left out lies at least 2.2 E - E above it. The 10 % over 2 E
+// absorbs the different summation order of rerank_kernel's E.
+template <bool L2>
+__global__ void __launch_bounds__(128) cert_margin_kernel(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp,
+                                                          const float* xbound, float* margin) {
+  const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (qq >= nq) return;
+  float q2 = 0.f, qb2 = 0.f, r2 = 0.f;
+  cert_sums(q + size_t(qq) * ldq, dp, lane, 32, q2, qb2, r2);
+  for (int o = 16; o > 0; o >>= 1) {
+    q2 += __shfl_xor_sync(kFull, q2, o);
+    qb2 += __shfl_xor_sync(kFull, qb2, o);
+    r2 += __shfl_xor_sync(kFull, r2, o);
+  }
+  if (lane == 0) margin[qq] = __double2float_ru(2.2 * cert_error<L2>(q2, qb2, r2, dp, xbound));
+}
+
 // One CTA per query: warps compute exact distances of the candidates, then each candidate's
 // rank in (dist, id) order places the first k.
 template <bool L2>
@@ -839,17 +914,10 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   const bool q_in_smem = a.dp <= 4096;
   const bool certify = a.fail_count != nullptr;
   float q2 = 0.f, qb2 = 0.f, r2 = 0.f;  // |q|^2, |q~|^2, |q~ - q|^2 (certification)
-  for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) {
-    const float v = a.q[size_t(q) * a.ldq + c];
-    if (q_in_smem) qs[c] = v;
-    if (certify) {
-      const float vb = __bfloat162float(__float2bfloat16_rn(v));
-      q2 = fmaf(v, v, q2);
-      qb2 = fmaf(vb, vb, qb2);
-      r2 = fmaf(vb - v, vb - v, r2);
-    }
-  }
+  if (q_in_smem)
+    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
   if (certify) {
+    cert_sums(a.q + size_t(q) * a.ldq, a.dp, threadIdx.x, blockDim.x, q2, qb2, r2);
     for (int o = 16; o > 0; o >>= 1) {
       q2 += __shfl_xor_sync(kFull, q2, o);
       qb2 += __shfl_xor_sync(kFull, qb2, o);
@@ -899,23 +967,12 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
       sqb2 += red[1][w];
       sr2 += red[2][w];
     }
-    // FP32 sums of d non-negative terms: inflate by (1 + d 2^-23) before use.
-    const double u = 5.9604644775390625e-08, dd = double(a.dp), infl = 1.0 + 2.0 * dd * u;
-    const double qn = sqrt(sq2 * infl), qbn = sqrt(sqb2 * infl), rq = sqrt(sr2 * infl);
-    const double R = double(a.xbound[0]) * infl, N = double(a.xbound[1]) * infl, Nb = double(a.xbound[2]) * infl;
-    // |bf16 score - q.x| <= |q~||x~ - x| + |q~ - q||x| + accumulation (8 d u |q~||x~|);
-    // |FP32 q.x - q.x| <= 2 d u |q||x|.
-    const double e_dot = qbn * R + rq * N + 8.0 * dd * u * qbn * Nb + 2.0 * dd * u * qn * N;
-    double e;
-    if (L2)  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
-      e = 2.0 * e_dot + dd * u * (qn * qn + N * N) + 4.0 * u * (qn * qn + N * N + 2.0 * qbn * Nb) +
-          (dd + 2.0) * u * (qn + N) * (qn + N);
-    else  // the two roundings of 1 - s
-      e = e_dot + 4.0 * u * (1.0 + qn * N);
-    e *= 1.1;  // margin over the (already worst-case) terms
+    const double e = cert_error<L2>(sq2, sqb2, sr2, a.dp, a.xbound);
     const float last = kp > 0 ? a.cand_d[size_t(q) * kp + kp - 1] : __int_as_float(0x7f800000);
     const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
-    const double L = double(fminf(last, thr0));
+    const uint32_t gk = a.gthr ? a.gthr[q] : kKeyNone;
+    const float g = gk != kKeyNone ? key_float(gk) : __int_as_float(0x7f800000);
+    const double L = double(fminf(fminf(last, thr0), g));
     const bool ok = isinf(L) || (L - e > double(dk));
     if (!ok) a.fail_list[atomicAdd(a.fail_count, 1u)] = q;
   }
@@ -929,7 +986,7 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
 __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uint32_t count, uint32_t nq,
                                                              const uint32_t* kp_per_query, uint32_t kp_all,
                                                              float* thr, const ServeHeader* hdr,
-                                                             const ServeQuery* sq) {
+                                                             const ServeQuery* sq, const float* margin) {
   __shared__ uint32_t hist[256];
   __shared__ uint32_t kmin, kmax, sel_prefix, sel_rank;
   const uint32_t q = blockIdx.x;
@@ -995,7 +1052,7 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
     // Upper end of the bucket: every key with this prefix is at most prefix | ~mask. A bucket
     // reaching past +inf (padding entries) gives no bound.
     const float t = key_float(diff ? (prefix | ~hi_mask) : kmin);
-    thr[q] = t == t ? t : __int_as_float(0x7f800000);
+    thr[q] = t != t ? __int_as_float(0x7f800000) : margin ? __fadd_ru(t, margin[q]) : t;
   }
 }
 
@@ -1260,16 +1317,28 @@ cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, 
 }
 
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
-                                 uint32_t kp, float* thr, cudaStream_t stream) {
+                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin) {
   if (nq == 0) return cudaSuccess;
-  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr, nullptr, nullptr);
+  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr, nullptr, nullptr, margin);
   return cudaGetLastError();
 }
 
 cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
                                 uint32_t max_queries, cudaStream_t stream) {
   if (max_queries == 0) return cudaSuccess;
-  sample_select_kernel<<<max_queries, 256, 0, stream>>>(in, 0, 0, nullptr, 0, thr, hdr, sq);
+  sample_select_kernel<<<max_queries, 256, 0, stream>>>(in, 0, 0, nullptr, 0, thr, hdr, sq, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
+                               bool l2, float* margin, cudaStream_t stream) {
+  if (nq == 0) return cudaSuccess;
+  if (!q || !xbound || !margin || ldq < dp) return cudaErrorInvalidValue;
+  const unsigned blocks = (nq + 3) / 4;
+  if (l2)
+    cert_margin_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, margin);
+  else
+    cert_margin_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, margin);
   return cudaGetLastError();
 }
 

@@ -67,6 +67,12 @@ struct TcArgs {
   uint32_t sample_tiles;
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
+  // Certified path (non-serving launches): per-query margin m, or nullptr. A compaction that holds
+  // at least kk entries may then lower the threshold to (its kk-th best) + m: with m above twice
+  // the certificate's error bound, no row beyond it can enter the top kk, so the list keeps only
+  // the rows the proof needs instead of a fixed k'.
+  const float* margin;
+  uint32_t kk;
   uint32_t nqb;  // query blocks (non-serving launches)
   // Non-serving launches: allow-bits (bit r & 31 of word r >> 5), one mask for every query
   // (mask_ld = 0) or one per query, mask_ld words apart; nullptr = no filter.
@@ -95,9 +101,10 @@ struct ServeFinishArgs {
 };
 cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, cudaStream_t stream);
 
-// Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q].
+// Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q]; plus
+// margin[q] (rounded up) when margin != nullptr.
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
-                                 uint32_t kp, float* thr, cudaStream_t stream);
+                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin = nullptr);
 // Serving mode: the same with nq, count (nsplit * sample_tiles * 128) from hdr and each query's
 // k' from sq; CTAs past hdr->nq exit.
 cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
@@ -113,11 +120,13 @@ struct RerankArgs {
   uint32_t l2;
   // Certification (exact results from the shortlist), when fail_count is set. Every row outside
   // a query's shortlist has an approximate distance >= L = min(k'-th shortlist entry, sample
-  // threshold); a bound E on |approximate - FP32 distance| (from the bf16 rounding residuals of
-  // query and rows, Cauchy-Schwarz, and accumulation terms) then shows that none of them can
-  // enter the top k when L - E > the k-th FP32 distance found. Queries that fail are listed.
+  // threshold, smallest shared threshold); a bound E on |approximate - FP32 distance| (from the
+  // bf16 rounding residuals of query and rows, Cauchy-Schwarz, and accumulation terms) then
+  // shows that none of them can enter the top k when L - E > the k-th FP32 distance found.
+  // Queries that fail are listed.
   const float* cand_d;     // [nq][kp] approximate distances of the merged shortlist, ascending
   const float* thr_init;   // per-query sample threshold, or nullptr (none)
+  const uint32_t* gthr;    // the shortlist pass's shared thresholds (order keys), or nullptr
   const float* xbound;     // [max |x~ - x|, max |x|, max |x~|] over the rows (x~ = bf16 row)
   uint32_t* fail_count;    // number of uncertified queries (atomic), or nullptr: no check
   uint32_t* fail_list;     // their query indices
@@ -165,6 +174,10 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
                            float* norms, cudaStream_t stream, float* bounds = nullptr);
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
+// Certified path: margin[q] = 2.2 x the rerank certificate's error bound E for query q (FP32
+// queries, row stride ldq, dp columns) over rows with bounds xbound (see RerankArgs).
+cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
+                               bool l2, float* margin, cudaStream_t stream);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
 // zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,

@@ -159,7 +159,16 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   they use gather mode unless the value is 0.
  *   "tiled_min_batch" (default 48): method "auto" runs unfiltered batches of at least this many
  *   queries in the register-blocked tiled kernel, smaller ones in the streaming scan kernel.
- *   "shortlist_oversample" (default 4): shortlist size factor of VSG_METHOD_BF16. */
+ *   "shortlist_oversample" (default 4): shortlist size factor of VSG_METHOD_BF16.
+ *   "tc_exact_min_batch" (default 128): method "auto" sends unfiltered batches of at least this
+ *   many queries (k <= 32) to VSG_METHOD_TC_EXACT unless the autotuner decided otherwise.
+ *   "sample_rows" (default 16384): rows the tensor-core paths score first, per query, for a
+ *   starting threshold (batches of 8+ queries, unless tuned per batch size).
+ *   "cert_margin" (default 1.3, >= 1): VSG_METHOD_TC_EXACT keeps, per query, the rows within
+ *   cert_margin x E of its k-th best approximate distance (E: the certificate's bound on
+ *   |approximate - FP32 distance|). A smaller value keeps fewer rows; a query whose k-th FP32
+ *   distance lies more than (cert_margin - 1) E above its k-th approximate one is then not
+ *   certified and runs again. Results are exact for every value. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

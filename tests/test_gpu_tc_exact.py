@@ -35,6 +35,29 @@ def test_tc_exact_equals_scan(gpu_ready, metric, unit):
     assert s1 - s0 < 30 and f1 - f0 <= s1 - s0  # the certificate holds for most queries
 
 
+@pytest.mark.parametrize("metric,unit", [("cosine", True), ("l2", False)])
+def test_tc_exact_any_margin_is_exact(gpu_ready, metric, unit):
+    # The margin only decides how many rows each query keeps: the smallest (1.0) leaves more
+    # queries to the later stages, a large one keeps k' rows; the results never change.
+    vsg = gpu_ready
+    x, q = _clustered(60_000, 256, 128, 64, unit, 205)
+    gpu = vsg.GpuBruteForceIndex(128, metric)
+    gpu.add(x)
+    assert gpu.get_tunable("cert_margin") == pytest.approx(1.3)
+    want = gpu.search(q, 10, method="skinny")
+    retried = {}
+    for m in (1.0, 1.3, 3.0):
+        gpu.set_tunable("cert_margin", m)
+        q0, s0, _ = gpu.tc_exact_stats()
+        _same(gpu.search(q, 10, method="tc_exact"), want)
+        q1, s1, _ = gpu.tc_exact_stats()
+        assert q1 - q0 == 256
+        retried[m] = s1 - s0
+    assert retried[1.0] >= retried[3.0]
+    with pytest.raises(ValueError):
+        gpu.set_tunable("cert_margin", 0.5)
+
+
 def test_tc_exact_falls_back_when_it_cannot_prove(gpu_ready):
     # Rows 1e-4 apart around a few centres: distances closer than the bf16 error bound, so most
     # queries are not certified and run in the scan kernel; the results must not change.

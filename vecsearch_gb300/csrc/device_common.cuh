@@ -330,18 +330,47 @@ struct WarpTopK {
 // list whose best entry does not beat acc's k-th. Whole warp.
 template <int E>
 __device__ __forceinline__ void warp_merge_lists(WarpTopK<E>& acc, const float* sd, const uint32_t* si,
-                                                 int nlists, size_t stride, int k, int lane) {
+                                                 int nlists, size_t stride, int k, int lane, int kk = 0,
+                                                 float mg = -1.f) {
   float kd;
   uint32_t ki;
-  acc.entry(k - 1, kd, ki);
-  for (int j = 0; j < nlists; ++j) {
-    const float* ld = sd + size_t(j) * stride;
-    const uint32_t* li = si + size_t(j) * stride;
-    if (!nb_less(ld[0], li[0], kd, ki)) continue;  // broadcast reads; nothing in this list wins
-    WarpTopK<E> b;
-    b.load(ld, li, k, lane);
-    acc.merge(b, lane);
+  // The bar a list's first entry must beat: the k-th entry so far, or with a margin (mg >= 0)
+  // the kk-th entry + mg when that is lower.
+  auto bar = [&] {
     acc.entry(k - 1, kd, ki);
+    if (mg >= 0.f) {
+      float td;
+      uint32_t ti;
+      acc.entry(kk - 1, td, ti);
+      td = __fadd_ru(td, mg);
+      if (nb_less(td, kNone, kd, ki)) {
+        kd = td;
+        ki = kNone;
+      }
+    }
+  };
+  bar();
+  // The lists' first entries are read 32 at a time (lane l: list base + l), so the reads that
+  // decide which lists to skip do not wait on one another.
+  for (int base = 0; base < nlists; base += 32) {
+    float hd = __int_as_float(0x7f800000);
+    uint32_t hi = kNone;
+    if (base + lane < nlists) {
+      hd = sd[size_t(base + lane) * stride];
+      hi = si[size_t(base + lane) * stride];
+    }
+    unsigned live = __ballot_sync(kFull, nb_less(hd, hi, kd, ki));
+    while (live) {
+      const int src = __ffs(live) - 1;
+      live &= live - 1;
+      const float fd = __shfl_sync(kFull, hd, src);
+      const uint32_t fi = __shfl_sync(kFull, hi, src);
+      if (!nb_less(fd, fi, kd, ki)) continue;  // the bar has moved past this list's best
+      WarpTopK<E> b;
+      b.load(sd + size_t(base + src) * stride, si + size_t(base + src) * stride, k, lane);
+      acc.merge(b, lane);
+      bar();
+    }
   }
 }
 

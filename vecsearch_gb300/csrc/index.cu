@@ -265,6 +265,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "sample_rows") {
       if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("sample_rows must be in [0, 2^20]");
       h->sample_rows = value;
+    } else if (nm == "cert_margin") {
+      if (!(value >= 1.0 && value <= 100.0)) throw std::invalid_argument("cert_margin must be in [1, 100]");
+      h->cert_margin = value;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -281,6 +284,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "shortlist_oversample") *value = h->shortlist_oversample;
     else if (nm == "sample_rows") *value = h->sample_rows;
     else if (nm == "tc_exact_min_batch") *value = h->tc_exact_min_batch;
+    else if (nm == "cert_margin") *value = h->cert_margin;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

@@ -138,7 +138,7 @@ struct vsg_index {
   double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
   uint64_t tc_exact_queries = 0, tc_exact_second = 0, tc_exact_fallbacks = 0;
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
-  DeviceBuffer qmargin;  // certified path: per-query margins above the k-th best (launch_cert_margin)
+  DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_cert_margin)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
@@ -166,6 +166,10 @@ struct vsg_index {
   // method "bf16": rows sampled for the starting thresholds (0: no sample pass) when nothing
   // else is tuned for the batch size; batches under 8 queries skip it.
   double sample_rows = 16384;
+  // method "tc_exact": rows within cert_margin x E of a query's k-th best are kept (E: the
+  // certificate's error bound). Any value >= 1 gives exact results; it trades kept rows against
+  // queries left uncertified.
+  double cert_margin = 1.3;
 
   // ---- autotuned schedules (vsg_autotune) ----
   // plain: for unfiltered method "auto" searches of at least `batch` queries (largest such entry),
@@ -459,7 +463,7 @@ struct vsg_index {
     vsg::TcArgs a{};
     choose_splits(nqg, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
     const size_t parts = nq * a.nsplit * kp;
-    part.reserve(parts * 8, 0, stream);
+    part.reserve(parts * 8 + nq * a.nsplit * 4, 0, stream);  // lists, then their lengths
     cand.reserve(nq * kp * 8, 0, stream);
     // One candidate buffer per CTA.
     const unsigned grid = unsigned(std::min<size_t>(nqg * a.nsplit, slots) * C);
@@ -472,10 +476,11 @@ struct vsg_index {
     // the list), which is all the certificate needs.
     const bool margins = certify && !f8;
     if (margins) {
-      qmargin.reserve(nq * sizeof(float), 0, stream);
+      qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
       VSG_CUDA(vsg::launch_cert_margin(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dp),
                                        static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
-                                       static_cast<float*>(qmargin.get()), s));
+                                       float(cert_margin), static_cast<float*>(qmargin.get()),
+                                       static_cast<float*>(qmargin.get()) + nq, s));
       a.margin = static_cast<const float*>(qmargin.get());
       a.kk = uint32_t(k);
     }
@@ -500,6 +505,7 @@ struct vsg_index {
     a.qnorm = static_cast<const float*>(qnorm.get());
     a.part_d = static_cast<float*>(part.get());
     a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
+    a.part_n = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 8);
     a.status = status_word();
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
@@ -511,15 +517,26 @@ struct vsg_index {
                          : te ? size_t(te->sample)
                          : nq >= 8 ? size_t(sample_rows) : 0;
     if (srows > 0 && tiles_per_split > 1) {
-      const uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
-      const size_t per_query = size_t(a.nsplit) * st * vsg::kTcRows;
+      vsg::TcArgs sa = a;
+      uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
+      unsigned sgrid = grid;
+      if (size_t(a.nsplit) * vsg::kTcRows > srows) {
+        // One tile per split would sample more rows than asked for (many splits, a small batch):
+        // sample the first tile of each of ceil(srows / 256) ranges spread over the rows instead.
+        const size_t tiles = ceil_div(size_t(n), size_t(vsg::kTcRows));
+        const size_t rps = ceil_div(tiles, ceil_div(srows, size_t(vsg::kTcRows))) * vsg::kTcRows;
+        sa.rows_per_split = uint32_t(rps);
+        sa.nsplit = uint32_t(ceil_div(size_t(n), rps));
+        st = 1;
+        sgrid = unsigned(std::min<size_t>(nqg * sa.nsplit, slots) * C);
+      }
+      const size_t per_query = size_t(sa.nsplit) * st * vsg::kTcRows;
       sample.reserve(nq * per_query * sizeof(float), 0, stream);
       thr.reserve(nq * sizeof(float), 0, stream);
-      vsg::TcArgs sa = a;
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
       sa.gthr = nullptr;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, grid, s));
+      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s));
       // (with margins: the k-th best sampled distance plus the margin)
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
                                          margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin));
@@ -530,6 +547,11 @@ struct vsg_index {
     float* cd = static_cast<float*>(cand.get());
     uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
     vsg::MergeArgs m{a.part_d, a.part_i, cd, ci, uint32_t(nq), a.nsplit, kp};
+    m.part_n = a.part_n;
+    if (margins) {  // the merged list keeps only the rows within the margin of its k-th best
+      m.margin = a.margin;
+      m.kk = uint32_t(k);
+    }
     VSG_CUDA(vsg::launch_merge(m, s));
     vsg::RerankArgs r{};
     r.x = static_cast<const float*>(x.get());
@@ -546,8 +568,9 @@ struct vsg_index {
     if (certify && !f8) {
       r.cand_d = cd;
       r.thr_init = a.thr_init;
-      r.xbound = static_cast<const float*>(xbound.get());
+      r.err = static_cast<const float*>(qmargin.get()) + nq;
       r.gthr = a.gthr;
+      r.margin = m.margin;
       r.fail_count = static_cast<uint32_t*>(fails.get());
       r.fail_list = r.fail_count + 1;
     }

@@ -40,6 +40,14 @@ struct MergeArgs {
   float* out_d;            // [nq][k]
   uint32_t* out_i;
   uint32_t nq, nsplit, k;
+  // Optional cut (the certified shortlist): with margin set, entries above (the kk-th best) +
+  // margin[q], rounded up, are dropped (written as +inf / none) and lists that start above it are
+  // not merged.
+  const float* margin;
+  uint32_t kk;
+  // Optional: the real entries of each list ([nq][nsplit], the rest of a list is padding). The
+  // merge then gathers only those and sorts them once, when they fit its staging area.
+  const uint32_t* part_n;
 };
 
 struct ScanShape {

@@ -566,6 +566,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, a.kk, mg, od, oi, lane);
         if (mine) {
           cnt = r.keep;
+          if (final_list && a.part_n) a.part_n[size_t(qg) * nsplit + split] = r.keep;
           if (r.ti != kNone || r.td != __int_as_float(0x7f800000)) {  // a threshold was set
             if (nb_less(r.td, r.ti, thr_d, thr_i)) {
               thr_d = r.td;
@@ -605,14 +606,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t c0 = r0 + c * 32;
             const uint32_t allow = allowed(c0);
             if (dump_row) {
+              float o[32];
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
                 const uint32_t row = c0 + uint32_t(j);
                 const float sc = F8 ? __uint_as_float(v[j]) * (qsc * __ldg(a.xscale + min(row, a.n - 1)))
                                     : __uint_as_float(v[j]);
                 const float dist = L2 ? l2_approx(qn, __ldg(a.xnorm + min(row, a.n - 1)), sc) : 1.f - sc;
-                dump_row[t * kTcRows + c * 32 + j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
+                o[j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
               }
+              // 16-byte stores (the row's 32 values are contiguous and 128-byte aligned).
+              float4* d4 = reinterpret_cast<float4*>(dump_row + t * kTcRows + c * 32);
+#pragma unroll
+              for (int j = 0; j < 8; ++j) d4[j] = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
             }
           }
         } else {
@@ -847,6 +853,46 @@ __device__ __forceinline__ float exact_distance(const float4* q4, const float4* 
   return L2 ? acc : 1.0f - acc;
 }
 
+// exact_distance for G rows at once (row g at x4[g], nullptr: skipped): the same arithmetic per
+// row, so the same bits, with the rows' loads in flight together.
+template <bool L2, int G>
+__device__ __forceinline__ void exact_distances(const float4* q4, const float4* const (&x4)[G], uint32_t nc, int lane,
+                                                float (&out)[G]) {
+  float acc[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) acc[g] = 0.f;
+  for (uint32_t c = lane; c < nc; c += 32) {
+    const float4 qv = q4[c];
+    float4 xv[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) xv[g] = x4[g] ? __ldg(x4[g] + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if constexpr (L2) {
+        float e = qv.x - xv[g].x;
+        acc[g] = fmaf(e, e, acc[g]);
+        e = qv.y - xv[g].y;
+        acc[g] = fmaf(e, e, acc[g]);
+        e = qv.z - xv[g].z;
+        acc[g] = fmaf(e, e, acc[g]);
+        e = qv.w - xv[g].w;
+        acc[g] = fmaf(e, e, acc[g]);
+      } else {
+        acc[g] = fmaf(qv.x, xv[g].x, acc[g]);
+        acc[g] = fmaf(qv.y, xv[g].y, acc[g]);
+        acc[g] = fmaf(qv.z, xv[g].z, acc[g]);
+        acc[g] = fmaf(qv.w, xv[g].w, acc[g]);
+      }
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc[g] += __shfl_xor_sync(kFull, acc[g], o);
+    out[g] = L2 ? acc[g] : 1.0f - acc[g];
+  }
+}
+
 // The certificate's bound E on |approximate - FP32 distance| for one query, from its sums
 // |q|^2, |q~|^2 and |q~ - q|^2 (FP32, d terms each; q~ = the bf16 query) and the rows' bounds
 // xbound = [max |x~ - x|, max |x|, max |x~|].
@@ -881,13 +927,16 @@ __device__ __forceinline__ void cert_sums(const float* q, uint32_t dp, uint32_t 
   }
 }
 
-// One warp per query: margin[q] = 2.2 E (rounded up). A shortlist that keeps every row within
-// this margin of its k-th best approximate distance certifies: the k-th FP32 distance is at most
-// that k-th best + E, and every row left out lies at least 2.2 E - E above it. The 10 % over 2 E
-// absorbs the different summation order of rerank_kernel's E.
+// One warp per query: err[q] = E and margin[q] = factor x E (both rounded up). A shortlist that
+// keeps every row within the margin m of its k-th best approximate distance a_k leaves out only
+// rows at or above a_k + m, so it certifies whenever the k-th FP32 distance is below
+// a_k + m - E. That always holds for m > 2 E (the k-th FP32 distance is at most a_k + E); the
+// bf16 roundings of real data stay far below their worst case E, so m = 1.3 E already certifies
+// nearly every query while keeping about half the rows of 2 E.
 template <bool L2>
 __global__ void __launch_bounds__(128) cert_margin_kernel(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp,
-                                                          const float* xbound, float* margin) {
+                                                          const float* xbound, float factor, float* margin,
+                                                          float* err) {
   const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (qq >= nq) return;
   float q2 = 0.f, qb2 = 0.f, r2 = 0.f;
@@ -897,56 +946,56 @@ __global__ void __launch_bounds__(128) cert_margin_kernel(const float* q, uint32
     qb2 += __shfl_xor_sync(kFull, qb2, o);
     r2 += __shfl_xor_sync(kFull, r2, o);
   }
-  if (lane == 0) margin[qq] = __double2float_ru(2.2 * cert_error<L2>(q2, qb2, r2, dp, xbound));
+  if (lane == 0) {
+    const double e = cert_error<L2>(q2, qb2, r2, dp, xbound);
+    err[qq] = __double2float_ru(e);
+    margin[qq] = __double2float_ru(double(factor) * e);
+  }
 }
 
 // One CTA per query: warps compute exact distances of the candidates, then each candidate's
-// rank in (dist, id) order places the first k.
+// rank in (dist, id) order places the first k. The candidate list is sorted with the missing
+// entries (none) at its end, so the real ones are a prefix.
 template <bool L2>
 __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   __shared__ float cd[kMaxK];
   __shared__ uint32_t ci[kMaxK];
   __shared__ __align__(16) float qs[4096];
-  __shared__ float red[3][8];
   __shared__ float dk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q = blockIdx.x, kp = a.kp, nc = a.dp / 4;
   const bool q_in_smem = a.dp <= 4096;
-  const bool certify = a.fail_count != nullptr;
-  float q2 = 0.f, qb2 = 0.f, r2 = 0.f;  // |q|^2, |q~|^2, |q~ - q|^2 (certification)
   if (q_in_smem)
     for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
-  if (certify) {
-    cert_sums(a.q + size_t(q) * a.ldq, a.dp, threadIdx.x, blockDim.x, q2, qb2, r2);
-    for (int o = 16; o > 0; o >>= 1) {
-      q2 += __shfl_xor_sync(kFull, q2, o);
-      qb2 += __shfl_xor_sync(kFull, qb2, o);
-      r2 += __shfl_xor_sync(kFull, r2, o);
-    }
-    if (lane == 0) {
-      red[0][warp] = q2;
-      red[1][warp] = qb2;
-      red[2][warp] = r2;
-    }
-  }
   if (threadIdx.x == 0) dk = __int_as_float(0x7f800000);
-  __syncthreads();
+  const uint32_t id0 = threadIdx.x < kp ? a.cand[size_t(q) * kp + threadIdx.x] : kNone;  // kp <= 128 < threads
+  if (threadIdx.x < kp) ci[threadIdx.x] = id0;
+  const uint32_t nreal = uint32_t(__syncthreads_count(id0 != kNone));
   const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.ldq);
-  for (uint32_t j = warp; j < kp; j += blockDim.x / 32) {
-    const uint32_t id = a.cand[size_t(q) * kp + j];
-    float d = __int_as_float(0x7f800000);
-    if (id != kNone) d = exact_distance<L2>(q4, reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp), nc, lane);
+  // Four candidates per warp at a time (candidates warp, warp + 8, ...: four in a row per warp).
+  constexpr int G = 4;
+  const uint32_t nwarps = blockDim.x / 32;
+  for (uint32_t j0 = warp; j0 < nreal; j0 += G * nwarps) {
+    const float4* x4[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const uint32_t j = j0 + uint32_t(g) * nwarps;
+      x4[g] = j < nreal ? reinterpret_cast<const float4*>(a.x + size_t(ci[j]) * a.dp) : nullptr;
+    }
+    float d[G];
+    exact_distances<L2, G>(q4, x4, nc, lane, d);
     if (lane == 0) {
-      cd[j] = d;
-      ci[j] = id;
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+        if (j0 + uint32_t(g) * nwarps < nreal) cd[j0 + uint32_t(g) * nwarps] = d[g];
     }
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < kp; j += blockDim.x) {
+  for (uint32_t j = threadIdx.x; j < nreal; j += blockDim.x) {
     const float dj = cd[j];
     const uint32_t ij = ci[j];
     uint32_t rank = 0;
-    for (uint32_t t = 0; t < kp; ++t)
+    for (uint32_t t = 0; t < nreal; ++t)
       rank += nb_less(cd[t], ci[t], dj, ij) || (cd[t] == dj && ci[t] == ij && t < j);
     if (rank < a.k) {
       a.out_d[size_t(q) * a.k + rank] = dj;
@@ -954,26 +1003,21 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
     }
     if (rank + 1 == a.k) dk = dj;  // the k-th FP32 distance
   }
-  for (uint32_t j = kp + threadIdx.x; j < a.k; j += blockDim.x) {  // k > kp: pad
+  for (uint32_t j = nreal + threadIdx.x; j < a.k; j += blockDim.x) {  // fewer than k candidates: pad
     a.out_d[size_t(q) * a.k + j] = __int_as_float(0x7f800000);
     a.out_i[size_t(q) * a.k + j] = kNone;
   }
-  if (!certify) return;
+  if (!a.fail_count) return;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double sq2 = 0, sqb2 = 0, sr2 = 0;
-    for (int w = 0; w < int(blockDim.x / 32); ++w) {
-      sq2 += red[0][w];
-      sqb2 += red[1][w];
-      sr2 += red[2][w];
-    }
-    const double e = cert_error<L2>(sq2, sqb2, sr2, a.dp, a.xbound);
     const float last = kp > 0 ? a.cand_d[size_t(q) * kp + kp - 1] : __int_as_float(0x7f800000);
     const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
     const uint32_t gk = a.gthr ? a.gthr[q] : kKeyNone;
     const float g = gk != kKeyNone ? key_float(gk) : __int_as_float(0x7f800000);
-    const double L = double(fminf(fminf(last, thr0), g));
-    const bool ok = isinf(L) || (L - e > double(dk));
+    const float cut = (a.margin && a.k <= kp) ? __fadd_ru(a.cand_d[size_t(q) * kp + a.k - 1], a.margin[q])
+                                               : __int_as_float(0x7f800000);
+    const double L = double(fminf(fminf(last, thr0), fminf(g, cut)));
+    const bool ok = isinf(L) || (L - double(a.err[q]) > double(dk));
     if (!ok) a.fail_list[atomicAdd(a.fail_count, 1u)] = q;
   }
 }
@@ -1007,12 +1051,25 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
     sel_rank = kp;  // 1-based rank still to find inside the current prefix
   }
   __syncthreads();
+  // Every value once per pass: float4 loads (count is a multiple of 4 and rows start 16-byte
+  // aligned: count = splits x tiles x 256), four independent keys per load.
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  const uint32_t n4 = count / 4;
+  auto each_key = [&](auto&& f) {
+#pragma unroll 4
+    for (uint32_t j = threadIdx.x; j < n4; j += blockDim.x) {
+      const float4 x = v4[j];
+      f(order_key(x.x));
+      f(order_key(x.y));
+      f(order_key(x.z));
+      f(order_key(x.w));
+    }
+  };
   uint32_t lo = 0xFFFFFFFFu, hi = 0u;
-  for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
-    const uint32_t key = order_key(v[j]);
+  each_key([&](uint32_t key) {
     lo = min(lo, key);
     hi = max(hi, key);
-  }
+  });
   lo = __reduce_min_sync(kFull, lo);
   hi = __reduce_max_sync(kFull, hi);
   if ((threadIdx.x & 31) == 0) {
@@ -1030,16 +1087,45 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
     for (int round = 0; round < 2; ++round) {
       for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
       __syncthreads();
-      for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
-        const uint32_t key = order_key(v[j]);
+      each_key([&](uint32_t key) {
         if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
-      }
+      });
       __syncthreads();
-      if (threadIdx.x == 0) {
-        uint32_t r = sel_rank, b = 0;
-        while (b < 255 && hist[b] < r) r -= hist[b++];
-        sel_prefix = prefix | (b << shift);
-        sel_rank = r;
+      if (threadIdx.x < 32) {
+        // The first bucket whose running count reaches the rank (bucket 255 if none does): lane
+        // l holds buckets 8l .. 8l + 7; a warp scan of their sums finds the lane, the lane its bucket.
+        const uint32_t l = threadIdx.x;
+        uint32_t c[8], sum = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          c[i] = hist[l * 8 + i];
+          sum += c[i];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(kFull, incl, o);
+          if (l >= uint32_t(o)) incl += t;
+        }
+        const uint32_t r = sel_rank;
+        const unsigned reach = __ballot_sync(kFull, incl >= r);
+        const uint32_t src = reach ? uint32_t(__ffs(reach) - 1) : 31u;
+        if (l == src) {
+          uint32_t rr = r - (incl - sum), bi = 7;
+          bool found = false;
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!found) {
+              if (c[i] >= rr || i == 7) {
+                bi = uint32_t(i);
+                found = true;
+              } else {
+                rr -= c[i];
+              }
+            }
+          sel_prefix = prefix | ((l * 8 + bi) << shift);
+          sel_rank = rr;
+        }
       }
       __syncthreads();
       prefix = sel_prefix;
@@ -1319,6 +1405,7 @@ cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, 
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
                                  uint32_t kp, float* thr, cudaStream_t stream, const float* margin) {
   if (nq == 0) return cudaSuccess;
+  if (count % 4 != 0 || reinterpret_cast<uintptr_t>(in) % 16 != 0) return cudaErrorInvalidValue;  // float4 loads
   sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr, nullptr, nullptr, margin);
   return cudaGetLastError();
 }
@@ -1331,19 +1418,20 @@ cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, co
 }
 
 cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
-                               bool l2, float* margin, cudaStream_t stream) {
+                               bool l2, float factor, float* margin, float* err, cudaStream_t stream) {
   if (nq == 0) return cudaSuccess;
-  if (!q || !xbound || !margin || ldq < dp) return cudaErrorInvalidValue;
+  if (!q || !xbound || !margin || !err || ldq < dp || !(factor >= 0.f)) return cudaErrorInvalidValue;
   const unsigned blocks = (nq + 3) / 4;
   if (l2)
-    cert_margin_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, margin);
+    cert_margin_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, factor, margin, err);
   else
-    cert_margin_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, margin);
+    cert_margin_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, factor, margin, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream) {
   if (a.kp > uint32_t(kMaxK)) return cudaErrorInvalidValue;
+  if (a.fail_count && (!a.err || !a.fail_list || !a.cand_d)) return cudaErrorInvalidValue;
   if (a.l2)
     rerank_kernel<true><<<a.nq, 256, 0, stream>>>(a);
   else

@@ -52,6 +52,7 @@ struct TcArgs {
   const float* qnorm;              // squared query norms (L2 only)
   float* part_d;                   // [nq][nsplit][kp] approximate distances, sorted
   uint32_t* part_i;
+  uint32_t* part_n;                // [nq][nsplit] real entries of each list, or nullptr
   int* status;
   uint32_t* gthr;
   // Serving mode (persistent): when hdr is set the grid has one CTA per SM, the batch shape
@@ -68,9 +69,9 @@ struct TcArgs {
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
   // Certified path (non-serving launches): per-query margin m, or nullptr. A compaction that holds
-  // at least kk entries may then lower the threshold to (its kk-th best) + m: with m above twice
-  // the certificate's error bound, no row beyond it can enter the top kk, so the list keeps only
-  // the rows the proof needs instead of a fixed k'.
+  // at least kk entries may then lower the threshold to (its kk-th best) + m, so the list keeps
+  // the rows near the top kk instead of a fixed k'. Every threshold is published to gthr, and
+  // the rerank's certificate takes the smallest, so any m keeps results exact.
   const float* margin;
   uint32_t kk;
   uint32_t nqb;  // query blocks (non-serving launches)
@@ -120,14 +121,17 @@ struct RerankArgs {
   uint32_t l2;
   // Certification (exact results from the shortlist), when fail_count is set. Every row outside
   // a query's shortlist has an approximate distance >= L = min(k'-th shortlist entry, sample
-  // threshold, smallest shared threshold); a bound E on |approximate - FP32 distance| (from the
-  // bf16 rounding residuals of query and rows, Cauchy-Schwarz, and accumulation terms) then
-  // shows that none of them can enter the top k when L - E > the k-th FP32 distance found.
-  // Queries that fail are listed.
+  // threshold, smallest shared threshold, merge cut); a bound E on |approximate - FP32 distance|
+  // (launch_cert_margin: from the bf16 rounding residuals of query and rows, Cauchy-Schwarz, and
+  // accumulation terms) then shows that none of them can enter the top k when L - E > the k-th
+  // FP32 distance found. Queries that fail are listed.
   const float* cand_d;     // [nq][kp] approximate distances of the merged shortlist, ascending
   const float* thr_init;   // per-query sample threshold, or nullptr (none)
   const uint32_t* gthr;    // the shortlist pass's shared thresholds (order keys), or nullptr
-  const float* xbound;     // [max |x~ - x|, max |x|, max |x~|] over the rows (x~ = bf16 row)
+  // The merge's cut, when the merge ran with these margins: rows above (k-th entry) + margin[q]
+  // were dropped, so that value bounds L too. nullptr: no cut.
+  const float* margin;
+  const float* err;        // per-query E (launch_cert_margin), needed when fail_count is set
   uint32_t* fail_count;    // number of uncertified queries (atomic), or nullptr: no check
   uint32_t* fail_list;     // their query indices
 };
@@ -174,10 +178,12 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
                            float* norms, cudaStream_t stream, float* bounds = nullptr);
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
-// Certified path: margin[q] = 2.2 x the rerank certificate's error bound E for query q (FP32
-// queries, row stride ldq, dp columns) over rows with bounds xbound (see RerankArgs).
+// Certified path: err[q] = the certificate's error bound E on |approximate - FP32 distance| for
+// query q (FP32 queries, row stride ldq, dp columns) over rows whose bf16 copies have the bounds
+// xbound = [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E; both
+// rounded up.
 cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
-                               bool l2, float* margin, cudaStream_t stream);
+                               bool l2, float factor, float* margin, float* err, cudaStream_t stream);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
 // zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,

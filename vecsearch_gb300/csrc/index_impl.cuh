@@ -330,39 +330,41 @@ struct vsg_index {
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
-  // Brings the BF16 copy and the norms up to the current rows (after a grow they are rebuilt).
+  // Brings the BF16 copy (tile-major, see vsg::tc_tiled_bytes) and the norms up to the current
+  // rows (after a grow they are rebuilt).
   void ensure_bf16() {
-    if (bf16_rows == n && xb.bytes() >= cap * dp * 2) return;
-    const size_t keep = xb.bytes() >= cap * dp * 2 ? bf16_rows : 0;
-    xb.reserve(cap * dp * 2, keep * dp * 2, stream);
+    const size_t need = vsg::tc_tiled_bytes(cap, uint32_t(dp), false);
+    if (bf16_rows == n && xb.bytes() >= need) return;
+    const size_t keep = xb.bytes() >= need ? bf16_rows : 0;
+    xb.reserve(need, vsg::tc_tiled_bytes(keep, uint32_t(dp), false), stream);
     xnorm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
     xbound.reserve(16, 0, stream);
     if (keep == 0) VSG_CUDA(cudaMemsetAsync(xbound.get(), 0, 16, stream));  // every row is converted again
     VSG_CUDA(vsg::launch_to_bf16(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dp),
-                                 uint32_t(dp), static_cast<char*>(xb.get()) + keep * dp * 2,
-                                 static_cast<float*>(xnorm.get()) + keep, stream,
-                                 static_cast<float*>(xbound.get())));
+                                 uint32_t(dp), xb.get(), static_cast<float*>(xnorm.get()) + keep, stream,
+                                 static_cast<float*>(xbound.get()), keep));
     VSG_CUDA(cudaStreamSynchronize(stream));
     bf16_rows = n;
   }
 
   size_t dp8() const { return (dim + 15) / 16 * 16; }
 
+  // The e4m3 copy (tile-major), its row scales and norms, and its tensor map.
   void ensure_fp8() {
-    const size_t d8 = dp8();
-    if (fp8_rows == n && x8.bytes() >= cap * d8) return;
-    const size_t keep = x8.bytes() >= cap * d8 ? fp8_rows : 0;
-    x8.reserve(cap * d8, keep * d8, stream);
+    const uint32_t d8 = uint32_t(dp8());
+    const size_t need = vsg::tc_tiled_bytes(cap, d8, true);
+    if (fp8_rows == n && x8.bytes() >= need) return;
+    const size_t keep = x8.bytes() >= need ? fp8_rows : 0;
+    x8.reserve(need, vsg::tc_tiled_bytes(keep, d8, true), stream);
     x8scale.reserve(cap * sizeof(float), keep * sizeof(float), stream);
     x8norm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
-    VSG_CUDA(vsg::launch_to_fp8(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dim),
-                                uint32_t(d8), static_cast<char*>(x8.get()) + keep * d8,
-                                static_cast<float*>(x8scale.get()) + keep, static_cast<float*>(x8norm.get()) + keep,
-                                stream));
+    VSG_CUDA(vsg::launch_to_fp8(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dim), d8,
+                                x8.get(), static_cast<float*>(x8scale.get()) + keep,
+                                static_cast<float*>(x8norm.get()) + keep, stream, keep));
     VSG_CUDA(cudaStreamSynchronize(stream));
     fp8_rows = n;
     if (xmap8_base != x8.get() || xmap8_rows != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap8, x8.get(), n, d8, uint32_t(vsg::kTcRows), true));
+      VSG_CUDA(vsg::tc_encode_tiled_map(&xmap8, x8.get(), n, d8, uint32_t(vsg::kTcRows), true));
       xmap8_base = x8.get();
       xmap8_rows = n;
     }
@@ -371,7 +373,7 @@ struct vsg_index {
   // Tensor map of the bf16 rows (re-encoded after a grow or an add).
   void ensure_xmap() {
     if (xmap_base != xb.get() || xmap_rows != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap, xb.get(), n, dp, uint32_t(vsg::kTcRows)));
+      VSG_CUDA(vsg::tc_encode_tiled_map(&xmap, xb.get(), n, uint32_t(dp), uint32_t(vsg::kTcRows), false));
       xmap_base = xb.get();
       xmap_rows = n;
     }
@@ -381,7 +383,8 @@ struct vsg_index {
     const int i = (cluster == 2 ? 0 : 1) + (f8 ? 2 : 0);
     const void* base = f8 ? x8.get() : xb.get();
     if (xmap_slice_base[i] != base || xmap_slice_rows[i] != n) {
-      VSG_CUDA(vsg::tc_encode_map(&xmap_slice[i], base, n, f8 ? dp8() : dp, uint32_t(vsg::kTcRows) / cluster, f8));
+      VSG_CUDA(vsg::tc_encode_tiled_map(&xmap_slice[i], base, n, uint32_t(f8 ? dp8() : dp),
+                                        uint32_t(vsg::kTcRows) / cluster, f8));
       xmap_slice_base[i] = base;
       xmap_slice_rows[i] = n;
     }

@@ -66,6 +66,12 @@ __host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t nkc, boo
 // compactions (one is due when the next 32 scores might not fit). The warp sort holds 32 E = cap.
 __host__ __device__ inline uint32_t tc_capacity(uint32_t kp) { return kp <= 16 ? 64 : kp <= 48 ? 128 : 256; }
 
+// Element offset of (row, column c) in a tile-major operand copy with nkc chunks of ce elements
+// (64 bf16 or 128 e4m3) per row.
+__host__ __device__ inline size_t tile_major_offset(size_t row, uint32_t c, uint32_t nkc, uint32_t ce) {
+  return ((row / kTcRows) * nkc + c / ce) * size_t(kTcRows) * ce + (row % kTcRows) * ce + c % ce;
+}
+
 // Approximate L2 distance from squared norms and the bf16 score: |q|^2 + |x|^2 - 2 s, rounded
 // the same way wherever it is computed (the prefilter, the append and the sample pass agree).
 __device__ __forceinline__ float l2_approx(float qn, float xn, float sc) { return __fmaf_rn(-2.f, sc, __fadd_rn(qn, xn)); }
@@ -443,8 +449,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
         }
         for (uint32_t t = 0; t < ntiles && ok; ++t) {
-          const int y = int(row_begin + t * kTcRows);
+          // Tile-major row copy: chunk kc of this tile is kTcRows chunk rows starting at y.
+          const uint32_t tile = row_begin / kTcRows + t;
           for (uint32_t kc = 0; kc < nkc; ++kc) {
+            const int y = int((tile * nkc + kc) * kTcRows);
             if (!mbar_wait(&empty[s], ph ^ 1)) {
               ok = false;
               break;
@@ -454,10 +462,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_arrive_expect_tx(&full[s], resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes);
             if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
             if (C > 1)  // this CTA's slice of the row chunk, for every CTA of the cluster
-              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, int(kc * kChunkElems),
-                             y + int(rank * slice_rows), &full[s], cmask, stream_policy);
+              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, 0, y + int(rank * slice_rows), &full[s],
+                             cmask, stream_policy);
             else
-              tma_load_2d(sb, &xmap, int(kc * kChunkElems), y, &full[s], stream_policy);
+              tma_load_2d(sb, &xmap, 0, y, &full[s], stream_policy);
             pending |= 1u << s;
             last_ph = (last_ph & ~(1u << s)) | (ph << s);
             if (++s == stages) {
@@ -735,14 +743,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // and, for certification, the rows' largest rounding residual and norms.
 __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim,
                                uint32_t dp, __nv_bfloat16* __restrict__ dst, float* __restrict__ norms,
-                               float* __restrict__ bounds) {
+                               float* __restrict__ bounds, size_t tile_row0) {
   const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
   const float* s = src + row * ld_src;
-  __nv_bfloat16* d = dst + row * dp;
+  const bool tiled = tile_row0 != kRowMajor;
+  const uint32_t nkc = (dp + kTcKChunk - 1) / kTcKChunk;
+  const uint32_t width = tiled ? nkc * uint32_t(kTcKChunk) : dp;  // tile-major chunks are whole
   float acc = 0.f, res = 0.f, accb = 0.f;
-  for (uint32_t c = lane; c < dp; c += 32) {
+  for (uint32_t c = lane; c < width; c += 32) {
     const float v = c < dim ? s[c] : 0.f;
     const __nv_bfloat16 b = __float2bfloat16_rn(v);
     acc = fmaf(v, v, acc);
@@ -750,7 +760,7 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, siz
     const float e = vb - v;  // exact: v and its rounding are within a factor of 2
     res = fmaf(e, e, res);
     accb = fmaf(vb, vb, accb);
-    d[c] = b;
+    dst[tiled ? tile_major_offset(tile_row0 + row, c, nkc, kTcKChunk) : row * dp + c] = b;
   }
   for (int o = 16; o > 0; o >>= 1) {
     acc += __shfl_xor_sync(kFull, acc, o);
@@ -770,7 +780,8 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, siz
 // FP32 rows -> e4m3 rows of stride dp8 bytes (columns >= dim are zero), one FP32 scale per row
 // (max |x| / 448, the largest finite e4m3; 1 for a zero row) and optional squared FP32 norms.
 __global__ void to_fp8_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8,
-                              uint8_t* __restrict__ dst, float* __restrict__ scale, float* __restrict__ norms) {
+                              uint8_t* __restrict__ dst, float* __restrict__ scale, float* __restrict__ norms,
+                              size_t tile_row0) {
   const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
@@ -787,9 +798,12 @@ __global__ void to_fp8_kernel(const float* __restrict__ src, size_t ld_src, size
   }
   const float sc = mx > 0.f ? mx / 448.f : 1.f;
   const float inv = 1.f / sc;
-  uint8_t* d = dst + row * dp8;
-  for (uint32_t c = lane; c < dp8; c += 32)
-    d[c] = c < dim ? uint8_t(__nv_cvt_float_to_fp8(s[c] * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+  const bool tiled = tile_row0 != kRowMajor;
+  const uint32_t nkc = (dp8 + 127) / 128;
+  const uint32_t width = tiled ? nkc * 128u : dp8;  // tile-major chunks are whole
+  for (uint32_t c = lane; c < width; c += 32)
+    dst[tiled ? tile_major_offset(tile_row0 + row, c, nkc, 128) : row * dp8 + c] =
+        c < dim ? uint8_t(__nv_cvt_float_to_fp8(s[c] * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
   if (lane == 0) {
     scale[row] = sc;
     if (norms) norms[row] = acc;
@@ -1348,21 +1362,43 @@ uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
-                           float* norms, cudaStream_t stream, float* bounds) {
+                           float* norms, cudaStream_t stream, float* bounds, size_t tile_row0) {
   if (rows == 0) return cudaSuccess;
   const size_t threads = rows * 32;
   to_bf16_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(
-      src, ld_src, rows, dim, dp, static_cast<__nv_bfloat16*>(dst), norms, bounds);
+      src, ld_src, rows, dim, dp, static_cast<__nv_bfloat16*>(dst), norms, bounds, tile_row0);
   return cudaGetLastError();
 }
 
+size_t tc_tiled_bytes(size_t rows, uint32_t dp, bool fp8) {
+  return (rows + kTcRows - 1) / kTcRows * size_t(tc_chunks(dp, fp8)) * kRowChunkBytes;
+}
+
+cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t rows, uint32_t dp, uint32_t box_rows,
+                                bool fp8) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  if (box_rows == 0 || box_rows > uint32_t(kTcRows) || !base || rows == 0) return cudaErrorInvalidValue;
+  const cuuint64_t dims[2] = {fp8 ? 128u : uint64_t(kTcKChunk),
+                              (rows + kTcRows - 1) / kTcRows * tc_chunks(dp, fp8) * uint64_t(kTcRows)};
+  const cuuint64_t strides[1] = {128};  // one 128-byte chunk row after another
+  const cuuint32_t box[2] = {fp8 ? 128u : uint32_t(kTcKChunk), box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                        const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
-                          float* scale, float* norms, cudaStream_t stream) {
+                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0) {
   if (rows == 0) return cudaSuccess;
   if (dp8 % 16 != 0 || dp8 < dim) return cudaErrorInvalidValue;
   const size_t threads = rows * 32;
   to_fp8_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp8,
-                                                                     static_cast<uint8_t*>(dst), scale, norms);
+                                                                     static_cast<uint8_t*>(dst), scale, norms,
+                                                                     tile_row0);
   return cudaGetLastError();
 }
 

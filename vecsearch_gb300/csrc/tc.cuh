@@ -158,10 +158,20 @@ uint32_t tc_buffer_capacity(uint32_t kp);
 
 // Encodes a 2-D tensor map over rows x dp elements (bf16: row stride dp * 2 bytes, 64 x box_rows
 // box; fp8: dp bytes, 128 x box_rows box), 128-byte swizzle; box_rows <= 256 (128 for a query
-// block, kTcRows for a row tile, kTcRows / cluster for a multicast slice). The driver's encoder
-// is looked up through the runtime on first use.
+// block). The driver's encoder is looked up through the runtime on first use.
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows,
                           bool fp8 = false);
+
+// Operand copies of the rows are stored tile-major: for each tile of kTcRows rows, its 128-byte
+// chunks one after another, each chunk holding that chunk of all kTcRows rows (chunk c of row r
+// at byte ((r / kTcRows) * nkc + c) * kTcRows * 128 + (r % kTcRows) * 128). Every row-chunk box
+// the shortlist kernel loads is then one contiguous 32 KB span. Bytes for `rows` rows:
+size_t tc_tiled_bytes(size_t rows, uint32_t dp, bool fp8);
+// Tensor map over such a copy of `rows` rows: a (64 bf16 | 128 e4m3) x (tiles * nkc * kTcRows)
+// matrix of 128-byte chunk rows, box_rows per box (kTcRows, or kTcRows / cluster for a multicast
+// slice), 128-byte swizzle.
+cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t rows, uint32_t dp, uint32_t box_rows,
+                                bool fp8);
 // Clusters of `cluster` CTAs of the shortlist kernel that can be resident at once (0 on error).
 uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
 
@@ -174,9 +184,11 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
                                 cudaStream_t stream);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
 // When bounds != nullptr, raises bounds[0..3) to the rows' max |x~ - x|, max |x| and max |x~|
-// (x~ = the bf16 row; FP32 sums, not yet inflated for their rounding).
+// (x~ = the bf16 row; FP32 sums, not yet inflated for their rounding). With tile_row0 set, dst
+// is a tile-major copy (tc_tiled_bytes) and the rows are its rows tile_row0, tile_row0 + 1, ...
+constexpr size_t kRowMajor = ~size_t(0);
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
-                           float* norms, cudaStream_t stream, float* bounds = nullptr);
+                           float* norms, cudaStream_t stream, float* bounds = nullptr, size_t tile_row0 = kRowMajor);
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
 // Certified path: err[q] = the certificate's error bound E on |approximate - FP32 distance| for
 // query q (FP32 queries, row stride ldq, dp columns) over rows whose bf16 copies have the bounds
@@ -186,7 +198,8 @@ cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32
                                bool l2, float factor, float* margin, float* err, cudaStream_t stream);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
 // zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
+// With tile_row0 set, dst is a tile-major copy as in launch_to_bf16.
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
-                          float* scale, float* norms, cudaStream_t stream);
+                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0 = kRowMajor);
 
 }  // namespace vsg

@@ -57,12 +57,16 @@ extern "C" {
 /* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The rerank kernel bounds the
  * difference between each row's bf16 approximate distance and its FP32 distance (from the bf16
  * rounding of the query and the rows), and proves that no row outside the shortlist can enter
- * the top k; queries it cannot prove run the shortlist pass again with k' = 120, and those it
- * still cannot prove run in the streaming scan kernel. Results equal
- * VSG_METHOD_SKINNY bit for bit, with or without a filter. Method AUTO uses it for batches of at
- * least "tc_exact_min_batch" queries with k <= 32 (filtered ones from twice that, or from it when
- * the allowed rows are too many for the gather scan), or where the autotuner picked it. k > 120
- * runs the FP32 kernels. The call waits on its stream to read the uncertified queries. */
+ * the top k; the shortlist keeps each query's rows within "cert_margin" x E of its k-th best (at
+ * most k' = 120). Queries it cannot prove run the shortlist pass again with k' = 120 if the first
+ * pass used fewer (a tuned choice), and those it still cannot prove run in the streaming scan
+ * kernel. Results equal VSG_METHOD_SKINNY bit for bit, with or without a filter. Method AUTO uses
+ * it for unfiltered batches of at least "tc_exact_min_batch" queries with k <= 32, or where the
+ * autotuner picked it; for filtered batches (k <= 32) of 8+ queries whose size times the largest
+ * allowed fraction of their host masks is at least 0.35, or with too many allowed rows for the
+ * gather scan, and for every filtered batch of at least half "tc_exact_min_batch" (device-resident
+ * masks: from "tc_exact_min_batch", or twice it when the gather scan applies). k > 120 runs the
+ * FP32 kernels. The call waits on its stream to read the uncertified queries. */
 #define VSG_METHOD_TC_EXACT 5u
 /* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
  * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32

@@ -111,15 +111,20 @@ def test_auto_routes_large_batches(gpu_ready):
     assert q1 - q0 == 256
     gpu.search(q[:64], 10)  # below the threshold: FP32 kernels
     gpu.search(q, 64)  # k > 32: FP32 kernels
+    # Filtered: the certified path when (batch x largest allowed fraction) >= 0.35, from 8 queries,
+    # and for every filtered batch from half the threshold (64 queries).
     few = np.zeros(len(x), bool)
-    few[::100] = True
-    gpu.search(q[:200], 10, filter=few)  # 1 % allowed, 200 queries: the gather scan
-    assert gpu.tc_exact_stats()[0] == q1
+    few[::100] = True  # 1 % allowed
+    gpu.search(q[:32], 10, filter=few)  # 32 x 0.01 < 0.35: the gather scan
     wide = np.ones(len(x), bool)
-    _same(gpu.search(q[:200], 10, filter=wide), gpu.search(q[:200], 10, method="skinny", filter=wide))
-    assert gpu.tc_exact_stats()[0] == q1 + 200  # a wide filter takes the certified path
+    gpu.search(q[:4], 10, filter=wide)  # fewer than 8 queries: the scan kernel
+    assert gpu.tc_exact_stats()[0] == q1
+    _same(gpu.search(q[:48], 10, filter=few), gpu.search(q[:48], 10, method="skinny", filter=few))
+    assert gpu.tc_exact_stats()[0] == q1 + 48  # 48 x 0.01 >= 0.35
+    _same(gpu.search(q[:16], 10, filter=wide), gpu.search(q[:16], 10, method="skinny", filter=wide))
+    assert gpu.tc_exact_stats()[0] == q1 + 64  # a wide filter from 8 queries
     _same(gpu.search(q, 10, filter=few), gpu.search(q, 10, method="skinny", filter=few))
-    assert gpu.tc_exact_stats()[0] == q1 + 456  # from 256 queries any filter does
+    assert gpu.tc_exact_stats()[0] == q1 + 320  # from 64 queries any filter
 
 
 def test_tc_exact_filtered(gpu_ready):

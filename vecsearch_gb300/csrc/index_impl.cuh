@@ -666,14 +666,23 @@ struct vsg_index {
     tc_exact_second += n1;
   }
 
-  bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask, bool gather) const {
+  bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask, bool gather,
+                    double allowed = -1.0) const {
     if (k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
     if (method == VSG_METHOD_TC_EXACT) return true;
     if (method != VSG_METHOD_AUTO) return false;
-    // Filtered: the gather scan reads only the allowed rows of each query, so it wins for small
-    // allowed sets at moderate batch; from twice the threshold the shortlist pass, whose reads
-    // the whole batch shares, wins whatever the selectivity (measured at 1M x 384).
-    if (dmask) return (!gather || double(nq) >= 2 * tc_exact_min_batch) && double(nq) >= tc_exact_min_batch && k <= 32;
+    // Filtered: the gather scan reads only the allowed rows of each query, about 3.3 us per query
+    // plus 0.375 ns per (query, allowed row) at d = 384, while the shortlist pass costs about the
+    // same at any selectivity (0.2 ms at 16 queries over 1M rows). So with the largest allowed
+    // fraction f known, the certified path takes batches of 8+ where nq f >= 0.35, and every
+    // batch from half the threshold (measured at 1M x 384). Without f (device masks): from the
+    // threshold when the scan would not gather, from twice it otherwise.
+    if (dmask) {
+      if (k > 32) return false;
+      if (allowed >= 0.0)
+        return nq >= 8 && (double(nq) >= 0.5 * tc_exact_min_batch || (!gather) || double(nq) * allowed >= 0.35);
+      return (!gather || double(nq) >= 2 * tc_exact_min_batch) && double(nq) >= tc_exact_min_batch;
+    }
     if (force_kernel >= 0) return force_kernel == 2;
     if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
     return double(nq) >= tc_exact_min_batch && k <= 32;
@@ -805,16 +814,17 @@ struct vsg_index {
     (family == VSG_METHOD_BF16 ? tune_bf16 : tune_plain) = table;
   }
 
+  // allowed: the largest allowed fraction of the masks when known (host masks), else -1.
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
-               uint32_t method = VSG_METHOD_AUTO) {
+               uint32_t method = VSG_METHOD_AUTO, double allowed = -1.0) {
     // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
     const size_t mld = dmask && per_query ? mask_ld : 0;  // 0: one mask for every query
     if ((method == VSG_METHOD_BF16 || method == VSG_METHOD_FP8) && k <= size_t(vsg::kTcMaxShortlist)) {
       enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, false, 0, method == VSG_METHOD_FP8, dmask, mld);
       return;
     }
-    if (use_tc_exact(method, nq, k, dmask, gather)) {
+    if (use_tc_exact(method, nq, k, dmask, gather, allowed)) {
       enqueue_tc_exact(dq, ldq, nq, k, out_ids, out_dists, s, dmask, mld);
       return;
     }
@@ -942,16 +952,17 @@ struct vsg_index {
     const float* dq = stage_queries(host_q, nq);
     const uint32_t* dm = nullptr;
     bool gather = false;
+    double allowed = -1.0;
     if (host_mask) {
       const size_t words = per_query ? nq * mask_ld : ceil_div(n, 32);
       dm = stage_mask(host_mask, words);
-      gather = allowed_fraction(host_mask, per_query ? nq : 1, per_query ? mask_ld : ceil_div(n, 32)) <=
-               gather_max_fraction;
+      allowed = allowed_fraction(host_mask, per_query ? nq : 1, per_query ? mask_ld : ceil_div(n, 32));
+      gather = allowed <= gather_max_fraction;
     }
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
     if (method == VSG_METHOD_BF16 && !dm && k <= size_t(vsg::kTcMaxShortlist)) ensure_bf16();
-    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method);
+    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method, allowed);
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
     VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));

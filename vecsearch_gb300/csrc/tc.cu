@@ -309,15 +309,6 @@ __device__ __forceinline__ void tmem_wait32(uint32_t (&v)[32]) {
 }
 
 
-// One column: every lane gets its own query's score in that column.
-__device__ __forceinline__ uint32_t tmem_ld1(uint32_t taddr) {
-  uint32_t v;
-  __syncwarp();
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(v) : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(v) : : "memory");
-  return v;
-}
-
 // The same for 64 columns at once (two loads and two waits per tile).
 __device__ __forceinline__ void tmem_issue64(uint32_t taddr, uint32_t (&v)[64]) {
   __syncwarp();
@@ -332,6 +323,22 @@ __device__ __forceinline__ void tmem_wait64(uint32_t (&v)[64]) {
                : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]), "+r"(v[30]), "+r"(v[31]), "+r"(v[32]), "+r"(v[33]), "+r"(v[34]), "+r"(v[35]), "+r"(v[36]), "+r"(v[37]), "+r"(v[38]), "+r"(v[39]), "+r"(v[40]), "+r"(v[41]), "+r"(v[42]), "+r"(v[43]), "+r"(v[44]), "+r"(v[45]), "+r"(v[46]), "+r"(v[47]), "+r"(v[48]), "+r"(v[49]), "+r"(v[50]), "+r"(v[51]), "+r"(v[52]), "+r"(v[53]), "+r"(v[54]), "+r"(v[55]), "+r"(v[56]), "+r"(v[57]), "+r"(v[58]), "+r"(v[59]), "+r"(v[60]), "+r"(v[61]), "+r"(v[62]), "+r"(v[63])
                :
                : "memory");
+}
+
+// v[B + j] for a run-time j in [0, 32): a tree of selects over compile-time indices, so the
+// array stays in registers (an indexed read would move it to local memory).
+template <int B>
+__device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[64], uint32_t j) {
+  uint32_t t16[16], t8[8], t4[4], t2[2];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) t16[i] = (j & 16u) ? v[B + 16 + i] : v[B + i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t8[i] = (j & 8u) ? t16[8 + i] : t16[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t4[i] = (j & 4u) ? t8[4 + i] : t8[i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) t2[i] = (j & 2u) ? t4[2 + i] : t4[i];
+  return (j & 1u) ? t2[1] : t2[0];
 }
 
 template <int E, bool L2, bool F8>
@@ -676,18 +683,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 compact_lanes(__ballot_sync(kFull, cnt + 32 > cap), false);
                 const int cg = h * 2 + c;
                 const uint32_t c0 = r0 + uint32_t(cg) * 32;
-                // Columns some lane needs, in a rolled warp-uniform loop (the code stays small):
-                // the column is read again from TMEM and its lanes append.
-                while (cols) {
-                  const int j = __ffs(cols) - 1;
-                  cols &= cols - 1;
-                  const float raw = __uint_as_float(tmem_ld1(tbase + uint32_t(cg * 32 + j)));
-                  const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
-                  if ((bits[c] >> j) & 1u) {
+                // Each lane walks its own candidate columns; the scores are still in v, picked
+                // by a select tree. The loop runs as often as the busiest lane needs.
+                uint32_t mine = bits[c];
+                while (__any_sync(kFull, mine != 0u)) {
+                  const bool has = mine != 0u;
+                  const uint32_t j = has ? uint32_t(__ffs(mine) - 1) : 0u;
+                  mine &= mine - 1u;
+                  const float raw = __uint_as_float(c == 0 ? pick32<0>(v, j) : pick32<32>(v, j));
+                  if (has) {
+                    const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
                     const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
-                    if (nb_less(dist, c0 + uint32_t(j), thr_d, thr_i)) {
+                    if (nb_less(dist, c0 + j, thr_d, thr_i)) {
                       wd[size_t(lane) * cap + cnt] = dist;
-                      wi[size_t(lane) * cap + cnt] = c0 + uint32_t(j);
+                      wi[size_t(lane) * cap + cnt] = c0 + j;
                       ++cnt;
                     }
                   }

@@ -25,7 +25,8 @@ The base (1.536 GB) is larger than L2 (129 MB), so no L2 flush is needed between
 
 --impl reference times the reference's CPU path (oracle port, all host threads) on the
 same workload and prints the same JSON line with "impl": "reference".
---mode precision / serve / filtered run configs 4 / 5 / 3 on their own.
+--mode precision / serve / filtered run configs 4 / 5 / 3 on their own; --mode worker times the
+GPU shard worker (one-query Search calls from concurrent clients).
 """
 import argparse
 import json
@@ -75,7 +76,7 @@ def parse():
     ap.add_argument("--filter-targets", default="100,1000,10000,50000,100000,200000",
                     help="filtered mode: allowed-row counts to sweep")
     ap.add_argument("--filter-batch", type=int, default=16, help="filtered mode: queries per search")
-    ap.add_argument("--mode", default="plain", choices=["plain", "precision", "serve", "filtered"],
+    ap.add_argument("--mode", default="plain", choices=["plain", "precision", "serve", "filtered", "worker"],
                     help="precision: config 4 (BF16 shortlist + rerank) sweep instead of the default line")
     ap.add_argument("--big", action="store_true", help="precision mode: add the 4M x 384 base")
     return ap.parse_args()
@@ -598,8 +599,65 @@ def run_serve(a):
     print(json.dumps(line), flush=True)
 
 
+def run_worker(a):
+    """The GPU shard worker (vecsearch_gb300.shard_worker) behind its Searcher method bodies:
+    `clients` threads each send one-query Search requests back to back (encoded as search.proto's
+    SearchRequest, decoded replies), for --duration seconds per client count. The worker's batcher
+    gathers concurrent calls into one exact device search. Reports calls/s, latency percentiles
+    and the mean batch formed. gRPC transport is not included (the GPU image has no grpcio)."""
+    import threading
+    import torch
+    import vecsearch_gb300 as vsg
+    from vecsearch_gb300 import shard_worker as W
+    torch.cuda.set_device(0)
+    x, q = make_data(a)
+    idx = vsg.GpuBruteForceIndex(a.dim, "cosine" if a.metric == "ip" else "l2")
+    idx.add(x)
+    reqs = [W.encode_search_request(q[i], a.k, 64) for i in range(len(q))]
+    rows = []
+    for clients in (1, 16, 64, 256):
+        s = W.ShardSearcher(idx, offset=0, shard_id=0, max_batch=256, max_wait_ms=0.2)
+        for i in range(8):  # warm-up
+            s.search(reqs[i])
+        lat = [[] for _ in range(clients)]
+        stop = time.perf_counter() + a.duration
+        b0, c0 = s.batches, s.calls
+
+        def client(c):
+            i = c
+            while time.perf_counter() < stop:
+                t = time.perf_counter()
+                s.search(reqs[i % len(reqs)])
+                lat[c].append(time.perf_counter() - t)
+                i += clients
+
+        t0 = time.perf_counter()
+        ts = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        el = time.perf_counter() - t0
+        calls, batches = s.calls - c0, s.batches - b0
+        s.close()
+        allv = np.sort(np.concatenate([np.asarray(v) for v in lat])) * 1e3
+        rows.append({"clients": clients, "calls_per_s": round(calls / el, 1),
+                     "p50_ms": round(float(np.percentile(allv, 50)), 3),
+                     "p99_ms": round(float(np.percentile(allv, 99)), 3),
+                     "mean_batch": round(calls / max(batches, 1), 1)})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    print(json.dumps({"metric": "GPU shard worker: exact top-k Search calls/s and latency by concurrent clients",
+                      "unit": "calls/s", "data": "synthetic",
+                      "config": {"workload": f"one shard of {a.n:,} x {a.dim} rows, k = {a.k}, one query per call",
+                                 "batcher": "up to 256 calls, 0.2 ms window, method auto"},
+                      "results": rows}), flush=True)
+
+
 def main():
     a = parse()
+    if a.mode == "worker":
+        run_worker(a)
+        return
     if a.mode == "serve":
         run_serve(a)
         return

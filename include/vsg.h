@@ -180,8 +180,8 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
  * vsg_autotune times candidate schedules for each batch size (queries 0.9 x_i + 0.1 x_j of rows;
  * CUDA events, the mean over 3 different batches after a warm-up) and keeps the fastest per batch size:
  *   method VSG_METHOD_AUTO: streaming scan, tiled kernel or certified shortlist (VSG_METHOD_TC_EXACT),
- *     with 1x or 2x the row splits for the FP32 kernels or a first-pass shortlist of 80 or 120 for
- *     the certified path, used by
+ *     with 1x or 2x the row splits for the FP32 kernels (the certified path runs with k' = 120;
+ *     a table loaded from a file may name a narrower first pass), used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
  *     (0, 4096 or 16384; 0 = no sample pass) and how many CTAs share each row tile through a

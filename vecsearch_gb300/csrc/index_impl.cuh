@@ -406,12 +406,10 @@ struct vsg_index {
   }
 
   // Certified exact path: the list keeps the rows within each query's margin of its k-th best,
-  // up to k' entries; the widest k' (120) certifies the most queries. The autotuner also tries
-  // the narrower exact_shortlist_min(k).
+  // up to k' entries. The widest k' (120) certifies the most queries and costs about the same as
+  // a narrower one (the candidate buffers are the same size), so it is always the first pass;
+  // a table entry may still name a narrower one.
   static uint32_t exact_shortlist_size(size_t) { return uint32_t(vsg::kTcMaxShortlist); }
-  static uint32_t exact_shortlist_min(size_t k) {
-    return uint32_t(std::min<size_t>(vsg::kTcMaxShortlist, std::max<size_t>(4 * k, 80)));
-  }
 
   uint32_t shortlist_size(size_t k) const {
     const double want = std::max<double>(double(k), shortlist_oversample * double(k));
@@ -773,12 +771,11 @@ struct vsg_index {
           for (int kern : {0, 1, 2}) {
             if (kern == 1 && b < 8) continue;  // the tiled kernel's tile is 64 queries at least
             if (kern == 2 && (b < 8 || k > size_t(vsg::kTcMaxShortlist))) continue;
-            // FP32 kernels: 1x or 2x the row splits; certified path: first-pass shortlist size
-            // (the shortlist path sizes its own splits)
+            // FP32 kernels: 1x or 2x the row splits; the certified path sizes its own splits
             for (int o = 0; o < 2; ++o) {
               const double f = kern == 2 ? 1.0 : (o == 0 ? 1.0 : 2.0);
-              const int kp = kern == 2 ? (o == 0 ? int(exact_shortlist_min(k)) : int(vsg::kTcMaxShortlist)) : -1;
-              if (kern == 2 && o == 1 && kp == int(exact_shortlist_min(k))) continue;
+              const int kp = kern == 2 ? int(exact_shortlist_size(k)) : -1;
+              if (kern == 2 && o == 1) continue;
               force_kernel = kern;
               force_split = f;
               force_exact_kp = kp;

@@ -9,7 +9,8 @@ query to every worker and merges their lists by (distance, id).
 Here the shard's rows live in a :class:`GpuBruteForceIndex` (loaded straight from the same
 ``VSHNSW01`` file, or from any array), so every answer is the shard's exact top k. A worker receives
 one query per call; a batcher thread gathers the calls that arrive together into one GPU search
-(up to ``max_batch`` queries, waiting at most ``max_wait_ms`` for company), runs it with the
+(up to ``max_batch`` queries; while the previous batch held several calls it also waits up to
+``max_wait_ms`` for company, so a lone caller is not delayed), runs it with the
 largest k among them, and hands each call the first k of its row. Exact lists are ordered by
 (distance, id), so the first k of a top-K list is the top k: batching never changes an answer.
 
@@ -221,12 +222,15 @@ class ShardSearcher:
         self._thread.join()
 
     def _loop(self):
+        last = 1  # calls in the previous batch
         while not self._stop.is_set():
             first = self._q.get()
             if first is None:
                 break
             group = [first]
-            deadline = time.perf_counter() + self.max_wait
+            # Wait for company only under load (the previous batch had several calls): a lone
+            # caller is searched at once.
+            deadline = time.perf_counter() + (self.max_wait if last > 1 else 0.0)
             while len(group) < self.max_batch:
                 left = deadline - time.perf_counter()
                 try:
@@ -237,6 +241,7 @@ class ShardSearcher:
                     self._stop.set()
                     break
                 group.append(item)
+            last = len(group)
             self._run(group)
 
     def _run(self, group):

@@ -170,3 +170,26 @@ def test_fp8_odd_shapes(gpu_ready):
             np.testing.assert_array_equal(fd, pd)
         else:
             assert vsg.recall_at_k(fi, pi, k) >= 0.95
+
+
+@pytest.mark.parametrize("sample_rows", [0, 16384])
+def test_merge_gather_and_overflow(gpu_ready, sample_rows):
+    # k = 100 (k' = 120) over ~130 splits of 1,536 rows. Without a sample pass every split keeps
+    # 120 rows, ~15,700 per query, more than the merge's gather staging (4,096): the list merge
+    # runs. With the 16K-row sample, ~1,200 rows per query survive: the gather merge sorts ten
+    # 128-entry chunks over eight warps. Both must give the same answers as the scan kernel.
+    vsg = gpu_ready
+    x, q = _data(200_000, 8, 64, 128, True, 85)
+    gpu = vsg.GpuBruteForceIndex(64, "cosine")
+    gpu.add(x)
+    gpu.set_tunable("sample_rows", sample_rows)
+    pi, pd = gpu.search(q, 100, method="skinny")
+    ei, ed = gpu.search(q, 100, method="tc_exact")
+    np.testing.assert_array_equal(ei, pi)
+    np.testing.assert_array_equal(ed.view(np.uint32), pd.view(np.uint32))
+    bi, bd = gpu.search(q, 100, method="bf16")
+    same = (bi == pi).all(1)
+    assert same.mean() >= 0.75, same.mean()
+    np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))
+    gi, _ = O.fp64_topk(x, q, 100, "ip")
+    assert vsg.recall_at_k(bi, gi, 100) >= 0.99

@@ -7,13 +7,19 @@ L2-normalised; 10,000 queries from the same mixture; inner product (cosine dista
 1 - q.x); k = 10. Synthetic data stands in for the reference's tweet embeddings
 (same 1M x 384 cosine shape).
 
-A step is one exact search of one batch (default batch 1: the HBM-bound case).
+A step is one exact search of one batch (default batch 1: the HBM-bound case). Method auto
+runs it on the certified path on an index this large: a bf16 tensor-core pass over a bf16 copy
+of the rows (half the FP32 bytes) keeps each query's candidates, an FP32 rerank computes their
+exact distances with the scan kernel's arithmetic and proves that no other row can enter the
+top k; unproven queries run in the FP32 scan kernel. Results equal the FP32 scan's bit for bit.
   value      queries/s with queries and results resident in HBM (device API), timed
              with CUDA events on the launching stream over exactly --steps steps.
   e2e        the same through the public host API (pinned host queries in, host
              results out, both copies inside the timed region).
-  roofline   the scan kernel: algorithmic bytes (base + queries + results) per launch
-             / its CUDA-event time, against the measured HBM copy bandwidth.
+  roofline   the dominant kernel of the timed steps (the bf16 shortlist pass, or the FP32 scan
+             kernel): algorithmic bytes (the rows once, in the type it reads, plus queries) per
+             launch / its CUDA-event time, against the measured HBM copy bandwidth.
+  gpu_launches  this index's kernel launches in the timed steps (counted by the library).
   cpu_baseline  the reference's CPU algorithm (oracle port of brute_force.cpp
              search_batch) on this host's cores, on a bounded sample.
   autotune   the schedule tables vsg_autotune picked for the sweep's batch sizes (taken after
@@ -46,7 +52,11 @@ sys.path.insert(0, ROOT)
 # The 1M-row entry is the 262,144-row capture (profiles/scan_kernel_1Mx384_b1.md: 402.69 MB read +
 # 3.31 MB written per launch) scaled by rows scanned (x 1,000,000 / 262,144); reads equal the
 # algorithmic bytes there, so traffic grows in proportion to the rows.
-MEASURED_TRAFFIC = {(1_000_000, 384, 1, 10, "ip"): 1_548_800_000}
+MEASURED_TRAFFIC = {(1_000_000, 384, 1, 10, "ip"): 1_548_800_000,
+                    # the certified path's shortlist main pass at batch 1: the 262,144-row capture
+                    # (profiles/tc_shortlist_kernel_262Kx384_b1_dram.md: 201.40 MB read + 3.15 MB
+                    # written per launch, reads = the bf16 rows once) scaled by rows
+                    ("tc", 1_000_000, 384, 1, 10, "ip"): 780_332_031}
 
 
 def parse():
@@ -68,8 +78,9 @@ def parse():
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="sweep with the built-in schedule rules")
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
-    ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16"],
-                    help="kernel of the main timed line (auto: the plain FP32 path by batch size)")
+    ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16", "tc_exact"],
+                    help="path of the main timed line (auto: the certified path on a large index, "
+                         "else the FP32 kernels by batch size)")
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000", help="serve mode: offered queries/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serve mode: seconds of arrivals per rate")
     ap.add_argument("--plain-max-rate", type=int, default=10000, help="serve mode: highest rate for the plain path")
@@ -206,8 +217,10 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, method="auto"):
-    """Device-resident search: (ms total over `steps`, scan ms total, merge ms total, launches)."""
+def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, method="auto", out=None):
+    """Device-resident search: (ms total over `steps`, scan ms total, merge ms total, searches
+    profiled). With `out` (a dict): out["kernels"] = this index's kernel launches in the timed
+    steps, out["tc_exact"] = whether they ran the certified path."""
     k = a.k
     out_i = torch.empty((batch, k), dtype=torch.int32, device=qd.device)
     out_d = torch.empty((batch, k), dtype=torch.float32, device=qd.device)
@@ -226,6 +239,9 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, meth
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
+    if out is not None:
+        tq0 = idx.tc_exact_stats()[0]
+        k0 = idx.kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -236,6 +252,9 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, meth
     if dist is not None:
         dist.barrier()
     ms = e0.elapsed_time(e1)
+    if out is not None:
+        out["kernels"] = idx.kernel_launches() - k0
+        out["tc_exact"] = idx.tc_exact_stats()[0] > tq0
     scan_ms, merge_ms, launches = idx.profile_read()
     idx.profile(False)
     idx.sync()
@@ -304,8 +323,9 @@ def run_ours(a):
     stream = torch.cuda.current_stream()
 
     sampler = ClockSampler(local)
+    info = {}
     ms, scan_ms, merge_ms, launches = time_device(idx, torch, qd, a, a.batch, a.steps, a.warmup, stream, dist,
-                                                  method=a.method)
+                                                  method=a.method, out=info)
     clocks = sampler.stop()
     if dist is not None:
         t = torch.tensor([ms], device=f"cuda:{local}")
@@ -335,17 +355,26 @@ def run_ours(a):
         e2e_s = float(t.item())
     e2e_qps = world * a.batch * e2e_steps / e2e_s
 
-    # roofline of the scan kernel
+    # roofline of the dominant kernel of the timed steps: the certified path's bf16 shortlist pass
+    # (method auto on a large index), else the FP32 scan kernel
     scan_avg_ms = scan_ms / max(launches, 1)
-    alg_bytes = a.n * a.dim * 4 + a.batch * a.dim * 4 + a.batch * a.k * 8
     peak, peak_kind = peaks()
+    if info.get("tc_exact"):
+        alg_bytes = a.n * a.dim * 2 + a.batch * a.dim * 2  # the bf16 rows once, the bf16 queries
+        traffic = MEASURED_TRAFFIC.get(("tc", a.n, a.dim, a.batch, a.k, a.metric))
+        kernel = "tc_shortlist_kernel (bf16 tcgen05 pass over the rows; certified exact path)"
+        dtype = "bf16 products, f32 accumulation and results"
+    else:
+        alg_bytes = a.n * a.dim * 4 + a.batch * a.dim * 4 + a.batch * a.k * 8
+        traffic = MEASURED_TRAFFIC.get((a.n, a.dim, a.batch, a.k, a.metric))
+        kernel = "scan_kernel (fused FP32 scan + top-k)"
+        dtype = "f32"
     achieved = alg_bytes / (scan_avg_ms / 1e3) / 1e9
-    traffic = MEASURED_TRAFFIC.get((a.n, a.dim, a.batch, a.k, a.metric))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                "kernel": "scan_kernel (fused FP32 scan + top-k)", "kernel_ms_avg": round(scan_avg_ms, 5),
-                "merge_ms_avg": round(merge_ms / max(launches, 1), 5)}
+                "kernel": kernel, "kernel_ms_avg": round(scan_avg_ms, 5),
+                "after_kernel_ms_avg": round(merge_ms / max(launches, 1), 5)}
 
     extra = {}
     bf16_peak = peaks_bf16()
@@ -363,11 +392,17 @@ def run_ours(a):
             if b > q.shape[0]:
                 continue
             st = max(3, min(300, int(3e4 / b)))
-            ms_b, scan_b, _, l_b = time_device(idx, torch, qd, a, b, st, 3, stream)
+            info_b = {}
+            ms_b, scan_b, _, l_b = time_device(idx, torch, qd, a, b, st, 3, stream, out=info_b)
             flops = 2.0 * a.n * a.dim * b
+            row_bytes = a.n * a.dim * (2 if info_b.get("tc_exact") else 4)  # rows read by the auto path
             row = {"batch": b, "qps": round(b * st / (ms_b / 1e3), 1), "ms_per_batch": round(ms_b / st, 4),
-                   "kernel_gbs": round((a.n * a.dim * 4) / (scan_b / l_b / 1e3) / 1e9, 1),
+                   "auto_path": "tc_exact" if info_b.get("tc_exact") else "fp32",
+                   "kernel_gbs": round(row_bytes / (scan_b / l_b / 1e3) / 1e9, 1),
                    "kernel_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)}
+            if b == 1:
+                ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method="skinny")
+                row["skinny_qps"] = round(b * max(3, st // 2) / (ms_m / 1e3), 1)
             if 8 <= b <= 256:  # both plain kernels near the auto crossover
                 for m in ("skinny", "tiled"):
                     ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method=m)
@@ -385,7 +420,7 @@ def run_ours(a):
             row["kernel_frac_hbm"] = round(row["kernel_gbs"] / peak, 4)
             row["kernel_frac_fp32"] = round(row["kernel_tflops"] / 80.5, 4)
             row["bf16_tc_frac"] = round(row["bf16_tc_tflops"] / bf16_peak, 4)
-            if b >= 8:  # certified exact tensor-core path: the scan kernel's results, bit for bit
+            if True:  # certified exact tensor-core path: the scan kernel's results, bit for bit
                 q0, s0, f0 = idx.tc_exact_stats()
                 ms_e, _, _, _ = time_device(idx, torch, qd, a, b, sb, 3, stream, method="tc_exact")
                 q1, s1, f1 = idx.tc_exact_stats()
@@ -421,12 +456,12 @@ def run_ours(a):
             "metric": f"exact top-{a.k} QPS at {a.n // 1000}Kx{a.dim}", "value": round(qps, 2),
             "unit": "queries/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": round(ms / a.steps, 5), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(workload(a),
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": dict(workload(a),
                                                                                      parallelism=f"replicas{world}"),
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 2), "unit": "queries/s", "h2d_bytes_per_step": a.batch * a.dim * 4,
                     "d2h_bytes_per_step": a.batch * a.k * 8, "steps": e2e_steps},
-            "gpu_launches": int(launches) * 2, "clocks": clocks,
+            "gpu_launches": int(info.get("kernels", 0)), "clocks": clocks,
         }
         line.update(extra)
         print(json.dumps(line), flush=True)

@@ -58,15 +58,15 @@ extern "C" {
  * difference between each row's bf16 approximate distance and its FP32 distance (from the bf16
  * rounding of the query and the rows), and proves that no row outside the shortlist can enter
  * the top k; the shortlist keeps each query's rows within "cert_margin" x E of its k-th best (at
- * most k' = 120). Queries it cannot prove run the shortlist pass again with k' = 120 if the first
- * pass used fewer (a tuned choice), and those it still cannot prove run in the streaming scan
- * kernel. Results equal VSG_METHOD_SKINNY bit for bit, with or without a filter. Method AUTO uses
- * it for unfiltered batches of at least "tc_exact_min_batch" queries with k <= 32, or where the
- * autotuner picked it; for filtered batches (k <= 32) of 8+ queries whose size times the largest
+ * most k' = 120). Queries it cannot prove run in the streaming scan kernel, launched on the
+ * device's own count of them (nothing waits on the host). Results equal VSG_METHOD_SKINNY bit for
+ * bit, with or without a filter. Method AUTO uses it for unfiltered batches (k <= 32) of at least
+ * "tc_exact_min_batch" queries, or of any size on an index of at least "tc_exact_min_elements",
+ * or where the autotuner picked it; for filtered batches (k <= 32) of 8+ queries whose size times the largest
  * allowed fraction of their host masks is at least 0.35, or with too many allowed rows for the
  * gather scan, and for every filtered batch of at least half "tc_exact_min_batch" (device-resident
  * masks: from "tc_exact_min_batch", or twice it when the gather scan applies). k > 120 runs the
- * FP32 kernels. The call waits on its stream to read the uncertified queries. */
+ * FP32 kernels. */
 #define VSG_METHOD_TC_EXACT 5u
 /* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
  * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32
@@ -167,7 +167,12 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   "tc_exact_min_batch" (default 128): method "auto" sends unfiltered batches of at least this
  *   many queries (k <= 32) to VSG_METHOD_TC_EXACT unless the autotuner decided otherwise.
  *   "sample_rows" (default 16384): rows the tensor-core paths score first, per query, for a
- *   starting threshold (batches of 8+ queries, unless tuned per batch size).
+ *   starting threshold (batches of 8+ queries; at most 4096 for smaller batches; unless tuned
+ *   per batch size).
+ *   "tc_exact_min_elements" (default 2^27): unfiltered batches below "tc_exact_min_batch" (k <=
+ *   32), down to one query, take VSG_METHOD_TC_EXACT under method "auto" when the index holds at
+ *   least this many elements (rows x padded dim): reading the bf16 copy (half the bytes) then
+ *   saves more than the shortlist path's fixed costs.
  *   "cert_margin" (default 1.3, >= 1): VSG_METHOD_TC_EXACT keeps, per query, the rows within
  *   cert_margin x E of its k-th best approximate distance (E: the certificate's bound on
  *   |approximate - FP32 distance|). A smaller value keeps fewer rows; a query whose k-th FP32
@@ -199,9 +204,15 @@ int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_
 int vsg_autotune_save(vsg_index* index, const char* path);
 int vsg_autotune_load(vsg_index* index, const char* path);
 
-/* Certified exact path counters since the index was created: queries searched, queries that
- * needed the second shortlist pass (k' = 120), and queries that ran in the scan kernel. */
+/* Certified exact path counters since the index was created: queries searched, queries the
+ * shortlist pass could not certify, and queries that ran in the scan kernel (the same queries:
+ * the one shortlist pass runs with k' = 120). The uncertified count is kept on the device, so
+ * this call waits for the index's queued work. */
 int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* second, uint64_t* fallbacks);
+
+/* Kernels this index has launched since it was created (searches, conversions; not the
+ * serving loop's graphs), for benchmarks that report their launch count. */
+int vsg_kernel_launches(vsg_index* index, uint64_t* launches);
 
 /* Kernel timing (new; the reference has none). While enabled, every search records CUDA events
  * on its stream around the scan kernel and around the merge kernel. vsg_profile_read waits for

@@ -228,9 +228,16 @@ class GpuBruteForceIndex:
     def load_tuning(self, path):
         _native.check(_native.lib().vsg_autotune_load(self._h, str(path).encode()))
 
+    def kernel_launches(self):
+        """Kernels this index has launched since it was created (searches and conversions)."""
+        v = ctypes.c_uint64()
+        _native.check(_native.lib().vsg_kernel_launches(self._h, ctypes.byref(v)))
+        return v.value
+
     def tc_exact_stats(self):
-        """(queries searched by the certified exact path, queries that needed its second shortlist
-        pass, queries it ran in the scan kernel) since the index was created."""
+        """(queries searched by the certified exact path, queries its shortlist pass could not
+        certify, queries it ran in the scan kernel) since the index was created; the last two are
+        the same queries. Waits for the index's queued work."""
         q, s2, f = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         _native.check(_native.lib().vsg_tc_exact_stats(self._h, ctypes.byref(q), ctypes.byref(s2), ctypes.byref(f)))
         return q.value, s2.value, f.value

@@ -265,6 +265,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "sample_rows") {
       if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("sample_rows must be in [0, 2^20]");
       h->sample_rows = value;
+    } else if (nm == "tc_exact_min_elements") {
+      if (!(value >= 0.0)) throw std::invalid_argument("tc_exact_min_elements must be >= 0");
+      h->tc_exact_min_elements = value;
     } else if (nm == "cert_margin") {
       if (!(value >= 1.0 && value <= 100.0)) throw std::invalid_argument("cert_margin must be in [1, 100]");
       h->cert_margin = value;
@@ -285,6 +288,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "sample_rows") *value = h->sample_rows;
     else if (nm == "tc_exact_min_batch") *value = h->tc_exact_min_batch;
     else if (nm == "cert_margin") *value = h->cert_margin;
+    else if (nm == "tc_exact_min_elements") *value = h->tc_exact_min_elements;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }
@@ -385,9 +389,19 @@ int vsg_tc_exact_stats(vsg_index* h, uint64_t* queries, uint64_t* second, uint64
   if (!h || !queries || !second || !fallbacks) return fail(VSG_ERR_INVALID, "index or output is NULL");
   return guarded([&] {
     std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    const uint64_t scanned = h->tc_stats_sync();
     *queries = h->tc_exact_queries;
-    *second = h->tc_exact_second;
-    *fallbacks = h->tc_exact_fallbacks;
+    *second = scanned;  // uncertified after the one shortlist pass (k' = 120 is the first pass)
+    *fallbacks = scanned;
+  });
+}
+
+int vsg_kernel_launches(vsg_index* h, uint64_t* launches) {
+  if (!h || !launches) return fail(VSG_ERR_INVALID, "index or output is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    *launches = h->kernel_launches;
   });
 }
 

@@ -136,7 +136,9 @@ struct vsg_index {
   // queries ([count][ids]), their gathered queries and FP32 results.
   DeviceBuffer xbound, fails, fids, fq, fout, fmask;
   double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
-  uint64_t tc_exact_queries = 0, tc_exact_second = 0, tc_exact_fallbacks = 0;
+  uint64_t tc_exact_queries = 0;  // queries sent to the certified path
+  DeviceBuffer tcstats;            // device tally of its uncertified queries (scan fallbacks)
+  uint64_t kernel_launches = 0;    // this index's kernel launches (vsg_kernel_launches)
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_cert_margin)
   size_t bf16_rows = 0;
@@ -166,6 +168,9 @@ struct vsg_index {
   // method "bf16": rows sampled for the starting thresholds (0: no sample pass) when nothing
   // else is tuned for the batch size; batches under 8 queries skip it.
   double sample_rows = 16384;
+  // method "auto": unfiltered batches below tc_exact_min_batch take the certified path when the
+  // index holds at least this many elements (rows x padded dim; 2^27 is ~350K rows at d = 384).
+  double tc_exact_min_elements = 134217728.0;
   // method "tc_exact": rows within cert_margin x E of a query's k-th best are kept (E: the
   // certificate's error bound). Any value >= 1 gives exact results; it trades kept rows against
   // queries left uncertified.
@@ -324,9 +329,11 @@ struct vsg_index {
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     VSG_CUDA(vsg::launch_tiled(a, metric == VSG_METRIC_L2, dim3(unsigned(nqb), a.nsplit), s));
+    ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), a.nsplit, uint32_t(k)};
     VSG_CUDA(vsg::launch_merge(m, s));
+    ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
@@ -343,6 +350,7 @@ struct vsg_index {
     VSG_CUDA(vsg::launch_to_bf16(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dp),
                                  uint32_t(dp), xb.get(), static_cast<float*>(xnorm.get()) + keep, stream,
                                  static_cast<float*>(xbound.get()), keep));
+    ++kernel_launches;
     VSG_CUDA(cudaStreamSynchronize(stream));
     bf16_rows = n;
   }
@@ -361,6 +369,7 @@ struct vsg_index {
     VSG_CUDA(vsg::launch_to_fp8(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dim), d8,
                                 x8.get(), static_cast<float*>(x8scale.get()) + keep,
                                 static_cast<float*>(x8norm.get()) + keep, stream, keep));
+    ++kernel_launches;
     VSG_CUDA(cudaStreamSynchronize(stream));
     fp8_rows = n;
     if (xmap8_base != x8.get() || xmap8_rows != n) {
@@ -445,11 +454,13 @@ struct vsg_index {
       q8scale.reserve(nq * sizeof(float), 0, stream);
       VSG_CUDA(vsg::launch_to_fp8(dq, ldq, nq, uint32_t(dim), uint32_t(dpo), q8.get(),
                                   static_cast<float*>(q8scale.get()), static_cast<float*>(qnorm.get()), s));
+      ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, uint32_t(vsg::kTcQueries), true));
     } else {
       qb.reserve(nq * dp * 2, 0, stream);
       VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
                                    static_cast<float*>(qnorm.get()), s));
+      ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp, uint32_t(vsg::kTcQueries)));
       ensure_xmap();
     }
@@ -482,6 +493,7 @@ struct vsg_index {
                                        static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
                                        float(cert_margin), static_cast<float*>(qmargin.get()),
                                        static_cast<float*>(qmargin.get()) + nq, s));
+      ++kernel_launches;
       a.margin = static_cast<const float*>(qmargin.get());
       a.kk = uint32_t(k);
     }
@@ -509,14 +521,15 @@ struct vsg_index {
     a.part_n = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 8);
     a.status = status_word();
     Timing* tm = profiling ? next_timing() : nullptr;
-    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     // Batches first score a sample of rows (whole tiles at the head of every split; 16K rows for
-    // 8+ queries unless tuned) and start each query at the k'-th best sampled distance, so the
+    // 8+ queries, 4K below, unless tuned) and start each query at the k'-th best sampled distance, so the
     // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
+    // (smaller batches sample at most 4K rows: the pass costs the same per query, and without it
+    // every row is a candidate until the first compactions)
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
-                         : nq >= 8 ? size_t(sample_rows) : 0;
+                         : nq >= 8 ? size_t(sample_rows) : std::min<size_t>(size_t(sample_rows), 4096);
     if (srows > 0 && tiles_per_split > 1) {
       vsg::TcArgs sa = a;
       uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
@@ -538,12 +551,16 @@ struct vsg_index {
       sa.sample_tiles = st;
       sa.gthr = nullptr;
       VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s));
+      ++kernel_launches;
       // (with margins: the k-th best sampled distance plus the margin)
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
                                          margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin));
+      ++kernel_launches;
       a.thr_init = static_cast<const float*>(thr.get());
     }
+    if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));  // the profile times the main pass alone
     VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s));
+    ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     float* cd = static_cast<float*>(cand.get());
     uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
@@ -554,6 +571,7 @@ struct vsg_index {
       m.kk = uint32_t(k);
     }
     VSG_CUDA(vsg::launch_merge(m, s));
+    ++kernel_launches;
     vsg::RerankArgs r{};
     r.x = static_cast<const float*>(x.get());
     r.q = dq;
@@ -576,92 +594,70 @@ struct vsg_index {
       r.fail_list = r.fail_count + 1;
     }
     VSG_CUDA(vsg::launch_rerank(r, s));
+    ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
   // Exact top-k through the shortlist. Queries whose result the rerank kernel cannot certify (see
-  // RerankArgs) run the shortlist pass again with the largest shortlist (k' = 120), and those
-  // still uncertified run in the streaming scan kernel, so results equal method skinny bit for
-  // bit. Waits on `s` after each stage to read the uncertified queries.
+  // RerankArgs) run in the streaming scan kernel, so results equal method skinny bit for bit.
+  // Nothing waits on the host: the rerank leaves the uncertified queries' count and indices on
+  // the device, and the fallback launches (gather, scan, scatter) are sized for all nq queries,
+  // their blocks past that count returning at once. A tally of uncertified queries stays on the
+  // device (tc_stats_sync reads it).
   void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                         cudaStream_t s, const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
     fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
-    auto read_fails = [&](size_t count) {
-      uint32_t nf = 0;
-      VSG_CUDA(cudaMemcpyAsync(&nf, fails.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-      VSG_CUDA(cudaStreamSynchronize(s));
-      if (nf > count) throw std::runtime_error("certification list overflow");
-      std::vector<uint32_t> ids(nf);
-      if (nf) {
-        VSG_CUDA(cudaMemcpyAsync(ids.data(), static_cast<uint32_t*>(fails.get()) + 1, nf * sizeof(uint32_t),
-                                 cudaMemcpyDeviceToHost, s));
-        VSG_CUDA(cudaStreamSynchronize(s));
-      }
-      return ids;
-    };
-    // First-pass shortlist: tuned per batch size (a wider one can spare the second pass).
+    tcstats.reserve(sizeof(unsigned long long), 0, stream);
+    // Shortlist cap: a tuned entry may name one; else 120, which certifies the most queries.
     const TuneEntry* te = dmask ? nullptr : lookup(tune_plain, nq);
     uint32_t kp1 = force_exact_kp > 0 ? uint32_t(force_exact_kp) : te && te->kernel == 2 ? te->exact_kp : 0u;
     kp1 = kp1 ? std::max<uint32_t>(std::min<uint32_t>(kp1, uint32_t(vsg::kTcMaxShortlist)), uint32_t(k))
               : exact_shortlist_size(k);
     VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
     enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);
-    std::vector<uint32_t> f1 = read_fails(nq);
     tc_exact_queries += nq;
-    if (f1.empty()) return;
-    // Stage 2: the uncertified queries, gathered, with k' = 120.
-    const size_t n1 = f1.size();
-    fids.reserve(2 * nq * sizeof(uint32_t), 0, stream);
-    uint32_t* d_f1 = static_cast<uint32_t*>(fids.get());
-    uint32_t* d_f2 = d_f1 + nq;
-    VSG_CUDA(cudaMemcpyAsync(d_f1, f1.data(), n1 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    fq.reserve(2 * n1 * dp * sizeof(float), 0, stream);
-    fout.reserve(2 * n1 * k * 8, 0, stream);
+    const uint32_t* d_count = static_cast<const uint32_t*>(fails.get());
+    const uint32_t* d_list = d_count + 1;
+    fq.reserve(nq * dp * sizeof(float), 0, stream);
+    fout.reserve(nq * k * 8, 0, stream);
     float* q1 = static_cast<float*>(fq.get());
-    float* q2 = q1 + n1 * dp;
     uint32_t* oi1 = static_cast<uint32_t*>(fout.get());
-    float* od1 = reinterpret_cast<float*>(oi1 + n1 * k);
-    uint32_t* oi2 = reinterpret_cast<uint32_t*>(od1 + n1 * k);
-    float* od2 = reinterpret_cast<float*>(oi2 + n1 * k);
-    VSG_CUDA(vsg::launch_gather_rows(q1, dq, ldq, uint32_t(dp), d_f1, uint32_t(n1), s));
+    float* od1 = reinterpret_cast<float*>(oi1 + nq * k);
+    VSG_CUDA(vsg::launch_gather_rows(q1, dq, ldq, uint32_t(dp), d_list, uint32_t(nq), s, d_count));
+    ++kernel_launches;
     // Per-query masks follow their queries (a shared mask stays as it is).
     const uint32_t* m1 = dmask;
-    uint32_t* m2 = nullptr;
     if (dmask && mask_ld) {
-      fmask.reserve(2 * n1 * mask_ld * sizeof(uint32_t), 0, stream);
+      fmask.reserve(nq * mask_ld * sizeof(uint32_t), 0, stream);
       uint32_t* g1 = static_cast<uint32_t*>(fmask.get());
-      m2 = g1 + n1 * mask_ld;
       VSG_CUDA(vsg::launch_gather_rows(reinterpret_cast<float*>(g1), reinterpret_cast<const float*>(dmask), mask_ld,
-                                       uint32_t(mask_ld), d_f1, uint32_t(n1), s));
+                                       uint32_t(mask_ld), d_list, uint32_t(nq), s, d_count));
+      ++kernel_launches;
       m1 = g1;
     }
-    std::vector<uint32_t> f2;
-    if (kp1 < uint32_t(vsg::kTcMaxShortlist)) {
-      VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
-      enqueue_bf16(q1, dp, n1, k, oi1, od1, s, true, uint32_t(vsg::kTcMaxShortlist), false, m1, mask_ld);
-      f2 = read_fails(n1);
-    } else {
-      f2.resize(n1);
-      for (size_t j = 0; j < n1; ++j) f2[j] = uint32_t(j);
+    // The scan kernel's masked full scan (its gather mode gives the same results); not profiled.
+    const bool prof = profiling;
+    profiling = false;
+    try {
+      enqueue(q1, dp, nq, k, m1, dmask && mask_ld, mask_ld, false, oi1, od1, s, VSG_METHOD_SKINNY, -1.0, d_count);
+    } catch (...) {
+      profiling = prof;
+      throw;
     }
-    // Stage 3: what is still uncertified, in the scan kernel.
-    if (!f2.empty()) {
-      const size_t n2 = f2.size();
-      VSG_CUDA(cudaMemcpyAsync(d_f2, f2.data(), n2 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-      VSG_CUDA(vsg::launch_gather_rows(q2, q1, dp, uint32_t(dp), d_f2, uint32_t(n2), s));
-      const uint32_t* mm = m1;
-      if (dmask && mask_ld) {
-        VSG_CUDA(vsg::launch_gather_rows(reinterpret_cast<float*>(m2), reinterpret_cast<const float*>(m1), mask_ld,
-                                         uint32_t(mask_ld), d_f2, uint32_t(n2), s));
-        mm = m2;
-      }
-      // The scan kernel's masked full scan (its gather mode gives the same results).
-      enqueue(q2, dp, n2, k, mm, dmask && mask_ld, mask_ld, false, oi2, od2, s, VSG_METHOD_SKINNY);
-      VSG_CUDA(vsg::launch_scatter_results(oi1, od1, oi2, od2, uint32_t(k), d_f2, uint32_t(n2), s));
-      tc_exact_fallbacks += n2;
-    }
-    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi1, od1, uint32_t(k), d_f1, uint32_t(n1), s));
-    tc_exact_second += n1;
+    profiling = prof;
+    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi1, od1, uint32_t(k), d_list, uint32_t(nq), s, d_count,
+                                         static_cast<unsigned long long*>(tcstats.get())));
+    ++kernel_launches;
+  }
+
+  // Queries of the certified path that the scan kernel answered (waits for the index's work).
+  uint64_t tc_stats_sync() {
+    if (!tcstats.get()) return 0;
+    unsigned long long v = 0;
+    VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
+    VSG_CUDA(cudaMemcpyAsync(&v, tcstats.get(), sizeof(v), cudaMemcpyDeviceToHost, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    return uint64_t(v);
   }
 
   bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask, bool gather,
@@ -683,7 +679,11 @@ struct vsg_index {
     }
     if (force_kernel >= 0) return force_kernel == 2;
     if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
-    return double(nq) >= tc_exact_min_batch && k <= 32;
+    if (k > 32) return false;
+    // Large batches amortise the shortlist path's fixed costs at any index size; smaller ones,
+    // down to one query, when the index is large enough that reading half the bytes (the bf16
+    // copy instead of the FP32 rows) saves more than those costs (about 30 us).
+    return double(nq) >= tc_exact_min_batch || double(n) * double(dp) >= tc_exact_min_elements;
   }
 
   bool use_tiled(uint32_t method, size_t nq, const uint32_t* dmask) const {
@@ -726,6 +726,7 @@ struct vsg_index {
     } else {  // queries near the index's rows (0.9 x_i + 0.1 x_j; none coincides with a row)
       VSG_CUDA(vsg::launch_midpoint_rows(static_cast<float*>(qbuf.get()), static_cast<const float*>(x.get()),
                                          uint32_t(dp), uint32_t(n), uint32_t(qrows), stream));
+      ++kernel_launches;
     }
     cudaEvent_t e0, e1;
     VSG_CUDA(cudaEventCreate(&e0));
@@ -770,7 +771,7 @@ struct vsg_index {
         } else {
           for (int kern : {0, 1, 2}) {
             if (kern == 1 && b < 8) continue;  // the tiled kernel's tile is 64 queries at least
-            if (kern == 2 && (b < 8 || k > size_t(vsg::kTcMaxShortlist))) continue;
+            if (kern == 2 && k > size_t(vsg::kTcMaxShortlist)) continue;
             // FP32 kernels: 1x or 2x the row splits; the certified path sizes its own splits
             for (int o = 0; o < 2; ++o) {
               const double f = kern == 2 ? 1.0 : (o == 0 ? 1.0 : 2.0);
@@ -812,9 +813,10 @@ struct vsg_index {
   }
 
   // allowed: the largest allowed fraction of the masks when known (host masks), else -1.
+  // nq_dev: scan path only, a device count of the queries to search (at most nq).
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
-               uint32_t method = VSG_METHOD_AUTO, double allowed = -1.0) {
+               uint32_t method = VSG_METHOD_AUTO, double allowed = -1.0, const uint32_t* nq_dev = nullptr) {
     // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
     const size_t mld = dmask && per_query ? mask_ld : 0;  // 0: one mask for every query
     if ((method == VSG_METHOD_BF16 || method == VSG_METHOD_FP8) && k <= size_t(vsg::kTcMaxShortlist)) {
@@ -857,7 +859,9 @@ struct vsg_index {
     a.counters = static_cast<uint32_t*>(counters.get());
     a.out_d = out_dists;
     a.out_i = out_ids;
+    a.nq_dev = nq_dev;
     VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
+    ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }

@@ -190,6 +190,9 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t qbase = blockIdx.x * QB;
+  // A count read on the device: whole query blocks past it leave before touching anything (the
+  // fused merge's counter of such a block is never used).
+  if (a.nq_dev && qbase >= *a.nq_dev) return;
   const uint32_t split = blockIdx.y;
   const uint32_t row_begin = split * a.rows_per_split;  // a multiple of 32
   const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
@@ -468,6 +471,7 @@ __global__ void __launch_bounds__(256) merge_kernel(const MergeArgs m) {
   __shared__ uint32_t si[8][kMaxK];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q = blockIdx.x;
+  if (m.nq_dev && q >= *m.nq_dev) return;
   const float mg = m.margin ? m.margin[q] : -1.f;
   const int kk = int(m.kk);
   WarpTopK<E> acc;
@@ -491,6 +495,7 @@ __global__ void __launch_bounds__(256) gather_merge_kernel(const MergeArgs m) {
   __shared__ uint32_t total;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q = blockIdx.x, k = m.k;
+  if (m.nq_dev && q >= *m.nq_dev) return;
   const size_t base = size_t(q) * m.nsplit * k;
   const float mg = m.margin ? m.margin[q] : -1.f;
   const int kk = int(m.kk);

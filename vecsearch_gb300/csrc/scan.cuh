@@ -32,6 +32,9 @@ struct ScanArgs {
   uint32_t* counters;
   float* out_d;
   uint32_t* out_i;
+  // Optional: the number of queries to search, read on the device (at most nq); the launch is
+  // sized for nq and query blocks past the count return at once.
+  const uint32_t* nq_dev;
 };
 
 struct MergeArgs {
@@ -48,6 +51,8 @@ struct MergeArgs {
   // Optional: the real entries of each list ([nq][nsplit], the rest of a list is padding). The
   // merge then gathers only those and sorts them once, when they fit its staging area.
   const uint32_t* part_n;
+  // Optional: the number of queries to merge, read on the device (at most nq).
+  const uint32_t* nq_dev;
 };
 
 struct ScanShape {

@@ -832,17 +832,20 @@ __global__ void midpoint_rows_kernel(float* dst, const float* src, uint32_t dp, 
 }
 
 __global__ void gather_rows_kernel(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                                   uint32_t count) {
+                                   uint32_t count, const uint32_t* count_dev) {
   const uint32_t j = blockIdx.x;
-  if (j >= count) return;
+  if (j >= count || (count_dev && j >= *count_dev)) return;
   const float* s = src + size_t(ids[j]) * ld;
   for (uint32_t c = threadIdx.x; c < dp; c += blockDim.x) dst[size_t(j) * dp + c] = s[c];
 }
 
 __global__ void scatter_results_kernel(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                       uint32_t k, const uint32_t* ids, uint32_t count) {
+                                       uint32_t k, const uint32_t* ids, uint32_t count, const uint32_t* count_dev,
+                                       unsigned long long* tally) {
   const uint32_t j = blockIdx.x;
-  if (j >= count) return;
+  const uint32_t cnt = count_dev ? min(count, *count_dev) : count;
+  if (tally && j == 0 && threadIdx.x == 0) atomicAdd(tally, (unsigned long long)cnt);
+  if (j >= cnt) return;
   const size_t o = size_t(ids[j]) * k;
   for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
     dst_i[o + c] = src_i[size_t(j) * k + c];
@@ -1419,16 +1422,17 @@ cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint
 }
 
 cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                               uint32_t count, cudaStream_t stream) {
+                               uint32_t count, cudaStream_t stream, const uint32_t* count_dev) {
   if (count == 0) return cudaSuccess;
-  gather_rows_kernel<<<count, 128, 0, stream>>>(dst, src, ld, dp, ids, count);
+  gather_rows_kernel<<<count, 128, 0, stream>>>(dst, src, ld, dp, ids, count, count_dev);
   return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream) {
+                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream,
+                                   const uint32_t* count_dev, unsigned long long* tally) {
   if (count == 0) return cudaSuccess;
-  scatter_results_kernel<<<count, 128, 0, stream>>>(dst_i, dst_d, src_i, src_d, k, ids, count);
+  scatter_results_kernel<<<count, 128, 0, stream>>>(dst_i, dst_d, src_i, src_d, k, ids, count, count_dev, tally);
   return cudaGetLastError();
 }
 

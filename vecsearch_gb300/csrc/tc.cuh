@@ -140,11 +140,15 @@ struct RerankArgs {
 cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
                                  cudaStream_t stream);
 // Gathers rows ids[0..count) of src (stride ld floats, dp copied) into dst (stride dp).
+// With count_dev set, only rows j < min(count, *count_dev) (a count read on the device; the launch
+// is sized for count).
 cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                               uint32_t count, cudaStream_t stream);
-// Scatters result rows j of (src_i, src_d) (k each) to rows ids[j] of (dst_i, dst_d).
+                               uint32_t count, cudaStream_t stream, const uint32_t* count_dev = nullptr);
+// Scatters result rows j of (src_i, src_d) (k each) to rows ids[j] of (dst_i, dst_d); count_dev as
+// above, and when tally is set the number of rows scattered is added to it.
 cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream);
+                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream,
+                                   const uint32_t* count_dev = nullptr, unsigned long long* tally = nullptr);
 
 // 128-byte chunks per row of an operand copy: dp bf16 (64 per chunk) or dp e4m3 (128 per chunk).
 uint32_t tc_chunks(uint32_t dp, bool fp8);

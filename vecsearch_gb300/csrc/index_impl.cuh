@@ -712,7 +712,7 @@ struct vsg_index {
     for (size_t i = 0; i < count; ++i) bmax = std::max(bmax, batches[i]);
     if (bmax == 0) throw std::invalid_argument("batch sizes must be > 0");
     // Each timed repetition takes another slice of the queries, so that costs that only some
-    // batches pay (the certified path's second pass) are averaged in.
+    // batches pay (the certified path's scan of unproven queries) are averaged in.
     constexpr int kReps = 4;
     const size_t qrows = std::max(bmax, std::min<size_t>(sample && nsample ? nsample : bmax * kReps, bmax * kReps));
     DeviceBuffer qbuf, obuf;

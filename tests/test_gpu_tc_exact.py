@@ -164,3 +164,24 @@ def test_bf16_filtered(gpu_ready):
         same = (bi == pi).all(1)
         assert same.mean() >= 0.97, (m, same.mean())
         np.testing.assert_array_equal(bd[same].view(np.uint32), pd[same].view(np.uint32))
+
+
+def test_auto_small_batches_on_large_index(gpu_ready):
+    # 360,000 x 384 = 138 M elements >= 2^27: method auto sends even one query to the certified
+    # path (reading the bf16 copy, half the bytes), with the scan kernel's answers bit for bit.
+    vsg = gpu_ready
+    x, q = _clustered(360_000, 32, 384, 256, True, 290)
+    gpu = vsg.GpuBruteForceIndex(384, "cosine")
+    gpu.add(x)
+    assert gpu.get_tunable("tc_exact_min_elements") == 2 ** 27
+    q0 = gpu.tc_exact_stats()[0]
+    k0 = gpu.kernel_launches()
+    for b in (1, 3, 17):
+        _same(gpu.search(q[:b], 10), gpu.search(q[:b], 10, method="skinny"))
+    assert gpu.tc_exact_stats()[0] - q0 == 21
+    assert gpu.kernel_launches() > k0
+    gpu.set_tunable("tc_exact_min_elements", 1e12)  # small batches back to the FP32 kernels
+    gpu.search(q[:4], 10)
+    assert gpu.tc_exact_stats()[0] - q0 == 21
+    with pytest.raises(ValueError):
+        gpu.set_tunable("tc_exact_min_elements", -1)

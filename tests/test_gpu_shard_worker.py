@@ -42,7 +42,8 @@ def test_worker_batches_on_gpu(gpu_ready, method):
     q, _ = D.portable_clustered(160, 96, 64, 0.35, seed=302, centroid_seed=301, unit=True)
     idx = vsg.GpuBruteForceIndex(96, "cosine")
     idx.add(x)
-    s = W.ShardSearcher(idx, offset=10_000, shard_id=0, method=method, max_batch=128, max_wait_ms=50.0)
+    s = W.ShardSearcher(idx, offset=10_000, shard_id=0, method=method, max_batch=128, max_wait_ms=50.0,
+                        wait_always=True)
     ks = [1 + (i * 5) % 32 for i in range(len(q))]
     out = [None] * len(q)
     barrier = threading.Barrier(len(q))

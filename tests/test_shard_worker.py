@@ -125,7 +125,7 @@ def _data(n=3000, d=24, nq=40, seed=5):
 def test_searcher_batches_concurrent_calls():
     x, q = _data()
     idx = NumpyExact(x)
-    s = W.ShardSearcher(idx, offset=1000, shard_id=3, max_batch=64, max_wait_ms=20.0)
+    s = W.ShardSearcher(idx, offset=1000, shard_id=3, max_batch=64, max_wait_ms=20.0, wait_always=True)
     ks = [1 + (i * 7) % 30 for i in range(len(q))]
     out = [None] * len(q)
     barrier = threading.Barrier(len(q))
@@ -198,3 +198,17 @@ def test_grpc_service_and_coordinator_merge():
             srv.stop(0)
         for s in searchers:
             s.close()
+
+
+def test_lone_caller_is_not_delayed():
+    # The batching window applies only after a batch of several calls: a lone caller is searched
+    # at once even with a long window.
+    import time
+    x, q = _data(n=200)
+    s = W.ShardSearcher(NumpyExact(x), max_batch=64, max_wait_ms=200.0)
+    t = time.perf_counter()
+    for i in range(5):
+        s.search(W.encode_search_request(q[i], 5))
+    assert time.perf_counter() - t < 0.5  # five 200 ms windows would take 1 s
+    assert s.batches == 5
+    s.close()

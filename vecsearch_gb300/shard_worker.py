@@ -198,16 +198,19 @@ class ShardSearcher:
     ``index``: a GpuBruteForceIndex (or any object with its ``search(queries, k, method)``,
     ``dim`` and ``len``) holding the shard's rows; ``offset``: global id of its first row.
     Calls from many threads are batched by one worker thread (see the module docstring);
-    ``max_batch=1`` searches each call on its own.
+    ``max_batch=1`` searches each call on its own, ``wait_always=True`` waits up to
+    ``max_wait_ms`` for company before every batch.
     """
 
-    def __init__(self, index, offset=0, shard_id=0, method="auto", max_batch=256, max_wait_ms=0.2):
+    def __init__(self, index, offset=0, shard_id=0, method="auto", max_batch=256, max_wait_ms=0.2,
+                 wait_always=False):
         self.index = index
         self.offset = int(offset)
         self.shard_id = int(shard_id)
         self.method = method
         self.max_batch = max(1, int(max_batch))
         self.max_wait = max(0.0, float(max_wait_ms)) / 1e3
+        self.wait_always = bool(wait_always)  # wait for company even after a lone call
         self.dim = int(index.dim)
         self._q = queue.Queue()
         self._stop = threading.Event()
@@ -230,7 +233,7 @@ class ShardSearcher:
             group = [first]
             # Wait for company only under load (the previous batch had several calls): a lone
             # caller is searched at once.
-            deadline = time.perf_counter() + (self.max_wait if last > 1 else 0.0)
+            deadline = time.perf_counter() + (self.max_wait if (last > 1 or self.wait_always) else 0.0)
             while len(group) < self.max_batch:
                 left = deadline - time.perf_counter()
                 try:

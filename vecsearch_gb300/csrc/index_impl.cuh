@@ -123,7 +123,7 @@ struct vsg_index {
   DeviceBuffer counters;  // per query block: CTAs done (the scan kernel's fused merge); kept zero
   // Precision form: BF16 copy of the rows (cap x dp) and FP32 squared norms, built on first use
   // and kept current by later adds; bf16 query staging; merged shortlist candidates.
-  DeviceBuffer xb, xnorm, qb, qnorm, cand, sample, thr;
+  DeviceBuffer xb, xnorm, qb, qnorm, sample, thr;
   // method "fp8": e4m3 copy of the rows (cap x dp8 bytes, dp8 = dim rounded up to 16), one FP32
   // scale per row, FP32 squared norms; e4m3 query staging and query scales.
   DeviceBuffer x8, x8scale, x8norm, q8, q8scale;
@@ -140,7 +140,7 @@ struct vsg_index {
   DeviceBuffer tcstats;            // device tally of its uncertified queries (scan fallbacks)
   uint64_t kernel_launches = 0;    // this index's kernel launches (vsg_kernel_launches)
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
-  DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_cert_margin)
+  DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_prepare_queries)
   size_t bf16_rows = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
@@ -429,6 +429,7 @@ struct vsg_index {
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                     cudaStream_t s, bool certify = false, uint32_t kp_force = 0, bool f8 = false,
                     const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
+    if (certify && f8) throw std::invalid_argument("the certificate is for the bf16 copy");
     const uint32_t kp = kp_force ? kp_force : certify ? exact_shortlist_size(k) : shortlist_size(k);
     // The operand copy, its norms (and rounding bounds or scales) cover every row before any
     // kernel reads them.
@@ -457,9 +458,20 @@ struct vsg_index {
       ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, uint32_t(vsg::kTcQueries), true));
     } else {
+      // One launch: bf16 queries and norms, shared thresholds reset, and on the certified path
+      // the bounds E, the margins and the zeroed uncertified count.
       qb.reserve(nq * dp * 2, 0, stream);
-      VSG_CUDA(vsg::launch_to_bf16(dq, ldq, nq, uint32_t(dim), uint32_t(dp), qb.get(),
-                                   static_cast<float*>(qnorm.get()), s));
+      gthr.reserve(nq * sizeof(uint32_t), 0, stream);
+      float* mgn = nullptr;
+      if (certify) {
+        qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
+        mgn = static_cast<float*>(qmargin.get());
+      }
+      VSG_CUDA(vsg::launch_prepare_queries(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dim), uint32_t(dp), qb.get(),
+                                           static_cast<float*>(qnorm.get()), static_cast<uint32_t*>(gthr.get()),
+                                           static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
+                                           float(cert_margin), mgn, mgn ? mgn + nq : nullptr,
+                                           certify ? static_cast<uint32_t*>(fails.get()) : nullptr, s));
       ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp, uint32_t(vsg::kTcQueries)));
       ensure_xmap();
@@ -476,24 +488,19 @@ struct vsg_index {
     choose_splits(nqg, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
     const size_t parts = nq * a.nsplit * kp;
     part.reserve(parts * 8 + nq * a.nsplit * 4, 0, stream);  // lists, then their lengths
-    cand.reserve(nq * kp * 8, 0, stream);
     // One candidate buffer per CTA.
     const unsigned grid = unsigned(std::min<size_t>(nqg * a.nsplit, slots) * C);
     const CUtensorMap& rowmap = C > 1 ? slice_map(C, f8) : f8 ? xmap8 : xmap;
     const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
-    gthr.reserve(nq * sizeof(uint32_t), 0, stream);
-    VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
+    if (f8) {  // (the bf16 queries' launch resets them)
+      gthr.reserve(nq * sizeof(uint32_t), 0, stream);
+      VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
+    }
     // Certified path: each query keeps only the rows within its margin of its k-th best (k' caps
     // the list), which is all the certificate needs.
     const bool margins = certify && !f8;
     if (margins) {
-      qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
-      VSG_CUDA(vsg::launch_cert_margin(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dp),
-                                       static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
-                                       float(cert_margin), static_cast<float*>(qmargin.get()),
-                                       static_cast<float*>(qmargin.get()) + nq, s));
-      ++kernel_launches;
       a.margin = static_cast<const float*>(qmargin.get());
       a.kk = uint32_t(k);
     }
@@ -562,44 +569,37 @@ struct vsg_index {
     VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    float* cd = static_cast<float*>(cand.get());
-    uint32_t* ci = reinterpret_cast<uint32_t*>(static_cast<char*>(cand.get()) + nq * kp * 4);
-    vsg::MergeArgs m{a.part_d, a.part_i, cd, ci, uint32_t(nq), a.nsplit, kp};
-    m.part_n = a.part_n;
-    if (margins) {  // the merged list keeps only the rows within the margin of its k-th best
-      m.margin = a.margin;
-      m.kk = uint32_t(k);
-    }
-    VSG_CUDA(vsg::launch_merge(m, s));
-    ++kernel_launches;
-    vsg::RerankArgs r{};
-    r.x = static_cast<const float*>(x.get());
-    r.q = dq;
-    r.cand = ci;
-    r.out_d = out_dists;
-    r.out_i = out_ids;
-    r.dp = uint32_t(dp);
-    r.ldq = uint32_t(ldq);
-    r.nq = uint32_t(nq);
-    r.kp = kp;
-    r.k = uint32_t(k);
-    r.l2 = a.l2;
+    // Merge, rerank and (certified path) certificate in one launch.
+    vsg::FinishArgs fa{};
+    fa.part_d = a.part_d;
+    fa.part_i = a.part_i;
+    fa.part_n = a.part_n;
+    fa.nq = uint32_t(nq);
+    fa.nsplit = a.nsplit;
+    fa.kp = kp;
+    fa.k = uint32_t(k);
+    fa.margin = margins ? a.margin : nullptr;  // the merged list keeps the rows within the margin
+    fa.x = static_cast<const float*>(x.get());
+    fa.q = dq;
+    fa.dp = uint32_t(dp);
+    fa.ldq = uint32_t(ldq);
+    fa.l2 = a.l2;
+    fa.out_d = out_dists;
+    fa.out_i = out_ids;
     if (certify && !f8) {
-      r.cand_d = cd;
-      r.thr_init = a.thr_init;
-      r.err = static_cast<const float*>(qmargin.get()) + nq;
-      r.gthr = a.gthr;
-      r.margin = m.margin;
-      r.fail_count = static_cast<uint32_t*>(fails.get());
-      r.fail_list = r.fail_count + 1;
+      fa.thr_init = a.thr_init;
+      fa.gthr = a.gthr;
+      fa.err = static_cast<const float*>(qmargin.get()) + nq;
+      fa.fail_count = static_cast<uint32_t*>(fails.get());
+      fa.fail_list = fa.fail_count + 1;
     }
-    VSG_CUDA(vsg::launch_rerank(r, s));
+    VSG_CUDA(vsg::launch_finish(fa, s));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
-  // Exact top-k through the shortlist. Queries whose result the rerank kernel cannot certify (see
-  // RerankArgs) run in the streaming scan kernel, so results equal method skinny bit for bit.
+  // Exact top-k through the shortlist. Queries whose result the finish kernel cannot certify (see
+  // vsg::FinishArgs) run in the streaming scan kernel, so results equal method skinny bit for bit.
   // Nothing waits on the host: the rerank leaves the uncertified queries' count and indices on
   // the device, and the fallback launches (gather, scan, scatter) are sized for all nq queries,
   // their blocks past that count returning at once. A tally of uncertified queries stays on the
@@ -613,8 +613,7 @@ struct vsg_index {
     uint32_t kp1 = force_exact_kp > 0 ? uint32_t(force_exact_kp) : te && te->kernel == 2 ? te->exact_kp : 0u;
     kp1 = kp1 ? std::max<uint32_t>(std::min<uint32_t>(kp1, uint32_t(vsg::kTcMaxShortlist)), uint32_t(k))
               : exact_shortlist_size(k);
-    VSG_CUDA(cudaMemsetAsync(fails.get(), 0, sizeof(uint32_t), s));
-    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);  // zeroes the count
     tc_exact_queries += nq;
     const uint32_t* d_count = static_cast<const uint32_t*>(fails.get());
     const uint32_t* d_list = d_count + 1;

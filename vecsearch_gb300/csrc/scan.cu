@@ -481,68 +481,6 @@ __global__ void __launch_bounds__(256) merge_kernel(const MergeArgs m) {
   if (warp == 0) merge_finish<E>(acc, m, q, sd, si, lane, kk, mg);
 }
 
-// The same merge when each list's length is known (m.part_n): the lists' real entries are
-// copied into shared memory (one list per thread, four loads in flight), each warp sorts chunks
-// of 32 E of them and merges the chunks into its list, and warp 0 merges the 8 lists. More
-// entries than the staging area holds: the list merge above.
-constexpr uint32_t kMergeStage = 4096;
-template <int E>
-__global__ void __launch_bounds__(256) gather_merge_kernel(const MergeArgs m) {
-  __shared__ float sd[8][kMaxK];
-  __shared__ uint32_t si[8][kMaxK];
-  __shared__ float stg_d[kMergeStage];
-  __shared__ uint32_t stg_i[kMergeStage];
-  __shared__ uint32_t total;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t q = blockIdx.x, k = m.k;
-  if (m.nq_dev && q >= *m.nq_dev) return;
-  const size_t base = size_t(q) * m.nsplit * k;
-  const float mg = m.margin ? m.margin[q] : -1.f;
-  const int kk = int(m.kk);
-  if (threadIdx.x == 0) total = 0;
-  __syncthreads();
-  for (uint32_t sp = threadIdx.x; sp < m.nsplit; sp += blockDim.x) {
-    const uint32_t len = min(m.part_n[size_t(q) * m.nsplit + sp], k);
-    if (!len) continue;
-    const uint32_t pos = atomicAdd(&total, len);
-    const float* ld = m.part_d + base + size_t(sp) * k;
-    const uint32_t* li = m.part_i + base + size_t(sp) * k;
-    for (uint32_t j = 0; j < len; j += 4) {
-      float dv[4];
-      uint32_t iv[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        dv[t] = j + t < len ? ld[j + t] : 0.f;
-        iv[t] = j + t < len ? li[j + t] : 0u;
-      }
-#pragma unroll
-      for (int t = 0; t < 4; ++t)
-        if (j + t < len && pos + j + t < kMergeStage) {
-          stg_d[pos + j + t] = dv[t];
-          stg_i[pos + j + t] = iv[t];
-        }
-    }
-  }
-  __syncthreads();
-  const uint32_t n_all = total;  // CTA-uniform
-  WarpTopK<E> acc;
-  acc.clear();
-  if (n_all > kMergeStage) {
-    merge_split_lists<E>(acc, m, q, sd, si, warp, lane, kk, mg);
-  } else {
-    constexpr uint32_t kChunk = 32u * E;
-    for (uint32_t c0 = uint32_t(warp) * kChunk; c0 < n_all; c0 += 8 * kChunk) {
-      WarpTopK<E> b;
-      b.load(stg_d + c0, stg_i + c0, int(min(n_all - c0, kChunk)), lane);
-      b.sort(lane);
-      acc.merge(b, lane);
-    }
-    acc.store(sd[warp], si[warp], int(k), lane);
-  }
-  __syncthreads();
-  if (warp == 0) merge_finish<E>(acc, m, q, sd, si, lane, kk, mg);
-}
-
 __global__ void fill_missing_kernel(float* d, uint32_t* i, size_t count) {
   for (size_t j = blockIdx.x * size_t(blockDim.x) + threadIdx.x; j < count; j += size_t(gridDim.x) * blockDim.x) {
     d[j] = __int_as_float(0x7f800000);
@@ -603,14 +541,7 @@ cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaSt
 cudaError_t launch_merge(const MergeArgs& m, cudaStream_t stream) {
   if (m.margin && (m.kk == 0 || m.kk > m.k)) return cudaErrorInvalidValue;
   if (m.nq == 0) return cudaSuccess;
-  if (m.part_n) {
-    if (m.k <= 32)
-      gather_merge_kernel<1><<<m.nq, 256, 0, stream>>>(m);
-    else if (m.k <= 64)
-      gather_merge_kernel<2><<<m.nq, 256, 0, stream>>>(m);
-    else
-      gather_merge_kernel<4><<<m.nq, 256, 0, stream>>>(m);
-  } else if (m.k <= 32) {
+  if (m.k <= 32) {
     merge_kernel<1><<<m.nq, 256, 0, stream>>>(m);
   } else if (m.k <= 64) {
     merge_kernel<2><<<m.nq, 256, 0, stream>>>(m);

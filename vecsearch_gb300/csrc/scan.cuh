@@ -48,9 +48,6 @@ struct MergeArgs {
   // not merged.
   const float* margin;
   uint32_t kk;
-  // Optional: the real entries of each list ([nq][nsplit], the rest of a list is padding). The
-  // merge then gathers only those and sorts them once, when they fit its staging area.
-  const uint32_t* part_n;
   // Optional: the number of queries to merge, read on the device (at most nq).
   const uint32_t* nq_dev;
 };

@@ -1,24 +1,31 @@
-// Precision form: BF16 tensor-core shortlist (tcgen05 + TMEM + TMA) and exact FP32 rerank.
+// Tensor-core paths: BF16 (or FP8-e4m3) shortlist (tcgen05 + TMEM + TMA) and exact FP32 rerank,
+// with an optional certificate that makes the result exact.
 //
 // The reference has no tensor-core path; its large-batch kernel is a CUDA-core SGEMM
-// (src/gpu_brute_force.cu:142-218). Here the base keeps an FP32 master copy and a BF16 copy.
+// (src/gpu_brute_force.cu:142-218). Here the base keeps an FP32 master copy and a tile-major
+// BF16 (or e4m3) copy.
 //
-// tc_shortlist_kernel: CTA = 128 queries x one row range; 6 warps.
-//   warp 0   TMA producer: per 128-row tile, 64-dim chunks of the bf16 query block (A) and of
-//            the bf16 rows (B), 16 KB each, 128-byte swizzled, into a ring of `stages` slots.
-//   warp 1   allocates 256 TMEM columns (two 128 x 128 FP32 accumulators); one lane issues
-//            tcgen05.mma kind::f16 (M = 128 queries, N = 128 rows, K = 16) over each chunk and
-//            commits the slot back to the producer and the finished tile to the epilogue.
-//   warps 2-5 epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, i.e. one query per thread;
-//            each thread streams its query's 128 scores (tcgen05.ld 32x32b.x32), appends those
-//            that beat its threshold (approximate distance 1 - s, or |q|^2 + |x|^2 - 2 s) to the
-//            query's buffer in shared memory, and the warp compacts a buffer that may overflow
-//            with a register bitonic sort that keeps the best kp; then it releases the accumulator.
-//   At the end each thread writes its list: the split's shortlist for merge_kernel.
-// rerank_kernel: per query, exact FP32 distances of the merged top-kp candidates with the
-//   streaming scan kernel's arithmetic (lane l sums 16-byte chunks l, l + 32, ... in order, then
-//   a butterfly over lanes 16, 8, 4, 2, 1), so a shortlist that holds the true top-k yields the
-//   scan kernel's results bit for bit; then the top-k by (dist, id).
+// prepare_queries_kernel: bf16 queries and norms, shared thresholds reset, certificate bounds E
+//   and margins (certified path).
+// tc_shortlist_kernel: CTA = 128 queries x a range of rows, one CTA per SM; 6 warps.
+//   warp 0   TMA producer: the query block stays resident in shared memory; each 256-row tile of
+//            the row copy arrives as 128-byte chunks (32 KB, one contiguous span of the
+//            tile-major copy) into a ring of `stages` slots.
+//   warp 1   allocates all 512 TMEM columns (two 128 x 256 FP32 accumulators); one lane issues
+//            tcgen05.mma (M = 128 queries, N = 256 rows, K = 16 bf16 or 32 e4m3) over each chunk
+//            and commits the slot back to the producer and the finished tile to the epilogue.
+//   warps 2-5 epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, one query per thread; per
+//            tile it tests all 256 scores against its threshold with bit masks and one vote per
+//            half, appends the few candidates to its query's global buffer, and compacts a
+//            buffer that may overflow (a warp bitonic sort keeping the best k', or with margins
+//            only the rows within the margin of the k-th best); thresholds are shared across
+//            a query's splits. At the end each thread writes its split's sorted list and length.
+//   A dump mode (the sample pass) writes raw approximate distances instead.
+// sample_select_kernel: per query, an upper bound of the k'-th (or k-th + margin) best sampled
+//   distance: the starting threshold.
+// finish_kernel: per query, the split lists merged, the exact FP32 distances of the merged rows
+//   with the streaming scan kernel's arithmetic (so a shortlist that holds the true top k yields
+//   the scan kernel's results bit for bit), the top k by (dist, id), and the certificate.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
@@ -940,73 +947,106 @@ __device__ double cert_error(double sq2, double sqb2, double sr2, uint32_t dp, c
   return e * 1.1;  // margin over the (already worst-case) terms
 }
 
-// The certificate's inputs for one query: |q|^2, |q~|^2 and |q~ - q|^2 over this thread's
-// columns c = first, first + step, ... below dp.
-__device__ __forceinline__ void cert_sums(const float* q, uint32_t dp, uint32_t first, uint32_t step, float& q2,
-                                          float& qb2, float& r2) {
-  for (uint32_t c = first; c < dp; c += step) {
-    const float v = q[c];
-    const float vb = __bfloat162float(__float2bfloat16_rn(v));
-    q2 = fmaf(v, v, q2);
-    qb2 = fmaf(vb, vb, qb2);
-    r2 = fmaf(vb - v, vb - v, r2);
-  }
-}
 
-// One warp per query: err[q] = E and margin[q] = factor x E (both rounded up). A shortlist that
-// keeps every row within the margin m of its k-th best approximate distance a_k leaves out only
-// rows at or above a_k + m, so it certifies whenever the k-th FP32 distance is below
-// a_k + m - E. That always holds for m > 2 E (the k-th FP32 distance is at most a_k + E); the
-// bf16 roundings of real data stay far below their worst case E, so m = 1.3 E already certifies
-// nearly every query while keeping about half the rows of 2 E.
-template <bool L2>
-__global__ void __launch_bounds__(128) cert_margin_kernel(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp,
-                                                          const float* xbound, float factor, float* margin,
-                                                          float* err) {
-  const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (qq >= nq) return;
-  float q2 = 0.f, qb2 = 0.f, r2 = 0.f;
-  cert_sums(q + size_t(qq) * ldq, dp, lane, 32, q2, qb2, r2);
-  for (int o = 16; o > 0; o >>= 1) {
-    q2 += __shfl_xor_sync(kFull, q2, o);
-    qb2 += __shfl_xor_sync(kFull, qb2, o);
-    r2 += __shfl_xor_sync(kFull, r2, o);
-  }
-  if (lane == 0) {
-    const double e = cert_error<L2>(q2, qb2, r2, dp, xbound);
-    err[qq] = __double2float_ru(e);
-    margin[qq] = __double2float_ru(double(factor) * e);
-  }
-}
-
-// One CTA per query: warps compute exact distances of the candidates, then each candidate's
-// rank in (dist, id) order places the first k. The candidate list is sorted with the missing
-// entries (none) at its end, so the real ones are a prefix.
-template <bool L2>
-__global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
-  __shared__ float cd[kMaxK];
-  __shared__ uint32_t ci[kMaxK];
-  __shared__ __align__(16) float qs[4096];
+// The shortlist path's tail (FinishArgs), one CTA of 256 threads per query.
+constexpr uint32_t kFinishStage = 4096;  // real list entries gathered into shared memory at most
+template <int E, bool L2>
+__global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
+  __shared__ float sd[8][kMaxK];
+  __shared__ uint32_t si[8][kMaxK];
+  __shared__ __align__(16) float stg_d[kFinishStage];  // the staging area, then the query
+  __shared__ uint32_t stg_i[kFinishStage];
+  __shared__ float md[kMaxK];  // the merged list: approximate distances and ids
+  __shared__ uint32_t mi[kMaxK];
+  __shared__ float cd[kMaxK];  // exact distances of its real entries
+  __shared__ uint32_t total;
   __shared__ float dk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t q = blockIdx.x, kp = a.kp, nc = a.dp / 4;
-  const bool q_in_smem = a.dp <= 4096;
+  const uint32_t q = blockIdx.x, kp = a.kp, k = a.k;
+  const size_t base = size_t(q) * a.nsplit * kp;
+  const float mg = a.margin ? a.margin[q] : -1.f;
+  const int kk = int(k);
+  if (threadIdx.x == 0) {
+    total = 0;
+    dk = __int_as_float(0x7f800000);
+  }
+  __syncthreads();
+  // ---- merge: one list per thread into the staging area, four loads in flight ----
+  for (uint32_t sp = threadIdx.x; sp < a.nsplit; sp += blockDim.x) {
+    const uint32_t len = min(a.part_n[size_t(q) * a.nsplit + sp], kp);
+    if (!len) continue;
+    const uint32_t pos = atomicAdd(&total, len);
+    const float* ld = a.part_d + base + size_t(sp) * kp;
+    const uint32_t* li = a.part_i + base + size_t(sp) * kp;
+    for (uint32_t j = 0; j < len; j += 4) {
+      float dv[4];
+      uint32_t iv[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        dv[t] = j + t < len ? ld[j + t] : 0.f;
+        iv[t] = j + t < len ? li[j + t] : 0u;
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (j + t < len && pos + j + t < kFinishStage) {
+          stg_d[pos + j + t] = dv[t];
+          stg_i[pos + j + t] = iv[t];
+        }
+    }
+  }
+  __syncthreads();
+  const uint32_t n_all = total;  // CTA-uniform
+  WarpTopK<E> acc;
+  acc.clear();
+  if (n_all > kFinishStage) {  // too many to stage: warp w merges lists w, w + 8, ...
+    if (uint32_t(warp) < a.nsplit)
+      warp_merge_lists<E>(acc, a.part_d + base + size_t(warp) * kp, a.part_i + base + size_t(warp) * kp,
+                          int((a.nsplit - warp + 7) / 8), size_t(8) * kp, int(kp), lane, kk, mg);
+  } else {  // warp w sorts chunks w, w + 8, ... of 32 E entries and merges them
+    constexpr uint32_t kChunk = 32u * E;
+    for (uint32_t c0 = uint32_t(warp) * kChunk; c0 < n_all; c0 += 8 * kChunk) {
+      WarpTopK<E> b;
+      b.load(stg_d + c0, stg_i + c0, int(min(n_all - c0, kChunk)), lane);
+      b.sort(lane);
+      acc.merge(b, lane);
+    }
+  }
+  acc.store(sd[warp], si[warp], int(kp), lane);
+  __syncthreads();
+  if (warp == 0) {
+    warp_merge_lists<E>(acc, sd[1], si[1], 7, kMaxK, int(kp), lane, kk, mg);
+    if (mg >= 0.f) {  // the cut: entries above the k-th + margin (the list stays sorted)
+      float td;
+      uint32_t ti;
+      acc.entry(kk - 1, td, ti);
+      const float cut = __fadd_ru(td, mg);
+#pragma unroll
+      for (int e = 0; e < E; ++e)
+        if (!nb_less(acc.d[e], acc.i[e], cut, kNone)) {
+          acc.d[e] = __int_as_float(0x7f800000);
+          acc.i[e] = kNone;
+        }
+    }
+    acc.store(md, mi, int(kp), lane);
+  }
+  __syncthreads();
+  // ---- rerank: exact FP32 distances of the real entries (a prefix of the sorted list) ----
+  const uint32_t nc = a.dp / 4;
+  float* qs = stg_d;  // the staging area is free now
+  const bool q_in_smem = a.dp <= kFinishStage;
   if (q_in_smem)
     for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
-  if (threadIdx.x == 0) dk = __int_as_float(0x7f800000);
-  const uint32_t id0 = threadIdx.x < kp ? a.cand[size_t(q) * kp + threadIdx.x] : kNone;  // kp <= 128 < threads
-  if (threadIdx.x < kp) ci[threadIdx.x] = id0;
+  const uint32_t id0 = threadIdx.x < kp ? mi[threadIdx.x] : kNone;  // kp <= 128 < threads
   const uint32_t nreal = uint32_t(__syncthreads_count(id0 != kNone));
   const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.ldq);
-  // Four candidates per warp at a time (candidates warp, warp + 8, ...: four in a row per warp).
-  constexpr int G = 4;
+  constexpr int G = 4;  // four candidates per warp at a time
   const uint32_t nwarps = blockDim.x / 32;
   for (uint32_t j0 = warp; j0 < nreal; j0 += G * nwarps) {
     const float4* x4[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       const uint32_t j = j0 + uint32_t(g) * nwarps;
-      x4[g] = j < nreal ? reinterpret_cast<const float4*>(a.x + size_t(ci[j]) * a.dp) : nullptr;
+      x4[g] = j < nreal ? reinterpret_cast<const float4*>(a.x + size_t(mi[j]) * a.dp) : nullptr;
     }
     float d[G];
     exact_distances<L2, G>(q4, x4, nc, lane, d);
@@ -1019,32 +1059,77 @@ __global__ void __launch_bounds__(256) rerank_kernel(const RerankArgs a) {
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < nreal; j += blockDim.x) {
     const float dj = cd[j];
-    const uint32_t ij = ci[j];
+    const uint32_t ij = mi[j];
     uint32_t rank = 0;
     for (uint32_t t = 0; t < nreal; ++t)
-      rank += nb_less(cd[t], ci[t], dj, ij) || (cd[t] == dj && ci[t] == ij && t < j);
-    if (rank < a.k) {
-      a.out_d[size_t(q) * a.k + rank] = dj;
-      a.out_i[size_t(q) * a.k + rank] = ij;
+      rank += nb_less(cd[t], mi[t], dj, ij) || (cd[t] == dj && mi[t] == ij && t < j);
+    if (rank < k) {
+      a.out_d[size_t(q) * k + rank] = dj;
+      a.out_i[size_t(q) * k + rank] = ij;
     }
-    if (rank + 1 == a.k) dk = dj;  // the k-th FP32 distance
+    if (rank + 1 == k) dk = dj;  // the k-th FP32 distance
   }
-  for (uint32_t j = nreal + threadIdx.x; j < a.k; j += blockDim.x) {  // fewer than k candidates: pad
-    a.out_d[size_t(q) * a.k + j] = __int_as_float(0x7f800000);
-    a.out_i[size_t(q) * a.k + j] = kNone;
+  for (uint32_t j = nreal + threadIdx.x; j < k; j += blockDim.x) {  // fewer than k candidates: pad
+    a.out_d[size_t(q) * k + j] = __int_as_float(0x7f800000);
+    a.out_i[size_t(q) * k + j] = kNone;
   }
   if (!a.fail_count) return;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const float last = kp > 0 ? a.cand_d[size_t(q) * kp + kp - 1] : __int_as_float(0x7f800000);
+    const float last = md[kp - 1];
     const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
     const uint32_t gk = a.gthr ? a.gthr[q] : kKeyNone;
     const float g = gk != kKeyNone ? key_float(gk) : __int_as_float(0x7f800000);
-    const float cut = (a.margin && a.k <= kp) ? __fadd_ru(a.cand_d[size_t(q) * kp + a.k - 1], a.margin[q])
-                                               : __int_as_float(0x7f800000);
+    const float cut = (a.margin && k <= kp) ? __fadd_ru(md[k - 1], a.margin[q]) : __int_as_float(0x7f800000);
     const double L = double(fminf(fminf(last, thr0), fminf(g, cut)));
     const bool ok = isinf(L) || (L - double(a.err[q]) > double(dk));
     if (!ok) a.fail_list[atomicAdd(a.fail_count, 1u)] = q;
+  }
+}
+
+// The queries of the bf16 shortlist path, one warp per query: the bf16 copy (stride dp, padding
+// columns zero) and the squared norm, as to_bf16_kernel writes them; the query's shared threshold
+// reset to none (gthr); and, with margins, err[q] = E and margin[q] = factor x E (both rounded
+// up). A shortlist that keeps every row within the margin m of its k-th best approximate distance
+// a_k leaves out only rows at or above a_k + m, so it certifies whenever the k-th FP32 distance is
+// below a_k + m - E. That always holds for m > 2 E (the k-th FP32 distance is at most a_k + E); the
+// bf16 roundings of real data stay far below their worst case E, so m = 1.3 E already certifies
+// nearly every query while keeping about half the rows of 2 E. The first thread also zeroes the
+// uncertified-query count.
+template <bool L2>
+__global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, uint32_t ldq, uint32_t nq,
+                                                              uint32_t dim, uint32_t dp, __nv_bfloat16* qb,
+                                                              float* qnorm, uint32_t* gthr, const float* xbound,
+                                                              float factor, float* margin, float* err,
+                                                              uint32_t* fails) {
+  if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
+  const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (qq >= nq) return;
+  const float* s = q + size_t(qq) * ldq;
+  __nv_bfloat16* d = qb + size_t(qq) * dp;
+  float q2 = 0.f, qb2 = 0.f, r2 = 0.f;
+  for (uint32_t c = lane; c < dp; c += 32) {
+    const float v = c < dim ? s[c] : 0.f;
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    const float vb = __bfloat162float(b);
+    q2 = fmaf(v, v, q2);
+    qb2 = fmaf(vb, vb, qb2);
+    r2 = fmaf(vb - v, vb - v, r2);
+    d[c] = b;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    q2 += __shfl_xor_sync(kFull, q2, o);
+    qb2 += __shfl_xor_sync(kFull, qb2, o);
+    r2 += __shfl_xor_sync(kFull, r2, o);
+  }
+  if (lane == 0) {
+    if (qnorm) qnorm[qq] = q2;
+    if (gthr) gthr[qq] = kKeyNone;
+    if (margin) {
+      const double e = cert_error<L2>(q2, qb2, r2, dp, xbound);
+      err[qq] = __double2float_ru(e);
+      margin[qq] = __double2float_ru(double(factor) * e);
+    }
   }
 }
 
@@ -1466,26 +1551,41 @@ cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
-                               bool l2, float factor, float* margin, float* err, cudaStream_t stream) {
-  if (nq == 0) return cudaSuccess;
-  if (!q || !xbound || !margin || !err || ldq < dp || !(factor >= 0.f)) return cudaErrorInvalidValue;
-  const unsigned blocks = (nq + 3) / 4;
-  if (l2)
-    cert_margin_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, factor, margin, err);
-  else
-    cert_margin_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xbound, factor, margin, err);
+cudaError_t launch_finish(const FinishArgs& a, cudaStream_t stream) {
+  if (a.nq == 0) return cudaSuccess;
+  if (a.kp == 0 || a.kp > uint32_t(kMaxK) || a.k == 0 || !a.part_n || (a.margin && a.k > a.kp))
+    return cudaErrorInvalidValue;
+  if (a.fail_count && (!a.err || !a.fail_list)) return cudaErrorInvalidValue;
+  const unsigned g = a.nq;
+  if (a.kp <= 32) {
+    if (a.l2) finish_kernel<1, true><<<g, 256, 0, stream>>>(a);
+    else finish_kernel<1, false><<<g, 256, 0, stream>>>(a);
+  } else if (a.kp <= 64) {
+    if (a.l2) finish_kernel<2, true><<<g, 256, 0, stream>>>(a);
+    else finish_kernel<2, false><<<g, 256, 0, stream>>>(a);
+  } else {
+    if (a.l2) finish_kernel<4, true><<<g, 256, 0, stream>>>(a);
+    else finish_kernel<4, false><<<g, 256, 0, stream>>>(a);
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream) {
-  if (a.kp > uint32_t(kMaxK)) return cudaErrorInvalidValue;
-  if (a.fail_count && (!a.err || !a.fail_list || !a.cand_d)) return cudaErrorInvalidValue;
-  if (a.l2)
-    rerank_kernel<true><<<a.nq, 256, 0, stream>>>(a);
+cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,
+                                   float* qnorm, uint32_t* gthr, const float* xbound, bool l2, float factor,
+                                   float* margin, float* err, uint32_t* fails, cudaStream_t stream) {
+  if (nq == 0) return cudaSuccess;
+  if (!q || !qb || ldq < dim || dp < dim || (margin && (!err || !xbound || !(factor >= 0.f))))
+    return cudaErrorInvalidValue;
+  const unsigned blocks = (nq + 3) / 4;
+  auto* dst = static_cast<__nv_bfloat16*>(qb);
+  if (l2)
+    prepare_queries_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
+                                                             margin, err, fails);
   else
-    rerank_kernel<false><<<a.nq, 256, 0, stream>>>(a);
+    prepare_queries_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
+                                                              margin, err, fails);
   return cudaGetLastError();
 }
+
 
 }  // namespace vsg

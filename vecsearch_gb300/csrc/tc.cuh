@@ -111,31 +111,6 @@ cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, c
 cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
                                 uint32_t max_queries, cudaStream_t stream);
 
-struct RerankArgs {
-  const float* x;          // FP32 master rows, n x dp
-  const float* q;          // FP32 queries, row stride ldq
-  const uint32_t* cand;    // [nq][kp] candidate ids (kNone = missing)
-  float* out_d;            // [nq][k]
-  uint32_t* out_i;
-  uint32_t dp, ldq, nq, kp, k;
-  uint32_t l2;
-  // Certification (exact results from the shortlist), when fail_count is set. Every row outside
-  // a query's shortlist has an approximate distance >= L = min(k'-th shortlist entry, sample
-  // threshold, smallest shared threshold, merge cut); a bound E on |approximate - FP32 distance|
-  // (launch_cert_margin: from the bf16 rounding residuals of query and rows, Cauchy-Schwarz, and
-  // accumulation terms) then shows that none of them can enter the top k when L - E > the k-th
-  // FP32 distance found. Queries that fail are listed.
-  const float* cand_d;     // [nq][kp] approximate distances of the merged shortlist, ascending
-  const float* thr_init;   // per-query sample threshold, or nullptr (none)
-  const uint32_t* gthr;    // the shortlist pass's shared thresholds (order keys), or nullptr
-  // The merge's cut, when the merge ran with these margins: rows above (k-th entry) + margin[q]
-  // were dropped, so that value bounds L too. nullptr: no cut.
-  const float* margin;
-  const float* err;        // per-query E (launch_cert_margin), needed when fail_count is set
-  uint32_t* fail_count;    // number of uncertified queries (atomic), or nullptr: no check
-  uint32_t* fail_list;     // their query indices
-};
-
 // count queries near rows of src (0.9 x_i + 0.1 x_j of its n rows, stride dp), for the autotuner.
 cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
                                  cudaStream_t stream);
@@ -193,13 +168,45 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
 constexpr size_t kRowMajor = ~size_t(0);
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
                            float* norms, cudaStream_t stream, float* bounds = nullptr, size_t tile_row0 = kRowMajor);
-cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t stream);
-// Certified path: err[q] = the certificate's error bound E on |approximate - FP32 distance| for
-// query q (FP32 queries, row stride ldq, dp columns) over rows whose bf16 copies have the bounds
-// xbound = [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E; both
-// rounded up.
-cudaError_t launch_cert_margin(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, const float* xbound,
-                               bool l2, float factor, float* margin, float* err, cudaStream_t stream);
+// The shortlist path's tail in one launch, one CTA per query: the split lists merged into the
+// query's best kp (the real entries, part_n, gathered into shared memory and sorted when they
+// fit, else the lists merged; with margins, lists above (k-th best) + margin skipped and the merged
+// list cut there), then the exact FP32 distances of the list's rows with the scan kernel's
+// arithmetic and the top k by (dist, id), all without a round trip through global memory.
+// Certification (exact results from the shortlist), when fail_count is set: every row outside the
+// list has an approximate distance >= L = min(k'-th list entry, sample threshold, the smallest
+// shared threshold, merge cut); the bound E on |approximate - FP32 distance| (from the bf16
+// rounding residuals of query and rows, Cauchy-Schwarz and accumulation terms; see
+// launch_prepare_queries) then shows that none of them can enter the top k when L - E > the k-th
+// FP32 distance found. Uncertified queries are counted (fail_count, atomic) and listed.
+struct FinishArgs {
+  const float* part_d;     // [nq][nsplit][kp] approximate distances, sorted per list
+  const uint32_t* part_i;
+  const uint32_t* part_n;  // [nq][nsplit] real entries of each list
+  uint32_t nq, nsplit, kp, k;
+  const float* margin;     // per-query margins (certified path), or nullptr
+  const float* x;          // FP32 master rows, n x dp
+  const float* q;          // FP32 queries, row stride ldq
+  uint32_t dp, ldq, l2;
+  float* out_d;            // [nq][k]
+  uint32_t* out_i;
+  const float* thr_init;   // per-query sample threshold, or nullptr (none)
+  const uint32_t* gthr;    // the shortlist pass's shared thresholds (order keys), or nullptr
+  const float* err;        // per-query E (launch_prepare_queries), needed when fail_count is set
+  uint32_t* fail_count;    // number of uncertified queries, or nullptr: no certificate
+  uint32_t* fail_list;     // their query indices
+};
+cudaError_t launch_finish(const FinishArgs& a, cudaStream_t stream);
+
+// The bf16 shortlist path's queries in one launch: bf16 copy qb (stride dp, padding zero) and
+// squared norms qnorm (optional) of the FP32 queries (row stride ldq, dim columns read); gthr[q]
+// reset to 0xFFFFFFFF (optional); with margin set (the certified path), err[q] = the certificate's
+// bound E on |approximate - FP32 distance| over rows whose bf16 copies have the bounds xbound =
+// [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E, both rounded up;
+// and *fails = 0 when fails is set.
+cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,
+                                   float* qnorm, uint32_t* gthr, const float* xbound, bool l2, float factor,
+                                   float* margin, float* err, uint32_t* fails, cudaStream_t stream);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
 // zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
 // With tile_row0 set, dst is a tile-major copy as in launch_to_bf16.

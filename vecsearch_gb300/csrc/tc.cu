@@ -928,25 +928,33 @@ __device__ __forceinline__ void exact_distances(const float4* q4, const float4* 
 
 // The certificate's bound E on |approximate - FP32 distance| for one query, from its sums
 // |q|^2, |q~|^2 and |q~ - q|^2 (FP32, d terms each; q~ = the bf16 query) and the rows' bounds
-// xbound = [max |x~ - x|, max |x|, max |x~|].
+// xbound = [max |x~ - x|, max |x|, max |x~|]. In FP32 with every operation rounded up: all terms
+// are non-negative and every operation is monotone, so the result is at least the formula's
+// exact value (FP64 would be as safe but is slow on GB300).
 template <bool L2>
-__device__ double cert_error(double sq2, double sqb2, double sr2, uint32_t dp, const float* xbound) {
-  // FP32 sums of d non-negative terms: inflate by (1 + d 2^-23) before use.
-  const double u = 5.9604644775390625e-08, dd = double(dp), infl = 1.0 + 2.0 * dd * u;
-  const double qn = sqrt(sq2 * infl), qbn = sqrt(sqb2 * infl), rq = sqrt(sr2 * infl);
-  const double R = double(xbound[0]) * infl, N = double(xbound[1]) * infl, Nb = double(xbound[2]) * infl;
+__device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const float* xbound) {
+  auto mul = [](float a, float b) { return __fmul_ru(a, b); };
+  auto add = [](float a, float b) { return __fadd_ru(a, b); };
+  const float u = 5.9604644775390625e-08f, dd = float(dp);  // 2^-24; dp is exact in FP32
+  const float du = mul(dd, u);
+  // FP32 sums of d non-negative terms: inflate by (1 + 2 d u) before use.
+  const float infl = add(1.f, mul(2.f, du));
+  const float qn = __fsqrt_ru(mul(sq2, infl)), qbn = __fsqrt_ru(mul(sqb2, infl)), rq = __fsqrt_ru(mul(sr2, infl));
+  const float R = mul(xbound[0], infl), N = mul(xbound[1], infl), Nb = mul(xbound[2], infl);
   // |bf16 score - q.x| <= |q~||x~ - x| + |q~ - q||x| + accumulation (8 d u |q~||x~|);
   // |FP32 q.x - q.x| <= 2 d u |q||x|.
-  const double e_dot = qbn * R + rq * N + 8.0 * dd * u * qbn * Nb + 2.0 * dd * u * qn * N;
-  double e;
-  if (L2)  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
-    e = 2.0 * e_dot + dd * u * (qn * qn + N * N) + 4.0 * u * (qn * qn + N * N + 2.0 * qbn * Nb) +
-        (dd + 2.0) * u * (qn + N) * (qn + N);
-  else  // the two roundings of 1 - s
-    e = e_dot + 4.0 * u * (1.0 + qn * N);
-  return e * 1.1;  // margin over the (already worst-case) terms
+  const float e_dot = add(add(mul(qbn, R), mul(rq, N)), add(mul(mul(8.f, du), mul(qbn, Nb)), mul(mul(2.f, du), mul(qn, N))));
+  float e;
+  if (L2) {  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
+    const float q2n2 = add(mul(qn, qn), mul(N, N));
+    const float qpn = add(qn, N);
+    e = add(add(mul(2.f, e_dot), mul(du, q2n2)),
+            add(mul(mul(4.f, u), add(q2n2, mul(2.f, mul(qbn, Nb)))), mul(mul(add(dd, 2.f), u), mul(qpn, qpn))));
+  } else {  // the two roundings of 1 - s
+    e = add(e_dot, mul(mul(4.f, u), add(1.f, mul(qn, N))));
+  }
+  return mul(e, 1.1f);  // margin over the (already worst-case) terms; 1.1f is above 1.1
 }
-
 
 // The shortlist path's tail (FinishArgs), one CTA of 256 threads per query.
 constexpr uint32_t kFinishStage = 4096;  // real list entries gathered into shared memory at most
@@ -1126,9 +1134,9 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, ui
     if (qnorm) qnorm[qq] = q2;
     if (gthr) gthr[qq] = kKeyNone;
     if (margin) {
-      const double e = cert_error<L2>(q2, qb2, r2, dp, xbound);
-      err[qq] = __double2float_ru(e);
-      margin[qq] = __double2float_ru(double(factor) * e);
+      const float e = cert_error<L2>(q2, qb2, r2, dp, xbound);
+      err[qq] = e;
+      margin[qq] = __fmul_ru(factor, e);
     }
   }
 }

@@ -177,7 +177,11 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   cert_margin x E of its k-th best approximate distance (E: the certificate's bound on
  *   |approximate - FP32 distance|). A smaller value keeps fewer rows; a query whose k-th FP32
  *   distance lies more than (cert_margin - 1) E above its k-th approximate one is then not
- *   certified and runs again. Results are exact for every value. */
+ *   certified and runs in the streaming scan kernel. Results are exact for every value.
+ *   "fallback_split_queries" (default 128, 0 to 2^20): VSG_METHOD_TC_EXACT's scan of the
+ *   queries it did not certify splits the rows as for at most this many queries, so that a few
+ *   such queries in a large batch still spread over the SMs (0: split as for the whole batch).
+ *   Results are the same for every value. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

@@ -74,6 +74,30 @@ def test_tc_exact_falls_back_when_it_cannot_prove(gpu_ready):
     assert q1 - q0 == 40 and s1 - s0 > 0 and f1 - f0 > 0  # both later stages ran
 
 
+def test_fallback_split_any_value_is_exact(gpu_ready):
+    # Half of a 300-query batch sits where the bf16 bound cannot separate rows, so many queries
+    # are left to the scan kernel. Its row splits follow fallback_split_queries (0: as for the
+    # whole batch); the results never change.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    centres = D.portable(50, 64, 210, normalize=True)
+    x = vsg.normalize(np.repeat(centres, 400, axis=0) + 1e-4 * D.portable(20_000, 64, 211))
+    near = centres[np.arange(150) % 50] + 1e-3 * D.portable(150, 64, 213)
+    q = vsg.normalize(np.concatenate([near, D.portable(150, 64, 214)]).astype(np.float32))
+    gpu = vsg.GpuBruteForceIndex(64, "cosine")
+    gpu.add(x)
+    assert gpu.get_tunable("fallback_split_queries") == 128
+    want = gpu.search(q, 10, method="skinny")
+    for v in (128, 0, 1, 8, 20_000):
+        gpu.set_tunable("fallback_split_queries", v)
+        q0, _, f0 = gpu.tc_exact_stats()
+        _same(gpu.search(q, 10, method="tc_exact"), want)
+        q1, _, f1 = gpu.tc_exact_stats()
+        assert q1 - q0 == 300 and f1 - f0 > 0
+    with pytest.raises(ValueError):
+        gpu.set_tunable("fallback_split_queries", -1)
+
+
 @pytest.mark.parametrize("n,d,nq,k", [(90, 37, 5, 10), (5000, 40, 131, 17), (30_000, 128, 200, 100),
                                       (300, 200, 1, 120)])
 def test_tc_exact_shapes(gpu_ready, n, d, nq, k):

@@ -271,6 +271,10 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "cert_margin") {
       if (!(value >= 1.0 && value <= 100.0)) throw std::invalid_argument("cert_margin must be in [1, 100]");
       h->cert_margin = value;
+    } else if (nm == "fallback_split_queries") {
+      if (!(value >= 0.0 && value <= 1048576.0))
+        throw std::invalid_argument("fallback_split_queries must be in [0, 2^20]");
+      h->fallback_split_queries = std::floor(value);
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -289,6 +293,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "tc_exact_min_batch") *value = h->tc_exact_min_batch;
     else if (nm == "cert_margin") *value = h->cert_margin;
     else if (nm == "tc_exact_min_elements") *value = h->tc_exact_min_elements;
+    else if (nm == "fallback_split_queries") *value = h->fallback_split_queries;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

@@ -175,6 +175,9 @@ struct vsg_index {
   // certificate's error bound). Any value >= 1 gives exact results; it trades kept rows against
   // queries left uncertified.
   double cert_margin = 1.3;
+  // method "tc_exact": the uncertified queries' scan splits the rows as for at most this many
+  // queries (0: as for the whole batch).
+  double fallback_split_queries = 128;
 
   // ---- autotuned schedules (vsg_autotune) ----
   // plain: for unfiltered method "auto" searches of at least `batch` queries (largest such entry),
@@ -249,7 +252,9 @@ struct vsg_index {
   };
 
   // filtered: the scan runs in gather mode; per_query: every query has its own mask.
-  Plan plan(size_t nq, size_t k, bool filtered = false, bool per_query = false) const {
+  // split_nq (unfiltered only): when nonzero and below nq, the row range is split as for that
+  // many queries, with factor 1, while the launch still covers all nq.
+  Plan plan(size_t nq, size_t k, bool filtered = false, bool per_query = false, size_t split_nq = 0) const {
     Plan p{};
     p.shape.l2 = metric == VSG_METRIC_L2;
     p.shape.qb = 1;  // next power of two >= nq, at most 8; one query per CTA for per-query masks,
@@ -270,7 +275,11 @@ struct vsg_index {
                                   " does not fit the scan kernel's shared memory");
     p.nqb = uint32_t(ceil_div(nq, size_t(p.shape.qb)));
     size_t want;
-    if (!filtered) {
+    if (!filtered && split_nq && nq > split_nq) {
+      const size_t blocks = ceil_div(split_nq, size_t(p.shape.qb));
+      want = std::max<size_t>(1, size_t(sms) / blocks);
+      want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));
+    } else if (!filtered) {
       want = std::max<size_t>(1, size_t(double(std::max<size_t>(1, size_t(sms) / p.nqb)) * split_factor(nq, false)));
       want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));  // >= 256 rows per split
     } else {
@@ -831,7 +840,11 @@ struct vsg_index {
       return;
     }
     gather = gather && dmask != nullptr;
-    const Plan p = plan(nq, k, gather, gather && per_query);
+    // With a device count (the certified path's fallback) only the few queries at the front run:
+    // split the rows as for at most fallback_split_queries so that one lone query block still
+    // spans many SMs. Planned for all nq, a batch of 4096 would give that block one split, one
+    // CTA over every row. The blocks past the count cost one launch and one load each.
+    const Plan p = plan(nq, k, gather, gather && per_query, nq_dev && !gather ? size_t(fallback_split_queries) : 0);
     const size_t parts = nq * p.nsplit * k;
     part.reserve(parts * 8, 0, stream);
     vsg::ScanArgs a{};

@@ -54,10 +54,10 @@ extern "C" {
 #define VSG_METHOD_SKINNY 2u
 #define VSG_METHOD_TILED 3u
 #define VSG_METHOD_BF16 4u
-/* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The rerank kernel bounds the
- * difference between each row's bf16 approximate distance and its FP32 distance (from the bf16
- * rounding of the query and the rows), and proves that no row outside the shortlist can enter
- * the top k; the shortlist keeps each query's rows within "cert_margin" x E of its k-th best (at
+/* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The finish kernel (merge,
+ * FP32 rerank, certificate) bounds the difference between each row's bf16 approximate distance
+ * and its FP32 distance (from the bf16 rounding of the query and the rows), and proves that no
+ * row outside the shortlist can enter the top k; the shortlist keeps each query's rows within "cert_margin" x E of its k-th best (at
  * most k' = 120). Queries it cannot prove run in the streaming scan kernel, launched on the
  * device's own count of them (nothing waits on the host). Results equal VSG_METHOD_SKINNY bit for
  * bit, with or without a filter. Method AUTO uses it for unfiltered batches (k <= 32) of at least

@@ -609,9 +609,9 @@ struct vsg_index {
 
   // Exact top-k through the shortlist. Queries whose result the finish kernel cannot certify (see
   // vsg::FinishArgs) run in the streaming scan kernel, so results equal method skinny bit for bit.
-  // Nothing waits on the host: the rerank leaves the uncertified queries' count and indices on
-  // the device, and the fallback launches (gather, scan, scatter) are sized for all nq queries,
-  // their blocks past that count returning at once. A tally of uncertified queries stays on the
+  // Nothing waits on the host: the finish kernel leaves the uncertified queries' count and
+  // indices on the device, and the fallback launches (gather, scan, scatter) are sized for all nq
+  // queries, their blocks past that count returning at once (the scan's row splits: plan()). A tally of uncertified queries stays on the
   // device (tc_stats_sync reads it).
   void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                         cudaStream_t s, const uint32_t* dmask = nullptr, size_t mask_ld = 0) {

@@ -71,7 +71,7 @@ struct TcArgs {
   // Certified path (non-serving launches): per-query margin m, or nullptr. A compaction that holds
   // at least kk entries may then lower the threshold to (its kk-th best) + m, so the list keeps
   // the rows near the top kk instead of a fixed k'. Every threshold is published to gthr, and
-  // the rerank's certificate takes the smallest, so any m keeps results exact.
+  // the finish kernel's certificate takes the smallest, so any m keeps results exact.
   const float* margin;
   uint32_t kk;
   uint32_t nqb;  // query blocks (non-serving launches)

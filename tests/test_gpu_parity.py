@@ -129,6 +129,50 @@ def test_batch_invariance_bitwise(gpu_ready, method):
     O.check_ids(other[0], all_i, x, q, metric, rel=REL_TIE)
 
 
+def test_concurrent_callers_get_their_own_results(gpu_ready):
+    # Host threads searching one index at once, with different methods, k, batch sizes and
+    # filters: the index serialises its calls (one mutex per index, as the reference's
+    # GpuBruteForceIndex does, src/gpu_brute_force.cu:351,430), so each call returns what it
+    # returns alone, bit for bit.
+    import threading
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x = D.portable(30_000, 96, 300, normalize=True)
+    q = D.portable(200, 96, 301, normalize=True)
+    gpu = vsg.GpuBruteForceIndex(96, "cosine")
+    gpu.add(x)
+    mask = np.zeros(len(x), bool)
+    mask[::3] = True
+    calls = [(q[:1], 10, "auto", None), (q[:37], 5, "skinny", None), (q, 10, "tc_exact", None),
+             (q[:150], 17, "tiled", None), (q[:64], 10, "auto", mask), (q[3:133], 10, "skinny", mask)]
+    want = [gpu.search(qq, k, method=m, filter=f) for qq, k, m, f in calls]
+    got = [[] for _ in calls]
+    errors = []
+    barrier = threading.Barrier(len(calls), timeout=120)
+
+    def run(j):
+        try:
+            qq, k, m, f = calls[j]
+            barrier.wait()
+            for _ in range(4):
+                got[j].append(gpu.search(qq, k, method=m, filter=f))
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(j,)) for j in range(len(calls))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=600)
+    assert not any(t.is_alive() for t in threads)
+    assert not errors, errors
+    for j, (wi, wd) in enumerate(want):
+        assert len(got[j]) == 4
+        for gi, gd in got[j]:
+            np.testing.assert_array_equal(gi, wi)
+            np.testing.assert_array_equal(gd.view(np.uint32), wd.view(np.uint32))
+
+
 def test_duplicate_rows_tie_to_lower_id(gpu_ready):
     # Equal distances go to the lower id (brute_force.cpp:152-169 merge order).
     vsg = gpu_ready

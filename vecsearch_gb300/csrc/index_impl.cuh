@@ -288,7 +288,7 @@ struct vsg_index {
       want = std::max(ceil_div(n, 32768), ceil_div(2 * size_t(sms), p.nqb));
       want = std::max<size_t>(1, std::min(want, ceil_div(n, 1024)));
     }
-    p.rows_per_split = uint32_t(ceil_div(ceil_div(n, want), 32) * 32);
+    p.rows_per_split = vsg::split_rows(ceil_div(ceil_div(n, want), 32) * 32, 32);
     p.nsplit = uint32_t(ceil_div(n, p.rows_per_split));
     return p;
   }
@@ -313,7 +313,7 @@ struct vsg_index {
         best = sp;
       }
     }
-    const size_t rps = ceil_div(ceil_div(n, best), align) * align;
+    const size_t rps = vsg::split_rows(ceil_div(ceil_div(n, best), align) * align, align);
     *rows_per_split = uint32_t(rps);
     *nsplit = uint32_t(ceil_div(n, rps));
   }
@@ -554,7 +554,8 @@ struct vsg_index {
         // One tile per split would sample more rows than asked for (many splits, a small batch):
         // sample the first tile of each of ceil(srows / 256) ranges spread over the rows instead.
         const size_t tiles = ceil_div(size_t(n), size_t(vsg::kTcRows));
-        const size_t rps = ceil_div(tiles, ceil_div(srows, size_t(vsg::kTcRows))) * vsg::kTcRows;
+        const size_t rps =
+            vsg::split_rows(ceil_div(tiles, ceil_div(srows, size_t(vsg::kTcRows))) * vsg::kTcRows, vsg::kTcRows);
         sa.rows_per_split = uint32_t(rps);
         sa.nsplit = uint32_t(ceil_div(size_t(n), rps));
         st = 1;

@@ -102,7 +102,7 @@ extern "C" int vsg_search_rows_noalloc(const float* d_rows, size_t n, size_t dim
   const size_t nqb = ceil_div(nq, size_t(shape.qb));
   size_t want = std::max<size_t>(1, size_t(g_sms[dev]) / nqb);
   want = std::min(want, std::max<size_t>(1, ceil_div(n, 256)));
-  const size_t rows_per_split = ceil_div(ceil_div(n, want), 32) * 32;
+  const size_t rows_per_split = vsg::split_rows(ceil_div(ceil_div(n, want), 32) * 32, 32);
   const size_t nsplit = ceil_div(n, rows_per_split);
   const size_t parts = nq * nsplit * k;
   if (kStatusBytes + parts * 8 > kNoAllocScratchBytes)

@@ -87,7 +87,7 @@ __device__ __forceinline__ uint32_t block_bits(const ScanArgs& a, uint32_t qbase
       if (qbase + b < a.nq) bits |= __ldg(a.mask + size_t(qbase + b) * a.mask_ld + w);
   }
   const uint32_t lo = w * 32;
-  if (lo + 32 > row_end) bits &= (1u << (row_end - lo)) - 1u;  // 0 < row_end - lo < 32 here
+  if (row_end - lo < 32) bits &= (1u << (row_end - lo)) - 1u;  // lo < row_end (no wrap near 2^32)
   return bits;
 }
 
@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   if (a.nq_dev && qbase >= *a.nq_dev) return;
   const uint32_t split = blockIdx.y;
   const uint32_t row_begin = split * a.rows_per_split;  // a multiple of 32
-  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
+  const uint64_t end64 = uint64_t(row_begin) + a.rows_per_split;  // can pass 2^32 near 2^32 rows
+  const uint32_t row_end = end64 < a.n ? uint32_t(end64) : a.n;
   const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + R - 1) / R : 0;
   const uint32_t stages = a.stages;
   // Without a filter, or for a masked full scan, the producer copies whole tiles of
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
         if (lane == 0) got = mbar_wait(&empty[s], ph ^ 1);
         return __shfl_sync(kFull, got ? 1 : 0, 0) != 0;
       };
-      const uint32_t wend = (row_end + 31) >> 5;
+      const uint32_t wend = (row_end >> 5) + ((row_end & 31u) != 0u);
       // The next step's filter words are loaded before this step is processed, so the
       // global-load latency overlaps the compaction and the slot filling.
       uint32_t next = (row_begin >> 5) + lane < wend ? block_bits<QB>(a, qbase, (row_begin >> 5) + lane, row_end) : 0u;

@@ -52,6 +52,14 @@ struct MergeArgs {
   const uint32_t* nq_dev;
 };
 
+// Rows per split as the kernels' 32-bit argument. Rounded up to `align`, a split can reach 2^32
+// rows on an index of nearly 2^32 rows; it is capped at the largest multiple of `align` below
+// 2^32, and callers derive the split count from the capped value.
+inline uint32_t split_rows(size_t rows, size_t align) {
+  const size_t cap = (size_t(0xFFFFFFFFu) / align) * align;
+  return uint32_t(rows < cap ? rows : cap);
+}
+
 struct ScanShape {
   int qb;      // queries per CTA: 1, 2, 4 or 8
   int rw;      // rows per warp per tile: 1, 2 or 4 (tile = 8 * rw rows)

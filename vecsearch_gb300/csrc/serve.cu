@@ -197,7 +197,8 @@ struct vsg_server {
     }
     const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
     const size_t want = std::max<size_t>(1, size_t(idx->sms) / nqb);
-    const size_t rps = ceil_div(ceil_div(idx->n, want), size_t(vsg::kTcRows)) * vsg::kTcRows;
+    const size_t rps = vsg::split_rows(ceil_div(ceil_div(idx->n, want), size_t(vsg::kTcRows)) * vsg::kTcRows,
+                                       vsg::kTcRows);
     hdr->nq = uint32_t(nq);
     hdr->nqb = uint32_t(nqb);
     hdr->rows_per_split = uint32_t(rps);

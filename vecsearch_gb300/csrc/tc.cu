@@ -439,6 +439,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t qb = (item % nqg) * C + rank, split = item / nqg;
     const uint32_t qbase = qb * kTcQueries;
     const uint32_t row_begin = split * rows_per_split;
+    // No 32-bit wrap: with its FP32 rows and a bf16 or e4m3 copy (160+ bytes a row) an index
+    // holds under 2^31 rows in HBM, so row_begin + rows_per_split < 2^32.
     uint32_t row_end = min(a.n, row_begin + rows_per_split);
     const uint32_t sample_tiles = persistent ? a.hdr->sample_tiles : a.sample_tiles;
     if (a.dump) row_end = min(row_end, row_begin + sample_tiles * kTcRows);  // sample pass

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(kThreads, 1) tiled_kernel(const TiledArgs a) {
   const uint32_t qbase = blockIdx.x * BM;
   const uint32_t split = blockIdx.y;
   const uint32_t row_begin = split * a.rows_per_split;
-  const uint32_t row_end = min(a.n, row_begin + a.rows_per_split);
+  const uint64_t end64 = uint64_t(row_begin) + a.rows_per_split;  // can pass 2^32 near 2^32 rows
+  const uint32_t row_end = end64 < a.n ? uint32_t(end64) : a.n;
   const uint32_t ntiles = row_end > row_begin ? (row_end - row_begin + kBN - 1) / kBN : 0;
   const uint32_t nk = (dp + kBK - 1) / kBK;
   const uint32_t nsteps = ntiles * nk;  // (tile, k-slice) pairs, streamed through one ring

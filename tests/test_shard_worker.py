@@ -212,3 +212,36 @@ def test_lone_caller_is_not_delayed():
     assert time.perf_counter() - t < 0.5  # five 200 ms windows would take 1 s
     assert s.batches == 5
     s.close()
+
+
+def test_command_line_mirrors_the_reference_worker():
+    # distributed/shard_worker.py:44-51: the same flags (plus the GPU's own), --cpus pins the process.
+    import os
+    a = W.parse_args(["--manifest", "m.json", "--shard-id", "2", "--port", "5001", "--threads", "3",
+                      "--cpus", "0"])
+    assert (a.manifest, a.shard_id, a.port, a.threads, a.cpus) == ("m.json", 2, 5001, 3, "0")
+    assert W.parse_args(["--manifest", "m", "--shard-id", "0", "--port", "1"]).cpus == ""
+    if not hasattr(os, "sched_getaffinity"):
+        pytest.skip("no CPU affinity on this platform")
+    before = os.sched_getaffinity(0)
+    one = min(before)
+    try:
+        W.pin_cpus(str(one))
+        assert os.sched_getaffinity(0) == {one}
+        W.pin_cpus("")  # nothing listed: unchanged
+        assert os.sched_getaffinity(0) == {one}
+    finally:
+        os.sched_setaffinity(0, before)
+
+
+def test_port_clash_fails_instead_of_sharing():
+    pytest.importorskip("grpc")
+    x, _ = _data(n=50)
+    s = W.ShardSearcher(NumpyExact(x))
+    srv, port = W.serve(s, 0, threads=2, host="127.0.0.1")
+    try:
+        with pytest.raises(RuntimeError):
+            W.serve(s, port, threads=2, host="127.0.0.1")
+    finally:
+        srv.stop(0)
+        s.close()

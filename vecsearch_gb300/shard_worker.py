@@ -32,7 +32,7 @@ import numpy as np
 
 __all__ = ["encode_search_request", "decode_search_request", "encode_search_response",
            "decode_search_response", "encode_info_response", "decode_info_response",
-           "ShardSearcher", "serve", "SERVICE"]
+           "ShardSearcher", "serve", "pin_cpus", "parse_args", "SERVICE"]
 
 SERVICE = "vecsearch.Searcher"
 
@@ -306,22 +306,41 @@ def serve(searcher, port, threads=8, host="[::]"):
     server = grpc.server(futures.ThreadPoolExecutor(max_workers=threads), options=[("grpc.so_reuseport", 0)])
     server.add_generic_rpc_handlers((grpc.method_handlers_generic_handler(
         SERVICE, {"Search": call(searcher.search), "Info": call(searcher.info)}),))
-    bound = server.add_insecure_port(f"{host}:{port}")
+    try:
+        bound = server.add_insecure_port(f"{host}:{port}")
+    except RuntimeError:
+        bound = 0
+    if bound == 0:  # a port clash fails here rather than sharing it (shard_worker.py:55)
+        server.stop(0)
+        raise RuntimeError(f"could not bind {host}:{port}")
     server.start()
     return server, bound
 
 
-def main(argv=None):
+def pin_cpus(cpus):
+    """--cpus of the reference worker (distributed/shard_worker.py:48-51): pin this process to
+    the listed CPUs, e.g. "2,3" (Linux; a no-op where affinity cannot be set or nothing is listed)."""
+    if cpus and hasattr(os, "sched_setaffinity"):
+        os.sched_setaffinity(0, {int(c) for c in cpus.split(",")})
+
+
+def parse_args(argv=None):
     ap = argparse.ArgumentParser(description="GPU shard worker for the vecsearch Searcher service")
     ap.add_argument("--manifest", required=True)
     ap.add_argument("--shard-id", type=int, required=True)
     ap.add_argument("--port", type=int, required=True)
     ap.add_argument("--threads", type=int, default=8, help="gRPC handler threads")
+    ap.add_argument("--cpus", default="", help="pin to CPUs, e.g. '2,3' (Linux)")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "tc_exact"])
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--max-wait-ms", type=float, default=0.2)
-    a = ap.parse_args(argv)
+    return ap.parse_args(argv)
+
+
+def main(argv=None):
+    a = parse_args(argv)
+    pin_cpus(a.cpus)
     from . import GpuBruteForceIndex
     shard = json.load(open(a.manifest))["shards"][a.shard_id]
     path = os.path.join(os.path.dirname(os.path.abspath(a.manifest)), shard["file"])

@@ -68,3 +68,33 @@ def test_helpers():
     n = vsg.normalize(x)
     assert np.allclose(n[0], [0.6, 0.8]) and np.all(np.isfinite(n))
     assert vsg.recall_at_k(np.array([[1, 2, 3]]), np.array([[3, 2, 9]]), 3) == pytest.approx(2 / 3)
+
+
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    # What an FFI caller does: a C99 program includes the header, links the library and calls it.
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from vecsearch_gb300 import build
+    so = build.build()
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "vsg.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "  vsg_index* h = NULL;\n"
+        "  int rc = vsg_create(0, VSG_METRIC_IP, 0, &h);  /* dim 0: rejected before any CUDA call */\n"
+        '  printf("%d %d %d %s\\n", vsg_cuda_available(), rc == VSG_ERR_INVALID, h == NULL,\n'
+        "         vsg_last_error()[0] ? \"msg\" : \"none\");\n"
+        "  vsg_destroy(NULL);\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "caller"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), so, "-Wl,-rpath," + os.path.dirname(so), "-o", str(exe)], check=True,
+                   capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=120).stdout.split()
+    assert out[1:] == ["1", "1", "msg"]
+    import torch
+    if not torch.cuda.is_available():
+        assert out[0] == "0"

@@ -1,7 +1,9 @@
-"""CPU: the streaming scan's launch plan (vsg_index::plan in vecsearch_gb300/csrc/index_impl.cuh),
-compiled from the library's own source into a host-only harness (tests/split_plan_main.cu, no
-CUDA calls). The splits cover every row exactly once with 32-bit sizes up to 2^32 - 2 rows, and
-the certified path's fallback scan splits as for at most 128 queries."""
+"""CPU: the index's planning logic (vecsearch_gb300/csrc/index_impl.cuh), compiled from the
+library's own source into a host-only harness (tests/split_plan_main.cu, no CUDA calls).
+- The streaming scan's launch plan: the splits cover every row exactly once with 32-bit sizes up to
+  2^32 - 2 rows, and the certified path's fallback scan splits as for at most 128 queries.
+- Method auto's routing between the certified path, the tiled and the scan kernel, at the
+  boundaries include/vsg.h documents."""
 import os
 import subprocess
 
@@ -26,7 +28,7 @@ def harness(tmp_path_factory):
                     "-Xlinker", "-rpath=" + lib_dir], check=True, capture_output=True, timeout=600)
 
     def plan(cases):
-        text = "".join(f"{n} {dp} {nq} {k} {s} {sms} {m}\n" for n, dp, nq, k, s, sms, m in cases)
+        text = "".join(f"plan {n} {dp} {nq} {k} {s} {sms} {m}\n" for n, dp, nq, k, s, sms, m in cases)
         out = subprocess.run([exe], input=text, capture_output=True, text=True, check=True, timeout=120).stdout
         rows = []
         for line in out.splitlines():
@@ -36,6 +38,14 @@ def harness(tmp_path_factory):
         assert len(rows) == len(cases)
         return rows
 
+    def route(cases):
+        text = "".join("route %d %d %d %d %d %d %d %r\n" % c for c in cases)
+        out = subprocess.run([exe], input=text, capture_output=True, text=True, check=True, timeout=120).stdout
+        rows = [tuple(map(int, line.split())) for line in out.splitlines()]
+        assert len(rows) == len(cases)
+        return rows
+
+    plan.route = route
     return plan
 
 
@@ -71,3 +81,46 @@ def test_near_2_to_32_rows(harness):
     n = 2**32 - 2
     p = harness([(n, 8, 4096, 10, 0, SMS, 0)])[0]  # one split wanted: capped below 2^32
     assert p["rps"] == 2**32 - 32 and p["nsplit"] == 2
+
+
+AUTO, SKINNY, TILED, BF16, TC_EXACT = 0, 2, 3, 4, 5
+
+
+def test_auto_routing(harness):
+    big, small = 1_000_000, 100_000  # rows at d = 384: above and below 2^27 elements
+    edge = 2**27 // 384  # 349,525 rows: 2^27 - 128 elements; one more row reaches 2^27
+    # (n, dp, nq, k, method, masked, gather, allowed) -> (certified path, tiled kernel)
+    want = {
+        (big, 384, 1, 10, AUTO, 0, 0, -1.0): (1, 0),       # a large index: every batch size
+        (big, 384, 1, 32, AUTO, 0, 0, -1.0): (1, 0),
+        (big, 384, 1, 33, AUTO, 0, 0, -1.0): (0, 0),       # k > 32: the FP32 kernels
+        (big, 384, 64, 100, AUTO, 0, 0, -1.0): (0, 1),
+        (small, 384, 1, 10, AUTO, 0, 0, -1.0): (0, 0),
+        (small, 384, 47, 10, AUTO, 0, 0, -1.0): (0, 0),
+        (small, 384, 48, 10, AUTO, 0, 0, -1.0): (0, 1),    # tiled_min_batch
+        (small, 384, 127, 10, AUTO, 0, 0, -1.0): (0, 1),
+        (small, 384, 128, 10, AUTO, 0, 0, -1.0): (1, 1),   # tc_exact_min_batch (checked first)
+        (edge, 384, 1, 10, AUTO, 0, 0, -1.0): (0, 0),
+        (edge + 1, 384, 1, 10, AUTO, 0, 0, -1.0): (1, 0),  # tc_exact_min_elements
+        (small, 384, 1, 120, TC_EXACT, 0, 0, -1.0): (1, 0),
+        (small, 384, 1, 121, TC_EXACT, 0, 0, -1.0): (0, 0),  # k' is capped at 120
+        (big, 384, 500, 10, SKINNY, 0, 0, -1.0): (0, 0),
+        (big, 384, 500, 10, TILED, 0, 0, -1.0): (0, 1),
+        (big, 384, 500, 10, BF16, 0, 0, -1.0): (0, 0),
+        # host masks, largest allowed fraction known
+        (big, 384, 7, 10, AUTO, 1, 0, 0.5): (0, 0),        # fewer than 8 queries
+        (big, 384, 8, 10, AUTO, 1, 1, 0.05): (1, 0),       # 8 x 0.05 >= 0.35
+        (big, 384, 8, 10, AUTO, 1, 1, 0.04): (0, 0),       # 8 x 0.04 < 0.35, gather scan
+        (big, 384, 8, 10, AUTO, 1, 0, 0.04): (1, 0),       # no gather: the masked full scan
+        (big, 384, 63, 10, AUTO, 1, 1, 0.001): (0, 0),
+        (big, 384, 64, 10, AUTO, 1, 1, 0.001): (1, 0),     # half of tc_exact_min_batch
+        (big, 384, 64, 33, AUTO, 1, 0, 0.5): (0, 0),       # k > 32
+        # device masks, fraction unknown
+        (big, 384, 127, 10, AUTO, 1, 0, -1.0): (0, 0),
+        (big, 384, 128, 10, AUTO, 1, 0, -1.0): (1, 0),
+        (big, 384, 255, 10, AUTO, 1, 1, -1.0): (0, 0),
+        (big, 384, 256, 10, AUTO, 1, 1, -1.0): (1, 0),     # twice the threshold with gather
+    }
+    got = harness.route(list(want))
+    for case, g in zip(want, got):
+        assert g == want[case], (case, g)

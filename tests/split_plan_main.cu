@@ -1,30 +1,40 @@
 // Test harness (host only, no CUDA calls) for the index's planning logic in
-// vecsearch_gb300/csrc/index_impl.cuh. Reads cases from stdin, one per line:
-//   plan  n dp nq k split_nq sms metric         -> "qb rw stages nqb rows_per_split nsplit"
+// vecsearch_gb300/csrc/index_impl.cuh. One index lives across the commands read from stdin, one
+// per line:
+//   plan  n dp nq k split_nq sms metric          -> "qb rw stages nqb rows_per_split nsplit"
 //   route n dp nq k method masked gather allowed -> "tc_exact tiled" (1 / 0 each)
-// (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). Built and run by
-// tests/test_split_plan.py.
+//   load PATH | save PATH                        -> the status of vsg_autotune_load / _save
+//   table method                                 -> "count" then "batch choice split extra" lines
+//   reset                                        -> a fresh index (empty tuning tables)
+// (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The tuning commands go
+// through the library's C ABI with this host-built index. Built and run by tests/test_split_plan.py.
 #include <cstdio>
 #include <cstring>
+#include <memory>
 
 #include "../vecsearch_gb300/csrc/index_impl.cuh"
 
+static std::unique_ptr<vsg_index> fresh() {
+  std::unique_ptr<vsg_index> h(new vsg_index);  // no stream, events or buffers: nothing here touches the device
+  h->sms = 152;
+  h->smem_optin = 232448;  // 227 KB, the opt-in shared memory of a GB300 CTA
+  return h;
+}
+
 int main() {
+  std::unique_ptr<vsg_index> idx = fresh();
   char cmd[16];
   while (std::scanf("%15s", cmd) == 1) {
-    vsg_index idx;  // no stream, events or buffers: nothing here touches the device
-    idx.sms = 152;
-    idx.smem_optin = 232448;  // 227 KB, the opt-in shared memory of a GB300 CTA
     unsigned long long n, dp, nq, k;
     if (std::strcmp(cmd, "plan") == 0) {
       unsigned long long split_nq, sms, metric;
       if (std::scanf("%llu %llu %llu %llu %llu %llu %llu", &n, &dp, &nq, &k, &split_nq, &sms, &metric) != 7) return 1;
-      idx.dim = idx.dp = dp;
-      idx.n = n;
-      idx.sms = int(sms);
-      idx.metric = uint32_t(metric);
+      idx->dim = idx->dp = dp;
+      idx->n = n;
+      idx->sms = int(sms);
+      idx->metric = uint32_t(metric);
       try {
-        const auto p = idx.plan(nq, k, false, false, split_nq);
+        const auto p = idx->plan(nq, k, false, false, split_nq);
         std::printf("%d %d %u %u %u %u\n", p.shape.qb, p.shape.rw, p.stages, p.nqb, p.rows_per_split, p.nsplit);
       } catch (const std::exception& e) {
         std::printf("error %s\n", e.what());
@@ -35,15 +45,32 @@ int main() {
       if (std::scanf("%llu %llu %llu %llu %llu %llu %llu %lf", &n, &dp, &nq, &k, &method, &masked, &gather,
                      &allowed) != 8)
         return 1;
-      idx.dim = idx.dp = dp;
-      idx.n = n;
+      idx->dim = idx->dp = dp;
+      idx->n = n;
       static const uint32_t word = ~0u;  // stands for a mask; never read
       const uint32_t* m = masked ? &word : nullptr;
-      std::printf("%d %d\n", idx.use_tc_exact(uint32_t(method), nq, k, m, gather != 0, allowed) ? 1 : 0,
-                  idx.use_tiled(uint32_t(method), nq, m) ? 1 : 0);
+      std::printf("%d %d\n", idx->use_tc_exact(uint32_t(method), nq, k, m, gather != 0, allowed) ? 1 : 0,
+                  idx->use_tiled(uint32_t(method), nq, m) ? 1 : 0);
+    } else if (std::strcmp(cmd, "load") == 0 || std::strcmp(cmd, "save") == 0) {
+      char path[4096];
+      if (std::scanf("%4095s", path) != 1) return 1;
+      const int rc = cmd[0] == 'l' ? vsg_autotune_load(idx.get(), path) : vsg_autotune_save(idx.get(), path);
+      std::printf("%d\n", rc);
+    } else if (std::strcmp(cmd, "table") == 0) {
+      unsigned method;
+      if (std::scanf("%u", &method) != 1) return 1;
+      size_t count = 64;
+      uint32_t batch[64], choice[64], extra[64];
+      double split[64];
+      if (vsg_autotune_table(idx.get(), method, &count, batch, choice, split, extra) != VSG_OK) return 1;
+      std::printf("%zu\n", count);
+      for (size_t i = 0; i < count && i < 64; ++i) std::printf("%u %u %.3f %u\n", batch[i], choice[i], split[i], extra[i]);
+    } else if (std::strcmp(cmd, "reset") == 0) {
+      idx = fresh();
     } else {
       return 1;
     }
+    std::fflush(stdout);
   }
   return 0;
 }

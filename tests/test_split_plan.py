@@ -3,7 +3,9 @@ library's own source into a host-only harness (tests/split_plan_main.cu, no CUDA
 - The streaming scan's launch plan: the splits cover every row exactly once with 32-bit sizes up to
   2^32 - 2 rows, and the certified path's fallback scan splits as for at most 128 queries.
 - Method auto's routing between the certified path, the tiled and the scan kernel, at the
-  boundaries include/vsg.h documents."""
+  boundaries include/vsg.h documents, and under a tuning table.
+- The tuning file (vsg_autotune_save / _load through the C ABI): round trip, malformed lines
+  skipped, files without the header rejected."""
 import os
 import subprocess
 
@@ -45,7 +47,13 @@ def harness(tmp_path_factory):
         assert len(rows) == len(cases)
         return rows
 
+    def raw(lines):
+        out = subprocess.run([exe], input="".join(l + "\n" for l in lines), capture_output=True, text=True,
+                             check=True, timeout=120).stdout
+        return out.splitlines()
+
     plan.route = route
+    plan.raw = raw
     return plan
 
 
@@ -124,3 +132,65 @@ def test_auto_routing(harness):
     got = harness.route(list(want))
     for case, g in zip(want, got):
         assert g == want[case], (case, g)
+
+
+TUNING = """vsg-tuning 1 dim 384 rows 1000000 metric 1 sms 152
+plain 1 2 1.000 120
+plain 48 1 2.000 0
+plain 128 2 1.000 200
+plain 256 3 1.000 0
+plain 512 1 0.000 0
+plain 1024 0 1.500
+bf16 8 16384 2
+bf16 64 4096 3
+bf16 128 0
+bf16 256 2000000 1
+junk line
+"""
+PLAIN_TABLE = [("1", "2", "1.000", "120"), ("48", "1", "2.000", "0"), ("128", "2", "1.000", "0"),
+         ("1024", "0", "1.500", "0")]  # kernel 3, split 0 dropped; a first pass above 128 reads as none
+BF16_TABLE = [("8", "16384", "1.000", "2"), ("128", "0", "1.000", "0")]  # cluster 3, sample > 2^20 dropped
+
+
+def _tables(lines):
+    out, i = [], 0
+    while i < len(lines):
+        n = int(lines[i])
+        out.append([tuple(l.split()) for l in lines[i + 1:i + 1 + n]])
+        i += 1 + n
+    return out
+
+
+def test_tuning_file_round_trip(harness, tmp_path):
+    src, dst = tmp_path / "in.txt", tmp_path / "out.txt"
+    src.write_text(TUNING)
+    out = harness.raw([f"load {src}", "table 0", "table 4", f"save {dst}", "reset", "table 0",
+                       f"load {dst}", "table 0", "table 4"])
+    assert out[0] == "0"
+    t = _tables(out[1:1 + 1 + len(PLAIN_TABLE) + 1 + len(BF16_TABLE)])
+    assert t == [PLAIN_TABLE, BF16_TABLE]
+    rest = out[1 + 1 + len(PLAIN_TABLE) + 1 + len(BF16_TABLE):]
+    assert rest[0] == "0" and rest[1] == "0" and rest[2] == "0"  # saved; a fresh index is untuned; reloaded
+    assert _tables(rest[3:]) == [PLAIN_TABLE, BF16_TABLE]
+    assert dst.read_text().startswith("vsg-tuning 1 dim 0 rows 0 metric 0 sms 152")
+
+
+def test_tuning_file_rejects(harness, tmp_path):
+    bad = tmp_path / "bad.txt"
+    bad.write_text("plain 1 2 1.000 120\n")  # no header
+    out = harness.raw([f"load {bad}", f"load {tmp_path / 'missing.txt'}", "table 0"])
+    assert out == ["1", "1", "0"]  # VSG_ERR_INVALID twice; the tables stay empty
+
+
+def test_routing_follows_a_tuning_table(harness, tmp_path):
+    src = tmp_path / "in.txt"
+    src.write_text(TUNING)
+    assert harness.raw([f"load {src}"]) == ["0"]
+    small = 100_000  # below 2^27 elements: untuned, batch 1 would take the scan kernel
+    cases = [(nq, want) for nq, want in ((1, "1 0"), (47, "1 0"), (48, "0 1"), (127, "0 1"), (128, "1 0"),
+                                         (1023, "1 0"), (1024, "0 0"), (5000, "0 0"))]
+    out = harness.raw([f"load {src}"] + [f"route {small} 384 {nq} 10 0 0 0 -1.0" for nq, _ in cases] +
+                      [f"route {small} 384 200 10 0 1 0 0.5"])  # masks ignore the table
+    assert out[0] == "0"
+    assert out[1:-1] == [w for _, w in cases]
+    assert out[-1] == "1 0"

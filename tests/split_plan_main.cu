@@ -1,16 +1,22 @@
-// Test harness (host only, no CUDA calls) for the index's planning logic in
-// vecsearch_gb300/csrc/index_impl.cuh. One index lives across the commands read from stdin, one
+// Test harness (host only, no CUDA calls) for the index's host logic in
+// vecsearch_gb300/csrc/index_impl.cuh and index.cu. One index lives across the commands read from stdin, one
 // per line:
 //   plan  n dp nq k split_nq sms metric          -> "qb rw stages nqb rows_per_split nsplit"
 //   route n dp nq k method masked gather allowed -> "tc_exact tiled" (1 / 0 each)
 //   load PATH | save PATH                        -> the status of vsg_autotune_load / _save
 //   table method                                 -> "count" then "batch choice split extra" lines
 //   reset                                        -> a fresh index (empty tuning tables)
-// (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The tuning commands go
-// through the library's C ABI with this host-built index. Built and run by tests/test_split_plan.py.
+//   set NAME value | get NAME                    -> vsg_set_tunable's status | "status value"
+//   below n nq k exact_below pattern             -> "status handled id dist" after
+//       vsg_hnsw_exact_below on a byte mask of n rows (pattern 0: none allowed, 1: all, m > 1:
+//       every m-th row; -1: no mask; -2: a mask one row short), outputs preset to 7 / 7.0.
+//       Only cases that stay on the host: no mask, too many allowed rows, or none allowed.
+// (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The load, save, table,
+// set, get and below commands go through the library's C ABI with this host-built index. Built and run by tests/test_split_plan.py.
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <vector>
 
 #include "../vecsearch_gb300/csrc/index_impl.cuh"
 
@@ -65,6 +71,32 @@ int main() {
       if (vsg_autotune_table(idx.get(), method, &count, batch, choice, split, extra) != VSG_OK) return 1;
       std::printf("%zu\n", count);
       for (size_t i = 0; i < count && i < 64; ++i) std::printf("%u %u %.3f %u\n", batch[i], choice[i], split[i], extra[i]);
+    } else if (std::strcmp(cmd, "set") == 0 || std::strcmp(cmd, "get") == 0) {
+      char name[64];
+      double v = 0;
+      if (std::scanf("%63s", name) != 1) return 1;
+      if (cmd[0] == 's') {
+        if (std::scanf("%lf", &v) != 1) return 1;
+        std::printf("%d\n", vsg_set_tunable(idx.get(), name, v));
+      } else {
+        const int rc = vsg_get_tunable(idx.get(), name, &v);
+        std::printf("%d %.17g\n", rc, v);
+      }
+    } else if (std::strcmp(cmd, "below") == 0) {
+      unsigned long long eb;
+      long long pattern;
+      if (std::scanf("%llu %llu %llu %llu %lld", &n, &nq, &k, &eb, &pattern) != 5) return 1;
+      idx->n = n;
+      idx->dim = idx->dp = 8;
+      std::vector<uint8_t> mask(n + 1, 0);
+      for (size_t i = 0; i < n; ++i) mask[i] = pattern == 1 || (pattern > 1 && i % size_t(pattern) == 0);
+      std::vector<float> q(nq * 8 + 8, 0.f);
+      std::vector<uint32_t> ids(nq * k + 1, 7u);
+      std::vector<float> d(nq * k + 1, 7.f);
+      int handled = -1;
+      const int rc = vsg_hnsw_exact_below(idx.get(), q.data(), nq, k, pattern == -1 ? nullptr : mask.data(),
+                                          pattern == -2 ? n - 1 : n, eb, ids.data(), d.data(), &handled);
+      std::printf("%d %d %u %g\n", rc, handled, ids[0], double(d[0]));
     } else if (std::strcmp(cmd, "reset") == 0) {
       idx = fresh();
     } else {

@@ -5,7 +5,9 @@ library's own source into a host-only harness (tests/split_plan_main.cu, no CUDA
 - Method auto's routing between the certified path, the tiled and the scan kernel, at the
   boundaries include/vsg.h documents, and under a tuning table.
 - The tuning file (vsg_autotune_save / _load through the C ABI): round trip, malformed lines
-  skipped, files without the header rejected."""
+  skipped, files without the header rejected.
+- Tunables' ranges (vsg_set_tunable / _get_tunable) and the exact_below switch's branches that
+  stay on the host (src/hnsw.cpp:325-328)."""
 import os
 import subprocess
 
@@ -194,3 +196,31 @@ def test_routing_follows_a_tuning_table(harness, tmp_path):
     assert out[0] == "0"
     assert out[1:-1] == [w for _, w in cases]
     assert out[-1] == "1 0"
+
+
+def test_tunables_through_the_abi(harness):
+    out = harness.raw(["get fallback_split_queries", "set fallback_split_queries 512", "get fallback_split_queries",
+                       "set fallback_split_queries 0", "get fallback_split_queries",
+                       "set fallback_split_queries -1", "set fallback_split_queries 2000000",
+                       "get cert_margin", "set cert_margin 0.5", "set cert_margin 2", "get cert_margin",
+                       "get tc_exact_min_elements", "set no_such_tunable 1", "get no_such_tunable"])
+    assert out[0] == "0 128" and out[1] == "0" and out[2] == "0 512" and out[3] == "0" and out[4] == "0 0"
+    assert out[5] == "1" and out[6] == "1"  # VSG_ERR_INVALID: out of range
+    assert out[7] == "0 1.3" and out[8] == "1" and out[9] == "0" and out[10] == "0 2"
+    assert out[11] == "0 134217728"
+    assert out[12] == "1" and out[13].split()[0] == "1"
+
+
+def test_exact_below_host_branches(harness):
+    # src/hnsw.cpp:325-328: no allowed row -> empty results; more than exact_below -> the graph.
+    out = harness.raw(["below 100 2 5 10 0",     # none allowed: handled, filled with none / +inf
+                       "below 100 2 5 10 1",     # 100 allowed > 10: the graph path, nothing written
+                       "below 100 2 5 0 3",      # exact_below 0, 34 allowed: the graph path
+                       "below 100 2 5 10 -1",    # no mask: the graph path
+                       "below 100 2 5 10 -2",    # a mask one row short: ValueError
+                       "below 100 2 129 10 0",   # k > 128: ValueError
+                       "below 100 0 5 10 0"])    # no queries: handled, nothing to write
+    assert out[0] == "0 1 4294967295 inf"
+    assert out[1] == "0 0 7 7" and out[2] == "0 0 7 7" and out[3] == "0 0 7 7"
+    assert out[4].split()[0] == "1" and out[5].split()[0] == "1"
+    assert out[6] == "0 1 7 7"

@@ -11,6 +11,10 @@
 //       vsg_hnsw_exact_below on a byte mask of n rows (pattern 0: none allowed, 1: all, m > 1:
 //       every m-th row; -1: no mask; -2: a mask one row short), outputs preset to 7 / 7.0.
 //       Only cases that stay on the host: no mask, too many allowed rows, or none allowed.
+//   add held m null                              -> vsg_add's status on an index holding `held` rows
+//       (only cases that fail or return before a copy: m = 0, NULL rows, too many rows)
+//   search n nq k method per_query mask_ld       -> "status id dist" of vsg_search_filtered with a
+//       mask when mask_ld > 0 (only cases that stay on the host: bad arguments, nq or k = 0, n = 0)
 // (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The load, save, table,
 // set, get and below commands go through the library's C ABI with this host-built index. Built and run by tests/test_split_plan.py.
 #include <cstdio>
@@ -97,6 +101,25 @@ int main() {
       const int rc = vsg_hnsw_exact_below(idx.get(), q.data(), nq, k, pattern == -1 ? nullptr : mask.data(),
                                           pattern == -2 ? n - 1 : n, eb, ids.data(), d.data(), &handled);
       std::printf("%d %d %u %g\n", rc, handled, ids[0], double(d[0]));
+    } else if (std::strcmp(cmd, "add") == 0) {
+      unsigned long long held, m, null_rows;
+      if (std::scanf("%llu %llu %llu", &held, &m, &null_rows) != 3) return 1;
+      idx->n = held;
+      idx->dim = idx->dp = 8;
+      float row[8] = {0};
+      std::printf("%d\n", vsg_add(idx.get(), null_rows ? nullptr : row, m));
+    } else if (std::strcmp(cmd, "search") == 0) {
+      unsigned long long method, per_query, mask_ld;
+      if (std::scanf("%llu %llu %llu %llu %llu %llu", &n, &nq, &k, &method, &per_query, &mask_ld) != 6) return 1;
+      idx->n = n;
+      idx->dim = idx->dp = 8;
+      std::vector<float> q(nq * 8 + 8, 0.f);
+      std::vector<uint32_t> words(nq * (mask_ld + 1) + 1, ~0u);
+      std::vector<uint32_t> ids(nq * k + 1, 7u);
+      std::vector<float> d(nq * k + 1, 7.f);
+      const int rc = vsg_search_filtered(idx.get(), q.data(), nq, k, mask_ld ? words.data() : nullptr, int(per_query),
+                                         mask_ld, ids.data(), d.data(), uint32_t(method));
+      std::printf("%d %u %g\n", rc, ids[0], double(d[0]));
     } else if (std::strcmp(cmd, "reset") == 0) {
       idx = fresh();
     } else {

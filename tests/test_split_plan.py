@@ -6,8 +6,8 @@ library's own source into a host-only harness (tests/split_plan_main.cu, no CUDA
   boundaries include/vsg.h documents, and under a tuning table.
 - The tuning file (vsg_autotune_save / _load through the C ABI): round trip, malformed lines
   skipped, files without the header rejected.
-- Tunables' ranges (vsg_set_tunable / _get_tunable) and the exact_below switch's branches that
-  stay on the host (src/hnsw.cpp:325-328)."""
+- Tunables' ranges (vsg_set_tunable / _get_tunable), the exact_below switch's branches that
+  stay on the host (src/hnsw.cpp:325-328), and add / search argument rules and the empty index."""
 import os
 import subprocess
 
@@ -224,3 +224,27 @@ def test_exact_below_host_branches(harness):
     assert out[1] == "0 0 7 7" and out[2] == "0 0 7 7" and out[3] == "0 0 7 7"
     assert out[4].split()[0] == "1" and out[5].split()[0] == "1"
     assert out[6] == "0 1 7 7"
+
+
+def test_add_and_search_argument_rules(harness):
+    # src/gpu_brute_force.cu:408 (length_error past 2^32 - 2 rows), :294-298 (k > 128), :427-435
+    # (empty index: none / +inf), bindings.cpp:165-186 (an unknown method is a ValueError).
+    full = 2**32 - 2
+    out = harness.raw([f"add {full} 1 0",         # 2^32 - 1 rows: VSG_ERR_LENGTH
+                       f"add {full - 1} 2 0",
+                       "add 10 0 1",              # m = 0: a no-op, even with NULL rows
+                       "add 10 3 1",              # NULL rows: VSG_ERR_INVALID
+                       "search 0 2 5 0 0 0",      # empty index: filled with none / +inf
+                       "search 0 2 5 9 0 0",      # unknown method
+                       "search 0 2 129 0 0 0",    # k > 128
+                       "search 50 0 5 0 0 0",     # nq = 0: a no-op
+                       "search 50 2 0 0 0 0",     # k = 0: a no-op
+                       "search 100 2 5 0 1 3",    # per-query masks closer than ceil(100 / 32) words
+                       "search 0 2 5 4 1 1"])     # empty index, any method and mask: filled
+    assert out[0] == "2" and out[1] == "2"
+    assert out[2] == "0" and out[3] == "1"
+    assert out[4] == "0 4294967295 inf"
+    assert out[5].split()[0] == "1" and out[6].split()[0] == "1"
+    assert out[7] == "0 7 7" and out[8] == "0 7 7"
+    assert out[9].split()[0] == "1"
+    assert out[10] == "0 4294967295 inf"

@@ -16,7 +16,7 @@
 //   search n nq k method per_query mask_ld       -> "status id dist" of vsg_search_filtered with a
 //       mask when mask_ld > 0 (only cases that stay on the host: bad arguments, nq or k = 0, n = 0)
 // (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The load, save, table,
-// set, get and below commands go through the library's C ABI with this host-built index. Built and run by tests/test_split_plan.py.
+// set, get and below commands go through the library's C ABI with this host-built index. Built and run by tests/test_host_logic.py.
 #include <cstdio>
 #include <cstring>
 #include <memory>

@@ -1,5 +1,5 @@
 """CPU: the index's planning logic (vecsearch_gb300/csrc/index_impl.cuh), compiled from the
-library's own source into a host-only harness (tests/split_plan_main.cu, no CUDA calls).
+library's own source into a host-only harness (tests/host_logic_main.cu, no CUDA calls).
 - The streaming scan's launch plan: the splits cover every row exactly once with 32-bit sizes up to
   2^32 - 2 rows, and the certified path's fallback scan splits as for at most 128 queries.
 - Method auto's routing between the certified path, the tiled and the scan kernel, at the
@@ -25,10 +25,10 @@ def harness(tmp_path_factory):
     if not os.path.exists(nvcc):
         pytest.skip("no nvcc")
     so = build.build()
-    exe = str(tmp_path_factory.mktemp("plan") / "split_plan")
+    exe = str(tmp_path_factory.mktemp("plan") / "host_logic")
     lib_dir = os.path.dirname(so)
     subprocess.run([nvcc, *build.ARCH, "-std=c++17", "-O1", "--expt-relaxed-constexpr",
-                    os.path.join(ROOT, "tests", "split_plan_main.cu"), "-o", exe, "-L", lib_dir, "-lvsg_gb300",
+                    os.path.join(ROOT, "tests", "host_logic_main.cu"), "-o", exe, "-L", lib_dir, "-lvsg_gb300",
                     "-Xlinker", "-rpath=" + lib_dir], check=True, capture_output=True, timeout=600)
 
     def plan(cases):

@@ -1,6 +1,6 @@
 // Test harness (host only, no CUDA calls) for the index's host logic in
-// vecsearch_gb300/csrc/index_impl.cuh and index.cu. One index lives across the commands read from stdin, one
-// per line:
+// vecsearch_gb300/csrc/index_impl.cuh and index.cu. One index lives across the commands read
+// from stdin, one per line:
 //   plan  n dp nq k split_nq sms metric          -> "qb rw stages nqb rows_per_split nsplit"
 //   route n dp nq k method masked gather allowed -> "tc_exact tiled" (1 / 0 each)
 //   load PATH | save PATH                        -> the status of vsg_autotune_load / _save
@@ -16,7 +16,8 @@
 //   search n nq k method per_query mask_ld       -> "status id dist" of vsg_search_filtered with a
 //       mask when mask_ld > 0 (only cases that stay on the host: bad arguments, nq or k = 0, n = 0)
 // (metric 0 = L2, 1 = IP; method as VSG_METHOD_*; allowed < 0 = unknown). The load, save, table,
-// set, get and below commands go through the library's C ABI with this host-built index. Built and run by tests/test_host_logic.py.
+// set, get, below, add and search commands go through the library's C ABI with this host-built
+// index. Built and run by tests/test_host_logic.py.
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -74,7 +75,8 @@ int main() {
       double split[64];
       if (vsg_autotune_table(idx.get(), method, &count, batch, choice, split, extra) != VSG_OK) return 1;
       std::printf("%zu\n", count);
-      for (size_t i = 0; i < count && i < 64; ++i) std::printf("%u %u %.3f %u\n", batch[i], choice[i], split[i], extra[i]);
+      for (size_t i = 0; i < count && i < 64; ++i)
+        std::printf("%u %u %.3f %u\n", batch[i], choice[i], split[i], extra[i]);
     } else if (std::strcmp(cmd, "set") == 0 || std::strcmp(cmd, "get") == 0) {
       char name[64];
       double v = 0;

@@ -98,3 +98,30 @@ def test_header_is_plain_c_and_links(lib, tmp_path):
     import torch
     if not torch.cuda.is_available():
         assert out[0] == "0"
+
+
+def test_filter_masks_follow_as_mask():
+    # python/bindings.cpp:18,28-36: None, or a 1-D array of len(index) entries cast to uint8
+    # (forcecast: 0.5 -> 0, 256 -> 0), nonzero = allowed; here also one mask per query (nq x n).
+    import vecsearch_gb300 as vsg
+
+    class Rows:  # _mask_words needs only the index's length
+        def __len__(self):
+            return 70
+
+    words = lambda f, nq=5: vsg.GpuBruteForceIndex._mask_words(Rows(), f, nq)
+    m = np.zeros(70, bool)
+    m[[0, 33, 69]] = True
+    w, per_query, ld = words(m)
+    assert (per_query, ld) == (0, 0) and w.tolist() == [1, 2, 32]
+    for same in (m.astype(np.uint8), m.astype(np.int64) * 3, m.astype(np.float32)):
+        assert words(same)[0].tolist() == [1, 2, 32]
+    cast = m.astype(np.float64) * 0.5  # 0.5 casts to 0: nothing allowed
+    cast[1] = 256.0  # wraps to 0 in the cast as well
+    cast[2] = 1.5  # 1
+    assert words(cast)[0].tolist() == [4, 0, 0]
+    w, per_query, ld = words(np.stack([m, ~m, m, m, m]))
+    assert (per_query, ld) == (1, 3) and w.shape == (5, 3) and w[1, 0] == (~1) & 0xFFFFFFFF
+    for bad in (np.zeros(69, bool), np.zeros((4, 70), bool), np.zeros((5, 71), bool), np.zeros((1, 5, 70), bool)):
+        with pytest.raises(ValueError):
+            words(bad)

@@ -59,8 +59,18 @@ def _parse_metric(metric):
 
 
 def _as_f32(a):
-    """py::array_t<float, c_style | forcecast> (bindings.cpp:18)."""
+    """py::array_t<float, c_style | forcecast> (bindings.cpp:17)."""
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _as_mask_u8(a):
+    """py::array_t<uint8_t, c_style | forcecast> (bindings.cpp:18): a mask of any numeric type is
+    cast to uint8 first (0.5 -> 0, 256 -> 0), then a nonzero byte allows its row."""
+    a = np.asarray(a)
+    if a.dtype == np.bool_ or a.dtype == np.uint8:
+        return a
+    with np.errstate(all="ignore"):  # the same unchecked cast numpy's forcecast makes
+        return a.astype(np.uint8)
 
 
 def _check_2d(a, dim):
@@ -131,7 +141,7 @@ class GpuBruteForceIndex:
     def _mask_words(self, filter, nq):
         """(words, per_query, ld) for the C ABI, with as_mask's validation (bindings.cpp:28-36)."""
         n = len(self)
-        f = np.asarray(filter)
+        f = _as_mask_u8(filter)
         if f.ndim == 1 and f.shape[0] == n:
             return np.ascontiguousarray(pack_bits(f)), 0, 0
         if f.ndim == 2 and f.shape == (nq, n):
@@ -284,7 +294,7 @@ class Server:
             if words.ndim != 1 or words.shape[0] != (len(self.index) + 31) // 32:
                 raise ValueError("filter_words must hold ceil(len(index) / 32) uint32 words")
         elif filter is not None:
-            f = np.asarray(filter)
+            f = _as_mask_u8(filter)
             if f.ndim != 1 or f.shape[0] != len(self.index):
                 raise ValueError(f"filter must be a 1-D bool array of length {len(self.index)}")
             words = np.ascontiguousarray(pack_bits(f))
@@ -343,7 +353,7 @@ class HNSWExactRoute:
         ids = np.empty((nq, k), np.uint32)
         dists = np.empty((nq, k), np.float32)
         if filter is not None:
-            mask = np.asarray(filter)
+            mask = _as_mask_u8(filter)
             if mask.ndim != 1 or mask.shape[0] != len(self.gpu):
                 raise ValueError(f"filter must be a 1-D bool array of length {len(self.gpu)}")
             mask = np.ascontiguousarray(mask != 0, dtype=np.uint8)

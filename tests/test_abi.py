@@ -125,3 +125,12 @@ def test_filter_masks_follow_as_mask():
     for bad in (np.zeros(69, bool), np.zeros((4, 70), bool), np.zeros((5, 71), bool), np.zeros((1, 5, 70), bool)):
         with pytest.raises(ValueError):
             words(bad)
+
+
+def test_k_converts_like_size_t():
+    # bindings.cpp:167 and :79 take k as size_t: integers (and numpy integers) >= 0 only.
+    import vecsearch_gb300 as vsg
+    assert vsg._as_k(10) == 10 and vsg._as_k(np.int64(5)) == 5 and vsg._as_k(0) == 0
+    for bad in (-1, 10.0, "10", None):
+        with pytest.raises(TypeError):
+            vsg._as_k(bad)

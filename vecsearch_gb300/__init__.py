@@ -12,6 +12,7 @@ Drop-in names (python/vecsearch/__init__.py and python/bindings.cpp of vecsearch
 * :class:`HNSWExactRoute` - the HNSW index's ``exact_below`` switch on the GPU.
 """
 import ctypes
+import operator
 
 import numpy as np
 
@@ -61,6 +62,18 @@ def _parse_metric(metric):
 def _as_f32(a):
     """py::array_t<float, c_style | forcecast> (bindings.cpp:17)."""
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _as_k(k):
+    """k as pybind converts it to size_t (bindings.cpp:167, :79): an integer (or anything with
+    __index__) that is not negative; anything else is a TypeError."""
+    try:
+        v = operator.index(k)
+    except TypeError:
+        raise TypeError(f"k must be a non-negative integer, got {k!r}") from None
+    if v < 0:
+        raise TypeError(f"k must be a non-negative integer, got {k!r}")
+    return v
 
 
 def _as_mask_u8(a):
@@ -157,9 +170,7 @@ class GpuBruteForceIndex:
         if q.ndim == 1:
             q = q.reshape(1, q.shape[0])
         _check_2d(q, self._dim)
-        k = int(k)
-        if k < 0:
-            raise ValueError("k must be >= 0")
+        k = _as_k(k)
         nq = q.shape[0]
         ids = np.empty((nq, k), np.uint32)
         dists = np.empty((nq, k), np.float32)
@@ -348,7 +359,7 @@ class HNSWExactRoute:
             q = q.reshape(1, q.shape[0])
         _check_2d(q, self.gpu.dim)
         nq = q.shape[0]
-        k = int(k)
+        k = _as_k(k)
         handled = ctypes.c_int(0)
         ids = np.empty((nq, k), np.uint32)
         dists = np.empty((nq, k), np.float32)

@@ -134,3 +134,29 @@ def test_k_converts_like_size_t():
     for bad in (-1, 10.0, "10", None):
         with pytest.raises(TypeError):
             vsg._as_k(bad)
+
+
+def test_exact_route_leaves_large_k_to_the_graph():
+    # The GPU index answers k <= 128 (gpu_brute_force.h:27); HNSWIndex.search has no such limit,
+    # so with a filter and k > 128 the route hands the call to the wrapped graph unchanged.
+    import vecsearch_gb300 as vsg
+
+    class Gpu:  # never reached for k > 128
+        dim = 4
+        _h = None
+
+        def __len__(self):
+            return 300
+
+    class Graph:
+        def search(self, queries, **kw):
+            self.kw = kw
+            return "graph"
+
+    g = Graph()
+    mask = np.ones(300, bool)
+    q = np.zeros((2, 4), np.float32)
+    assert vsg.HNSWExactRoute(Gpu(), graph=g).search(q, k=200, filter=mask, exact_below=300) == "graph"
+    assert g.kw["k"] == 200 and g.kw["exact_below"] == 300 and g.kw["filter"] is mask
+    with pytest.raises(ValueError):
+        vsg.HNSWExactRoute(Gpu()).search(q, k=200, filter=mask, exact_below=300)

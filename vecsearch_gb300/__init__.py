@@ -347,6 +347,9 @@ class HNSWExactRoute:
     that allows no row the result is all -1 / +inf; with 0 < allowed <= exact_below it is the
     exact filtered scan (search_exact, hnsw.cpp:336-354) computed on the GPU; otherwise the
     wrapped graph search answers. ``graph`` may be None when only the exact route is used.
+    The GPU index returns at most 128 neighbours (GpuBruteForceIndex.kMaxK); a larger k is left
+    to the wrapped HNSWIndex.search, which then runs its own exact scan (or, without a graph,
+    is a ValueError).
     """
 
     def __init__(self, gpu_index, graph=None):
@@ -363,7 +366,9 @@ class HNSWExactRoute:
         handled = ctypes.c_int(0)
         ids = np.empty((nq, k), np.uint32)
         dists = np.empty((nq, k), np.float32)
-        if filter is not None:
+        if filter is not None and k > _native.MAX_K and self.graph is None:
+            raise ValueError(f"k must be at most {_native.MAX_K} on the GPU route without a graph")
+        if filter is not None and k <= _native.MAX_K:
             mask = _as_mask_u8(filter)
             if mask.ndim != 1 or mask.shape[0] != len(self.gpu):
                 raise ValueError(f"filter must be a 1-D bool array of length {len(self.gpu)}")

@@ -119,7 +119,8 @@ int vsg_search_filtered(vsg_index* index, const float* queries, size_t nq, size_
  * If the mask allows no row, fills VSG_NONE / +inf and sets *handled = 1 (hnsw.cpp:326).
  * If 0 < allowed rows <= exact_below, runs the exact filtered scan on the GPU (in place of
  * search_exact, hnsw.cpp:336-354) and sets *handled = 1. Otherwise sets *handled = 0 and
- * writes nothing: the caller runs its graph search (hnsw.cpp:329-333). */
+ * writes nothing: the caller runs its graph search (hnsw.cpp:329-333). k > VSG_MAX_K ->
+ * VSG_ERR_INVALID: HNSWIndex has no such limit, so a caller keeps search_exact for larger k. */
 int vsg_hnsw_exact_below(vsg_index* index, const float* queries, size_t nq, size_t k,
                          const uint8_t* allowed, size_t allowed_len, size_t exact_below,
                          uint32_t* out_ids, float* out_dists, int* handled);

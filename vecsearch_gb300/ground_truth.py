@@ -24,8 +24,10 @@ __all__ = ["ground_truth"]
 def ground_truth(xb, xq, k=100, metric="ip", batch=4096, method="auto", device=0, return_distances=False):
     """Exact top-k ids (int64 [nq, k], -1 where the base has fewer than k rows) of every query.
 
-    method "auto" (exact FP32) by default; "bf16" takes the tensor-core shortlist + FP32 rerank
-    (k <= 120), whose ids equal the exact ones whenever each query's shortlist holds its top k.
+    method "auto" by default: exact, through the FP32 kernels or (large indexes, k <= 32) the
+    certified tensor-core path, whose results equal the FP32 scan's bit for bit; "tc_exact" forces
+    the latter. "bf16" takes the tensor-core shortlist + FP32 rerank without the certificate
+    (k <= 120): its ids equal the exact ones whenever each query's shortlist holds its top k.
     """
     from . import GpuBruteForceIndex
     xb = np.ascontiguousarray(xb, dtype=np.float32)
@@ -63,7 +65,7 @@ def main(argv=None):
     ap.add_argument("--k", type=int, default=100)
     ap.add_argument("--metric", default="ip", choices=["ip", "cosine", "l2"])
     ap.add_argument("--batch", type=int, default=4096)
-    ap.add_argument("--method", default="auto", choices=["auto", "tiled", "skinny", "bf16"])
+    ap.add_argument("--method", default="auto", choices=["auto", "tiled", "skinny", "tc_exact", "bf16"])
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     xb = np.load(os.path.join(a.data, "base.npy"))

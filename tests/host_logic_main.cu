@@ -5,6 +5,7 @@
 //   route n dp nq k method masked gather allowed -> "tc_exact tiled" (1 / 0 each)
 //   load PATH | save PATH                        -> the status of vsg_autotune_load / _save
 //   table method                                 -> "count" then "batch choice split extra" lines
+//   splits n blocks align min_rows factor slots  -> "rows_per_split nsplit" of choose_splits
 //   reset                                        -> a fresh index (empty tuning tables)
 //   set NAME value | get NAME                    -> vsg_set_tunable's status | "status value"
 //   below n nq k exact_below pattern             -> "status handled id dist" after
@@ -122,6 +123,14 @@ int main() {
       const int rc = vsg_search_filtered(idx.get(), q.data(), nq, k, mask_ld ? words.data() : nullptr, int(per_query),
                                          mask_ld, ids.data(), d.data(), uint32_t(method));
       std::printf("%d %u %g\n", rc, ids[0], double(d[0]));
+    } else if (std::strcmp(cmd, "splits") == 0) {
+      unsigned long long blocks, align, min_rows, slots;
+      double factor;
+      if (std::scanf("%llu %llu %llu %llu %lf %llu", &n, &blocks, &align, &min_rows, &factor, &slots) != 6) return 1;
+      idx->n = n;
+      uint32_t rps = 0, nsplit = 0;
+      idx->choose_splits(blocks, align, min_rows, &rps, &nsplit, factor, slots);
+      std::printf("%u %u\n", rps, nsplit);
     } else if (std::strcmp(cmd, "reset") == 0) {
       idx = fresh();
     } else {

@@ -248,3 +248,27 @@ def test_add_and_search_argument_rules(harness):
     assert out[7] == "0 7 7" and out[8] == "0 7 7"
     assert out[9].split()[0] == "1"
     assert out[10] == "0 4294967295 inf"
+
+
+def test_choose_splits_fills_whole_waves(harness):
+    # The tiled and shortlist kernels' row splits: aligned to whole tiles, covering every row, and
+    # never more than four times the wanted count (at least 1024 rows a split).
+    cases = [(n, b, align, 1024, f, slots)
+             for n in (5_000, 262_144, 1_000_000, 2**32 - 2)
+             for b in (1, 3, 16, 32, 151, 400)
+             for align in (128, 256)
+             for f in (1.0, 2.0)
+             for slots in (152, 304)]
+    out = harness.raw(["splits %d %d %d %d %r %d" % c for c in cases])
+    assert len(out) == len(cases)
+    got = {}
+    for (n, b, align, min_rows, f, slots), line in zip(cases, out):
+        rps, ns = map(int, line.split())
+        assert rps % align == 0 and 0 < rps < 2**32 and ns == -(-n // rps), (n, b, rps, ns)
+        s0 = max(1, int(max(1, slots // b) * f))
+        assert 1 <= ns <= max(1, min(-(-n // min_rows), 4 * s0))
+        got[(n, b, align, f, slots)] = ns
+    # One query block over 1M rows wants 152 splits; rounded to 256-row tiles they become 151
+    # splits of 26 tiles (the ideal share is 25.7 tiles), so one of 152 SMs has no split.
+    assert got[(1_000_000, 1, 256, 1.0, 152)] == 151
+    assert got[(1_000_000, 16, 256, 1.0, 152)] * 16 % 152 == 0  # 16 blocks x 19 splits: 2 waves

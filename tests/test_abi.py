@@ -160,3 +160,15 @@ def test_exact_route_leaves_large_k_to_the_graph():
     assert g.kw["k"] == 200 and g.kw["exact_below"] == 300 and g.kw["filter"] is mask
     with pytest.raises(ValueError):
         vsg.HNSWExactRoute(Gpu()).search(q, k=200, filter=mask, exact_below=300)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    # No CPU fallback: without the built library every entry point raises.
+    import vecsearch_gb300 as vsg
+    from vecsearch_gb300 import _native
+    monkeypatch.setattr(_native, "_lib", None)
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "libvsg_gb300.so"))
+    with pytest.raises(ImportError):
+        _native.lib()
+    with pytest.raises(ImportError):
+        vsg.GpuBruteForceIndex(8)

@@ -163,7 +163,7 @@ def test_exact_route_leaves_large_k_to_the_graph():
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
-    # No CPU fallback: without the built library every entry point raises.
+    # No CPU fallback: without the built library every compute entry point raises.
     import vecsearch_gb300 as vsg
     from vecsearch_gb300 import _native
     monkeypatch.setattr(_native, "_lib", None)
@@ -172,3 +172,4 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         _native.lib()
     with pytest.raises(ImportError):
         vsg.GpuBruteForceIndex(8)
+    assert vsg.cuda_available() is False  # the probe answers as a build without CUDA does

@@ -27,8 +27,14 @@ DeviceTimeoutError = _native.DeviceTimeoutError
 
 
 def cuda_available() -> bool:
-    """True if the CUDA runtime sees a GPU (cuda_available(), gpu_brute_force.cu:334-341)."""
-    return bool(_native.lib().vsg_cuda_available())
+    """True if the library is built and the CUDA runtime sees a GPU (cuda_available(),
+    gpu_brute_force.cu:334-341; False without the build, as bindings.cpp:191-197 returns in a
+    build without CUDA). The index itself raises ImportError without the library."""
+    try:
+        l = _native.lib()
+    except ImportError:
+        return False
+    return bool(l.vsg_cuda_available())
 
 
 def normalize(x: np.ndarray) -> np.ndarray:

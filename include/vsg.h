@@ -194,18 +194,18 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
  *     a table loaded from a file may name a narrower first pass), used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
- *     (0, 4096 or 16384; 0 = no sample pass) and how many CTAs share each row tile through a
- *     multicast cluster (1, 2 or 4; cluster = 0 in a table means the built-in rule).
+ *     (0, 4096 or 16384; 0 = no sample pass).
  * vsg_autotune_table copies a table out (count: capacity in, entries out; choice = kernel or
- * sampled rows; cluster: CTAs per cluster of bf16 entries, first-pass shortlist of certified
- * entries). vsg_autotune_save / _load persist both tables as a small text file. */
+ * sampled rows; exact_kp: first-pass shortlist of certified entries, 0 for bf16 entries).
+ * vsg_autotune_save / _load persist both tables as a small text file ("vsg-tuning 2"; files of
+ * version 1 load too, their bf16 lines' third column ignored). */
 int vsg_autotune(vsg_index* index, const size_t* batches, size_t count, size_t k, uint32_t method);
 /* The same timed on a sample of the caller's queries (nq host rows, stride dim; repeated to fill
  * the largest batch): the certified path's choices depend on how queries sit among the rows. */
 int vsg_autotune_with_queries(vsg_index* index, const float* queries, size_t nq, const size_t* batches,
                               size_t count, size_t k, uint32_t method);
 int vsg_autotune_table(vsg_index* index, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
-                       double* split, uint32_t* cluster);
+                       double* split, uint32_t* exact_kp);
 int vsg_autotune_save(vsg_index* index, const char* path);
 int vsg_autotune_load(vsg_index* index, const char* path);
 

@@ -43,7 +43,7 @@ def test_autotune_table_and_results(gpu_ready, tmp_path):
     assert other.tuning() == []
     other.load_tuning(path)
     assert other.tuning() == table
-    assert path.read_text().startswith("vsg-tuning 1 dim 96")
+    assert path.read_text().startswith("vsg-tuning 2 dim 96")
 
 
 def test_autotune_bf16(gpu_ready):
@@ -52,7 +52,7 @@ def test_autotune_bf16(gpu_ready):
     idx, x = _index(vsg, n=80_000, d=128, metric="cosine", seed=91)
     table = idx.autotune((8, 64, 256), k=10, method="bf16")
     assert [e["batch"] for e in table] == [8, 64, 256]
-    assert all(e["sample"] in (0, 4096, 16384) and e["cluster"] in (1, 2, 4) for e in table)
+    assert all(set(e) == {"batch", "sample"} and e["sample"] in (0, 4096, 16384) for e in table)
     q = D.portable(256, 128, 92, normalize=True)
     bi, bd = idx.search(q, 10, method="bf16")
     gi, _ = O.fp64_topk(x, q, 10, "cosine")

@@ -151,7 +151,8 @@ junk line
 """
 PLAIN_TABLE = [("1", "2", "1.000", "120"), ("48", "1", "2.000", "0"), ("128", "2", "1.000", "0"),
          ("1024", "0", "1.500", "0")]  # kernel 3, split 0 dropped; a first pass above 128 reads as none
-BF16_TABLE = [("8", "16384", "1.000", "2"), ("128", "0", "1.000", "0")]  # cluster 3, sample > 2^20 dropped
+# A third bf16 column (CTAs per cluster, version-1 files) is ignored; a sample above 2^20 is dropped.
+BF16_TABLE = [("8", "16384", "1.000", "0"), ("64", "4096", "1.000", "0"), ("128", "0", "1.000", "0")]
 
 
 def _tables(lines):
@@ -174,7 +175,7 @@ def test_tuning_file_round_trip(harness, tmp_path):
     rest = out[1 + 1 + len(PLAIN_TABLE) + 1 + len(BF16_TABLE):]
     assert rest[0] == "0" and rest[1] == "0" and rest[2] == "0"  # saved; a fresh index is untuned; reloaded
     assert _tables(rest[3:]) == [PLAIN_TABLE, BF16_TABLE]
-    assert dst.read_text().startswith("vsg-tuning 1 dim 0 rows 0 metric 0 sms 152")
+    assert dst.read_text().startswith("vsg-tuning 2 dim 0 rows 0 metric 0 sms 152")
 
 
 def test_tuning_file_rejects(harness, tmp_path):

@@ -233,21 +233,20 @@ class GpuBruteForceIndex:
 
     def tuning(self, method="auto"):
         """The tuned table. Exact methods: [{"batch", "kernel", "split"} (+ "shortlist": first-pass k'
-        of the certified path)]; bf16: [{"batch", "sample" (rows sampled, 0 = none), "cluster"
-        (CTAs sharing each row tile, 0 = built-in rule)}]."""
+        of the certified path)]; bf16: [{"batch", "sample" (rows sampled, 0 = none)}]."""
         cnt = ctypes.c_size_t(64)
         bt = (ctypes.c_uint32 * 64)()
         ch = (ctypes.c_uint32 * 64)()
         sp = (ctypes.c_double * 64)()
-        cl = (ctypes.c_uint32 * 64)()
+        kp = (ctypes.c_uint32 * 64)()
         _native.check(_native.lib().vsg_autotune_table(self._h, _native.METHODS[method], ctypes.byref(cnt), bt, ch,
-                                                       sp, cl))
+                                                       sp, kp))
         n = min(cnt.value, 64)
         if method == "bf16":
-            return [{"batch": bt[i], "sample": int(ch[i]), "cluster": int(cl[i])} for i in range(n)]
+            return [{"batch": bt[i], "sample": int(ch[i])} for i in range(n)]
         names = {0: "skinny", 1: "tiled", 2: "tc_exact"}
         return [dict({"batch": bt[i], "kernel": names[ch[i]], "split": sp[i]},
-                     **({"shortlist": int(cl[i])} if ch[i] == 2 else {})) for i in range(n)]
+                     **({"shortlist": int(kp[i])} if ch[i] == 2 else {})) for i in range(n)]
 
     def save_tuning(self, path):
         _native.check(_native.lib().vsg_autotune_save(self._h, str(path).encode()))

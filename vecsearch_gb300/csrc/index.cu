@@ -318,7 +318,7 @@ int vsg_autotune(vsg_index* h, const size_t* batches, size_t count, size_t k, ui
 }
 
 int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* batch, uint32_t* choice,
-                       double* split, uint32_t* cluster) {
+                       double* split, uint32_t* exact_kp) {
   if (!h || !count) return fail(VSG_ERR_INVALID, "index or count is NULL");
   return guarded([&] {
     std::lock_guard<std::mutex> g(h->mu);
@@ -329,7 +329,7 @@ int vsg_autotune_table(vsg_index* h, uint32_t method, size_t* count, uint32_t* b
       if (batch) batch[i] = t[i].batch;
       if (choice) choice[i] = method == VSG_METHOD_BF16 ? t[i].sample : t[i].kernel;
       if (split) split[i] = t[i].split;
-      if (cluster) cluster[i] = method == VSG_METHOD_BF16 ? t[i].cluster : t[i].exact_kp;
+      if (exact_kp) exact_kp[i] = method == VSG_METHOD_BF16 ? 0u : t[i].exact_kp;
     }
   });
 }
@@ -340,10 +340,10 @@ int vsg_autotune_save(vsg_index* h, const char* path) {
     std::lock_guard<std::mutex> g(h->mu);
     FILE* f = std::fopen(path, "w");
     if (!f) throw std::runtime_error(std::string("cannot open ") + path);
-    std::fprintf(f, "vsg-tuning 1 dim %zu rows %zu metric %u sms %d\n", h->dim, h->n, h->metric, h->sms);
+    std::fprintf(f, "vsg-tuning 2 dim %zu rows %zu metric %u sms %d\n", h->dim, h->n, h->metric, h->sms);
     for (const auto& e : h->tune_plain)
       std::fprintf(f, "plain %u %u %.3f %u\n", e.batch, e.kernel, e.split, e.exact_kp);
-    for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u %u\n", e.batch, e.sample, e.cluster);
+    for (const auto& e : h->tune_bf16) std::fprintf(f, "bf16 %u %u\n", e.batch, e.sample);
     const bool ok = std::fclose(f) == 0;
     if (!ok) throw std::runtime_error(std::string("write failed: ") + path);
   });
@@ -361,7 +361,8 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
       vsg_index::TuneEntry e;
       unsigned b = 0, c = 0;
       double sp = 1.0;
-      if (std::strncmp(line, "vsg-tuning 1", 12) == 0) {
+      // Version 1 files carried a third bf16 column (CTAs per cluster); it is read and ignored.
+      if (std::strncmp(line, "vsg-tuning 1", 12) == 0 || std::strncmp(line, "vsg-tuning 2", 12) == 0) {
         header = true;
       } else if (std::sscanf(line, "plain %u %u %lf", &b, &c, &sp) == 3 && c <= 2 && sp > 0) {
         unsigned kp = 0;
@@ -372,12 +373,9 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
         e.exact_kp = kp <= 128 ? kp : 0;
         plain.push_back(e);
       } else if (std::strncmp(line, "bf16 ", 5) == 0) {
-        unsigned cl = 0;
-        const int got = std::sscanf(line, "bf16 %u %u %u", &b, &c, &cl);
-        if (got >= 2 && c <= (1u << 20) && (cl == 0 || cl == 1 || cl == 2 || cl == 4)) {
+        if (std::sscanf(line, "bf16 %u %u", &b, &c) == 2 && c <= (1u << 20)) {
           e.batch = b;
           e.sample = c;
-          e.cluster = cl;
           bf16.push_back(e);
         }
       }

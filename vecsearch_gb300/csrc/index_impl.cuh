@@ -145,13 +145,6 @@ struct vsg_index {
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
   size_t xmap_rows = 0;
-  // Row maps with 64- and 32-row boxes (clusters of 2 and 4 multicast slices of a row chunk).
-  CUtensorMap xmap_slice[4]{};  // [bf16 / e4m3][cluster 2 / 4]
-  const void* xmap_slice_base[4] = {nullptr, nullptr, nullptr, nullptr};
-  size_t xmap_slice_rows[4] = {0, 0, 0, 0};
-  // Clusters of 2 / 4 shortlist CTAs resident at once, by (stages, dp) (0: not known yet).
-  uint32_t max_clusters[2] = {0, 0};
-  uint32_t max_clusters_key = 0;
   PinnedBuffer pin_in, pin_out;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
@@ -185,13 +178,12 @@ struct vsg_index {
   // bf16: rows the sampled-threshold pass scores (0: none).
   struct TuneEntry {
     uint32_t batch = 0, kernel = 0, sample = 16384;
-    uint32_t cluster = 0;  // bf16: CTAs per cluster (0: the default rule)
     uint32_t exact_kp = 0;  // exact methods, kernel 2: first-pass shortlist of the certified path (0: default)
     double split = 1.0;
   };
   std::vector<TuneEntry> tune_plain, tune_bf16;
   // Overrides used while the tuner times a candidate (-1 / 0 = not forced).
-  int force_kernel = -1, force_sample = -1, force_cluster = -1, force_exact_kp = -1;
+  int force_kernel = -1, force_sample = -1, force_exact_kp = -1;
   double force_split = 0.0;
 
   static const TuneEntry* lookup(const std::vector<TuneEntry>& t, size_t nq) {
@@ -397,32 +389,6 @@ struct vsg_index {
     }
   }
 
-  const CUtensorMap& slice_map(uint32_t cluster, bool f8) {
-    const int i = (cluster == 2 ? 0 : 1) + (f8 ? 2 : 0);
-    const void* base = f8 ? x8.get() : xb.get();
-    if (xmap_slice_base[i] != base || xmap_slice_rows[i] != n) {
-      VSG_CUDA(vsg::tc_encode_tiled_map(&xmap_slice[i], base, n, uint32_t(f8 ? dp8() : dp),
-                                        uint32_t(vsg::kTcRows) / cluster, f8));
-      xmap_slice_base[i] = base;
-      xmap_slice_rows[i] = n;
-    }
-    return xmap_slice[i];
-  }
-
-  // CTAs per cluster for a batch of nqb query blocks: the largest of 4 / 2 / 1 that the batch
-  // fills, unless tuned (0 in the table = this rule), and only if such clusters can be resident.
-  uint32_t pick_cluster(size_t nqb, uint32_t tuned, uint32_t stages, uint32_t resident, uint32_t nkc, bool f8) {
-    uint32_t c = tuned ? tuned : nqb >= 4 ? 4u : nqb >= 2 ? 2u : 1u;
-    const uint32_t key = stages * 65536u + nkc * 4u + resident * 2u + (f8 ? 1u : 0u);
-    if (max_clusters_key != key) {
-      max_clusters[0] = vsg::tc_max_clusters(2, stages, nkc, resident, metric == VSG_METRIC_L2, f8);
-      max_clusters[1] = vsg::tc_max_clusters(4, stages, nkc, resident, metric == VSG_METRIC_L2, f8);
-      max_clusters_key = key;
-    }
-    while (c > 1 && max_clusters[c == 2 ? 0 : 1] == 0) c /= 2;
-    return c;
-  }
-
   // Certified exact path: the list keeps the rows within each query's margin of its k-th best,
   // up to k' entries. The widest k' (120) certifies the most queries and costs about the same as
   // a narrower one (the candidate buffers are the same size), so it is always the first pass;
@@ -487,19 +453,15 @@ struct vsg_index {
     }
     const size_t nqb = ceil_div(nq, size_t(vsg::kTcQueries));
     const TuneEntry* te = lookup(tune_bf16, nq);
-    // Clusters of C CTAs share each row tile (multicast); items are (group of C query blocks,
-    // split), taken round-robin by the clusters that fit on the GPU at once.
-    const uint32_t C = pick_cluster(nqb, force_cluster >= 0 ? uint32_t(force_cluster) : te ? te->cluster : 0u,
-                                    stages, resident, nkc, f8);
-    const size_t nqg = ceil_div(nqb, size_t(C));
-    const size_t slots = C > 1 ? size_t(max_clusters[C == 2 ? 0 : 1]) : size_t(sms);
+    // Items are (query block, split), taken round-robin by one CTA per SM.
+    const size_t slots = size_t(sms);
     vsg::TcArgs a{};
-    choose_splits(nqg, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
+    choose_splits(nqb, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
     const size_t parts = nq * a.nsplit * kp;
     part.reserve(parts * 8 + nq * a.nsplit * 4, 0, stream);  // lists, then their lengths
     // One candidate buffer per CTA.
-    const unsigned grid = unsigned(std::min<size_t>(nqg * a.nsplit, slots) * C);
-    const CUtensorMap& rowmap = C > 1 ? slice_map(C, f8) : f8 ? xmap8 : xmap;
+    const unsigned grid = unsigned(std::min<size_t>(nqb * a.nsplit, slots));
+    const CUtensorMap& rowmap = f8 ? xmap8 : xmap;
     const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
     if (f8) {  // (the bf16 queries' launch resets them)
@@ -522,7 +484,6 @@ struct vsg_index {
     a.mask_ld = uint32_t(mask_ld);
     a.xscale = f8 ? static_cast<const float*>(x8scale.get()) : nullptr;
     a.qscale = f8 ? static_cast<const float*>(q8scale.get()) : nullptr;
-    a.cluster = C;
     a.kp = kp;
     a.stages = stages;
     a.resident = resident;
@@ -559,7 +520,7 @@ struct vsg_index {
         sa.rows_per_split = uint32_t(rps);
         sa.nsplit = uint32_t(ceil_div(size_t(n), rps));
         st = 1;
-        sgrid = unsigned(std::min<size_t>(nqg * sa.nsplit, slots) * C);
+        sgrid = unsigned(std::min<size_t>(nqb * sa.nsplit, slots));
       }
       const size_t per_query = size_t(sa.nsplit) * st * vsg::kTcRows;
       sample.reserve(nq * per_query * sizeof(float), 0, stream);
@@ -764,17 +725,12 @@ struct vsg_index {
         pick.batch = uint32_t(b);
         float best = 1e30f;
         if (family == VSG_METHOD_BF16) {
-          for (int cl : {1, 2, 4}) {
-            if (cl > 1 && ceil_div(b, size_t(vsg::kTcQueries)) < size_t(cl)) continue;
-            for (int smp : {0, 4096, 16384}) {
-              force_sample = smp;
-              force_cluster = cl;
-              const float t = time_it(b, VSG_METHOD_BF16);
-              if (t < best) {
-                best = t;
-                pick.sample = uint32_t(smp);
-                pick.cluster = uint32_t(cl);
-              }
+          for (int smp : {0, 4096, 16384}) {
+            force_sample = smp;
+            const float t = time_it(b, VSG_METHOD_BF16);
+            if (t < best) {
+              best = t;
+              pick.sample = uint32_t(smp);
             }
           }
         } else {
@@ -804,7 +760,6 @@ struct vsg_index {
     } catch (...) {
       force_kernel = -1;
       force_sample = -1;
-      force_cluster = -1;
       force_exact_kp = -1;
       force_split = 0;
       cudaEventDestroy(e0);
@@ -813,7 +768,6 @@ struct vsg_index {
     }
     force_kernel = -1;
     force_sample = -1;
-    force_cluster = -1;
     force_exact_kp = -1;
     force_split = 0;
     cudaEventDestroy(e0);

@@ -227,22 +227,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// The same copy multicast to the CTAs of `mask` in the cluster: the box lands at the same
-// shared-memory offset in each, and each one's barrier at `bar`'s offset counts its bytes.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
-                                               uint16_t mask, uint64_t policy) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      ".L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5, %6;" ::"r"(smem_addr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar)), "h"(mask), "l"(policy)
-      : "memory");
-}
-
-// Every thread of every CTA of the cluster: arrives and waits (release / acquire).
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 __device__ __forceinline__ uint64_t policy_evict_last() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -276,14 +260,6 @@ __device__ __forceinline__ void tc_mma_f8(uint32_t d_tmem, uint64_t adesc, uint6
 
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
-               : "memory");
-}
-
-// The same arrival on the barrier at `bar`'s offset in every CTA of `mask`.
-__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                   smem_addr(bar)),
-               "h"(mask)
                : "memory");
 }
 
@@ -379,14 +355,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t nqb = persistent ? a.hdr->nqb : a.nqb;
   const uint32_t nsplit = persistent ? a.hdr->nsplit : a.nsplit;
   const uint32_t rows_per_split = persistent ? a.hdr->rows_per_split : a.rows_per_split;
-  const uint32_t nitems = persistent ? a.hdr->items : ((nqb + max(1u, a.cluster) - 1) / max(1u, a.cluster)) * nsplit;
+  const uint32_t nitems = persistent ? a.hdr->items : nqb * nsplit;
   constexpr uint32_t cap = 32u * E;
-  // Cluster of C CTAs (non-serving launches): rank r takes query block qg * C + r of a group.
-  const uint32_t C = persistent ? 1u : max(1u, a.cluster);
-  const uint32_t rank = blockIdx.x % C, cid = blockIdx.x / C, nclusters = gridDim.x / C;
-  const uint16_t cmask = uint16_t((1u << C) - 1u);
-  const uint32_t slice_rows = kTcRows / C;  // rows of each row chunk this CTA loads for all
-  const uint32_t nqg = (nqb + C - 1) / C;
   __shared__ uint32_t item_slot;
   __shared__ __align__(16) float xs_buf[4][L2 ? kTcRows : 1];  // epilogue warps' row norms of a tile (L2)
   __shared__ __align__(16) float xsc_buf[4][F8 ? kTcRows : 1];  // ... and row scales (e4m3 copies)
@@ -394,7 +364,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], C);  // one arrival from every CTA's MMAs (the slot is shared)
+      mbar_init(&empty[s], 1);  // the MMAs that read the slot have completed
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
@@ -416,7 +386,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  if (C > 1) cluster_sync();  // every CTA's barriers exist before any copy or arrival reaches them
 
   // Ring, accumulator and query-block positions carry over from one item to the next; every
   // role walks the same items and tiles in the same order, so they stay in step.
@@ -431,12 +400,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint64_t keep_policy = policy_evict_last();
 
   for (uint32_t iter = 0;; ++iter) {
-    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : cid + iter * nclusters;
+    if (tid == 0) item_slot = persistent ? atomicAdd(&a.hdr->next, 1u) : blockIdx.x + iter * gridDim.x;
     __syncthreads();
     const uint32_t item = item_slot;
     __syncthreads();  // everyone has read the slot before thread 0 may overwrite it
     if (item >= nitems) break;
-    const uint32_t qb = (item % nqg) * C + rank, split = item / nqg;
+    const uint32_t qb = item % nqb, split = item / nqb;
     const uint32_t qbase = qb * kTcQueries;
     const uint32_t row_begin = split * rows_per_split;
     // No 32-bit wrap: with its FP32 rows and a bf16 or e4m3 copy (160+ bytes a row) an index
@@ -477,11 +446,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             unsigned char* sb = resident ? st : st + kChunkBytes;
             mbar_arrive_expect_tx(&full[s], resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes);
             if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
-            if (C > 1)  // this CTA's slice of the row chunk, for every CTA of the cluster
-              tma_load_2d_mc(sb + size_t(rank) * slice_rows * 128, &xmap, 0, y + int(rank * slice_rows), &full[s],
-                             cmask, stream_policy);
-            else
-              tma_load_2d(sb, &xmap, 0, y, &full[s], stream_policy);
+            tma_load_2d(sb, &xmap, 0, y, &full[s], stream_policy);
             pending |= 1u << s;
             last_ph = (last_ph & ~(1u << s)) | (ph << s);
             if (++s == stages) {
@@ -522,11 +487,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               else
                 tc_mma(d, sw128_desc(sa + kk * 32), sw128_desc(sb + kk * 32), (kc | kk) != 0 ? 1u : 0u);
             }
-            // The slot is free once these MMAs have read it (in every CTA it was multicast to).
-            if (C > 1)
-              tc_commit_mc(&empty[s], cmask);
-            else
-              tc_commit(&empty[s]);
+            tc_commit(&empty[s]);  // the slot is free once these MMAs have read it
             if (++s == stages) {
               s = 0;
               ph ^= 1;
@@ -747,8 +708,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   tc_fence_before();
   __syncthreads();
-  // No CTA leaves while another may still multicast rows or arrivals into its shared memory.
-  if (C > 1) cluster_sync();
   if (warp == 1) {
     tc_fence_after();
     __syncwarp();
@@ -1350,8 +1309,7 @@ uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident, bool l2
   // The kernel's static shared memory comes on top: the work slot, and 1 KB of row norms (L2)
   // and of row scales (e4m3 copies) per epilogue warp.
   // The deepest ring that fits is taken, so a CTA always uses more than half of an SM's shared
-  // memory: one CTA per SM, which owns all 512 TMEM columns (two CTAs, one waiting for the
-  // other's columns, could otherwise stall clusters that span both SMs).
+  // memory: one CTA per SM, which owns all 512 TMEM columns (a second CTA would wait for them).
   const size_t kStatic = 576 + (l2 ? 4 * kTcRows * 4 : 0) + (fp8 ? 4 * kTcRows * 4 : 0);
   const size_t half = budget / 2 + 1;
   budget = budget > kStatic ? budget - kStatic : 0;
@@ -1421,51 +1379,13 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
     if (a.stages < 3) return cudaErrorInvalidValue;
   }
   if (grid == 0) return cudaSuccess;
-  const uint32_t C = a.hdr ? 1u : std::max(1u, a.cluster);
-  if ((C != 1 && C != 2 && C != 4) || grid % C != 0) return cudaErrorInvalidValue;
   cudaError_t e = tc_prepare(a.stages, nkc, a.resident, a.l2 != 0, a.fp8 != 0);
   if (e != cudaSuccess) return e;
   const size_t smem = tc_smem_bytes(a.stages, nkc, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
   const TcKernel fn = kTcKernels[a.fp8 ? 1 : 0][a.l2 ? 1 : 0][cap == 64 ? 0 : cap == 128 ? 1 : 2];
-  if (C > 1) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kTcThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, fn, qmap, xmap, a);
-  }
   fn<<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
   return cudaGetLastError();
-}
-
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8) {
-  if (tc_prepare(stages, nkc, resident, l2, fp8) != cudaSuccess) return 0;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cluster * 64);
-  cfg.blockDim = dim3(kTcThreads);
-  cfg.dynamicSmemBytes = tc_smem_bytes(stages, nkc, resident);
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, kTcKernels[fp8 ? 1 : 0][l2 ? 1 : 0][1], &cfg) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  return uint32_t(n);
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,

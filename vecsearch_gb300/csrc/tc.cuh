@@ -79,11 +79,6 @@ struct TcArgs {
   // (mask_ld = 0) or one per query, mask_ld words apart; nullptr = no filter.
   const uint32_t* mask;
   uint32_t mask_ld;
-  // Non-serving launches: CTAs per thread-block cluster (1, 2 or 4). The C CTAs of a cluster take
-  // C consecutive query blocks of one split; each loads 128 / C rows of every row chunk and
-  // multicasts them to all C, so the cluster reads each row tile from L2 once. Needs the row map
-  // encoded with a 64 x (128 / C) box (xmap argument of the launch) and grid % C == 0.
-  uint32_t cluster;
 };
 
 // Serving mode, after the persistent shortlist kernel: per query (one CTA each, CTAs past
@@ -147,12 +142,9 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
 // the shortlist kernel loads is then one contiguous 32 KB span. Bytes for `rows` rows:
 size_t tc_tiled_bytes(size_t rows, uint32_t dp, bool fp8);
 // Tensor map over such a copy of `rows` rows: a (64 bf16 | 128 e4m3) x (tiles * nkc * kTcRows)
-// matrix of 128-byte chunk rows, box_rows per box (kTcRows, or kTcRows / cluster for a multicast
-// slice), 128-byte swizzle.
+// matrix of 128-byte chunk rows, box_rows per box (kTcRows), 128-byte swizzle.
 cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t rows, uint32_t dp, uint32_t box_rows,
                                 bool fp8);
-// Clusters of `cluster` CTAs of the shortlist kernel that can be resident at once (0 on error).
-uint32_t tc_max_clusters(uint32_t cluster, uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
 
 // Sets the shared-memory limit of the shortlist kernels of one variant (metric, operand type) for
 // (stages, nkc, resident); launch_tc_shortlist does it too, but a launch being captured into a

@@ -47,16 +47,22 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# DRAM bytes per scan launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum),
-# keyed by (n, dim, batch, k, metric); the summaries are committed under profiles/.
-# The 1M-row entry is the 262,144-row capture (profiles/scan_kernel_1Mx384_b1.md: 402.69 MB read +
-# 3.31 MB written per launch) scaled by rows scanned (x 1,000,000 / 262,144); reads equal the
-# algorithmic bytes there, so traffic grows in proportion to the rows.
-MEASURED_TRAFFIC = {(1_000_000, 384, 1, 10, "ip"): 1_548_800_000,
-                    # the certified path's shortlist main pass at batch 1: the 262,144-row capture
-                    # (profiles/tc_shortlist_kernel_262Kx384_b1_dram.md: 201.40 MB read + 3.15 MB
-                    # written per launch, reads = the bf16 rows once) scaled by rows
-                    ("tc", 1_000_000, 384, 1, 10, "ip"): 780_332_031}
+# DRAM bytes per launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on a 262,144-row case of the same kernel and scaled by rows scanned:
+# reads equal the algorithmic bytes there, so traffic grows in proportion to the rows. Keyed by
+# (kernel, dim, batch, k, metric); None for configurations without a capture.
+#   scan: the FP32 scan kernel, 402.69 MB read + 3.31 MB written per 262,144-row launch
+#   tc:   the certified path's bf16 shortlist main pass, 201.40 MB read + 3.15 MB written
+MEASURED_TRAFFIC_262K = {("scan", 384, 1, 10, "ip"): 406_000_000,
+                         ("tc", 384, 1, 10, "ip"): 204_550_000}
+
+
+def measured_traffic(kernel, n, dim, batch, k, metric):
+    """(bytes per launch scaled to n rows, source) or (None, reason)."""
+    t = MEASURED_TRAFFIC_262K.get((kernel, dim, batch, k, metric))
+    if t is None:
+        return None, "no ncu capture of this configuration"
+    return int(round(t * n / 262_144)), "ncu capture at 262,144 rows, scaled by rows"
 
 
 def parse():
@@ -78,6 +84,9 @@ def parse():
     ap.add_argument("--no-recall", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="sweep with the built-in schedule rules")
     ap.add_argument("--no-filtered", action="store_true", help="skip the filtered (config 3) sweep")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size parity checks")
+    ap.add_argument("--no-serve", action="store_true", help="skip the short serving-latency check")
+    ap.add_argument("--parity-queries", type=int, default=512, help="queries checked per cosine k=10 batch")
     ap.add_argument("--method", default="auto", choices=["auto", "skinny", "tiled", "bf16", "tc_exact"],
                     help="path of the main timed line (auto: the certified path on a large index, "
                          "else the FP32 kernels by batch size)")
@@ -111,13 +120,14 @@ def workload(a):
     }
 
 
-def peaks_bf16():
-    """Measured dense bf16 TFLOP/s (burst) from MEASURED_PEAKS.json, else the 1,900 fallback."""
+def peaks_bf16(key="bf16_tflops"):
+    """Measured dense bf16 TFLOP/s from MEASURED_PEAKS.json (burst, or `key`), else the fallback
+    (1,900 burst, 1,700 sustained)."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["bf16_tflops"])
+            return float(json.load(f)[key])
     except (OSError, KeyError, ValueError):
-        return 1900.0
+        return 1700.0 if "sustained" in key else 1900.0
 
 
 def peaks():
@@ -209,7 +219,8 @@ def run_reference(a):
         "impl": "reference", "metric": f"exact top-{a.k} QPS at {a.n // 1000}Kx{a.dim}", "value": round(v, 2),
         "unit": "queries/s", "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
         "ms_per_step": round(el * 1e3 / steps, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(a),
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload(a), parallelism=f"replicas{a.gpus}"),
         "cpu_baseline": {"value": round(v, 2), "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} searches of batch {a.batch} over the full base ({el:.1f} s)"},
         "e2e": {"value": round(v, 2), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -302,6 +313,135 @@ def filtered_sweep(idx, torch, x, q, a, stream, batch=16, targets=(100, 1000, 10
     return res
 
 
+def hbm_roofline(alg_bytes, kernel_ms, peak, peak_kind, traffic, traffic_source, kernel):
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+            "traffic_source": traffic_source, "algorithmic_bytes_per_launch": alg_bytes, "kernel": kernel,
+            "kernel_ms_avg": round(kernel_ms, 5)}
+
+
+PARITY_RULE = ("distances within rtol 1e-5 + atol 2e-6 of the oracle port's; ids equal the oracle port's and the "
+               "FP64 oracle's except at near-ties (a different row only at the k-th place within 1e-6 relative, "
+               "rows of one list in another order within 1e-5 relative)")
+
+
+def _parity_case(O, x, q, ids, dists, k, metric, cores, truth_i):
+    """The parity rule for one set of results: against the oracle port (the reference's CPU
+    algorithm restated, all host threads) and the FP64 oracle's ids."""
+    wi, wd = O.search(x, q, k, metric, num_threads=cores)
+    row = {"queries": int(len(q)), "vs_oracle": True, "vs_fp64": True, "near_ties_tolerated": 0}
+    try:
+        np.testing.assert_allclose(dists, wd, rtol=1e-5, atol=2e-6)
+        row["near_ties_tolerated"] += O.check_ids(ids, O.ids_to_int64(wi), x, q, metric)
+    except AssertionError as e:
+        row["vs_oracle"] = False
+        row["error"] = str(e)[:200]
+    try:
+        row["near_ties_tolerated"] += O.check_ids(ids, truth_i, x, q, metric)
+    except AssertionError as e:
+        row["vs_fp64"] = False
+        row["error_fp64"] = str(e)[:200]
+    return row
+
+
+def parity_checks(vsg, idx, x, q, a):
+    """Full-size parity of method auto (the drop-in's default) at 1M x 384: cosine k = 10 at
+    batches 1, 128 and 4096 (the first --parity-queries queries of each), cosine k = 100 at batch
+    128, and L2 k = 10 on unnormalised rows of the same mixture at batches 1 and 128. Each result
+    set is checked against the oracle port of the reference's search_batch and the FP64 oracle.
+    Returns (report, FP64 top-10 of the cosine queries, for reuse)."""
+    from oracle import oracle as O
+    from vecsearch_gb300 import datasets as D
+    t0 = time.perf_counter()
+    cores = os.cpu_count() or 1
+    nchk = min(a.parity_queries, len(q))
+    cases = []
+
+    def run_case(index, xx, qq, k, metric, batch, truth_i):
+        # every query of qq is searched in batches of `batch`; the first len(truth_i) are checked
+        s0 = index.tc_exact_stats()
+        parts = [index.search(qq[i:i + batch], k) for i in range(0, len(qq), batch)]
+        ids = np.concatenate([p[0] for p in parts])[:len(truth_i)]
+        dists = np.concatenate([p[1] for p in parts])[:len(truth_i)]
+        s1 = index.tc_exact_stats()
+        row = {"metric": metric, "k": k, "batch": batch, "method": "auto",
+               "path": "tc_exact" if s1[0] > s0[0] else "fp32 kernels",
+               "uncertified_to_scan": int(s1[1] - s0[1])}
+        row.update(_parity_case(O, xx, qq[:len(truth_i)], ids, dists, k, metric, cores, truth_i))
+        cases.append(row)
+
+    truth10 = O.fp64_topk(x, q[:nchk], 10, "ip")
+    run_case(idx, x, q[:nchk], 10, "ip", 1, truth10[0])
+    run_case(idx, x, q[:nchk], 10, "ip", 128, truth10[0])
+    if len(q) >= 4096:
+        run_case(idx, x, q[:4096], 10, "ip", 4096, truth10[0])
+    n100 = min(128, len(q))
+    run_case(idx, x, q[:n100], 100, "ip", 128, O.fp64_topk(x, q[:n100], 100, "ip")[0])
+    # L2 on unnormalised rows of the same mixture (config 2's L2 variant)
+    xl, _ = D.clustered(a.n, a.dim, a.clusters, 0.35, seed=0, centroid_seed=2, unit=False)
+    ql, _ = D.clustered(128, a.dim, a.clusters, 0.35, seed=1, centroid_seed=2, unit=False)
+    il = vsg.GpuBruteForceIndex(a.dim, "l2")
+    il.add(xl)
+    tl = O.fp64_topk(xl, ql, 10, "l2")[0]
+    run_case(il, xl, ql[:32], 10, "l2", 1, tl[:32])
+    run_case(il, xl, ql, 10, "l2", 128, tl)
+    del il, xl
+    return ({"rule": PARITY_RULE, "all_pass": all(c["vs_oracle"] and c["vs_fp64"] for c in cases), "cases": cases,
+             "seconds": round(time.perf_counter() - t0, 1)}, truth10)
+
+
+def precision_checks(vsg, idx, torch, qd, x, q, a, stream, truth):
+    """Config 4 at batch 128 on the bench's base: the approximate precision forms (bf16 copy with
+    k' = 40, e4m3 copy with k' = 80; exact FP32 rerank of the shortlist) - recall@10 and max
+    |distance error| against the FP64 oracle on 128 queries, and device QPS."""
+    from oracle import oracle as O
+    nq = min(128, len(q))
+    gi = truth[0][:nq] if truth is not None else O.fp64_topk(x, q[:nq], 10, "ip")[0]
+    a2 = argparse.Namespace(**vars(a))
+    a2.k = 10
+    out = []
+    for method, over in (("bf16", 4), ("fp8", 8)):
+        idx.set_tunable("shortlist_oversample", over)
+        ids, dists = idx.search(q[:nq], 10, method=method)
+        err = 0.0
+        for i in range(nq):
+            ok = ids[i] >= 0
+            d64 = O.fp64_distances(x, q[i:i + 1], "ip", ids[i][ok])[0]
+            err = max(err, float(np.max(np.abs(dists[i][ok].astype(np.float64) - d64))))
+        ms, _, _, _ = time_device(idx, torch, qd, a2, 128, 20, 3, stream, method=method)
+        out.append({"copy": method, "k": 10, "k_prime": 10 * over, "batch": 128, "queries_checked": nq,
+                    "recall_at_10_vs_fp64": vsg.recall_at_k(ids, gi, 10), "max_abs_dist_err_vs_fp64": err,
+                    "qps": round(128 * 20 / (ms / 1e3), 1)})
+    idx.set_tunable("shortlist_oversample", 4)
+    return out
+
+
+def serve_setup(a, idx, vsg):
+    from vecsearch_gb300 import datasets as D
+    groups = D.zipf_groups(a.n, 2000, 1.1, seed=3)
+    sizes = np.bincount(groups, minlength=2000)
+    cand = [g for g in range(2000) if sizes[g] >= 100][:64]
+    words_by_group = {g: D.pack_bits(groups == g) for g in cand}
+    return groups, words_by_group
+
+
+def serve_check(vsg, idx, q, a, rates=(5000, 20000), duration=1.0):
+    """Config 5's request mix through the continuous-batching server at two offered loads, one
+    second each: achieved QPS and p50 / p99 latency (submit to completion)."""
+    groups, words = serve_setup(a, idx, vsg)
+    srv = vsg.Server(idx, max_batch=1024, max_k=100, slots=2)
+    try:
+        serve_load(idx, srv, None, q, groups, words, 2000, 0.3, 1)  # warm-up
+        rows = [serve_load(idx, srv, None, q, groups, words, r, duration, 10 + i) for i, r in enumerate(rates)]
+        st = srv.stats()
+    finally:
+        srv.close()
+    return {"workload": "open-loop Poisson arrivals; requests of 1-64 queries (log-uniform), k 10 or 100, 30% "
+                        "filtered to one Zipf(1.1) group of 2,000", "server": "2 slots x 1024 queries",
+            "duration_s": duration, "loads": rows, "server_stats": st}
+
+
 def run_ours(a):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -361,23 +501,20 @@ def run_ours(a):
     peak, peak_kind = peaks()
     if info.get("tc_exact"):
         alg_bytes = a.n * a.dim * 2 + a.batch * a.dim * 2  # the bf16 rows once, the bf16 queries
-        traffic = MEASURED_TRAFFIC.get(("tc", a.n, a.dim, a.batch, a.k, a.metric))
+        traffic, tsrc = measured_traffic("tc", a.n, a.dim, a.batch, a.k, a.metric)
         kernel = "tc_shortlist_kernel (bf16 tcgen05 pass over the rows; certified exact path)"
         dtype = "bf16 products, f32 accumulation and results"
     else:
         alg_bytes = a.n * a.dim * 4 + a.batch * a.dim * 4 + a.batch * a.k * 8
-        traffic = MEASURED_TRAFFIC.get((a.n, a.dim, a.batch, a.k, a.metric))
+        traffic, tsrc = measured_traffic("scan", a.n, a.dim, a.batch, a.k, a.metric)
         kernel = "scan_kernel (fused FP32 scan + top-k)"
         dtype = "f32"
-    achieved = alg_bytes / (scan_avg_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                "kernel": kernel, "kernel_ms_avg": round(scan_avg_ms, 5),
-                "after_kernel_ms_avg": round(merge_ms / max(launches, 1), 5)}
+    roofline = hbm_roofline(alg_bytes, scan_avg_ms, peak, peak_kind, traffic, tsrc, kernel)
+    roofline["after_kernel_ms_avg"] = round(merge_ms / max(launches, 1), 5)
 
     extra = {}
     bf16_peak = peaks_bf16()
+    bf16_sustained = peaks_bf16("bf16_tflops_sustained")
     if rank == 0 and a.sweep and world == 1:
         sweep = []
         tb = [int(s) for s in a.sweep.split(",") if s and int(s) <= q.shape[0]]
@@ -418,7 +555,10 @@ def run_ours(a):
             # (nominal 80.5 TFLOP/s) for the FP32 kernels at large batch, bf16 tensor (measured)
             # for the shortlist kernel
             row["kernel_frac_hbm"] = round(row["kernel_gbs"] / peak, 4)
-            row["kernel_frac_fp32"] = round(row["kernel_tflops"] / 80.5, 4)
+            if info_b.get("tc_exact"):  # the bf16 tensor-core pass, against the sustained bf16 peak
+                row["kernel_frac_bf16_sustained"] = round(row["kernel_tflops"] / bf16_sustained, 4)
+            else:
+                row["kernel_frac_fp32"] = round(row["kernel_tflops"] / 80.5, 4)
             row["bf16_tc_frac"] = round(row["bf16_tc_tflops"] / bf16_peak, 4)
             if True:  # certified exact tensor-core path: the scan kernel's results, bit for bit
                 q0, s0, f0 = idx.tc_exact_stats()
@@ -434,11 +574,29 @@ def run_ours(a):
         extra["filtered_sweep"] = filtered_sweep(idx, torch, qd, q, a, stream)
         extra["filtered_sweep_b256"] = filtered_sweep(idx, torch, qd, q, a, stream, batch=256)
 
+    if rank == 0 and world == 1 and a.metric == "ip" and a.n >= 8 * a.dim:
+        # the plain FP32 scan kernel at batch 1 (the drop-in's HBM-bound kernel)
+        stp = max(20, min(a.steps, 300))
+        _, sc_ms, _, sc_l = time_device(idx, torch, qd, a, 1, stp, 5, stream, method="skinny")
+        t_plain, tsrc_plain = measured_traffic("scan", a.n, a.dim, 1, a.k, a.metric)
+        extra["roofline_plain"] = hbm_roofline(a.n * a.dim * 4 + a.dim * 4 + a.k * 8, sc_ms / max(sc_l, 1), peak,
+                                               peak_kind, t_plain, tsrc_plain,
+                                               "scan_kernel (fused FP32 scan + top-k), batch 1, method skinny")
+
+    truth = None
+    if rank == 0 and world == 1 and not a.no_parity and a.metric == "ip":
+        extra["parity"], truth = parity_checks(vsg, idx, x, q, a)
+        extra["precision"] = precision_checks(vsg, idx, torch, qd, x, q, a, stream, truth)
+
+    if rank == 0 and world == 1 and not a.no_serve and a.metric == "ip":
+        extra["serve"] = serve_check(vsg, idx, q, a)
+
     if rank == 0 and not a.no_recall:
         from oracle import oracle as O
         nchk = min(a.batch, 16) if a.batch > 1 else 8
         ids, _ = idx.search(q[:nchk], a.k)
-        gi, _ = O.fp64_topk(x, q[:nchk], a.k, a.metric)
+        gi = truth[0][:nchk] if truth is not None and truth[0].shape[1] == a.k else O.fp64_topk(x, q[:nchk], a.k,
+                                                                                                 a.metric)[0]
         extra["recall_vs_fp64"] = vsg.recall_at_k(ids, gi, a.k)
         try:
             extra["near_ties_tolerated"] = O.check_ids(ids, gi, x, q[:nchk], a.metric)
@@ -456,8 +614,8 @@ def run_ours(a):
             "metric": f"exact top-{a.k} QPS at {a.n // 1000}Kx{a.dim}", "value": round(qps, 2),
             "unit": "queries/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": round(ms / a.steps, 5), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": dict(workload(a),
-                                                                                     parallelism=f"replicas{world}"),
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": dict(workload(a), parallelism=f"replicas{world}"),
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 2), "unit": "queries/s", "h2d_bytes_per_step": a.batch * a.dim * 4,
                     "d2h_bytes_per_step": a.batch * a.k * 8, "steps": e2e_steps},
@@ -606,15 +764,11 @@ def run_serve(a):
     """Config 5: the continuous-batching server vs the plain per-call FP32 path under open-loop load."""
     import torch
     import vecsearch_gb300 as vsg
-    from vecsearch_gb300 import datasets as D
     torch.cuda.set_device(0)
     x, q = make_data(a)
-    groups = D.zipf_groups(a.n, 2000, 1.1, seed=3)
-    sizes = np.bincount(groups, minlength=2000)
     idx = vsg.GpuBruteForceIndex(a.dim, "cosine")
     idx.add(x)
-    cand = [g for g in range(2000) if sizes[g] >= 100][:64]
-    words_by_group = {g: D.pack_bits(groups == g) for g in cand}
+    groups, words_by_group = serve_setup(a, idx, vsg)
     srv = vsg.Server(idx, max_batch=1024, max_k=100, slots=2)
     rates = [int(r) for r in a.rates.split(",") if r]
     serve_load(idx, srv, x, q, groups, words_by_group, 2000, 0.3, 1)  # warm-up

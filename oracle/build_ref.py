@@ -11,7 +11,9 @@ Two libraries:
   CMakeLists.txt:43-51), so on x86 it runs the AVX2 branch of distance.h.
   The reference's cmake build is not used.
 
-Usage: ``python oracle/build_ref.py [--ref /path/to/vecsearch]``.
+Usage: ``python oracle/build_ref.py [--ref /path/to/vecsearch]``. Without ``--ref`` the
+reference tree is taken from the environment variable ``VSG_REFERENCE_SRC``, else from the
+recipe's default location.
 """
 import argparse
 import os
@@ -19,7 +21,12 @@ import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DEFAULT = "/root/reference"
+REF_DEFAULT = os.environ.get("VSG_REFERENCE_SRC", "/root/reference")
+
+
+def reference_present(ref=REF_DEFAULT):
+    """True where the reference's CPU sources can be compiled (or were compiled already)."""
+    return os.path.exists(os.path.join(ref, "src")) or os.path.exists(os.path.join(HERE, "_ref", "libvsref.so"))
 
 
 def _run(cmd):

@@ -108,8 +108,19 @@ def fp64_topk(x, q, k, metric="ip", allowed=None, chunk=65536):
             if rows.size == 0:
                 continue
         d = fp64_distances(x, q, metric, rows)
+        ri = np.broadcast_to(rows, (nq, rows.size))
+        kk = max(4 * k, k + 16)
+        if rows.size > kk:
+            # Preselect the kk smallest of the chunk per query (linear time); every row left out is
+            # at or above the largest kept value, so when that value lies above the k-th smallest
+            # kept one no row that ties the k-th is lost. Otherwise the whole chunk is sorted.
+            part = np.argpartition(d, kk - 1, axis=1)[:, :kk]
+            pd = np.take_along_axis(d, part, 1)
+            kth = np.partition(pd, k - 1, axis=1)[:, k - 1]
+            if np.all(pd.max(1) > kth):
+                d, ri = pd, np.take_along_axis(ri, part, 1)
         cat_d = np.concatenate([best_d, d], 1)
-        cat_i = np.concatenate([best_i, np.broadcast_to(rows, (nq, rows.size))], 1)
+        cat_i = np.concatenate([best_i, ri], 1)
         order = np.lexsort((cat_i, cat_d), axis=1)[:, :k]
         best_d = np.take_along_axis(cat_d, order, 1)
         best_i = np.take_along_axis(cat_i, order, 1)

@@ -16,7 +16,10 @@ The cases restate the reference's own tests:
   chunks        tests/python/test_gpu.py:48-57         70000 x 16, 5000 queries, k = 10
   filter_exact  tests/cpp/test_filter.cpp:87-97        5000 x 32, 100 queries, ~1% mask, exact_below 1000
   filter_third  tests/python/test_bindings.py:76-91    3000 x 64, mask[::3], exact_below = n
-  c1            config 1: 100k x 384 unit rows, 256-cluster mixture, IP, 64 queries, k = 10
+  c1            config 1: 100k x 384 unit rows, 256-cluster mixture, IP, 1,000 queries, k = 10
+  c1_k100       the same base, the first 256 of those queries, k = 100 (config 2's larger k)
+  c2_l2_100k    config 2's L2 variant at 100k rows: unnormalised rows of the same mixture, 256
+                queries, k = 10
   hnsw_small_l2.vshnsw   HNSWIndex::save (src/hnsw.cpp:375-389) of 150 x 13 rows, L2: the file
                 the device index loads its vectors from (HNSW_FILE below regenerates the rows)
 
@@ -67,10 +70,15 @@ def inputs(case):
         mask = np.zeros(3000, np.uint8)
         mask[::3] = 1
         return D.portable(3000, 64, 0), D.portable(100, 64, 11), 10, "l2", {"mask": mask, "exact_below": 3000}
-    if name == "c1":
+    if name in ("c1", "c1_k100"):
         x, _ = D.portable_clustered(100_000, 384, 256, 0.35, seed=0, centroid_seed=2)
-        q, _ = D.portable_clustered(64, 384, 256, 0.35, seed=1, centroid_seed=2)
-        return x, q, 10, "ip", {}
+        nq = 1000 if name == "c1" else 256
+        q, _ = D.portable_clustered(nq, 384, 256, 0.35, seed=1, centroid_seed=2)
+        return x, q, 10 if name == "c1" else 100, "ip", {}
+    if name == "c2_l2_100k":
+        x, _ = D.portable_clustered(100_000, 384, 256, 0.35, seed=0, centroid_seed=2, unit=False)
+        q, _ = D.portable_clustered(256, 384, 256, 0.35, seed=1, centroid_seed=2, unit=False)
+        return x, q, 10, "l2", {}
     raise KeyError(name)
 
 
@@ -89,6 +97,8 @@ CASES = [
     {"name": "filter_exact"},
     {"name": "filter_third"},
     {"name": "c1"},
+    {"name": "c1_k100"},
+    {"name": "c2_l2_100k"},
 ]
 
 
@@ -110,12 +120,16 @@ def hnsw_file_rows():
     return D.portable(HNSW_FILE["n"], HNSW_FILE["d"], HNSW_FILE["seed"])
 
 
-def main():
+def main(names=None):
+    """Regenerates every fixture, or only the named cases."""
     if build_reference() is None:
         sys.exit("the reference sources are not present; fixtures can only be made where they are")
     ref = Reference()
-    ref.hnsw_save(hnsw_file_rows(), os.path.join(OUT, HNSW_FILE["name"]), HNSW_FILE["metric"])
+    if not names:
+        ref.hnsw_save(hnsw_file_rows(), os.path.join(OUT, HNSW_FILE["name"]), HNSW_FILE["metric"])
     for c in CASES:
+        if names and c["name"] not in names:
+            continue
         x, q, k, metric, extra = inputs(c)
         if "mask" in extra:
             ids, dists = ref.hnsw_exact(x, q, k, extra["mask"], extra["exact_below"], metric, num_threads=4)
@@ -126,4 +140,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

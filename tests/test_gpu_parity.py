@@ -190,15 +190,49 @@ def test_duplicate_rows_tie_to_lower_id(gpu_ready):
             assert (row_d[a] == row_d[a:a + 3]).all() and list(row_i[a:a + 3]) == sorted(row_i[a:a + 3])
 
 
-def test_c1_config_against_fp64(gpu_ready):
-    # Config 1 (100k x 384 clustered unit rows, IP, k = 10): reference ids and FP64 recall 1.0.
+# Config-shape fixtures: the reference's outputs for 100k x 384 rows from a 256-cluster mixture.
+#   c1          unit rows, 1,000 queries, IP, k = 10 (config 1: batch sizes 1 and 128)
+#   c1_k100     the same base, 256 queries, k = 100
+#   c2_l2_100k  unnormalised rows of the same mixture, 256 queries, L2, k = 10
+# Every method runs each case at batch 1 and batch 128 over the queries in order. Method auto
+# takes the scan kernel at batch 1 on an index this small and the certified tensor-core path
+# (tc_exact) at batch 128; tc_exact runs the certified path at both.
+CONFIG_CASES = {"c1": 1000, "c1_k100": 256, "c2_l2_100k": 256}
+CONFIG_METHODS = ["auto", "tc_exact", "skinny", "tiled"]
+
+
+@pytest.fixture(scope="module")
+def config_indexes(gpu_ready):
     vsg = gpu_ready
-    want_i, want_d, x, q, k, metric, _ = load_golden("c1")
-    gpu = vsg.GpuBruteForceIndex(384, "cosine")
-    gpu.add(x)
-    for b in (1, 8, 64):
-        ids, dists = gpu.search(q[:b], k)
-        assert_parity(ids, dists, want_i[:b], want_d[:b], x, q[:b], metric)
+    out = {}
+    for name in CONFIG_CASES:
+        want_i, want_d, x, q, k, metric, _ = load_golden(name)
+        gpu = vsg.GpuBruteForceIndex(384, metric)
+        gpu.add(x)
+        out[name] = (want_i, want_d, x, q, k, metric, gpu)
+    yield out
+    out.clear()
+
+
+@pytest.mark.parametrize("batch", [1, 128])
+@pytest.mark.parametrize("method", CONFIG_METHODS)
+@pytest.mark.parametrize("name", list(CONFIG_CASES))
+def test_config_cases_against_reference(config_indexes, name, method, batch):
+    want_i, want_d, x, q, k, metric, gpu = config_indexes[name]
+    nq = len(q) if batch > 1 or name == "c1" else 64  # batch 1: every c1 query, 64 of the others
+    q0 = gpu.tc_exact_stats()[0]
+    parts = [gpu.search(q[s:min(s + batch, nq)], k, method=method) for s in range(0, nq, batch)]
+    ids = np.concatenate([p[0] for p in parts])
+    dists = np.concatenate([p[1] for p in parts])
+    assert_parity(ids, dists, want_i[:nq], want_d[:nq], x, q[:nq], metric)
+    certified = gpu.tc_exact_stats()[0] - q0
+    if method == "tc_exact" or (method == "auto" and batch == 128 and k <= 32):
+        assert certified == nq  # the certified path answered (its unproven queries via the scan)
+
+
+def test_c1_config_against_fp64(config_indexes):
+    # Config 1: the GPU's ids against the FP64 oracle (recall 1.0 up to the near-tie rule).
+    _, _, x, q, k, metric, gpu = config_indexes["c1"]
     gi, _ = O.fp64_topk(x, q, k, metric)
     ids, _ = gpu.search(q, k)
     O.check_ids(ids, gi, x, q, metric, rel=REL_TIE)

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from oracle.build_ref import reference_present
 from tests.conftest import load_golden
 from tests.golden.make_golden import CASES
 
@@ -12,10 +13,19 @@ BF_CASES = [c["name"] for c in CASES if not c["name"].startswith("filter")]
 FILTER_CASES = [c["name"] for c in CASES if c["name"].startswith("filter")]
 
 
+# The config-shape fixtures (100k x 384 rows) are checked on a prefix of their queries so that
+# the CPU suite stays short: the reference answers each query on its own (batch == single,
+# tests/cpp/test_brute_force.cpp:22-43), so a prefix of the queries has a prefix of the answers.
+CONFIG_PREFIX = 48
+
+
 @pytest.mark.parametrize("name", BF_CASES)
 def test_oracle_matches_reference_bitwise(name):
     want_i, want_d, x, q, k, metric, _ = load_golden(name)
-    for threads in (1, 3):
+    big = x.shape[0] * x.shape[1] > 10_000_000
+    if big:
+        want_i, want_d, q = want_i[:CONFIG_PREFIX], want_d[:CONFIG_PREFIX], q[:CONFIG_PREFIX]
+    for threads in ((4,) if big else (1, 3)):
         ids, dists = O.search(x, q, k, metric, num_threads=threads)
         np.testing.assert_array_equal(ids, want_i)
         np.testing.assert_array_equal(dists.view(np.uint32), want_d.view(np.uint32))
@@ -57,6 +67,7 @@ def test_k_prefix_property():
 def test_fp64_parity_rule_on_reference_outputs():
     # The reference's FP32 ids agree with the FP64 oracle up to the near-tie rule.
     want_i, want_d, x, q, k, metric, _ = load_golden("c1")
+    want_i, want_d, q = want_i[:200], want_d[:200], q[:200]
     gi, gd = O.fp64_topk(x, q, k, metric)
     O.check_ids(O.ids_to_int64(want_i), gi, x, q, metric)
     np.testing.assert_allclose(want_d, gd, rtol=0, atol=2e-6)
@@ -70,8 +81,7 @@ def test_check_ids_rejects_a_planted_mismatch():
         O.check_ids(bad, O.ids_to_int64(want_i), x, q, metric)
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(O.HERE), "oracle", "_ref", "libvsref.so"))
-                    and not os.path.exists("/root/reference/src"), reason="reference not built here")
+@pytest.mark.skipif(not reference_present(), reason="reference not built here")
 def test_oracle_vs_live_reference_dims():
     # distance.h tails (tests/cpp/test_distance.cpp:24-25 dims) and single == batch
     from oracle.build_ref import build_reference

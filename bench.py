@@ -228,10 +228,14 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, method="auto", out=None):
+def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, method="auto", out=None,
+                profile_steps=None):
     """Device-resident search: (ms total over `steps`, scan ms total, merge ms total, searches
-    profiled). With `out` (a dict): out["kernels"] = this index's kernel launches in the timed
-    steps, out["tc_exact"] = whether they ran the certified path."""
+    profiled). The timed steps run without the library's kernel events (their launches chain as
+    dependents); profile_steps more steps (default: as many) then record CUDA events around the
+    dominant kernel and the one after it, each launched on its own. With `out` (a dict):
+    out["kernels"] = this index's kernel launches in the timed steps, out["tc_exact"] = whether
+    they ran the certified path."""
     k = a.k
     out_i = torch.empty((batch, k), dtype=torch.int32, device=qd.device)
     out_d = torch.empty((batch, k), dtype=torch.float32, device=qd.device)
@@ -246,7 +250,6 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, meth
     for i in range(warmup):
         step(i)
     torch.cuda.synchronize()
-    idx.profile(True)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -266,6 +269,10 @@ def time_device(idx, torch, qd, a, batch, steps, warmup, stream, dist=None, meth
     if out is not None:
         out["kernels"] = idx.kernel_launches() - k0
         out["tc_exact"] = idx.tc_exact_stats()[0] > tq0
+    idx.profile(True)
+    for i in range(steps if profile_steps is None else profile_steps):
+        step(warmup + steps + i)
+    torch.cuda.synchronize()
     scan_ms, merge_ms, launches = idx.profile_read()
     idx.profile(False)
     idx.sync()
@@ -409,7 +416,7 @@ def precision_checks(vsg, idx, torch, qd, x, q, a, stream, truth):
             ok = ids[i] >= 0
             d64 = O.fp64_distances(x, q[i:i + 1], "ip", ids[i][ok])[0]
             err = max(err, float(np.max(np.abs(dists[i][ok].astype(np.float64) - d64))))
-        ms, _, _, _ = time_device(idx, torch, qd, a2, 128, 20, 3, stream, method=method)
+        ms, _, _, _ = time_device(idx, torch, qd, a2, 128, 20, 3, stream, method=method, profile_steps=0)
         out.append({"copy": method, "k": 10, "k_prime": 10 * over, "batch": 128, "queries_checked": nq,
                     "recall_at_10_vs_fp64": vsg.recall_at_k(ids, gi, 10), "max_abs_dist_err_vs_fp64": err,
                     "qps": round(128 * 20 / (ms / 1e3), 1)})
@@ -465,7 +472,7 @@ def run_ours(a):
     sampler = ClockSampler(local)
     info = {}
     ms, scan_ms, merge_ms, launches = time_device(idx, torch, qd, a, a.batch, a.steps, a.warmup, stream, dist,
-                                                  method=a.method, out=info)
+                                                  method=a.method, out=info, profile_steps=min(a.steps, 200))
     clocks = sampler.stop()
     if dist is not None:
         t = torch.tensor([ms], device=f"cuda:{local}")
@@ -538,11 +545,13 @@ def run_ours(a):
                    "kernel_gbs": round(row_bytes / (scan_b / l_b / 1e3) / 1e9, 1),
                    "kernel_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)}
             if b == 1:
-                ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method="skinny")
+                ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method="skinny",
+                                            profile_steps=0)
                 row["skinny_qps"] = round(b * max(3, st // 2) / (ms_m / 1e3), 1)
             if 8 <= b <= 256:  # both plain kernels near the auto crossover
                 for m in ("skinny", "tiled"):
-                    ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method=m)
+                    ms_m, _, _, _ = time_device(idx, torch, qd, a, b, max(3, st // 2), 3, stream, method=m,
+                                                profile_steps=0)
                     row[m + "_qps"] = round(b * max(3, st // 2) / (ms_m / 1e3), 1)
             # precision form: BF16 tensor-core shortlist (k' = 4k) + exact FP32 rerank
             sb = max(3, min(200, int(2e5 / b)))
@@ -562,7 +571,7 @@ def run_ours(a):
             row["bf16_tc_frac"] = round(row["bf16_tc_tflops"] / bf16_peak, 4)
             if True:  # certified exact tensor-core path: the scan kernel's results, bit for bit
                 q0, s0, f0 = idx.tc_exact_stats()
-                ms_e, _, _, _ = time_device(idx, torch, qd, a, b, sb, 3, stream, method="tc_exact")
+                ms_e, _, _, _ = time_device(idx, torch, qd, a, b, sb, 3, stream, method="tc_exact", profile_steps=0)
                 q1, s1, f1 = idx.tc_exact_stats()
                 row["tc_exact_qps"] = round(b * sb / (ms_e / 1e3), 1)
                 row["tc_exact_uncertified"] = round((s1 - s0) / max(q1 - q0, 1), 4)
@@ -685,10 +694,12 @@ def run_precision(a):
                             stp = max(3, min(50, int(2e4 / b)))
                             best = None
                             for m in (("skinny", "tiled") if b <= 512 else ("tiled",)):
-                                msp, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method=m)
+                                msp, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method=m,
+                                                           profile_steps=0)
                                 best = msp if best is None else min(best, msp)
                             row["plain_qps"][b] = round(b * stp / (best / 1e3), 1)
-                            mse, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method="tc_exact")
+                            mse, _, _, _ = time_device(idx, torch, qd, a2, b, stp, 2, stream, method="tc_exact",
+                                                       profile_steps=0)
                             row["exact_tc_qps"][b] = round(b * stp / (mse / 1e3), 1)
                     ids, dists = idx.search(q[:nchk], k, method=dtype)
                     gi, gd = truth[k]

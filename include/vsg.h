@@ -45,10 +45,9 @@ extern "C" {
  * Methods 0-3 return the same exact top-k; the method only picks the kernel (naive and skinny:
  * the streaming scan kernel; tiled: the register-blocked kernel; auto: by batch size).
  * VSG_METHOD_BF16 (new) is the precision form: a BF16 tensor-core pass keeps a shortlist of
- * k' = min(120, max(k, oversample x k)) rows per query by approximate distance, then an exact
+ * k' = min(448, max(k, oversample x k)) rows per query by approximate distance, then an exact
  * FP32 rerank of the shortlist returns the top-k with the streaming kernel's arithmetic. It is
- * exact whenever the shortlist holds the true top-k. Filters apply to the shortlist; k > 120 runs
- * the exact FP32 kernels instead. */
+ * exact whenever the shortlist holds the true top-k. Filters apply to the shortlist. */
 #define VSG_METHOD_AUTO 0u
 #define VSG_METHOD_NAIVE 1u
 #define VSG_METHOD_SKINNY 2u
@@ -57,21 +56,20 @@ extern "C" {
 /* VSG_METHOD_TC_EXACT (new): the shortlist path with a certificate. The finish kernel (merge,
  * FP32 rerank, certificate) bounds the difference between each row's bf16 approximate distance
  * and its FP32 distance (from the bf16 rounding of the query and the rows), and proves that no
- * row outside the shortlist can enter the top k; the shortlist keeps each query's rows within "cert_margin" x E of its k-th best (at
- * most k' = 120). Queries it cannot prove run in the streaming scan kernel, launched on the
- * device's own count of them (nothing waits on the host). Results equal VSG_METHOD_SKINNY bit for
- * bit, with or without a filter. Method AUTO uses it for unfiltered batches (k <= 32) of at least
- * "tc_exact_min_batch" queries, or of any size on an index of at least "tc_exact_min_elements",
- * or where the autotuner picked it; for filtered batches (k <= 32) of 8+ queries whose size times the largest
+ * row outside the shortlist can enter the top k; the shortlist keeps each query's rows within
+ * "cert_margin" x E of its k-th best (at most k' = 120 for k <= 16, 448 above). Queries it cannot
+ * prove run in the streaming scan kernel, launched on the device's own count of them (nothing
+ * waits on the host). Results equal VSG_METHOD_SKINNY bit for bit, with or without a filter, for
+ * every k <= 128. Method AUTO uses it for unfiltered batches of at least "tc_exact_min_batch"
+ * queries, or of any size on an index of at least "tc_exact_min_elements", or where the
+ * autotuner picked it; for filtered batches (k <= 32) of 8+ queries whose size times the largest
  * allowed fraction of their host masks is at least 0.35, or with too many allowed rows for the
  * gather scan, and for every filtered batch of at least half "tc_exact_min_batch" (device-resident
- * masks: from "tc_exact_min_batch", or twice it when the gather scan applies). k > 120 runs the
- * FP32 kernels. */
+ * masks: from "tc_exact_min_batch", or twice it when the gather scan applies). */
 #define VSG_METHOD_TC_EXACT 5u
 /* VSG_METHOD_FP8 (new): the precision form over an FP8-e4m3 copy of the rows with one FP32 scale
  * per row (and per query): half the bytes of the bf16 copy, a coarser score, the same exact FP32
- * rerank of a shortlist of k' = min(120, max(k, oversample x k)) rows. k > 120 runs the FP32
- * kernels. */
+ * rerank of a shortlist of k' = min(448, max(k, oversample x k)) rows. */
 #define VSG_METHOD_FP8 6u
 
 #define VSG_NONE 0xFFFFFFFFu /* GpuBruteForceIndex::kNone (gpu_brute_force.h:26) */
@@ -182,7 +180,14 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   "fallback_split_queries" (default 128, 0 to 2^20): VSG_METHOD_TC_EXACT's scan of the
  *   queries it did not certify splits the rows as for at most this many queries, so that a few
  *   such queries in a large batch still spread over the SMs (0: split as for the whole batch).
- *   Results are the same for every value. */
+ *   Results are the same for every value.
+ *   "wait_limit_s" (default 2, 1e-6 to 60): how long one kernel wait on another part of the same
+ *   kernel (a copy landing, a slot freed, an accumulator filled) may last before the kernel winds
+ *   down and the search returns VSG_ERR_DEVICE_TIMEOUT; the index stays usable. A CTA always
+ *   waits up to 2 s for its own copies and MMAs before it exits, whatever this value.
+ *   "test_stall_wait" (0 or 1; for testing the failure path): 1 makes the next search's scan or
+ *   shortlist kernels first wait on a barrier that nothing completes, so that wait runs out after
+ *   "wait_limit_s" and the search returns VSG_ERR_DEVICE_TIMEOUT; it resets to 0 after that search. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 
@@ -190,7 +195,7 @@ int vsg_get_tunable(vsg_index* index, const char* name, double* value);
  * vsg_autotune times candidate schedules for each batch size (queries 0.9 x_i + 0.1 x_j of rows;
  * CUDA events, the mean over 3 different batches after a warm-up) and keeps the fastest per batch size:
  *   method VSG_METHOD_AUTO: streaming scan, tiled kernel or certified shortlist (VSG_METHOD_TC_EXACT),
- *     with 1x or 2x the row splits for the FP32 kernels (the certified path runs with k' = 120;
+ *     with 1x or 2x the row splits for the FP32 kernels (the certified path runs with its default k';
  *     a table loaded from a file may name a narrower first pass), used by
  *     unfiltered method-auto searches of at least that many queries (largest tuned batch <= nq);
  *   method VSG_METHOD_BF16: how many rows the shortlist path samples for its starting thresholds
@@ -211,7 +216,7 @@ int vsg_autotune_load(vsg_index* index, const char* path);
 
 /* Certified exact path counters since the index was created: queries searched, queries the
  * shortlist pass could not certify, and queries that ran in the scan kernel (the same queries:
- * the one shortlist pass runs with k' = 120). The uncertified count is kept on the device, so
+ * there is one shortlist pass). The uncertified count is kept on the device, so
  * this call waits for the index's queued work. */
 int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* second, uint64_t* fallbacks);
 
@@ -228,11 +233,13 @@ int vsg_profile_read(vsg_index* index, double* scan_ms, double* merge_ms, size_t
 
 /* Serving loop (new; the reference answers one call at a time, python/bindings.cpp:165-186, and its
  * shard worker calls the index per request, distributed/shard_worker.py:26-36). A worker thread
- * batches requests continuously onto the BF16 shortlist + exact FP32 rerank path: requests that
- * arrive while others run join the next free slot; each slot replays one CUDA graph (persistent
- * shortlist kernel, fused merge + rerank). Results equal vsg_search with VSG_METHOD_BF16 and do not
- * depend on the other requests in a batch.
- *   vsg_server_create: max_batch queries per slot (a request may not exceed it), k <= max_k <= 120,
+ * batches requests continuously onto the certified tensor-core path: requests that arrive while
+ * others run join the next free slot; each slot replays one CUDA graph (query preparation with the
+ * certificate's bounds, sample pass, persistent shortlist kernel, finish kernel with the
+ * certificate, and the FP32 scan of the queries it could not prove, launched on the device's count
+ * of them). Every result equals vsg_search with VSG_METHOD_SKINNY bit for bit and does not depend
+ * on the other requests in a batch.
+ *   vsg_server_create: max_batch queries per slot (a request may not exceed it), k <= max_k <= 128,
  *     up to `slots` slots, fewer if half of the free HBM cannot hold them (VSG_ERR_NOMEM if none
  *     fits). The index must not be added to while a server uses it.
  *   vsg_server_submit: host queries (nq x dim), optional host allow-bits (ceil(size / 32) words,
@@ -240,7 +247,9 @@ int vsg_profile_read(vsg_index* index, double* scan_ms, double* merge_ms, size_t
  *     valid until vsg_server_wait returns; returns a ticket.
  *   vsg_server_wait: blocks until the request is done (or timeout_s > 0 passes:
  *     VSG_ERR_DEVICE_TIMEOUT); latency_ms = submit to completion. A ticket is waited for once.
- *   vsg_server_stats: micro-batches launched, queries and requests submitted, slots. */
+ *   vsg_server_stats: micro-batches launched, queries and requests submitted, slots.
+ *   vsg_server_uncertified: queries of finished micro-batches that the certificate could not
+ *     prove (answered by the FP32 scan in the same graph). */
 typedef struct vsg_server vsg_server;
 int vsg_server_create(vsg_index* index, size_t max_batch, size_t max_k, size_t slots, vsg_server** out);
 int vsg_server_submit(vsg_server* server, const float* queries, size_t nq, size_t k, const uint32_t* mask_words,
@@ -248,6 +257,7 @@ int vsg_server_submit(vsg_server* server, const float* queries, size_t nq, size_
 int vsg_server_wait(vsg_server* server, uint64_t ticket, double timeout_s, double* latency_ms);
 int vsg_server_stats(vsg_server* server, uint64_t* batches, uint64_t* queries, uint64_t* requests,
                      uint64_t* slots);
+int vsg_server_uncertified(vsg_server* server, uint64_t* queries);
 void vsg_server_destroy(vsg_server* server);
 
 /* Exact top-k over caller-owned device buffers, for callers that cannot allocate device memory
@@ -257,8 +267,9 @@ void vsg_server_destroy(vsg_server* server);
  *
  * d_rows: n x dim device floats (row stride dim); d_queries: nq x dim device floats; dim a multiple
  * of 4, both pointers 16-byte aligned. Results go to d_out_ids / d_out_dists (nq x k, device), with
- * the same order and padding as vsg_search. Work is queued on `stream` (a cudaStream_t, NULL =
- * legacy default stream), and the call waits for it so it can report a device-side failure.
+ * the same order and padding as vsg_search (n == 0 fills every result with VSG_NONE / +inf). Work
+ * is queued on `stream` (a cudaStream_t, NULL = legacy default stream), and the call waits for it
+ * so it can report a device-side failure.
  *
  * It allocates nothing: its scratch (the per-split top-k lists and a status word) is one static
  * 4 MiB device array in the library, which every GPU that loads the library holds until exit.

@@ -1,9 +1,8 @@
-"""GPU: the continuous-batching server (persistent BF16 shortlist kernel in CUDA graphs).
+"""GPU: the continuous-batching server (certified tensor-core path in CUDA graphs).
 
-A request's result must equal the index's own BF16 shortlist search for unfiltered requests
-(bitwise: the same shortlist and the same exact rerank) and the exact filtered search for
-filtered ones (parity rule of test_gpu_parity.py), and must be the same alone and inside a
-burst of other requests.
+Every served result must equal the index's FP32 scan kernel (method skinny) bit for bit, filtered
+or not, and the oracle (the reference's CPU search restated) within the parity rule of
+test_gpu_parity.py; and it must be the same alone and inside a burst of other requests.
 """
 import threading
 
@@ -25,7 +24,7 @@ def served(gpu_ready):
     groups = D.zipf_groups(len(x), 200, 1.1, seed=93)
     idx = vsg.GpuBruteForceIndex(128, "cosine")
     idx.add(x)
-    srv = vsg.Server(idx, max_batch=256, max_k=20, slots=2)
+    srv = vsg.Server(idx, max_batch=256, max_k=100, slots=2)
     yield vsg, idx, srv, x, q, groups
     srv.close()
 
@@ -35,14 +34,19 @@ def _requests(q, groups, rng, n):
     for _ in range(n):
         m = int(np.exp(rng.uniform(0, np.log(32))))  # 1..32 queries, log-uniform
         m = min(m, len(q) - pos) or 1
-        k = int(rng.choice([10, 20]))
+        k = int(rng.choice([10, 20, 100]))
         filt = (groups == int(rng.integers(0, 40))) if rng.random() < 0.3 else None
         reqs.append((q[pos:pos + m], k, filt))
         pos = (pos + m) % (len(q) - 32)
     return reqs
 
 
-def test_server_matches_index_paths(served):
+def _same(got, want):
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[1].view(np.uint32), want[1].view(np.uint32))
+
+
+def test_server_is_exact(served):
     vsg, idx, srv, x, q, groups = served
     rng = np.random.default_rng(5)
     reqs = _requests(q, groups, rng, 40)
@@ -50,15 +54,37 @@ def test_server_matches_index_paths(served):
     for (r, k, f), t in zip(reqs, tickets):
         ids, dists, lat = srv.wait(t, timeout=30)
         assert ids.shape == (len(r), k) and lat > 0
-        if f is None:
-            bi, bd = idx.search(r, k, method="bf16")
-            np.testing.assert_array_equal(ids, bi)
-            np.testing.assert_array_equal(dists.view(np.uint32), bd.view(np.uint32))
-        else:
-            wi, wd = O.search(x, r, k, "ip", num_threads=4, allowed=f.astype(np.uint8))
-            assert_parity(ids, dists, wi, wd, x, r, "ip")
+        _same((ids, dists), idx.search(r, k, method="skinny", filter=f))
+        wi, wd = O.search(x, r, k, "ip", num_threads=4, allowed=None if f is None else f.astype(np.uint8))
+        assert_parity(ids, dists, wi, wd, x, r, "ip")
     st = srv.stats()
     assert st["requests"] >= 40 and st["batches"] >= 1 and st["slots"] >= 1
+    assert st["uncertified"] < st["queries"] // 10  # the certificate holds for most queries
+
+
+def test_server_falls_back_when_it_cannot_prove(gpu_ready):
+    # Rows 1e-4 apart around a few centres: distances closer than the bf16 error bound, so most
+    # queries are not certified and run in the FP32 scan inside the slot's graph, filtered or
+    # not; results still equal the scan's bit for bit.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    centres = D.portable(50, 64, 210, normalize=True)
+    x = vsg.normalize(np.repeat(centres, 400, axis=0) + 1e-4 * D.portable(20_000, 64, 211))
+    q = vsg.normalize(centres[:40] + 1e-3 * D.portable(40, 64, 212))
+    idx = vsg.GpuBruteForceIndex(64, "cosine")
+    idx.add(x)
+    mask = np.zeros(len(x), bool)
+    mask[::3] = True
+    srv = vsg.Server(idx, max_batch=64, max_k=100, slots=2)
+    try:
+        reqs = [(q[:17], 10, None), (q[17:40], 100, mask), (q[5:6], 33, None), (q[20:36], 10, mask)]
+        tickets = [srv.submit(r, k, f) for r, k, f in reqs]
+        for (r, k, f), t in zip(reqs, tickets):
+            ids, dists, _ = srv.wait(t, timeout=30)
+            _same((ids, dists), idx.search(r, k, method="skinny", filter=f))
+        assert srv.stats()["uncertified"] > 0  # the fallback ran
+    finally:
+        srv.close()
 
 
 def test_alone_equals_in_the_mix(served):
@@ -91,6 +117,6 @@ def test_server_rejects_bad_requests(served):
     with pytest.raises(ValueError):
         srv.submit(q[:300], 10)  # more queries than a slot holds
     with pytest.raises(ValueError):
-        srv.submit(q[:3], 21)  # k above max_k
+        srv.submit(q[:3], 101)  # k above max_k
     with pytest.raises(ValueError):
         srv.submit(q[:3], 10, np.ones(5, bool))

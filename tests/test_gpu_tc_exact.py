@@ -131,10 +131,12 @@ def test_auto_routes_large_batches(gpu_ready):
     assert gpu.get_tunable("tc_exact_min_batch") == 128
     q0 = gpu.tc_exact_stats()[0]
     _same(gpu.search(q, 10), gpu.search(q, 10, method="skinny"))  # auto: 256 >= 128, k <= 32
+    assert gpu.tc_exact_stats()[0] - q0 == 256
+    _same(gpu.search(q, 64), gpu.search(q, 64, method="skinny"))  # every k <= 128 unfiltered
     q1 = gpu.tc_exact_stats()[0]
-    assert q1 - q0 == 256
+    assert q1 - q0 == 512
     gpu.search(q[:64], 10)  # below the threshold: FP32 kernels
-    gpu.search(q, 64)  # k > 32: FP32 kernels
+    gpu.search(q[:64], 100)
     # Filtered: the certified path when (batch x largest allowed fraction) >= 0.35, from 8 queries,
     # and for every filtered batch from half the threshold (64 queries).
     few = np.zeros(len(x), bool)

@@ -103,8 +103,8 @@ def test_auto_routing(harness):
     want = {
         (big, 384, 1, 10, AUTO, 0, 0, -1.0): (1, 0),       # a large index: every batch size
         (big, 384, 1, 32, AUTO, 0, 0, -1.0): (1, 0),
-        (big, 384, 1, 33, AUTO, 0, 0, -1.0): (0, 0),       # k > 32: the FP32 kernels
-        (big, 384, 64, 100, AUTO, 0, 0, -1.0): (0, 1),
+        (big, 384, 1, 33, AUTO, 0, 0, -1.0): (1, 0),       # every k <= 128
+        (big, 384, 64, 100, AUTO, 0, 0, -1.0): (1, 1),
         (small, 384, 1, 10, AUTO, 0, 0, -1.0): (0, 0),
         (small, 384, 47, 10, AUTO, 0, 0, -1.0): (0, 0),
         (small, 384, 48, 10, AUTO, 0, 0, -1.0): (0, 1),    # tiled_min_batch
@@ -113,7 +113,7 @@ def test_auto_routing(harness):
         (edge, 384, 1, 10, AUTO, 0, 0, -1.0): (0, 0),
         (edge + 1, 384, 1, 10, AUTO, 0, 0, -1.0): (1, 0),  # tc_exact_min_elements
         (small, 384, 1, 120, TC_EXACT, 0, 0, -1.0): (1, 0),
-        (small, 384, 1, 121, TC_EXACT, 0, 0, -1.0): (0, 0),  # k' is capped at 120
+        (small, 384, 1, 128, TC_EXACT, 0, 0, -1.0): (1, 0),  # k' up to 448 covers every k
         (big, 384, 500, 10, SKINNY, 0, 0, -1.0): (0, 0),
         (big, 384, 500, 10, TILED, 0, 0, -1.0): (0, 1),
         (big, 384, 500, 10, BF16, 0, 0, -1.0): (0, 0),

@@ -59,6 +59,54 @@ def test_noalloc_matches_regular_entry_point(gpu_ready, metric):
         np.testing.assert_allclose(od.cpu().numpy(), rd.cpu().numpy(), rtol=RTOL, atol=ATOL)
 
 
+@pytest.mark.parametrize("n,dim,k,metric", [(30000, 36, 10, "l2"),   # dim % 8 == 4: no padding here
+                                             (20000, 132, 17, "ip"),
+                                             (50, 64, 100, "l2")])    # k > n: padded with -1 / +inf
+def test_noalloc_matches_oracle(gpu_ready, n, dim, k, metric):
+    # The same entry point against the oracle (the reference's CPU search restated) with the
+    # parity rule of the other tests: distances within rtol 1e-5 + atol 2e-6, ids equal except
+    # at near-ties. Two calls in a row with different shapes reuse the static scratch.
+    import torch
+
+    from oracle import oracle as O
+    from vecsearch_gb300 import _native
+    from vecsearch_gb300 import datasets as D
+
+    lib = _native.lib()
+    x = D.portable(n, dim, 23, normalize=metric == "ip")
+    q = D.portable(40, dim, 24, normalize=metric == "ip")
+    xd = torch.from_numpy(x).cuda()
+    qd = torch.from_numpy(q).cuda()
+    code = _native.METRIC_L2 if metric == "l2" else _native.METRIC_IP
+    for nq in (40, 3):
+        oi = torch.full((nq, k), 7, dtype=torch.int32, device="cuda")
+        od = torch.full((nq, k), -1.0, dtype=torch.float32, device="cuda")
+        assert _noalloc(lib, xd, n, dim, code, qd, nq, k, oi, od) == _native.OK, lib.vsg_last_error()
+        torch.cuda.synchronize()
+        wi, wd = O.search(x, q[:nq], k, metric, num_threads=4)
+        ids = oi.cpu().numpy().astype(np.int64)
+        dists = od.cpu().numpy()
+        np.testing.assert_allclose(dists, wd, rtol=RTOL, atol=ATOL)
+        O.check_ids(ids, O.ids_to_int64(wi), x, q[:nq], metric)
+        assert ((ids >= 0) == np.isfinite(dists)).all()
+
+
+def test_noalloc_empty_rows_fill_missing(gpu_ready):
+    # No rows: every result is -1 / +inf, as the regular search fills an empty index.
+    import torch
+
+    from vecsearch_gb300 import _native
+
+    lib = _native.lib()
+    q = torch.zeros((4, 16), device="cuda")
+    oi = torch.zeros((4, 5), dtype=torch.int32, device="cuda")
+    od = torch.zeros((4, 5), dtype=torch.float32, device="cuda")
+    x = torch.zeros((1, 16), device="cuda")
+    assert _noalloc(lib, x, 0, 16, _native.METRIC_L2, q, 4, 5, oi, od) == _native.OK, lib.vsg_last_error()
+    torch.cuda.synchronize()
+    assert (oi.cpu().numpy() == -1).all() and np.isinf(od.cpu().numpy()).all()
+
+
 def test_noalloc_rejects_oversize_and_bad_shapes(gpu_ready):
     import torch
 

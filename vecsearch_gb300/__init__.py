@@ -10,6 +10,8 @@ Drop-in names (python/vecsearch/__init__.py and python/bindings.cpp of vecsearch
   one row per query.
 * :func:`cuda_available`, :func:`normalize`, :func:`recall_at_k`.
 * :class:`HNSWExactRoute` - the HNSW index's ``exact_below`` switch on the GPU.
+* :func:`pybind_module` - the same GpuBruteForceIndex and cuda_available as a compiled pybind11
+  module (``_vecsearch_gb300``), the form the reference's own bindings take.
 """
 import ctypes
 import operator
@@ -20,7 +22,7 @@ from . import _native
 from .datasets import pack_bits
 
 __all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "Server", "cuda_available", "normalize", "recall_at_k",
-           "hnsw_file_info", "DeviceTimeoutError"]
+           "hnsw_file_info", "DeviceTimeoutError", "pybind_module"]
 __version__ = "0.1.0"
 
 DeviceTimeoutError = _native.DeviceTimeoutError
@@ -35,6 +37,25 @@ def cuda_available() -> bool:
     except ImportError:
         return False
     return bool(l.vsg_cuda_available())
+
+
+def pybind_module():
+    """The pybind11 front end, module ``_vecsearch_gb300`` (GpuBruteForceIndex with the reference's
+    constructor, add, search, dim and len; cuda_available), or None where it was not built
+    (pybind11's headers absent). It calls the same library as this package."""
+    import importlib.machinery
+    import importlib.util
+    import os
+    from . import build as _build
+    path = _build.pybind_module_path()
+    if not os.path.exists(path):
+        return None
+    _native.lib()  # the library first: the module links against the same file
+    loader = importlib.machinery.ExtensionFileLoader("_vecsearch_gb300", path)
+    spec = importlib.util.spec_from_file_location("_vecsearch_gb300", path, loader=loader)
+    mod = importlib.util.module_from_spec(spec)
+    loader.exec_module(mod)
+    return mod
 
 
 def normalize(x: np.ndarray) -> np.ndarray:
@@ -280,7 +301,9 @@ class GpuBruteForceIndex:
 
 
 class Server:
-    """Continuous-batching search over a GpuBruteForceIndex (BF16 shortlist + exact FP32 rerank).
+    """Continuous-batching exact search over a GpuBruteForceIndex: the certified tensor-core path
+    (BF16 shortlist, exact FP32 rerank, a proof per query, the FP32 scan for queries it cannot
+    prove), so every result equals ``index.search(..., method="skinny")`` bit for bit.
 
     ``submit(queries, k, filter=None)`` queues a request and returns a ticket; ``wait(ticket)``
     returns ``(ids int64 [nq, k], dists float32 [nq, k], latency_ms)``. Requests arriving while
@@ -329,9 +352,13 @@ class Server:
         return _ids_to_int64(ids), dists, lat.value
 
     def stats(self):
+        """Micro-batches, queries, requests, slots, and the queries the certificate could not prove
+        (answered by the FP32 scan inside the same graph)."""
         v = [ctypes.c_uint64() for _ in range(4)]
         _native.check(_native.lib().vsg_server_stats(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("batches", "queries", "requests", "slots"), (x.value for x in v)))
+        u = ctypes.c_uint64()
+        _native.check(_native.lib().vsg_server_uncertified(self._h, ctypes.byref(u)))
+        return dict(zip(("batches", "queries", "requests", "slots", "uncertified"), [x.value for x in v] + [u.value]))
 
     def close(self):
         if self._h:

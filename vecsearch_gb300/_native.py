@@ -57,6 +57,7 @@ SIGNATURES = {
     "vsg_server_submit": (_INT, [_P, _P, _SZ, _SZ, _P, _P, _P, ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_server_wait": (_INT, [_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     "vsg_server_stats": (_INT, [_P] + [ctypes.POINTER(ctypes.c_uint64)] * 4),
+    "vsg_server_uncertified": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_server_destroy": (None, [_P]),
     "vsg_search_rows_noalloc": (_INT, [_P, _SZ, _SZ, _U32, _P, _SZ, _SZ, _P, _P, _P]),
 }

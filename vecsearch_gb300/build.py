@@ -2,7 +2,10 @@
 
 Each translation unit under csrc/ is compiled in parallel with nvcc, then linked
 into one shared library with the static CUDA runtime, so the library depends on
-nothing but the driver. ``python -m vecsearch_gb300.build [--verbose]``.
+nothing but the driver. Then the pybind11 front end (csrc/pybind_module.cpp, the
+reference's GpuBruteForceIndex surface) is compiled with g++ against it, where
+pybind11's headers are installed (the pybind11 package or PyTorch's copy).
+``python -m vecsearch_gb300.build [--verbose]``.
 """
 import concurrent.futures
 import os
@@ -40,8 +43,54 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def pybind_include():
+    """pybind11's headers: the pybind11 package, else the copy PyTorch ships (found without
+    importing torch); None if neither is installed."""
+    import importlib.util
+    try:
+        import pybind11
+        return pybind11.get_include()
+    except ImportError:
+        pass
+    spec = importlib.util.find_spec("torch")
+    for loc in (spec.submodule_search_locations or []) if spec else []:
+        inc = os.path.join(loc, "include")
+        if os.path.exists(os.path.join(inc, "pybind11", "pybind11.h")):
+            return inc
+    return None
+
+
+def pybind_module_path():
+    import sysconfig
+    return os.path.join(OUT_DIR, "_vecsearch_gb300" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def build_pybind(lib, verbose=False, force=False):
+    """The pybind11 front end (csrc/pybind_module.cpp) linked against the library; returns its path,
+    or None where pybind11's or Python's headers are missing."""
+    import sysconfig
+    pyinc = sysconfig.get_paths().get("include")
+    pbinc = pybind_include()
+    if not pbinc or not pyinc or not os.path.exists(os.path.join(pyinc, "Python.h")):
+        return None
+    src = os.path.join(CSRC, "pybind_module.cpp")
+    out = pybind_module_path()
+    if force or _stale(out, [src, lib] + _headers()):
+        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden",
+               "-I", pyinc, "-I", pbinc, src, "-o", out + ".tmp", "-L", OUT_DIR, "-l:" + LIB_NAME,
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed: " + " ".join(cmd))
+        os.replace(out + ".tmp", out)
+    return out
+
+
 def build(verbose=False, force=False):
-    """Builds (if stale) and returns the path of the shared library."""
+    """Builds (if stale) and returns the path of the shared library (and the pybind11 front end
+    where its headers are present)."""
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = nvcc_path()
     flags = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -70,6 +119,7 @@ def build(verbose=False, force=False):
         tmp = lib + ".tmp"
         subprocess.run([nvcc, *ARCH, "-shared", "-cudart", "static", *objs, "-o", tmp, "-lpthread"], check=True)
         os.replace(tmp, lib)
+    build_pybind(lib, verbose, force)
     return lib
 
 

@@ -22,6 +22,18 @@ constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s for any singl
 
 enum DevStatus : int { kDevOk = 0, kDevTimeout = 1 };
 
+// Programmatic dependent launch. A kernel launched with the programmatic stream serialization
+// attribute may start while the kernel before it in the stream still runs. It calls pdl_wait
+// before it reads anything a predecessor wrote or writes anything a predecessor may still read;
+// the wait returns once the predecessor has completed and its writes are visible (and, since the
+// predecessor waited the same way, every earlier kernel of the chain). Every thread of such a
+// kernel passes a pdl_wait before it exits, which keeps that ordering transitive. pdl_trigger lets
+// the next kernel start launching once every CTA of this one has called it (so all of them are
+// resident and a waiting dependent can never hold an SM one of them needs). Both return at once
+// in a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ bool nb_less(float ad, uint32_t ai, float bd, uint32_t bi) {
   return ad < bd || (ad == bd && ai < bi);
 }
@@ -65,13 +77,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for the phase with the given parity to complete. False after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Waits for the phase with the given parity to complete. False after limit_ns (kWaitLimitNs by
+// default; a kernel's waits on other roles take its tunable limit, the waits that drain its own
+// copies and MMAs before it exits keep the default).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+    if ((it & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
   }
 }
 

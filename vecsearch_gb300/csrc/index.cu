@@ -275,6 +275,12 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
       if (!(value >= 0.0 && value <= 1048576.0))
         throw std::invalid_argument("fallback_split_queries must be in [0, 2^20]");
       h->fallback_split_queries = std::floor(value);
+    } else if (nm == "wait_limit_s") {
+      if (!(value >= 1e-6 && value <= 60.0)) throw std::invalid_argument("wait_limit_s must be in [1e-6, 60]");
+      h->wait_limit_s = value;
+    } else if (nm == "test_stall_wait") {
+      if (value != 0.0 && value != 1.0) throw std::invalid_argument("test_stall_wait must be 0 or 1");
+      h->stall_next = value != 0.0;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -294,6 +300,8 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "cert_margin") *value = h->cert_margin;
     else if (nm == "tc_exact_min_elements") *value = h->tc_exact_min_elements;
     else if (nm == "fallback_split_queries") *value = h->fallback_split_queries;
+    else if (nm == "wait_limit_s") *value = h->wait_limit_s;
+    else if (nm == "test_stall_wait") *value = h->stall_next ? 1.0 : 0.0;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

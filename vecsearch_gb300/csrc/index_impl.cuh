@@ -133,9 +133,9 @@ struct vsg_index {
   size_t xmap8_rows = 0;
   DeviceBuffer cbuf;  // shortlist kernel: per-CTA candidate buffers (dists then ids)
   // Certified exact path (method tc_exact): rounding bounds of the bf16 rows, uncertified
-  // queries ([count][ids]), their gathered queries and FP32 results.
-  DeviceBuffer xbound, fails, fids, fq, fout, fmask;
-  double tc_exact_min_batch = 128;  // method auto, unfiltered, k <= 32: batches from this size
+  // queries ([count][ids]), their gathered queries and masks.
+  DeviceBuffer xbound, fails, fq, fmask;
+  double tc_exact_min_batch = 128;  // method auto, unfiltered: batches from this size
   uint64_t tc_exact_queries = 0;  // queries sent to the certified path
   DeviceBuffer tcstats;            // device tally of its uncertified queries (scan fallbacks)
   uint64_t kernel_launches = 0;    // this index's kernel launches (vsg_kernel_launches)
@@ -156,7 +156,7 @@ struct vsg_index {
   double gather_max_fraction = 0.10;
   // method "auto" uses the register-blocked tiled kernel from this batch size up.
   double tiled_min_batch = 48;
-  // method "bf16": the tensor-core pass keeps k' = min(120, max(k, oversample x k)) per query.
+  // method "bf16": the tensor-core pass keeps k' = min(448, max(k, oversample x k)) per query.
   double shortlist_oversample = 4;
   // method "bf16": rows sampled for the starting thresholds (0: no sample pass) when nothing
   // else is tuned for the batch size; batches under 8 queries skip it.
@@ -171,6 +171,13 @@ struct vsg_index {
   // method "tc_exact": the uncertified queries' scan splits the rows as for at most this many
   // queries (0: as for the whole batch).
   double fallback_split_queries = 128;
+  // Limit of one kernel wait on another role (seconds); past it the kernel winds down and the
+  // search reports VSG_ERR_DEVICE_TIMEOUT. The waits that drain a CTA's own copies keep 2 s.
+  double wait_limit_s = 2.0;
+  // Test hook ("test_stall_wait"): the next search's scan or shortlist kernels first wait on a
+  // barrier that nothing completes, so that wait runs out after wait_limit_s.
+  bool stall_next = false;
+  uint64_t wait_ns() const { return uint64_t(wait_limit_s * 1e9); }
 
   // ---- autotuned schedules (vsg_autotune) ----
   // plain: for unfiltered method "auto" searches of at least `batch` queries (largest such entry),
@@ -390,10 +397,11 @@ struct vsg_index {
   }
 
   // Certified exact path: the list keeps the rows within each query's margin of its k-th best,
-  // up to k' entries. The widest k' (120) certifies the most queries and costs about the same as
-  // a narrower one (the candidate buffers are the same size), so it is always the first pass;
-  // a table entry may still name a narrower one.
-  static uint32_t exact_shortlist_size(size_t) { return uint32_t(vsg::kTcMaxShortlist); }
+  // up to k' entries. For k <= 16, k' = 120: the rows within the margin (about 50-120 for
+  // k = 10 on 1M clustered unit rows) fit, and the 256-entry candidate buffers sort fast; larger
+  // k take the widest list (448; about 260-420 rows lie within the margin of the 100th-128th
+  // best there). A table entry may still name another k'.
+  static uint32_t exact_shortlist_size(size_t k) { return k <= 16 ? 120u : uint32_t(vsg::kTcMaxShortlist); }
 
   uint32_t shortlist_size(size_t k) const {
     const double want = std::max<double>(double(k), shortlist_oversample * double(k));
@@ -497,6 +505,8 @@ struct vsg_index {
     a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
     a.part_n = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 8);
     a.status = status_word();
+    a.wait_ns = wait_ns();
+    a.stall = stall_next ? 1u : 0u;
     Timing* tm = profiling ? next_timing() : nullptr;
     // Batches first score a sample of rows (whole tiles at the head of every split; 16K rows for
     // 8+ queries, 4K below, unless tuned) and start each query at the k'-th best sampled distance, so the
@@ -507,6 +517,10 @@ struct vsg_index {
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
                          : nq >= 8 ? size_t(sample_rows) : std::min<size_t>(size_t(sample_rows), 4096);
+    // After the query preparation the path's kernels run as a chain of programmatic dependent
+    // launches (each may start while the one before it finishes); not while profiling, whose
+    // events time the main pass on its own.
+    const bool pdl = !f8 && !profiling;
     if (srows > 0 && tiles_per_split > 1) {
       vsg::TcArgs sa = a;
       uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
@@ -528,19 +542,20 @@ struct vsg_index {
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
       sa.gthr = nullptr;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s));
+      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s, pdl));
       ++kernel_launches;
       // (with margins: the k-th best sampled distance plus the margin)
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
-                                         margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin));
+                                         margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin,
+                                         pdl));
       ++kernel_launches;
       a.thr_init = static_cast<const float*>(thr.get());
     }
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));  // the profile times the main pass alone
-    VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s));
+    VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s, pdl));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    // Merge, rerank and (certified path) certificate in one launch.
+    // Cut, rerank and (certified path) certificate in one launch.
     vsg::FinishArgs fa{};
     fa.part_d = a.part_d;
     fa.part_i = a.part_i;
@@ -549,75 +564,74 @@ struct vsg_index {
     fa.nsplit = a.nsplit;
     fa.kp = kp;
     fa.k = uint32_t(k);
-    fa.margin = margins ? a.margin : nullptr;  // the merged list keeps the rows within the margin
+    fa.margin = margins ? a.margin : nullptr;  // the cut keeps the rows within the margin
     fa.x = static_cast<const float*>(x.get());
+    fa.n = uint32_t(n);
     fa.q = dq;
     fa.dp = uint32_t(dp);
     fa.ldq = uint32_t(ldq);
     fa.l2 = a.l2;
     fa.out_d = out_dists;
     fa.out_i = out_ids;
+    fa.status = status_word();
+    fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * kp));
     if (certify && !f8) {
       fa.thr_init = a.thr_init;
       fa.gthr = a.gthr;
       fa.err = static_cast<const float*>(qmargin.get()) + nq;
       fa.fail_count = static_cast<uint32_t*>(fails.get());
       fa.fail_list = fa.fail_count + 1;
+      // each uncertified query's FP32 row (and per-query mask) goes to its fallback slot
+      fq.reserve(nq * dp * sizeof(float), 0, stream);
+      fa.fq = static_cast<float*>(fq.get());
+      if (dmask && mask_ld) {
+        fmask.reserve(nq * mask_ld * sizeof(uint32_t), 0, stream);
+        fa.qmask = dmask;
+        fa.fmask = static_cast<uint32_t*>(fmask.get());
+        fa.mask_ld = uint32_t(mask_ld);
+      }
+      tcstats.reserve(sizeof(unsigned long long), 0, stream);
+      fa.tally = static_cast<unsigned long long*>(tcstats.get());
     }
-    VSG_CUDA(vsg::launch_finish(fa, s));
+    VSG_CUDA(vsg::launch_finish(fa, uint32_t(nq), s, pdl));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
   }
 
   // Exact top-k through the shortlist. Queries whose result the finish kernel cannot certify (see
   // vsg::FinishArgs) run in the streaming scan kernel, so results equal method skinny bit for bit.
-  // Nothing waits on the host: the finish kernel leaves the uncertified queries' count and
-  // indices on the device, and the fallback launches (gather, scan, scatter) are sized for all nq
-  // queries, their blocks past that count returning at once (the scan's row splits: plan()). A tally of uncertified queries stays on the
-  // device (tc_stats_sync reads it).
+  // Nothing waits on the host: the finish kernel leaves the uncertified queries' count, indices,
+  // FP32 rows (and per-query masks) on the device, and one scan launch sized for all nq queries,
+  // its blocks past that count returning at once, writes their results over theirs (its fused
+  // merge maps slot j to query fail_list[j]; row splits: plan()). A tally of uncertified queries
+  // stays on the device (tc_stats_sync reads it).
   void enqueue_tc_exact(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                         cudaStream_t s, const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
     fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
     tcstats.reserve(sizeof(unsigned long long), 0, stream);
-    // Shortlist cap: a tuned entry may name one; else 120, which certifies the most queries.
+    // Shortlist cap: a tuned entry may name one; else exact_shortlist_size(k).
     const TuneEntry* te = dmask ? nullptr : lookup(tune_plain, nq);
     uint32_t kp1 = force_exact_kp > 0 ? uint32_t(force_exact_kp) : te && te->kernel == 2 ? te->exact_kp : 0u;
     kp1 = kp1 ? std::max<uint32_t>(std::min<uint32_t>(kp1, uint32_t(vsg::kTcMaxShortlist)), uint32_t(k))
               : exact_shortlist_size(k);
-    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);  // zeroes the count
+    // zeroes the count; the finish kernel fills the fallback's rows and masks
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);
     tc_exact_queries += nq;
     const uint32_t* d_count = static_cast<const uint32_t*>(fails.get());
     const uint32_t* d_list = d_count + 1;
-    fq.reserve(nq * dp * sizeof(float), 0, stream);
-    fout.reserve(nq * k * 8, 0, stream);
-    float* q1 = static_cast<float*>(fq.get());
-    uint32_t* oi1 = static_cast<uint32_t*>(fout.get());
-    float* od1 = reinterpret_cast<float*>(oi1 + nq * k);
-    VSG_CUDA(vsg::launch_gather_rows(q1, dq, ldq, uint32_t(dp), d_list, uint32_t(nq), s, d_count));
-    ++kernel_launches;
     // Per-query masks follow their queries (a shared mask stays as it is).
-    const uint32_t* m1 = dmask;
-    if (dmask && mask_ld) {
-      fmask.reserve(nq * mask_ld * sizeof(uint32_t), 0, stream);
-      uint32_t* g1 = static_cast<uint32_t*>(fmask.get());
-      VSG_CUDA(vsg::launch_gather_rows(reinterpret_cast<float*>(g1), reinterpret_cast<const float*>(dmask), mask_ld,
-                                       uint32_t(mask_ld), d_list, uint32_t(nq), s, d_count));
-      ++kernel_launches;
-      m1 = g1;
-    }
+    const uint32_t* m1 = dmask && mask_ld ? static_cast<const uint32_t*>(fmask.get()) : dmask;
     // The scan kernel's masked full scan (its gather mode gives the same results); not profiled.
     const bool prof = profiling;
     profiling = false;
     try {
-      enqueue(q1, dp, nq, k, m1, dmask && mask_ld, mask_ld, false, oi1, od1, s, VSG_METHOD_SKINNY, -1.0, d_count);
+      enqueue(static_cast<const float*>(fq.get()), dp, nq, k, m1, dmask && mask_ld, mask_ld, false, out_ids,
+              out_dists, s, VSG_METHOD_SKINNY, -1.0, d_count, d_list, !prof);
     } catch (...) {
       profiling = prof;
       throw;
     }
     profiling = prof;
-    VSG_CUDA(vsg::launch_scatter_results(out_ids, out_dists, oi1, od1, uint32_t(k), d_list, uint32_t(nq), s, d_count,
-                                         static_cast<unsigned long long*>(tcstats.get())));
-    ++kernel_launches;
   }
 
   // Queries of the certified path that the scan kernel answered (waits for the index's work).
@@ -632,7 +646,7 @@ struct vsg_index {
 
   bool use_tc_exact(uint32_t method, size_t nq, size_t k, const uint32_t* dmask, bool gather,
                     double allowed = -1.0) const {
-    if (k > size_t(vsg::kTcMaxShortlist) || n == 0) return false;
+    if (k > size_t(vsg::kTcMaxShortlist) || k > VSG_MAX_K || n == 0) return false;
     if (method == VSG_METHOD_TC_EXACT) return true;
     if (method != VSG_METHOD_AUTO) return false;
     // Filtered: the gather scan reads only the allowed rows of each query, about 3.3 us per query
@@ -649,7 +663,6 @@ struct vsg_index {
     }
     if (force_kernel >= 0) return force_kernel == 2;
     if (const TuneEntry* e = lookup(tune_plain, nq)) return e->kernel == 2;
-    if (k > 32) return false;
     // Large batches amortise the shortlist path's fixed costs at any index size; smaller ones,
     // down to one query, when the index is large enough that reading half the bytes (the bf16
     // copy instead of the FP32 rows) saves more than those costs (about 30 us).
@@ -675,7 +688,7 @@ struct vsg_index {
     if (n == 0) throw std::invalid_argument("the index is empty");
     if (k == 0 || k > VSG_MAX_K) throw std::invalid_argument("k must be in [1, 128]");
     if (family == VSG_METHOD_BF16) {
-      if (k > size_t(vsg::kTcMaxShortlist)) throw std::invalid_argument("k must be <= 120 for the bf16 path");
+      if (k > size_t(vsg::kTcMaxShortlist)) throw std::invalid_argument("k is above the bf16 path's shortlist");
       ensure_bf16();
     }
     size_t bmax = 0;
@@ -777,10 +790,13 @@ struct vsg_index {
 
   // allowed: the largest allowed fraction of the masks when known (host masks), else -1.
   // nq_dev: scan path only, a device count of the queries to search (at most nq).
+  // out_map (with nq_dev): query j's results go to row out_map[j] of the outputs. pdl: the scan
+  // is launched as a dependent of the kernel before it (the certified path's finish kernel).
   void enqueue(const float* dq, size_t ldq, size_t nq, size_t k, const uint32_t* dmask, bool per_query,
                size_t mask_ld, bool gather, uint32_t* out_ids, float* out_dists, cudaStream_t s,
-               uint32_t method = VSG_METHOD_AUTO, double allowed = -1.0, const uint32_t* nq_dev = nullptr) {
-    // The shortlist holds at most 120 rows per query: larger k runs the exact FP32 kernels.
+               uint32_t method = VSG_METHOD_AUTO, double allowed = -1.0, const uint32_t* nq_dev = nullptr,
+               const uint32_t* out_map = nullptr, bool pdl = false) {
+    // (A shortlist holds at most kTcMaxShortlist rows per query, which every k <= 128 fits.)
     const size_t mld = dmask && per_query ? mask_ld : 0;  // 0: one mask for every query
     if ((method == VSG_METHOD_BF16 || method == VSG_METHOD_FP8) && k <= size_t(vsg::kTcMaxShortlist)) {
       enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, false, 0, method == VSG_METHOD_FP8, dmask, mld);
@@ -819,6 +835,8 @@ struct vsg_index {
     a.nsplit = p.nsplit;
     a.stages = p.stages;
     a.gather = gather ? 1u : 0u;
+    a.wait_ns = wait_ns();
+    a.stall = stall_next ? 1u : 0u;
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     // The last CTA of each query block merges the splits in the scan kernel itself.
@@ -827,7 +845,8 @@ struct vsg_index {
     a.out_d = out_dists;
     a.out_i = out_ids;
     a.nq_dev = nq_dev;
-    VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s));
+    a.out_map = out_map;
+    VSG_CUDA(vsg::launch_scan(p.shape, a, dim3(p.nqb, p.nsplit), s, pdl));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
@@ -930,7 +949,13 @@ struct vsg_index {
     uint32_t* di = res_ids();
     float* dd = res_dists(nq, k);
     if (method == VSG_METHOD_BF16 && !dm && k <= size_t(vsg::kTcMaxShortlist)) ensure_bf16();
-    enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method, allowed);
+    try {
+      enqueue(dq, dp, nq, k, dm, per_query, mask_ld, gather, di, dd, stream, method, allowed);
+    } catch (...) {
+      stall_next = false;
+      throw;
+    }
+    stall_next = false;  // the test hook covers one search
     const size_t bytes = 16 + nq * k * 8;
     pin_out.reserve(bytes);
     VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), bytes, cudaMemcpyDeviceToHost, stream));

@@ -73,12 +73,18 @@ extern "C" int vsg_search_rows_noalloc(const float* d_rows, size_t n, size_t dim
   if (metric != VSG_METRIC_L2 && metric != VSG_METRIC_IP) return fail(VSG_ERR_INVALID, "unknown metric");
   if (k > VSG_MAX_K) return fail(VSG_ERR_INVALID, "k must be <= " + std::to_string(VSG_MAX_K));
   if (nq == 0 || k == 0) return VSG_OK;
-  if (n == 0) return fail(VSG_ERR_INVALID, "n must be > 0");
   if (n >= VSG_NONE) return fail(VSG_ERR_LENGTH, "at most 2^32 - 2 rows");
   if (dim == 0 || dim % 4 != 0) return fail(VSG_ERR_INVALID, "dim must be a positive multiple of 4");
-  if (!d_rows || !d_queries || !d_out_ids || !d_out_dists) return fail(VSG_ERR_INVALID, "NULL pointer");
+  if (!d_queries || !d_out_ids || !d_out_dists || (n && !d_rows)) return fail(VSG_ERR_INVALID, "NULL pointer");
   if (reinterpret_cast<uintptr_t>(d_rows) % 16 || reinterpret_cast<uintptr_t>(d_queries) % 16)
     return fail(VSG_ERR_INVALID, "rows and queries must be 16-byte aligned");
+  if (n == 0) {  // no rows: every result is missing (VSG_NONE / +inf), as vsg_search fills it
+    cudaStream_t s0 = static_cast<cudaStream_t>(stream);
+    cudaError_t e0 = vsg::launch_fill_missing(d_out_dists, d_out_ids, nq * k, s0);
+    if (e0 == cudaSuccess) e0 = cudaStreamSynchronize(s0);
+    if (e0 != cudaSuccess) return fail(VSG_ERR_CUDA, std::string("fill: ") + cudaGetErrorString(e0));
+    return VSG_OK;
+  }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(VSG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));

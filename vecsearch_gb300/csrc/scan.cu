@@ -24,6 +24,7 @@
 #include <mutex>
 
 #include "device_common.cuh"
+#include "launch.cuh"
 #include "scan.cuh"
 
 namespace vsg {
@@ -79,7 +80,14 @@ __device__ __forceinline__ float acc4(const float4 q, const float4 x, float a) {
 template <int QB>
 __device__ __forceinline__ uint32_t block_bits(const ScanArgs& a, uint32_t qbase, uint32_t w, uint32_t row_end) {
   uint32_t bits = 0;
-  if (a.mask_ld == 0) {
+  if (a.mask_ptrs) {  // per-query pointers; no filter (nullptr) allows every row
+#pragma unroll
+    for (int b = 0; b < QB; ++b)
+      if (qbase + b < a.nq) {
+        const uint32_t* p = a.mask_ptrs[qbase + b];
+        bits |= p ? __ldg(p + w) : 0xFFFFFFFFu;
+      }
+  } else if (a.mask_ld == 0) {
     bits = __ldg(a.mask + w);
   } else {
 #pragma unroll
@@ -131,7 +139,8 @@ __device__ __forceinline__ void scan_epilogue(const ScanArgs& a, const SmemLayou
   __syncthreads();
   if (!last_cta) return;
   __threadfence();
-  const uint32_t nvalid = min(uint32_t(QB), a.nq - qbase);
+  const uint32_t nlive = a.nq_dev ? min(a.nq, *a.nq_dev) : a.nq;  // qbase < nlive (checked at the start)
+  const uint32_t nvalid = min(uint32_t(QB), nlive - qbase);
   // Stage split lists in the ring, one query at a time, in rounds that fit (the ring holds at
   // least 512 entries; k <= 128).
   const size_t ring_entries = (L.ld_off - L.ring_off) / (2 * sizeof(float));
@@ -162,7 +171,8 @@ __device__ __forceinline__ void scan_epilogue(const ScanArgs& a, const SmemLayou
     acc.load(lst_d + size_t(b) * k, lst_i + size_t(b) * k, int(k), lane);
     warp_merge_lists<E>(acc, lst_d + size_t(QB + b) * k, lst_i + size_t(QB + b) * k, kScanWarps - 1,
                         size_t(QB) * k, int(k), lane);
-    acc.store(a.out_d + size_t(qbase + b) * k, a.out_i + size_t(qbase + b) * k, int(k), lane);
+    const size_t row = a.out_map ? size_t(a.out_map[qbase + b]) : size_t(qbase + b);
+    acc.store(a.out_d + row * k, a.out_i + row * k, int(k), lane);
   }
   if (tid == 0) a.counters[blockIdx.x] = 0;  // ready for the next launch
 }
@@ -190,6 +200,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t qbase = blockIdx.x * QB;
+  pdl_trigger();
+  pdl_wait();
   // A count read on the device: whole query blocks past it leave before touching anything (the
   // fused merge's counter of such a block is never used).
   if (a.nq_dev && qbase >= *a.nq_dev) return;
@@ -204,11 +216,14 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
   // allowed rows from the filter bits and copies only those.
   const bool gather = a.mask != nullptr && a.gather != 0;
 
+  const unsigned long long wl = a.wait_ns ? a.wait_ns : kWaitLimitNs;
+  const bool stall = a.stall != 0 && stages < uint32_t(kMaxStages);
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kScanWarps);
     }
+    if (stall) mbar_init(&full[kMaxStages - 1], 1);  // nothing ever arrives on it
     mbar_fence_init();
   }
   {  // queries of the block (rows >= nq become zeros), and empty lists
@@ -246,8 +261,8 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
       if (lane == 0) {
         for (uint32_t t = 0; t < ntiles; ++t) {
           const uint32_t r0 = row_begin + t * R;
-          if (a.mask && tile_filtered_out<QB, R>(a, qbase, r0, row_end)) continue;
-          if (!mbar_wait(&empty[s], ph ^ 1)) {
+          if ((a.mask || a.mask_ptrs) && tile_filtered_out<QB, R>(a, qbase, r0, row_end)) continue;
+          if (!mbar_wait(&empty[s], ph ^ 1, wl)) {
             ok = false;
             break;
           }
@@ -286,7 +301,7 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
       };
       auto open_slot = [&]() -> bool {
         bool got = true;
-        if (lane == 0) got = mbar_wait(&empty[s], ph ^ 1);
+        if (lane == 0) got = mbar_wait(&empty[s], ph ^ 1, wl);
         return __shfl_sync(kFull, got ? 1 : 0, 0) != 0;
       };
       const uint32_t wend = (row_end >> 5) + ((row_end & 31u) != 0u);
@@ -357,12 +372,18 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
     const uint32_t lrow = uint32_t(warp * RW + vr);  // the finished value's row within a tile
     // A masked full scan checks every pair; gather slots hold only allowed rows, but for
     // per-query masks with QB > 1 they hold the block's union.
-    const bool check_bits = a.mask != nullptr && (!gather || (a.mask_ld != 0 && QB > 1));
+    const bool check_bits = (a.mask != nullptr && (!gather || (a.mask_ld != 0 && QB > 1))) || a.mask_ptrs != nullptr;
     uint32_t s = 0, ph = 0;
-    for (uint32_t t = 0; gather || t < ntiles; ++t) {
-      if (!gather && a.mask && tile_filtered_out<QB, R>(a, qbase, row_begin + t * R, row_end)) continue;
+    bool live = true;
+    if (stall && !__all_sync(kFull, mbar_wait(&full[kMaxStages - 1], 0, wl))) {  // the test hook's wait
+      if (lane == 0) atomicExch(a.status, kDevTimeout);
+      live = false;
+    }
+    for (uint32_t t = 0; live && (gather || t < ntiles); ++t) {
+      if (!gather && (a.mask || a.mask_ptrs) && tile_filtered_out<QB, R>(a, qbase, row_begin + t * R, row_end))
+        continue;
       // warp-uniform decision, so no lane leaves while the others shuffle
-      if (!__all_sync(kFull, mbar_wait(&full[s], ph))) {
+      if (!__all_sync(kFull, mbar_wait(&full[s], ph, wl))) {
         if (lane == 0) atomicExch(a.status, kDevTimeout);
         break;
       }
@@ -402,8 +423,10 @@ __global__ void __launch_bounds__(kScanThreads, 1) scan_kernel(const ScanArgs a)
       ReduceScatter<V, 16>::run(acc, lane);
       const float dist = L2 ? acc[0] : 1.0f - acc[0];
       bool pass = owner && lrow < rows && qbase + vb < a.nq;  // padded query slots never compete
-      if (pass && check_bits)
-        pass = (__ldg(a.mask + size_t(qbase + vb) * a.mask_ld + (row >> 5)) >> (row & 31)) & 1u;
+      if (pass && check_bits) {
+        const uint32_t* p = a.mask_ptrs ? a.mask_ptrs[qbase + vb] : a.mask + size_t(qbase + vb) * a.mask_ld;
+        pass = p == nullptr || ((__ldg(p + (row >> 5)) >> (row & 31)) & 1u);
+      }
       if (pass) pass = nb_less(dist, row, my_d[vb * k + k - 1], my_i[vb * k + k - 1]);
       unsigned bal = __ballot_sync(kFull, pass);
       while (bal) {
@@ -490,7 +513,7 @@ __global__ void fill_missing_kernel(float* d, uint32_t* i, size_t count) {
 }
 
 template <int QB, int RW, bool L2>
-cudaError_t launch_one(const ScanArgs& a, dim3 grid, cudaStream_t stream) {
+cudaError_t launch_one(const ScanArgs& a, dim3 grid, cudaStream_t stream, bool launch = true, bool pdl = false) {
   const size_t smem = scan_layout(QB, RW, a.dp, a.k, a.stages).total;
   // Largest dynamic shared-memory size already allowed for this instantiation, per device.
   static std::mutex mu;
@@ -506,21 +529,22 @@ cudaError_t launch_one(const ScanArgs& a, dim3 grid, cudaStream_t stream) {
       if (dev < 64) configured[dev] = smem;
     }
   }
-  scan_kernel<QB, RW, L2><<<grid, kScanThreads, smem, stream>>>(a);
-  return cudaGetLastError();
+  if (!launch) return cudaSuccess;
+  return launch_kernel(scan_kernel<QB, RW, L2>, grid, dim3(kScanThreads), smem, stream, pdl, a);
 }
 
 template <int QB, int RW>
-cudaError_t launch_metric(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st) {
-  return s.l2 ? launch_one<QB, RW, true>(a, grid, st) : launch_one<QB, RW, false>(a, grid, st);
+cudaError_t launch_metric(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st, bool launch, bool pdl) {
+  return s.l2 ? launch_one<QB, RW, true>(a, grid, st, launch, pdl) : launch_one<QB, RW, false>(a, grid, st, launch, pdl);
 }
 
 template <int QB>
-cudaError_t launch_rw(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st) {
+cudaError_t launch_rw(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t st, bool launch = true,
+                      bool pdl = false) {
   switch (s.rw) {
-    case 1: return launch_metric<QB, 1>(s, a, grid, st);
-    case 2: return launch_metric<QB, 2>(s, a, grid, st);
-    default: return launch_metric<QB, 4>(s, a, grid, st);
+    case 1: return launch_metric<QB, 1>(s, a, grid, st, launch, pdl);
+    case 2: return launch_metric<QB, 2>(s, a, grid, st, launch, pdl);
+    default: return launch_metric<QB, 4>(s, a, grid, st, launch, pdl);
   }
 }
 
@@ -530,12 +554,25 @@ size_t scan_smem_bytes(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t sta
   return scan_layout(s.qb, s.rw, dp, k, stages).total;
 }
 
-cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream) {
+cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream, bool pdl) {
   switch (s.qb) {
-    case 1: return launch_rw<1>(s, a, grid, stream);
-    case 2: return launch_rw<2>(s, a, grid, stream);
-    case 4: return launch_rw<4>(s, a, grid, stream);
-    default: return launch_rw<8>(s, a, grid, stream);
+    case 1: return launch_rw<1>(s, a, grid, stream, true, pdl);
+    case 2: return launch_rw<2>(s, a, grid, stream, true, pdl);
+    case 4: return launch_rw<4>(s, a, grid, stream, true, pdl);
+    default: return launch_rw<8>(s, a, grid, stream, true, pdl);
+  }
+}
+
+cudaError_t scan_prepare(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t stages) {
+  ScanArgs a{};
+  a.dp = dp;
+  a.k = k;
+  a.stages = stages;
+  switch (s.qb) {
+    case 1: return launch_rw<1>(s, a, dim3(1), nullptr, false);
+    case 2: return launch_rw<2>(s, a, dim3(1), nullptr, false);
+    case 4: return launch_rw<4>(s, a, dim3(1), nullptr, false);
+    default: return launch_rw<8>(s, a, dim3(1), nullptr, false);
   }
 }
 

@@ -14,7 +14,7 @@ constexpr int kMaxStages = 8;
 // One fused pass: distances of a block of QB queries against a row range, the
 // filter applied per (query, row), and each warp's running top-k.
 struct ScanArgs {
-  const float* x;          // base rows, n x dp floats (dp = padded dim, multiple of 8)
+  const float* x;          // base rows, n x dp floats (dp: a multiple of 4; the index pads to 8)
   const float* q;          // queries, row stride ldq floats; rows >= nq are never read
   const uint32_t* mask;    // nullptr, or allow-bits: bit (r & 31) of word (r >> 5)
   uint64_t mask_ld;        // words between two queries' masks; 0 = one mask for all queries
@@ -35,6 +35,18 @@ struct ScanArgs {
   // Optional: the number of queries to search, read on the device (at most nq); the launch is
   // sized for nq and query blocks past the count return at once.
   const uint32_t* nq_dev;
+  // Optional, instead of mask: one device pointer per query to its allow-bits, nullptr for a query
+  // without a filter (a masked full scan: gather must be 0).
+  const uint32_t* const* mask_ptrs;
+  // Optional, with the fused merge: query j's final list goes to row out_map[j] of out_d / out_i
+  // instead of row j (with nq_dev set, only queries j < *nq_dev are written).
+  const uint32_t* out_map;
+  // Limit of one wait on another role, in ns (0: 2 s). The waits that drain the CTA's own copies
+  // before it exits always take 2 s.
+  uint64_t wait_ns;
+  // Test hook: 1 makes the consumer warps first wait on a barrier nothing completes, so that wait
+  // runs out after wait_ns and the kernel winds down with kDevTimeout (needs stages < kMaxStages).
+  uint32_t stall;
 };
 
 struct MergeArgs {
@@ -69,7 +81,12 @@ struct ScanShape {
 // Shared-memory bytes the scan kernel needs for a shape, dim and k with `stages` ring slots.
 size_t scan_smem_bytes(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t stages);
 
-cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream);
+// pdl: launched as a programmatic dependent of the previous kernel in the stream (the kernel
+// waits for it before reading anything).
+cudaError_t launch_scan(const ScanShape& s, const ScanArgs& a, dim3 grid, cudaStream_t stream, bool pdl = false);
+// Sets the scan kernel's shared-memory limit for (shape, dp, k, stages) without launching, for a
+// launch that is then captured into a CUDA graph.
+cudaError_t scan_prepare(const ScanShape& s, uint32_t dp, uint32_t k, uint32_t stages);
 cudaError_t launch_merge(const MergeArgs& m, cudaStream_t stream);
 cudaError_t launch_fill_missing(float* out_d, uint32_t* out_i, size_t count, cudaStream_t stream);
 

@@ -1,13 +1,17 @@
-// Serving loop: continuous batching over the tensor-core shortlist path.
+// Serving loop: continuous batching over the certified tensor-core path (exact results).
 //
 // The reference serves queries one call at a time (python/bindings.cpp:165-186; its gRPC shard
 // worker, distributed/shard_worker.py:26-36, calls the index per request). Here a worker thread
 // keeps requests of any size, k and filter flowing onto the GPU:
 //   * a request (host queries, k, optional allow-bits, host outputs) is queued by submit();
 //   * each slot owns device and pinned buffers sized for `max_batch` queries and a CUDA graph
-//     captured once: queries -> bf16, reset of the work counter, the persistent shortlist kernel
-//     (one CTA per SM claiming (query block, split) items; per-query k' and filter), and the
-//     fused merge + exact FP32 rerank kernel;
+//     captured once: the query preparation (bf16 queries, norms, certificate bounds E and
+//     margins), reset of the work counter, the sample pass and its select, the persistent
+//     shortlist kernel (one CTA per SM claiming (query block, split) items; per-query k, k',
+//     margin and filter), the finish kernel (cut, exact FP32 rerank, certificate; it hands each
+//     query it could not certify, with its filter, to the fallback), the FP32 scan kernel
+//     launched on the device's count of those queries, and their results scattered into place.
+//     So every served result equals the FP32 scan's (method skinny) bit for bit;
 //   * the worker admits queued requests into every free slot as soon as it frees (up to the
 //     slot's query and filter capacity), copies the micro-batch in, launches the graph and the
 //     copies out on the slot's stream, and completes requests when the slot's event fires. So
@@ -15,7 +19,7 @@
 //     copies and kernels overlap on the device;
 //   * the number of slots is bounded by free HBM at creation (half of it at most).
 // A request's result does not depend on the other requests in its micro-batch: every query's
-// scores, shortlist and rerank are computed independently (bitwise).
+// scores, shortlist, rerank, certificate and fallback scan are computed independently (bitwise).
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -53,6 +57,9 @@ struct Slot {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   DeviceBuffer d_in, d_qb, d_qn, d_part, d_out, d_sample, d_thr, d_cbuf, d_gthr;
+  // certified path: margins then bounds E; [uncertified count | their indices]; the fallback
+  // scan's queries, filter pointers, split lists, results and fused-merge counters
+  DeviceBuffer d_margin, d_fails, d_fq, d_mptr, d_spart, d_fout, d_counters;
   PinnedBuffer h_in, h_out;
   CUtensorMap qmap{};
   std::vector<Request*> reqs;
@@ -78,12 +85,10 @@ struct vsg_server {
   std::thread worker;
   bool stop = false;
   uint64_t next_ticket = 1;
-  uint64_t n_batches = 0, n_queries = 0, n_requests = 0;
+  uint64_t n_batches = 0, n_queries = 0, n_requests = 0, n_uncertified = 0;
+  vsg_index::Plan fb;  // the fallback scan's plan: cap_q queries, rows split as for a few
 
-  uint32_t shortlist(uint32_t k) const {
-    const double want = std::max<double>(double(k), idx->shortlist_oversample * double(k));
-    return uint32_t(std::min<double>(double(kp_max), std::ceil(want)));
-  }
+  uint32_t shortlist(uint32_t k) const { return vsg_index::exact_shortlist_size(k); }
 
   void build_slot(Slot& s) {
     VSG_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
@@ -93,9 +98,9 @@ struct vsg_server {
     std::memset(s.h_in.get(), 0, in_bytes);
     s.d_qb.reserve(cap_q * idx->dp * 2, 0, s.stream);
     s.d_qn.reserve(cap_q * sizeof(float), 0, s.stream);
-    // split lists: at most max(cap_q, 128 * SMs) (query, split) pairs of kp_max entries
+    // split lists and their lengths: at most max(cap_q, 128 * SMs) (query, split) pairs of kp_max
     const size_t pairs = std::max(cap_q, size_t(vsg::kTcQueries) * size_t(idx->sms));
-    s.d_part.reserve(pairs * kp_max * 8, 0, s.stream);
+    s.d_part.reserve(pairs * kp_max * 8 + pairs * 4, 0, s.stream);
     s.d_out.reserve(out_k * 8 + 16, 0, s.stream);
     // sample pass: per query nsplit * sample_tiles * 128 <= max(kSample + one split's tiles, ...) distances
     s.d_sample.reserve(cap_q * sample_per_query * sizeof(float), 0, s.stream);
@@ -104,6 +109,14 @@ struct vsg_server {
     const size_t cbuf_entries = size_t(idx->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(kp_max));
     s.d_cbuf.reserve(cbuf_entries * 8, 0, s.stream);
     s.d_gthr.reserve(cap_q * sizeof(uint32_t), 0, s.stream);
+    s.d_margin.reserve(2 * cap_q * sizeof(float), 0, s.stream);
+    s.d_fails.reserve((1 + cap_q) * sizeof(uint32_t), 0, s.stream);
+    s.d_fq.reserve(cap_q * idx->dp * sizeof(float), 0, s.stream);
+    s.d_mptr.reserve(cap_q * sizeof(const uint32_t*), 0, s.stream);
+    const size_t sparts = cap_q * size_t(fb.nsplit) * max_k;
+    s.d_spart.reserve(sparts * 8, 0, s.stream);
+    s.d_fout.reserve(cap_q * max_k * 8, 0, s.stream);
+    s.d_counters.reserve(size_t(fb.nqb) * sizeof(uint32_t), 0, s.stream);  // zero: the scan keeps them so
     s.h_out.reserve(out_k * 8 + 16);
     char* din = static_cast<char*>(s.d_in.get());
     auto* hdr = reinterpret_cast<vsg::ServeHeader*>(din);
@@ -113,13 +126,16 @@ struct vsg_server {
     float* out_d = static_cast<float*>(s.d_out.get());
     uint32_t* out_i = reinterpret_cast<uint32_t*>(out_d + out_k);
     int* status = reinterpret_cast<int*>(out_i + out_k);
+    float* margin = static_cast<float*>(s.d_margin.get());
+    uint32_t* fails = static_cast<uint32_t*>(s.d_fails.get());
+    const bool l2 = idx->metric == VSG_METRIC_L2;
     vsg::TcArgs a{};
     a.n = uint32_t(idx->n);
     a.dp = uint32_t(idx->dp);
     a.kp = uint32_t(kp_max);
     a.stages = uint32_t(stages);
     a.resident = resident;
-    a.l2 = idx->metric == VSG_METRIC_L2 ? 1u : 0u;
+    a.l2 = l2 ? 1u : 0u;
     a.cbuf_d = static_cast<float*>(s.d_cbuf.get());
     a.cbuf_i = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_cbuf.get()) + cbuf_entries * 4);
     a.gthr = static_cast<uint32_t*>(s.d_gthr.get());
@@ -127,28 +143,84 @@ struct vsg_server {
     a.qnorm = static_cast<const float*>(s.d_qn.get());
     a.part_d = static_cast<float*>(s.d_part.get());
     a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_part.get()) + pairs * kp_max * 4);
+    a.part_n = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_part.get()) + pairs * kp_max * 8);
     a.status = status;
     a.hdr = hdr;
     a.sq = sq;
-    vsg::ServeFinishArgs f{hdr, sq, a.part_d, a.part_i, static_cast<const float*>(idx->x.get()), dq, out_d, out_i,
-                           uint32_t(idx->dp), uint32_t(kp_max), a.l2};
-    VSG_CUDA(vsg::tc_prepare(a.stages, vsg::tc_chunks(a.dp, false), a.resident, a.l2 != 0, false));  // before capture
+    a.margin = margin;  // each query keeps the rows within its margin of its k-th best
+    vsg::FinishArgs f{};
+    f.part_d = a.part_d;
+    f.part_i = a.part_i;
+    f.part_n = a.part_n;
+    f.kp = uint32_t(kp_max);
+    f.margin = margin;
+    f.x = static_cast<const float*>(idx->x.get());
+    f.n = uint32_t(idx->n);
+    f.q = dq;
+    f.dp = uint32_t(idx->dp);
+    f.ldq = uint32_t(idx->dp);
+    f.l2 = a.l2;
+    f.out_d = out_d;
+    f.out_i = out_i;
+    f.thr_init = static_cast<const float*>(s.d_thr.get());
+    f.gthr = a.gthr;
+    f.err = margin + cap_q;
+    f.fail_count = fails;
+    f.fail_list = fails + 1;
+    f.status = status;
+    f.hdr = hdr;
+    f.sq = sq;
+    f.stage_cap = 4096;  // more entries: the finish kernel reads the lists in global memory
+    f.fq = static_cast<float*>(s.d_fq.get());  // uncertified queries' rows and filters, for the scan
+    f.fmask_ptrs = static_cast<const uint32_t**>(s.d_mptr.get());
+    // The fallback scan: gathered queries, their filters by pointer, cap_q queries of which only
+    // the device's uncertified count run; the fused merge writes max_k results per query.
+    vsg::ScanArgs sc{};
+    sc.x = static_cast<const float*>(idx->x.get());
+    sc.q = static_cast<const float*>(s.d_fq.get());
+    sc.ldq = uint32_t(idx->dp);
+    sc.mask_ptrs = static_cast<const uint32_t* const*>(s.d_mptr.get());
+    sc.part_d = static_cast<float*>(s.d_spart.get());
+    sc.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(s.d_spart.get()) + sparts * 4);
+    sc.status = status;
+    sc.n = uint32_t(idx->n);
+    sc.dp = uint32_t(idx->dp);
+    sc.nq = uint32_t(cap_q);
+    sc.k = uint32_t(max_k);
+    sc.rows_per_split = fb.rows_per_split;
+    sc.nsplit = fb.nsplit;
+    sc.stages = fb.stages;
+    sc.counters = static_cast<uint32_t*>(s.d_counters.get());
+    float* fout_d = static_cast<float*>(s.d_fout.get());
+    uint32_t* fout_i = reinterpret_cast<uint32_t*>(fout_d + cap_q * max_k);
+    sc.out_d = fout_d;
+    sc.out_i = fout_i;
+    sc.nq_dev = fails;
+    // kernel attributes before capture
+    VSG_CUDA(vsg::tc_prepare(a.stages, vsg::tc_chunks(a.dp, false), a.resident, l2, false));
+    VSG_CUDA(vsg::finish_prepare(f.dp, f.stage_cap));
+    VSG_CUDA(vsg::scan_prepare(fb.shape, sc.dp, sc.k, sc.stages));
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
-    VSG_CUDA(vsg::launch_to_bf16(dq, idx->dp, cap_q, uint32_t(idx->dp), uint32_t(idx->dp), s.d_qb.get(),
-                                 static_cast<float*>(s.d_qn.get()), s.stream));
-    // Sample pass: the head tiles of every split give each query a starting threshold.
+    VSG_CUDA(vsg::launch_prepare_queries(dq, uint32_t(idx->dp), uint32_t(cap_q), uint32_t(idx->dp), uint32_t(idx->dp),
+                                         s.d_qb.get(), static_cast<float*>(s.d_qn.get()), a.gthr,
+                                         static_cast<const float*>(idx->xbound.get()), l2, float(idx->cert_margin),
+                                         margin, margin + cap_q, fails, s.stream));
+    // Sample pass: the head tiles of every split give each query a starting threshold (its k-th
+    // best sampled distance plus its margin).
     vsg::TcArgs sa = a;
     sa.dump = static_cast<float*>(s.d_sample.get());
     sa.gthr = nullptr;
     VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
     VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, sa, unsigned(idx->sms), s.stream));
     VSG_CUDA(vsg::launch_serve_select(hdr, sq, sa.dump, static_cast<float*>(s.d_thr.get()), uint32_t(cap_q),
-                                      s.stream));
+                                      s.stream, margin));
     a.thr_init = static_cast<const float*>(s.d_thr.get());
     VSG_CUDA(cudaMemsetAsync(&hdr->next, 0, sizeof(uint32_t), s.stream));
-    VSG_CUDA(cudaMemsetAsync(a.gthr, 0xFF, cap_q * sizeof(uint32_t), s.stream));
     VSG_CUDA(vsg::launch_tc_shortlist(s.qmap, idx->xmap, a, unsigned(idx->sms), s.stream));
-    VSG_CUDA(vsg::launch_serve_finish(f, uint32_t(cap_q), s.stream));
+    VSG_CUDA(vsg::launch_finish(f, uint32_t(cap_q), s.stream));
+    VSG_CUDA(vsg::launch_scan(fb.shape, sc, dim3(fb.nqb, fb.nsplit), s.stream));
+    VSG_CUDA(vsg::launch_serve_scatter(fails, fails + 1, sq, fout_d, fout_i, uint32_t(max_k), out_d, out_i, nullptr,
+                                       uint32_t(cap_q), s.stream));
     VSG_CUDA(cudaStreamEndCapture(s.stream, &s.graph));
     VSG_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
   }
@@ -223,6 +295,8 @@ struct vsg_server {
       e = cudaMemcpyAsync(hout + out_k * 4, dout + out_k * 4, size_t(out) * 4, cudaMemcpyDeviceToHost, s.stream);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(hout + out_k * 8, dout + out_k * 8, sizeof(int), cudaMemcpyDeviceToHost, s.stream);
+    if (e == cudaSuccess)  // the certified path's uncertified count of this micro-batch
+      e = cudaMemcpyAsync(hout + out_k * 8 + 4, s.d_fails.get(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
     if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -248,7 +322,9 @@ struct vsg_server {
     const float* od = reinterpret_cast<const float*>(hout);
     const uint32_t* oi = reinterpret_cast<const uint32_t*>(hout + out_k * 4);
     int st = 0;
+    uint32_t unproven = 0;
     std::memcpy(&st, hout + out_k * 8, sizeof(int));
+    std::memcpy(&unproven, hout + out_k * 8 + 4, sizeof(uint32_t));
     uint32_t off = 0;
     const auto now = Clock::now();
     for (Request* r : s.reqs) {
@@ -259,10 +335,11 @@ struct vsg_server {
       }
       off += uint32_t(cnt);
     }
-    if (st != 0) {  // a kernel gave up on a wait: clear the status word before the slot is reused
-      int zero = 0;
+    if (st != 0) {  // a kernel gave up on a wait: clear the status word and the fallback scan's
+                    // merge counters before the slot is reused
       char* dout = static_cast<char*>(s.d_out.get());
-      cudaMemcpyAsync(dout + out_k * 8, &zero, sizeof(int), cudaMemcpyHostToDevice, s.stream);
+      cudaMemsetAsync(dout + out_k * 8, 0, sizeof(int), s.stream);
+      cudaMemsetAsync(s.d_counters.get(), 0, s.d_counters.bytes(), s.stream);
       cudaStreamSynchronize(s.stream);
     }
     std::lock_guard<std::mutex> g(mu);
@@ -272,6 +349,7 @@ struct vsg_server {
       r->t_done = now;
     }
     n_batches += 1;
+    if (st == 0) n_uncertified += unproven;
     s.reqs.clear();
     s.busy = false;
     cv_done.notify_all();
@@ -348,8 +426,8 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
   vsg::set_last_error("");
   try {
     if (max_batch == 0 || slots == 0) throw std::invalid_argument("max_batch and slots must be > 0");
-    if (max_k == 0 || max_k > size_t(vsg::kTcMaxShortlist))
-      throw std::invalid_argument("max_k must be in [1, " + std::to_string(vsg::kTcMaxShortlist) + "]");
+    if (max_k == 0 || max_k > size_t(VSG_MAX_K))
+      throw std::invalid_argument("max_k must be in [1, " + std::to_string(VSG_MAX_K) + "]");
     std::unique_ptr<vsg_server> s(new vsg_server());
     s->idx = h;
     {
@@ -358,12 +436,13 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
       VSG_CUDA(cudaSetDevice(h->device));
       h->ensure_bf16();
       h->ensure_xmap();
+      // the fallback scan of uncertified queries: rows split as for a few queries
+      s->fb = h->plan(max_batch, max_k, false, false, std::max<size_t>(1, size_t(h->fallback_split_queries)));
     }
     s->cap_q = max_batch;
     s->cap_masks = std::min<size_t>(max_batch, 128);
     s->max_k = max_k;
-    s->kp_max = std::min<size_t>(vsg::kTcMaxShortlist, size_t(std::ceil(std::max<double>(
-                                                           double(max_k), h->shortlist_oversample * double(max_k)))));
+    s->kp_max = vsg_index::exact_shortlist_size(max_k);
     s->stages = vsg::tc_pick_stages(vsg::tc_chunks(uint32_t(h->dp), false), h->smem_optin - 1024, &s->resident,
                                     h->metric == VSG_METRIC_L2, false);
     if (s->stages < 2) throw std::invalid_argument("shortlist does not fit the tensor-core kernel's shared memory");
@@ -377,9 +456,12 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     s->sample_per_query = kSampleRows + size_t(vsg::kTcRows) * size_t(h->sms);
     // Admission by free HBM: each slot's workspace is fixed; use at most half of what is free.
     const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms));
-    const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * s->kp_max * 8 +
+    const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * (s->kp_max * 8 + 4) +
                             s->out_k * 8 + 16 + max_batch * (s->sample_per_query + 2) * sizeof(float) +
-                            size_t(h->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(s->kp_max)) * 8;
+                            size_t(h->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(s->kp_max)) * 8 +
+                            max_batch * (3 * sizeof(float) + sizeof(uint32_t) + sizeof(void*)) +  // margins, E, fails
+                            max_batch * h->dp * sizeof(float) +                                    // fallback queries
+                            max_batch * max_k * 8 * (size_t(s->fb.nsplit) + 1) + size_t(s->fb.nqb) * 4;
     size_t free_b = 0, total_b = 0;
     VSG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const size_t fit = (free_b / 2) / std::max<size_t>(per_slot, 1);
@@ -454,6 +536,13 @@ int vsg_server_stats(vsg_server* s, uint64_t* batches, uint64_t* queries, uint64
   if (queries) *queries = s->n_queries;
   if (requests) *requests = s->n_requests;
   if (slots) *slots = s->slots.size();
+  return VSG_OK;
+}
+
+int vsg_server_uncertified(vsg_server* s, uint64_t* queries) {
+  if (!s || !queries) return sfail(VSG_ERR_INVALID, "server or output is NULL");
+  std::lock_guard<std::mutex> g(s->mu);
+  *queries = s->n_uncertified;
   return VSG_OK;
 }
 

@@ -34,6 +34,7 @@
 #include <mutex>
 
 #include "device_common.cuh"
+#include "launch.cuh"
 #include "tc.cuh"
 
 namespace vsg {
@@ -71,7 +72,9 @@ __host__ __device__ inline TcLayout tc_layout(uint32_t stages, uint32_t nkc, boo
 
 // Candidate-buffer capacity per query: the kp kept entries plus room for many appends between
 // compactions (one is due when the next 32 scores might not fit). The warp sort holds 32 E = cap.
-__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) { return kp <= 16 ? 64 : kp <= 48 ? 128 : 256; }
+__host__ __device__ inline uint32_t tc_capacity(uint32_t kp) {
+  return kp <= 16 ? 64 : kp <= 48 ? 128 : kp <= 120 ? 256 : 512;
+}
 
 // Element offset of (row, column c) in a tile-major operand copy with nkc chunks of ce elements
 // (64 bf16 or 128 e4m3) per row.
@@ -196,6 +199,10 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
       keep = compact_query<1>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     else if (E > 2 && n <= 64)
       keep = compact_query<(E > 2 ? 2 : E)>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
+    else if (E > 4 && n <= 128)
+      keep = compact_query<(E > 4 ? 4 : E)>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
+    else if (E > 8 && n <= 256)
+      keep = compact_query<(E > 8 ? 8 : E)>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     else
       keep = compact_query<E>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     if (lane == src) {
@@ -348,6 +355,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* aempty = afull + 1;            // ... and no MMA reads it any more
   uint64_t* done = aempty + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* stall_bar = done + 2;  // after the TMEM slot word; within the 256 bytes of barriers
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool persistent = a.hdr != nullptr;
@@ -373,6 +381,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     mbar_init(afull, 1);
     mbar_init(aempty, 1);
     mbar_init(done, 1);
+    if (a.stall) mbar_init(stall_bar, 1);  // nothing ever arrives on it
     mbar_fence_init();
   }
   if (warp == 1) {
@@ -386,6 +395,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  const unsigned long long wl = a.wait_ns ? a.wait_ns : kWaitLimitNs;
+  pdl_trigger();
+  // Launched as a dependent of the previous kernel: the producer of a non-serving launch with a
+  // resident query block first fills the ring with row chunks (the operand copy of the rows was
+  // written long before), then waits; every other thread waits before the first item.
+  const bool prefetch_rows = !persistent && resident && warp == 0 && lane == 0;
+  bool waited = false;
+  if (!prefetch_rows) {
+    pdl_wait();
+    waited = true;
+  }
 
   // Ring, accumulator and query-block positions carry over from one item to the next; every
   // role walks the same items and tiles in the same order, so they stay in step.
@@ -420,9 +440,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 0) {
       // ---------------- TMA producer ----------------
       if (lane == 0) {
+        // Row chunk c of this item: chunk c % nkc of tile c / nkc (tile-major copy: kTcRows chunk
+        // rows starting at y).
+        const uint32_t nch = ntiles * nkc;
+        auto issue_rows = [&](uint32_t c) {
+          const uint32_t tile = row_begin / kTcRows + c / nkc, kc = c % nkc;
+          const int y = int((tile * nkc + kc) * kTcRows);
+          if (!mbar_wait(&empty[s], ph ^ 1, wl)) {
+            ok = false;
+            return;
+          }
+          unsigned char* st = ring + size_t(s) * L.slot;
+          unsigned char* sb = resident ? st : st + kChunkBytes;
+          mbar_arrive_expect_tx(&full[s], resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes);
+          if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
+          tma_load_2d(sb, &xmap, 0, y, &full[s], stream_policy);
+          pending |= 1u << s;
+          last_ph = (last_ph & ~(1u << s)) | (ph << s);
+          if (++s == stages) {
+            s = 0;
+            ph ^= 1;
+          }
+        };
+        uint32_t c0 = 0;
+        if (!waited) {  // first item: rows before the wait, the query block after it
+          for (const uint32_t pre = min(nch, stages); c0 < pre && ok; ++c0) issue_rows(c0);
+          pdl_wait();
+          waited = true;
+        }
         if (load_a) {
           // The previous block's MMAs have finished before its chunks are overwritten.
-          if (!mbar_wait(aempty, aph ^ 1u)) {
+          if (!mbar_wait(aempty, aph ^ 1u, wl)) {
             ok = false;
           } else {
             mbar_arrive_expect_tx(afull, nkc * kChunkBytes);
@@ -433,46 +481,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             a_last = aph;
           }
         }
-        for (uint32_t t = 0; t < ntiles && ok; ++t) {
-          // Tile-major row copy: chunk kc of this tile is kTcRows chunk rows starting at y.
-          const uint32_t tile = row_begin / kTcRows + t;
-          for (uint32_t kc = 0; kc < nkc; ++kc) {
-            const int y = int((tile * nkc + kc) * kTcRows);
-            if (!mbar_wait(&empty[s], ph ^ 1)) {
-              ok = false;
-              break;
-            }
-            unsigned char* st = ring + size_t(s) * L.slot;
-            unsigned char* sb = resident ? st : st + kChunkBytes;
-            mbar_arrive_expect_tx(&full[s], resident ? kRowChunkBytes : kRowChunkBytes + kChunkBytes);
-            if (!resident) tma_load_2d(st, &qmap, int(kc * kChunkElems), int(qbase), &full[s], keep_policy);
-            tma_load_2d(sb, &xmap, 0, y, &full[s], stream_policy);
-            pending |= 1u << s;
-            last_ph = (last_ph & ~(1u << s)) | (ph << s);
-            if (++s == stages) {
-              s = 0;
-              ph ^= 1;
-            }
-          }
-        }
+        for (uint32_t c = c0; c < nch && ok; ++c) issue_rows(c);
       }
     } else if (warp == 1) {
       // ---------------- MMA issuer ----------------
       if (lane == 0) {
         if (load_a) {
-          if (!mbar_wait(afull, aph)) ok = false;
+          if (!mbar_wait(afull, aph, wl)) ok = false;
           tc_fence_after();
         }
         for (uint32_t t = 0; t < ntiles && ok; ++t, ++tglob) {
           const uint32_t b = tglob & 1, use = tglob >> 1;
-          if (!mbar_wait(&tempty[b], (use & 1) ^ 1)) {
+          if (!mbar_wait(&tempty[b], (use & 1) ^ 1, wl)) {
             ok = false;
             break;
           }
           tc_fence_after();
           const uint32_t d = tmem_base + b * kTcRows;
           for (uint32_t kc = 0; kc < nkc; ++kc) {
-            if (!mbar_wait(&full[s], ph)) {
+            if (!mbar_wait(&full[s], ph, wl)) {
               ok = false;
               break;
             }
@@ -507,13 +534,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t qg = qbase + uint32_t(m);
       const bool qvalid = qg < nq;
       const uint32_t kp = (persistent && qvalid) ? a.sq[qg].kp : a.kp;
+      const uint32_t kk = (persistent && qvalid) ? a.sq[qg].k : a.kk;  // the margin's rank (k)
       const uint32_t* qmask = !qvalid ? nullptr
                               : persistent ? a.sq[qg].mask
                               : a.mask ? a.mask + size_t(qg) * a.mask_ld : nullptr;
       const float qn = (L2 && qvalid) ? a.qnorm[qg] : 0.f;
       const float qsc = (F8 && qvalid) ? a.qscale[qg] : 1.f;  // e4m3 copies: the query's scale
       // Certified path: the margin above the kk-th best beyond which no row is needed (-1: none).
-      const float mg = (!persistent && a.margin && qvalid) ? a.margin[qg] : -1.f;
+      const float mg = (a.margin && qvalid) ? a.margin[qg] : -1.f;
       float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers
       uint32_t* wi = a.cbuf_i + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;
       uint32_t* gq = (a.gthr && qvalid && !a.dump) ? a.gthr + qg : nullptr;
@@ -548,7 +576,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           od = a.part_d + o;
           oi = a.part_i + o;
         }
-        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, a.kk, mg, od, oi, lane);
+        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, kk, mg, od, oi, lane);
         if (mine) {
           cnt = r.keep;
           if (final_list && a.part_n) a.part_n[size_t(qg) * nsplit + split] = r.keep;
@@ -563,11 +591,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       };
       uint32_t gkey = kKeyNone;  // other splits' published k'-th best, loaded one tile ahead
-      for (uint32_t t = 0; t < ntiles; ++t, ++tglob) {
+      if (a.stall && !__all_sync(kFull, mbar_wait(stall_bar, 0, wl))) {  // the test hook's wait
+        if (lane == 0) atomicExch(a.status, kDevTimeout);
+        ok = false;
+      }
+      for (uint32_t t = 0; t < ntiles && ok; ++t, ++tglob) {
         const uint32_t b = tglob & 1, use = tglob >> 1;
         tighten(gkey);
         gkey = gq ? ld_relaxed(gq) : kKeyNone;
-        if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1))) {
+        if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1, wl))) {
           if (lane == 0) atomicExch(a.status, kDevTimeout);
           ok = false;
           break;
@@ -692,6 +724,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (!__syncthreads_and(ok)) break;  // a role gave up: no further items
   }
 
+  if (!waited) pdl_wait();  // a CTA without items still waits before it exits
   if (warp == 0 && lane == 0) {
     // Wait (bounded) until every issued copy has landed before the CTA may exit.
     for (uint32_t i = 0; i < stages; ++i)
@@ -799,25 +832,18 @@ __global__ void midpoint_rows_kernel(float* dst, const float* src, uint32_t dp, 
     dst[size_t(r) * dp + c] = 0.9f * src[size_t(i) * dp + c] + 0.1f * src[size_t(j) * dp + c];
 }
 
-__global__ void gather_rows_kernel(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                                   uint32_t count, const uint32_t* count_dev) {
-  const uint32_t j = blockIdx.x;
-  if (j >= count || (count_dev && j >= *count_dev)) return;
-  const float* s = src + size_t(ids[j]) * ld;
-  for (uint32_t c = threadIdx.x; c < dp; c += blockDim.x) dst[size_t(j) * dp + c] = s[c];
-}
-
-__global__ void scatter_results_kernel(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                       uint32_t k, const uint32_t* ids, uint32_t count, const uint32_t* count_dev,
-                                       unsigned long long* tally) {
-  const uint32_t j = blockIdx.x;
-  const uint32_t cnt = count_dev ? min(count, *count_dev) : count;
+// Serving fallback, after the scan: the first k of slot j's kmax results go to query
+// fail_list[j]'s place in the output block; the count is added to the tally.
+__global__ void serve_scatter_kernel(const uint32_t* count, const uint32_t* fail_list, const ServeQuery* sq,
+                                     const float* src_d, const uint32_t* src_i, uint32_t kmax, float* out_d,
+                                     uint32_t* out_i, unsigned long long* tally) {
+  const uint32_t j = blockIdx.x, cnt = *count;
   if (tally && j == 0 && threadIdx.x == 0) atomicAdd(tally, (unsigned long long)cnt);
   if (j >= cnt) return;
-  const size_t o = size_t(ids[j]) * k;
-  for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
-    dst_i[o + c] = src_i[size_t(j) * k + c];
-    dst_d[o + c] = src_d[size_t(j) * k + c];
+  const ServeQuery s = sq[fail_list[j]];
+  for (uint32_t c = threadIdx.x; c < s.k; c += blockDim.x) {
+    out_d[s.out_off + c] = src_d[size_t(j) * kmax + c];
+    out_i[s.out_off + c] = src_i[size_t(j) * kmax + c];
   }
 }
 
@@ -917,143 +943,318 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
   return mul(e, 1.1f);  // margin over the (already worst-case) terms; 1.1f is above 1.1
 }
 
-// The shortlist path's tail (FinishArgs), one CTA of 256 threads per query.
-constexpr uint32_t kFinishStage = 4096;  // real list entries gathered into shared memory at most
-template <int E, bool L2>
-__global__ void __launch_bounds__(256) finish_kernel(const FinishArgs a) {
-  __shared__ float sd[8][kMaxK];
-  __shared__ uint32_t si[8][kMaxK];
-  __shared__ __align__(16) float stg_d[kFinishStage];  // the staging area, then the query
-  __shared__ uint32_t stg_i[kFinishStage];
-  __shared__ float md[kMaxK];  // the merged list: approximate distances and ids
-  __shared__ uint32_t mi[kMaxK];
-  __shared__ float cd[kMaxK];  // exact distances of its real entries
-  __shared__ uint32_t total;
-  __shared__ float dk;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t q = blockIdx.x, kp = a.kp, k = a.k;
-  const size_t base = size_t(q) * a.nsplit * kp;
-  const float mg = a.margin ? a.margin[q] : -1.f;
-  const int kk = int(k);
-  if (threadIdx.x == 0) {
-    total = 0;
-    dk = __int_as_float(0x7f800000);
+// The shortlist path's tail (FinishArgs), one CTA of kFinishThreads per query.
+//   1. Stage: every split's real list entries (part_n of them) are copied into shared memory when
+//      they fit (stage_cap entries), else the passes below read the lists in global memory.
+//   2. Cut: the `target`-th smallest approximate distance (k with margins, else the shortlist
+//      size k') by exact radix selection on order keys (a min / max pass, then 8-bit rounds below
+//      the highest bit where the keys differ); the cut is that value, plus the margin (rounded
+//      up) on the certified path. Every entry at or below the cut is reranked, at most
+//      kRerankMax: beyond that the cut drops to the entries strictly below the kRerankMax-th.
+//   3. Rerank: the exact FP32 distance of every kept row with the scan kernel's arithmetic (lane
+//      l sums 16-byte chunks l, l + 32, ... in order, then a butterfly over lanes 16 .. 1), so a
+//      candidate set that holds the true top k yields the scan kernel's results bit for bit.
+//   4. The top k by (FP32 dist, id) by rank counting; the k-th FP32 distance D_k.
+//   5. Certificate (fail_count set): every row left out has approximate distance >= L = min(sample
+//      threshold, final shared threshold, the cut when it left entries out); if L - E > D_k
+//      (rounded down) no such row can enter the top k, else the query is listed for the scan.
+// Nothing is read when the status word says a shortlist kernel gave up (its lists may be stale),
+// and row ids at or beyond n are never dereferenced.
+constexpr int kFinishThreads = 512;
+constexpr uint32_t kRerankMax = 1024;
+constexpr uint32_t kKeyAll = 0xFFFFFFFFu;  // cut key that keeps every entry
+
+struct FinishSmem {
+  size_t qs, cd, ci, cx, sd, si, total;  // byte offsets: query, candidates (approx, id, exact), staging
+};
+__host__ __device__ inline FinishSmem finish_smem(uint32_t dp, uint32_t stage_cap) {
+  FinishSmem L;
+  const size_t qbytes = dp <= 4096 ? (size_t(dp) * 4 + 15) / 16 * 16 : 0;
+  L.qs = 0;
+  L.cd = qbytes;
+  L.ci = L.cd + kRerankMax * 4;
+  L.cx = L.ci + kRerankMax * 4;
+  L.sd = L.cx + kRerankMax * 4;
+  L.si = L.sd + size_t(stage_cap) * 4;
+  L.total = L.si + size_t(stage_cap) * 4;
+  return L;
+}
+
+template <bool L2>
+__global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs a) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank;
+  __shared__ float s_dk;
+  pdl_trigger();
+  pdl_wait();
+  const uint32_t q = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int nwarps = kFinishThreads / 32;
+  const bool serving = a.hdr != nullptr;
+  if (serving && q >= a.hdr->nq) return;
+  if (a.status && *reinterpret_cast<const volatile int*>(a.status) != 0) return;  // lists may be stale
+  const uint32_t nsplit = serving ? a.hdr->nsplit : a.nsplit;
+  uint32_t k, sel;
+  size_t out_off;
+  if (serving) {
+    const ServeQuery s = a.sq[q];
+    k = s.k;
+    sel = s.kp;
+    out_off = s.out_off;
+  } else {
+    k = a.k;
+    sel = a.kp;
+    out_off = size_t(q) * a.k;
   }
+  const float mg = a.margin ? a.margin[q] : -1.f;
+  const uint32_t target = mg >= 0.f ? k : sel;
+  const FinishSmem L = finish_smem(a.dp, a.stage_cap);
+  float* qs = reinterpret_cast<float*>(fsm + L.qs);
+  float* cand_d = reinterpret_cast<float*>(fsm + L.cd);
+  uint32_t* cand_i = reinterpret_cast<uint32_t*>(fsm + L.ci);
+  float* cand_x = reinterpret_cast<float*>(fsm + L.cx);
+  float* stg_d = reinterpret_cast<float*>(fsm + L.sd);
+  uint32_t* stg_i = reinterpret_cast<uint32_t*>(fsm + L.si);
+  const size_t base = size_t(q) * nsplit * a.kp;
+  const uint32_t* lens = a.part_n + size_t(q) * nsplit;
+  if (tid == 0) {
+    s_total = 0;
+    s_cnt = 0;
+    s_kmin = 0xFFFFFFFFu;
+    s_kmax = 0u;
+    s_dk = __int_as_float(0x7f800000);
+  }
+  const float* qrow = a.q + size_t(q) * a.ldq;
+  if (L.cd > 0)
+    for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
   __syncthreads();
-  // ---- merge: one list per thread into the staging area, four loads in flight ----
-  for (uint32_t sp = threadIdx.x; sp < a.nsplit; sp += blockDim.x) {
-    const uint32_t len = min(a.part_n[size_t(q) * a.nsplit + sp], kp);
+  // ---- 1. stage: one list per thread, eight loads in flight ----
+  for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
+    const uint32_t len = min(lens[sp], a.kp);
     if (!len) continue;
-    const uint32_t pos = atomicAdd(&total, len);
-    const float* ld = a.part_d + base + size_t(sp) * kp;
-    const uint32_t* li = a.part_i + base + size_t(sp) * kp;
-    for (uint32_t j = 0; j < len; j += 4) {
-      float dv[4];
-      uint32_t iv[4];
+    const uint32_t pos = atomicAdd(&s_total, len);
+    if (pos + len > a.stage_cap) continue;  // too many to stage: the passes read the lists
+    const float* ld = a.part_d + base + size_t(sp) * a.kp;
+    const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
+    for (uint32_t j = 0; j < len; j += 8) {
+      float dv[8];
+      uint32_t iv[8];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
+      for (int t = 0; t < 8; ++t) {
         dv[t] = j + t < len ? ld[j + t] : 0.f;
         iv[t] = j + t < len ? li[j + t] : 0u;
       }
 #pragma unroll
-      for (int t = 0; t < 4; ++t)
-        if (j + t < len && pos + j + t < kFinishStage) {
+      for (int t = 0; t < 8; ++t)
+        if (j + t < len) {
           stg_d[pos + j + t] = dv[t];
           stg_i[pos + j + t] = iv[t];
         }
     }
   }
   __syncthreads();
-  const uint32_t n_all = total;  // CTA-uniform
-  WarpTopK<E> acc;
-  acc.clear();
-  if (n_all > kFinishStage) {  // too many to stage: warp w merges lists w, w + 8, ...
-    if (uint32_t(warp) < a.nsplit)
-      warp_merge_lists<E>(acc, a.part_d + base + size_t(warp) * kp, a.part_i + base + size_t(warp) * kp,
-                          int((a.nsplit - warp + 7) / 8), size_t(8) * kp, int(kp), lane, kk, mg);
-  } else {  // warp w sorts chunks w, w + 8, ... of 32 E entries and merges them
-    constexpr uint32_t kChunk = 32u * E;
-    for (uint32_t c0 = uint32_t(warp) * kChunk; c0 < n_all; c0 += 8 * kChunk) {
-      WarpTopK<E> b;
-      b.load(stg_d + c0, stg_i + c0, int(min(n_all - c0, kChunk)), lane);
-      b.sort(lane);
-      acc.merge(b, lane);
-    }
-  }
-  acc.store(sd[warp], si[warp], int(kp), lane);
-  __syncthreads();
-  if (warp == 0) {
-    warp_merge_lists<E>(acc, sd[1], si[1], 7, kMaxK, int(kp), lane, kk, mg);
-    if (mg >= 0.f) {  // the cut: entries above the k-th + margin (the list stays sorted)
-      float td;
-      uint32_t ti;
-      acc.entry(kk - 1, td, ti);
-      const float cut = __fadd_ru(td, mg);
-#pragma unroll
-      for (int e = 0; e < E; ++e)
-        if (!nb_less(acc.d[e], acc.i[e], cut, kNone)) {
-          acc.d[e] = __int_as_float(0x7f800000);
-          acc.i[e] = kNone;
+  const uint32_t total = s_total;  // CTA-uniform
+  const bool staged = total <= a.stage_cap;
+  // Every entry once, as (order key, approximate distance, id).
+  auto each = [&](auto&& f) {
+    if (staged) {
+      for (uint32_t e = tid; e < total; e += kFinishThreads) f(order_key(stg_d[e]), stg_d[e], stg_i[e]);
+    } else {
+      for (uint32_t sp = warp; sp < nsplit; sp += nwarps) {
+        const uint32_t len = min(lens[sp], a.kp);
+        const float* ld = a.part_d + base + size_t(sp) * a.kp;
+        const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
+        for (uint32_t j = lane; j < len; j += 32) {
+          const float d = ld[j];
+          f(order_key(d), d, li[j]);
         }
+      }
     }
-    acc.store(md, mi, int(kp), lane);
+  };
+  // ---- 2. the cut ----
+  // Exact rank-th smallest key (1 <= rank <= total): CTA-uniform result.
+  auto select_key = [&](uint32_t rank) -> uint32_t {
+    uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+    each([&](uint32_t key, float, uint32_t) {
+      lo = min(lo, key);
+      hi = max(hi, key);
+    });
+    lo = __reduce_min_sync(kFull, lo);
+    hi = __reduce_max_sync(kFull, hi);
+    if (lane == 0) {
+      atomicMin(&s_kmin, lo);
+      atomicMax(&s_kmax, hi);
+    }
+    __syncthreads();
+    const uint32_t kmin = s_kmin, kmax = s_kmax;
+    __syncthreads();
+    if (tid == 0) {
+      s_kmin = 0xFFFFFFFFu;  // ready for the next selection
+      s_kmax = 0u;
+    }
+    __syncthreads();
+    const uint32_t diff = kmin ^ kmax;
+    if (!diff) return kmin;
+    int lo_bit = 32 - __clz(diff);  // bits [0, lo_bit) remain to resolve; above them all keys agree
+    uint32_t mask = lo_bit == 32 ? 0u : (0xFFFFFFFFu << lo_bit);
+    uint32_t prefix = kmin & mask;
+    uint32_t remaining = rank;
+    while (lo_bit > 0) {
+      const int nb = min(8, lo_bit);
+      const int shift = lo_bit - nb;
+      const uint32_t bmask = (1u << nb) - 1u;
+      for (int b = tid; b < 256; b += kFinishThreads) hist[b] = 0;
+      __syncthreads();
+      each([&](uint32_t key, float, uint32_t) {
+        if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & bmask], 1u);
+      });
+      __syncthreads();
+      if (warp == 0) {  // the first bucket whose running count reaches `remaining`
+        uint32_t c[8], sum = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          c[i] = hist[lane * 8 + i];
+          sum += c[i];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(kFull, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const unsigned reach = __ballot_sync(kFull, incl >= remaining);
+        const int src = reach ? __ffs(reach) - 1 : 31;
+        if (lane == src) {
+          uint32_t rr = remaining - (incl - sum), bi = 7;
+          bool found = false;
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!found) {
+              if (c[i] >= rr || i == 7) {
+                bi = uint32_t(i);
+                found = true;
+              } else {
+                rr -= c[i];
+              }
+            }
+          s_prefix = prefix | ((uint32_t(lane) * 8u + bi) << shift);
+          s_rank = rr;
+        }
+      }
+      __syncthreads();
+      prefix = s_prefix;
+      remaining = s_rank;
+      mask |= bmask << shift;
+      lo_bit = shift;
+      __syncthreads();
+    }
+    return prefix;
+  };
+  uint32_t cut_key = kKeyAll;  // keep entries with key <= cut_key (or < when strict)
+  bool strict = false;
+  if (total > target) {
+    const uint32_t tk = select_key(target);
+    cut_key = mg >= 0.f ? order_key(__fadd_ru(key_float(tk), mg)) : tk;
   }
+  // count the entries the cut keeps; more than kRerankMax: keep those strictly below the
+  // kRerankMax-th smallest instead (fewer than kRerankMax)
+  {
+    uint32_t c = 0;
+    each([&](uint32_t key, float, uint32_t) { c += key <= cut_key ? 1u : 0u; });
+    c = __reduce_add_sync(kFull, c);
+    if (lane == 0) atomicAdd(&s_cnt, c);
+    __syncthreads();
+    const uint32_t kept = s_cnt;
+    __syncthreads();
+    if (tid == 0) s_cnt = 0;
+    __syncthreads();
+    if (kept > kRerankMax) {
+      cut_key = select_key(kRerankMax);
+      strict = true;
+    }
+  }
+  // the cut's share of the certificate's L: only when it left an entry out
+  each([&](uint32_t key, float d, uint32_t id) {
+    if (strict ? key < cut_key : key <= cut_key) {
+      const uint32_t slot = atomicAdd(&s_cnt, 1u);
+      cand_d[slot] = d;
+      cand_i[slot] = id;
+    }
+  });
   __syncthreads();
-  // ---- rerank: exact FP32 distances of the real entries (a prefix of the sorted list) ----
-  const uint32_t nc = a.dp / 4;
-  float* qs = stg_d;  // the staging area is free now
-  const bool q_in_smem = a.dp <= kFinishStage;
-  if (q_in_smem)
-    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.ldq + c];
-  const uint32_t id0 = threadIdx.x < kp ? mi[threadIdx.x] : kNone;  // kp <= 128 < threads
-  const uint32_t nreal = uint32_t(__syncthreads_count(id0 != kNone));
-  const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.ldq);
-  constexpr int G = 4;  // four candidates per warp at a time
-  const uint32_t nwarps = blockDim.x / 32;
-  for (uint32_t j0 = warp; j0 < nreal; j0 += G * nwarps) {
+  const uint32_t nc = s_cnt;  // <= kRerankMax
+  const bool cut_left_out = nc < total;
+  // ---- 3. rerank ----
+  const float4* q4 = reinterpret_cast<const float4*>(L.cd > 0 ? qs : qrow);
+  const uint32_t nch = a.dp / 4;
+  constexpr int G = 4;  // rows per warp in flight
+  for (uint32_t j0 = warp; j0 < nc; j0 += G * nwarps) {
     const float4* x4[G];
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       const uint32_t j = j0 + uint32_t(g) * nwarps;
-      x4[g] = j < nreal ? reinterpret_cast<const float4*>(a.x + size_t(mi[j]) * a.dp) : nullptr;
+      const uint32_t id = j < nc ? cand_i[j] : kNone;
+      x4[g] = id < a.n ? reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp) : nullptr;
     }
     float d[G];
-    exact_distances<L2, G>(q4, x4, nc, lane, d);
+    exact_distances<L2, G>(q4, x4, nch, lane, d);
     if (lane == 0) {
 #pragma unroll
-      for (int g = 0; g < G; ++g)
-        if (j0 + uint32_t(g) * nwarps < nreal) cd[j0 + uint32_t(g) * nwarps] = d[g];
+      for (int g = 0; g < G; ++g) {
+        const uint32_t j = j0 + uint32_t(g) * nwarps;
+        if (j < nc) cand_x[j] = x4[g] ? d[g] : __int_as_float(0x7f800000);
+      }
     }
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < nreal; j += blockDim.x) {
-    const float dj = cd[j];
-    const uint32_t ij = mi[j];
+  // ---- 4. top k by (FP32 dist, id) ----
+  for (uint32_t j = tid; j < nc; j += kFinishThreads) {
+    const float dj = cand_x[j];
+    const uint32_t ij = cand_i[j];
     uint32_t rank = 0;
-    for (uint32_t t = 0; t < nreal; ++t)
-      rank += nb_less(cd[t], mi[t], dj, ij) || (cd[t] == dj && mi[t] == ij && t < j);
+    for (uint32_t t = 0; t < nc; ++t) rank += nb_less(cand_x[t], cand_i[t], dj, ij) || (cand_x[t] == dj && cand_i[t] == ij && t < j);
     if (rank < k) {
-      a.out_d[size_t(q) * k + rank] = dj;
-      a.out_i[size_t(q) * k + rank] = ij;
+      const bool real = ij < a.n && dj == dj && dj != __int_as_float(0x7f800000);
+      a.out_d[out_off + rank] = real ? dj : __int_as_float(0x7f800000);
+      a.out_i[out_off + rank] = real ? ij : kNone;
     }
-    if (rank + 1 == k) dk = dj;  // the k-th FP32 distance
+    if (rank + 1 == k) s_dk = dj;
   }
-  for (uint32_t j = nreal + threadIdx.x; j < k; j += blockDim.x) {  // fewer than k candidates: pad
-    a.out_d[size_t(q) * k + j] = __int_as_float(0x7f800000);
-    a.out_i[size_t(q) * k + j] = kNone;
+  for (uint32_t j = nc + tid; j < k; j += kFinishThreads) {  // fewer than k candidates: pad
+    a.out_d[out_off + j] = __int_as_float(0x7f800000);
+    a.out_i[out_off + j] = kNone;
   }
   if (!a.fail_count) return;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const float last = md[kp - 1];
+  // ---- 5. certificate ----
+  __shared__ int s_slot;
+  if (tid == 0) {
     const float thr0 = a.thr_init ? a.thr_init[q] : __int_as_float(0x7f800000);
     const uint32_t gk = a.gthr ? a.gthr[q] : kKeyNone;
     const float g = gk != kKeyNone ? key_float(gk) : __int_as_float(0x7f800000);
-    const float cut = (a.margin && k <= kp) ? __fadd_ru(md[k - 1], a.margin[q]) : __int_as_float(0x7f800000);
-    const double L = double(fminf(fminf(last, thr0), fminf(g, cut)));
-    const bool ok = isinf(L) || (L - double(a.err[q]) > double(dk));
-    if (!ok) a.fail_list[atomicAdd(a.fail_count, 1u)] = q;
+    const float lc = cut_left_out ? key_float(cut_key) : __int_as_float(0x7f800000);
+    const float lb = fminf(fminf(thr0, g), lc);
+    const bool ok = isinf(lb) || __fsub_rd(lb, a.err[q]) > s_dk;
+    s_slot = -1;
+    if (!ok) {
+      const uint32_t j = atomicAdd(a.fail_count, 1u);
+      a.fail_list[j] = q;
+      s_slot = int(j);
+      if (a.tally) atomicAdd(a.tally, 1ull);
+    }
   }
+  __syncthreads();
+  // An uncertified query takes fallback slot j: its FP32 row (and its filter) go there for the
+  // scan kernel that follows.
+  const int j = s_slot;
+  if (j < 0) return;
+  if (a.fq)
+    for (uint32_t c = tid; c < a.dp; c += kFinishThreads) a.fq[size_t(j) * a.dp + c] = L.cd > 0 ? qs[c] : qrow[c];
+  if (a.fmask)
+    for (uint32_t w = tid; w < a.mask_ld; w += kFinishThreads)
+      a.fmask[size_t(j) * a.mask_ld + w] = a.qmask[size_t(q) * a.mask_ld + w];
+  if (a.fmask_ptrs && tid == 0) a.fmask_ptrs[j] = serving ? a.sq[q].mask : nullptr;
 }
 
 // The queries of the bf16 shortlist path, one warp per query: the bf16 copy (stride dp, padding
@@ -1071,6 +1272,8 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, ui
                                                               float* qnorm, uint32_t* gthr, const float* xbound,
                                                               float factor, float* margin, float* err,
                                                               uint32_t* fails) {
+  pdl_trigger();  // the head of a chain of dependent launches: the next kernel may start launching
+  pdl_wait();
   if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
   const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (qq >= nq) return;
@@ -1113,6 +1316,8 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
                                                              const ServeQuery* sq, const float* margin) {
   __shared__ uint32_t hist[256];
   __shared__ uint32_t kmin, kmax, sel_prefix, sel_rank;
+  pdl_trigger();
+  pdl_wait();
   const uint32_t q = blockIdx.x;
   if (hdr) {  // serving mode: the batch shape comes from the header
     nq = hdr->nq;
@@ -1120,7 +1325,8 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
   }
   if (q >= nq) return;
   const float* v = in + size_t(q) * count;
-  const uint32_t kp = sq ? sq[q].kp : kp_per_query ? kp_per_query[q] : kp_all;
+  // (with margins: the k-th best sampled distance plus the query's margin)
+  const uint32_t kp = sq ? (margin ? sq[q].k : sq[q].kp) : kp_per_query ? kp_per_query[q] : kp_all;
   if (kp > count) {  // fewer than kp values: no bound (+inf keeps everything)
     if (threadIdx.x == 0) thr[q] = __int_as_float(0x7f800000);
     return;
@@ -1222,63 +1428,6 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
   }
 }
 
-// Serving mode tail, one CTA per query: warps merge split shortlists (approximate distances) in
-// registers, warp 0 merges the 8 results into the query's best kp, the 8 warps rerank those
-// exactly (the scan kernel's arithmetic) and the first k by (dist, id) are written.
-template <int E, bool L2>
-__global__ void __launch_bounds__(256) serve_finish_kernel(const ServeFinishArgs a) {
-  __shared__ float sd[8][32 * E];
-  __shared__ uint32_t si[8][32 * E];
-  __shared__ float cd[32 * E];
-  __shared__ uint32_t ci[32 * E];
-  __shared__ __align__(16) float qs[4096];
-  const uint32_t q = blockIdx.x;
-  if (q >= a.hdr->nq) return;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const ServeQuery sq = a.sq[q];
-  const uint32_t kp = sq.kp, k = sq.k, nsplit = a.hdr->nsplit;
-  const size_t base = size_t(q) * nsplit * a.kp_max;
-  WarpTopK<E> acc;
-  acc.clear();
-  if (uint32_t(warp) < nsplit)
-    warp_merge_lists<E>(acc, a.part_d + base + size_t(warp) * a.kp_max, a.part_i + base + size_t(warp) * a.kp_max,
-                        int((nsplit - warp + 7) / 8), size_t(8) * a.kp_max, int(kp), lane);
-  acc.store(sd[warp], si[warp], int(kp), lane);
-  const bool q_in_smem = a.dp <= 4096;
-  if (q_in_smem)
-    for (uint32_t c = threadIdx.x; c < a.dp; c += blockDim.x) qs[c] = a.q[size_t(q) * a.dp + c];
-  __syncthreads();
-  if (warp == 0) {
-    warp_merge_lists<E>(acc, sd[1], si[1], 7, 32 * E, int(kp), lane);
-    acc.store(cd, ci, int(kp), lane);
-  }
-  __syncthreads();
-  const float4* q4 = reinterpret_cast<const float4*>(q_in_smem ? qs : a.q + size_t(q) * a.dp);
-  for (uint32_t j = warp; j < kp; j += 8) {
-    const uint32_t id = ci[j];
-    float d = __int_as_float(0x7f800000);
-    if (id != kNone) d = exact_distance<L2>(q4, reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp), a.dp / 4, lane);
-    __syncwarp();
-    if (lane == 0) cd[j] = d;
-  }
-  __syncthreads();
-  for (uint32_t j = threadIdx.x; j < kp; j += blockDim.x) {
-    const float dj = cd[j];
-    const uint32_t ij = ci[j];
-    uint32_t rank = 0;
-    for (uint32_t t = 0; t < kp; ++t)
-      rank += nb_less(cd[t], ci[t], dj, ij) || (cd[t] == dj && ci[t] == ij && t < j);
-    if (rank < k) {
-      a.out_d[sq.out_off + rank] = dj;
-      a.out_i[sq.out_off + rank] = ij;
-    }
-  }
-  for (uint32_t j = kp + threadIdx.x; j < k; j += blockDim.x) {
-    a.out_d[sq.out_off + j] = __int_as_float(0x7f800000);
-    a.out_i[sq.out_off + j] = kNone;
-  }
-}
-
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1342,13 +1491,17 @@ cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uin
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// Every instantiation of the shortlist kernel: [fp8][l2][E = 2, 4, 8].
+// Every instantiation of the shortlist kernel: [fp8][l2][E = 2, 4, 8, 16].
 using TcKernel = void (*)(const CUtensorMap, const CUtensorMap, const TcArgs);
-const TcKernel kTcKernels[2][2][3] = {
-    {{tc_shortlist_kernel<2, false, false>, tc_shortlist_kernel<4, false, false>, tc_shortlist_kernel<8, false, false>},
-     {tc_shortlist_kernel<2, true, false>, tc_shortlist_kernel<4, true, false>, tc_shortlist_kernel<8, true, false>}},
-    {{tc_shortlist_kernel<2, false, true>, tc_shortlist_kernel<4, false, true>, tc_shortlist_kernel<8, false, true>},
-     {tc_shortlist_kernel<2, true, true>, tc_shortlist_kernel<4, true, true>, tc_shortlist_kernel<8, true, true>}}};
+const TcKernel kTcKernels[2][2][4] = {
+    {{tc_shortlist_kernel<2, false, false>, tc_shortlist_kernel<4, false, false>, tc_shortlist_kernel<8, false, false>,
+      tc_shortlist_kernel<16, false, false>},
+     {tc_shortlist_kernel<2, true, false>, tc_shortlist_kernel<4, true, false>, tc_shortlist_kernel<8, true, false>,
+      tc_shortlist_kernel<16, true, false>}},
+    {{tc_shortlist_kernel<2, false, true>, tc_shortlist_kernel<4, false, true>, tc_shortlist_kernel<8, false, true>,
+      tc_shortlist_kernel<16, false, true>},
+     {tc_shortlist_kernel<2, true, true>, tc_shortlist_kernel<4, true, true>, tc_shortlist_kernel<8, true, true>,
+      tc_shortlist_kernel<16, true, true>}}};
 
 cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8) {
   if (stages < 2 || stages > uint32_t(kMaxTcStages) || nkc == 0) return cudaErrorInvalidValue;
@@ -1371,7 +1524,7 @@ cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2
 }
 
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, bool pdl) {
   if (a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist) || !a.cbuf_d || !a.cbuf_i) return cudaErrorInvalidValue;
   if (a.fp8 && (!a.xscale || !a.qscale)) return cudaErrorInvalidValue;
   const uint32_t nkc = tc_chunks(a.dp, a.fp8 != 0);
@@ -1383,9 +1536,8 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
   if (e != cudaSuccess) return e;
   const size_t smem = tc_smem_bytes(a.stages, nkc, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
-  const TcKernel fn = kTcKernels[a.fp8 ? 1 : 0][a.l2 ? 1 : 0][cap == 64 ? 0 : cap == 128 ? 1 : 2];
-  fn<<<grid, kTcThreads, smem, stream>>>(qmap, xmap, a);
-  return cudaGetLastError();
+  const TcKernel fn = kTcKernels[a.fp8 ? 1 : 0][a.l2 ? 1 : 0][cap == 64 ? 0 : cap == 128 ? 1 : cap == 256 ? 2 : 3];
+  return launch_kernel(fn, dim3(grid), dim3(kTcThreads), smem, stream, pdl, qmap, xmap, a);
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
@@ -1436,68 +1588,65 @@ cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint
   return cudaGetLastError();
 }
 
-cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                               uint32_t count, cudaStream_t stream, const uint32_t* count_dev) {
-  if (count == 0) return cudaSuccess;
-  gather_rows_kernel<<<count, 128, 0, stream>>>(dst, src, ld, dp, ids, count, count_dev);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream,
-                                   const uint32_t* count_dev, unsigned long long* tally) {
-  if (count == 0) return cudaSuccess;
-  scatter_results_kernel<<<count, 128, 0, stream>>>(dst_i, dst_d, src_i, src_d, k, ids, count, count_dev, tally);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, cudaStream_t stream) {
+cudaError_t launch_serve_scatter(const uint32_t* count, const uint32_t* fail_list, const ServeQuery* sq,
+                                 const float* src_d, const uint32_t* src_i, uint32_t kmax, float* out_d,
+                                 uint32_t* out_i, unsigned long long* tally, uint32_t max_queries,
+                                 cudaStream_t stream) {
   if (max_queries == 0) return cudaSuccess;
-  if (a.kp_max <= 32) {
-    if (a.l2) serve_finish_kernel<1, true><<<max_queries, 256, 0, stream>>>(a);
-    else serve_finish_kernel<1, false><<<max_queries, 256, 0, stream>>>(a);
-  } else if (a.kp_max <= 64) {
-    if (a.l2) serve_finish_kernel<2, true><<<max_queries, 256, 0, stream>>>(a);
-    else serve_finish_kernel<2, false><<<max_queries, 256, 0, stream>>>(a);
-  } else {
-    if (a.l2) serve_finish_kernel<4, true><<<max_queries, 256, 0, stream>>>(a);
-    else serve_finish_kernel<4, false><<<max_queries, 256, 0, stream>>>(a);
-  }
+  serve_scatter_kernel<<<max_queries, 128, 0, stream>>>(count, fail_list, sq, src_d, src_i, kmax, out_d, out_i,
+                                                        tally);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
-                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin) {
+                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin, bool pdl) {
   if (nq == 0) return cudaSuccess;
   if (count % 4 != 0 || reinterpret_cast<uintptr_t>(in) % 16 != 0) return cudaErrorInvalidValue;  // float4 loads
-  sample_select_kernel<<<nq, 256, 0, stream>>>(in, count, nq, kp_per_query, kp, thr, nullptr, nullptr, margin);
-  return cudaGetLastError();
+  return launch_kernel(sample_select_kernel, dim3(nq), dim3(256), 0, stream, pdl, in, count, nq, kp_per_query, kp,
+                       thr, static_cast<const ServeHeader*>(nullptr), static_cast<const ServeQuery*>(nullptr),
+                       margin);
 }
 
 cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
-                                uint32_t max_queries, cudaStream_t stream) {
+                                uint32_t max_queries, cudaStream_t stream, const float* margin) {
   if (max_queries == 0) return cudaSuccess;
-  sample_select_kernel<<<max_queries, 256, 0, stream>>>(in, 0, 0, nullptr, 0, thr, hdr, sq, nullptr);
+  sample_select_kernel<<<max_queries, 256, 0, stream>>>(in, 0, 0, nullptr, 0, thr, hdr, sq, margin);
   return cudaGetLastError();
 }
 
-cudaError_t launch_finish(const FinishArgs& a, cudaStream_t stream) {
-  if (a.nq == 0) return cudaSuccess;
-  if (a.kp == 0 || a.kp > uint32_t(kMaxK) || a.k == 0 || !a.part_n || (a.margin && a.k > a.kp))
-    return cudaErrorInvalidValue;
-  if (a.fail_count && (!a.err || !a.fail_list)) return cudaErrorInvalidValue;
-  const unsigned g = a.nq;
-  if (a.kp <= 32) {
-    if (a.l2) finish_kernel<1, true><<<g, 256, 0, stream>>>(a);
-    else finish_kernel<1, false><<<g, 256, 0, stream>>>(a);
-  } else if (a.kp <= 64) {
-    if (a.l2) finish_kernel<2, true><<<g, 256, 0, stream>>>(a);
-    else finish_kernel<2, false><<<g, 256, 0, stream>>>(a);
-  } else {
-    if (a.l2) finish_kernel<4, true><<<g, 256, 0, stream>>>(a);
-    else finish_kernel<4, false><<<g, 256, 0, stream>>>(a);
+size_t finish_smem_bytes(uint32_t dp, uint32_t stage_cap) { return finish_smem(dp, stage_cap).total; }
+
+cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap) {
+  const size_t smem = finish_smem_bytes(dp, stage_cap);
+  static std::mutex mu;
+  static size_t configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  if (dev >= 64 || smem > configured[dev]) {
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(finish_kernel<false>),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(reinterpret_cast<const void*>(finish_kernel<true>),
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    if (dev < 64) configured[dev] = smem;
   }
-  return cudaGetLastError();
+  return cudaSuccess;
+}
+
+cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t stream, bool pdl) {
+  if (grid == 0) return cudaSuccess;
+  if (a.kp == 0 || a.kp > uint32_t(kTcMaxShortlist) || !a.part_n || a.dp % 4 != 0) return cudaErrorInvalidValue;
+  if (!a.hdr && (a.k == 0 || a.k > uint32_t(kMaxK))) return cudaErrorInvalidValue;
+  if (a.hdr && !a.sq) return cudaErrorInvalidValue;
+  if (a.fail_count && (!a.err || !a.fail_list)) return cudaErrorInvalidValue;
+  cudaError_t e = finish_prepare(a.dp, a.stage_cap);
+  if (e != cudaSuccess) return e;
+  const size_t smem = finish_smem_bytes(a.dp, a.stage_cap);
+  return launch_kernel(a.l2 ? finish_kernel<true> : finish_kernel<false>, dim3(grid), dim3(kFinishThreads), smem,
+                       stream, pdl, a);
 }
 
 cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,

@@ -10,7 +10,13 @@ namespace vsg {
 constexpr int kTcQueries = 128;  // queries per CTA (TMEM lanes, MMA M)
 constexpr int kTcRows = 256;     // base rows per tile (MMA N; one accumulator of 256 TMEM columns)
 constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swizzle row)
-constexpr int kTcMaxShortlist = 120;  // largest per-query shortlist (its buffer fits shared memory)
+// Largest per-query shortlist k' of one split's list: candidate buffers hold 64 (k' <= 16), 128
+// (<= 48), 256 (<= 120) or 512 (<= 448) entries per query, so a list of k' always leaves room
+// for 64 appends between compactions.
+constexpr int kTcMaxShortlist = 448;
+// Entries of the split lists the finish kernel stages in shared memory per query at most; beyond
+// that its passes read the lists in global memory.
+constexpr uint32_t kFinishStageMax = 16384;
 
 // Serving mode: one entry per query of a micro-batch (device memory).
 struct ServeQuery {
@@ -31,7 +37,7 @@ struct ServeHeader {
 };
 
 struct TcArgs {
-  uint32_t n, dp, nq, kp;          // dp: padded elements per row of the operand copies; kp <= 120
+  uint32_t n, dp, nq, kp;          // dp: padded elements per row of the operand copies; kp <= 448
   uint32_t rows_per_split, nsplit;  // rows_per_split: a multiple of kTcRows
   uint32_t stages;
   uint32_t resident;               // 1: the query block stays in shared memory for a whole item
@@ -68,10 +74,10 @@ struct TcArgs {
   uint32_t sample_tiles;
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
-  // Certified path (non-serving launches): per-query margin m, or nullptr. A compaction that holds
-  // at least kk entries may then lower the threshold to (its kk-th best) + m, so the list keeps
-  // the rows near the top kk instead of a fixed k'. Every threshold is published to gthr, and
-  // the finish kernel's certificate takes the smallest, so any m keeps results exact.
+  // Certified path: per-query margin m, or nullptr. A compaction that holds at least kk entries
+  // (serving mode: the query's k from sq) may then lower the threshold to (its kk-th best) + m, so
+  // the list keeps the rows near the top kk instead of a fixed k'. Every threshold is published
+  // to gthr, and the finish kernel's certificate takes the smallest, so any m keeps results exact.
   const float* margin;
   uint32_t kk;
   uint32_t nqb;  // query blocks (non-serving launches)
@@ -79,47 +85,37 @@ struct TcArgs {
   // (mask_ld = 0) or one per query, mask_ld words apart; nullptr = no filter.
   const uint32_t* mask;
   uint32_t mask_ld;
+  // Limit of one wait on another role, in ns (0: 2 s). The waits that drain the CTA's own copies
+  // and MMAs before it exits always take 2 s.
+  uint64_t wait_ns;
+  // Test hook: 1 makes the epilogue warps first wait on a barrier nothing completes, so that wait
+  // runs out after wait_ns and the kernel winds down with kDevTimeout.
+  uint32_t stall;
 };
-
-// Serving mode, after the persistent shortlist kernel: per query (one CTA each, CTAs past
-// hdr->nq exit), merge the splits' shortlists by approximate distance, rerank the best kp
-// exactly in FP32 and write the top k at out + sq[q].out_off.
-struct ServeFinishArgs {
-  const ServeHeader* hdr;
-  const ServeQuery* sq;
-  const float* part_d;     // [nq][nsplit][kp_max]
-  const uint32_t* part_i;
-  const float* x;          // FP32 master rows
-  const float* q;          // FP32 queries, stride dp
-  float* out_d;
-  uint32_t* out_i;
-  uint32_t dp, kp_max, l2;
-};
-cudaError_t launch_serve_finish(const ServeFinishArgs& a, uint32_t max_queries, cudaStream_t stream);
 
 // Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q]; plus
 // margin[q] (rounded up) when margin != nullptr.
+// pdl: launched as a programmatic dependent of the previous kernel in the stream (every launcher
+// below with that flag; the kernels wait for their predecessors before touching their outputs).
 cudaError_t launch_sample_select(const float* in, uint32_t count, uint32_t nq, const uint32_t* kp_per_query,
-                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin = nullptr);
+                                 uint32_t kp, float* thr, cudaStream_t stream, const float* margin = nullptr,
+                                 bool pdl = false);
 // Serving mode: the same with nq, count (nsplit * sample_tiles * 128) from hdr and each query's
-// k' from sq; CTAs past hdr->nq exit.
+// k' from sq (with margins: its k-th sampled distance plus margin[q]); CTAs past hdr->nq exit.
 cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, const float* in, float* thr,
-                                uint32_t max_queries, cudaStream_t stream);
+                                uint32_t max_queries, cudaStream_t stream, const float* margin = nullptr);
+
+// Serving mode, the certified path's fallback after the scan (a launch sized for max_queries,
+// reading the uncertified count on the device): the first sq.k of the scan's kmax results of slot
+// j go to query fail_list[j]'s place in the output block, and the count is added to tally.
+cudaError_t launch_serve_scatter(const uint32_t* count, const uint32_t* fail_list, const ServeQuery* sq,
+                                 const float* src_d, const uint32_t* src_i, uint32_t kmax, float* out_d,
+                                 uint32_t* out_i, unsigned long long* tally, uint32_t max_queries,
+                                 cudaStream_t stream);
 
 // count queries near rows of src (0.9 x_i + 0.1 x_j of its n rows, stride dp), for the autotuner.
 cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
                                  cudaStream_t stream);
-// Gathers rows ids[0..count) of src (stride ld floats, dp copied) into dst (stride dp).
-// With count_dev set, only rows j < min(count, *count_dev) (a count read on the device; the launch
-// is sized for count).
-cudaError_t launch_gather_rows(float* dst, const float* src, size_t ld, uint32_t dp, const uint32_t* ids,
-                               uint32_t count, cudaStream_t stream, const uint32_t* count_dev = nullptr);
-// Scatters result rows j of (src_i, src_d) (k each) to rows ids[j] of (dst_i, dst_d); count_dev as
-// above, and when tally is set the number of rows scattered is added to it.
-cudaError_t launch_scatter_results(uint32_t* dst_i, float* dst_d, const uint32_t* src_i, const float* src_d,
-                                   uint32_t k, const uint32_t* ids, uint32_t count, cudaStream_t stream,
-                                   const uint32_t* count_dev = nullptr, unsigned long long* tally = nullptr);
-
 // 128-byte chunks per row of an operand copy: dp bf16 (64 per chunk) or dp e4m3 (128 per chunk).
 uint32_t tc_chunks(uint32_t dp, bool fp8);
 // Shared memory of the shortlist kernel: ring depth, chunks per row, resident query block or not.
@@ -152,7 +148,7 @@ cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t row
 cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
 // grid: CTAs (x only); the candidate buffers must hold grid * 128 * tc_buffer_capacity(kp) entries.
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
-                                cudaStream_t stream);
+                                cudaStream_t stream, bool pdl = false);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
 // When bounds != nullptr, raises bounds[0..3) to the rows' max |x~ - x|, max |x| and max |x~|
 // (x~ = the bf16 row; FP32 sums, not yet inflated for their rounding). With tile_row0 set, dst
@@ -160,35 +156,57 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
 constexpr size_t kRowMajor = ~size_t(0);
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,
                            float* norms, cudaStream_t stream, float* bounds = nullptr, size_t tile_row0 = kRowMajor);
-// The shortlist path's tail in one launch, one CTA per query: the split lists merged into the
-// query's best kp (the real entries, part_n, gathered into shared memory and sorted when they
-// fit, else the lists merged; with margins, lists above (k-th best) + margin skipped and the merged
-// list cut there), then the exact FP32 distances of the list's rows with the scan kernel's
-// arithmetic and the top k by (dist, id), all without a round trip through global memory.
+// The shortlist path's tail in one launch, one CTA per query: the real entries of the query's
+// split lists (part_n of each, staged in shared memory when they fit in stage_cap), a cut at the
+// target-th smallest approximate distance (k plus the query's margin on the certified path,
+// else the shortlist size k'), the exact FP32 distances of every entry at or below the cut (at
+// most 1,024) with the scan kernel's arithmetic, and the top k by (dist, id).
 // Certification (exact results from the shortlist), when fail_count is set: every row outside the
-// list has an approximate distance >= L = min(k'-th list entry, sample threshold, the smallest
-// shared threshold, merge cut); the bound E on |approximate - FP32 distance| (from the bf16
-// rounding residuals of query and rows, Cauchy-Schwarz and accumulation terms; see
-// launch_prepare_queries) then shows that none of them can enter the top k when L - E > the k-th
-// FP32 distance found. Uncertified queries are counted (fail_count, atomic) and listed.
+// reranked set has an approximate distance >= L = min(sample threshold, the smallest shared
+// threshold, the cut when it left entries out); the bound E on |approximate - FP32 distance|
+// (from the bf16 rounding residuals of query and rows, Cauchy-Schwarz and accumulation terms; see
+// launch_prepare_queries) then shows that none of them can enter the top k when L - E (rounded
+// down) > the k-th FP32 distance found. Uncertified queries are counted (fail_count, atomic) and
+// listed. Serving mode (hdr set): the batch shape comes from hdr, each query's k, k' and output
+// offset from sq, and CTAs past hdr->nq exit. The kernel reads nothing when *status is set (a
+// shortlist kernel gave up and its lists may be stale); row ids >= n are never dereferenced.
 struct FinishArgs {
   const float* part_d;     // [nq][nsplit][kp] approximate distances, sorted per list
   const uint32_t* part_i;
   const uint32_t* part_n;  // [nq][nsplit] real entries of each list
-  uint32_t nq, nsplit, kp, k;
+  uint32_t nq, nsplit, kp, k;  // kp: the lists' stride (<= kTcMaxShortlist) and, without margins, k'
   const float* margin;     // per-query margins (certified path), or nullptr
   const float* x;          // FP32 master rows, n x dp
+  uint32_t n;
   const float* q;          // FP32 queries, row stride ldq
   uint32_t dp, ldq, l2;
-  float* out_d;            // [nq][k]
+  float* out_d;            // [nq][k], or at sq[q].out_off in serving mode
   uint32_t* out_i;
   const float* thr_init;   // per-query sample threshold, or nullptr (none)
   const uint32_t* gthr;    // the shortlist pass's shared thresholds (order keys), or nullptr
   const float* err;        // per-query E (launch_prepare_queries), needed when fail_count is set
   uint32_t* fail_count;    // number of uncertified queries, or nullptr: no certificate
   uint32_t* fail_list;     // their query indices
+  const int* status;       // the shortlist kernels' status word, or nullptr
+  const ServeHeader* hdr;  // serving mode, or nullptr
+  const ServeQuery* sq;
+  uint32_t stage_cap;      // list entries staged in shared memory at most (<= kFinishStageMax)
+  // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
+  // FP32 row into fq row j (stride dp), its per-query mask (qmask row q, mask_ld words) into fmask
+  // row j, or (serving) its filter pointer into fmask_ptrs[j]; tally counts them. Each optional.
+  float* fq;
+  const uint32_t* qmask;
+  uint32_t* fmask;
+  uint32_t mask_ld;
+  const uint32_t** fmask_ptrs;
+  unsigned long long* tally;
 };
-cudaError_t launch_finish(const FinishArgs& a, cudaStream_t stream);
+// Dynamic shared memory of the finish kernel, and its attribute set up to that size (done by
+// launch_finish too; a launch captured into a CUDA graph should find it done).
+size_t finish_smem_bytes(uint32_t dp, uint32_t stage_cap);
+cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap);
+// grid: nq, or the largest batch in serving mode.
+cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t stream, bool pdl = false);
 
 // The bf16 shortlist path's queries in one launch: bf16 copy qb (stride dp, padding zero) and
 // squared norms qnorm (optional) of the FP32 queries (row stride ldq, dim columns read); gthr[q]

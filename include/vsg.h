@@ -42,8 +42,10 @@ extern "C" {
 #define VSG_METRIC_IP 1u
 
 /* Same values as vecsearch::GpuMethod (include/vecsearch/gpu_brute_force.h:16-21).
- * Methods 0-3 return the same exact top-k; the method only picks the kernel (naive and skinny:
- * the streaming scan kernel; tiled: the register-blocked kernel; auto: by batch size).
+ * Methods 0-3 return the same exact top-k, bit for bit; the method only picks the kernel (naive
+ * and skinny: the streaming scan kernel; tiled: the register-blocked kernel, whose per-split
+ * lists of a few more than k rows are reranked with the scan kernel's arithmetic and certified,
+ * its unproven queries answered by the scan kernel; auto: by batch size).
  * VSG_METHOD_BF16 (new) is the precision form: a BF16 tensor-core pass keeps a shortlist of
  * k' = min(448, max(k, oversample x k)) rows per query by approximate distance, then an exact
  * FP32 rerank of the shortlist returns the top-k with the streaming kernel's arithmetic. It is
@@ -219,6 +221,11 @@ int vsg_autotune_load(vsg_index* index, const char* path);
  * there is one shortlist pass). The uncertified count is kept on the device, so
  * this call waits for the index's queued work. */
 int vsg_tc_exact_stats(vsg_index* index, uint64_t* queries, uint64_t* second, uint64_t* fallbacks);
+
+/* Tiled path counters since the index was created (new): queries searched by the tiled FP32
+ * kernel, and those its certificate could not prove, which the scan kernel answered. Waits for
+ * the index's queued work. */
+int vsg_tiled_stats(vsg_index* index, uint64_t* queries, uint64_t* fallbacks);
 
 /* Kernels this index has launched since it was created (searches, conversions; not the
  * serving loop's graphs), for benchmarks that report their launch count. */

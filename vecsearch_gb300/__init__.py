@@ -289,6 +289,13 @@ class GpuBruteForceIndex:
         _native.check(_native.lib().vsg_tc_exact_stats(self._h, ctypes.byref(q), ctypes.byref(s2), ctypes.byref(f)))
         return q.value, s2.value, f.value
 
+    def tiled_stats(self):
+        """(queries searched by the tiled FP32 kernel, queries its certificate could not prove and
+        the scan kernel answered) since the index was created. Waits for the index's queued work."""
+        q, f = ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(_native.lib().vsg_tiled_stats(self._h, ctypes.byref(q), ctypes.byref(f)))
+        return q.value, f.value
+
     def profile(self, enable=True):
         """Start (or stop) recording CUDA-event times of the scan and merge kernels."""
         _native.check(_native.lib().vsg_profile_enable(self._h, int(enable)))

@@ -46,6 +46,7 @@ SIGNATURES = {
     "vsg_add_hnsw_file": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(_SZ)]),
     "vsg_tc_exact_stats": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                   ctypes.POINTER(ctypes.c_uint64)]),
+    "vsg_tiled_stats": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_kernel_launches": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_autotune": (_INT, [_P, ctypes.POINTER(_SZ), _SZ, _SZ, _U32]),
     "vsg_autotune_with_queries": (_INT, [_P, ctypes.c_void_p, _SZ, ctypes.POINTER(_SZ), _SZ, _SZ, _U32]),

@@ -38,6 +38,17 @@ __device__ __forceinline__ bool nb_less(float ad, uint32_t ai, float bd, uint32_
   return ad < bd || (ad == bd && ai < bi);
 }
 
+// Float -> unsigned key with the same order (negative values flipped), and back. A per-query
+// threshold published by several CTAs is kept as such a key (atomicMin); kKeyNone = not set.
+constexpr uint32_t kKeyNone = 0xFFFFFFFFu;
+__device__ __forceinline__ uint32_t order_key(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t key) {
+  return __uint_as_float((key & 0x80000000u) ? (key & 0x7FFFFFFFu) : ~key);
+}
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

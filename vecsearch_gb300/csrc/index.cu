@@ -408,6 +408,16 @@ int vsg_tc_exact_stats(vsg_index* h, uint64_t* queries, uint64_t* second, uint64
   });
 }
 
+int vsg_tiled_stats(vsg_index* h, uint64_t* queries, uint64_t* fallbacks) {
+  if (!h || !queries || !fallbacks) return fail(VSG_ERR_INVALID, "index or output is NULL");
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(h->mu);
+    VSG_CUDA(cudaSetDevice(h->device));
+    *fallbacks = h->tiled_stats_sync();
+    *queries = h->tiled_queries;
+  });
+}
+
 int vsg_kernel_launches(vsg_index* h, uint64_t* launches) {
   if (!h || !launches) return fail(VSG_ERR_INVALID, "index or output is NULL");
   return guarded([&] {

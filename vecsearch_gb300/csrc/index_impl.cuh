@@ -142,6 +142,11 @@ struct vsg_index {
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_prepare_queries)
   size_t bf16_rows = 0;
+  // Tiled path: an upper bound of the rows' norms (a float's bits) over the first xmax_rows rows,
+  // the queries it searched and a device tally of those its certificate left to the scan kernel.
+  DeviceBuffer xmax, tiledstats;
+  size_t xmax_rows = 0;
+  uint64_t tiled_queries = 0;
   CUtensorMap xmap{};
   const void* xmap_base = nullptr;
   size_t xmap_rows = 0;
@@ -317,32 +322,109 @@ struct vsg_index {
     *nsplit = uint32_t(ceil_div(n, rps));
   }
 
+  // Raises the rows' norm bound over rows added since the last call.
+  void ensure_xmax() {
+    if (xmax_rows == n && xmax.get()) return;
+    xmax.reserve(16, 0, stream);
+    VSG_CUDA(vsg::launch_row_norm_max(static_cast<const float*>(x.get()) + xmax_rows * dp, n - xmax_rows,
+                                      uint32_t(dp), static_cast<uint32_t*>(xmax.get()), stream));
+    ++kernel_launches;
+    xmax_rows = n;
+  }
+
+  // The tiled FP32 kernel as a shortlist with a certificate, like the tensor-core path: the
+  // kernel keeps each split's best kp = tiled_list_size(k) rows by its own FP32 arithmetic and
+  // publishes every full list's last entry; the finish kernel reranks the rows within the margin
+  // of each query's k-th best with the scan kernel's arithmetic and proves that no row left out
+  // can enter the top k (E: launch_prepare_fp32_queries); unproven queries run in the scan kernel
+  // (launched on the device's count of them, as in enqueue_tc_exact). Results equal method skinny
+  // bit for bit.
   void enqueue_tiled(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                      cudaStream_t s) {
-    const size_t bm = size_t(vsg::tiled_block_queries(uint32_t(k), uint32_t(nq)));
+    const uint32_t kp = vsg::tiled_list_size(uint32_t(k));
+    const size_t bm = size_t(vsg::tiled_block_queries(kp, uint32_t(nq)));
     const size_t nqb = ceil_div(nq, bm);
     vsg::TiledArgs a{};
     choose_splits(nqb, 128, 1024, &a.rows_per_split, &a.nsplit, split_factor(nq, false));
-    const size_t parts = nq * a.nsplit * k;
-    part.reserve(parts * 8, 0, stream);
+    const size_t parts = nq * a.nsplit * kp;
+    part.reserve(parts * 8 + nq * a.nsplit * 4, 0, stream);  // lists, then their lengths
+    ensure_xmax();
+    fails.reserve((nq + 1) * sizeof(uint32_t), 0, stream);
+    tiledstats.reserve(sizeof(unsigned long long), 0, stream);
+    gthr.reserve(nq * sizeof(uint32_t), 0, stream);
+    qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
+    fq.reserve(nq * dp * sizeof(float), 0, stream);
+    float* mgn = static_cast<float*>(qmargin.get());
+    uint32_t* d_fail = static_cast<uint32_t*>(fails.get());
+    VSG_CUDA(vsg::launch_prepare_fp32_queries(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dp), metric == VSG_METRIC_L2,
+                                              static_cast<const uint32_t*>(xmax.get()), float(cert_margin),
+                                              static_cast<uint32_t*>(gthr.get()), mgn, mgn + nq, d_fail, s));
+    ++kernel_launches;
     a.x = static_cast<const float*>(x.get());
     a.q = dq;
     a.ldq = uint32_t(ldq);
     a.part_d = static_cast<float*>(part.get());
     a.part_i = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 4);
+    a.part_n = reinterpret_cast<uint32_t*>(static_cast<char*>(part.get()) + parts * 8);
+    a.gthr = static_cast<uint32_t*>(gthr.get());
     a.n = uint32_t(n);
     a.dp = uint32_t(dp);
     a.nq = uint32_t(nq);
-    a.k = uint32_t(k);
+    a.kp = kp;
     Timing* tm = profiling ? next_timing() : nullptr;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));
     VSG_CUDA(vsg::launch_tiled(a, metric == VSG_METRIC_L2, dim3(unsigned(nqb), a.nsplit), s));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[1], s));
-    vsg::MergeArgs m{a.part_d, a.part_i, out_dists, out_ids, uint32_t(nq), a.nsplit, uint32_t(k)};
-    VSG_CUDA(vsg::launch_merge(m, s));
+    vsg::FinishArgs fa{};
+    fa.part_d = a.part_d;
+    fa.part_i = a.part_i;
+    fa.part_n = a.part_n;
+    fa.nq = uint32_t(nq);
+    fa.nsplit = a.nsplit;
+    fa.kp = kp;
+    fa.k = uint32_t(k);
+    fa.margin = mgn;  // the cut keeps the rows within the margin of the k-th best
+    fa.x = a.x;
+    fa.n = uint32_t(n);
+    fa.q = dq;
+    fa.dp = uint32_t(dp);
+    fa.ldq = uint32_t(ldq);
+    fa.l2 = metric == VSG_METRIC_L2 ? 1u : 0u;
+    fa.out_d = out_dists;
+    fa.out_i = out_ids;
+    fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * kp));
+    fa.gthr = a.gthr;
+    fa.err = mgn + nq;
+    fa.fail_count = d_fail;
+    fa.fail_list = d_fail + 1;
+    fa.fq = static_cast<float*>(fq.get());
+    fa.tally = static_cast<unsigned long long*>(tiledstats.get());
+    const bool pdl = !profiling;
+    VSG_CUDA(vsg::launch_finish(fa, uint32_t(nq), s, pdl));
     ++kernel_launches;
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[2], s));
+    tiled_queries += nq;
+    const bool prof = profiling;
+    profiling = false;
+    try {
+      enqueue(static_cast<const float*>(fq.get()), dp, nq, k, nullptr, false, 0, false, out_ids, out_dists, s,
+              VSG_METHOD_SKINNY, -1.0, d_fail, d_fail + 1, pdl);
+    } catch (...) {
+      profiling = prof;
+      throw;
+    }
+    profiling = prof;
+  }
+
+  // Queries of the tiled path that the scan kernel answered (waits for the index's work).
+  uint64_t tiled_stats_sync() {
+    if (!tiledstats.get()) return 0;
+    unsigned long long v = 0;
+    VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
+    VSG_CUDA(cudaMemcpyAsync(&v, tiledstats.get(), sizeof(v), cudaMemcpyDeviceToHost, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    return uint64_t(v);
   }
 
   // Brings the BF16 copy (tile-major, see vsg::tc_tiled_bytes) and the norms up to the current

@@ -47,7 +47,6 @@ constexpr uint32_t kChunkBytes = kTcQueries * 128;    // 16 KB: a chunk of the 1
 constexpr uint32_t kRowChunkBytes = kTcRows * 128;    // 32 KB: a chunk of a 256-row tile (B)
 constexpr uint32_t kTmemCols = 2 * kTcRows;           // two accumulators: all 512 columns
 constexpr int kMaxTcStages = 8;
-constexpr uint32_t kKeyNone = 0xFFFFFFFFu;  // shared threshold not set
 
 // Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16
 // (bits 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at 24-28.
@@ -85,15 +84,6 @@ __host__ __device__ inline size_t tile_major_offset(size_t row, uint32_t c, uint
 // Approximate L2 distance from squared norms and the bf16 score: |q|^2 + |x|^2 - 2 s, rounded
 // the same way wherever it is computed (the prefilter, the append and the sample pass agree).
 __device__ __forceinline__ float l2_approx(float qn, float xn, float sc) { return __fmaf_rn(-2.f, sc, __fadd_rn(qn, xn)); }
-
-// Float -> unsigned key with the same order (negative values flipped), and back.
-__device__ __forceinline__ uint32_t order_key(float f) {
-  const uint32_t u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float key_float(uint32_t key) {
-  return __uint_as_float((key & 0x80000000u) ? (key & 0x7FFFFFFFu) : ~key);
-}
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
   uint32_t v;

@@ -11,8 +11,17 @@
 //   * after the last k-slice the block is written to a shared score tile as distances, and
 //     each warp scans the scores of its queries against the query's current k-th best
 //     (dist, id), inserting the few that beat it into the query's sorted list;
-//   * at the end the lists are written as the split's top-k for merge_kernel.
+//   * at the end each list (kp entries, a few more than k) is written with its length, and a
+//     full list publishes its last entry to the query's shared threshold (atomicMin): every
+//     row the split left out has a distance at or above it.
 // No distance ever reaches global memory. FP32 FMA-bound: 2 * BM * 128 * d flops per tile.
+//
+// The kernel sums each distance's d products in one FMA chain, a different order from the scan
+// kernel's (lane-strided chunks, then a butterfly), so near-ties can order differently. Its lists
+// are therefore a shortlist: the finish kernel reranks the rows near each query's k-th best with
+// the scan kernel's arithmetic and proves, from a bound E on the difference between the two
+// evaluations (launch_prepare_fp32_queries), that no row left out can enter the top k; queries
+// it cannot prove run in the scan kernel. The results are the scan kernel's, bit for bit.
 #include <mutex>
 
 #include "device_common.cuh"
@@ -62,7 +71,7 @@ __global__ void __launch_bounds__(kThreads, 1) tiled_kernel(const TiledArgs a) {
   constexpr int TM = BM / 16;
   constexpr int kStages = 3;
   extern __shared__ __align__(128) unsigned char smem[];
-  const uint32_t dp = a.dp, k = a.k;
+  const uint32_t dp = a.dp, k = a.kp;
   const TiledLayout L = tiled_layout(BM, k, kStages);
   float* stage_base = reinterpret_cast<float*>(smem);
   float* score = reinterpret_cast<float*>(smem + L.score_off);
@@ -214,16 +223,95 @@ __global__ void __launch_bounds__(kThreads, 1) tiled_kernel(const TiledArgs a) {
     const uint32_t qg = qbase + m;
     if (qg >= a.nq) break;
     const size_t o = (size_t(qg) * a.nsplit + split) * k;
+    const float* ld = lst_d + size_t(m) * k;
+    const uint32_t* li = lst_i + size_t(m) * k;
+    uint32_t real = 0;  // the list is sorted: its real entries come first
     for (uint32_t j = lane; j < k; j += 32) {
-      a.part_d[o + j] = lst_d[size_t(m) * k + j];
-      a.part_i[o + j] = lst_i[size_t(m) * k + j];
+      a.part_d[o + j] = ld[j];
+      a.part_i[o + j] = li[j];
+      real += li[j] != kNone ? 1u : 0u;
     }
+    real = __reduce_add_sync(kFull, real);
+    if (lane == 0) {
+      a.part_n[size_t(qg) * a.nsplit + split] = real;
+      if (real == k) atomicMin(a.gthr + qg, order_key(ld[k - 1]));
+    }
+  }
+}
+
+// One warp per row (grid-stride): an upper bound of the row's norm, max-reduced into *out.
+__global__ void row_norm_max_kernel(const float* __restrict__ x, size_t rows, uint32_t dp, uint32_t* out) {
+  const uint32_t lane = threadIdx.x & 31;
+  const size_t warps = size_t(gridDim.x) * (blockDim.x >> 5);
+  const float u = 5.9604644775390625e-08f;  // 2^-24
+  const float infl = __fadd_ru(1.f, __fmul_ru(2.f, __fmul_ru(float(dp), u)));
+  float best = 0.f;
+  for (size_t r = size_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    const float* row = x + r * dp;
+    float s = 0.f;
+    for (uint32_t c = lane; c < dp; c += 32) s = fmaf(row[c], row[c], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    best = fmaxf(best, __fsqrt_ru(__fmul_ru(s, infl)));
+  }
+  if (lane == 0 && best > 0.f) atomicMax(out, __float_as_uint(best));  // non-negative: bits order as values
+}
+
+// |e1 - e2| for two FP32 evaluations of one distance from the same d terms (products for IP,
+// squared differences for L2), summed in different orders with FMAs. Any order of d terms is
+// within gamma_d sum|terms| of the exact sum, gamma_d = d u / (1 - d u) <= d u (1 + 2 d u) (u =
+// 2^-24, d u <= 1/4), so two evaluations differ by at most 2 gamma_d sum|terms|:
+//   IP: sum|q_i x_i| <= |q| X (X: the rows' norm bound); the two roundings of 1 - s add at most
+//       u (1 + |q| X) each.
+//   L2: a difference q_i - x_i is rounded once (relative u), so its square is within 3u of
+//       (q_i - x_i)^2; D = sum (q_i - x_i)^2 <= (|q| + X)^2; total 2 (gamma_d + 4u) (|q| + X)^2.
+// |q| comes from an FP32 sum of squares inflated by (1 + 2 d u). Every operation rounds up, and
+// the result gets a 1.1 margin.
+template <bool L2>
+__device__ float fp32_pair_error(float sq2, uint32_t dp, float xmax) {
+  auto mul = [](float a, float b) { return __fmul_ru(a, b); };
+  auto add = [](float a, float b) { return __fadd_ru(a, b); };
+  const float u = 5.9604644775390625e-08f;
+  const float du = mul(float(dp), u);
+  const float infl = add(1.f, mul(2.f, du));
+  const float g = mul(du, infl);  // gamma_d
+  const float qn = __fsqrt_ru(mul(sq2, infl));
+  float e;
+  if (L2) {
+    const float s = add(qn, xmax);
+    e = mul(mul(2.f, add(g, mul(4.f, u))), mul(s, s));
+  } else {
+    const float qx = mul(qn, xmax);
+    e = add(mul(mul(2.f, g), qx), mul(mul(2.f, u), add(1.f, qx)));
+  }
+  return mul(e, 1.1f);
+}
+
+template <bool L2>
+__global__ void __launch_bounds__(128) prepare_fp32_queries_kernel(const float* q, uint32_t ldq, uint32_t nq,
+                                                                   uint32_t dp, const uint32_t* xmax_bits,
+                                                                   float factor, uint32_t* gthr, float* margin,
+                                                                   float* err, uint32_t* fails) {
+  pdl_trigger();  // the head of a chain: the next kernel may start launching
+  if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
+  const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (qq >= nq) return;
+  const float* s = q + size_t(qq) * ldq;
+  float q2 = 0.f;
+  for (uint32_t c = lane; c < dp; c += 32) q2 = fmaf(s[c], s[c], q2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) q2 += __shfl_xor_sync(kFull, q2, o);
+  if (lane == 0) {
+    gthr[qq] = kKeyNone;
+    const float e = fp32_pair_error<L2>(q2, dp, __uint_as_float(*xmax_bits));
+    err[qq] = e;
+    margin[qq] = __fmul_ru(factor, e);
   }
 }
 
 template <int BM, bool L2>
 cudaError_t launch_tiled_one(const TiledArgs& a, dim3 grid, cudaStream_t stream) {
-  const size_t smem = tiled_layout(BM, a.k, 3).total;
+  const size_t smem = tiled_layout(BM, a.kp, 3).total;
   static std::mutex mu;
   static size_t configured[64] = {};
   int dev = 0;
@@ -243,14 +331,43 @@ cudaError_t launch_tiled_one(const TiledArgs& a, dim3 grid, cudaStream_t stream)
 
 }  // namespace
 
-int tiled_block_queries(uint32_t k, uint32_t nq) { return k <= 32 && nq > 64 ? 128 : 64; }
+uint32_t tiled_list_size(uint32_t k) {
+  const uint32_t kp = (k + (k / 4 > 8 ? k / 4 : 8) + 7) / 8 * 8;
+  return kp < uint32_t(kMaxK) ? kp : uint32_t(kMaxK);
+}
 
-size_t tiled_smem_bytes(uint32_t k, uint32_t nq) {
-  return tiled_layout(tiled_block_queries(k, nq), k, 3).total;
+int tiled_block_queries(uint32_t kp, uint32_t nq) { return kp <= 48 && nq > 64 ? 128 : 64; }
+
+size_t tiled_smem_bytes(uint32_t kp, uint32_t nq) {
+  return tiled_layout(tiled_block_queries(kp, nq), kp, 3).total;
+}
+
+cudaError_t launch_row_norm_max(const float* x, size_t rows, uint32_t dp, uint32_t* xmax_bits, cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  if (!x || !xmax_bits || dp == 0) return cudaErrorInvalidValue;
+  const size_t blocks = (rows + 7) / 8;  // 8 warps a block
+  row_norm_max_kernel<<<unsigned(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(x, rows, dp, xmax_bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prepare_fp32_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dp, bool l2,
+                                        const uint32_t* xmax_bits, float factor, uint32_t* gthr, float* margin,
+                                        float* err, uint32_t* fails, cudaStream_t stream) {
+  if (nq == 0) return cudaSuccess;
+  if (!q || !xmax_bits || !gthr || !margin || !err || ldq < dp || !(factor >= 0.f)) return cudaErrorInvalidValue;
+  const unsigned blocks = (nq + 3) / 4;
+  if (l2)
+    prepare_fp32_queries_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xmax_bits, factor, gthr, margin,
+                                                                  err, fails);
+  else
+    prepare_fp32_queries_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dp, xmax_bits, factor, gthr, margin,
+                                                                   err, fails);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_tiled(const TiledArgs& a, bool l2, dim3 grid, cudaStream_t stream) {
-  if (tiled_block_queries(a.k, a.nq) == 128)
+  if (!a.part_n || !a.gthr || a.kp == 0 || a.kp > uint32_t(kMaxK)) return cudaErrorInvalidValue;
+  if (tiled_block_queries(a.kp, a.nq) == 128)
     return l2 ? launch_tiled_one<128, true>(a, grid, stream) : launch_tiled_one<128, false>(a, grid, stream);
   return l2 ? launch_tiled_one<64, true>(a, grid, stream) : launch_tiled_one<64, false>(a, grid, stream);
 }

@@ -135,6 +135,18 @@ int vsg_hnsw_exact_below(vsg_index* index, const float* queries, size_t nq, size
 int vsg_hnsw_file_info(const char* path, size_t* dim, size_t* rows, uint32_t* metric);
 int vsg_add_hnsw_file(vsg_index* index, const char* path, size_t* added);
 
+/* Exact neighbour candidates for an HNSW build in insertion order (new). The reference's insert
+ * (HNSWIndex::insert, src/hnsw.cpp:247-309, in id order from HNSWIndex::add) searches the graph of
+ * the nodes before it for ef_construction candidates; here row i's list is the exact k nearest of
+ * rows 0 .. i-1 by (dist, id), padded with VSG_NONE / +inf while i < k. rows: n x dim host floats
+ * (stride dim); out_ids / out_dists: n x k host arrays. k <= VSG_MAX_K, else VSG_ERR_INVALID.
+ * Rows go through the device in batches of `batch` (0: 1024): each batch is searched against the
+ * rows before it (an index that grows with the build) and against its own earlier rows (one
+ * prefix filter per query), and the two lists are merged by (dist, id). Distances are the scan
+ * kernel's, so every list equals one exact search over rows 0 .. i-1. Blocks until done. */
+int vsg_insert_candidates(const float* rows, size_t n, size_t dim, uint32_t metric, int device, size_t k,
+                          size_t batch, uint32_t* out_ids, float* out_dists);
+
 /* Device-resident search (new: the serving/throughput form of search()). Queries, mask and
  * outputs are device pointers; queries have row stride ldq floats (ldq >= dim). Work is queued
  * on `stream` (a cudaStream_t; NULL = legacy default stream) and the call returns without

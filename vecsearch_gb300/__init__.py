@@ -22,7 +22,7 @@ from . import _native
 from .datasets import pack_bits
 
 __all__ = ["GpuBruteForceIndex", "HNSWExactRoute", "Server", "cuda_available", "normalize", "recall_at_k",
-           "hnsw_file_info", "DeviceTimeoutError", "pybind_module"]
+           "hnsw_file_info", "insert_candidates", "DeviceTimeoutError", "pybind_module"]
 __version__ = "0.1.0"
 
 DeviceTimeoutError = _native.DeviceTimeoutError
@@ -126,6 +126,27 @@ def _ids_to_int64(ids):
 
 def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def insert_candidates(x, k, metric="l2", batch=1024, device=0):
+    """Exact neighbour candidates for building an HNSW graph in insertion order: row i's list is
+    the k nearest of rows 0 .. i-1 by (dist, id) (the nodes HNSWIndex::insert, src/hnsw.cpp:247-309,
+    searches when it inserts node i), padded with -1 / +inf while i < k. Returns
+    (ids int64 [n, k], dists float32 [n, k]). Batches of `batch` rows are searched against the rows
+    before them and against their own earlier rows on the GPU, then merged."""
+    x = _as_f32(x)
+    if x.ndim != 2:
+        raise ValueError("expected a 2-D array of rows")
+    n, dim = x.shape
+    k = operator.index(k)
+    if k < 0:
+        raise TypeError("k must be a non-negative integer")
+    ids = np.empty((n, k), dtype=np.uint32)
+    dists = np.empty((n, k), dtype=np.float32)
+    if n and k:
+        _native.check(_native.lib().vsg_insert_candidates(_ptr(x), n, dim, _parse_metric(metric), int(device), k,
+                                                          int(batch), _ptr(ids), _ptr(dists)))
+    return _ids_to_int64(ids), dists
 
 
 class GpuBruteForceIndex:

@@ -44,6 +44,7 @@ SIGNATURES = {
     "vsg_get_tunable": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
     "vsg_hnsw_file_info": (_INT, [ctypes.c_char_p, ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.POINTER(_U32)]),
     "vsg_add_hnsw_file": (_INT, [_P, ctypes.c_char_p, ctypes.POINTER(_SZ)]),
+    "vsg_insert_candidates": (_INT, [_P, _SZ, _SZ, _U32, ctypes.c_int, _SZ, _SZ, _P, _P]),
     "vsg_tc_exact_stats": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                   ctypes.POINTER(ctypes.c_uint64)]),
     "vsg_tiled_stats": (_INT, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),

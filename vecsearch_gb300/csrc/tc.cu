@@ -865,33 +865,44 @@ __device__ __forceinline__ float exact_distance(const float4* q4, const float4* 
 
 // exact_distance for G rows at once (row g at x4[g], nullptr: skipped): the same arithmetic per
 // row, so the same bits, with the rows' loads in flight together.
-template <bool L2, int G>
+template <bool L2, int G, int kAhead>
 __device__ __forceinline__ void exact_distances(const float4* q4, const float4* const (&x4)[G], uint32_t nc, int lane,
                                                 float (&out)[G]) {
+  // The loads of kAhead chunk steps (kAhead x 16 bytes a row per lane) are issued before any is
+  // used; the sums still take the chunks in increasing order.
   float acc[G];
 #pragma unroll
   for (int g = 0; g < G; ++g) acc[g] = 0.f;
-  for (uint32_t c = lane; c < nc; c += 32) {
-    const float4 qv = q4[c];
-    float4 xv[G];
+  for (uint32_t c0 = lane; c0 < nc; c0 += 32u * kAhead) {
+    float4 xv[kAhead][G];
 #pragma unroll
-    for (int g = 0; g < G; ++g) xv[g] = x4[g] ? __ldg(x4[g] + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < kAhead; ++u) {
+      const uint32_t c = c0 + 32u * u;
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      if constexpr (L2) {
-        float e = qv.x - xv[g].x;
-        acc[g] = fmaf(e, e, acc[g]);
-        e = qv.y - xv[g].y;
-        acc[g] = fmaf(e, e, acc[g]);
-        e = qv.z - xv[g].z;
-        acc[g] = fmaf(e, e, acc[g]);
-        e = qv.w - xv[g].w;
-        acc[g] = fmaf(e, e, acc[g]);
-      } else {
-        acc[g] = fmaf(qv.x, xv[g].x, acc[g]);
-        acc[g] = fmaf(qv.y, xv[g].y, acc[g]);
-        acc[g] = fmaf(qv.z, xv[g].z, acc[g]);
-        acc[g] = fmaf(qv.w, xv[g].w, acc[g]);
+      for (int g = 0; g < G; ++g) xv[u][g] = (c < nc && x4[g]) ? __ldg(x4[g] + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const uint32_t c = c0 + 32u * u;
+      if (c >= nc) break;
+      const float4 qv = q4[c];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        if constexpr (L2) {
+          float e = qv.x - xv[u][g].x;
+          acc[g] = fmaf(e, e, acc[g]);
+          e = qv.y - xv[u][g].y;
+          acc[g] = fmaf(e, e, acc[g]);
+          e = qv.z - xv[u][g].z;
+          acc[g] = fmaf(e, e, acc[g]);
+          e = qv.w - xv[u][g].w;
+          acc[g] = fmaf(e, e, acc[g]);
+        } else {
+          acc[g] = fmaf(qv.x, xv[u][g].x, acc[g]);
+          acc[g] = fmaf(qv.y, xv[u][g].y, acc[g]);
+          acc[g] = fmaf(qv.z, xv[u][g].z, acc[g]);
+          acc[g] = fmaf(qv.w, xv[u][g].w, acc[g]);
+        }
       }
     }
   }
@@ -935,7 +946,10 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
 
 // The shortlist path's tail (FinishArgs), one CTA of kFinishThreads per query.
 //   1. Stage: every split's real list entries (part_n of them) are copied into shared memory when
-//      they fit (stage_cap entries), else the passes below read the lists in global memory.
+//      they fit (stage_cap entries), else the passes below read the lists in global memory. With
+//      up to 1,024 lists the copy is flat: the lengths are scanned into offsets and every thread
+//      copies independent entries (one thread per list left a few threads walking long lists
+//      with dependent loads: most of the kernel's time at batch 1).
 //   2. Cut: the `target`-th smallest approximate distance (k with margins, else the shortlist
 //      size k') by exact radix selection on order keys (a min / max pass, then 8-bit rounds below
 //      the highest bit where the keys differ); the cut is that value, plus the margin (rounded
@@ -953,6 +967,7 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
 constexpr int kFinishThreads = 512;
 constexpr uint32_t kRerankMax = 1024;
 constexpr uint32_t kKeyAll = 0xFFFFFFFFu;  // cut key that keeps every entry
+constexpr uint32_t kStageSplits = 1024;    // lists the flat staging copy handles at most
 
 struct FinishSmem {
   size_t qs, cd, ci, cx, sd, si, total;  // byte offsets: query, candidates (approx, id, exact), staging
@@ -970,11 +985,15 @@ __host__ __device__ inline FinishSmem finish_smem(uint32_t dp, uint32_t stage_ca
   return L;
 }
 
-template <bool L2>
+// kWide (a batch no larger than the SM count: one CTA per SM, registers to spare): the rerank
+// loads three chunk steps of each row before using them, so a 384-dim row arrives in one round
+// trip; otherwise one step at a time, with fewer registers, so two CTAs share an SM.
+template <bool L2, bool kWide>
 __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs a) {
   extern __shared__ __align__(16) unsigned char fsm[];
   __shared__ uint32_t hist[256];
   __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank;
+  __shared__ uint32_t s_off[kStageSplits + 1];  // list offsets of the flat staging copy
   __shared__ float s_dk;
   pdl_trigger();
   pdl_wait();
@@ -1019,28 +1038,88 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   if (L.cd > 0)
     for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
   __syncthreads();
-  // ---- 1. stage: one list per thread, eight loads in flight ----
-  for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
-    const uint32_t len = min(lens[sp], a.kp);
-    if (!len) continue;
-    const uint32_t pos = atomicAdd(&s_total, len);
-    if (pos + len > a.stage_cap) continue;  // too many to stage: the passes read the lists
-    const float* ld = a.part_d + base + size_t(sp) * a.kp;
-    const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
-    for (uint32_t j = 0; j < len; j += 8) {
-      float dv[8];
-      uint32_t iv[8];
+  // ---- 1. stage ----
+  // Up to kStageSplits lists: their lengths are scanned into offsets, then every thread copies
+  // entries of any list (found by binary search over the offsets), four at a time, so the copy
+  // runs with many independent loads in flight. More lists: one list per thread.
+  if (nsplit <= kStageSplits) {
+    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
+    if (tid == 0) s_off[0] = 0;
+    __syncthreads();
+    if (warp == 0) {  // inclusive scan of s_off[1 .. nsplit]: lane l sums a run of consecutive lists
+      const uint32_t per = (nsplit + 31) / 32;
+      const uint32_t b0 = min(nsplit, uint32_t(lane) * per), b1 = min(nsplit, b0 + per);
+      uint32_t sum = 0;
+      for (uint32_t i = b0; i < b1; ++i) sum += s_off[i + 1];
+      uint32_t incl = sum;
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        dv[t] = j + t < len ? ld[j + t] : 0.f;
-        iv[t] = j + t < len ? li[j + t] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
       }
+      uint32_t run = incl - sum;
+      for (uint32_t i = b0; i < b1; ++i) {
+        run += s_off[i + 1];
+        s_off[i + 1] = run;
+      }
+      if (lane == 31) s_total = incl;
+    }
+    __syncthreads();
+    const uint32_t tot = s_total;
+    if (tot <= a.stage_cap) {
+      for (uint32_t e0 = tid; e0 < tot; e0 += 4 * kFinishThreads) {
+        float dv[4];
+        uint32_t iv[4];
 #pragma unroll
-      for (int t = 0; t < 8; ++t)
-        if (j + t < len) {
-          stg_d[pos + j + t] = dv[t];
-          stg_i[pos + j + t] = iv[t];
+        for (int t = 0; t < 4; ++t) {
+          const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
+          dv[t] = 0.f;
+          iv[t] = 0u;
+          if (e < tot) {  // the list holding entry e: the largest sp with s_off[sp] <= e
+            uint32_t lo = 0, hi = nsplit;
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (s_off[mid] <= e) lo = mid;
+              else hi = mid;
+            }
+            const size_t at = base + size_t(lo) * a.kp + (e - s_off[lo]);
+            dv[t] = a.part_d[at];
+            iv[t] = a.part_i[at];
+          }
         }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
+          if (e < tot) {
+            stg_d[e] = dv[t];
+            stg_i[e] = iv[t];
+          }
+        }
+      }
+    }
+  } else {
+    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
+      const uint32_t len = min(lens[sp], a.kp);
+      if (!len) continue;
+      const uint32_t pos = atomicAdd(&s_total, len);
+      if (pos + len > a.stage_cap) continue;  // too many to stage: the passes read the lists
+      const float* ld = a.part_d + base + size_t(sp) * a.kp;
+      const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
+      for (uint32_t j = 0; j < len; j += 8) {
+        float dv[8];
+        uint32_t iv[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          dv[t] = j + t < len ? ld[j + t] : 0.f;
+          iv[t] = j + t < len ? li[j + t] : 0u;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (j + t < len) {
+            stg_d[pos + j + t] = dv[t];
+            stg_i[pos + j + t] = iv[t];
+          }
+      }
     }
   }
   __syncthreads();
@@ -1188,7 +1267,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       x4[g] = id < a.n ? reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp) : nullptr;
     }
     float d[G];
-    exact_distances<L2, G>(q4, x4, nch, lane, d);
+    exact_distances<L2, G, kWide ? 3 : 1>(q4, x4, nch, lane, d);
     if (lane == 0) {
 #pragma unroll
       for (int g = 0; g < G; ++g) {
@@ -1202,8 +1281,16 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   for (uint32_t j = tid; j < nc; j += kFinishThreads) {
     const float dj = cand_x[j];
     const uint32_t ij = cand_i[j];
-    uint32_t rank = 0;
-    for (uint32_t t = 0; t < nc; ++t) rank += nb_less(cand_x[t], cand_i[t], dj, ij) || (cand_x[t] == dj && cand_i[t] == ij && t < j);
+    // rank = entries before (dj, ij) in (dist, id, position) order; branch-free and unrolled, so
+    // the shared-memory loads overlap
+    auto before = [&](uint32_t t) -> uint32_t {
+      const float xt = cand_x[t];
+      const uint32_t it = cand_i[t];
+      return uint32_t((xt < dj) | ((xt == dj) & ((it < ij) | ((it == ij) & (t < j)))));
+    };
+    uint32_t rank = 0, t = 0;
+    for (; t + 4 <= nc; t += 4) rank += before(t) + before(t + 1) + before(t + 2) + before(t + 3);
+    for (; t < nc; ++t) rank += before(t);
     if (rank < k) {
       const bool real = ij < a.n && dj == dj && dj != __int_as_float(0x7f800000);
       a.out_d[out_off + rank] = real ? dj : __int_as_float(0x7f800000);
@@ -1615,11 +1702,12 @@ cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap) {
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> g(mu);
   if (dev >= 64 || smem > configured[dev]) {
-    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(finish_kernel<false>),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(reinterpret_cast<const void*>(finish_kernel<true>),
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const void* kernels[4] = {reinterpret_cast<const void*>(finish_kernel<false, false>),
+                              reinterpret_cast<const void*>(finish_kernel<true, false>),
+                              reinterpret_cast<const void*>(finish_kernel<false, true>),
+                              reinterpret_cast<const void*>(finish_kernel<true, true>)};
+    for (const void* f : kernels)
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     if (dev < 64) configured[dev] = smem;
   }
@@ -1635,8 +1723,14 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
   cudaError_t e = finish_prepare(a.dp, a.stage_cap);
   if (e != cudaSuccess) return e;
   const size_t smem = finish_smem_bytes(a.dp, a.stage_cap);
-  return launch_kernel(a.l2 ? finish_kernel<true> : finish_kernel<false>, dim3(grid), dim3(kFinishThreads), smem,
-                       stream, pdl, a);
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const bool wide = grid <= uint32_t(sms);
+  auto* kern = a.l2 ? (wide ? finish_kernel<true, true> : finish_kernel<true, false>)
+                    : (wide ? finish_kernel<false, true> : finish_kernel<false, false>);
+  return launch_kernel(kern, dim3(grid), dim3(kFinishThreads), smem, stream, pdl, a);
 }
 
 cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,

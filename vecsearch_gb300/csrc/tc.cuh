@@ -15,8 +15,9 @@ constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swi
 // for 64 appends between compactions.
 constexpr int kTcMaxShortlist = 448;
 // Entries of the split lists the finish kernel stages in shared memory per query at most; beyond
-// that its passes read the lists in global memory.
-constexpr uint32_t kFinishStageMax = 16384;
+// that its passes read the lists in global memory (192 KB of staging: with the query and the
+// candidate arrays it fits the 227 KB of a CTA for every dim up to 4,096).
+constexpr uint32_t kFinishStageMax = 24576;
 
 // Serving mode: one entry per query of a micro-batch (device memory).
 struct ServeQuery {

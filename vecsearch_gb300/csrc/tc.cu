@@ -1035,17 +1035,20 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     s_dk = __int_as_float(0x7f800000);
   }
   const float* qrow = a.q + size_t(q) * a.ldq;
+  // The query and (for the flat copy below) the lists' lengths load in the same round trip.
+  const bool flat = nsplit <= kStageSplits;
   if (L.cd > 0)
     for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
+  if (flat) {
+    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
+    if (tid == 0) s_off[0] = 0;
+  }
   __syncthreads();
   // ---- 1. stage ----
   // Up to kStageSplits lists: their lengths are scanned into offsets, then every thread copies
   // entries of any list (found by binary search over the offsets), four at a time, so the copy
   // runs with many independent loads in flight. More lists: one list per thread.
-  if (nsplit <= kStageSplits) {
-    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
-    if (tid == 0) s_off[0] = 0;
-    __syncthreads();
+  if (flat) {
     if (warp == 0) {  // inclusive scan of s_off[1 .. nsplit]: lane l sums a run of consecutive lists
       const uint32_t per = (nsplit + 31) / 32;
       const uint32_t b0 = min(nsplit, uint32_t(lane) * per), b1 = min(nsplit, b0 + per);
@@ -1226,32 +1229,30 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     const uint32_t tk = select_key(target);
     cut_key = mg >= 0.f ? order_key(__fadd_ru(key_float(tk), mg)) : tk;
   }
-  // count the entries the cut keeps; more than kRerankMax: keep those strictly below the
-  // kRerankMax-th smallest instead (fewer than kRerankMax)
-  {
-    uint32_t c = 0;
-    each([&](uint32_t key, float, uint32_t) { c += key <= cut_key ? 1u : 0u; });
-    c = __reduce_add_sync(kFull, c);
-    if (lane == 0) atomicAdd(&s_cnt, c);
+  // Collect the entries the cut keeps (the first kRerankMax of them); more than kRerankMax: keep
+  // those strictly below the kRerankMax-th smallest instead (fewer than kRerankMax) and collect
+  // again.
+  auto collect = [&]() {
+    each([&](uint32_t key, float d, uint32_t id) {
+      if (strict ? key < cut_key : key <= cut_key) {
+        const uint32_t slot = atomicAdd(&s_cnt, 1u);
+        if (slot < kRerankMax) {
+          cand_d[slot] = d;
+          cand_i[slot] = id;
+        }
+      }
+    });
     __syncthreads();
-    const uint32_t kept = s_cnt;
-    __syncthreads();
+  };
+  collect();
+  if (s_cnt > kRerankMax) {  // CTA-uniform
+    __syncthreads();  // every thread has read the count
     if (tid == 0) s_cnt = 0;
-    __syncthreads();
-    if (kept > kRerankMax) {
-      cut_key = select_key(kRerankMax);
-      strict = true;
-    }
+    cut_key = select_key(kRerankMax);
+    strict = true;
+    collect();
   }
   // the cut's share of the certificate's L: only when it left an entry out
-  each([&](uint32_t key, float d, uint32_t id) {
-    if (strict ? key < cut_key : key <= cut_key) {
-      const uint32_t slot = atomicAdd(&s_cnt, 1u);
-      cand_d[slot] = d;
-      cand_i[slot] = id;
-    }
-  });
-  __syncthreads();
   const uint32_t nc = s_cnt;  // <= kRerankMax
   const bool cut_left_out = nc < total;
   // ---- 3. rerank ----
@@ -1357,14 +1358,39 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, ui
   const float* s = q + size_t(qq) * ldq;
   __nv_bfloat16* d = qb + size_t(qq) * dp;
   float q2 = 0.f, qb2 = 0.f, r2 = 0.f;
-  for (uint32_t c = lane; c < dp; c += 32) {
-    const float v = c < dim ? s[c] : 0.f;
+  auto one = [&](float v, uint32_t c) {
+    v = c < dim ? v : 0.f;
     const __nv_bfloat16 b = __float2bfloat16_rn(v);
     const float vb = __bfloat162float(b);
     q2 = fmaf(v, v, q2);
     qb2 = fmaf(vb, vb, qb2);
     r2 = fmaf(vb - v, vb - v, r2);
-    d[c] = b;
+    return b;
+  };
+  if ((ldq & 3u) == 0 && (reinterpret_cast<uintptr_t>(q) & 15u) == 0 && (dp & 3u) == 0) {
+    // 16-byte loads, four chunk steps issued before any is used (a 384-dim query in one round trip)
+    const float4* s4 = reinterpret_cast<const float4*>(s);
+    const uint32_t n4 = dp / 4;
+    for (uint32_t c0 = lane; c0 < n4; c0 += 32u * 4u) {
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t c = c0 + 32u * u;
+        v[u] = c < n4 ? s4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t c = c0 + 32u * u;
+        if (c >= n4) break;
+        const __nv_bfloat162 lo = __halves2bfloat162(one(v[u].x, 4 * c), one(v[u].y, 4 * c + 1));
+        const __nv_bfloat162 hi = __halves2bfloat162(one(v[u].z, 4 * c + 2), one(v[u].w, 4 * c + 3));
+        __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(d + 4 * c);
+        d2[0] = lo;
+        d2[1] = hi;
+      }
+    }
+  } else {
+    for (uint32_t c = lane; c < dp; c += 32) d[c] = one(c < dim ? s[c] : 0.f, c);
   }
   for (int o = 16; o > 0; o >>= 1) {
     q2 += __shfl_xor_sync(kFull, q2, o);

@@ -547,12 +547,13 @@ struct vsg_index {
     const size_t slots = size_t(sms);
     vsg::TcArgs a{};
     choose_splits(nqb, vsg::kTcRows, 1024, &a.rows_per_split, &a.nsplit, 1.0, slots);
-    const size_t parts = nq * a.nsplit * kp;
-    part.reserve(parts * 8 + nq * a.nsplit * 4, 0, stream);  // lists, then their lengths
-    // One candidate buffer per CTA.
+    const size_t groups = vsg::tc_groups(kp);  // lists per (query, split)
+    const size_t parts = nq * a.nsplit * groups * kp;
+    part.reserve(parts * 8 + nq * a.nsplit * groups * 4, 0, stream);  // lists, then their lengths
+    // Candidate buffers: one set per epilogue group of each CTA.
     const unsigned grid = unsigned(std::min<size_t>(nqb * a.nsplit, slots));
     const CUtensorMap& rowmap = f8 ? xmap8 : xmap;
-    const size_t cbuf_entries = size_t(grid) * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
+    const size_t cbuf_entries = size_t(grid) * groups * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
     if (f8) {  // (the bf16 queries' launch resets them)
       gthr.reserve(nq * sizeof(uint32_t), 0, stream);
@@ -656,7 +657,8 @@ struct vsg_index {
     fa.out_d = out_dists;
     fa.out_i = out_ids;
     fa.status = status_word();
-    fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * kp));
+    fa.lists_per_split = uint32_t(groups);
+    fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
     if (certify && !f8) {
       fa.thr_init = a.thr_init;
       fa.gthr = a.gthr;

@@ -98,15 +98,17 @@ struct vsg_server {
     std::memset(s.h_in.get(), 0, in_bytes);
     s.d_qb.reserve(cap_q * idx->dp * 2, 0, s.stream);
     s.d_qn.reserve(cap_q * sizeof(float), 0, s.stream);
-    // split lists and their lengths: at most max(cap_q, 128 * SMs) (query, split) pairs of kp_max
-    const size_t pairs = std::max(cap_q, size_t(vsg::kTcQueries) * size_t(idx->sms));
+    // split lists and their lengths: at most max(cap_q, 128 * SMs) (query, split) pairs, each with
+    // tc_groups lists of kp_max
+    const size_t groups = vsg::tc_groups(uint32_t(kp_max));
+    const size_t pairs = std::max(cap_q, size_t(vsg::kTcQueries) * size_t(idx->sms)) * groups;
     s.d_part.reserve(pairs * kp_max * 8 + pairs * 4, 0, s.stream);
     s.d_out.reserve(out_k * 8 + 16, 0, s.stream);
     // sample pass: per query nsplit * sample_tiles * 128 <= max(kSample + one split's tiles, ...) distances
     s.d_sample.reserve(cap_q * sample_per_query * sizeof(float), 0, s.stream);
     s.d_thr.reserve(cap_q * sizeof(float), 0, s.stream);
     // one candidate buffer per CTA of the persistent kernel, one shared threshold per query
-    const size_t cbuf_entries = size_t(idx->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(kp_max));
+    const size_t cbuf_entries = size_t(idx->sms) * groups * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(kp_max));
     s.d_cbuf.reserve(cbuf_entries * 8, 0, s.stream);
     s.d_gthr.reserve(cap_q * sizeof(uint32_t), 0, s.stream);
     s.d_margin.reserve(2 * cap_q * sizeof(float), 0, s.stream);
@@ -171,6 +173,7 @@ struct vsg_server {
     f.hdr = hdr;
     f.sq = sq;
     f.stage_cap = 4096;  // more entries: the finish kernel reads the lists in global memory
+    f.lists_per_split = uint32_t(groups);
     f.fq = static_cast<float*>(s.d_fq.get());  // uncertified queries' rows and filters, for the scan
     f.fmask_ptrs = static_cast<const uint32_t**>(s.d_mptr.get());
     // The fallback scan: gathered queries, their filters by pointer, cap_q queries of which only
@@ -455,10 +458,11 @@ int vsg_server_create(vsg_index* h, size_t max_batch, size_t max_k, size_t slots
     // nsplit * sample_tiles * 128 < kSampleRows + nsplit * 128 <= kSampleRows + 128 * SMs
     s->sample_per_query = kSampleRows + size_t(vsg::kTcRows) * size_t(h->sms);
     // Admission by free HBM: each slot's workspace is fixed; use at most half of what is free.
-    const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms));
+    const size_t groups = vsg::tc_groups(uint32_t(s->kp_max));
+    const size_t pairs = std::max(max_batch, size_t(vsg::kTcQueries) * size_t(h->sms)) * groups;
     const size_t per_slot = s->in_bytes + max_batch * h->dp * 2 + max_batch * 4 + pairs * (s->kp_max * 8 + 4) +
                             s->out_k * 8 + 16 + max_batch * (s->sample_per_query + 2) * sizeof(float) +
-                            size_t(h->sms) * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(s->kp_max)) * 8 +
+                            size_t(h->sms) * groups * vsg::kTcQueries * vsg::tc_buffer_capacity(uint32_t(s->kp_max)) * 8 +
                             max_batch * (3 * sizeof(float) + sizeof(uint32_t) + sizeof(void*)) +  // margins, E, fails
                             max_batch * h->dp * sizeof(float) +                                    // fallback queries
                             max_batch * max_k * 8 * (size_t(s->fb.nsplit) + 1) + size_t(s->fb.nqb) * 4;

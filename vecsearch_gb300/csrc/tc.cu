@@ -41,7 +41,18 @@ namespace vsg {
 
 namespace {
 
-constexpr int kTcThreads = 192;
+// Epilogue groups: with candidate buffers of up to 256 entries (k' <= 120) two groups of four
+// epilogue warps share every accumulator tile, group g taking its columns 128 g .. 128 g + 127,
+// so two warps share each SM sub-partition and a tile's epilogue takes half as long (with one
+// warp per sub-partition the MMAs of the next tile but one waited on it about a fifth of the time
+// at large batches: two accumulators leave the epilogue one tile's MMAs). Each group keeps its
+// own candidate buffers and writes its own list per (query, split). Larger buffers keep one
+// group: the warp sort of 512 entries needs more registers than two groups leave a thread.
+// With two groups the CTA has ten warps: the TMA producer, the MMA issuer and the epilogue
+// warps 2-9 (group 0: warps 2-5, group 1: warps 6-9; warp w reads TMEM lanes 32 (w % 4) ..).
+// Two sub-partitions then hold three warps, so a thread has at most 168 registers.
+__host__ __device__ constexpr int tc_groups_cap(uint32_t cap) { return cap <= 256u ? 2 : 1; }
+__host__ __device__ constexpr int tc_threads_cap(uint32_t cap) { return 64 + 128 * tc_groups_cap(cap); }
 // A row of either operand copy is cut into chunks of 128 bytes (64 bf16 or 128 e4m3 elements).
 constexpr uint32_t kChunkBytes = kTcQueries * 128;    // 16 KB: a chunk of the 128-query block (A)
 constexpr uint32_t kRowChunkBytes = kTcRows * 128;    // 32 KB: a chunk of a 256-row tile (B)
@@ -305,13 +316,12 @@ __device__ __forceinline__ void tmem_wait64(uint32_t (&v)[64]) {
                : "memory");
 }
 
-// v[B + j] for a run-time j in [0, 32): a tree of selects over compile-time indices, so the
-// array stays in registers (an indexed read would move it to local memory).
-template <int B>
-__device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[64], uint32_t j) {
+// v[j] for a run-time j in [0, 32): a tree of selects over compile-time indices, so the array
+// stays in registers (an indexed read would move it to local memory).
+__device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[32], uint32_t j) {
   uint32_t t16[16], t8[8], t4[4], t2[2];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) t16[i] = (j & 16u) ? v[B + 16 + i] : v[B + i];
+  for (int i = 0; i < 16; ++i) t16[i] = (j & 16u) ? v[16 + i] : v[i];
 #pragma unroll
   for (int i = 0; i < 8; ++i) t8[i] = (j & 8u) ? t16[8 + i] : t16[i];
 #pragma unroll
@@ -322,7 +332,7 @@ __device__ __forceinline__ uint32_t pick32(const uint32_t (&v)[64], uint32_t j) 
 }
 
 template <int E, bool L2, bool F8>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
     tc_shortlist_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap xmap,
                         const TcArgs a) {
   extern __shared__ unsigned char smem_raw[];
@@ -348,6 +358,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* stall_bar = done + 2;  // after the TMEM slot word; within the 256 bytes of barriers
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr uint32_t G = uint32_t(tc_groups_cap(32u * E));  // epilogue groups, lists per (query, split)
+  constexpr int kEpi0 = 2;                                    // the first epilogue warp
   const bool persistent = a.hdr != nullptr;
   const uint32_t nq = persistent ? a.hdr->nq : a.nq;
   const uint32_t nqb = persistent ? a.hdr->nqb : a.nqb;
@@ -356,8 +368,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t nitems = persistent ? a.hdr->items : nqb * nsplit;
   constexpr uint32_t cap = 32u * E;
   __shared__ uint32_t item_slot;
-  __shared__ __align__(16) float xs_buf[4][L2 ? kTcRows : 1];  // epilogue warps' row norms of a tile (L2)
-  __shared__ __align__(16) float xsc_buf[4][F8 ? kTcRows : 1];  // ... and row scales (e4m3 copies)
+  __shared__ __align__(16) float xs_buf[4 * G][L2 ? kTcRows : 1];  // epilogue warps' row norms of a tile (L2)
+  __shared__ __align__(16) float xsc_buf[4 * G][F8 ? kTcRows : 1];  // ... and row scales (e4m3 copies)
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -366,7 +378,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+      mbar_init(&tempty[b], 4 * G);  // one arrival per epilogue warp
     }
     mbar_init(afull, 1);
     mbar_init(aempty, 1);
@@ -514,12 +526,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         if (load_a && ok) tc_commit(aempty);  // the block may be replaced once these MMAs are done
       }
-    } else {
+    } else if (warp >= kEpi0) {
       // ---------------- epilogue: one query per thread ----------------
       // Each thread appends scores that beat its query's threshold to the query's buffer (global
       // memory, rarely touched once the threshold is tight); when a buffer may overflow in the
       // next 32 scores, the warp sorts it together and keeps the best kp (the new threshold).
-      const uint32_t quarter = uint32_t(warp & 3);
+      const uint32_t quarter = uint32_t(warp & 3);  // TMEM lanes 32 quarter .. + 31
+      const uint32_t ew = uint32_t(warp - kEpi0);     // epilogue warp 0 .. 4 G - 1
+      const uint32_t group = ew / 4;                  // takes columns [group, group + 1) x 256 / G
       const int m = int(quarter) * 32 + lane;
       const uint32_t qg = qbase + uint32_t(m);
       const bool qvalid = qg < nq;
@@ -532,8 +546,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const float qsc = (F8 && qvalid) ? a.qscale[qg] : 1.f;  // e4m3 copies: the query's scale
       // Certified path: the margin above the kk-th best beyond which no row is needed (-1: none).
       const float mg = (a.margin && qvalid) ? a.margin[qg] : -1.f;
-      float* wd = a.cbuf_d + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;  // this warp's 32 buffers
-      uint32_t* wi = a.cbuf_i + (size_t(blockIdx.x) * kTcQueries + quarter * 32) * cap;
+      // this warp's 32 buffers
+      float* wd = a.cbuf_d + ((size_t(blockIdx.x) * G + group) * kTcQueries + quarter * 32) * cap;
+      uint32_t* wi = a.cbuf_i + ((size_t(blockIdx.x) * G + group) * kTcQueries + quarter * 32) * cap;
       uint32_t* gq = (a.gthr && qvalid && !a.dump) ? a.gthr + qg : nullptr;
       // A sampled threshold bounds the k'-th best from above: rows at or below it are kept.
       float thr_d = (a.thr_init && qvalid) ? a.thr_init[qg] : __int_as_float(0x7f800000);
@@ -561,15 +576,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const bool mine = (lanes >> lane) & 1u;
         float* od = nullptr;
         uint32_t* oi = nullptr;
-        if (final_list && mine) {  // the split's shortlist (lists are a.kp apart)
-          const size_t o = (size_t(qg) * nsplit + split) * a.kp;
+        if (final_list && mine) {  // this group's shortlist of the split (lists are a.kp apart)
+          const size_t o = (size_t(qg) * nsplit * G + size_t(split) * G + group) * a.kp;
           od = a.part_d + o;
           oi = a.part_i + o;
         }
         const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, kk, mg, od, oi, lane);
         if (mine) {
           cnt = r.keep;
-          if (final_list && a.part_n) a.part_n[size_t(qg) * nsplit + split] = r.keep;
+          if (final_list && a.part_n) a.part_n[size_t(qg) * nsplit * G + size_t(split) * G + group] = r.keep;
           if (r.ti != kNone || r.td != __int_as_float(0x7f800000)) {  // a threshold was set
             if (nb_less(r.td, r.ti, thr_d, thr_i)) {
               thr_d = r.td;
@@ -606,7 +621,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-uniform
                        // (a.dump): lanes of padded query slots take it too and store nothing.
 #pragma unroll 1
-          for (uint32_t c = 0; c < kTcRows / 32; ++c) {
+          for (uint32_t c = group * (kTcRows / 32 / G); c < (group + 1) * (kTcRows / 32 / G); ++c) {
             uint32_t v[32];
             tmem_issue32(tbase + c * 32, v);
             tmem_wait32(v);
@@ -633,8 +648,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           // (the largest score, or the smallest distance with the same expression as the
           // append) and one vote per half; the per-score path runs only when some lane may have
           // a candidate.
-          float* xs = xs_buf[quarter];
-          float* xsc = xsc_buf[quarter];
+          float* xs = xs_buf[ew];
+          float* xsc = xsc_buf[ew];
           if constexpr (L2) {
 #pragma unroll
             for (int c = 0; c < kTcRows / 32; ++c)
@@ -647,50 +662,43 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           if (L2 || F8) __syncwarp();
 #pragma unroll 1
-          for (int h = 0; h < kTcRows / 64; ++h) {
-            uint32_t v[64];
-            tmem_issue64(tbase + uint32_t(h) * 64, v);
-            tmem_wait64(v);
-            // Per 32 columns, the entries that may beat the threshold (the prefilter's test) as a
-            // bit mask; one vote per half, and only the columns some lane needs go further.
-            uint32_t bits[2];
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-              const int cg = h * 2 + c;
+          for (int cg = int(group) * (kTcRows / 32 / G); cg < int(group + 1) * (kTcRows / 32 / G); ++cg) {
+            // Room for this chunk's appends, made before its scores are loaded (the out-of-line
+            // sort then runs with few live registers).
+            compact_lanes(__ballot_sync(kFull, cnt + 32 > cap), false);
+            uint32_t v[32];
+            tmem_issue32(tbase + uint32_t(cg) * 32, v);
+            tmem_wait32(v);
+            // The chunk's entries that may beat the threshold (the prefilter's test) as a bit
+            // mask; one vote per 32 columns, and only the columns some lane needs go further.
+            uint32_t bits;
+            {
               uint32_t m[4] = {0u, 0u, 0u, 0u};  // four interleaved chains
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
-                const float sc = F8 ? __uint_as_float(v[c * 32 + j]) * (qsc * xsc[cg * 32 + j])
-                                    : __uint_as_float(v[c * 32 + j]);
+                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * xsc[cg * 32 + j]) : __uint_as_float(v[j]);
                 const bool p = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) <= thr_d : sc >= s_lo;
                 m[j & 3] |= p ? (1u << j) : 0u;
               }
-              bits[c] = (m[0] | m[1] | m[2] | m[3]) & allowed(r0 + uint32_t(cg) * 32);
+              bits = (m[0] | m[1] | m[2] | m[3]) & allowed(r0 + uint32_t(cg) * 32);
             }
-            if (__any_sync(kFull, (bits[0] | bits[1]) != 0u)) {  // rare once the threshold is tight
-#pragma unroll
-              for (int c = 0; c < 2; ++c) {
-                uint32_t cols = __reduce_or_sync(kFull, bits[c]);
-                if (!cols) continue;
-                compact_lanes(__ballot_sync(kFull, cnt + 32 > cap), false);
-                const int cg = h * 2 + c;
-                const uint32_t c0 = r0 + uint32_t(cg) * 32;
-                // Each lane walks its own candidate columns; the scores are still in v, picked
-                // by a select tree. The loop runs as often as the busiest lane needs.
-                uint32_t mine = bits[c];
-                while (__any_sync(kFull, mine != 0u)) {
-                  const bool has = mine != 0u;
-                  const uint32_t j = has ? uint32_t(__ffs(mine) - 1) : 0u;
-                  mine &= mine - 1u;
-                  const float raw = __uint_as_float(c == 0 ? pick32<0>(v, j) : pick32<32>(v, j));
-                  if (has) {
-                    const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
-                    const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
-                    if (nb_less(dist, c0 + j, thr_d, thr_i)) {
-                      wd[size_t(lane) * cap + cnt] = dist;
-                      wi[size_t(lane) * cap + cnt] = c0 + j;
-                      ++cnt;
-                    }
+            if (__any_sync(kFull, bits != 0u)) {  // rare once the threshold is tight
+              const uint32_t c0 = r0 + uint32_t(cg) * 32;
+              // Each lane walks its own candidate columns; the scores are still in v, picked
+              // by a select tree. The loop runs as often as the busiest lane needs.
+              uint32_t mine = bits;
+              while (__any_sync(kFull, mine != 0u)) {
+                const bool has = mine != 0u;
+                const uint32_t j = has ? uint32_t(__ffs(mine) - 1) : 0u;
+                mine &= mine - 1u;
+                const float raw = __uint_as_float(pick32(v, j));
+                if (has) {
+                  const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
+                  const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
+                  if (nb_less(dist, c0 + j, thr_d, thr_i)) {
+                    wd[size_t(lane) * cap + cnt] = dist;
+                    wi[size_t(lane) * cap + cnt] = c0 + j;
+                    ++cnt;
                   }
                 }
               }
@@ -703,7 +711,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (lane == 0) mbar_arrive(&tempty[b]);
       }
       if (a.dump) {  // sample pass: tiles past the split's end read as +inf
-        if (dump_row)
+        if (dump_row && group == 0)
           for (uint32_t j = ntiles * kTcRows; j < sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
       } else {
         // Sort every buffer, keep the best kp and write the split's shortlist.
@@ -1003,7 +1011,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   const bool serving = a.hdr != nullptr;
   if (serving && q >= a.hdr->nq) return;
   if (a.status && *reinterpret_cast<const volatile int*>(a.status) != 0) return;  // lists may be stale
-  const uint32_t nsplit = serving ? a.hdr->nsplit : a.nsplit;
+  const uint32_t nsplit = (serving ? a.hdr->nsplit : a.nsplit) * max(1u, a.lists_per_split);  // lists
   uint32_t k, sel;
   size_t out_off;
   if (serving) {
@@ -1562,7 +1570,7 @@ uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident, bool l2
   // and of row scales (e4m3 copies) per epilogue warp.
   // The deepest ring that fits is taken, so a CTA always uses more than half of an SM's shared
   // memory: one CTA per SM, which owns all 512 TMEM columns (a second CTA would wait for them).
-  const size_t kStatic = 576 + (l2 ? 4 * kTcRows * 4 : 0) + (fp8 ? 4 * kTcRows * 4 : 0);
+  const size_t kStatic = 576 + (l2 ? 8 * kTcRows * 4 : 0) + (fp8 ? 8 * kTcRows * 4 : 0);
   const size_t half = budget / 2 + 1;
   budget = budget > kStatic ? budget - kStatic : 0;
   for (uint32_t s = kMaxTcStages; s >= 3; --s)
@@ -1577,6 +1585,8 @@ uint32_t tc_pick_stages(uint32_t nkc, size_t budget, uint32_t* resident, bool l2
 }
 
 uint32_t tc_buffer_capacity(uint32_t kp) { return tc_capacity(kp); }
+
+uint32_t tc_groups(uint32_t kp) { return uint32_t(tc_groups_cap(tc_capacity(kp))); }
 
 cudaError_t tc_encode_map(CUtensorMap* map, const void* base, uint64_t rows, uint64_t dp, uint32_t box_rows,
                           bool fp8) {
@@ -1640,7 +1650,7 @@ cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap
   const size_t smem = tc_smem_bytes(a.stages, nkc, a.resident);
   const uint32_t cap = tc_capacity(a.kp);
   const TcKernel fn = kTcKernels[a.fp8 ? 1 : 0][a.l2 ? 1 : 0][cap == 64 ? 0 : cap == 128 ? 1 : cap == 256 ? 2 : 3];
-  return launch_kernel(fn, dim3(grid), dim3(kTcThreads), smem, stream, pdl, qmap, xmap, a);
+  return launch_kernel(fn, dim3(grid), dim3(unsigned(tc_threads_cap(cap))), smem, stream, pdl, qmap, xmap, a);
 }
 
 cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp, void* dst,

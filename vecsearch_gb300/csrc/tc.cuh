@@ -117,6 +117,10 @@ cudaError_t launch_serve_scatter(const uint32_t* count, const uint32_t* fail_lis
 // count queries near rows of src (0.9 x_i + 0.1 x_j of its n rows, stride dp), for the autotuner.
 cudaError_t launch_midpoint_rows(float* dst, const float* src, uint32_t dp, uint32_t n, uint32_t count,
                                  cudaStream_t stream);
+// Epilogue groups of the shortlist kernel for a shortlist of kp: each writes its own list per
+// (query, split), so a split has tc_groups(kp) lists (2 for kp <= 120, else 1); the candidate
+// buffers hold tc_groups(kp) x 128 x tc_buffer_capacity(kp) entries per CTA.
+uint32_t tc_groups(uint32_t kp);
 // 128-byte chunks per row of an operand copy: dp bf16 (64 per chunk) or dp e4m3 (128 per chunk).
 uint32_t tc_chunks(uint32_t dp, bool fp8);
 // Shared memory of the shortlist kernel: ring depth, chunks per row, resident query block or not.
@@ -147,7 +151,8 @@ cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t row
 // (stages, nkc, resident); launch_tc_shortlist does it too, but a launch being captured into a
 // CUDA graph should find it done.
 cudaError_t tc_prepare(uint32_t stages, uint32_t nkc, uint32_t resident, bool l2, bool fp8);
-// grid: CTAs (x only); the candidate buffers must hold grid * 128 * tc_buffer_capacity(kp) entries.
+// grid: CTAs (x only); the candidate buffers must hold grid * tc_groups(kp) * 128 *
+// tc_buffer_capacity(kp) entries, the lists nq * nsplit * tc_groups(kp) of kp (and their lengths).
 cudaError_t launch_tc_shortlist(const CUtensorMap& qmap, const CUtensorMap& xmap, const TcArgs& a, unsigned grid,
                                 cudaStream_t stream, bool pdl = false);
 // FP32 -> bf16 rows (stride dp, padding copied as zeros) and, when norms != nullptr, squared norms.
@@ -174,7 +179,7 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
 struct FinishArgs {
   const float* part_d;     // [nq][nsplit][kp] approximate distances, sorted per list
   const uint32_t* part_i;
-  const uint32_t* part_n;  // [nq][nsplit] real entries of each list
+  const uint32_t* part_n;  // [nq][nsplit x lists_per_split] real entries of each list
   uint32_t nq, nsplit, kp, k;  // kp: the lists' stride (<= kTcMaxShortlist) and, without margins, k'
   const float* margin;     // per-query margins (certified path), or nullptr
   const float* x;          // FP32 master rows, n x dp
@@ -192,6 +197,7 @@ struct FinishArgs {
   const ServeHeader* hdr;  // serving mode, or nullptr
   const ServeQuery* sq;
   uint32_t stage_cap;      // list entries staged in shared memory at most (<= kFinishStageMax)
+  uint32_t lists_per_split;  // lists of each split (the shortlist kernel's tc_groups(kp)); 0 = 1
   // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
   // FP32 row into fq row j (stride dp), its per-query mask (qmask row q, mask_ld words) into fmask
   // row j, or (serving) its filter pointer into fmask_ptrs[j]; tally counts them. Each optional.

@@ -104,7 +104,7 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 
 // Sorts the first `cnt` buffered entries of one query (entry j at bd[j] / bi[j], global memory)
 // and keeps the best min(cnt, kp): back into the buffer, or, when out_d is set, into out_d /
-// out_i as a sorted list of kp entries padded with (+inf, none). thr becomes entry kp - 1 when
+// out_i as a sorted list (its length is returned; nothing is written past it). thr becomes entry kp - 1 when
 // cnt >= kp, else (+inf, none). With a margin (mg >= 0) and at least kk entries, thr drops to
 // (entry kk - 1) + mg, rounded up, when that is lower, and only the entries at or below it are
 // kept. Returns the kept count.
@@ -143,14 +143,10 @@ __device__ __forceinline__ uint32_t compact_query(float* bd, uint32_t* bi, uint3
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const uint32_t j = uint32_t(e * 32 + lane);
-      if (j < kp) {
-        out_d[j] = j < keep ? w.d[e] : __int_as_float(0x7f800000);
-        out_i[j] = j < keep ? w.i[e] : kNone;
+      if (j < keep) {
+        out_d[j] = w.d[e];
+        out_i[j] = w.i[e];
       }
-    }
-    for (uint32_t j = uint32_t(32 * E + lane); j < kp; j += 32) {  // a smaller sort than the list
-      out_d[j] = __int_as_float(0x7f800000);
-      out_i[j] = kNone;
     }
   } else {
     __syncwarp();  // every lane has read its entries before any is overwritten
@@ -180,8 +176,12 @@ struct CompactResult {
 template <int E>
 __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsigned lanes, uint32_t cnt,
                                                    uint32_t kp, uint32_t kk, float mg, float* out_d, uint32_t* out_i,
-                                                   int lane) {
+                                                   int lane, float thr_d, uint32_t thr_i) {
   CompactResult r{cnt, __int_as_float(0x7f800000), kNone};
+  // Final lists of many queries at once (large batches) are copied without a sort; a few (small
+  // batches, where the finish kernel's cost follows the lists' lengths) are sorted so that the
+  // margin cut at their own k-th entry shortens them.
+  const bool copy_final = __any_sync(kFull, out_d != nullptr) && __popc(lanes) > 8;  // warp-uniform
   while (lanes) {
     const int src = __ffs(lanes) - 1;
     lanes &= lanes - 1;
@@ -194,9 +194,30 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
     const float m1 = __shfl_sync(kFull, mg, src);
     float* bd = wd + size_t(src) * (32 * E);
     uint32_t* bi = wi + size_t(src) * (32 * E);
-    // The smallest sort that holds the buffered entries (a final list is often short).
     uint32_t keep;
-    if (E > 1 && n <= 32)
+    if (copy_final && n <= k) {
+      // A final list that fits needs no sort (the lists' readers take their entries in any
+      // order): the warp copies the entries at or below the query's threshold, 32 at a time.
+      const float t_d = __shfl_sync(kFull, thr_d, src);
+      const uint32_t t_i = __shfl_sync(kFull, thr_i, src);
+      __syncwarp();  // the lanes' appends are visible to the whole warp
+      keep = 0;
+      for (uint32_t j0 = 0; j0 < n; j0 += 32) {
+        const uint32_t j = j0 + uint32_t(lane);
+        const float dv = j < n ? bd[j] : 0.f;
+        const uint32_t iv = j < n ? bi[j] : kNone;
+        const bool take = j < n && (nb_less(dv, iv, t_d, t_i) || (dv == t_d && iv == t_i));
+        const unsigned bal = __ballot_sync(kFull, take);
+        if (take) {
+          const uint32_t at = keep + __popc(bal & ((1u << lane) - 1u));
+          od[at] = dv;
+          oi[at] = iv;
+        }
+        keep += __popc(bal);
+      }
+      td = __int_as_float(0x7f800000);
+      ti = kNone;
+    } else if (E > 1 && n <= 32)  // else the smallest sort that holds the buffered entries
       keep = compact_query<1>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
     else if (E > 2 && n <= 64)
       keep = compact_query<(E > 2 ? 2 : E)>(bd, bi, n, k, k1, m1, lane, td, ti, od, oi);
@@ -581,7 +602,7 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
           od = a.part_d + o;
           oi = a.part_i + o;
         }
-        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, kk, mg, od, oi, lane);
+        const CompactResult r = compact_warp<E>(wd, wi, lanes, cnt, kp, kk, mg, od, oi, lane, thr_d, thr_i);
         if (mine) {
           cnt = r.keep;
           if (final_list && a.part_n) a.part_n[size_t(qg) * nsplit * G + size_t(split) * G + group] = r.keep;

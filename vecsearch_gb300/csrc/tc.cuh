@@ -177,7 +177,7 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
 // offset from sq, and CTAs past hdr->nq exit. The kernel reads nothing when *status is set (a
 // shortlist kernel gave up and its lists may be stale); row ids >= n are never dereferenced.
 struct FinishArgs {
-  const float* part_d;     // [nq][nsplit][kp] approximate distances, sorted per list
+  const float* part_d;     // [nq][nsplit][kp] approximate distances (part_n of each list, any order)
   const uint32_t* part_i;
   const uint32_t* part_n;  // [nq][nsplit x lists_per_split] real entries of each list
   uint32_t nq, nsplit, kp, k;  // kp: the lists' stride (<= kTcMaxShortlist) and, without margins, k'

@@ -515,6 +515,19 @@ struct vsg_index {
     // Queries to bf16 / e4m3 (rows past nq are zero-filled by the copy engine) and their norms.
     qnorm.reserve(nq * sizeof(float), 0, stream);
     CUtensorMap qmap;
+    // bf16 queries: one launch (bf16 queries and norms, shared thresholds reset, and on the
+    // certified path the bounds E, the margins and the zeroed uncertified count), made below
+    // once it is known whether it also computes the sample (small batches).
+    float* mgn = nullptr;
+    auto launch_prep = [&](const vsg::PrepSample* smp) {
+      VSG_CUDA(vsg::launch_prepare_queries(smp, dq, uint32_t(ldq), uint32_t(nq), uint32_t(dim), uint32_t(dp), qb.get(),
+                                           static_cast<float*>(qnorm.get()), static_cast<uint32_t*>(gthr.get()),
+                                           static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
+                                           float(cert_margin), mgn, mgn ? mgn + nq : nullptr,
+                                           certify ? static_cast<uint32_t*>(fails.get()) : nullptr, s));
+      ++kernel_launches;
+    };
+    bool prep_done = f8;
     if (f8) {
       q8.reserve(nq * dpo, 0, stream);
       q8scale.reserve(nq * sizeof(float), 0, stream);
@@ -523,21 +536,12 @@ struct vsg_index {
       ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, uint32_t(vsg::kTcQueries), true));
     } else {
-      // One launch: bf16 queries and norms, shared thresholds reset, and on the certified path
-      // the bounds E, the margins and the zeroed uncertified count.
       qb.reserve(nq * dp * 2, 0, stream);
       gthr.reserve(nq * sizeof(uint32_t), 0, stream);
-      float* mgn = nullptr;
       if (certify) {
         qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
         mgn = static_cast<float*>(qmargin.get());
       }
-      VSG_CUDA(vsg::launch_prepare_queries(dq, uint32_t(ldq), uint32_t(nq), uint32_t(dim), uint32_t(dp), qb.get(),
-                                           static_cast<float*>(qnorm.get()), static_cast<uint32_t*>(gthr.get()),
-                                           static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
-                                           float(cert_margin), mgn, mgn ? mgn + nq : nullptr,
-                                           certify ? static_cast<uint32_t*>(fails.get()) : nullptr, s));
-      ++kernel_launches;
       VSG_CUDA(vsg::tc_encode_map(&qmap, qb.get(), nq, dp, uint32_t(vsg::kTcQueries)));
       ensure_xmap();
     }
@@ -625,8 +629,22 @@ struct vsg_index {
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
       sa.gthr = nullptr;
-      VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s, pdl));
-      ++kernel_launches;
+      // Certified path, up to 4 queries with ranges sampled: the query preparation computes the
+      // sample in FP32 (one launch less before the main pass). Its k-th distance plus the margin
+      // m = f E (f > 1) still lets at least k sampled rows through (each approximate distance lies
+      // within E of the FP32 one), and every bound the certificate takes stays a bound.
+      const bool fp32_sample = margins && !prep_done && st == 1 && nq <= 4 && nq <= vsg::kPrepSampleQueries &&
+                               dp <= vsg::kPrepSampleDim;
+      if (fp32_sample) {
+        vsg::PrepSample smp{static_cast<const float*>(x.get()), uint32_t(n), sa.rows_per_split, sa.nsplit, sa.dump};
+        launch_prep(&smp);
+        prep_done = true;
+      } else {
+        if (!prep_done) launch_prep(nullptr);
+        prep_done = true;
+        VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s, pdl));
+        ++kernel_launches;
+      }
       // (with margins: the k-th best sampled distance plus the margin)
       VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
                                          margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin,
@@ -634,6 +652,7 @@ struct vsg_index {
       ++kernel_launches;
       a.thr_init = static_cast<const float*>(thr.get());
     }
+    if (!prep_done) launch_prep(nullptr);
     if (tm) VSG_CUDA(cudaEventRecord(tm->ev[0], s));  // the profile times the main pass alone
     VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, a, grid, s, pdl));
     ++kernel_launches;

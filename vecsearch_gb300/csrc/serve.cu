@@ -204,7 +204,7 @@ struct vsg_server {
     VSG_CUDA(vsg::finish_prepare(f.dp, f.stage_cap));
     VSG_CUDA(vsg::scan_prepare(fb.shape, sc.dp, sc.k, sc.stages));
     VSG_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
-    VSG_CUDA(vsg::launch_prepare_queries(dq, uint32_t(idx->dp), uint32_t(cap_q), uint32_t(idx->dp), uint32_t(idx->dp),
+    VSG_CUDA(vsg::launch_prepare_queries(nullptr, dq, uint32_t(idx->dp), uint32_t(cap_q), uint32_t(idx->dp), uint32_t(idx->dp),
                                          s.d_qb.get(), static_cast<float*>(s.d_qn.get()), a.gthr,
                                          static_cast<const float*>(idx->xbound.get()), l2, float(idx->cert_margin),
                                          margin, margin + cap_q, fails, s.stream));

@@ -1364,6 +1364,63 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   if (a.fmask_ptrs && tid == 0) a.fmask_ptrs[j] = serving ? a.sq[q].mask : nullptr;
 }
 
+// FP32 sample blocks of prepare_queries_kernel (small batches, PrepSample): each block takes 32
+// sampled rows, a warp 8 of them; the queries (nq <= 8, padded dim <= 1,024) sit in shared memory.
+// Lane l sums chunks l, l + 32, ... of its row against every query, then a butterfly.
+template <bool L2>
+__device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const float* q, uint32_t ldq, uint32_t nq,
+                                  uint32_t dim, uint32_t dp) {
+  __shared__ float4 qsm[kPrepSampleQueries * kPrepSampleDim / 4];
+  const uint32_t n4 = dp / 4, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t i = threadIdx.x; i < nq * n4; i += blockDim.x) {
+    const uint32_t b = i / n4, c = i % n4;
+    const float* src = q + size_t(b) * ldq + 4 * c;
+    qsm[i] = make_float4(4 * c < dim ? src[0] : 0.f, 4 * c + 1 < dim ? src[1] : 0.f, 4 * c + 2 < dim ? src[2] : 0.f,
+                         4 * c + 3 < dim ? src[3] : 0.f);
+  }
+  __syncthreads();
+  const uint32_t total = smp.ranges * uint32_t(kTcRows);
+  for (uint32_t rr = sb * 32 + warp * 8; rr < min(total, sb * 32 + warp * 8 + 8); ++rr) {
+    const uint32_t row = (rr / kTcRows) * smp.rps + rr % kTcRows;
+    const bool valid = row < smp.n;
+    const float4* x4 = reinterpret_cast<const float4*>(smp.x + size_t(valid ? row : 0) * dp);
+    float acc[kPrepSampleQueries];
+#pragma unroll
+    for (int b = 0; b < int(kPrepSampleQueries); ++b) acc[b] = 0.f;
+    for (uint32_t c = lane; c < n4; c += 32) {
+      const float4 xv = __ldg(x4 + c);
+#pragma unroll
+      for (int b = 0; b < int(kPrepSampleQueries); ++b) {
+        if (uint32_t(b) >= nq) break;
+        const float4 qv = qsm[b * n4 + c];
+        if constexpr (L2) {
+          float e = qv.x - xv.x;
+          acc[b] = fmaf(e, e, acc[b]);
+          e = qv.y - xv.y;
+          acc[b] = fmaf(e, e, acc[b]);
+          e = qv.z - xv.z;
+          acc[b] = fmaf(e, e, acc[b]);
+          e = qv.w - xv.w;
+          acc[b] = fmaf(e, e, acc[b]);
+        } else {
+          acc[b] = fmaf(qv.x, xv.x, acc[b]);
+          acc[b] = fmaf(qv.y, xv.y, acc[b]);
+          acc[b] = fmaf(qv.z, xv.z, acc[b]);
+          acc[b] = fmaf(qv.w, xv.w, acc[b]);
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < int(kPrepSampleQueries); ++b) {
+      if (uint32_t(b) >= nq) break;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(kFull, acc[b], o);
+      if (lane == 0)
+        smp.dump[size_t(b) * total + rr] = valid ? (L2 ? acc[b] : 1.f - acc[b]) : __int_as_float(0x7f800000);
+    }
+  }
+}
+
 // The queries of the bf16 shortlist path, one warp per query: the bf16 copy (stride dp, padding
 // columns zero) and the squared norm, as to_bf16_kernel writes them; the query's shared threshold
 // reset to none (gthr); and, with margins, err[q] = E and margin[q] = factor x E (both rounded
@@ -1378,9 +1435,14 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, ui
                                                               uint32_t dim, uint32_t dp, __nv_bfloat16* qb,
                                                               float* qnorm, uint32_t* gthr, const float* xbound,
                                                               float factor, float* margin, float* err,
-                                                              uint32_t* fails) {
+                                                              uint32_t* fails, PrepSample smp) {
   pdl_trigger();  // the head of a chain of dependent launches: the next kernel may start launching
   pdl_wait();
+  const uint32_t qblocks = (nq + 3) / 4;
+  if (blockIdx.x >= qblocks) {  // FP32 sample blocks (block-uniform)
+    prep_sample_block<L2>(smp, blockIdx.x - qblocks, q, ldq, nq, dim, dp);
+    return;
+  }
   if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
   const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (qq >= nq) return;
@@ -1790,20 +1852,28 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
   return launch_kernel(kern, dim3(grid), dim3(kFinishThreads), smem, stream, pdl, a);
 }
 
-cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,
-                                   float* qnorm, uint32_t* gthr, const float* xbound, bool l2, float factor,
-                                   float* margin, float* err, uint32_t* fails, cudaStream_t stream) {
+cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
+                                   uint32_t dp, void* qb, float* qnorm, uint32_t* gthr, const float* xbound, bool l2,
+                                   float factor, float* margin, float* err, uint32_t* fails, cudaStream_t stream) {
   if (nq == 0) return cudaSuccess;
   if (!q || !qb || ldq < dim || dp < dim || (margin && (!err || !xbound || !(factor >= 0.f))))
     return cudaErrorInvalidValue;
-  const unsigned blocks = (nq + 3) / 4;
+  PrepSample smp{};
+  unsigned blocks = (nq + 3) / 4;
+  if (sample) {
+    if (nq > kPrepSampleQueries || dp > kPrepSampleDim || dp % 4 != 0 || ldq % 4 != 0 || !sample->x ||
+        !sample->dump || sample->ranges == 0 || sample->rps < uint32_t(kTcRows))
+      return cudaErrorInvalidValue;
+    smp = *sample;
+    blocks += (smp.ranges * uint32_t(kTcRows) + 31) / 32;
+  }
   auto* dst = static_cast<__nv_bfloat16*>(qb);
   if (l2)
     prepare_queries_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
-                                                             margin, err, fails);
+                                                             margin, err, fails, smp);
   else
     prepare_queries_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
-                                                              margin, err, fails);
+                                                              margin, err, fails, smp);
   return cudaGetLastError();
 }
 

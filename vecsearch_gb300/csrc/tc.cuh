@@ -215,13 +215,27 @@ cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap);
 // grid: nq, or the largest batch in serving mode.
 cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t stream, bool pdl = false);
 
+// Small batches of the certified path: the sampled distances are computed in FP32 by extra blocks
+// of the query preparation instead of a tensor-core sample pass (one launch less before the main
+// pass). The sample is the first 256 rows of each of `ranges` row ranges of rps rows (rows past n
+// read +inf), written as dump[q * ranges * 256 + r * 256 + j].
+struct PrepSample {
+  const float* x;   // FP32 rows, stride dp
+  uint32_t n, rps, ranges;
+  float* dump;
+};
+// The most queries and the largest padded dim the FP32 sample takes (its queries sit in shared
+// memory: 8 x 1,024 floats).
+constexpr uint32_t kPrepSampleQueries = 8, kPrepSampleDim = 1024;
+
 // The bf16 shortlist path's queries in one launch: bf16 copy qb (stride dp, padding zero) and
 // squared norms qnorm (optional) of the FP32 queries (row stride ldq, dim columns read); gthr[q]
 // reset to 0xFFFFFFFF (optional); with margin set (the certified path), err[q] = the certificate's
 // bound E on |approximate - FP32 distance| over rows whose bf16 copies have the bounds xbound =
 // [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E, both rounded up;
 // and *fails = 0 when fails is set.
-cudaError_t launch_prepare_queries(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim, uint32_t dp, void* qb,
+cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
+                                   uint32_t dp, void* qb,
                                    float* qnorm, uint32_t* gthr, const float* xbound, bool l2, float factor,
                                    float* margin, float* err, uint32_t* fails, cudaStream_t stream);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a

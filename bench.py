@@ -48,21 +48,27 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # DRAM bytes per launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on a 262,144-row case of the same kernel and scaled by rows scanned:
-# reads equal the algorithmic bytes there, so traffic grows in proportion to the rows. Keyed by
-# (kernel, dim, batch, k, metric); None for configurations without a capture.
+# dram__bytes_write.sum) on a 262,144-row case of the same kernel at batch 1, k = 10, cosine:
 #   scan: the FP32 scan kernel, 402.69 MB read + 3.31 MB written per 262,144-row launch
 #   tc:   the certified path's bf16 shortlist main pass, 201.40 MB read + 3.15 MB written
-MEASURED_TRAFFIC_262K = {("scan", 384, 1, 10, "ip"): 406_000_000,
-                         ("tc", 384, 1, 10, "ip"): 204_550_000}
+# The rows dominate (reads equal the algorithmic bytes there), so a launch's traffic is taken as
+# the measured bytes per row times the rows scanned, plus the configuration's own query, norm
+# and list bytes: queries (dim x 4, bf16 copy dim x 2) and, for L2, the rows' norms (4 a row).
+MEASURED_TRAFFIC_262K = {("scan", 384): 406_000_000, ("tc", 384): 204_550_000}
 
 
 def measured_traffic(kernel, n, dim, batch, k, metric):
-    """(bytes per launch scaled to n rows, source) or (None, reason)."""
-    t = MEASURED_TRAFFIC_262K.get((kernel, dim, batch, k, metric))
+    """(bytes per launch for n rows at this batch, k and metric, source) or (None, reason)."""
+    t = MEASURED_TRAFFIC_262K.get((kernel, dim))
     if t is None:
-        return None, "no ncu capture of this configuration"
-    return int(round(t * n / 262_144)), "ncu capture at 262,144 rows, scaled by rows"
+        return None, "no ncu capture of this kernel at this dim"
+    per_row = (t - (dim * 4 if kernel == "scan" else dim * 2)) / 262_144  # less the one query of the capture
+    extra = batch * dim * (4 if kernel == "scan" else 2) + batch * k * 8 + (n * 4 if metric == "l2" and kernel == "tc" else 0)
+    exact = batch == 1 and k == 10 and metric == "ip"
+    src = ("ncu capture at 262,144 rows, scaled by rows" if exact else
+           "ncu capture at 262,144 rows (batch 1, k 10, cosine): bytes per row scaled by rows, plus this "
+           "configuration's query, list and norm bytes")
+    return int(round(per_row * n + extra)), src
 
 
 def parse():

@@ -211,3 +211,21 @@ def test_auto_small_batches_on_large_index(gpu_ready):
     assert gpu.tc_exact_stats()[0] - q0 == 21
     with pytest.raises(ValueError):
         gpu.set_tunable("tc_exact_min_elements", -1)
+
+
+@pytest.mark.parametrize("metric,unit,d", [("cosine", True, 384), ("l2", False, 200), ("cosine", True, 1024)])
+def test_fp32_sample_small_batches(gpu_ready, metric, unit, d):
+    # Up to 4 queries on an index with many splits: the query preparation computes the 4K-row
+    # sample in FP32 (no tensor-core sample pass). Every batch size 1-4, k = 10 and 100 (the k-th
+    # sampled distance decides the start), padded dims 384, 200 and 1,024 (the largest it takes):
+    # the scan kernel's results bit for bit.
+    vsg = gpu_ready
+    x, q = _clustered(150_001, 12, d, 64, unit, 300 + d)
+    gpu = vsg.GpuBruteForceIndex(d, metric)
+    gpu.add(x)
+    for k in (10, 100):
+        want = gpu.search(q, k, method="skinny")
+        for b in (1, 2, 3, 4):
+            for s in range(0, 12, b):
+                got = gpu.search(q[s:s + b], k, method="tc_exact")
+                _same(got, (want[0][s:s + b], want[1][s:s + b]))

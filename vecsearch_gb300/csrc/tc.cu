@@ -981,6 +981,7 @@ constexpr int kFinishThreads = 512;
 constexpr uint32_t kRerankMax = 1024;
 constexpr uint32_t kKeyAll = 0xFFFFFFFFu;  // cut key that keeps every entry
 constexpr uint32_t kStageSplits = 1024;    // lists the flat staging copy handles at most
+constexpr uint32_t kSmallSelect = 256;     // staged entries up to which the cut ranks them in one pass
 
 struct FinishSmem {
   size_t qs, cd, ci, cx, sd, si, total;  // byte offsets: query, candidates (approx, id, exact), staging
@@ -1007,6 +1008,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   __shared__ uint32_t hist[256];
   __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank;
   __shared__ uint32_t s_off[kStageSplits + 1];  // list offsets of the flat staging copy
+  __shared__ uint32_t s_keep, s_gkey;
   __shared__ float s_dk;
   pdl_trigger();
   pdl_wait();
@@ -1054,7 +1056,11 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
   if (flat) {
     for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
-    if (tid == 0) s_off[0] = 0;
+    if (tid == 0) {
+      s_off[0] = 0;
+      s_keep = 0;
+      s_gkey = a.gthr ? a.gthr[q] : kKeyNone;
+    }
   }
   __syncthreads();
   // ---- 1. stage ----
@@ -1083,7 +1089,14 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     __syncthreads();
     const uint32_t tot = s_total;
     if (tot <= a.stage_cap) {
-      for (uint32_t e0 = tid; e0 < tot; e0 += 4 * kFinishThreads) {
+      // Only the entries at or below the query's final shared threshold g are staged: every
+      // split list that published g holds at least its k (or k') entries at or below it, so the
+      // cut and the rerank never need the others, and the certificate's L (which takes g) covers
+      // them. The kept entries are packed by warp (a ballot, one shared atomic per warp).
+      const uint32_t gk = s_gkey;
+      // (warp-uniform trip count: the ballots below need every lane)
+      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += 4 * kFinishThreads) {
+        const uint32_t e0 = w0 + uint32_t(lane);
         float dv[4];
         uint32_t iv[4];
 #pragma unroll
@@ -1106,12 +1119,19 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
           const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
-          if (e < tot) {
-            stg_d[e] = dv[t];
-            stg_i[e] = iv[t];
+          const bool take = e < tot && order_key(dv[t]) <= gk;
+          const unsigned bal = __ballot_sync(kFull, take);
+          uint32_t at = 0;
+          if (lane == 0 && bal) at = atomicAdd(&s_keep, uint32_t(__popc(bal)));
+          at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
+          if (take) {
+            stg_d[at] = dv[t];
+            stg_i[at] = iv[t];
           }
         }
       }
+      __syncthreads();
+      if (tid == 0) s_total = s_keep;
     }
   } else {
     for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
@@ -1160,6 +1180,25 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // ---- 2. the cut ----
   // Exact rank-th smallest key (1 <= rank <= total): CTA-uniform result.
   auto select_key = [&](uint32_t rank) -> uint32_t {
+    if (staged && total <= kSmallSelect) {
+      // Few entries: each thread ranks its own entry against all of them in one pass (shared
+      // reads every thread makes at once), ties by position, so the ranks are a permutation.
+      if (uint32_t(tid) < total) {
+        const uint32_t mine = order_key(stg_d[tid]);
+        uint32_t below = 0, e = 0;
+        auto lt = [&](uint32_t j) -> uint32_t {
+          const uint32_t o = order_key(stg_d[j]);
+          return uint32_t((o < mine) | ((o == mine) & (j < uint32_t(tid))));
+        };
+        for (; e + 4 <= total; e += 4) below += lt(e) + lt(e + 1) + lt(e + 2) + lt(e + 3);
+        for (; e < total; ++e) below += lt(e);
+        if (below + 1 == rank) s_prefix = mine;
+      }
+      __syncthreads();
+      const uint32_t r = s_prefix;
+      __syncthreads();
+      return r;
+    }
     uint32_t lo = 0xFFFFFFFFu, hi = 0u;
     each([&](uint32_t key, float, uint32_t) {
       lo = min(lo, key);

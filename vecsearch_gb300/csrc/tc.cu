@@ -1008,7 +1008,6 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   __shared__ uint32_t hist[256];
   __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank;
   __shared__ uint32_t s_off[kStageSplits + 1];  // list offsets of the flat staging copy
-  __shared__ uint32_t s_keep, s_gkey;
   __shared__ float s_dk;
   pdl_trigger();
   pdl_wait();
@@ -1056,11 +1055,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
   if (flat) {
     for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
-    if (tid == 0) {
-      s_off[0] = 0;
-      s_keep = 0;
-      s_gkey = a.gthr ? a.gthr[q] : kKeyNone;
-    }
+    if (tid == 0) s_off[0] = 0;
   }
   __syncthreads();
   // ---- 1. stage ----
@@ -1089,14 +1084,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     __syncthreads();
     const uint32_t tot = s_total;
     if (tot <= a.stage_cap) {
-      // Only the entries at or below the query's final shared threshold g are staged: every
-      // split list that published g holds at least its k (or k') entries at or below it, so the
-      // cut and the rerank never need the others, and the certificate's L (which takes g) covers
-      // them. The kept entries are packed by warp (a ballot, one shared atomic per warp).
-      const uint32_t gk = s_gkey;
-      // (warp-uniform trip count: the ballots below need every lane)
-      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += 4 * kFinishThreads) {
-        const uint32_t e0 = w0 + uint32_t(lane);
+      for (uint32_t e0 = tid; e0 < tot; e0 += 4 * kFinishThreads) {
         float dv[4];
         uint32_t iv[4];
 #pragma unroll
@@ -1119,19 +1107,12 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
           const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
-          const bool take = e < tot && order_key(dv[t]) <= gk;
-          const unsigned bal = __ballot_sync(kFull, take);
-          uint32_t at = 0;
-          if (lane == 0 && bal) at = atomicAdd(&s_keep, uint32_t(__popc(bal)));
-          at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
-          if (take) {
-            stg_d[at] = dv[t];
-            stg_i[at] = iv[t];
+          if (e < tot) {
+            stg_d[e] = dv[t];
+            stg_i[e] = iv[t];
           }
         }
       }
-      __syncthreads();
-      if (tid == 0) s_total = s_keep;
     }
   } else {
     for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
@@ -1387,13 +1368,17 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   if (a.fmask_ptrs && tid == 0) a.fmask_ptrs[j] = serving ? a.sq[q].mask : nullptr;
 }
 
-// FP32 sample blocks of prepare_queries_kernel (small batches, PrepSample): each block takes 32
-// sampled rows, a warp 8 of them; the queries (nq <= 8, padded dim <= 1,024) sit in shared memory.
-// Lane l sums chunks l, l + 32, ... of its row against every query, then a butterfly.
+// FP32 sample blocks of prepare_queries_kernel (small batches, PrepSample): each block takes
+// kPrepRowsPerBlock sampled rows, a warp two of them with both rows' loads issued before any sum
+// (so every block's loads are in flight at once); the queries (nq <= 8, padded dim <= 1,024) sit
+// in shared memory. Lane l sums chunks l, l + 32, ... of a row against every query, then a
+// butterfly.
+constexpr uint32_t kPrepRowsPerBlock = 8;
 template <bool L2>
 __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const float* q, uint32_t ldq, uint32_t nq,
                                   uint32_t dim, uint32_t dp) {
-  __shared__ float4 qsm[kPrepSampleQueries * kPrepSampleDim / 4];
+  extern __shared__ float4 qsm[];  // nq x dp / 4 (dynamic: only launches with sample blocks have it)
+  constexpr int kMaxC = int(kPrepSampleDim / 4 / 32);  // chunk steps a lane takes at most (8)
   const uint32_t n4 = dp / 4, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t i = threadIdx.x; i < nq * n4; i += blockDim.x) {
     const uint32_t b = i / n4, c = i % n4;
@@ -1403,33 +1388,52 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
   }
   __syncthreads();
   const uint32_t total = smp.ranges * uint32_t(kTcRows);
-  for (uint32_t rr = sb * 32 + warp * 8; rr < min(total, sb * 32 + warp * 8 + 8); ++rr) {
+  const uint32_t rr0 = sb * kPrepRowsPerBlock + warp * 2;
+  if (rr0 >= total) return;
+  float4 xv[2][kMaxC];
+  bool valid[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t rr = rr0 + uint32_t(h);
     const uint32_t row = (rr / kTcRows) * smp.rps + rr % kTcRows;
-    const bool valid = row < smp.n;
-    const float4* x4 = reinterpret_cast<const float4*>(smp.x + size_t(valid ? row : 0) * dp);
+    valid[h] = rr < total && row < smp.n;
+    const float4* x4 = reinterpret_cast<const float4*>(smp.x + size_t(valid[h] ? row : 0) * dp);
+#pragma unroll
+    for (int u = 0; u < kMaxC; ++u) {
+      const uint32_t c = lane + 32u * uint32_t(u);
+      xv[h][u] = c < n4 ? __ldg(x4 + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t rr = rr0 + uint32_t(h);
+    if (rr >= total) break;  // warp-uniform
     float acc[kPrepSampleQueries];
 #pragma unroll
     for (int b = 0; b < int(kPrepSampleQueries); ++b) acc[b] = 0.f;
-    for (uint32_t c = lane; c < n4; c += 32) {
-      const float4 xv = __ldg(x4 + c);
+#pragma unroll
+    for (int u = 0; u < kMaxC; ++u) {
+      const uint32_t c = lane + 32u * uint32_t(u);
+      if (c >= n4) break;
 #pragma unroll
       for (int b = 0; b < int(kPrepSampleQueries); ++b) {
         if (uint32_t(b) >= nq) break;
         const float4 qv = qsm[b * n4 + c];
+        const float4 x = xv[h][u];
         if constexpr (L2) {
-          float e = qv.x - xv.x;
+          float e = qv.x - x.x;
           acc[b] = fmaf(e, e, acc[b]);
-          e = qv.y - xv.y;
+          e = qv.y - x.y;
           acc[b] = fmaf(e, e, acc[b]);
-          e = qv.z - xv.z;
+          e = qv.z - x.z;
           acc[b] = fmaf(e, e, acc[b]);
-          e = qv.w - xv.w;
+          e = qv.w - x.w;
           acc[b] = fmaf(e, e, acc[b]);
         } else {
-          acc[b] = fmaf(qv.x, xv.x, acc[b]);
-          acc[b] = fmaf(qv.y, xv.y, acc[b]);
-          acc[b] = fmaf(qv.z, xv.z, acc[b]);
-          acc[b] = fmaf(qv.w, xv.w, acc[b]);
+          acc[b] = fmaf(qv.x, x.x, acc[b]);
+          acc[b] = fmaf(qv.y, x.y, acc[b]);
+          acc[b] = fmaf(qv.z, x.z, acc[b]);
+          acc[b] = fmaf(qv.w, x.w, acc[b]);
         }
       }
     }
@@ -1439,7 +1443,7 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(kFull, acc[b], o);
       if (lane == 0)
-        smp.dump[size_t(b) * total + rr] = valid ? (L2 ? acc[b] : 1.f - acc[b]) : __int_as_float(0x7f800000);
+        smp.dump[size_t(b) * total + rr] = valid[h] ? (L2 ? acc[b] : 1.f - acc[b]) : __int_as_float(0x7f800000);
     }
   }
 }
@@ -1883,20 +1887,22 @@ cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uin
     return cudaErrorInvalidValue;
   PrepSample smp{};
   unsigned blocks = (nq + 3) / 4;
+  size_t smem = 0;
   if (sample) {
     if (nq > kPrepSampleQueries || dp > kPrepSampleDim || dp % 4 != 0 || ldq % 4 != 0 || !sample->x ||
         !sample->dump || sample->ranges == 0 || sample->rps < uint32_t(kTcRows))
       return cudaErrorInvalidValue;
     smp = *sample;
-    blocks += (smp.ranges * uint32_t(kTcRows) + 31) / 32;
+    blocks += (smp.ranges * uint32_t(kTcRows) + kPrepRowsPerBlock - 1) / kPrepRowsPerBlock;
+    smem = size_t(nq) * dp * sizeof(float);  // <= 32 KB
   }
   auto* dst = static_cast<__nv_bfloat16*>(qb);
   if (l2)
-    prepare_queries_kernel<true><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
-                                                             margin, err, fails, smp);
+    prepare_queries_kernel<true><<<blocks, 128, smem, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound,
+                                                                factor, margin, err, fails, smp);
   else
-    prepare_queries_kernel<false><<<blocks, 128, 0, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound, factor,
-                                                              margin, err, fails, smp);
+    prepare_queries_kernel<false><<<blocks, 128, smem, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound,
+                                                                 factor, margin, err, fails, smp);
   return cudaGetLastError();
 }
 

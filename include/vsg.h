@@ -180,8 +180,8 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   "tc_exact_min_batch" (default 128): method "auto" sends unfiltered batches of at least this
  *   many queries (k <= 32) to VSG_METHOD_TC_EXACT unless the autotuner decided otherwise.
  *   "sample_rows" (default 16384): rows the tensor-core paths score first, per query, for a
- *   starting threshold (batches of 8+ queries; at most 4096 for smaller batches; unless tuned
- *   per batch size).
+ *   starting threshold (batches of 8+ queries with k > 16; at most 4096 for smaller batches or
+ *   k <= 16; unless tuned per batch size).
  *   "tc_exact_min_elements" (default 2^27): unfiltered batches below "tc_exact_min_batch" (k <=
  *   32), down to one query, take VSG_METHOD_TC_EXACT under method "auto" when the index holds at
  *   least this many elements (rows x padded dim): reading the bf16 copy (half the bytes) then
@@ -201,7 +201,12 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   waits up to 2 s for its own copies and MMAs before it exits, whatever this value.
  *   "test_stall_wait" (0 or 1; for testing the failure path): 1 makes the next search's scan or
  *   shortlist kernels first wait on a barrier that nothing completes, so that wait runs out after
- *   "wait_limit_s" and the search returns VSG_ERR_DEVICE_TIMEOUT; it resets to 0 after that search. */
+ *   "wait_limit_s" and the search returns VSG_ERR_DEVICE_TIMEOUT; it resets to 0 after that search.
+ *   "host_graph_max_batch" (default 16, 0 to 1024): vsg_search (unfiltered) of at most this many
+ *   queries, repeated with the same shape (queries, k, method), replays one CUDA graph of the
+ *   whole search, copies included, instead of issuing it call by call; captured on the second
+ *   search of a shape, dropped when rows are added, a tunable or tuning table is set or a buffer is
+ *   reallocated. Results are the same for every value; 0 switches it off. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

@@ -229,3 +229,23 @@ def test_fp32_sample_small_batches(gpu_ready, metric, unit, d):
             for s in range(0, 12, b):
                 got = gpu.search(q[s:s + b], k, method="tc_exact")
                 _same(got, (want[0][s:s + b], want[1][s:s + b]))
+
+
+@pytest.mark.parametrize("metric,unit", [("cosine", True), ("l2", False)])
+def test_tc_exact_neighbours_in_few_splits(gpu_ready, metric, unit):
+    # Rows ordered by cluster: a query's near rows sit in a few splits, so those splits' lists hold
+    # many entries within the finish kernel's bound from the lists' heads (sorted lists are then
+    # read in several runs) while most lists hold none. Batches 1-8 (sorted lists) and 20 (lists
+    # with only their smallest entry first), k = 10, 100 and 128: the scan kernel's results bit
+    # for bit.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    x, labels = D.portable_clustered(200_000, 256, 32, 0.35, seed=310, centroid_seed=311, unit=unit)
+    x = np.ascontiguousarray(x[np.argsort(labels, kind="stable")])
+    q, _ = D.portable_clustered(20, 256, 32, 0.35, seed=312, centroid_seed=311, unit=unit)
+    gpu = vsg.GpuBruteForceIndex(256, metric)
+    gpu.add(x)
+    for k in (10, 100, 128):
+        want = gpu.search(q, k, method="skinny")
+        for b in (1, 3, 8, 20):
+            _same(gpu.search(q[:b], k, method="tc_exact"), (want[0][:b], want[1][:b]))

@@ -130,6 +130,7 @@ int vsg_add(vsg_index* h, const float* rows, size_t m) {
     VSG_CUDA(cudaEventRecord(h->done, h->stream));
     VSG_CUDA(cudaStreamSynchronize(h->stream));
     h->n += m;
+    ++h->config_gen;
   });
 }
 
@@ -281,9 +282,13 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "test_stall_wait") {
       if (value != 0.0 && value != 1.0) throw std::invalid_argument("test_stall_wait must be 0 or 1");
       h->stall_next = value != 0.0;
+    } else if (nm == "host_graph_max_batch") {
+      if (!(value >= 0.0 && value <= 1024.0)) throw std::invalid_argument("host_graph_max_batch must be in [0, 1024]");
+      h->host_graph_max_batch = std::floor(value);
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
+    ++h->config_gen;  // a captured search graph may hold the old value
   });
 }
 
@@ -302,6 +307,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "fallback_split_queries") *value = h->fallback_split_queries;
     else if (nm == "wait_limit_s") *value = h->wait_limit_s;
     else if (nm == "test_stall_wait") *value = h->stall_next ? 1.0 : 0.0;
+    else if (nm == "host_graph_max_batch") *value = h->host_graph_max_batch;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }
@@ -317,6 +323,7 @@ int vsg_autotune_with_queries(vsg_index* h, const float* queries, size_t nq, con
     VSG_CUDA(cudaSetDevice(h->device));
     VSG_CUDA(cudaStreamWaitEvent(h->stream, h->done, 0));
     h->autotune(batches, count, k, method, queries, nq);
+    ++h->config_gen;
     VSG_CUDA(cudaEventRecord(h->done, h->stream));
   });
 }
@@ -393,6 +400,7 @@ int vsg_autotune_load(vsg_index* h, const char* path) {
     std::lock_guard<std::mutex> g(h->mu);
     h->tune_plain = plain;
     h->tune_bf16 = bf16;
+    ++h->config_gen;
   });
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -39,6 +40,10 @@ struct DeviceTimeout : std::runtime_error {
 
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 
+// Counts every (re)allocation of a DeviceBuffer or PinnedBuffer in the process: a CUDA graph
+// captured at one value holds no pointer that has been freed since while the value is the same.
+inline std::atomic<uint64_t> g_alloc_epoch{0};
+
 // Grow-only device buffer, zero-filled when (re)allocated; `keep` bytes of the old
 // contents are copied over (gpu_brute_force.cu:37-56).
 class DeviceBuffer {
@@ -66,6 +71,7 @@ class DeviceBuffer {
     if (p_) cudaFree(p_);
     p_ = raw;
     n_ = bytes;
+    g_alloc_epoch.fetch_add(1);
   }
 
  private:
@@ -89,6 +95,7 @@ class PinnedBuffer {
     if (p_) cudaFreeHost(p_);
     p_ = raw;
     n_ = bytes;
+    g_alloc_epoch.fetch_add(1);
   }
 
  private:
@@ -141,6 +148,7 @@ struct vsg_index {
   uint64_t kernel_launches = 0;    // this index's kernel launches (vsg_kernel_launches)
   DeviceBuffer gthr;  // shortlist kernel: per-query shared thresholds (order keys)
   DeviceBuffer qmargin;  // certified path: per-query margins, then error bounds (launch_prepare_queries)
+  DeviceBuffer prep_ticket;  // the FP32 sample's block ticket (PrepSample), zero between launches
   size_t bf16_rows = 0;
   // Tiled path: an upper bound of the rows' norms (a float's bits) over the first xmax_rows rows,
   // the queries it searched and a device tally of those its certificate left to the scan kernel.
@@ -151,6 +159,25 @@ struct vsg_index {
   const void* xmap_base = nullptr;
   size_t xmap_rows = 0;
   PinnedBuffer pin_in, pin_out;
+  // Blocking host searches (search_host) of one repeated shape replay a CUDA graph of the whole
+  // chain: the copy of the queries in (from pin_in), every kernel, the copy of the result block
+  // out (to pin_out). One launch call queues everything, so the device never waits for the host
+  // between kernels; issuing the chain call by call took ~20 us of host time at batch 1, longer
+  // than the kernels before the main pass. The graph is captured on the second search of a shape
+  // (the first allocates every buffer it needs) and dropped when what it captured may change:
+  // another shape, rows added, a tunable or tuning table set (config_gen), any buffer reallocated
+  // (g_alloc_epoch).
+  struct HostGraph {
+    cudaGraphExec_t exec = nullptr;
+    size_t nq = 0, k = 0, n = 0;
+    uint32_t method = 0;
+    uint64_t gen = 0, epoch = 0;
+    uint64_t launches = 0, tc_queries = 0, tiled_q = 0;  // counted per replay
+    bool ran = false;     // the shape ran once without the graph
+    bool failed = false;  // its capture failed: it runs without a graph
+  } hgraph;
+  uint64_t config_gen = 0;
+  double host_graph_max_batch = 16;  // blocking searches of at most this many queries; 0: none
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
   std::mutex mu;
@@ -217,6 +244,7 @@ struct vsg_index {
       cudaStreamSynchronize(stream);
     }
     destroy_timings();
+    if (hgraph.exec) cudaGraphExecDestroy(hgraph.exec);
     if (done) cudaEventDestroy(done);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -247,6 +275,7 @@ struct vsg_index {
   void reset_after_failure() {
     VSG_CUDA(cudaMemsetAsync(status_word(), 0, sizeof(int), stream));
     if (counters.get()) VSG_CUDA(cudaMemsetAsync(counters.get(), 0, counters.bytes(), stream));
+    if (prep_ticket.get()) VSG_CUDA(cudaMemsetAsync(prep_ticket.get(), 0, prep_ticket.bytes(), stream));
     VSG_CUDA(cudaStreamSynchronize(stream));
   }
 
@@ -394,6 +423,7 @@ struct vsg_index {
     fa.out_d = out_dists;
     fa.out_i = out_ids;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * kp));
+    fa.sorted_lists = 1;  // the tiled kernel keeps every list sorted
     fa.gthr = a.gthr;
     fa.err = mgn + nq;
     fa.fail_count = d_fail;
@@ -599,11 +629,13 @@ struct vsg_index {
     // 8+ queries, 4K below, unless tuned) and start each query at the k'-th best sampled distance, so the
     // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
-    // (smaller batches sample at most 4K rows: the pass costs the same per query, and without it
-    // every row is a candidate until the first compactions)
+    // (smaller batches, and k <= 16, sample at most 4K rows; without a sample every row is a
+    // candidate until the first compactions, which made batch 1 at 1M x 384 21 % slower. Measured
+    // at 1M x 384 on the certified path: k = 10 ran 2.6-4 % faster with 4K than with 16K sampled
+    // rows at batches 8-64, k = 100 up to 1.9x slower)
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
-                         : nq >= 8 ? size_t(sample_rows) : std::min<size_t>(size_t(sample_rows), 4096);
+                         : nq >= 8 && k > 16 ? size_t(sample_rows) : std::min<size_t>(size_t(sample_rows), 4096);
     // After the query preparation the path's kernels run as a chain of programmatic dependent
     // launches (each may start while the one before it finishes); not while profiling, whose
     // events time the main pass on its own.
@@ -629,14 +661,18 @@ struct vsg_index {
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
       sa.gthr = nullptr;
-      // Certified path, up to 4 queries with ranges sampled: the query preparation computes the
-      // sample in FP32 (one launch less before the main pass). Its k-th distance plus the margin
-      // m = f E (f > 1) still lets at least k sampled rows through (each approximate distance lies
-      // within E of the FP32 one), and every bound the certificate takes stays a bound.
+      // Certified path, up to 4 queries with ranges sampled: the query preparation scores the
+      // sample in FP32 and selects the thresholds itself (two launches less before the main pass).
+      // A k-th distance in FP32 plus the margin m = f E (f > 1) still lets at least k sampled rows
+      // through (each approximate distance lies within E of the FP32 one), and every bound the
+      // certificate takes stays a bound.
       const bool fp32_sample = margins && !prep_done && st == 1 && nq <= 4 && nq <= vsg::kPrepSampleQueries &&
-                               dp <= vsg::kPrepSampleDim;
+                               dp <= vsg::kPrepSampleDim && size_t(sa.nsplit) * vsg::kTcRows <= vsg::kPrepSampleRows;
       if (fp32_sample) {
-        vsg::PrepSample smp{static_cast<const float*>(x.get()), uint32_t(n), sa.rows_per_split, sa.nsplit, sa.dump};
+        prep_ticket.reserve(sizeof(uint32_t), 0, stream);  // zero-filled; each launch leaves it zero
+        vsg::PrepSample smp{static_cast<const float*>(x.get()), uint32_t(n), sa.rows_per_split, sa.nsplit,
+                            sa.dump, static_cast<float*>(thr.get()), uint32_t(k),
+                            static_cast<uint32_t*>(prep_ticket.get())};
         launch_prep(&smp);
         prep_done = true;
       } else {
@@ -644,12 +680,12 @@ struct vsg_index {
         prep_done = true;
         VSG_CUDA(vsg::launch_tc_shortlist(qmap, rowmap, sa, sgrid, s, pdl));
         ++kernel_launches;
+        // (with margins: the k-th best sampled distance plus the margin)
+        VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
+                                           margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s,
+                                           a.margin, pdl));
+        ++kernel_launches;
       }
-      // (with margins: the k-th best sampled distance plus the margin)
-      VSG_CUDA(vsg::launch_sample_select(sa.dump, uint32_t(per_query), uint32_t(nq), nullptr,
-                                         margins ? uint32_t(k) : kp, static_cast<float*>(thr.get()), s, a.margin,
-                                         pdl));
-      ++kernel_launches;
       a.thr_init = static_cast<const float*>(thr.get());
     }
     if (!prep_done) launch_prep(nullptr);
@@ -677,6 +713,7 @@ struct vsg_index {
     fa.out_i = out_ids;
     fa.status = status_word();
     fa.lists_per_split = uint32_t(groups);
+    fa.sorted_lists = nq <= vsg::kSortedListQueries ? 1u : 0u;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
     if (certify && !f8) {
       fa.thr_init = a.thr_init;
@@ -1033,9 +1070,104 @@ struct vsg_index {
     return n ? double(best) / double(n) : 0.0;
   }
 
+  void drop_graph() {
+    if (hgraph.exec) cudaGraphExecDestroy(hgraph.exec);
+    hgraph.exec = nullptr;
+  }
+
+  // Captures the chain of an unfiltered blocking search of nq queries (host_graph_search); false
+  // (nothing kept, no error left set) when the chain cannot be captured.
+  bool capture_graph(size_t nq, size_t k, uint32_t method) {
+    drop_graph();
+    pin_in.reserve(nq * dim * sizeof(float));
+    pin_out.reserve(16 + nq * k * 8);
+    reserve_results(nq, k);
+    q.reserve(nq * dp * sizeof(float), 0, stream);
+    const uint64_t l0 = kernel_launches, t0 = tc_exact_queries, i0 = tiled_queries;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    bool ok = true;
+    try {
+      float* dq = static_cast<float*>(q.get());
+      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), pin_in.get(), dim * sizeof(float), dim * sizeof(float), nq,
+                                 cudaMemcpyHostToDevice, stream));
+      enqueue(dq, dp, nq, k, nullptr, false, 0, false, res_ids(), res_dists(nq, k), stream, method, -1.0);
+      VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), 16 + nq * k * 8, cudaMemcpyDeviceToHost, stream));
+    } catch (...) {
+      ok = false;  // (an allocation or a sync inside the chain: capture refuses both)
+    }
+    const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (ok && e == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    hgraph.launches = kernel_launches - l0;
+    hgraph.tc_queries = tc_exact_queries - t0;
+    hgraph.tiled_q = tiled_queries - i0;
+    kernel_launches = l0;  // nothing ran: the replays count
+    tc_exact_queries = t0;
+    tiled_queries = i0;
+    if (!exec) return false;
+    hgraph.exec = exec;
+    hgraph.epoch = g_alloc_epoch.load();
+    return true;
+  }
+
+  // A blocking unfiltered search through the shape's graph; false when it does not apply (the
+  // caller runs the search without it).
+  bool host_graph_search(const float* host_q, size_t nq, size_t k, uint32_t method, uint32_t* out_ids,
+                         float* out_dists) {
+    HostGraph& g = hgraph;
+    if (!(g.nq == nq && g.k == k && g.method == method && g.n == n && g.gen == config_gen)) {
+      drop_graph();  // a new shape: it runs once without a graph, and is captured the next time
+      g.nq = nq;
+      g.k = k;
+      g.method = method;
+      g.n = n;
+      g.gen = config_gen;
+      g.ran = false;
+      g.failed = false;
+      return false;
+    }
+    if (!g.ran || g.failed) return false;
+    VSG_CUDA(cudaSetDevice(device));
+    VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
+    if (!g.exec || g.epoch != g_alloc_epoch.load()) {
+      if (!capture_graph(nq, k, method)) {
+        g.failed = true;
+        return false;
+      }
+    }
+    std::memcpy(pin_in.get(), host_q, nq * dim * sizeof(float));
+    VSG_CUDA(cudaGraphLaunch(g.exec, stream));
+    kernel_launches += g.launches;
+    tc_exact_queries += g.tc_queries;
+    tiled_queries += g.tiled_q;
+    VSG_CUDA(cudaEventRecord(done, stream));
+    VSG_CUDA(cudaStreamSynchronize(stream));
+    const char* h = static_cast<const char*>(pin_out.get());
+    int st = 0;
+    std::memcpy(&st, h, sizeof(int));
+    if (st != 0) {
+      reset_after_failure();
+      throw DeviceTimeout("a search kernel's wait ran past its time limit");
+    }
+    std::memcpy(out_ids, h + 16, nq * k * 4);
+    std::memcpy(out_dists, h + 16 + nq * k * 4, nq * k * 4);
+    return true;
+  }
+
   // Full host-to-host search: stage, enqueue, copy the result block back, check status.
   void search_host(const float* host_q, size_t nq, size_t k, const uint32_t* host_mask, bool per_query,
                    size_t mask_ld, uint32_t* out_ids, float* out_dists, uint32_t method = VSG_METHOD_AUTO) {
+    const bool graphable = !host_mask && !stall_next && !profiling && double(nq) <= host_graph_max_batch;
+    if (graphable) {
+      if (method == VSG_METHOD_BF16 && k <= size_t(vsg::kTcMaxShortlist)) ensure_bf16();
+      if (host_graph_search(host_q, nq, k, method, out_ids, out_dists)) return;
+    }
     VSG_CUDA(cudaSetDevice(device));
     VSG_CUDA(cudaStreamWaitEvent(stream, done, 0));
     reserve_results(nq, k);
@@ -1073,5 +1205,6 @@ struct vsg_index {
     }
     std::memcpy(out_ids, h + 16, nq * k * 4);
     std::memcpy(out_dists, h + 16 + nq * k * 4, nq * k * 4);
+    if (graphable) hgraph.ran = true;  // its buffers exist: the next search of the shape is captured
   }
 };

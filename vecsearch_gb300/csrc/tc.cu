@@ -181,7 +181,8 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
   // Final lists of many queries at once (large batches) are copied without a sort; a few (small
   // batches, where the finish kernel's cost follows the lists' lengths) are sorted so that the
   // margin cut at their own k-th entry shortens them.
-  const bool copy_final = __any_sync(kFull, out_d != nullptr) && __popc(lanes) > 8;  // warp-uniform
+  const bool copy_final =
+      __any_sync(kFull, out_d != nullptr) && __popc(lanes) > int(kSortedListQueries);  // warp-uniform
   while (lanes) {
     const int src = __ffs(lanes) - 1;
     lanes &= lanes - 1;
@@ -196,12 +197,15 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
     uint32_t* bi = wi + size_t(src) * (32 * E);
     uint32_t keep;
     if (copy_final && n <= k) {
-      // A final list that fits needs no sort (the lists' readers take their entries in any
-      // order): the warp copies the entries at or below the query's threshold, 32 at a time.
+      // A final list that fits needs no sort: the warp copies the entries at or below the query's
+      // threshold, 32 at a time, and then swaps the smallest (by order key, then id) to the front,
+      // since the finish kernel bounds the k-th best from the lists' first entries.
       const float t_d = __shfl_sync(kFull, thr_d, src);
       const uint32_t t_i = __shfl_sync(kFull, thr_i, src);
       __syncwarp();  // the lanes' appends are visible to the whole warp
       keep = 0;
+      unsigned long long best = ~0ull;
+      uint32_t best_at = 0;
       for (uint32_t j0 = 0; j0 < n; j0 += 32) {
         const uint32_t j = j0 + uint32_t(lane);
         const float dv = j < n ? bd[j] : 0.f;
@@ -212,8 +216,29 @@ __device__ __noinline__ CompactResult compact_warp(float* wd, uint32_t* wi, unsi
           const uint32_t at = keep + __popc(bal & ((1u << lane) - 1u));
           od[at] = dv;
           oi[at] = iv;
+          const unsigned long long key = (static_cast<unsigned long long>(order_key(dv)) << 32) | iv;
+          if (key < best) {
+            best = key;
+            best_at = at;
+          }
         }
         keep += __popc(bal);
+      }
+      unsigned long long least = best;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(kFull, least, o);
+        least = other < least ? other : least;
+      }
+      const unsigned holder = __ballot_sync(kFull, best == least && least != ~0ull);
+      __syncwarp();  // every lane's copies are visible before the swap reads slot 0
+      if (holder && lane == __ffs(holder) - 1 && best_at != 0) {
+        const float d0 = od[0];
+        const uint32_t i0 = oi[0];
+        od[best_at] = d0;
+        oi[best_at] = i0;
+        od[0] = key_float(uint32_t(best >> 32));
+        oi[0] = uint32_t(best);
       }
       td = __int_as_float(0x7f800000);
       ti = kNone;
@@ -958,11 +983,17 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
 }
 
 // The shortlist path's tail (FinishArgs), one CTA of kFinishThreads per query.
-//   1. Stage: every split's real list entries (part_n of them) are copied into shared memory when
+//   1. Stage: the split lists' real entries (part_n of each) are copied into shared memory when
 //      they fit (stage_cap entries), else the passes below read the lists in global memory. With
 //      up to 1,024 lists the copy is flat: the lengths are scanned into offsets and every thread
 //      copies independent entries (one thread per list left a few threads walking long lists
-//      with dependent loads: most of the kernel's time at batch 1).
+//      with dependent loads). With margins, each list's first entry is its smallest (every
+//      producer writes them so), and these heads come in with the lengths: the k-th smallest head
+//      h bounds the k-th best a_k from above (k lists hold an entry at or below it), so no entry
+//      above c = h + margin can be reranked, and only the lists whose head is at or below c are
+//      read, their entries above c dropped. (At batch 1 the lists held ~2,800 entries for ~70
+//      reranked rows: no split sees enough of the query's near rows for its own k-th best to be
+//      tight.)
 //   2. Cut: the `target`-th smallest approximate distance (k with margins, else the shortlist
 //      size k') by exact radix selection on order keys (a min / max pass, then 8-bit rounds below
 //      the highest bit where the keys differ); the cut is that value, plus the margin (rounded
@@ -971,7 +1002,8 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
 //   3. Rerank: the exact FP32 distance of every kept row with the scan kernel's arithmetic (lane
 //      l sums 16-byte chunks l, l + 32, ... in order, then a butterfly over lanes 16 .. 1), so a
 //      candidate set that holds the true top k yields the scan kernel's results bit for bit.
-//   4. The top k by (FP32 dist, id) by rank counting; the k-th FP32 distance D_k.
+//   4. The top k by (FP32 dist, id): a bitonic sort of (order key, id) pairs in shared memory;
+//      the k-th FP32 distance D_k.
 //   5. Certificate (fail_count set): every row left out has approximate distance >= L = min(sample
 //      threshold, final shared threshold, the cut when it left entries out); if L - E > D_k
 //      (rounded down) no such row can enter the top k, else the query is listed for the scan.
@@ -993,9 +1025,11 @@ __host__ __device__ inline FinishSmem finish_smem(uint32_t dp, uint32_t stage_ca
   L.cd = qbytes;
   L.ci = L.cd + kRerankMax * 4;
   L.cx = L.ci + kRerankMax * 4;
+  // (at least kRerankMax entries: the top-k sort reuses the staging area as 8-byte keys)
+  const size_t stage = stage_cap > kRerankMax ? stage_cap : kRerankMax;
   L.sd = L.cx + kRerankMax * 4;
-  L.si = L.sd + size_t(stage_cap) * 4;
-  L.total = L.si + size_t(stage_cap) * 4;
+  L.si = L.sd + stage * 4;
+  L.total = L.si + stage * 4;
   return L;
 }
 
@@ -1006,7 +1040,7 @@ template <bool L2, bool kWide>
 __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs a) {
   extern __shared__ __align__(16) unsigned char fsm[];
   __shared__ uint32_t hist[256];
-  __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank;
+  __shared__ uint32_t s_total, s_cnt, s_kmin, s_kmax, s_prefix, s_rank, s_all, s_heads, s_staged;
   __shared__ uint32_t s_off[kStageSplits + 1];  // list offsets of the flat staging copy
   __shared__ float s_dk;
   pdl_trigger();
@@ -1046,142 +1080,46 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     s_cnt = 0;
     s_kmin = 0xFFFFFFFFu;
     s_kmax = 0u;
+    s_all = 0;
+    s_heads = 0;
+    s_staged = 0;
     s_dk = __int_as_float(0x7f800000);
   }
   const float* qrow = a.q + size_t(q) * a.ldq;
-  // The query and (for the flat copy below) the lists' lengths load in the same round trip.
+  // The query and (for the flat copy below) the lists' lengths and heads load in the same round
+  // trip; the heads' order keys sit in cand_x until the rerank needs it (kKeyAll: empty list).
   const bool flat = nsplit <= kStageSplits;
+  const bool by_heads = flat && mg >= 0.f;
+  uint32_t* hkey = reinterpret_cast<uint32_t*>(cand_x);
   if (L.cd > 0)
     for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
   if (flat) {
-    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) s_off[sp + 1] = min(lens[sp], a.kp);
+    uint32_t sum = 0, nonempty = 0;
+    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
+      const uint32_t len = min(lens[sp], a.kp);
+      // (read whatever the length: slot 0 of every list exists, and an empty list's is ignored)
+      const float head = by_heads ? a.part_d[base + size_t(sp) * a.kp] : 0.f;
+      s_off[sp + 1] = len;
+      sum += len;
+      nonempty += len ? 1u : 0u;
+      if (by_heads) hkey[sp] = len ? order_key(head) : kKeyAll;
+    }
+    sum = __reduce_add_sync(kFull, sum);
+    nonempty = __reduce_add_sync(kFull, nonempty);
+    if (lane == 0 && sum) {
+      atomicAdd(&s_all, sum);
+      atomicAdd(&s_heads, nonempty);
+    }
     if (tid == 0) s_off[0] = 0;
   }
   __syncthreads();
-  // ---- 1. stage ----
-  // Up to kStageSplits lists: their lengths are scanned into offsets, then every thread copies
-  // entries of any list (found by binary search over the offsets), four at a time, so the copy
-  // runs with many independent loads in flight. More lists: one list per thread.
-  if (flat) {
-    if (warp == 0) {  // inclusive scan of s_off[1 .. nsplit]: lane l sums a run of consecutive lists
-      const uint32_t per = (nsplit + 31) / 32;
-      const uint32_t b0 = min(nsplit, uint32_t(lane) * per), b1 = min(nsplit, b0 + per);
-      uint32_t sum = 0;
-      for (uint32_t i = b0; i < b1; ++i) sum += s_off[i + 1];
-      uint32_t incl = sum;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
-      }
-      uint32_t run = incl - sum;
-      for (uint32_t i = b0; i < b1; ++i) {
-        run += s_off[i + 1];
-        s_off[i + 1] = run;
-      }
-      if (lane == 31) s_total = incl;
-    }
-    __syncthreads();
-    const uint32_t tot = s_total;
-    if (tot <= a.stage_cap) {
-      for (uint32_t e0 = tid; e0 < tot; e0 += 4 * kFinishThreads) {
-        float dv[4];
-        uint32_t iv[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
-          dv[t] = 0.f;
-          iv[t] = 0u;
-          if (e < tot) {  // the list holding entry e: the largest sp with s_off[sp] <= e
-            uint32_t lo = 0, hi = nsplit;
-            while (hi - lo > 1) {
-              const uint32_t mid = (lo + hi) >> 1;
-              if (s_off[mid] <= e) lo = mid;
-              else hi = mid;
-            }
-            const size_t at = base + size_t(lo) * a.kp + (e - s_off[lo]);
-            dv[t] = a.part_d[at];
-            iv[t] = a.part_i[at];
-          }
-        }
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const uint32_t e = e0 + uint32_t(t) * kFinishThreads;
-          if (e < tot) {
-            stg_d[e] = dv[t];
-            stg_i[e] = iv[t];
-          }
-        }
-      }
-    }
-  } else {
-    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
-      const uint32_t len = min(lens[sp], a.kp);
-      if (!len) continue;
-      const uint32_t pos = atomicAdd(&s_total, len);
-      if (pos + len > a.stage_cap) continue;  // too many to stage: the passes read the lists
-      const float* ld = a.part_d + base + size_t(sp) * a.kp;
-      const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
-      for (uint32_t j = 0; j < len; j += 8) {
-        float dv[8];
-        uint32_t iv[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-          dv[t] = j + t < len ? ld[j + t] : 0.f;
-          iv[t] = j + t < len ? li[j + t] : 0u;
-        }
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
-          if (j + t < len) {
-            stg_d[pos + j + t] = dv[t];
-            stg_i[pos + j + t] = iv[t];
-          }
-      }
-    }
-  }
-  __syncthreads();
-  const uint32_t total = s_total;  // CTA-uniform
-  const bool staged = total <= a.stage_cap;
-  // Every entry once, as (order key, approximate distance, id).
-  auto each = [&](auto&& f) {
-    if (staged) {
-      for (uint32_t e = tid; e < total; e += kFinishThreads) f(order_key(stg_d[e]), stg_d[e], stg_i[e]);
-    } else {
-      for (uint32_t sp = warp; sp < nsplit; sp += nwarps) {
-        const uint32_t len = min(lens[sp], a.kp);
-        const float* ld = a.part_d + base + size_t(sp) * a.kp;
-        const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
-        for (uint32_t j = lane; j < len; j += 32) {
-          const float d = ld[j];
-          f(order_key(d), d, li[j]);
-        }
-      }
-    }
-  };
-  // ---- 2. the cut ----
-  // Exact rank-th smallest key (1 <= rank <= total): CTA-uniform result.
-  auto select_key = [&](uint32_t rank) -> uint32_t {
-    if (staged && total <= kSmallSelect) {
-      // Few entries: each thread ranks its own entry against all of them in one pass (shared
-      // reads every thread makes at once), ties by position, so the ranks are a permutation.
-      if (uint32_t(tid) < total) {
-        const uint32_t mine = order_key(stg_d[tid]);
-        uint32_t below = 0, e = 0;
-        auto lt = [&](uint32_t j) -> uint32_t {
-          const uint32_t o = order_key(stg_d[j]);
-          return uint32_t((o < mine) | ((o == mine) & (j < uint32_t(tid))));
-        };
-        for (; e + 4 <= total; e += 4) below += lt(e) + lt(e + 1) + lt(e + 2) + lt(e + 3);
-        for (; e < total; ++e) below += lt(e);
-        if (below + 1 == rank) s_prefix = mine;
-      }
-      __syncthreads();
-      const uint32_t r = s_prefix;
-      __syncthreads();
-      return r;
-    }
+  // ---- 2. the cut (selection; used on the heads first) ----
+  // The rank-th smallest key of `each_key`'s keys (1 <= rank <= their count): exact after enough
+  // 8-bit rounds, or after `rounds` rounds the largest key of the bucket holding it (an upper
+  // bound). CTA-uniform result.
+  auto radix_select = [&](auto&& each_key, uint32_t rank, int rounds) -> uint32_t {
     uint32_t lo = 0xFFFFFFFFu, hi = 0u;
-    each([&](uint32_t key, float, uint32_t) {
+    each_key([&](uint32_t key) {
       lo = min(lo, key);
       hi = max(hi, key);
     });
@@ -1205,13 +1143,13 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     uint32_t mask = lo_bit == 32 ? 0u : (0xFFFFFFFFu << lo_bit);
     uint32_t prefix = kmin & mask;
     uint32_t remaining = rank;
-    while (lo_bit > 0) {
+    for (int round = 0; lo_bit > 0 && round < rounds; ++round) {
       const int nb = min(8, lo_bit);
       const int shift = lo_bit - nb;
       const uint32_t bmask = (1u << nb) - 1u;
       for (int b = tid; b < 256; b += kFinishThreads) hist[b] = 0;
       __syncthreads();
-      each([&](uint32_t key, float, uint32_t) {
+      each_key([&](uint32_t key) {
         if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & bmask], 1u);
       });
       __syncthreads();
@@ -1254,11 +1192,244 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       lo_bit = shift;
       __syncthreads();
     }
-    return prefix;
+    return prefix | ~mask;  // every unresolved bit set: the bucket's largest key (exact when none)
   };
-  uint32_t cut_key = kKeyAll;  // keep entries with key <= cut_key (or < when strict)
+  // The heads' bound c (order key): the k-th smallest head, to 16 bits below the heads' highest
+  // differing bit (rounded up to its bucket's end), plus the margin, rounded up. Fewer than k
+  // non-empty lists: every list is read.
+  uint32_t c_key = kKeyAll;
+  bool direct = false;  // sorted lists under the heads' bound: read in runs (below)
+  if (by_heads && k > 0 && s_heads >= k) {  // CTA-uniform
+    const uint32_t h = radix_select(
+        [&](auto&& f) {
+          for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads)
+            if (hkey[sp] != kKeyAll) f(hkey[sp]);
+        },
+        k, 2);
+    c_key = order_key(__fadd_ru(key_float(h), mg));
+    if (key_float(c_key) != key_float(c_key)) c_key = kKeyAll;  // NaN: no bound
+    // (wide variant only: the shortlist's sorted lists come with at most kSortedListQueries
+    // queries, and the run reader would push the narrow variant past its registers)
+    direct = kWide && a.sorted_lists != 0 && c_key != kKeyAll;
+    if (!direct) {  // only the lists whose head is at or below c are read
+      for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads)
+        if (hkey[sp] > c_key) s_off[sp + 1] = 0;
+      __syncthreads();
+    }
+  }
+  // Appends (d, id) to the staging area when `keep` (warp-uniform call; any order); past
+  // stage_cap nothing is written and the count alone grows (the passes then read the lists).
+  // The row of a kept entry is also prefetched into L2 for the rerank (most kept entries are
+  // reranked; the rows are scattered over HBM, so the rerank's loads otherwise wait on DRAM).
+  auto append = [&](bool keep, float d, uint32_t id) {
+    const unsigned bal = __ballot_sync(kFull, keep);
+    uint32_t at = 0;
+    if (lane == 0 && bal) at = atomicAdd(&s_staged, uint32_t(__popc(bal)));
+    at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
+    if (keep && at < a.stage_cap) {
+      stg_d[at] = d;
+      stg_i[at] = id;
+    }
+    for (unsigned m = bal; m; m &= m - 1) {  // each kept row's 128-byte lines, one a lane
+      const uint32_t rid = __shfl_sync(kFull, id, __ffs(m) - 1);
+      if (rid < a.n) {
+        const char* row = reinterpret_cast<const char*>(a.x + size_t(rid) * a.dp);
+        for (uint32_t b = uint32_t(lane) * 128u; b < a.dp * 4u; b += 32u * 128u)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(row + b));
+      }
+    }
+  };
+  // ---- 1. stage ----
+  // Sorted lists under the heads' bound: the entries at or below c are a prefix of each list
+  // whose head is at or below c, so the lists are read in runs of kDirectRun entries from the
+  // head, every run of every such list at once (no offsets to scan, one round trip a run); a
+  // list whose run ended at or below c with entries left goes on to the next run.
+  // Otherwise, up to kStageSplits lists: their lengths are scanned into offsets, then every thread
+  // copies entries of any list (found by binary search over the offsets), four at a time, so the
+  // copy runs with many independent loads in flight (with the heads' bound, only the entries at
+  // or below c). More lists: one list per thread.
+  if (direct) {
+    constexpr uint32_t kDirectRun = 8;
+    uint32_t* cur = reinterpret_cast<uint32_t*>(cand_d);  // this run's lists (cand_d / cand_i
+    uint32_t* nxt = cand_i;                               // are free until the collection)
+    for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < nsplit; w0 += kFinishThreads) {
+      const uint32_t sp = w0 + uint32_t(lane);
+      const bool take = sp < nsplit && hkey[sp] <= c_key;  // (an empty list's key is above c)
+      const unsigned bal = __ballot_sync(kFull, take);
+      uint32_t at = 0;
+      if (lane == 0 && bal) at = atomicAdd(&s_total, uint32_t(__popc(bal)));
+      at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
+      if (take) cur[at] = sp;
+    }
+    __syncthreads();
+    uint32_t nl = s_total;
+    for (uint32_t j0 = 0; nl > 0; j0 += kDirectRun) {  // CTA-uniform
+      if (tid == 0) s_rank = 0;  // the next run's list count
+      __syncthreads();
+      const uint32_t tot = nl * kDirectRun;
+      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += kFinishThreads) {
+        const uint32_t e = w0 + uint32_t(lane);
+        uint32_t sp = 0, j = 0, len = 0, iv = 0;
+        float dv = 0.f;
+        if (e < tot) {
+          sp = cur[e / kDirectRun];
+          j = j0 + e % kDirectRun;
+          len = s_off[sp + 1];
+          if (j < len) {
+            const size_t at = base + size_t(sp) * a.kp + j;
+            dv = a.part_d[at];
+            iv = a.part_i[at];
+          }
+        }
+        const bool keep = j < len && order_key(dv) <= c_key;
+        append(keep, dv, iv);
+        const bool more = keep && e % kDirectRun == kDirectRun - 1 && j + 1 < len;
+        const unsigned bal = __ballot_sync(kFull, more);
+        uint32_t at = 0;
+        if (lane == 0 && bal) at = atomicAdd(&s_rank, uint32_t(__popc(bal)));
+        at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
+        if (more) nxt[at] = sp;
+      }
+      __syncthreads();
+      nl = s_rank;
+      uint32_t* t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+  } else if (flat) {
+    if (warp == 0) {  // inclusive scan of s_off[1 .. nsplit]: lane l sums a run of consecutive lists
+      const uint32_t per = (nsplit + 31) / 32;
+      const uint32_t b0 = min(nsplit, uint32_t(lane) * per), b1 = min(nsplit, b0 + per);
+      uint32_t sum = 0;
+      for (uint32_t i = b0; i < b1; ++i) sum += s_off[i + 1];
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+      }
+      uint32_t run = incl - sum;
+      for (uint32_t i = b0; i < b1; ++i) {
+        run += s_off[i + 1];
+        s_off[i + 1] = run;
+      }
+      if (lane == 31) s_total = incl;
+    }
+    __syncthreads();
+    const uint32_t tot = s_total;
+    if (tot <= a.stage_cap) {
+      // (warp-uniform loop: the heads' filter appends with one ballot per step)
+      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += 4 * kFinishThreads) {
+        float dv[4];
+        uint32_t iv[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const uint32_t e = w0 + uint32_t(lane) + uint32_t(t) * kFinishThreads;
+          dv[t] = 0.f;
+          iv[t] = 0u;
+          if (e < tot) {  // the list holding entry e: the largest sp with s_off[sp] <= e
+            uint32_t lo = 0, hi = nsplit;
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (s_off[mid] <= e) lo = mid;
+              else hi = mid;
+            }
+            const size_t at = base + size_t(lo) * a.kp + (e - s_off[lo]);
+            dv[t] = a.part_d[at];
+            iv[t] = a.part_i[at];
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const uint32_t e = w0 + uint32_t(lane) + uint32_t(t) * kFinishThreads;
+          if (c_key != kKeyAll) {  // CTA-uniform
+            append(e < tot && order_key(dv[t]) <= c_key, dv[t], iv[t]);
+          } else if (e < tot) {
+            stg_d[e] = dv[t];
+            stg_i[e] = iv[t];
+          }
+        }
+      }
+    }
+  } else {
+    for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads) {
+      const uint32_t len = min(lens[sp], a.kp);
+      if (!len) continue;
+      const uint32_t pos = atomicAdd(&s_total, len);
+      if (pos + len > a.stage_cap) continue;  // too many to stage: the passes read the lists
+      const float* ld = a.part_d + base + size_t(sp) * a.kp;
+      const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
+      for (uint32_t j = 0; j < len; j += 8) {
+        float dv[8];
+        uint32_t iv[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          dv[t] = j + t < len ? ld[j + t] : 0.f;
+          iv[t] = j + t < len ? li[j + t] : 0u;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (j + t < len) {
+            stg_d[pos + j + t] = dv[t];
+            stg_i[pos + j + t] = iv[t];
+          }
+      }
+    }
+  }
+  __syncthreads();
+  // all: every list entry; total: the entries the passes below take (the staged ones, or every
+  // list entry when the lists to read did not fit). CTA-uniform.
+  const uint32_t all = flat ? s_all : s_total;
+  const bool staged = direct ? s_staged <= a.stage_cap : s_total <= a.stage_cap;
+  const uint32_t total = !staged ? all : c_key != kKeyAll ? s_staged : s_total;
+  // Every entry once, as (order key, approximate distance, id).
+  auto each = [&](auto&& f) {
+    if (staged) {
+      for (uint32_t e = tid; e < total; e += kFinishThreads) f(order_key(stg_d[e]), stg_d[e], stg_i[e]);
+    } else {
+      for (uint32_t sp = warp; sp < nsplit; sp += nwarps) {
+        const uint32_t len = min(lens[sp], a.kp);
+        const float* ld = a.part_d + base + size_t(sp) * a.kp;
+        const uint32_t* li = a.part_i + base + size_t(sp) * a.kp;
+        for (uint32_t j = lane; j < len; j += 32) {
+          const float d = ld[j];
+          f(order_key(d), d, li[j]);
+        }
+      }
+    }
+  };
+  // ---- 2. the cut ----
+  // Exact rank-th smallest key (1 <= rank <= total): CTA-uniform result.
+  auto select_key = [&](uint32_t rank) -> uint32_t {
+    if (staged && total <= kSmallSelect) {
+      // Few entries: each thread ranks its own entry against all of them in one pass (shared
+      // reads every thread makes at once), ties by position, so the ranks are a permutation.
+      if (uint32_t(tid) < total) {
+        const uint32_t mine = order_key(stg_d[tid]);
+        uint32_t below = 0, e = 0;
+        auto lt = [&](uint32_t j) -> uint32_t {
+          const uint32_t o = order_key(stg_d[j]);
+          return uint32_t((o < mine) | ((o == mine) & (j < uint32_t(tid))));
+        };
+        for (; e + 4 <= total; e += 4) below += lt(e) + lt(e + 1) + lt(e + 2) + lt(e + 3);
+        for (; e < total; ++e) below += lt(e);
+        if (below + 1 == rank) s_prefix = mine;
+      }
+      __syncthreads();
+      const uint32_t r = s_prefix;
+      __syncthreads();
+      return r;
+    }
+    return radix_select([&](auto&& f) { each([&](uint32_t key, float, uint32_t) { f(key); }); }, rank, 4);
+  };
+  // keep entries with key <= cut_key (or < when strict); the heads' bound c already left out every
+  // entry above it. A staged set no larger than one rerank pass is reranked whole: the exact cut
+  // would not save a pass.
+  constexpr int G = kWide ? 6 : 4;  // rows per warp in flight in the rerank (96 a pass when wide)
+  uint32_t cut_key = c_key;
   bool strict = false;
-  if (total > target) {
+  const bool whole = c_key != kKeyAll && staged && total <= uint32_t(G * nwarps);
+  if (total > target && !whole) {
     const uint32_t tk = select_key(target);
     cut_key = mg >= 0.f ? order_key(__fadd_ru(key_float(tk), mg)) : tk;
   }
@@ -1287,11 +1458,10 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   }
   // the cut's share of the certificate's L: only when it left an entry out
   const uint32_t nc = s_cnt;  // <= kRerankMax
-  const bool cut_left_out = nc < total;
+  const bool cut_left_out = nc < all;
   // ---- 3. rerank ----
   const float4* q4 = reinterpret_cast<const float4*>(L.cd > 0 ? qs : qrow);
   const uint32_t nch = a.dp / 4;
-  constexpr int G = 4;  // rows per warp in flight
   for (uint32_t j0 = warp; j0 < nc; j0 += G * nwarps) {
     const float4* x4[G];
 #pragma unroll
@@ -1312,25 +1482,50 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   }
   __syncthreads();
   // ---- 4. top k by (FP32 dist, id) ----
-  for (uint32_t j = tid; j < nc; j += kFinishThreads) {
-    const float dj = cand_x[j];
-    const uint32_t ij = cand_i[j];
-    // rank = entries before (dj, ij) in (dist, id, position) order; branch-free and unrolled, so
-    // the shared-memory loads overlap
-    auto before = [&](uint32_t t) -> uint32_t {
-      const float xt = cand_x[t];
-      const uint32_t it = cand_i[t];
-      return uint32_t((xt < dj) | ((xt == dj) & ((it < ij) | ((it == ij) & (t < j)))));
-    };
-    uint32_t rank = 0, t = 0;
-    for (; t + 4 <= nc; t += 4) rank += before(t) + before(t + 1) + before(t + 2) + before(t + 3);
-    for (; t < nc; ++t) rank += before(t);
-    if (rank < k) {
-      const bool real = ij < a.n && dj == dj && dj != __int_as_float(0x7f800000);
-      a.out_d[out_off + rank] = real ? dj : __int_as_float(0x7f800000);
-      a.out_i[out_off + rank] = real ? ij : kNone;
+  // Each candidate's rank among (order key of the distance, id) pairs, counted against all of them
+  // (one 8-byte shared load each, the same address across the warp; equal pairs ranked by
+  // position, so the ranks are a permutation). The pairs sit in the staging area, free once the
+  // candidates are collected (at least kRerankMax x 8 bytes). A NaN distance ranks as +inf (written
+  // as a missing result) and -0 as +0: the order is the float order of the distances, then ids.
+  {
+    unsigned long long* sk = reinterpret_cast<unsigned long long*>(fsm + L.sd);
+    for (uint32_t j = tid; j < nc; j += kFinishThreads) {
+      float dj = cand_x[j] + 0.f;  // -0 -> +0
+      if (dj != dj) dj = __int_as_float(0x7f800000);
+      sk[j] = (static_cast<unsigned long long>(order_key(dj)) << 32) | cand_i[j];
     }
-    if (rank + 1 == k) s_dk = dj;
+    __syncthreads();
+    // gs consecutive lanes share one candidate, each counting every gs-th pair (then a butterfly
+    // over the group), so few candidates still keep every warp busy: the count is a chain of
+    // dependent compares, slow on one warp per scheduler.
+    uint32_t gs = 1;
+    while (gs < 32 && gs * 2 * nc <= kFinishThreads) gs *= 2;
+    const uint32_t part = uint32_t(tid) & (gs - 1);
+    for (uint32_t j0 = 0; j0 < nc; j0 += kFinishThreads / gs) {  // CTA-uniform
+      const uint32_t j = j0 + uint32_t(tid) / gs;
+      const unsigned long long kj = j < nc ? sk[j] : 0ull;
+      uint32_t rank = 0;
+      if (j < nc) {
+        const uint32_t cnt = (nc - part + gs - 1) / gs;  // pairs part, part + gs, ...
+#pragma unroll 4
+        for (uint32_t i = 0; i < cnt; ++i) {
+          const uint32_t t = part + i * gs;
+          const unsigned long long kt = sk[t];
+          rank += uint32_t(kt < kj) | (uint32_t(kt == kj) & uint32_t(t < j));
+        }
+      }
+      for (uint32_t o = 1; o < gs; o <<= 1) rank += __shfl_xor_sync(kFull, rank, int(o));
+      if (j < nc && part == 0) {
+        const float dj = key_float(uint32_t(kj >> 32));
+        const uint32_t ij = uint32_t(kj);
+        if (rank < k) {
+          const bool real = ij < a.n && dj != __int_as_float(0x7f800000);
+          a.out_d[out_off + rank] = real ? dj : __int_as_float(0x7f800000);
+          a.out_i[out_off + rank] = real ? ij : kNone;
+        }
+        if (rank + 1 == k) s_dk = dj;
+      }
+    }
   }
   for (uint32_t j = nc + tid; j < k; j += kFinishThreads) {  // fewer than k candidates: pad
     a.out_d[out_off + j] = __int_as_float(0x7f800000);
@@ -1389,7 +1584,10 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
   __syncthreads();
   const uint32_t total = smp.ranges * uint32_t(kTcRows);
   const uint32_t rr0 = sb * kPrepRowsPerBlock + warp * 2;
-  if (rr0 >= total) return;
+  __shared__ float wmin[kPrepRowsPerBlock / 2][kPrepSampleQueries];  // per warp and query
+  if (lane < kPrepSampleQueries) wmin[warp][lane] = __int_as_float(0x7f800000);
+  __syncwarp();
+  if (rr0 < total) {  // warp-uniform
   float4 xv[2][kMaxC];
   bool valid[2];
 #pragma unroll
@@ -1442,9 +1640,151 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
       if (uint32_t(b) >= nq) break;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(kFull, acc[b], o);
-      if (lane == 0)
-        smp.dump[size_t(b) * total + rr] = valid[h] ? (L2 ? acc[b] : 1.f - acc[b]) : __int_as_float(0x7f800000);
+      if (lane == 0 && valid[h]) wmin[warp][b] = fminf(wmin[warp][b], L2 ? acc[b] : 1.f - acc[b]);
     }
+  }
+  }
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    float m = wmin[0][threadIdx.x];
+#pragma unroll
+    for (int w = 1; w < int(kPrepRowsPerBlock / 2); ++w) m = fminf(m, wmin[w][threadIdx.x]);
+    const uint32_t blocks = (total + kPrepRowsPerBlock - 1) / kPrepRowsPerBlock;
+    smp.bmin[size_t(threadIdx.x) * blocks + sb] = m;
+  }
+}
+
+// The end of every block of a query preparation with an FP32 sample: a ticket, and the last block
+// to take one selects each query's threshold from the sample blocks' minima (PrepSample). Up to
+// four queries at a time, with the whole block on each (4 minima a thread per query, in
+// registers): a min / max pass over the keys, then two 8-bit histogram rounds below their highest
+// differing bit (warp q scans query q's histogram); the bucket's largest key bounds the k-th
+// smallest from above. Only thread 0 fences, after the block's barrier (the barrier orders the
+// block's writes before its fence), on both sides of the ticket.
+constexpr int kSelPer = int(kPrepSampleRows / kPrepRowsPerBlock / 128);  // minima a thread holds per query (4)
+__device__ void prep_sample_select(const PrepSample& smp, uint32_t nq, uint32_t blocks, const float* margin) {
+  __shared__ uint32_t hist[4][256];
+  __shared__ uint32_t s_lo[4], s_hi[4], s_prefix[4], s_mask[4], s_rank[4], s_active[4];
+  __shared__ int s_shift[4];
+  __shared__ uint32_t s_last;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  __syncthreads();  // this block's minima and margins are written
+  if (tid == 0) {
+    __threadfence();
+    s_last = atomicAdd(smp.ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+    if (s_last) {
+      __threadfence();  // every other block's writes, before the reads below
+      *smp.ticket = 0;  // every block has taken its ticket: ready for the next launch
+    }
+  }
+  __syncthreads();
+  if (!s_last) return;
+  const bool fits = smp.k >= 1 && smp.k <= blocks && blocks <= 128u * kSelPer;  // CTA-uniform
+  for (uint32_t q0 = 0; q0 < nq; q0 += 4) {  // CTA-uniform
+    const uint32_t nqs = min(nq - q0, 4u);
+    uint32_t key[4][kSelPer];  // kKeyNone past the end: never counted
+#pragma unroll
+    for (int qi = 0; qi < 4; ++qi)
+#pragma unroll
+      for (int i = 0; i < kSelPer; ++i) {
+        const uint32_t j = tid + 128u * uint32_t(i);
+        key[qi][i] = (fits && uint32_t(qi) < nqs && j < blocks)
+                         ? order_key(__ldcg(smp.bmin + size_t(q0 + uint32_t(qi)) * blocks + j))
+                         : kKeyNone;
+      }
+    if (tid < 4) {
+      s_lo[tid] = 0xFFFFFFFFu;
+      s_hi[tid] = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int qi = 0; qi < 4; ++qi) {
+      uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+#pragma unroll
+      for (int i = 0; i < kSelPer; ++i)
+        if (key[qi][i] != kKeyNone) {
+          lo = min(lo, key[qi][i]);
+          hi = max(hi, key[qi][i]);
+        }
+      lo = __reduce_min_sync(kFull, lo);
+      hi = __reduce_max_sync(kFull, hi);
+      if (lane == 0 && uint32_t(qi) < nqs) {
+        atomicMin(&s_lo[qi], lo);
+        atomicMax(&s_hi[qi], hi);
+      }
+    }
+    __syncthreads();
+    if (tid < nqs) {  // each query's starting prefix: the bits above the highest differing one
+      const uint32_t diff = s_lo[tid] ^ s_hi[tid];
+      const int top = diff ? 31 - __clz(diff) : 0;
+      s_active[tid] = (fits && diff) ? 1u : 0u;
+      s_shift[tid] = max(top - 7, 0);
+      s_mask[tid] = top == 31 ? 0u : (0xFFFFFFFFu << (top + 1));
+      s_prefix[tid] = s_lo[tid] & s_mask[tid];
+      s_rank[tid] = smp.k;
+    }
+    __syncthreads();
+    for (int round = 0; round < 2; ++round) {
+      for (uint32_t b = tid; b < 4u * 256u; b += blockDim.x) (&hist[0][0])[b] = 0;
+      __syncthreads();
+#pragma unroll
+      for (int qi = 0; qi < 4; ++qi) {
+        if (uint32_t(qi) >= nqs || !s_active[qi]) continue;
+        const uint32_t mask = s_mask[qi], prefix = s_prefix[qi];
+        const int shift = s_shift[qi];
+#pragma unroll
+        for (int i = 0; i < kSelPer; ++i)
+          if (key[qi][i] != kKeyNone && (key[qi][i] & mask) == prefix)
+            atomicAdd(&hist[qi][(key[qi][i] >> shift) & 255u], 1u);
+      }
+      __syncthreads();
+      if (w < nqs && s_active[w]) {  // warp q: the first bucket of query q whose running count reaches its rank
+        const uint32_t rank = s_rank[w];
+        uint32_t c[8], sum = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          c[i] = hist[w][lane * 8 + i];
+          sum += c[i];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t u = __shfl_up_sync(kFull, incl, o);
+          if (lane >= uint32_t(o)) incl += u;
+        }
+        const unsigned reach = __ballot_sync(kFull, incl >= rank);
+        const int src = reach ? __ffs(reach) - 1 : 31;
+        if (int(lane) == src) {
+          uint32_t rr = rank - (incl - sum), bi = 7;
+          bool found = false;
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!found) {
+              if (c[i] >= rr || i == 7) {
+                bi = uint32_t(i);
+                found = true;
+              } else {
+                rr -= c[i];
+              }
+            }
+          const int shift = s_shift[w];
+          s_prefix[w] |= (lane * 8u + bi) << shift;
+          s_mask[w] |= 0xFFu << shift;
+          s_rank[w] = rr;
+          if (shift == 0) s_active[w] = 0;  // every bit resolved
+          s_shift[w] = max(shift - 8, 0);
+        }
+      }
+      __syncthreads();
+    }
+    if (tid < nqs) {
+      const uint32_t diff = s_lo[tid] ^ s_hi[tid];
+      // the bucket's largest key (every unresolved bit set); equal keys: the key itself
+      const float t = !fits ? __int_as_float(0x7f800000) : key_float(diff ? (s_prefix[tid] | ~s_mask[tid]) : s_lo[tid]);
+      smp.thr[q0 + tid] =
+          t != t ? __int_as_float(0x7f800000) : margin ? __fadd_ru(t, __ldcg(margin + q0 + tid)) : t;
+    }
+    __syncthreads();  // the shared state is reused by the next four queries
   }
 }
 
@@ -1458,18 +1798,10 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
 // nearly every query while keeping about half the rows of 2 E. The first thread also zeroes the
 // uncertified-query count.
 template <bool L2>
-__global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, uint32_t ldq, uint32_t nq,
-                                                              uint32_t dim, uint32_t dp, __nv_bfloat16* qb,
-                                                              float* qnorm, uint32_t* gthr, const float* xbound,
-                                                              float factor, float* margin, float* err,
-                                                              uint32_t* fails, PrepSample smp) {
-  pdl_trigger();  // the head of a chain of dependent launches: the next kernel may start launching
-  pdl_wait();
-  const uint32_t qblocks = (nq + 3) / 4;
-  if (blockIdx.x >= qblocks) {  // FP32 sample blocks (block-uniform)
-    prep_sample_block<L2>(smp, blockIdx.x - qblocks, q, ldq, nq, dim, dp);
-    return;
-  }
+__device__ __forceinline__ void prepare_query_warp(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
+                                                   uint32_t dp, __nv_bfloat16* qb, float* qnorm, uint32_t* gthr,
+                                                   const float* xbound, float factor, float* margin, float* err,
+                                                   uint32_t* fails) {
   if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
   const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (qq >= nq) return;
@@ -1524,6 +1856,25 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, ui
       margin[qq] = __fmul_ru(factor, e);
     }
   }
+}
+
+// The query preparation: one warp per query in the first ceil(nq / 4) blocks, the FP32 sample
+// (PrepSample, when set) in the blocks after them.
+template <bool L2>
+__global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, uint32_t ldq, uint32_t nq,
+                                                              uint32_t dim, uint32_t dp, __nv_bfloat16* qb,
+                                                              float* qnorm, uint32_t* gthr, const float* xbound,
+                                                              float factor, float* margin, float* err,
+                                                              uint32_t* fails, PrepSample smp) {
+  pdl_trigger();  // the head of a chain of dependent launches: the next kernel may start launching
+  pdl_wait();
+  const uint32_t qblocks = (nq + 3) / 4;
+  if (blockIdx.x >= qblocks) {  // FP32 sample blocks (block-uniform)
+    prep_sample_block<L2>(smp, blockIdx.x - qblocks, q, ldq, nq, dim, dp);
+  } else {
+    prepare_query_warp<L2>(q, ldq, nq, dim, dp, qb, qnorm, gthr, xbound, factor, margin, err, fails);
+  }
+  if (smp.thr) prep_sample_select(smp, nq, gridDim.x - qblocks, margin);
 }
 
 // One CTA per query: an upper bound of the kp-th smallest of `count` values, by radix selection
@@ -1890,7 +2241,8 @@ cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uin
   size_t smem = 0;
   if (sample) {
     if (nq > kPrepSampleQueries || dp > kPrepSampleDim || dp % 4 != 0 || ldq % 4 != 0 || !sample->x ||
-        !sample->dump || sample->ranges == 0 || sample->rps < uint32_t(kTcRows))
+        !sample->bmin || !sample->thr || !sample->ticket || sample->ranges == 0 ||
+        sample->ranges * uint32_t(kTcRows) > kPrepSampleRows || sample->rps < uint32_t(kTcRows))
       return cudaErrorInvalidValue;
     smp = *sample;
     blocks += (smp.ranges * uint32_t(kTcRows) + kPrepRowsPerBlock - 1) / kPrepRowsPerBlock;

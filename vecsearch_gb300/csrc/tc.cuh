@@ -18,6 +18,11 @@ constexpr int kTcMaxShortlist = 448;
 // that its passes read the lists in global memory (192 KB of staging: with the query and the
 // candidate arrays it fits the 227 KB of a CTA for every dim up to 4,096).
 constexpr uint32_t kFinishStageMax = 24576;
+// The shortlist kernel writes a query's final list of a split sorted by (dist, id) when the warp
+// that holds the query has at most this many real queries (few queries: the sort lets the margin
+// cut shorten the list), else unsorted with its smallest entry first. So a batch of at most this
+// many queries has sorted lists only.
+constexpr uint32_t kSortedListQueries = 8;
 
 // Serving mode: one entry per query of a micro-batch (device memory).
 struct ServeQuery {
@@ -177,7 +182,8 @@ cudaError_t launch_to_bf16(const float* src, size_t ld_src, size_t rows, uint32_
 // offset from sq, and CTAs past hdr->nq exit. The kernel reads nothing when *status is set (a
 // shortlist kernel gave up and its lists may be stale); row ids >= n are never dereferenced.
 struct FinishArgs {
-  const float* part_d;     // [nq][nsplit][kp] approximate distances (part_n of each list, any order)
+  const float* part_d;     // [nq][nsplit][kp] approximate distances (part_n of each list; its
+                           // smallest by (order key, id) first, the rest in any order)
   const uint32_t* part_i;
   const uint32_t* part_n;  // [nq][nsplit x lists_per_split] real entries of each list
   uint32_t nq, nsplit, kp, k;  // kp: the lists' stride (<= kTcMaxShortlist) and, without margins, k'
@@ -198,6 +204,7 @@ struct FinishArgs {
   const ServeQuery* sq;
   uint32_t stage_cap;      // list entries staged in shared memory at most (<= kFinishStageMax)
   uint32_t lists_per_split;  // lists of each split (the shortlist kernel's tc_groups(kp)); 0 = 1
+  uint32_t sorted_lists;     // 1: every list is sorted by (dist, id) (kSortedListQueries)
   // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
   // FP32 row into fq row j (stride dp), its per-query mask (qmask row q, mask_ld words) into fmask
   // row j, or (serving) its filter pointer into fmask_ptrs[j]; tally counts them. Each optional.
@@ -215,18 +222,27 @@ cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap);
 // grid: nq, or the largest batch in serving mode.
 cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t stream, bool pdl = false);
 
-// Small batches of the certified path: the sampled distances are computed in FP32 by extra blocks
-// of the query preparation instead of a tensor-core sample pass (one launch less before the main
-// pass). The sample is the first 256 rows of each of `ranges` row ranges of rps rows (rows past n
-// read +inf), written as dump[q * ranges * 256 + r * 256 + j].
+// Small batches of the certified path: the sample is scored in FP32 by extra blocks of the query
+// preparation, and its threshold selected there too, instead of a tensor-core sample pass and a
+// select launch (two launches less before the main pass). The sample is the first 256 rows of
+// each of `ranges` row ranges of rps rows (rows past n read +inf); each sample block writes, per
+// query, the smallest distance of its rows to bmin[q * blocks + block]. The last block to finish
+// (a ticket counter, zero between launches) sets thr[q] = the k-th smallest of the query's block
+// minima, rounded up to 16 bits below their highest differing bit, plus the query's margin:
+// k blocks each hold a row at or below it, so it bounds the k-th best FP32 distance from above.
 struct PrepSample {
   const float* x;   // FP32 rows, stride dp
   uint32_t n, rps, ranges;
-  float* dump;
+  float* bmin;      // nq x sample blocks
+  float* thr;       // nq thresholds out
+  uint32_t k;
+  uint32_t* ticket; // zero before the launch; the last block sets it back to zero
 };
 // The most queries and the largest padded dim the FP32 sample takes (its queries sit in shared
 // memory: 8 x 1,024 floats).
 constexpr uint32_t kPrepSampleQueries = 8, kPrepSampleDim = 1024;
+// The most sampled rows it takes (ranges x 256): the last block selects from 512 block minima.
+constexpr uint32_t kPrepSampleRows = 4096;
 
 // The bf16 shortlist path's queries in one launch: bf16 copy qb (stride dp, padding zero) and
 // squared norms qnorm (optional) of the FP32 queries (row stride ldq, dim columns read); gthr[q]

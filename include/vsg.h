@@ -180,8 +180,8 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   "tc_exact_min_batch" (default 128): method "auto" sends unfiltered batches of at least this
  *   many queries (k <= 32) to VSG_METHOD_TC_EXACT unless the autotuner decided otherwise.
  *   "sample_rows" (default 16384): rows the tensor-core paths score first, per query, for a
- *   starting threshold (batches of 8+ queries with k > 16; at most 4096 for smaller batches or
- *   k <= 16; unless tuned per batch size).
+ *   starting threshold (batches of 8+ queries; at most 4096 for smaller batches, and for batches
+ *   of up to 64 queries with k <= 16; unless tuned per batch size).
  *   "tc_exact_min_elements" (default 2^27): unfiltered batches below "tc_exact_min_batch" (k <=
  *   32), down to one query, take VSG_METHOD_TC_EXACT under method "auto" when the index holds at
  *   least this many elements (rows x padded dim): reading the bf16 copy (half the bytes) then

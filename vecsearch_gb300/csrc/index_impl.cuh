@@ -629,13 +629,15 @@ struct vsg_index {
     // 8+ queries, 4K below, unless tuned) and start each query at the k'-th best sampled distance, so the
     // main pass keeps only rows that can still make the shortlist.
     const uint32_t tiles_per_split = uint32_t(ceil_div(a.rows_per_split, size_t(vsg::kTcRows)));
-    // (smaller batches, and k <= 16, sample at most 4K rows; without a sample every row is a
-    // candidate until the first compactions, which made batch 1 at 1M x 384 21 % slower. Measured
-    // at 1M x 384 on the certified path: k = 10 ran 2.6-4 % faster with 4K than with 16K sampled
-    // rows at batches 8-64, k = 100 up to 1.9x slower)
+    // (batches under 8 queries, and batches of up to 64 with k <= 16, sample at most 4K rows;
+    // without a sample every row is a candidate until the first compactions, which made batch 1 at
+    // 1M x 384 21 % slower. Measured at 1M x 384 on the certified path: k = 10 ran 2.6-4 % faster
+    // with 4K than with 16K sampled rows at batches 8-64, but 6 % slower at 1024, where the
+    // epilogue sets the pace and a looser start costs appends; k = 100 up to 1.9x slower with 4K)
+    const bool small_sample = nq < 8 || (k <= 16 && nq <= 64);
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
-                         : nq >= 8 && k > 16 ? size_t(sample_rows) : std::min<size_t>(size_t(sample_rows), 4096);
+                         : small_sample ? std::min<size_t>(size_t(sample_rows), 4096) : size_t(sample_rows);
     // After the query preparation the path's kernels run as a chain of programmatic dependent
     // launches (each may start while the one before it finishes); not while profiling, whose
     // events time the main pass on its own.

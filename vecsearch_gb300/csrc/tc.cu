@@ -56,6 +56,7 @@ __host__ __device__ constexpr int tc_threads_cap(uint32_t cap) { return 64 + 128
 // A row of either operand copy is cut into chunks of 128 bytes (64 bf16 or 128 e4m3 elements).
 constexpr uint32_t kChunkBytes = kTcQueries * 128;    // 16 KB: a chunk of the 128-query block (A)
 constexpr uint32_t kRowChunkBytes = kTcRows * 128;    // 32 KB: a chunk of a 256-row tile (B)
+constexpr uint32_t kL2Ahead = 8;  // row chunks a CTA prefetches into L2 past its ring before its first wait
 constexpr uint32_t kTmemCols = 2 * kTcRows;           // two accumulators: all 512 columns
 constexpr int kMaxTcStages = 8;
 
@@ -281,6 +282,13 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// Brings the box at (x, y) of a tensor map into L2 (no shared memory, no barrier).
+__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y)
+               : "memory");
+}
+
 __device__ __forceinline__ uint64_t policy_evict_last() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -497,6 +505,12 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
         uint32_t c0 = 0;
         if (!waited) {  // first item: rows before the wait, the query block after it
           for (const uint32_t pre = min(nch, stages); c0 < pre && ok; ++c0) issue_rows(c0);
+          // The next kL2Ahead chunks into L2 as well: at small batches HBM idles while the query
+          // preparation runs, and these are the first bytes the ring asks for after the wait.
+          for (uint32_t c = c0; c < min(nch, c0 + kL2Ahead); ++c) {
+            const uint32_t tile = row_begin / kTcRows + c / nkc, kc = c % nkc;
+            tma_prefetch_l2(&xmap, 0, int((tile * nkc + kc) * kTcRows));
+          }
           pdl_wait();
           waited = true;
         }
@@ -1659,9 +1673,16 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
 // four queries at a time, with the whole block on each (4 minima a thread per query, in
 // registers): a min / max pass over the keys, then two 8-bit histogram rounds below their highest
 // differing bit (warp q scans query q's histogram); the bucket's largest key bounds the k-th
-// smallest from above. Only thread 0 fences, after the block's barrier (the barrier orders the
-// block's writes before its fence), on both sides of the ticket.
+// smallest from above. Only thread 0 takes the ticket, with an acquire-release atomic after the
+// block's barrier (the barrier orders the block's writes before it). Equal bins within a warp are
+// added once (a match over the warp): most minima fall into two or three bins, where one shared
+// atomic per value serialized for 1.3 us a round.
 constexpr int kSelPer = int(kPrepSampleRows / kPrepRowsPerBlock / 128);  // minima a thread holds per query (4)
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
 __device__ void prep_sample_select(const PrepSample& smp, uint32_t nq, uint32_t blocks, const float* margin) {
   __shared__ uint32_t hist[4][256];
   __shared__ uint32_t s_lo[4], s_hi[4], s_prefix[4], s_mask[4], s_rank[4], s_active[4];
@@ -1670,12 +1691,8 @@ __device__ void prep_sample_select(const PrepSample& smp, uint32_t nq, uint32_t 
   const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   __syncthreads();  // this block's minima and margins are written
   if (tid == 0) {
-    __threadfence();
-    s_last = atomicAdd(smp.ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
-    if (s_last) {
-      __threadfence();  // every other block's writes, before the reads below
-      *smp.ticket = 0;  // every block has taken its ticket: ready for the next launch
-    }
+    s_last = atomic_add_acq_rel(smp.ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+    if (s_last) *smp.ticket = 0;  // every block has taken its ticket: ready for the next launch
   }
   __syncthreads();
   if (!s_last) return;
@@ -1729,13 +1746,16 @@ __device__ void prep_sample_select(const PrepSample& smp, uint32_t nq, uint32_t 
       __syncthreads();
 #pragma unroll
       for (int qi = 0; qi < 4; ++qi) {
-        if (uint32_t(qi) >= nqs || !s_active[qi]) continue;
+        if (uint32_t(qi) >= nqs || !s_active[qi]) continue;  // CTA-uniform
         const uint32_t mask = s_mask[qi], prefix = s_prefix[qi];
         const int shift = s_shift[qi];
 #pragma unroll
-        for (int i = 0; i < kSelPer; ++i)
-          if (key[qi][i] != kKeyNone && (key[qi][i] & mask) == prefix)
-            atomicAdd(&hist[qi][(key[qi][i] >> shift) & 255u], 1u);
+        for (int i = 0; i < kSelPer; ++i) {
+          const bool in = key[qi][i] != kKeyNone && (key[qi][i] & mask) == prefix;
+          const uint32_t bin = in ? (key[qi][i] >> shift) & 255u : 256u;  // 256: not counted
+          const unsigned same = __match_any_sync(kFull, bin);
+          if (in && lane == uint32_t(__ffs(same) - 1)) atomicAdd(&hist[qi][bin], uint32_t(__popc(same)));
+        }
       }
       __syncthreads();
       if (w < nqs && s_active[w]) {  // warp q: the first bucket of query q whose running count reaches its rank

@@ -228,8 +228,8 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
 // each of `ranges` row ranges of rps rows (rows past n read +inf); each sample block writes, per
 // query, the smallest distance of its rows to bmin[q * blocks + block]. The last block to finish
 // (a ticket counter, zero between launches) sets thr[q] = the k-th smallest of the query's block
-// minima, rounded up to 16 bits below their highest differing bit, plus the query's margin:
-// k blocks each hold a row at or below it, so it bounds the k-th best FP32 distance from above.
+// minima plus the query's margin: k blocks each hold a row at or below it, so it bounds the k-th
+// best FP32 sampled distance from above.
 struct PrepSample {
   const float* x;   // FP32 rows, stride dp
   uint32_t n, rps, ranges;

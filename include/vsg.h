@@ -206,7 +206,9 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   queries, repeated with the same shape (queries, k, method), replays one CUDA graph of the
  *   whole search, copies included, instead of issuing it call by call; captured on the second
  *   search of a shape, dropped when rows are added, a tunable or tuning table is set or a buffer is
- *   reallocated. Results are the same for every value; 0 switches it off. */
+ *   reallocated. Results are the same for every value; 0 switches it off.
+ *   "host_graph_direct" (default 1, 0 or 1): in those graphs the certified path's kernels read
+ *   the queries from the pinned staging buffer themselves instead of a copy into device memory. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

@@ -29,6 +29,7 @@ def test_replays_equal_call_by_call(gpu_ready, method):
     ref.add(x)
     ref.set_tunable("host_graph_max_batch", 0)
     assert gpu.get_tunable("host_graph_max_batch") == 16
+    gpu.set_tunable("host_graph_direct", 0)  # the copy into device memory (direct reads: below)
     for b, k in ((1, 10), (3, 100), (16, 10)):
         launches = []
         for rep in range(6):  # call by call, captured, then replays, each with other queries
@@ -39,6 +40,27 @@ def test_replays_equal_call_by_call(gpu_ready, method):
         # the capture and the replays count the graph's kernels (the first call may also build
         # the index's bf16 copy)
         assert min(launches) > 0 and len(set(launches[1:])) == 1 and launches[0] >= launches[1]
+
+
+def test_direct_queries_equal_copied(gpu_ready):
+    # host_graph_direct (the default): the certified path's kernels read the queries from the
+    # pinned staging buffer themselves (no copy in); padded rows (dim 37 -> 40) included. The
+    # copied form is checked by test_replays_equal_call_by_call with direct reads off.
+    vsg = gpu_ready
+    from vecsearch_gb300 import datasets as D
+    for d in (200, 37):
+        x, _ = D.portable_clustered(120_000, d, 64, 0.35, seed=620 + d, centroid_seed=621)
+        q, _ = D.portable_clustered(24, d, 64, 0.35, seed=622 + d, centroid_seed=621)
+        gpu = vsg.GpuBruteForceIndex(d, "cosine")
+        gpu.add(x)
+        assert gpu.get_tunable("host_graph_direct") == 1
+        for b, k in ((1, 10), (4, 100)):
+            want = gpu.search(q, k, method="skinny")
+            for rep in range(5):
+                s = (rep * b) % 20
+                _same(gpu.search(q[s:s + b], k, method="tc_exact"), (want[0][s:s + b], want[1][s:s + b]))
+    with pytest.raises(ValueError):
+        gpu.set_tunable("host_graph_direct", 2)
 
 
 def test_graph_dropped_on_changes(gpu_ready):

@@ -249,3 +249,26 @@ def test_tc_exact_neighbours_in_few_splits(gpu_ready, metric, unit):
         want = gpu.search(q, k, method="skinny")
         for b in (1, 3, 8, 20):
             _same(gpu.search(q[:b], k, method="tc_exact"), (want[0][:b], want[1][:b]))
+
+
+@pytest.mark.parametrize("metric,unit,d", [("cosine", True, 384), ("l2", False, 200)])
+def test_tc_exact_over_e4m3_copy(gpu_ready, metric, unit, d):
+    # "cert_fp8_max_batch": small batches of the certified path read the e4m3 copy (one scale per
+    # row and per query) with a bound E that covers its roundings; a wider margin keeps more rows
+    # (about a whole cluster of these ~290-row clusters; clusters larger than the finish kernel's
+    # 2,048 reranked rows would leave the queries to the scan), and the results are still the scan
+    # kernel's bit for bit. Batches 1-4 (FP32 sample) and 8 (tensor-core sample), k = 10 and 100.
+    vsg = gpu_ready
+    x, q = _clustered(150_000, 24, d, 512, unit, 330 + d)
+    gpu = vsg.GpuBruteForceIndex(d, metric)
+    gpu.add(x)
+    gpu.set_tunable("cert_fp8_max_batch", 8)
+    for k in (10, 100):
+        want = gpu.search(q, k, method="skinny")
+        for b in (1, 3, 8):
+            for s in range(0, 16, b):
+                _same(gpu.search(q[s:s + b], k, method="tc_exact"), (want[0][s:s + b], want[1][s:s + b]))
+    q0, s0, f0 = gpu.tc_exact_stats()
+    gpu.search(q[:8], 10, method="tc_exact")
+    q1, s1, f1 = gpu.tc_exact_stats()
+    assert q1 - q0 == 8 and s1 - s0 <= 2  # the certificate holds for nearly every query

@@ -285,6 +285,12 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "host_graph_max_batch") {
       if (!(value >= 0.0 && value <= 1024.0)) throw std::invalid_argument("host_graph_max_batch must be in [0, 1024]");
       h->host_graph_max_batch = std::floor(value);
+    } else if (nm == "cert_fp8_max_batch") {
+      if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("cert_fp8_max_batch must be in [0, 2^20]");
+      h->cert_fp8_max_batch = std::floor(value);
+    } else if (nm == "host_graph_direct") {
+      if (value != 0.0 && value != 1.0) throw std::invalid_argument("host_graph_direct must be 0 or 1");
+      h->host_graph_direct = value;
     } else {
       throw std::invalid_argument("unknown tunable '" + nm + "'");
     }
@@ -308,6 +314,8 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "wait_limit_s") *value = h->wait_limit_s;
     else if (nm == "test_stall_wait") *value = h->stall_next ? 1.0 : 0.0;
     else if (nm == "host_graph_max_batch") *value = h->host_graph_max_batch;
+    else if (nm == "host_graph_direct") *value = h->host_graph_direct;
+    else if (nm == "cert_fp8_max_batch") *value = h->cert_fp8_max_batch;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

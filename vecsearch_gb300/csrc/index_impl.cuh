@@ -134,6 +134,7 @@ struct vsg_index {
   // method "fp8": e4m3 copy of the rows (cap x dp8 bytes, dp8 = dim rounded up to 16), one FP32
   // scale per row, FP32 squared norms; e4m3 query staging and query scales.
   DeviceBuffer x8, x8scale, x8norm, q8, q8scale;
+  DeviceBuffer xbound8;  // the e4m3 rows' rounding bounds (certified path over the e4m3 copy)
   size_t fp8_rows = 0;
   CUtensorMap xmap8{};
   const void* xmap8_base = nullptr;
@@ -175,9 +176,15 @@ struct vsg_index {
     uint64_t launches = 0, tc_queries = 0, tiled_q = 0;  // counted per replay
     bool ran = false;     // the shape ran once without the graph
     bool failed = false;  // its capture failed: it runs without a graph
+    bool direct = false;  // the kernels read the queries in pin_in (stride dp) themselves
   } hgraph;
   uint64_t config_gen = 0;
   double host_graph_max_batch = 16;  // blocking searches of at most this many queries; 0: none
+  // Certified searches of at most this many queries read the e4m3 copy of the rows (0: none).
+  double cert_fp8_max_batch = 0;
+  // 1: on the certified path the graph's kernels read the queries straight from the pinned
+  // staging buffer (no copy in; measured 1.5 us less a blocking search at batch 1)
+  double host_graph_direct = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // last queued search on this index (any stream)
   std::mutex mu;
@@ -486,9 +493,12 @@ struct vsg_index {
     x8.reserve(need, vsg::tc_tiled_bytes(keep, d8, true), stream);
     x8scale.reserve(cap * sizeof(float), keep * sizeof(float), stream);
     x8norm.reserve(cap * sizeof(float), keep * sizeof(float), stream);
+    xbound8.reserve(16, 0, stream);
+    if (keep == 0) VSG_CUDA(cudaMemsetAsync(xbound8.get(), 0, 16, stream));  // every row is converted again
     VSG_CUDA(vsg::launch_to_fp8(static_cast<const float*>(x.get()) + keep * dp, dp, n - keep, uint32_t(dim), d8,
                                 x8.get(), static_cast<float*>(x8scale.get()) + keep,
-                                static_cast<float*>(x8norm.get()) + keep, stream, keep));
+                                static_cast<float*>(x8norm.get()) + keep, stream, keep,
+                                static_cast<float*>(xbound8.get())));
     ++kernel_launches;
     VSG_CUDA(cudaStreamSynchronize(stream));
     fp8_rows = n;
@@ -524,13 +534,12 @@ struct vsg_index {
   void enqueue_bf16(const float* dq, size_t ldq, size_t nq, size_t k, uint32_t* out_ids, float* out_dists,
                     cudaStream_t s, bool certify = false, uint32_t kp_force = 0, bool f8 = false,
                     const uint32_t* dmask = nullptr, size_t mask_ld = 0) {
-    if (certify && f8) throw std::invalid_argument("the certificate is for the bf16 copy");
     const uint32_t kp = kp_force ? kp_force : certify ? exact_shortlist_size(k) : shortlist_size(k);
     // The operand copy, its norms (and rounding bounds or scales) cover every row before any
     // kernel reads them.
     if (f8) {
       ensure_fp8();
-      if (!x8.get() || !x8scale.get() || !x8norm.get() || fp8_rows != n)
+      if (!x8.get() || !x8scale.get() || !x8norm.get() || !xbound8.get() || fp8_rows != n)
         throw std::runtime_error("the e4m3 copy of the rows is missing");
     } else {
       ensure_bf16();
@@ -545,20 +554,30 @@ struct vsg_index {
     // Queries to bf16 / e4m3 (rows past nq are zero-filled by the copy engine) and their norms.
     qnorm.reserve(nq * sizeof(float), 0, stream);
     CUtensorMap qmap;
-    // bf16 queries: one launch (bf16 queries and norms, shared thresholds reset, and on the
-    // certified path the bounds E, the margins and the zeroed uncertified count), made below
-    // once it is known whether it also computes the sample (small batches).
+    // bf16 queries (and e4m3 queries on the certified path): one launch (the queries and their
+    // norms, shared thresholds reset, and on the certified path the bounds E, the margins and the
+    // zeroed uncertified count), made below once it is known whether it also computes the sample
+    // (small batches).
     float* mgn = nullptr;
     auto launch_prep = [&](const vsg::PrepSample* smp) {
-      VSG_CUDA(vsg::launch_prepare_queries(smp, dq, uint32_t(ldq), uint32_t(nq), uint32_t(dim), uint32_t(dp), qb.get(),
-                                           static_cast<float*>(qnorm.get()), static_cast<uint32_t*>(gthr.get()),
-                                           static_cast<const float*>(xbound.get()), metric == VSG_METRIC_L2,
-                                           float(cert_margin), mgn, mgn ? mgn + nq : nullptr,
-                                           certify ? static_cast<uint32_t*>(fails.get()) : nullptr, s));
+      VSG_CUDA(vsg::launch_prepare_queries(smp, dq, uint32_t(ldq), uint32_t(nq), uint32_t(dim), uint32_t(dp),
+                                           f8 ? q8.get() : qb.get(), static_cast<float*>(qnorm.get()),
+                                           static_cast<uint32_t*>(gthr.get()),
+                                           static_cast<const float*>(f8 ? xbound8.get() : xbound.get()),
+                                           metric == VSG_METRIC_L2, float(cert_margin), mgn, mgn ? mgn + nq : nullptr,
+                                           certify ? static_cast<uint32_t*>(fails.get()) : nullptr, s,
+                                           f8 ? static_cast<float*>(q8scale.get()) : nullptr, uint32_t(dpo)));
       ++kernel_launches;
     };
-    bool prep_done = f8;
-    if (f8) {
+    bool prep_done = f8 && !certify;
+    if (f8 && certify) {  // e4m3 queries, their bounds and margins in the query preparation
+      q8.reserve(nq * dpo, 0, stream);
+      q8scale.reserve(nq * sizeof(float), 0, stream);
+      gthr.reserve(nq * sizeof(uint32_t), 0, stream);
+      qmargin.reserve(2 * nq * sizeof(float), 0, stream);  // margins, then the bounds E
+      mgn = static_cast<float*>(qmargin.get());
+      VSG_CUDA(vsg::tc_encode_map(&qmap, q8.get(), nq, dpo, uint32_t(vsg::kTcQueries), true));
+    } else if (f8) {
       q8.reserve(nq * dpo, 0, stream);
       q8scale.reserve(nq * sizeof(float), 0, stream);
       VSG_CUDA(vsg::launch_to_fp8(dq, ldq, nq, uint32_t(dim), uint32_t(dpo), q8.get(),
@@ -589,13 +608,13 @@ struct vsg_index {
     const CUtensorMap& rowmap = f8 ? xmap8 : xmap;
     const size_t cbuf_entries = size_t(grid) * groups * vsg::kTcQueries * vsg::tc_buffer_capacity(kp);
     cbuf.reserve(cbuf_entries * 8, 0, stream);
-    if (f8) {  // (the bf16 queries' launch resets them)
+    if (f8 && !certify) {  // (the query preparation resets them)
       gthr.reserve(nq * sizeof(uint32_t), 0, stream);
       VSG_CUDA(cudaMemsetAsync(gthr.get(), 0xFF, nq * sizeof(uint32_t), s));
     }
     // Certified path: each query keeps only the rows within its margin of its k-th best (k' caps
     // the list), which is all the certificate needs.
-    const bool margins = certify && !f8;
+    const bool margins = certify;
     if (margins) {
       a.margin = static_cast<const float*>(qmargin.get());
       a.kk = uint32_t(k);
@@ -641,7 +660,7 @@ struct vsg_index {
     // After the query preparation the path's kernels run as a chain of programmatic dependent
     // launches (each may start while the one before it finishes); not while profiling, whose
     // events time the main pass on its own.
-    const bool pdl = !f8 && !profiling;
+    const bool pdl = !(f8 && !certify) && !profiling;
     if (srows > 0 && tiles_per_split > 1) {
       vsg::TcArgs sa = a;
       uint32_t st = uint32_t(std::min<size_t>(tiles_per_split, ceil_div(srows, size_t(a.nsplit) * vsg::kTcRows)));
@@ -717,7 +736,7 @@ struct vsg_index {
     fa.lists_per_split = uint32_t(groups);
     fa.sorted_lists = nq <= vsg::kSortedListQueries ? 1u : 0u;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
-    if (certify && !f8) {
+    if (certify) {
       fa.thr_init = a.thr_init;
       fa.gthr = a.gthr;
       fa.err = static_cast<const float*>(qmargin.get()) + nq;
@@ -756,8 +775,10 @@ struct vsg_index {
     uint32_t kp1 = force_exact_kp > 0 ? uint32_t(force_exact_kp) : te && te->kernel == 2 ? te->exact_kp : 0u;
     kp1 = kp1 ? std::max<uint32_t>(std::min<uint32_t>(kp1, uint32_t(vsg::kTcMaxShortlist)), uint32_t(k))
               : exact_shortlist_size(k);
-    // zeroes the count; the finish kernel fills the fallback's rows and masks
-    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, false, dmask, mask_ld);
+    // zeroes the count; the finish kernel fills the fallback's rows and masks. Batches of up to
+    // cert_fp8_max_batch queries read the e4m3 copy (half the bytes; a wider margin).
+    const bool f8 = double(nq) <= cert_fp8_max_batch;
+    enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, f8, dmask, mask_ld);
     tc_exact_queries += nq;
     const uint32_t* d_count = static_cast<const uint32_t*>(fails.get());
     const uint32_t* d_list = d_count + 1;
@@ -1081,10 +1102,20 @@ struct vsg_index {
   // (nothing kept, no error left set) when the chain cannot be captured.
   bool capture_graph(size_t nq, size_t k, uint32_t method) {
     drop_graph();
-    pin_in.reserve(nq * dim * sizeof(float));
+    pin_in.reserve(nq * dp * sizeof(float));
     pin_out.reserve(16 + nq * k * 8);
     reserve_results(nq, k);
     q.reserve(nq * dp * sizeof(float), 0, stream);
+    // Direct: the kernels read the pinned staging buffer through its device address (the
+    // certified path only, whose kernels read the queries with plain loads).
+    float* hq = nullptr;
+    if (host_graph_direct > 0 && use_tc_exact(method, nq, k, nullptr, false, -1.0)) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, pin_in.get()) == cudaSuccess && at.devicePointer)
+        hq = static_cast<float*>(at.devicePointer);
+      cudaGetLastError();
+    }
+    hgraph.direct = hq != nullptr;
     const uint64_t l0 = kernel_launches, t0 = tc_exact_queries, i0 = tiled_queries;
     cudaGraph_t graph = nullptr;
     if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
@@ -1093,9 +1124,10 @@ struct vsg_index {
     }
     bool ok = true;
     try {
-      float* dq = static_cast<float*>(q.get());
-      VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), pin_in.get(), dim * sizeof(float), dim * sizeof(float), nq,
-                                 cudaMemcpyHostToDevice, stream));
+      float* dq = hq ? hq : static_cast<float*>(q.get());
+      if (!hq)
+        VSG_CUDA(cudaMemcpy2DAsync(dq, dp * sizeof(float), pin_in.get(), dim * sizeof(float), dim * sizeof(float),
+                                   nq, cudaMemcpyHostToDevice, stream));
       enqueue(dq, dp, nq, k, nullptr, false, 0, false, res_ids(), res_dists(nq, k), stream, method, -1.0);
       VSG_CUDA(cudaMemcpyAsync(pin_out.get(), res.get(), 16 + nq * k * 8, cudaMemcpyDeviceToHost, stream));
     } catch (...) {
@@ -1143,7 +1175,15 @@ struct vsg_index {
         return false;
       }
     }
-    std::memcpy(pin_in.get(), host_q, nq * dim * sizeof(float));
+    if (g.direct) {  // rows dp apart, padding zero
+      float* hq = static_cast<float*>(pin_in.get());
+      for (size_t i = 0; i < nq; ++i) {
+        std::memcpy(hq + i * dp, host_q + i * dim, dim * sizeof(float));
+        std::fill(hq + i * dp + dim, hq + (i + 1) * dp, 0.f);
+      }
+    } else {
+      std::memcpy(pin_in.get(), host_q, nq * dim * sizeof(float));
+    }
     VSG_CUDA(cudaGraphLaunch(g.exec, stream));
     kernel_launches += g.launches;
     tc_exact_queries += g.tc_queries;

@@ -829,11 +829,19 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, size_t ld_src, siz
   }
 }
 
+// e4m3 byte -> its value (exact in FP32).
+__device__ __forceinline__ float e4m3_value(uint8_t b) {
+  return __half2float(__half(__nv_cvt_fp8_to_halfraw(__nv_fp8_storage_t(b), __NV_E4M3)));
+}
+
 // FP32 rows -> e4m3 rows of stride dp8 bytes (columns >= dim are zero), one FP32 scale per row
 // (max |x| / 448, the largest finite e4m3; 1 for a zero row) and optional squared FP32 norms.
+// With bounds set, the rows' rounding bounds as for the bf16 copy (max |x~ - x|, max |x|,
+// max |x~|, raised with atomicMax), where x~ = e4m3 value x scale: the differences and the
+// copy's norms are summed in FP64 from exact products (4 + 24 significant bits), and rounded up.
 __global__ void to_fp8_kernel(const float* __restrict__ src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8,
                               uint8_t* __restrict__ dst, float* __restrict__ scale, float* __restrict__ norms,
-                              size_t tile_row0) {
+                              float* __restrict__ bounds, size_t tile_row0) {
   const size_t row = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (row >= rows) return;
@@ -853,12 +861,31 @@ __global__ void to_fp8_kernel(const float* __restrict__ src, size_t ld_src, size
   const bool tiled = tile_row0 != kRowMajor;
   const uint32_t nkc = (dp8 + 127) / 128;
   const uint32_t width = tiled ? nkc * 128u : dp8;  // tile-major chunks are whole
-  for (uint32_t c = lane; c < width; c += 32)
-    dst[tiled ? tile_major_offset(tile_row0 + row, c, nkc, 128) : row * dp8 + c] =
-        c < dim ? uint8_t(__nv_cvt_float_to_fp8(s[c] * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+  double res = 0.0, accb = 0.0;
+  for (uint32_t c = lane; c < width; c += 32) {
+    const float v = c < dim ? s[c] : 0.f;
+    const uint8_t b = c < dim ? uint8_t(__nv_cvt_float_to_fp8(v * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+    dst[tiled ? tile_major_offset(tile_row0 + row, c, nkc, 128) : row * dp8 + c] = b;
+    if (bounds && c < dim) {
+      const double xt = double(e4m3_value(b)) * double(sc);  // exact
+      const double e = xt - double(v);
+      res = fma(e, e, res);
+      accb = fma(xt, xt, accb);
+    }
+  }
+  if (bounds)
+    for (int o = 16; o > 0; o >>= 1) {
+      res += __shfl_xor_sync(kFull, res, o);
+      accb += __shfl_xor_sync(kFull, accb, o);
+    }
   if (lane == 0) {
     scale[row] = sc;
     if (norms) norms[row] = acc;
+    if (bounds) {  // non-negative floats order like their bit patterns
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 0, __float_as_uint(__double2float_ru(sqrt(res))));
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 1, __float_as_uint(sqrtf(acc)));
+      atomicMax(reinterpret_cast<unsigned*>(bounds) + 2, __float_as_uint(__double2float_ru(sqrt(accb))));
+    }
   }
 }
 
@@ -970,8 +997,10 @@ __device__ __forceinline__ void exact_distances(const float4* q4, const float4* 
 // |q|^2, |q~|^2 and |q~ - q|^2 (FP32, d terms each; q~ = the bf16 query) and the rows' bounds
 // xbound = [max |x~ - x|, max |x|, max |x~|]. In FP32 with every operation rounded up: all terms
 // are non-negative and every operation is monotone, so the result is at least the formula's
-// exact value (FP64 would be as safe but is slow on GB300).
-template <bool L2>
+// exact value (FP64 would be as safe but is slow on GB300). F8: q~ and x~ are the e4m3 copies
+// times their scales, and the score the kernel uses is (sum of e4m3 products) x (query scale x row
+// scale), two more FP32 roundings: at most 2 u (1 + u) |q~||x~|, taken as 4 u |q~||x~|.
+template <bool L2, bool F8 = false>
 __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const float* xbound) {
   auto mul = [](float a, float b) { return __fmul_ru(a, b); };
   auto add = [](float a, float b) { return __fadd_ru(a, b); };
@@ -983,7 +1012,8 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
   const float R = mul(xbound[0], infl), N = mul(xbound[1], infl), Nb = mul(xbound[2], infl);
   // |bf16 score - q.x| <= |q~||x~ - x| + |q~ - q||x| + accumulation (8 d u |q~||x~|);
   // |FP32 q.x - q.x| <= 2 d u |q||x|.
-  const float e_dot = add(add(mul(qbn, R), mul(rq, N)), add(mul(mul(8.f, du), mul(qbn, Nb)), mul(mul(2.f, du), mul(qn, N))));
+  float e_dot = add(add(mul(qbn, R), mul(rq, N)), add(mul(mul(8.f, du), mul(qbn, Nb)), mul(mul(2.f, du), mul(qn, N))));
+  if (F8) e_dot = add(e_dot, mul(mul(4.f, u), mul(qbn, Nb)));
   float e;
   if (L2) {  // norms (d u each), two roundings of |q|^2 + |x|^2 - 2 s, FP32 squared differences
     const float q2n2 = add(mul(qn, qn), mul(N, N));
@@ -1024,7 +1054,7 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
 // Nothing is read when the status word says a shortlist kernel gave up (its lists may be stale),
 // and row ids at or beyond n are never dereferenced.
 constexpr int kFinishThreads = 512;
-constexpr uint32_t kRerankMax = 1024;
+constexpr uint32_t kRerankMax = 2048;  // (the e4m3 copy's wider margin keeps ~1,000 rows at 1M x 384)
 constexpr uint32_t kKeyAll = 0xFFFFFFFFu;  // cut key that keeps every entry
 constexpr uint32_t kStageSplits = 1024;    // lists the flat staging copy handles at most
 constexpr uint32_t kSmallSelect = 256;     // staged entries up to which the cut ranks them in one pass
@@ -1878,21 +1908,80 @@ __device__ __forceinline__ void prepare_query_warp(const float* q, uint32_t ldq,
   }
 }
 
+// The e4m3 form of prepare_query_warp (the certified path over the e4m3 copy): per query its
+// scale max |q| / 448 (as to_fp8_kernel takes it), its e4m3 row (stride dpo bytes, padding
+// zero), the squared FP32 norm, and with margins E from the sums |q~|^2 and |q~ - q|^2 (q~ = e4m3
+// value x scale; FP64 from exact products, rounded up) and the e4m3 rows' bounds.
+template <bool L2>
+__device__ __forceinline__ void prepare_query_warp_f8(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
+                                                      uint32_t dp, uint32_t dpo, uint8_t* q8, float* qscale,
+                                                      float* qnorm, uint32_t* gthr, const float* xbound,
+                                                      float factor, float* margin, float* err, uint32_t* fails) {
+  if (fails && blockIdx.x == 0 && threadIdx.x == 0) *fails = 0;
+  const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (qq >= nq) return;
+  const float* s = q + size_t(qq) * ldq;
+  float mx = 0.f, q2 = 0.f;
+  for (uint32_t c = lane; c < dim; c += 32) {
+    const float v = s[c];
+    mx = fmaxf(mx, fabsf(v));
+    q2 = fmaf(v, v, q2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    q2 += __shfl_xor_sync(kFull, q2, o);
+  }
+  const float sc = mx > 0.f ? mx / 448.f : 1.f;
+  const float inv = 1.f / sc;
+  double res = 0.0, accb = 0.0;
+  for (uint32_t c = lane; c < dpo; c += 32) {
+    const float v = c < dim ? s[c] : 0.f;
+    const uint8_t b = c < dim ? uint8_t(__nv_cvt_float_to_fp8(v * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+    q8[size_t(qq) * dpo + c] = b;
+    const double xt = double(e4m3_value(b)) * double(sc);  // exact
+    const double e = xt - double(v);
+    res = fma(e, e, res);
+    accb = fma(xt, xt, accb);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    res += __shfl_xor_sync(kFull, res, o);
+    accb += __shfl_xor_sync(kFull, accb, o);
+  }
+  if (lane == 0) {
+    qscale[qq] = sc;
+    if (qnorm) qnorm[qq] = q2;
+    if (gthr) gthr[qq] = kKeyNone;
+    if (margin) {
+      const float e = cert_error<L2, true>(q2, __double2float_ru(accb), __double2float_ru(res), dp, xbound);
+      err[qq] = e;
+      margin[qq] = __fmul_ru(factor, e);
+    }
+  }
+}
+
 // The query preparation: one warp per query in the first ceil(nq / 4) blocks, the FP32 sample
 // (PrepSample, when set) in the blocks after them.
-template <bool L2>
+template <bool L2, bool F8>
 __global__ void __launch_bounds__(128) prepare_queries_kernel(const float* q, uint32_t ldq, uint32_t nq,
-                                                              uint32_t dim, uint32_t dp, __nv_bfloat16* qb,
-                                                              float* qnorm, uint32_t* gthr, const float* xbound,
-                                                              float factor, float* margin, float* err,
-                                                              uint32_t* fails, PrepSample smp) {
-  pdl_trigger();  // the head of a chain of dependent launches: the next kernel may start launching
+                                                              uint32_t dim, uint32_t dp, void* qout, uint32_t dpo,
+                                                              float* qscale, float* qnorm, uint32_t* gthr,
+                                                              const float* xbound, float factor, float* margin,
+                                                              float* err, uint32_t* fails, PrepSample smp) {
+  // The head of a chain of dependent launches: the next kernel may start launching at once, except
+  // with an FP32 sample, where it launches when this grid ends. Its CTAs, waiting on this grid on
+  // every SM, slowed the sample's threshold select (2.4 to 3.1 us) and the whole batch-1 chain
+  // ended 2.4 us later.
+  if (!smp.thr) pdl_trigger();
   pdl_wait();
   const uint32_t qblocks = (nq + 3) / 4;
   if (blockIdx.x >= qblocks) {  // FP32 sample blocks (block-uniform)
     prep_sample_block<L2>(smp, blockIdx.x - qblocks, q, ldq, nq, dim, dp);
+  } else if constexpr (F8) {
+    prepare_query_warp_f8<L2>(q, ldq, nq, dim, dp, dpo, static_cast<uint8_t*>(qout), qscale, qnorm, gthr, xbound,
+                              factor, margin, err, fails);
   } else {
-    prepare_query_warp<L2>(q, ldq, nq, dim, dp, qb, qnorm, gthr, xbound, factor, margin, err, fails);
+    prepare_query_warp<L2>(q, ldq, nq, dim, dp, static_cast<__nv_bfloat16*>(qout), qnorm, gthr, xbound, factor,
+                           margin, err, fails);
   }
   if (smp.thr) prep_sample_select(smp, nq, gridDim.x - qblocks, margin);
 }
@@ -2165,13 +2254,13 @@ cudaError_t tc_encode_tiled_map(CUtensorMap* map, const void* base, uint64_t row
 }
 
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
-                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0) {
+                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0, float* bounds) {
   if (rows == 0) return cudaSuccess;
   if (dp8 % 16 != 0 || dp8 < dim) return cudaErrorInvalidValue;
   const size_t threads = rows * 32;
   to_fp8_kernel<<<unsigned((threads + 255) / 256), 256, 0, stream>>>(src, ld_src, rows, dim, dp8,
                                                                      static_cast<uint8_t*>(dst), scale, norms,
-                                                                     tile_row0);
+                                                                     bounds, tile_row0);
   return cudaGetLastError();
 }
 
@@ -2252,9 +2341,11 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
 
 cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
                                    uint32_t dp, void* qb, float* qnorm, uint32_t* gthr, const float* xbound, bool l2,
-                                   float factor, float* margin, float* err, uint32_t* fails, cudaStream_t stream) {
+                                   float factor, float* margin, float* err, uint32_t* fails, cudaStream_t stream,
+                                   float* qscale, uint32_t dpo) {
   if (nq == 0) return cudaSuccess;
-  if (!q || !qb || ldq < dim || dp < dim || (margin && (!err || !xbound || !(factor >= 0.f))))
+  if (!q || !qb || ldq < dim || dp < dim || (margin && (!err || !xbound || !(factor >= 0.f))) ||
+      (qscale && (dpo < dim || dpo % 16 != 0)))
     return cudaErrorInvalidValue;
   PrepSample smp{};
   unsigned blocks = (nq + 3) / 4;
@@ -2268,13 +2359,10 @@ cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uin
     blocks += (smp.ranges * uint32_t(kTcRows) + kPrepRowsPerBlock - 1) / kPrepRowsPerBlock;
     smem = size_t(nq) * dp * sizeof(float);  // <= 32 KB
   }
-  auto* dst = static_cast<__nv_bfloat16*>(qb);
-  if (l2)
-    prepare_queries_kernel<true><<<blocks, 128, smem, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound,
-                                                                factor, margin, err, fails, smp);
-  else
-    prepare_queries_kernel<false><<<blocks, 128, smem, stream>>>(q, ldq, nq, dim, dp, dst, qnorm, gthr, xbound,
-                                                                 factor, margin, err, fails, smp);
+  auto* kern = qscale ? (l2 ? prepare_queries_kernel<true, true> : prepare_queries_kernel<false, true>)
+                      : (l2 ? prepare_queries_kernel<true, false> : prepare_queries_kernel<false, false>);
+  kern<<<blocks, 128, smem, stream>>>(q, ldq, nq, dim, dp, qb, qscale ? dpo : dp, qscale, qnorm, gthr, xbound, factor,
+                                      margin, err, fails, smp);
   return cudaGetLastError();
 }
 

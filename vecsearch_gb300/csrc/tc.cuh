@@ -15,9 +15,9 @@ constexpr int kTcKChunk = 64;    // bf16 dims per staged chunk (one 128-byte swi
 // for 64 appends between compactions.
 constexpr int kTcMaxShortlist = 448;
 // Entries of the split lists the finish kernel stages in shared memory per query at most; beyond
-// that its passes read the lists in global memory (192 KB of staging: with the query and the
+// that its passes read the lists in global memory (176 KB of staging: with the query and the
 // candidate arrays it fits the 227 KB of a CTA for every dim up to 4,096).
-constexpr uint32_t kFinishStageMax = 24576;
+constexpr uint32_t kFinishStageMax = 22528;
 // The shortlist kernel writes a query's final list of a split sorted by (dist, id) when the warp
 // that holds the query has at most this many real queries (few queries: the sort lets the margin
 // cut shorten the list), else unsorted with its smallest entry first. So a batch of at most this
@@ -250,14 +250,20 @@ constexpr uint32_t kPrepSampleRows = 4096;
 // bound E on |approximate - FP32 distance| over rows whose bf16 copies have the bounds xbound =
 // [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E, both rounded up;
 // and *fails = 0 when fails is set.
+// qscale set: the certified path over the e4m3 copy; qb then receives e4m3 rows (stride dpo bytes,
+// a multiple of 16) with qscale[q] = max |q| / 448, E covers the e4m3 roundings (xbound: the e4m3
+// rows' bounds from launch_to_fp8), and the rest is as above.
 cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
                                    uint32_t dp, void* qb,
                                    float* qnorm, uint32_t* gthr, const float* xbound, bool l2, float factor,
-                                   float* margin, float* err, uint32_t* fails, cudaStream_t stream);
+                                   float* margin, float* err, uint32_t* fails, cudaStream_t stream,
+                                   float* qscale = nullptr, uint32_t dpo = 0);
 // FP32 rows -> e4m3 rows (stride dp8 bytes, padding zero) with scale[r] = max |x_r| / 448 (1 for a
 // zero row; saturating round to nearest of x / scale) and squared FP32 norms when norms != nullptr.
 // With tile_row0 set, dst is a tile-major copy as in launch_to_bf16.
+// bounds (optional): the rows' rounding bounds for the certificate, as launch_to_bf16 writes them.
 cudaError_t launch_to_fp8(const float* src, size_t ld_src, size_t rows, uint32_t dim, uint32_t dp8, void* dst,
-                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0 = kRowMajor);
+                          float* scale, float* norms, cudaStream_t stream, size_t tile_row0 = kRowMajor,
+                          float* bounds = nullptr);
 
 }  // namespace vsg

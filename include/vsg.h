@@ -208,7 +208,14 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   search of a shape, dropped when rows are added, a tunable or tuning table is set or a buffer is
  *   reallocated. Results are the same for every value; 0 switches it off.
  *   "host_graph_direct" (default 1, 0 or 1): in those graphs the certified path's kernels read
- *   the queries from the pinned staging buffer themselves instead of a copy into device memory. */
+ *   the queries from the pinned staging buffer themselves instead of a copy into device memory.
+ *   "cert_fp8_max_batch" (default 16): VSG_METHOD_TC_EXACT batches of at most this many queries
+ *   with k <= 16 read an e4m3 copy of the rows (one FP32 scale per row, built on first use; half
+ *   the bf16 copy's bytes) with a bound E that covers its roundings; results stay bit-identical to
+ *   VSG_METHOD_SKINNY. 0 keeps every batch on the bf16 copy.
+ *   "cert_fp8_sample_rows" (default 32768): rows sampled for those searches' starting thresholds.
+ *   "finish_cluster" (default 8, 1 to 8): CTAs per query sharing the certified path's FP32 rerank
+ *   (a thread-block cluster) when the batch times this fits the SM count; else one CTA a query. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

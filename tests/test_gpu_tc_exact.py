@@ -263,12 +263,47 @@ def test_tc_exact_over_e4m3_copy(gpu_ready, metric, unit, d):
     gpu = vsg.GpuBruteForceIndex(d, metric)
     gpu.add(x)
     gpu.set_tunable("cert_fp8_max_batch", 8)
-    for k in (10, 100):
-        want = gpu.search(q, k, method="skinny")
-        for b in (1, 3, 8):
-            for s in range(0, 16, b):
-                _same(gpu.search(q[s:s + b], k, method="tc_exact"), (want[0][s:s + b], want[1][s:s + b]))
+    for cluster in (1, 8):  # the finish kernel's rerank on one CTA, or shared by 8 in a cluster
+        gpu.set_tunable("finish_cluster", cluster)
+        for k in (10, 100):
+            want = gpu.search(q, k, method="skinny")
+            for b in (1, 3, 8):
+                for s in range(0, 16, b):
+                    _same(gpu.search(q[s:s + b], k, method="tc_exact"), (want[0][s:s + b], want[1][s:s + b]))
     q0, s0, f0 = gpu.tc_exact_stats()
     gpu.search(q[:8], 10, method="tc_exact")
     q1, s1, f1 = gpu.tc_exact_stats()
     assert q1 - q0 == 8 and s1 - s0 <= 2  # the certificate holds for nearly every query
+
+
+@pytest.mark.parametrize("cluster", [2, 8])
+def test_tc_exact_finish_cluster(gpu_ready, cluster):
+    # "finish_cluster": the finish kernel of a small batch runs as a cluster of CTAs per query,
+    # rank 0 staging and cutting, every rank reranking a share through distributed shared memory;
+    # batches whose CTAs would exceed the SM count run with one CTA a query. Bit for bit the scan's.
+    vsg = gpu_ready
+    x, q = _clustered(200_000, 160, 256, 128, True, 360 + cluster)
+    gpu = vsg.GpuBruteForceIndex(256, "cosine")
+    gpu.add(x)
+    gpu.set_tunable("finish_cluster", cluster)
+    assert gpu.get_tunable("finish_cluster") == cluster
+    for k in (10, 100):
+        want = gpu.search(q, k, method="skinny")
+        for b in (1, 5, 16, 40, 160):
+            _same(gpu.search(q[:b], k, method="tc_exact"), (want[0][:b], want[1][:b]))
+    with pytest.raises(ValueError):
+        gpu.set_tunable("finish_cluster", 9)
+
+
+def test_tc_exact_e4m3_wide_rows_use_bf16(gpu_ready):
+    # Rows wider than the e4m3 query preparation takes (1,100 dims -> 1,104 > 1,024) stay on the
+    # bf16 copy under cert_fp8_max_batch: still the scan kernel's results.
+    vsg = gpu_ready
+    x, q = _clustered(20_000, 6, 1100, 64, True, 390)
+    gpu = vsg.GpuBruteForceIndex(1100, "cosine")
+    gpu.add(x)
+    gpu.set_tunable("cert_fp8_max_batch", 8)
+    gpu.set_tunable("finish_cluster", 8)
+    want = gpu.search(q, 10, method="skinny")
+    for b in (1, 6):
+        _same(gpu.search(q[:b], 10, method="tc_exact"), (want[0][:b], want[1][:b]))

@@ -180,8 +180,15 @@ struct vsg_index {
   } hgraph;
   uint64_t config_gen = 0;
   double host_graph_max_batch = 16;  // blocking searches of at most this many queries; 0: none
-  // Certified searches of at most this many queries read the e4m3 copy of the rows (0: none).
-  double cert_fp8_max_batch = 0;
+  // Certified searches of at most this many queries, k <= 16, read the e4m3 copy of the rows
+  // (0: none), starting from a sample of cert_fp8_sample_rows rows. Measured at 1M x 384, k = 10:
+  // 1.14-1.24x the bf16 copy's QPS at batches 1-16, 0.89-0.93x at 32-64; k = 100 needs ~1,000
+  // reranked rows a query and ran at 0.15-0.5x.
+  double cert_fp8_max_batch = 16;
+  double cert_fp8_sample_rows = 32768;
+  // Certified path: CTAs per query in the finish kernel when the batch times it fits the SMs
+  // (1-8; k = 100 at batches 1-8 on the bf16 copy ran 9-10 % faster with 8).
+  double finish_cluster = 8;
   // 1: on the certified path the graph's kernels read the queries straight from the pinned
   // staging buffer (no copy in; measured 1.5 us less a blocking search at batch 1)
   double host_graph_direct = 1;
@@ -653,9 +660,13 @@ struct vsg_index {
     // 1M x 384 21 % slower. Measured at 1M x 384 on the certified path: k = 10 ran 2.6-4 % faster
     // with 4K than with 16K sampled rows at batches 8-64, but 6 % slower at 1024, where the
     // epilogue sets the pace and a looser start costs appends; k = 100 up to 1.9x slower with 4K)
+    // The certified path over the e4m3 copy samples cert_fp8_sample_rows: its margin is ~16x the
+    // bf16 copy's, and a start from 4K rows (about 4 rows of a query's 1,000-row cluster at
+    // 1M x 384) kept every list full of rows far above the cluster for the whole pass.
     const bool small_sample = nq < 8 || (k <= 16 && nq <= 64);
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
                          : te ? size_t(te->sample)
+                         : f8 && certify ? size_t(cert_fp8_sample_rows)
                          : small_sample ? std::min<size_t>(size_t(sample_rows), 4096) : size_t(sample_rows);
     // After the query preparation the path's kernels run as a chain of programmatic dependent
     // launches (each may start while the one before it finishes); not while profiling, whose
@@ -676,8 +687,11 @@ struct vsg_index {
         st = 1;
         sgrid = unsigned(std::min<size_t>(nqb * sa.nsplit, slots));
       }
-      const size_t per_query = size_t(sa.nsplit) * st * vsg::kTcRows;
-      sample.reserve(nq * per_query * sizeof(float), 0, stream);
+      // (with margins and k <= 32, the sample pass writes each 32 rows' smallest distance only:
+      // the select then reads 32x fewer values; its bound is the k-th smallest of those minima)
+      sa.dump_min = margins && k <= 32 ? 1u : 0u;
+      const size_t per_query = size_t(sa.nsplit) * st * (sa.dump_min ? vsg::kTcRows / 32 : vsg::kTcRows);
+      sample.reserve(nq * size_t(sa.nsplit) * st * vsg::kTcRows * sizeof(float), 0, stream);
       thr.reserve(nq * sizeof(float), 0, stream);
       sa.dump = static_cast<float*>(sample.get());
       sa.sample_tiles = st;
@@ -735,6 +749,9 @@ struct vsg_index {
     fa.status = status_word();
     fa.lists_per_split = uint32_t(groups);
     fa.sorted_lists = nq <= vsg::kSortedListQueries ? 1u : 0u;
+    // Small batches rerank over a cluster of CTAs per query (the e4m3 copy's wider margin keeps
+    // ~1,000 rows to rerank at 1M x 384, ~20 us on one SM).
+    fa.cluster = certify && double(nq * size_t(finish_cluster)) <= double(sms) ? uint32_t(finish_cluster) : 1u;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
     if (certify) {
       fa.thr_init = a.thr_init;
@@ -777,7 +794,7 @@ struct vsg_index {
               : exact_shortlist_size(k);
     // zeroes the count; the finish kernel fills the fallback's rows and masks. Batches of up to
     // cert_fp8_max_batch queries read the e4m3 copy (half the bytes; a wider margin).
-    const bool f8 = double(nq) <= cert_fp8_max_batch;
+    const bool f8 = double(nq) <= cert_fp8_max_batch && k <= 16 && dp8() <= vsg::kPrepSampleDim;  // (the query preparation's width)
     enqueue_bf16(dq, ldq, nq, k, out_ids, out_dists, s, true, kp1, f8, dmask, mask_ld);
     tc_exact_queries += nq;
     const uint32_t* d_count = static_cast<const uint32_t*>(fails.get());

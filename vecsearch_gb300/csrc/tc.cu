@@ -613,7 +613,8 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
           }
         }
       };
-      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * sample_tiles * kTcRows
+      const uint32_t dump_per_tile = a.dump_min ? uint32_t(kTcRows / 32) : uint32_t(kTcRows);
+      float* dump_row = (a.dump && qvalid) ? a.dump + (size_t(qg) * nsplit + split) * sample_tiles * dump_per_tile
                                            : nullptr;
       auto compact_lanes = [&](unsigned lanes, bool final_list) {
         if (!lanes) return;
@@ -681,10 +682,17 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
                 const float dist = L2 ? l2_approx(qn, __ldg(a.xnorm + min(row, a.n - 1)), sc) : 1.f - sc;
                 o[j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
               }
-              // 16-byte stores (the row's 32 values are contiguous and 128-byte aligned).
-              float4* d4 = reinterpret_cast<float4*>(dump_row + t * kTcRows + c * 32);
+              if (a.dump_min) {  // the 32 rows' smallest distance only
+                float m = o[0];
 #pragma unroll
-              for (int j = 0; j < 8; ++j) d4[j] = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
+                for (int j = 1; j < 32; ++j) m = fminf(m, o[j]);
+                dump_row[t * (kTcRows / 32) + c] = m;
+              } else {
+                // 16-byte stores (the row's 32 values are contiguous and 128-byte aligned).
+                float4* d4 = reinterpret_cast<float4*>(dump_row + t * kTcRows + c * 32);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) d4[j] = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
+              }
             }
           }
         } else {
@@ -756,7 +764,8 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
       }
       if (a.dump) {  // sample pass: tiles past the split's end read as +inf
         if (dump_row && group == 0)
-          for (uint32_t j = ntiles * kTcRows; j < sample_tiles * kTcRows; ++j) dump_row[j] = __int_as_float(0x7f800000);
+          for (uint32_t j = ntiles * dump_per_tile; j < sample_tiles * dump_per_tile; ++j)
+            dump_row[j] = __int_as_float(0x7f800000);
       } else {
         // Sort every buffer, keep the best kp and write the split's shortlist.
         compact_lanes(ok ? __ballot_sync(kFull, qvalid) : 0u, true);
@@ -1026,6 +1035,37 @@ __device__ float cert_error(float sq2, float sqb2, float sr2, uint32_t dp, const
   return mul(e, 1.1f);  // margin over the (already worst-case) terms; 1.1f is above 1.1
 }
 
+// Thread-block cluster helpers (sm_90+): the CTA's rank and the cluster's size along x, a barrier
+// over every thread of the cluster (release / acquire: shared-memory writes before it are seen
+// after it), and 4-byte loads and stores in rank r's shared memory at the address a variable has
+// in this CTA's.
+__device__ __forceinline__ uint32_t cluster_nctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_addr(const void* local, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_addr(local)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ uint32_t ld_cluster_u32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_cluster_f32(uint32_t addr, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
 // The shortlist path's tail (FinishArgs), one CTA of kFinishThreads per query.
 //   1. Stage: the split lists' real entries (part_n of each) are copied into shared memory when
 //      they fit (stage_cap entries), else the passes below read the lists in global memory. With
@@ -1089,7 +1129,10 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   __shared__ float s_dk;
   pdl_trigger();
   pdl_wait();
-  const uint32_t q = blockIdx.x;
+  // A query may have a cluster of CTAs (launched so for small batches, wide variant): rank 0 does
+  // everything but share the rerank, which every CTA of the cluster does (below).
+  const uint32_t csize = kWide ? cluster_nctarank() : 1u, crank = csize > 1 ? cluster_ctarank() : 0u;
+  const uint32_t q = blockIdx.x / csize;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int nwarps = kFinishThreads / 32;
   const bool serving = a.hdr != nullptr;
@@ -1130,6 +1173,44 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     s_dk = __int_as_float(0x7f800000);
   }
   const float* qrow = a.q + size_t(q) * a.ldq;
+  constexpr int G = kWide ? 6 : 4;  // rows per warp in flight in the rerank (96 a pass of a CTA when wide)
+  // The rerank's share of cluster rank crank: warps crank x nwarps + warp of all csize x nwarps,
+  // G rows each in flight; rank 0's candidate ids in, FP32 distances out (its shared memory).
+  auto rerank_share = [&](uint32_t nc) {
+    const float4* q4 = reinterpret_cast<const float4*>(L.cd > 0 ? qs : qrow);
+    const uint32_t nch = a.dp / 4, wall = csize * uint32_t(nwarps);
+    for (uint32_t j0 = crank * uint32_t(nwarps) + uint32_t(warp); j0 < nc; j0 += G * wall) {
+      const float4* x4[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const uint32_t j = j0 + uint32_t(g) * wall;
+        uint32_t id = kNone;
+        if (j < nc) id = csize > 1 ? ld_cluster_u32(cluster_addr(cand_i + j, 0)) : cand_i[j];
+        x4[g] = id < a.n ? reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp) : nullptr;
+      }
+      float d[G];
+      exact_distances<L2, G, kWide ? 3 : 1>(q4, x4, nch, lane, d);
+      if (lane == 0) {
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const uint32_t j = j0 + uint32_t(g) * wall;
+          if (j >= nc) continue;
+          const float v = x4[g] ? d[g] : __int_as_float(0x7f800000);
+          if (csize > 1) st_cluster_f32(cluster_addr(cand_x + j, 0), v);
+          else cand_x[j] = v;
+        }
+      }
+    }
+  };
+  if (crank != 0) {  // (CTA-uniform) a cluster member: the query, rank 0's candidates, a share
+    if (L.cd > 0)
+      for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
+    __syncthreads();
+    cluster_sync_all();  // rank 0 has collected its candidates
+    rerank_share(ld_cluster_u32(cluster_addr(&s_cnt, 0)));
+    cluster_sync_all();  // every share is in rank 0's shared memory
+    return;
+  }
   // The query and (for the flat copy below) the lists' lengths and heads load in the same round
   // trip; the heads' order keys sit in cand_x until the rerank needs it (kKeyAll: empty list).
   const bool flat = nsplit <= kStageSplits;
@@ -1264,7 +1345,9 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // Appends (d, id) to the staging area when `keep` (warp-uniform call; any order); past
   // stage_cap nothing is written and the count alone grows (the passes then read the lists).
   // The row of a kept entry is also prefetched into L2 for the rerank (most kept entries are
-  // reranked; the rows are scattered over HBM, so the rerank's loads otherwise wait on DRAM).
+  // reranked; the rows are scattered over HBM, so the rerank's loads otherwise wait on DRAM). Not
+  // when a cluster shares the rerank: its CTAs load their own rows, and one SM issuing ~12,000
+  // line prefetches for ~1,000 rows took 15 us.
   auto append = [&](bool keep, float d, uint32_t id) {
     const unsigned bal = __ballot_sync(kFull, keep);
     uint32_t at = 0;
@@ -1274,7 +1357,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       stg_d[at] = d;
       stg_i[at] = id;
     }
-    for (unsigned m = bal; m; m &= m - 1) {  // each kept row's 128-byte lines, one a lane
+    for (unsigned m = csize > 1 ? 0u : bal; m; m &= m - 1) {  // each kept row's 128-byte lines, one a lane
       const uint32_t rid = __shfl_sync(kFull, id, __ffs(m) - 1);
       if (rid < a.n) {
         const char* row = reinterpret_cast<const char*>(a.x + size_t(rid) * a.dp);
@@ -1311,28 +1394,42 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       if (tid == 0) s_rank = 0;  // the next run's list count
       __syncthreads();
       const uint32_t tot = nl * kDirectRun;
-      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += kFinishThreads) {
-        const uint32_t e = w0 + uint32_t(lane);
-        uint32_t sp = 0, j = 0, len = 0, iv = 0;
-        float dv = 0.f;
-        if (e < tot) {
-          sp = cur[e / kDirectRun];
-          j = j0 + e % kDirectRun;
-          len = s_off[sp + 1];
-          if (j < len) {
-            const size_t at = base + size_t(sp) * a.kp + j;
-            dv = a.part_d[at];
-            iv = a.part_i[at];
+      // kDirectAhead entries a thread, all loaded before any is appended (one round trip)
+      constexpr int kDirectAhead = 4;
+      for (uint32_t w0 = uint32_t(tid) & ~31u; w0 < tot; w0 += kDirectAhead * kFinishThreads) {
+        uint32_t sp[kDirectAhead], j[kDirectAhead], len[kDirectAhead], iv[kDirectAhead];
+        float dv[kDirectAhead];
+#pragma unroll
+        for (int p = 0; p < kDirectAhead; ++p) {
+          const uint32_t e = w0 + uint32_t(lane) + uint32_t(p) * kFinishThreads;
+          sp[p] = 0;
+          j[p] = 0;
+          len[p] = 0;
+          iv[p] = 0;
+          dv[p] = 0.f;
+          if (e < tot) {
+            sp[p] = cur[e / kDirectRun];
+            j[p] = j0 + e % kDirectRun;
+            len[p] = s_off[sp[p] + 1];
+            if (j[p] < len[p]) {
+              const size_t at = base + size_t(sp[p]) * a.kp + j[p];
+              dv[p] = a.part_d[at];
+              iv[p] = a.part_i[at];
+            }
           }
         }
-        const bool keep = j < len && order_key(dv) <= c_key;
-        append(keep, dv, iv);
-        const bool more = keep && e % kDirectRun == kDirectRun - 1 && j + 1 < len;
-        const unsigned bal = __ballot_sync(kFull, more);
-        uint32_t at = 0;
-        if (lane == 0 && bal) at = atomicAdd(&s_rank, uint32_t(__popc(bal)));
-        at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
-        if (more) nxt[at] = sp;
+#pragma unroll
+        for (int p = 0; p < kDirectAhead; ++p) {
+          const uint32_t e = w0 + uint32_t(lane) + uint32_t(p) * kFinishThreads;
+          const bool keep = j[p] < len[p] && order_key(dv[p]) <= c_key;
+          append(keep, dv[p], iv[p]);
+          const bool more = keep && e % kDirectRun == kDirectRun - 1 && j[p] + 1 < len[p];
+          const unsigned bal = __ballot_sync(kFull, more);
+          uint32_t at = 0;
+          if (lane == 0 && bal) at = atomicAdd(&s_rank, uint32_t(__popc(bal)));
+          at = __shfl_sync(kFull, at, 0) + __popc(bal & ((1u << lane) - 1u));
+          if (more) nxt[at] = sp[p];
+        }
       }
       __syncthreads();
       nl = s_rank;
@@ -1467,12 +1564,11 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     return radix_select([&](auto&& f) { each([&](uint32_t key, float, uint32_t) { f(key); }); }, rank, 4);
   };
   // keep entries with key <= cut_key (or < when strict); the heads' bound c already left out every
-  // entry above it. A staged set no larger than one rerank pass is reranked whole: the exact cut
-  // would not save a pass.
-  constexpr int G = kWide ? 6 : 4;  // rows per warp in flight in the rerank (96 a pass when wide)
+  // entry above it. A staged set no larger than one rerank pass (two with a cluster, whose passes
+  // are short) is reranked whole: the exact cut would not save a pass.
   uint32_t cut_key = c_key;
   bool strict = false;
-  const bool whole = c_key != kKeyAll && staged && total <= uint32_t(G * nwarps);
+  const bool whole = c_key != kKeyAll && staged && total <= uint32_t(G * nwarps) * (csize > 1 ? 2u * csize : 1u);
   if (total > target && !whole) {
     const uint32_t tk = select_key(target);
     cut_key = mg >= 0.f ? order_key(__fadd_ru(key_float(tk), mg)) : tk;
@@ -1504,26 +1600,9 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   const uint32_t nc = s_cnt;  // <= kRerankMax
   const bool cut_left_out = nc < all;
   // ---- 3. rerank ----
-  const float4* q4 = reinterpret_cast<const float4*>(L.cd > 0 ? qs : qrow);
-  const uint32_t nch = a.dp / 4;
-  for (uint32_t j0 = warp; j0 < nc; j0 += G * nwarps) {
-    const float4* x4[G];
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const uint32_t j = j0 + uint32_t(g) * nwarps;
-      const uint32_t id = j < nc ? cand_i[j] : kNone;
-      x4[g] = id < a.n ? reinterpret_cast<const float4*>(a.x + size_t(id) * a.dp) : nullptr;
-    }
-    float d[G];
-    exact_distances<L2, G, kWide ? 3 : 1>(q4, x4, nch, lane, d);
-    if (lane == 0) {
-#pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const uint32_t j = j0 + uint32_t(g) * nwarps;
-        if (j < nc) cand_x[j] = x4[g] ? d[g] : __int_as_float(0x7f800000);
-      }
-    }
-  }
+  if (csize > 1) cluster_sync_all();  // the candidates are ready for the cluster's shares
+  rerank_share(nc);
+  if (csize > 1) cluster_sync_all();  // every share is in
   __syncthreads();
   // ---- 4. top k by (FP32 dist, id) ----
   // Each candidate's rank among (order key of the distance, id) pairs, counted against all of them
@@ -1531,7 +1610,12 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // position, so the ranks are a permutation). The pairs sit in the staging area, free once the
   // candidates are collected (at least kRerankMax x 8 bytes). A NaN distance ranks as +inf (written
   // as a missing result) and -0 as +0: the order is the float order of the distances, then ids.
+  // More than kRankAll candidates: the k-th smallest distance key is selected first (exact radix
+  // selection), and only the candidates at or below it are ranked, among themselves (every other
+  // candidate comes after them); ranking 980 against all took 51 us. (Wide variant: batches up
+  // to the SM count.)
   {
+    constexpr uint32_t kRankAll = 256, kRankSel = kRerankMax / 2;  // (kRankSel pairs fit cand_d + cand_i)
     unsigned long long* sk = reinterpret_cast<unsigned long long*>(fsm + L.sd);
     for (uint32_t j = tid; j < nc; j += kFinishThreads) {
       float dj = cand_x[j] + 0.f;  // -0 -> +0
@@ -1539,27 +1623,51 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       sk[j] = (static_cast<unsigned long long>(order_key(dj)) << 32) | cand_i[j];
     }
     __syncthreads();
+    const unsigned long long* rk = sk;
+    uint32_t nr = nc;
+    // (wide variant only: in the narrow one the selection's registers would spill)
+    if (kWide && nc > kRankAll && k < nc) {  // CTA-uniform
+      const uint32_t kd = radix_select(
+          [&](auto&& f) {
+            for (uint32_t j = tid; j < nc; j += kFinishThreads) f(uint32_t(sk[j] >> 32));
+          },
+          k, 4);
+      unsigned long long* sel = reinterpret_cast<unsigned long long*>(fsm + L.cd);  // cand_d, cand_i: free
+      if (tid == 0) s_staged = 0;
+      __syncthreads();
+      for (uint32_t j = tid; j < nc; j += kFinishThreads)
+        if (uint32_t(sk[j] >> 32) <= kd) {
+          const uint32_t at = atomicAdd(&s_staged, 1u);
+          if (at < kRankSel) sel[at] = sk[j];
+        }
+      __syncthreads();
+      if (s_staged <= kRankSel) {  // (else every candidate is ranked: more ties than that)
+        rk = sel;
+        nr = s_staged;
+      }
+      __syncthreads();
+    }
     // gs consecutive lanes share one candidate, each counting every gs-th pair (then a butterfly
     // over the group), so few candidates still keep every warp busy: the count is a chain of
     // dependent compares, slow on one warp per scheduler.
     uint32_t gs = 1;
-    while (gs < 32 && gs * 2 * nc <= kFinishThreads) gs *= 2;
+    while (gs < 32 && gs * 2 * nr <= kFinishThreads) gs *= 2;
     const uint32_t part = uint32_t(tid) & (gs - 1);
-    for (uint32_t j0 = 0; j0 < nc; j0 += kFinishThreads / gs) {  // CTA-uniform
+    for (uint32_t j0 = 0; j0 < nr; j0 += kFinishThreads / gs) {  // CTA-uniform
       const uint32_t j = j0 + uint32_t(tid) / gs;
-      const unsigned long long kj = j < nc ? sk[j] : 0ull;
+      const unsigned long long kj = j < nr ? rk[j] : 0ull;
       uint32_t rank = 0;
-      if (j < nc) {
-        const uint32_t cnt = (nc - part + gs - 1) / gs;  // pairs part, part + gs, ...
+      if (j < nr) {
+        const uint32_t cnt = (nr - part + gs - 1) / gs;  // pairs part, part + gs, ...
 #pragma unroll 4
         for (uint32_t i = 0; i < cnt; ++i) {
           const uint32_t t = part + i * gs;
-          const unsigned long long kt = sk[t];
+          const unsigned long long kt = rk[t];
           rank += uint32_t(kt < kj) | (uint32_t(kt == kj) & uint32_t(t < j));
         }
       }
       for (uint32_t o = 1; o < gs; o <<= 1) rank += __shfl_xor_sync(kFull, rank, int(o));
-      if (j < nc && part == 0) {
+      if (j < nr && part == 0) {
         const float dj = key_float(uint32_t(kj >> 32));
         const uint32_t ij = uint32_t(kj);
         if (rank < k) {
@@ -1911,7 +2019,7 @@ __device__ __forceinline__ void prepare_query_warp(const float* q, uint32_t ldq,
 // The e4m3 form of prepare_query_warp (the certified path over the e4m3 copy): per query its
 // scale max |q| / 448 (as to_fp8_kernel takes it), its e4m3 row (stride dpo bytes, padding
 // zero), the squared FP32 norm, and with margins E from the sums |q~|^2 and |q~ - q|^2 (q~ = e4m3
-// value x scale; FP64 from exact products, rounded up) and the e4m3 rows' bounds.
+// value x scale) and the e4m3 rows' bounds.
 template <bool L2>
 __device__ __forceinline__ void prepare_query_warp_f8(const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
                                                       uint32_t dp, uint32_t dpo, uint8_t* q8, float* qscale,
@@ -1921,11 +2029,21 @@ __device__ __forceinline__ void prepare_query_warp_f8(const float* q, uint32_t l
   const uint32_t qq = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (qq >= nq) return;
   const float* s = q + size_t(qq) * ldq;
+  // The row in registers, four columns a lane per step (columns 4 (32 u + lane) ..; dims up to
+  // 32 x 4 x kF8Steps), loaded in one round trip; the scale needs its maximum before any byte.
+  constexpr int kF8Steps = int(kPrepSampleDim / 128);
+  float4 v[kF8Steps];
   float mx = 0.f, q2 = 0.f;
-  for (uint32_t c = lane; c < dim; c += 32) {
-    const float v = s[c];
-    mx = fmaxf(mx, fabsf(v));
-    q2 = fmaf(v, v, q2);
+#pragma unroll
+  for (int u = 0; u < kF8Steps; ++u) {
+    const uint32_t c = 4u * (32u * uint32_t(u) + lane);
+    v[u] = make_float4(c < dim ? s[c] : 0.f, c + 1 < dim ? s[c + 1] : 0.f, c + 2 < dim ? s[c + 2] : 0.f,
+                       c + 3 < dim ? s[c + 3] : 0.f);
+  }
+#pragma unroll
+  for (int u = 0; u < kF8Steps; ++u) {
+    mx = fmaxf(fmaxf(mx, fmaxf(fabsf(v[u].x), fabsf(v[u].y))), fmaxf(fabsf(v[u].z), fabsf(v[u].w)));
+    q2 = fmaf(v[u].x, v[u].x, fmaf(v[u].y, v[u].y, fmaf(v[u].z, v[u].z, fmaf(v[u].w, v[u].w, q2))));
   }
   for (int o = 16; o > 0; o >>= 1) {
     mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
@@ -1933,15 +2051,25 @@ __device__ __forceinline__ void prepare_query_warp_f8(const float* q, uint32_t l
   }
   const float sc = mx > 0.f ? mx / 448.f : 1.f;
   const float inv = 1.f / sc;
-  double res = 0.0, accb = 0.0;
-  for (uint32_t c = lane; c < dpo; c += 32) {
-    const float v = c < dim ? s[c] : 0.f;
-    const uint8_t b = c < dim ? uint8_t(__nv_cvt_float_to_fp8(v * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
-    q8[size_t(qq) * dpo + c] = b;
-    const double xt = double(e4m3_value(b)) * double(sc);  // exact
-    const double e = xt - double(v);
-    res = fma(e, e, res);
-    accb = fma(xt, xt, accb);
+  // |q~ - q|^2 and |q~|^2 in FP32: e = fma(b, sc, -q) rounds the exact difference once (relative
+  // u), and the sums carry cert_error's (1 + 2 d u) inflation, far above those per-term roundings
+  // (FP64 here took the preparation from ~1.5 to 5 us).
+  float res = 0.f, accb = 0.f;
+  auto one = [&](float x, uint32_t c) -> uint32_t {
+    const uint8_t b = c < dim ? uint8_t(__nv_cvt_float_to_fp8(x * inv, __NV_SATFINITE, __NV_E4M3)) : uint8_t(0);
+    const float bv = e4m3_value(b);
+    const float e = fmaf(bv, sc, -x);
+    const float xt = __fmul_ru(fabsf(bv), sc);  // |q~_i| rounded up
+    res = fmaf(e, e, res);
+    accb = fmaf(xt, xt, accb);
+    return b;
+  };
+#pragma unroll
+  for (int u = 0; u < kF8Steps; ++u) {
+    const uint32_t c = 4u * (32u * uint32_t(u) + lane);
+    if (c >= dpo) break;
+    const uint32_t w = one(v[u].x, c) | (one(v[u].y, c + 1) << 8) | (one(v[u].z, c + 2) << 16) | (one(v[u].w, c + 3) << 24);
+    *reinterpret_cast<uint32_t*>(q8 + size_t(qq) * dpo + c) = w;  // dpo is a multiple of 16
   }
   for (int o = 16; o > 0; o >>= 1) {
     res += __shfl_xor_sync(kFull, res, o);
@@ -1952,7 +2080,8 @@ __device__ __forceinline__ void prepare_query_warp_f8(const float* q, uint32_t l
     if (qnorm) qnorm[qq] = q2;
     if (gthr) gthr[qq] = kKeyNone;
     if (margin) {
-      const float e = cert_error<L2, true>(q2, __double2float_ru(accb), __double2float_ru(res), dp, xbound);
+      // (the difference's single rounding: one more u on each term of |q~ - q|^2)
+      const float e = cert_error<L2, true>(q2, accb, __fmul_ru(res, 1.f + 4.f * 5.9604644775390625e-08f), dp, xbound);
       err[qq] = e;
       margin[qq] = __fmul_ru(factor, e);
     }
@@ -2336,6 +2465,9 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
   const bool wide = grid <= uint32_t(sms);
   auto* kern = a.l2 ? (wide ? finish_kernel<true, true> : finish_kernel<true, false>)
                     : (wide ? finish_kernel<false, true> : finish_kernel<false, false>);
+  const uint32_t c = a.cluster;
+  if (c > 1 && wide && !a.hdr && c <= 8 && grid * c <= uint32_t(sms))
+    return launch_kernel_cluster(kern, dim3(grid * c), dim3(kFinishThreads), smem, stream, pdl, c, a);
   return launch_kernel(kern, dim3(grid), dim3(kFinishThreads), smem, stream, pdl, a);
 }
 
@@ -2345,7 +2477,7 @@ cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uin
                                    float* qscale, uint32_t dpo) {
   if (nq == 0) return cudaSuccess;
   if (!q || !qb || ldq < dim || dp < dim || (margin && (!err || !xbound || !(factor >= 0.f))) ||
-      (qscale && (dpo < dim || dpo % 16 != 0)))
+      (qscale && (dpo < dim || dpo % 16 != 0 || dpo > kPrepSampleDim)))
     return cudaErrorInvalidValue;
   PrepSample smp{};
   unsigned blocks = (nq + 3) / 4;

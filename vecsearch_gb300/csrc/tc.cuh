@@ -78,6 +78,10 @@ struct TcArgs {
   // to dump[q][split * sample_tiles * 128 + j]; no shortlist is kept.
   float* dump;
   uint32_t sample_tiles;
+  // Sample pass with dump_min set: the smallest distance of each 32 rows only, to
+  // dump[q][split * sample_tiles * 8 + j] (the k-th smallest of these minima still bounds the k-th
+  // smallest sampled distance from above: k of the 32-row groups each hold a row at or below it).
+  uint32_t dump_min;
   // Main pass: per-query starting threshold (the k'-th smallest sampled distance), or nullptr.
   const float* thr_init;
   // Certified path: per-query margin m, or nullptr. A compaction that holds at least kk entries
@@ -205,6 +209,9 @@ struct FinishArgs {
   uint32_t stage_cap;      // list entries staged in shared memory at most (<= kFinishStageMax)
   uint32_t lists_per_split;  // lists of each split (the shortlist kernel's tc_groups(kp)); 0 = 1
   uint32_t sorted_lists;     // 1: every list is sorted by (dist, id) (kSortedListQueries)
+  // CTAs per query (a thread-block cluster; at most 8, and nq x cluster at most the SM count,
+  // else 1): rank 0 does all but the rerank, which the cluster shares. 0 or 1: one CTA.
+  uint32_t cluster;
   // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
   // FP32 row into fq row j (stride dp), its per-query mask (qmask row q, mask_ld words) into fmask
   // row j, or (serving) its filter pointer into fmask_ptrs[j]; tally counts them. Each optional.
@@ -251,7 +258,7 @@ constexpr uint32_t kPrepSampleRows = 4096;
 // [max |x~ - x|, max |x|, max |x~|] (x~ = bf16 row), and margin[q] = factor x E, both rounded up;
 // and *fails = 0 when fails is set.
 // qscale set: the certified path over the e4m3 copy; qb then receives e4m3 rows (stride dpo bytes,
-// a multiple of 16) with qscale[q] = max |q| / 448, E covers the e4m3 roundings (xbound: the e4m3
+// a multiple of 16, at most kPrepSampleDim) with qscale[q] = max |q| / 448, E covers the e4m3 roundings (xbound: the e4m3
 // rows' bounds from launch_to_fp8), and the rest is as above.
 cudaError_t launch_prepare_queries(const PrepSample* sample, const float* q, uint32_t ldq, uint32_t nq, uint32_t dim,
                                    uint32_t dp, void* qb,

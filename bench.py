@@ -57,13 +57,19 @@ sys.path.insert(0, ROOT)
 MEASURED_TRAFFIC_262K = {("scan", 384): 406_000_000, ("tc", 384): 204_550_000}
 
 
+def uses_e4m3(idx, batch, k, dim):
+    """Whether a certified search of this shape reads the e4m3 copy (the library's rule)."""
+    return batch <= idx.get_tunable("cert_fp8_max_batch") and k <= 16 and (dim + 15) // 16 * 16 <= 1024
+
+
 def measured_traffic(kernel, n, dim, batch, k, metric):
     """(bytes per launch for n rows at this batch, k and metric, source) or (None, reason)."""
     t = MEASURED_TRAFFIC_262K.get((kernel, dim))
     if t is None:
         return None, "no ncu capture of this kernel at this dim"
-    per_row = (t - (dim * 4 if kernel == "scan" else dim * 2)) / 262_144  # less the one query of the capture
-    extra = batch * dim * (4 if kernel == "scan" else 2) + batch * k * 8 + (n * 4 if metric == "l2" and kernel == "tc" else 0)
+    qb = {"scan": 4, "tc": 2, "tc8": 1}[kernel]  # query bytes per dimension
+    per_row = (t - dim * qb) / 262_144  # less the one query of the capture
+    extra = batch * dim * qb + batch * k * 8 + (n * 4 if metric == "l2" and kernel != "scan" else 0)
     exact = batch == 1 and k == 10 and metric == "ip"
     src = ("ncu capture at 262,144 rows, scaled by rows" if exact else
            "ncu capture at 262,144 rows (batch 1, k 10, cosine): bytes per row scaled by rows, plus this "
@@ -512,7 +518,14 @@ def run_ours(a):
     # (method auto on a large index), else the FP32 scan kernel
     scan_avg_ms = scan_ms / max(launches, 1)
     peak, peak_kind = peaks()
-    if info.get("tc_exact"):
+    if info.get("tc_exact") and uses_e4m3(idx, a.batch, a.k, a.dim):
+        # the e4m3 rows once with their FP32 scales, the e4m3 queries (and, for L2, the row norms)
+        d8 = (a.dim + 15) // 16 * 16
+        alg_bytes = a.n * (d8 + 4) + a.batch * d8 + (a.n * 4 if a.metric == "l2" else 0)
+        traffic, tsrc = measured_traffic("tc8", a.n, a.dim, a.batch, a.k, a.metric)
+        kernel = "tc_shortlist_kernel (e4m3 tcgen05 pass over the rows; certified exact path)"
+        dtype = "e4m3 products (FP32 scale per row and query), f32 accumulation and results"
+    elif info.get("tc_exact"):
         alg_bytes = a.n * a.dim * 2 + a.batch * a.dim * 2  # the bf16 rows once, the bf16 queries
         traffic, tsrc = measured_traffic("tc", a.n, a.dim, a.batch, a.k, a.metric)
         kernel = "tc_shortlist_kernel (bf16 tcgen05 pass over the rows; certified exact path)"
@@ -545,9 +558,11 @@ def run_ours(a):
             info_b = {}
             ms_b, scan_b, _, l_b = time_device(idx, torch, qd, a, b, st, 3, stream, out=info_b)
             flops = 2.0 * a.n * a.dim * b
-            row_bytes = a.n * a.dim * (2 if info_b.get("tc_exact") else 4)  # rows read by the auto path
+            e8 = bool(info_b.get("tc_exact")) and uses_e4m3(idx, b, a.k, a.dim)
+            # rows read by the auto path: e4m3 (+ its scales), bf16 or FP32
+            row_bytes = a.n * ((a.dim + 15) // 16 * 16 + 4) if e8 else a.n * a.dim * (2 if info_b.get("tc_exact") else 4)
             row = {"batch": b, "qps": round(b * st / (ms_b / 1e3), 1), "ms_per_batch": round(ms_b / st, 4),
-                   "auto_path": "tc_exact" if info_b.get("tc_exact") else "fp32",
+                   "auto_path": ("tc_exact_e4m3" if e8 else "tc_exact") if info_b.get("tc_exact") else "fp32",
                    "kernel_gbs": round(row_bytes / (scan_b / l_b / 1e3) / 1e9, 1),
                    "kernel_tflops": round(flops / (scan_b / l_b / 1e3) / 1e12, 2)}
             if b == 1:

@@ -48,13 +48,18 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # DRAM bytes per launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on a 262,144-row case of the same kernel at batch 1, k = 10, cosine:
-#   scan: the FP32 scan kernel, 402.69 MB read + 3.31 MB written per 262,144-row launch
-#   tc:   the certified path's bf16 shortlist main pass, 201.40 MB read + 3.15 MB written
+# dram__bytes_write.sum) at batch 1, k = 10, cosine, 384 dims, on a case of the same kernel:
+#   scan: the FP32 scan kernel, 262,144 rows: 402.69 MB read + 3.31 MB written
+#   tc:   the certified path's bf16 shortlist main pass, 262,144 rows: 201.40 MB read + 3.15 MB
+#         written
+#   tc8:  the certified path's e4m3 shortlist main pass, 393,216 rows (the smallest base the
+#         certified path takes at batch 1): 152.65 MB read + 0.10 MB written (mean of 4 launches)
 # The rows dominate (reads equal the algorithmic bytes there), so a launch's traffic is taken as
 # the measured bytes per row times the rows scanned, plus the configuration's own query, norm
-# and list bytes: queries (dim x 4, bf16 copy dim x 2) and, for L2, the rows' norms (4 a row).
-MEASURED_TRAFFIC_262K = {("scan", 384): 406_000_000, ("tc", 384): 204_550_000}
+# and list bytes: queries (dim x 4, bf16 copy dim x 2, e4m3 copy dim x 1) and, for L2, the rows'
+# norms (4 a row).
+MEASURED_TRAFFIC = {("scan", 384): (262_144, 406_000_000), ("tc", 384): (262_144, 204_550_000),
+                    ("tc8", 384): (393_216, 152_748_800)}
 
 
 def uses_e4m3(idx, batch, k, dim):
@@ -64,16 +69,17 @@ def uses_e4m3(idx, batch, k, dim):
 
 def measured_traffic(kernel, n, dim, batch, k, metric):
     """(bytes per launch for n rows at this batch, k and metric, source) or (None, reason)."""
-    t = MEASURED_TRAFFIC_262K.get((kernel, dim))
-    if t is None:
+    m = MEASURED_TRAFFIC.get((kernel, dim))
+    if m is None:
         return None, "no ncu capture of this kernel at this dim"
+    rows, t = m
     qb = {"scan": 4, "tc": 2, "tc8": 1}[kernel]  # query bytes per dimension
-    per_row = (t - dim * qb) / 262_144  # less the one query of the capture
+    per_row = (t - dim * qb) / rows  # less the one query of the capture
     extra = batch * dim * qb + batch * k * 8 + (n * 4 if metric == "l2" and kernel != "scan" else 0)
     exact = batch == 1 and k == 10 and metric == "ip"
-    src = ("ncu capture at 262,144 rows, scaled by rows" if exact else
-           "ncu capture at 262,144 rows (batch 1, k 10, cosine): bytes per row scaled by rows, plus this "
-           "configuration's query, list and norm bytes")
+    src = (f"ncu capture at {rows:,} rows, scaled by rows" if exact else
+           f"ncu capture at {rows:,} rows (batch 1, k 10, cosine): bytes per row scaled by rows, plus "
+           "this configuration's query, list and norm bytes")
     return int(round(per_row * n + extra)), src
 
 

@@ -214,6 +214,8 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   the bf16 copy's bytes) with a bound E that covers its roundings; results stay bit-identical to
  *   VSG_METHOD_SKINNY. 0 keeps every batch on the bf16 copy.
  *   "cert_fp8_sample_rows" (default 32768): rows sampled for those searches' starting thresholds.
+ *   "cert_prefetch_max_batch" (default 16): those searches of at most this many queries prefetch
+ *   each row their shortlists take into L2 during the pass over the rows, for the exact rerank.
  *   "finish_cluster" (default 8, 1 to 8): CTAs per query sharing the certified path's FP32 rerank
  *   (a thread-block cluster) when the batch times this fits the SM count; else one CTA a query. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);

@@ -186,6 +186,10 @@ struct vsg_index {
   // reranked rows a query and ran at 0.15-0.5x.
   double cert_fp8_max_batch = 16;
   double cert_fp8_sample_rows = 32768;
+  // Certified searches over the e4m3 copy of at most this many queries prefetch every row their
+  // lists take into L2 during the main pass (one bulk prefetch a row), for the finish kernel's
+  // rerank of ~1,000 rows a query; 0: none.
+  double cert_prefetch_max_batch = 16;
   // Certified path: CTAs per query in the finish kernel when the batch times it fits the SMs
   // (1-8; k = 100 at batches 1-8 on the bf16 copy ran 9-10 % faster with 8).
   double finish_cluster = 8;
@@ -650,6 +654,10 @@ struct vsg_index {
     a.status = status_word();
     a.wait_ns = wait_ns();
     a.stall = stall_next ? 1u : 0u;
+    if (certify && f8 && double(nq) <= cert_prefetch_max_batch) {
+      a.xf = static_cast<const float*>(x.get());  // (dp: a multiple of 4)
+      a.xf_ld = uint32_t(dp);
+    }
     Timing* tm = profiling ? next_timing() : nullptr;
     // Batches first score a sample of rows (whole tiles at the head of every split; 16K rows for
     // 8+ queries, 4K below, unless tuned) and start each query at the k'-th best sampled distance, so the
@@ -752,6 +760,7 @@ struct vsg_index {
     // Small batches rerank over a cluster of CTAs per query (the e4m3 copy's wider margin keeps
     // ~1,000 rows to rerank at 1M x 384, ~20 us on one SM).
     fa.cluster = certify && double(nq * size_t(finish_cluster)) <= double(sms) ? uint32_t(finish_cluster) : 1u;
+    fa.rows_in_l2 = a.xf ? 1u : 0u;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
     if (certify) {
       fa.thr_init = a.thr_init;

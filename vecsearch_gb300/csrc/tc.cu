@@ -406,8 +406,11 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
   const uint32_t nitems = persistent ? a.hdr->items : nqb * nsplit;
   constexpr uint32_t cap = 32u * E;
   __shared__ uint32_t item_slot;
-  __shared__ __align__(16) float xs_buf[4 * G][L2 ? kTcRows : 1];  // epilogue warps' row norms of a tile (L2)
-  __shared__ __align__(16) float xsc_buf[4 * G][F8 ? kTcRows : 1];  // ... and row scales (e4m3 copies)
+  // Epilogue warps' row norms (L2) and row scales (e4m3 copies) of their group's columns of a
+  // tile, two tiles' worth (the next tile's are copied in while this one's are used).
+  constexpr uint32_t kGroupRows = kTcRows / G;
+  __shared__ __align__(16) float xs_buf[4 * G][2][L2 ? kGroupRows : 4];
+  __shared__ __align__(16) float xsc_buf[4 * G][2][F8 ? kGroupRows : 4];
 
   if (tid == 0) {
     for (uint32_t s = 0; s < stages; ++s) {
@@ -645,16 +648,53 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
         if (lane == 0) atomicExch(a.status, kDevTimeout);
         ok = false;
       }
+      // The norms and scales of this group's columns of tile tt into buffer sb, copied without
+      // registers (16 bytes a lane) one tile ahead of their use: loaded after the accumulator's
+      // wait they put a DRAM round trip into every tile. Rows at or past n read row n - 1 (their
+      // columns are never allowed). One commit group per call, also when there is nothing to copy.
+      // A warp whose 32 query slots are all padding (small batches) only keeps the tile handshake.
+      const bool live = __any_sync(kFull, qvalid);
+      auto stage_rows = [&](uint32_t tt, uint32_t sb) {
+        if constexpr (L2 || F8) {
+          if (live && tt < ntiles) {
+            const uint32_t rb = row_begin + tt * kTcRows + group * kGroupRows;
+            for (uint32_t p = uint32_t(lane) * 4u; p < kGroupRows; p += 128u) {
+              const uint32_t row = rb + p;
+              if (row + 4u <= a.n) {  // (row is a multiple of 4: 16-byte aligned)
+                if constexpr (L2) cp_async16(&xs_buf[ew][sb][p], a.xnorm + row, true);
+                if constexpr (F8) cp_async16(&xsc_buf[ew][sb][p], a.xscale + row, true);
+              } else {
+#pragma unroll
+                for (uint32_t i = 0; i < 4; ++i) {
+                  const uint32_t r = min(row + i, a.n - 1);
+                  if constexpr (L2) xs_buf[ew][sb][p + i] = __ldg(a.xnorm + r);
+                  if constexpr (F8) xsc_buf[ew][sb][p + i] = __ldg(a.xscale + r);
+                }
+              }
+            }
+          }
+          cp_async_commit();
+        }
+      };
+      stage_rows(0, tglob & 1);
       for (uint32_t t = 0; t < ntiles && ok; ++t, ++tglob) {
         const uint32_t b = tglob & 1, use = tglob >> 1;
         tighten(gkey);
         gkey = gq ? ld_relaxed(gq) : kKeyNone;
+        stage_rows(t + 1, b ^ 1u);  // (buffer b ^ 1 held the previous tile's, done with)
         if (!__all_sync(kFull, mbar_wait(&tfull[b], use & 1, wl))) {
           if (lane == 0) atomicExch(a.status, kDevTimeout);
           ok = false;
           break;
         }
         tc_fence_after();
+        if constexpr (L2 || F8) {  // this tile's copies (the next tile's may still be in flight)
+          cp_async_wait<1>();
+          __syncwarp();
+        }
+        const float* xs = xs_buf[ew][b];    // column j of chunk cg at (cg - cg0) x 32 + j
+        const float* xsc = xsc_buf[ew][b];
+        const int cg0 = int(group) * (kTcRows / 32 / G);
         const uint32_t r0 = row_begin + t * kTcRows;
         const uint32_t tbase = tmem_base + ((quarter * 32) << 16) + b * kTcRows;
         // Allowed rows of chunk c (32 rows from c0): inside the split, real query, filter bit.
@@ -663,8 +703,9 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
           if (qmask && al) al &= __ldg(qmask + (c0 >> 5));
           return qvalid ? al : 0u;
         };
-        if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-uniform
-                       // (a.dump): lanes of padded query slots take it too and store nothing.
+        if (!live) {
+        } else if (a.dump) {  // sample pass: raw distances out, nothing kept. The branch is warp-
+                              // uniform (a.dump): lanes of padded query slots take it too and store nothing.
 #pragma unroll 1
           for (uint32_t c = group * (kTcRows / 32 / G); c < (group + 1) * (kTcRows / 32 / G); ++c) {
             uint32_t v[32];
@@ -674,12 +715,11 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
             const uint32_t allow = allowed(c0);
             if (dump_row) {
               float o[32];
+              const int at = (int(c) - cg0) * 32;
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
-                const uint32_t row = c0 + uint32_t(j);
-                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * __ldg(a.xscale + min(row, a.n - 1)))
-                                    : __uint_as_float(v[j]);
-                const float dist = L2 ? l2_approx(qn, __ldg(a.xnorm + min(row, a.n - 1)), sc) : 1.f - sc;
+                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * xsc[at + j]) : __uint_as_float(v[j]);
+                const float dist = L2 ? l2_approx(qn, xs[at + j], sc) : 1.f - sc;
                 o[j] = ((allow >> j) & 1u) ? dist : __int_as_float(0x7f800000);
               }
               if (a.dump_min) {  // the 32 rows' smallest distance only
@@ -700,21 +740,10 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
           // (the largest score, or the smallest distance with the same expression as the
           // append) and one vote per half; the per-score path runs only when some lane may have
           // a candidate.
-          float* xs = xs_buf[ew];
-          float* xsc = xsc_buf[ew];
-          if constexpr (L2) {
-#pragma unroll
-            for (int c = 0; c < kTcRows / 32; ++c)
-              xs[c * 32 + lane] = __ldg(a.xnorm + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
-          }
-          if constexpr (F8) {  // the rows' scales (shared by the warp; each lane applies its query's)
-#pragma unroll
-            for (int c = 0; c < kTcRows / 32; ++c)
-              xsc[c * 32 + lane] = __ldg(a.xscale + min(r0 + uint32_t(c * 32 + lane), a.n - 1));
-          }
-          if (L2 || F8) __syncwarp();
+          // (the rows' scales are shared by the warp; each lane applies its query's)
 #pragma unroll 1
-          for (int cg = int(group) * (kTcRows / 32 / G); cg < int(group + 1) * (kTcRows / 32 / G); ++cg) {
+          for (int cg = cg0; cg < cg0 + kTcRows / 32 / G; ++cg) {
+            const int at = (cg - cg0) * 32;
             // Room for this chunk's appends, made before its scores are loaded (the out-of-line
             // sort then runs with few live registers).
             compact_lanes(__ballot_sync(kFull, cnt + 32 > cap), false);
@@ -728,8 +757,8 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
               uint32_t m[4] = {0u, 0u, 0u, 0u};  // four interleaved chains
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
-                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * xsc[cg * 32 + j]) : __uint_as_float(v[j]);
-                const bool p = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) <= thr_d : sc >= s_lo;
+                const float sc = F8 ? __uint_as_float(v[j]) * (qsc * xsc[at + j]) : __uint_as_float(v[j]);
+                const bool p = L2 ? l2_approx(qn, xs[at + j], sc) <= thr_d : sc >= s_lo;
                 m[j & 3] |= p ? (1u << j) : 0u;
               }
               bits = (m[0] | m[1] | m[2] | m[3]) & allowed(r0 + uint32_t(cg) * 32);
@@ -745,23 +774,25 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
                 mine &= mine - 1u;
                 const float raw = __uint_as_float(pick32(v, j));
                 if (has) {
-                  const float sc = F8 ? raw * (qsc * xsc[cg * 32 + j]) : raw;
-                  const float dist = L2 ? l2_approx(qn, xs[cg * 32 + j], sc) : 1.f - sc;
+                  const float sc = F8 ? raw * (qsc * xsc[at + j]) : raw;
+                  const float dist = L2 ? l2_approx(qn, xs[at + j], sc) : 1.f - sc;
                   if (nb_less(dist, c0 + j, thr_d, thr_i)) {
                     wd[size_t(lane) * cap + cnt] = dist;
                     wi[size_t(lane) * cap + cnt] = c0 + j;
                     ++cnt;
+                    if (a.xf) bulk_prefetch_l2(a.xf + size_t(c0 + j) * a.xf_ld, a.xf_ld * 4u);
                   }
                 }
               }
             }
           }
-          if (L2 || F8) __syncwarp();  // the next tile rewrites xs / xsc
         }
+        if (L2 || F8) __syncwarp();  // every lane is done with buffer b before it is copied into again
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[b]);
       }
+      if constexpr (L2 || F8) cp_async_wait<0>();  // (an early exit may leave copies in flight)
       if (a.dump) {  // sample pass: tiles past the split's end read as +inf
         if (dump_row && group == 0)
           for (uint32_t j = ntiles * dump_per_tile; j < sample_tiles * dump_per_tile; ++j)
@@ -1075,9 +1106,10 @@ __device__ __forceinline__ void st_cluster_f32(uint32_t addr, float v) {
 //      producer writes them so), and these heads come in with the lengths: the k-th smallest head
 //      h bounds the k-th best a_k from above (k lists hold an entry at or below it), so no entry
 //      above c = h + margin can be reranked, and only the lists whose head is at or below c are
-//      read, their entries above c dropped. (At batch 1 the lists held ~2,800 entries for ~70
-//      reranked rows: no split sees enough of the query's near rows for its own k-th best to be
-//      tight.)
+//      read, their entries above c dropped. (At batch 1 over the bf16 copy the lists held ~2,800
+//      entries for ~70 reranked rows: no split sees enough of the query's near rows for its own
+//      k-th best to be tight.) With margins and no more entries in all than the rerank takes in
+//      one pass (two with a cluster), every entry is staged and reranked without a bound.
 //   2. Cut: the `target`-th smallest approximate distance (k with margins, else the shortlist
 //      size k') by exact radix selection on order keys (a min / max pass, then 8-bit rounds below
 //      the highest bit where the keys differ); the cut is that value, plus the margin (rounded
@@ -1086,8 +1118,9 @@ __device__ __forceinline__ void st_cluster_f32(uint32_t addr, float v) {
 //   3. Rerank: the exact FP32 distance of every kept row with the scan kernel's arithmetic (lane
 //      l sums 16-byte chunks l, l + 32, ... in order, then a butterfly over lanes 16 .. 1), so a
 //      candidate set that holds the true top k yields the scan kernel's results bit for bit.
-//   4. The top k by (FP32 dist, id): a bitonic sort of (order key, id) pairs in shared memory;
-//      the k-th FP32 distance D_k.
+//   4. The top k by (FP32 dist, id): each candidate's rank among the (order key, id) pairs,
+//      counted in shared memory (beyond 256 candidates, among those at or below a bound of the
+//      k-th key only); the k-th FP32 distance D_k.
 //   5. Certificate (fail_count set): every row left out has approximate distance >= L = min(sample
 //      threshold, final shared threshold, the cut when it left entries out); if L - E > D_k
 //      (rounded down) no such row can enter the top k, else the query is listed for the scan.
@@ -1137,7 +1170,10 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   constexpr int nwarps = kFinishThreads / 32;
   const bool serving = a.hdr != nullptr;
   if (serving && q >= a.hdr->nq) return;
-  if (a.status && *reinterpret_cast<const volatile int*>(a.status) != 0) return;  // lists may be stale
+  // A shortlist kernel that gave up may have left stale lists: nothing is used then (the status is
+  // read here and tested once the first loads, harmless either way, are issued; CTA-uniform, and
+  // the same for every CTA of a cluster, before any cluster barrier).
+  const bool stale = a.status && *reinterpret_cast<const volatile int*>(a.status) != 0;
   const uint32_t nsplit = (serving ? a.hdr->nsplit : a.nsplit) * max(1u, a.lists_per_split);  // lists
   uint32_t k, sel;
   size_t out_off;
@@ -1203,6 +1239,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     }
   };
   if (crank != 0) {  // (CTA-uniform) a cluster member: the query, rank 0's candidates, a share
+    if (stale) return;
     if (L.cd > 0)
       for (uint32_t c = tid; c < a.dp; c += kFinishThreads) qs[c] = qrow[c];
     __syncthreads();
@@ -1237,16 +1274,19 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     }
     if (tid == 0) s_off[0] = 0;
   }
+  if (stale) return;
   __syncthreads();
   // ---- 2. the cut (selection; used on the heads first) ----
   // The rank-th smallest key of `each_key`'s keys (1 <= rank <= their count): exact after enough
   // 8-bit rounds, or after `rounds` rounds the largest key of the bucket holding it (an upper
-  // bound). CTA-uniform result.
+  // bound). CTA-uniform result. each_key calls f(key, valid) for every key.
   auto radix_select = [&](auto&& each_key, uint32_t rank, int rounds) -> uint32_t {
     uint32_t lo = 0xFFFFFFFFu, hi = 0u;
-    each_key([&](uint32_t key) {
-      lo = min(lo, key);
-      hi = max(hi, key);
+    each_key([&](uint32_t key, bool ok) {
+      if (ok) {
+        lo = min(lo, key);
+        hi = max(hi, key);
+      }
     });
     lo = __reduce_min_sync(kFull, lo);
     hi = __reduce_max_sync(kFull, hi);
@@ -1274,8 +1314,8 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       const uint32_t bmask = (1u << nb) - 1u;
       for (int b = tid; b < 256; b += kFinishThreads) hist[b] = 0;
       __syncthreads();
-      each_key([&](uint32_t key) {
-        if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & bmask], 1u);
+      each_key([&](uint32_t key, bool ok) {
+        if (ok && (key & mask) == prefix) atomicAdd(&hist[(key >> shift) & bmask], 1u);
       });
       __syncthreads();
       if (warp == 0) {  // the first bucket whose running count reaches `remaining`
@@ -1322,20 +1362,30 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // The heads' bound c (order key): the k-th smallest head, to 16 bits below the heads' highest
   // differing bit (rounded up to its bucket's end), plus the margin, rounded up. Fewer than k
   // non-empty lists: every list is read.
+  // Certified path with few entries in all (at most one rerank pass, two with a cluster): every
+  // entry is staged and reranked, and no bound is needed (at batch 1 over the e4m3 copy every list
+  // entry was under it, and its select took ~1.8 us).
+  const uint32_t whole_cap = uint32_t(G * nwarps) * (csize > 1 ? 2u * csize : 1u);
+  const bool few = by_heads && s_all <= whole_cap && s_all <= a.stage_cap;  // CTA-uniform
   uint32_t c_key = kKeyAll;
   bool direct = false;  // sorted lists under the heads' bound: read in runs (below)
-  if (by_heads && k > 0 && s_heads >= k) {  // CTA-uniform
+  if (by_heads && !few && k > 0 && s_heads >= k) {  // CTA-uniform
     const uint32_t h = radix_select(
         [&](auto&& f) {
-          for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads)
-            if (hkey[sp] != kKeyAll) f(hkey[sp]);
+          for (uint32_t s0 = 0; s0 < nsplit; s0 += kFinishThreads) {
+            const uint32_t sp = s0 + uint32_t(tid);
+            const uint32_t key = sp < nsplit ? hkey[sp] : kKeyAll;
+            f(key, key != kKeyAll);
+          }
         },
         k, 2);
     c_key = order_key(__fadd_ru(key_float(h), mg));
     if (key_float(c_key) != key_float(c_key)) c_key = kKeyAll;  // NaN: no bound
     // (wide variant only: the shortlist's sorted lists come with at most kSortedListQueries
-    // queries, and the run reader would push the narrow variant past its registers)
-    direct = kWide && a.sorted_lists != 0 && c_key != kKeyAll;
+    // queries, and the run reader would push the narrow variant past its registers). Only lists
+    // holding more entries than one load of every thread (four) covers: the flat copy below reads
+    // those in one round trip, the runs take one a run.
+    direct = kWide && a.sorted_lists != 0 && c_key != kKeyAll && s_all > 4u * kFinishThreads;
     if (!direct) {  // only the lists whose head is at or below c are read
       for (uint32_t sp = tid; sp < nsplit; sp += kFinishThreads)
         if (hkey[sp] > c_key) s_off[sp + 1] = 0;
@@ -1345,9 +1395,9 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // Appends (d, id) to the staging area when `keep` (warp-uniform call; any order); past
   // stage_cap nothing is written and the count alone grows (the passes then read the lists).
   // The row of a kept entry is also prefetched into L2 for the rerank (most kept entries are
-  // reranked; the rows are scattered over HBM, so the rerank's loads otherwise wait on DRAM). Not
-  // when a cluster shares the rerank: its CTAs load their own rows, and one SM issuing ~12,000
-  // line prefetches for ~1,000 rows took 15 us.
+  // reranked; the rows are scattered over HBM, so the rerank's loads otherwise wait on DRAM): not
+  // when the main pass did so already, nor when a cluster shares the rerank (its CTAs load their
+  // own rows; one SM issuing ~12,000 line prefetches for ~1,000 rows took 15 us).
   auto append = [&](bool keep, float d, uint32_t id) {
     const unsigned bal = __ballot_sync(kFull, keep);
     uint32_t at = 0;
@@ -1357,7 +1407,7 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       stg_d[at] = d;
       stg_i[at] = id;
     }
-    for (unsigned m = csize > 1 ? 0u : bal; m; m &= m - 1) {  // each kept row's 128-byte lines, one a lane
+    for (unsigned m = csize > 1 || a.rows_in_l2 ? 0u : bal; m; m &= m - 1) {  // a row's lines, one a lane
       const uint32_t rid = __shfl_sync(kFull, id, __ffs(m) - 1);
       if (rid < a.n) {
         const char* row = reinterpret_cast<const char*>(a.x + size_t(rid) * a.dp);
@@ -1561,14 +1611,32 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
       __syncthreads();
       return r;
     }
-    return radix_select([&](auto&& f) { each([&](uint32_t key, float, uint32_t) { f(key); }); }, rank, 4);
+    return radix_select(
+        [&](auto&& f) {  // every entry's key, warp-uniform calls
+          if (staged) {
+            for (uint32_t e0 = 0; e0 < total; e0 += kFinishThreads) {
+              const uint32_t e = e0 + uint32_t(tid);
+              f(e < total ? order_key(stg_d[e]) : 0u, e < total);
+            }
+          } else {
+            for (uint32_t sp = warp; sp < nsplit; sp += nwarps) {
+              const uint32_t len = min(lens[sp], a.kp);
+              const float* ld = a.part_d + base + size_t(sp) * a.kp;
+              for (uint32_t j0 = 0; j0 < len; j0 += 32) {
+                const uint32_t j = j0 + uint32_t(lane);
+                f(j < len ? order_key(ld[j]) : 0u, j < len);
+              }
+            }
+          }
+        },
+        rank, 4);
   };
   // keep entries with key <= cut_key (or < when strict); the heads' bound c already left out every
   // entry above it. A staged set no larger than one rerank pass (two with a cluster, whose passes
   // are short) is reranked whole: the exact cut would not save a pass.
   uint32_t cut_key = c_key;
   bool strict = false;
-  const bool whole = c_key != kKeyAll && staged && total <= uint32_t(G * nwarps) * (csize > 1 ? 2u * csize : 1u);
+  const bool whole = staged && total <= whole_cap && (c_key != kKeyAll || few);
   if (total > target && !whole) {
     const uint32_t tk = select_key(target);
     cut_key = mg >= 0.f ? order_key(__fadd_ru(key_float(tk), mg)) : tk;
@@ -1610,10 +1678,10 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
   // position, so the ranks are a permutation). The pairs sit in the staging area, free once the
   // candidates are collected (at least kRerankMax x 8 bytes). A NaN distance ranks as +inf (written
   // as a missing result) and -0 as +0: the order is the float order of the distances, then ids.
-  // More than kRankAll candidates: the k-th smallest distance key is selected first (exact radix
-  // selection), and only the candidates at or below it are ranked, among themselves (every other
-  // candidate comes after them); ranking 980 against all took 51 us. (Wide variant: batches up
-  // to the SM count.)
+  // More than kRankAll candidates: an upper bound of the k-th smallest distance key is selected
+  // first (one radix round: the end of its bucket), and only the candidates at or below it are
+  // ranked, among themselves (every other candidate comes after them); ranking 980 against all
+  // took 51 us. (Wide variant: batches up to the SM count.)
   {
     constexpr uint32_t kRankAll = 256, kRankSel = kRerankMax / 2;  // (kRankSel pairs fit cand_d + cand_i)
     unsigned long long* sk = reinterpret_cast<unsigned long long*>(fsm + L.sd);
@@ -1627,11 +1695,15 @@ __global__ void __launch_bounds__(kFinishThreads) finish_kernel(const FinishArgs
     uint32_t nr = nc;
     // (wide variant only: in the narrow one the selection's registers would spill)
     if (kWide && nc > kRankAll && k < nc) {  // CTA-uniform
+      // (one 8-bit round: the end of the bucket holding the k-th key, a few keys above it)
       const uint32_t kd = radix_select(
           [&](auto&& f) {
-            for (uint32_t j = tid; j < nc; j += kFinishThreads) f(uint32_t(sk[j] >> 32));
+            for (uint32_t j0 = 0; j0 < nc; j0 += kFinishThreads) {
+              const uint32_t j = j0 + uint32_t(tid);
+              f(j < nc ? uint32_t(sk[j] >> 32) : 0u, j < nc);
+            }
           },
-          k, 4);
+          k, 1);
       unsigned long long* sel = reinterpret_cast<unsigned long long*>(fsm + L.cd);  // cand_d, cand_i: free
       if (tid == 0) s_staged = 0;
       __syncthreads();
@@ -2149,22 +2221,45 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
   __syncthreads();
   // Every value once per pass: float4 loads (count is a multiple of 4 and rows start 16-byte
   // aligned: count = splits x tiles x 256), four independent keys per load.
+  // Up to 4,096 values (the small samples) are loaded once and kept in registers for the three
+  // passes; more are read again each pass.
   const float4* v4 = reinterpret_cast<const float4*>(v);
   const uint32_t n4 = count / 4;
+  constexpr uint32_t kCached = 4;  // float4 values a thread keeps
+  const bool cached = n4 <= kCached * blockDim.x;
+  float4 held[kCached];
+#pragma unroll
+  for (uint32_t i = 0; i < kCached; ++i) {
+    const uint32_t j = threadIdx.x + i * blockDim.x;
+    held[i] = cached && j < n4 ? v4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  // f(key, valid) for every value.
   auto each_key = [&](auto&& f) {
+    auto four = [&](const float4& x, bool ok) {
+      f(order_key(x.x), ok);
+      f(order_key(x.y), ok);
+      f(order_key(x.z), ok);
+      f(order_key(x.w), ok);
+    };
+    if (cached) {
+#pragma unroll
+      for (uint32_t i = 0; i < kCached; ++i)
+        if (i * blockDim.x < n4) four(held[i], threadIdx.x + i * blockDim.x < n4);
+    } else {
+      const uint32_t rounds = (n4 + blockDim.x - 1) / blockDim.x;
 #pragma unroll 4
-    for (uint32_t j = threadIdx.x; j < n4; j += blockDim.x) {
-      const float4 x = v4[j];
-      f(order_key(x.x));
-      f(order_key(x.y));
-      f(order_key(x.z));
-      f(order_key(x.w));
+      for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t j = threadIdx.x + r * blockDim.x;
+        four(j < n4 ? v4[j] : make_float4(0.f, 0.f, 0.f, 0.f), j < n4);
+      }
     }
   };
   uint32_t lo = 0xFFFFFFFFu, hi = 0u;
-  each_key([&](uint32_t key) {
-    lo = min(lo, key);
-    hi = max(hi, key);
+  each_key([&](uint32_t key, bool ok) {
+    if (ok) {
+      lo = min(lo, key);
+      hi = max(hi, key);
+    }
   });
   lo = __reduce_min_sync(kFull, lo);
   hi = __reduce_max_sync(kFull, hi);
@@ -2183,8 +2278,8 @@ __global__ void __launch_bounds__(256) sample_select_kernel(const float* in, uin
     for (int round = 0; round < 2; ++round) {
       for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
       __syncthreads();
-      each_key([&](uint32_t key) {
-        if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+      each_key([&](uint32_t key, bool ok) {
+        if (ok && (key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
       });
       __syncthreads();
       if (threadIdx.x < 32) {

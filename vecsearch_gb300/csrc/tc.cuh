@@ -101,6 +101,11 @@ struct TcArgs {
   // Test hook: 1 makes the epilogue warps first wait on a barrier nothing completes, so that wait
   // runs out after wait_ns and the kernel winds down with kDevTimeout.
   uint32_t stall;
+  // Main pass of a small certified batch: the FP32 rows (xf_ld floats apart, xf_ld a multiple of
+  // 4), or nullptr. Every row a list takes is prefetched into L2 (one bulk prefetch), so the
+  // finish kernel's rerank of it reads L2 instead of waiting on DRAM.
+  const float* xf;
+  uint32_t xf_ld;
 };
 
 // Per-query k'-th smallest of `count` sampled distances (row q at in + q * count) -> thr[q]; plus
@@ -212,6 +217,9 @@ struct FinishArgs {
   // CTAs per query (a thread-block cluster; at most 8, and nq x cluster at most the SM count,
   // else 1): rank 0 does all but the rerank, which the cluster shares. 0 or 1: one CTA.
   uint32_t cluster;
+  // 1: the main pass prefetched every row its lists took into L2 (TcArgs::xf); otherwise a
+  // one-CTA finish prefetches each staged row itself.
+  uint32_t rows_in_l2;
   // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
   // FP32 row into fq row j (stride dp), its per-query mask (qmask row q, mask_ld words) into fmask
   // row j, or (serving) its filter pointer into fmask_ptrs[j]; tally counts them. Each optional.

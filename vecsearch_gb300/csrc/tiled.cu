@@ -55,17 +55,6 @@ __host__ __device__ inline TiledLayout tiled_layout(int bm, uint32_t k, int stag
   return L;
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
-               "r"(valid ? 16 : 0)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 template <int BM, bool L2>
 __global__ void __launch_bounds__(kThreads, 1) tiled_kernel(const TiledArgs a) {
   constexpr int TM = BM / 16;

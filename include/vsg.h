@@ -215,9 +215,12 @@ const float* vsg_device_rows(const vsg_index* index, size_t* padded_dim);
  *   VSG_METHOD_SKINNY. 0 keeps every batch on the bf16 copy.
  *   "cert_fp8_sample_rows" (default 32768): rows sampled for those searches' starting thresholds.
  *   "cert_prefetch_max_batch" (default 16): those searches of at most this many queries prefetch
- *   each row their shortlists take into L2 during the pass over the rows, for the exact rerank.
- *   "finish_cluster" (default 8, 1 to 8): CTAs per query sharing the certified path's FP32 rerank
- *   (a thread-block cluster) when the batch times this fits the SM count; else one CTA a query. */
+ *   the rows of their shortlists into L2 as the pass over the rows writes them, for the exact
+ *   rerank.
+ *   "finish_cluster" (default 8, 1 to 16): CTAs per query sharing the certified path's FP32 rerank
+ *   (a thread-block cluster) when the batch times this fits the SM count; else one CTA a query.
+ *   "finish_cluster_one" (default 16, 1 to 16): the same for a search of one query. Sizes above 8
+ *   run as 8 on a device where such a cluster does not fit. */
 int vsg_set_tunable(vsg_index* index, const char* name, double value);
 int vsg_get_tunable(vsg_index* index, const char* name, double* value);
 

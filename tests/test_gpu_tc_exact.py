@@ -263,8 +263,13 @@ def test_tc_exact_over_e4m3_copy(gpu_ready, metric, unit, d):
     gpu = vsg.GpuBruteForceIndex(d, metric)
     gpu.add(x)
     gpu.set_tunable("cert_fp8_max_batch", 8)
-    for cluster in (1, 8):  # the finish kernel's rerank on one CTA, or shared by 8 in a cluster
+    assert gpu.get_tunable("cert_prefetch_max_batch") == 16
+    # the finish kernel's rerank on one CTA, or shared by 8 in a cluster; the kept rows prefetched
+    # into L2 by the main pass ("cert_prefetch_max_batch") or by a one-CTA finish kernel
+    for cluster, prefetch in ((1, 16), (8, 16), (16, 16), (1, 0)):
         gpu.set_tunable("finish_cluster", cluster)
+        gpu.set_tunable("finish_cluster_one", cluster)
+        gpu.set_tunable("cert_prefetch_max_batch", prefetch)
         for k in (10, 100):
             want = gpu.search(q, k, method="skinny")
             for b in (1, 3, 8):
@@ -274,9 +279,11 @@ def test_tc_exact_over_e4m3_copy(gpu_ready, metric, unit, d):
     gpu.search(q[:8], 10, method="tc_exact")
     q1, s1, f1 = gpu.tc_exact_stats()
     assert q1 - q0 == 8 and s1 - s0 <= 2  # the certificate holds for nearly every query
+    with pytest.raises(ValueError):
+        gpu.set_tunable("cert_prefetch_max_batch", -1)
 
 
-@pytest.mark.parametrize("cluster", [2, 8])
+@pytest.mark.parametrize("cluster", [2, 8, 16])
 def test_tc_exact_finish_cluster(gpu_ready, cluster):
     # "finish_cluster": the finish kernel of a small batch runs as a cluster of CTAs per query,
     # rank 0 staging and cutting, every rank reranking a share through distributed shared memory;
@@ -291,8 +298,11 @@ def test_tc_exact_finish_cluster(gpu_ready, cluster):
         want = gpu.search(q, k, method="skinny")
         for b in (1, 5, 16, 40, 160):
             _same(gpu.search(q[:b], k, method="tc_exact"), (want[0][:b], want[1][:b]))
+    gpu.set_tunable("finish_cluster_one", cluster)  # (batch 1 has its own, default 16)
+    for b in (1, 3):
+        _same(gpu.search(q[:b], 10, method="tc_exact"), (want[0][:b, :10], want[1][:b, :10]))
     with pytest.raises(ValueError):
-        gpu.set_tunable("finish_cluster", 9)
+        gpu.set_tunable("finish_cluster", 17)
 
 
 def test_tc_exact_e4m3_wide_rows_use_bf16(gpu_ready):

@@ -294,9 +294,9 @@ int vsg_set_tunable(vsg_index* h, const char* name, double value) {
     } else if (nm == "cert_prefetch_max_batch") {
       if (!(value >= 0.0 && value <= 1048576.0)) throw std::invalid_argument("cert_prefetch_max_batch must be in [0, 2^20]");
       h->cert_prefetch_max_batch = std::floor(value);
-    } else if (nm == "finish_cluster") {
-      if (!(value >= 1.0 && value <= 8.0)) throw std::invalid_argument("finish_cluster must be in [1, 8]");
-      h->finish_cluster = std::floor(value);
+    } else if (nm == "finish_cluster" || nm == "finish_cluster_one") {
+      if (!(value >= 1.0 && value <= 16.0)) throw std::invalid_argument(nm + " must be in [1, 16]");
+      (nm == "finish_cluster" ? h->finish_cluster : h->finish_cluster_one) = std::floor(value);
     } else if (nm == "host_graph_direct") {
       if (value != 0.0 && value != 1.0) throw std::invalid_argument("host_graph_direct must be 0 or 1");
       h->host_graph_direct = value;
@@ -328,6 +328,7 @@ int vsg_get_tunable(vsg_index* h, const char* name, double* value) {
     else if (nm == "cert_fp8_sample_rows") *value = h->cert_fp8_sample_rows;
     else if (nm == "cert_prefetch_max_batch") *value = h->cert_prefetch_max_batch;
     else if (nm == "finish_cluster") *value = h->finish_cluster;
+    else if (nm == "finish_cluster_one") *value = h->finish_cluster_one;
     else throw std::invalid_argument("unknown tunable '" + nm + "'");
   });
 }

@@ -186,13 +186,16 @@ struct vsg_index {
   // reranked rows a query and ran at 0.15-0.5x.
   double cert_fp8_max_batch = 16;
   double cert_fp8_sample_rows = 32768;
-  // Certified searches over the e4m3 copy of at most this many queries prefetch every row their
-  // lists take into L2 during the main pass (one bulk prefetch a row), for the finish kernel's
-  // rerank of ~1,000 rows a query; 0: none.
+  // Certified searches over the e4m3 copy of at most this many queries prefetch the rows of their
+  // final lists into L2 as the main pass writes them (one bulk prefetch a row), for the finish
+  // kernel's rerank of ~1,000 rows a query; 0: none.
   double cert_prefetch_max_batch = 16;
   // Certified path: CTAs per query in the finish kernel when the batch times it fits the SMs
-  // (1-8; k = 100 at batches 1-8 on the bf16 copy ran 9-10 % faster with 8).
+  // (1-16; k = 100 at batches 1-8 on the bf16 copy ran 9-10 % faster with 8 than with 1), and for
+  // a search of one query (finish_cluster_one: 16 ran batch 1 at 1M x 384 2.7 % faster than 8,
+  // while 16 at batch 8 ran 5 % slower than 8).
   double finish_cluster = 8;
+  double finish_cluster_one = 16;
   // 1: on the certified path the graph's kernels read the queries straight from the pinned
   // staging buffer (no copy in; measured 1.5 us less a blocking search at batch 1)
   double host_graph_direct = 1;
@@ -672,9 +675,11 @@ struct vsg_index {
     // bf16 copy's, and a start from 4K rows (about 4 rows of a query's 1,000-row cluster at
     // 1M x 384) kept every list full of rows far above the cluster for the whole pass.
     const bool small_sample = nq < 8 || (k <= 16 && nq <= 64);
+    // (the tuning table's sample sizes are timed on the bf16 copy: not for the e4m3 copy, whose
+    // margin needs the larger start; a 16K sample picked for batch 16 ran it 30 % slower)
     const size_t srows = force_sample >= 0 ? size_t(force_sample)
-                         : te ? size_t(te->sample)
                          : f8 && certify ? size_t(cert_fp8_sample_rows)
+                         : te ? size_t(te->sample)
                          : small_sample ? std::min<size_t>(size_t(sample_rows), 4096) : size_t(sample_rows);
     // After the query preparation the path's kernels run as a chain of programmatic dependent
     // launches (each may start while the one before it finishes); not while profiling, whose
@@ -759,7 +764,8 @@ struct vsg_index {
     fa.sorted_lists = nq <= vsg::kSortedListQueries ? 1u : 0u;
     // Small batches rerank over a cluster of CTAs per query (the e4m3 copy's wider margin keeps
     // ~1,000 rows to rerank at 1M x 384, ~20 us on one SM).
-    fa.cluster = certify && double(nq * size_t(finish_cluster)) <= double(sms) ? uint32_t(finish_cluster) : 1u;
+    const size_t fc = size_t(nq == 1 ? finish_cluster_one : finish_cluster);
+    fa.cluster = certify && double(nq * fc) <= double(sms) ? uint32_t(fc) : 1u;
     fa.rows_in_l2 = a.xf ? 1u : 0u;
     fa.stage_cap = uint32_t(std::min<size_t>(vsg::kFinishStageMax, size_t(a.nsplit) * groups * kp));
     if (certify) {

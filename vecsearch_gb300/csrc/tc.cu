@@ -780,7 +780,6 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
                     wd[size_t(lane) * cap + cnt] = dist;
                     wi[size_t(lane) * cap + cnt] = c0 + j;
                     ++cnt;
-                    if (a.xf) bulk_prefetch_l2(a.xf + size_t(c0 + j) * a.xf_ld, a.xf_ld * 4u);
                   }
                 }
               }
@@ -800,6 +799,13 @@ __global__ void __launch_bounds__(tc_threads_cap(32u * E), 1)
       } else {
         // Sort every buffer, keep the best kp and write the split's shortlist.
         compact_lanes(ok ? __ballot_sync(kFull, qvalid) : 0u, true);
+        if (a.xf) {  // its rows into L2 for the finish kernel's rerank (which starts a few us
+          __syncwarp();  // after the pass, once every split is done; the warp wrote the lists)
+          if (ok && qvalid) {
+            const uint32_t* li = a.part_i + (size_t(qg) * nsplit * G + size_t(split) * G + group) * a.kp;
+            for (uint32_t e = 0; e < cnt; ++e) bulk_prefetch_l2(a.xf + size_t(li[e]) * a.xf_ld, a.xf_ld * 4u);
+          }
+        }
       }
     }
     if (load_a) ++aitem;
@@ -1888,11 +1894,6 @@ __device__ void prep_sample_block(const PrepSample& smp, uint32_t sb, const floa
 // added once (a match over the warp): most minima fall into two or three bins, where one shared
 // atomic per value serialized for 1.3 us a round.
 constexpr int kSelPer = int(kPrepSampleRows / kPrepRowsPerBlock / 128);  // minima a thread holds per query (4)
-__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
-  uint32_t old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
 __device__ void prep_sample_select(const PrepSample& smp, uint32_t nq, uint32_t blocks, const float* margin) {
   __shared__ uint32_t hist[4][256];
   __shared__ uint32_t s_lo[4], s_hi[4], s_prefix[4], s_mask[4], s_rank[4], s_active[4];
@@ -2523,10 +2524,11 @@ cudaError_t launch_serve_select(const ServeHeader* hdr, const ServeQuery* sq, co
 
 size_t finish_smem_bytes(uint32_t dp, uint32_t stage_cap) { return finish_smem(dp, stage_cap).total; }
 
-cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap) {
+cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap, bool* cluster16) {
   const size_t smem = finish_smem_bytes(dp, stage_cap);
   static std::mutex mu;
   static size_t configured[64] = {};
+  static bool fits16[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -2538,9 +2540,34 @@ cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap) {
                               reinterpret_cast<const void*>(finish_kernel<true, true>)};
     for (const void* f : kernels)
       if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    // 16-CTA clusters of the wide variants (both metrics alike): allowed, then asked whether one
+    // can be resident at this shared memory size
+    for (int i = 2; i < 4 && e == cudaSuccess; ++i)
+      e = cudaFuncSetAttribute(kernels[i], cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    if (dev < 64) configured[dev] = smem;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(kFinishThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = 16;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    const bool ok16 = cudaOccupancyMaxActiveClusters(&clusters, finish_kernel<false, true>, &cfg) == cudaSuccess &&
+                      clusters >= 1;
+    (void)cudaGetLastError();  // (a refused query leaves no error behind)
+    if (dev < 64) {
+      configured[dev] = smem;
+      fits16[dev] = ok16;
+    }
+    if (cluster16) *cluster16 = ok16;
+    return cudaSuccess;
   }
+  if (cluster16) *cluster16 = dev < 64 && fits16[dev];
   return cudaSuccess;
 }
 
@@ -2550,7 +2577,8 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
   if (!a.hdr && (a.k == 0 || a.k > uint32_t(kMaxK))) return cudaErrorInvalidValue;
   if (a.hdr && !a.sq) return cudaErrorInvalidValue;
   if (a.fail_count && (!a.err || !a.fail_list)) return cudaErrorInvalidValue;
-  cudaError_t e = finish_prepare(a.dp, a.stage_cap);
+  bool fits16 = false;
+  cudaError_t e = finish_prepare(a.dp, a.stage_cap, &fits16);
   if (e != cudaSuccess) return e;
   const size_t smem = finish_smem_bytes(a.dp, a.stage_cap);
   int dev = 0, sms = 0;
@@ -2560,8 +2588,8 @@ cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t strea
   const bool wide = grid <= uint32_t(sms);
   auto* kern = a.l2 ? (wide ? finish_kernel<true, true> : finish_kernel<true, false>)
                     : (wide ? finish_kernel<false, true> : finish_kernel<false, false>);
-  const uint32_t c = a.cluster;
-  if (c > 1 && wide && !a.hdr && c <= 8 && grid * c <= uint32_t(sms))
+  const uint32_t c = a.cluster > 8 && !fits16 ? 8u : a.cluster;
+  if (c > 1 && wide && !a.hdr && c <= 16 && grid * c <= uint32_t(sms))
     return launch_kernel_cluster(kern, dim3(grid * c), dim3(kFinishThreads), smem, stream, pdl, c, a);
   return launch_kernel(kern, dim3(grid), dim3(kFinishThreads), smem, stream, pdl, a);
 }

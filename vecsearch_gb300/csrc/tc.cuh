@@ -102,8 +102,8 @@ struct TcArgs {
   // runs out after wait_ns and the kernel winds down with kDevTimeout.
   uint32_t stall;
   // Main pass of a small certified batch: the FP32 rows (xf_ld floats apart, xf_ld a multiple of
-  // 4), or nullptr. Every row a list takes is prefetched into L2 (one bulk prefetch), so the
-  // finish kernel's rerank of it reads L2 instead of waiting on DRAM.
+  // 4), or nullptr. Every row of a split's final list is prefetched into L2 (one bulk prefetch a
+  // row) as the list is written, so the finish kernel's rerank of it reads L2 instead of DRAM.
   const float* xf;
   uint32_t xf_ld;
 };
@@ -214,10 +214,11 @@ struct FinishArgs {
   uint32_t stage_cap;      // list entries staged in shared memory at most (<= kFinishStageMax)
   uint32_t lists_per_split;  // lists of each split (the shortlist kernel's tc_groups(kp)); 0 = 1
   uint32_t sorted_lists;     // 1: every list is sorted by (dist, id) (kSortedListQueries)
-  // CTAs per query (a thread-block cluster; at most 8, and nq x cluster at most the SM count,
-  // else 1): rank 0 does all but the rerank, which the cluster shares. 0 or 1: one CTA.
+  // CTAs per query (a thread-block cluster; at most 16, and nq x cluster at most the SM count,
+  // else 1; 16 runs as 8 where such clusters do not fit): rank 0 does all but the rerank, which
+  // the cluster shares. 0 or 1: one CTA.
   uint32_t cluster;
-  // 1: the main pass prefetched every row its lists took into L2 (TcArgs::xf); otherwise a
+  // 1: the main pass prefetched the rows of its final lists into L2 (TcArgs::xf); otherwise a
   // one-CTA finish prefetches each staged row itself.
   uint32_t rows_in_l2;
   // The fallback's inputs, written for each uncertified query at its slot j in fail_list: its
@@ -231,9 +232,11 @@ struct FinishArgs {
   unsigned long long* tally;
 };
 // Dynamic shared memory of the finish kernel, and its attribute set up to that size (done by
-// launch_finish too; a launch captured into a CUDA graph should find it done).
+// launch_finish too; a launch captured into a CUDA graph should find it done). cluster16, when
+// given, tells whether a cluster of 16 CTAs (a non-portable size: one GPC must hold them all) of
+// the wide variant fits this device.
 size_t finish_smem_bytes(uint32_t dp, uint32_t stage_cap);
-cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap);
+cudaError_t finish_prepare(uint32_t dp, uint32_t stage_cap, bool* cluster16 = nullptr);
 // grid: nq, or the largest batch in serving mode.
 cudaError_t launch_finish(const FinishArgs& a, uint32_t grid, cudaStream_t stream, bool pdl = false);
 

@@ -212,6 +212,19 @@ def test_tunables_through_the_abi(harness):
     assert out[12] == "1" and out[13].split()[0] == "1"
 
 
+def test_certified_path_tunables(harness):
+    # defaults and ranges of the certified path's tunables (include/vsg.h)
+    names = {"finish_cluster": ("8", 16, 17), "finish_cluster_one": ("16", 1, 0),
+             "cert_prefetch_max_batch": ("16", 0, -1), "cert_fp8_max_batch": ("16", 0, -1),
+             "cert_fp8_sample_rows": ("32768", 65536, -1), "host_graph_max_batch": ("16", 0, 1025),
+             "host_graph_direct": ("1", 0, 2)}
+    for name, (default, ok, bad) in names.items():
+        out = harness.raw([f"get {name}", f"set {name} {ok}", f"get {name}", f"set {name} {bad}", f"get {name}"])
+        assert out[0] == f"0 {default}", (name, out)
+        assert out[1] == "0" and out[2] == f"0 {ok}", (name, out)
+        assert out[3] == "1" and out[4] == f"0 {ok}", (name, out)  # out of range: rejected, value kept
+
+
 def test_exact_below_host_branches(harness):
     # src/hnsw.cpp:325-328: no allowed row -> empty results; more than exact_below -> the graph.
     out = harness.raw(["below 100 2 5 10 0",     # none allowed: handled, filled with none / +inf

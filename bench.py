@@ -390,8 +390,9 @@ def parity_checks(vsg, idx, x, q, a):
         ids = np.concatenate([p[0] for p in parts])[:len(truth_i)]
         dists = np.concatenate([p[1] for p in parts])[:len(truth_i)]
         s1 = index.tc_exact_stats()
+        copy = "e4m3" if uses_e4m3(index, batch, k, xx.shape[1]) else "bf16"
         row = {"metric": metric, "k": k, "batch": batch, "method": "auto",
-               "path": "tc_exact" if s1[0] > s0[0] else "fp32 kernels",
+               "path": f"tc_exact ({copy} copy)" if s1[0] > s0[0] else "fp32 kernels",
                "uncertified_to_scan": int(s1[1] - s0[1])}
         row.update(_parity_case(O, xx, qq[:len(truth_i)], ids, dists, k, metric, cores, truth_i))
         cases.append(row)
